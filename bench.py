@@ -1,0 +1,364 @@
+"""Benchmark of the island-model DE generation loop on GB300.
+
+Workload (the island-model configuration the headline metric is quoted on): 64 islands x
+P = 100, D = 30, rotated Rastrigin z = M (0.0512 (x - o)) (CEC2014 F9 form, f - f*), F = 0.5,
+CR = 0.9, DE/rand/1/bin, ring migration of each island's best 5 into the next island's worst
+5 every 50 generations; seeded synthetic o ~ U[-80, 80]^30 and Haar M.
+
+A step is one generation over all islands (6400 exact evaluations). `value` is exact
+evaluations/s over the whole job with the population resident in HBM; `e2e` is the same rate
+through the reference-shaped C ABI (API_DE_GenerateNewPopulation_f32 / API_evaluateFitness_f32
+/ API_DE_SelectSurvival_f32) with host buffers, the initial upload and a per-generation
+fitness read-back inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl speo|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "speo-gpu-single-control_gb300"))
+sys.path.insert(0, str(REPO / "oracle"))
+
+METRIC = "exact-eval gens/s & evals/s to 1e-8 error: surrogate vs plain DE, same GB300"
+N_ISLANDS, POP, DIM, FUNC = 64, 100, 30, 9
+INTERVAL, MIGRANTS = 50, 5
+SEED = 9 * 2  # run_seed(node 1, function 9, run 1) = (1 + 9) * (1 + 9) is used below
+
+
+def run_seed() -> int:
+    from speo_gb300.instances import run_seed as rs
+
+    return rs(1, FUNC, 1)
+
+
+def peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            out, _ = self.proc.communicate(timeout=10)
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flush_l2(buf) -> None:
+    buf.add_(1.0)   # writes 512 MB, > 4x the 129 MB L2
+
+
+def island_table(device: str, rank: int):
+    from speo_gb300.device import SegmentSpec, SegmentTable
+    from speo_gb300.instances import make_instance
+
+    seed = run_seed()
+    inst = [make_instance(seed, DIM)]
+    specs = [SegmentSpec(pop_size=POP, dim=DIM, func_id=FUNC, instance=0, seed=seed * 1000003 + rank,
+                         ring_next=(i + 1) % N_ISLANDS) for i in range(N_ISLANDS)]
+    # tiles of 50 rows: two balanced tiles per island
+    return SegmentTable(specs, inst, tile_rows=50, device=device)
+
+
+def capture_epoch(tab, torch):
+    """One CUDA graph = INTERVAL generations (an even number, so the buffers end where they
+    started) + the ring migration."""
+    assert INTERVAL % 2 == 0
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        start = tab.cur
+        tab.generation()          # warm the kernel variant (sets its smem attribute) outside capture
+        tab.generation()
+        assert tab.cur == start
+        with torch.cuda.graph(g, stream=s):
+            for _ in range(INTERVAL):
+                tab.generation()
+            tab.migrate(MIGRANTS)
+    torch.cuda.current_stream().wait_stream(s)
+    return g
+
+
+def bench_speo(args) -> dict:
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from speo_gb300 import _lib
+
+    L = _lib.load()
+    tab = island_table(dev, rank)
+    tab.init_population()
+    graph = capture_epoch(tab, torch)
+    epochs_w = max(1, (args.warmup + INTERVAL - 1) // INTERVAL)
+    epochs = max(1, (args.steps + INTERVAL - 1) // INTERVAL)
+    steps = epochs * INTERVAL
+    for _ in range(epochs_w):
+        graph.replay()
+    torch.cuda.synchronize()
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(epochs)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(epochs):
+            flush_l2(flush)                        # L2 flushed between timed epochs
+            ev[i][0].record()
+            graph.replay()
+            ev[i][1].record()
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    evals_per_step = N_ISLANDS * POP
+    value = evals_per_step * steps * world / (ms / 1e3)
+
+    # ---- dominant kernel: average launch time of the fused generation kernel ---------------
+    # (a graph of back-to-back launches, so host launch overhead does not enter the average)
+    kl = 100
+    kg = torch.cuda.CUDAGraph()
+    cs = torch.cuda.Stream()
+    cs.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(cs):
+        with torch.cuda.graph(kg, stream=cs):
+            for _ in range(kl):
+                tab.generation()
+    torch.cuda.current_stream().wait_stream(cs)
+    s = torch.cuda.current_stream()
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    flush_l2(flush)
+    k0.record(s)
+    for _ in range(reps):
+        kg.replay()
+    k1.record(s)
+    torch.cuda.synchronize()
+    launch_ms = k0.elapsed_time(k1) / (kl * reps)
+    alg_bytes = evals_per_step * (5 * DIM * 4 + 2 * 4)       # 4 row reads + 1 row write + 2 fitness
+    pk = peaks()
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    rows, errs = tab.best_f64()
+    best_err = float(errs.min().item())
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": steps,
+        "warmup": epochs_w * INTERVAL, "ms_per_step": ms / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": "island model: 64 islands x P=100, D=30, rotated Rastrigin (F9 form), "
+                               "DE/rand/1/bin F=0.5 CR=0.9, ring best-5 -> worst-5 every 50 generations",
+                   "islands": N_ISLANDS, "pop_size": POP, "dim": DIM, "migration_interval": INTERVAL,
+                   "migrants": MIGRANTS, "step": "one generation over all islands (6400 exact evaluations)",
+                   "l2": "flushed (512 MB write) before each timed 50-generation epoch; the population "
+                         "(1.5 MB) stays L2-resident within an epoch as in a real run",
+                   "graph": "one CUDA graph per epoch: 50 fused generation launches + 2 migration launches"},
+        "gens_per_s": steps * world / (ms / 1e3) / world,
+        "best_error_f64_after_run": best_err,
+        "roofline": {"kernel": "k_generation<1,1> (fused generate+evaluate+select)", "bound": "hbm",
+                     "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
+                     "traffic": None, "peak_src": pk["src"],
+                     "alg_bytes_per_launch": alg_bytes, "launch_us": launch_ms * 1e3},
+        "gpu_launches": epochs * (INTERVAL + 2),
+        "clocks": clk.summary(),
+    }
+    out["e2e"] = bench_e2e(L, dev, torch, args)
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline(sample_s=args.cpu_sample_s)
+    return out
+
+
+def bench_e2e(L, dev, torch, args) -> dict:
+    """Reference-shaped C ABI with host buffers: initial population + instance uploaded from
+    pinned host memory, then per generation generate / evaluate / select and a read-back of
+    the generation's fitness vector; all inside the timed region."""
+    from speo_gb300 import _lib
+    from speo_gb300.instances import make_instance
+
+    n = N_ISLANDS * POP
+    ld = 32
+    o, M = make_instance(run_seed(), DIM)
+    rot = np.zeros((ld, DIM), dtype=np.float32)
+    rot[:DIM] = M.T
+    sh = np.zeros(ld, dtype=np.float32)
+    sh[:DIM] = o
+    rng = np.random.default_rng(0)
+    h_pop = torch.from_numpy(rng.uniform(-100, 100, (n, ld)).astype(np.float32)).pin_memory()
+    h_pop[:, DIM:] = 0
+    h_rot = torch.from_numpy(rot).pin_memory()
+    h_sh = torch.from_numpy(sh).pin_memory()
+    h_fit = torch.zeros(n, dtype=torch.float32).pin_memory()
+    pop, cand = torch.empty(n, ld, device=dev), torch.zeros(n, ld, device=dev)
+    pfit, cfit = torch.empty(n, device=dev), torch.empty(n, device=dev)
+    d_rot, d_sh = torch.empty(ld, DIM, device=dev), torch.empty(ld, device=dev)
+    rng_state = torch.zeros(16, dtype=torch.int32, device=dev)
+    perm = torch.arange(n, dtype=torch.int32, device=dev)
+    best = torch.zeros(N_ISLANDS, dtype=torch.int32, device=dev)
+    info = (_lib.DEInfoF32 * N_ISLANDS)(*[_lib.DEInfoF32(0.9, 0.5, 4, POP) for _ in range(N_ISLANDS)])
+    h_info = torch.frombuffer(bytearray(bytes(info)), dtype=torch.uint8).pin_memory()
+    d_info = torch.empty_like(h_info, device=dev)
+    ii = _lib.IslandInfo(n, N_ISLANDS, perm.data_ptr())
+    pi = _lib.ProblemInfoF32(DIM, FUNC, 1, 0, run_seed(), 0, 0, 100.0, -100.0)
+    P = _lib.PopulationF32(pop.data_ptr(), pfit.data_ptr())
+    C = _lib.PopulationF32(cand.data_ptr(), cfit.data_ptr())
+    stream = torch.cuda.current_stream()
+    L.speo_set_stream(ctypes.c_void_p(stream.cuda_stream))
+    _lib.check(L.API_Initilize_f32(C, rng_state.data_ptr(), ii, pi), "API_Initilize_f32")
+    steps = max(100, min(args.steps, 2000))
+
+    def run(nsteps):
+        pop.copy_(h_pop, non_blocking=True)
+        d_rot.copy_(h_rot, non_blocking=True)
+        d_sh.copy_(h_sh, non_blocking=True)
+        d_info.copy_(h_info, non_blocking=True)
+        L.API_evaluateFitness_f32(pfit.data_ptr(), None, None, pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(),
+                                  None, None, None, None, n, DIM, 0.0, FUNC)
+        for _ in range(nsteps):
+            L.API_DE_GenerateNewPopulation_f32(C, P, best.data_ptr(), ii, d_info.data_ptr(), rng_state.data_ptr(),
+                                               pi)
+            L.API_evaluateFitness_f32(cfit.data_ptr(), None, None, cand.data_ptr(), d_sh.data_ptr(),
+                                      d_rot.data_ptr(), None, None, None, None, n, DIM, 0.0, FUNC)
+            L.API_DE_SelectSurvival_f32(P, C, ii, pi)
+            h_fit.copy_(pfit, non_blocking=True)
+        stream.synchronize()
+
+    run(20)
+    t0 = time.perf_counter()
+    run(steps)
+    dt = time.perf_counter() - t0
+    _lib.check(L.API_CheckCUDAError(), "e2e")
+    L.speo_set_stream(None)
+    h2d = (n * ld + ld * DIM + ld) * 4 + len(bytes(info))
+    return {"value": n * steps / dt, "unit": "evals/s", "h2d_bytes_per_step": h2d / steps,
+            "d2h_bytes_per_step": n * 4, "steps": steps,
+            "path": "API_DE_GenerateNewPopulation_f32 + API_evaluateFitness_f32 + API_DE_SelectSurvival_f32, "
+                    "64 sub-islands of 100"}
+
+
+def cpu_workload_sample(sample_s: float, threads: int):
+    """FP64 island loop of the oracle port on the host cores: (evals/s, gens done)."""
+    import speo_oracle
+    from speo_gb300.instances import make_instance
+
+    o, M = make_instance(run_seed(), DIM)
+    ld = 32
+    n = N_ISLANDS * POP
+    pop = speo_oracle.init_population(n, ld, DIM, -100.0, 100.0, run_seed()).astype(np.float64)
+    fit = speo_oracle.evaluate_rows(FUNC, pop.astype(np.float32), DIM, o, M)
+    gens, total_evals, t_used = 0, 0, 0.0
+    chunk = 2
+    while t_used < sample_s:
+        t0 = time.perf_counter()
+        total_evals += speo_oracle.run_islands_f64(N_ISLANDS, POP, DIM, ld, FUNC, 0.5, 0.9, -100.0, 100.0, o, M,
+                                                   run_seed(), gens, chunk, INTERVAL, MIGRANTS, pop, fit, threads)
+        t_used += time.perf_counter() - t0
+        gens += chunk
+        chunk = min(chunk * 2, 200)
+    return total_evals / t_used, gens, t_used
+
+
+def cpu_baseline(sample_s: float = 12.0) -> dict:
+    threads = os.cpu_count() or 1
+    rate, gens, t = cpu_workload_sample(sample_s, threads)
+    return {"value": rate, "unit": "evals/s", "cores": threads, "kind": "port",
+            "sample": f"{gens} generations of the same 64x100 D=30 island workload in FP64 "
+                      f"(oracle restatement of the reference's DE + CEC2014 objective), {t:.1f} s, "
+                      f"{threads} threads over islands"}
+
+
+def bench_reference(args) -> dict:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    rate, gens, t = cpu_workload_sample(min(60.0, max(10.0, 0.002 * args.steps)), threads)
+    return {"metric": METRIC, "value": rate, "unit": "evals/s", "n_gpus": 0, "steps": gens, "warmup": 0,
+            "ms_per_step": t * 1e3 / gens, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "island model: 64 islands x P=100, D=30, rotated Rastrigin (F9 form), "
+                                   "DE/rand/1/bin F=0.5 CR=0.9, ring best-5 -> worst-5 every 50 generations"},
+            "cpu_baseline": {"value": rate, "unit": "evals/s", "cores": threads, "kind": "port",
+                             "sample": f"{gens} generations, {t:.1f} s (the reference's compiled CPU objective "
+                                       "cannot run on the Arm box; the oracle port restates it)"},
+            "e2e": {"value": rate, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--warmup", type=int, default=500)
+    ap.add_argument("--impl", default="speo", choices=["speo", "reference"])
+    ap.add_argument("--cpu-sample-s", type=float, default=12.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    out = bench_reference(args) if args.impl == "reference" else bench_speo(args)
+    if out is not None and int(os.environ.get("RANK", "0")) == 0:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

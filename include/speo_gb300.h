@@ -1,0 +1,255 @@
+/*
+ * speo_gb300.h -- C ABI of the GB300 (sm_103a) island-model differential-evolution library.
+ *
+ * Two groups of entry points:
+ *
+ *  1. Drop-in replacements for the reference's CUDA_EA_library C entry points. Same names,
+ *     same argument meaning, same by-value struct layouts, so a caller compiled against the
+ *     reference headers links against libspeo_gb300.so unchanged:
+ *        API_Initilize                 <- CUDA_EA_library/EA_CUDA.h:41-42   (kernel_EA_CUDA.cu:121-134)
+ *        API_CheckCUDAError            <- CUDA_EA_library/EA_CUDA.h:43-44   (kernel_EA_CUDA.cu:64-69)
+ *        API_DE_GenerateNewPopulation  <- CUDA_EA_library/DE_CUDA.cc:2-3    (kernel_DE_CUDA.cu:291-302)
+ *        API_DE_SelectSurvival         <- CUDA_EA_library/DE_CUDA.cc:4-5    (kernel_DE_CUDA.cu:329-338)
+ *        API_evaluateFitness           <- CUDA_EA_library/CEC2014_CUDA.h:35-37 (kernel_CEC2014_CUDA.cu:1672-1797)
+ *     The unsuffixed names use `real = double`, the layout the reference ships with
+ *     (CUDA_EA_library/config.h:31-34). The `_f32` names are the `real = float` layout
+ *     (the reference's GPU_SINGLE_PRECISION build) and are the fast path.
+ *     Differences from the reference, all deliberate:
+ *       - the `curandState*` slot is an opaque Philox key/counter block (speo_rng_state);
+ *         a caller's existing curandState allocation is large enough to hold it;
+ *       - every individual gets a trial and a selection step, also when the population
+ *         size is not a multiple of 16 (the reference leaves the last P mod 16 untouched);
+ *       - the best-in-sub-island search honours the sub-island offset;
+ *       - errors are returned as status codes, never exit(); no implicit device sync
+ *         except in API_CheckCUDAError, which synchronises like the reference's.
+ *
+ *  2. GB300-native extensions (speo_*): a fused generate+evaluate+select generation kernel
+ *     over a table of segments (islands / independent runs of uneven size), the on-device
+ *     ring migration that replaces the reference's MPI exchange (src/migrate.cc:46-136),
+ *     the tcgen05 rotation GEMM in BF16 3-term split precision, FP64 re-evaluation of each
+ *     segment's best, and the online MLP surrogate.
+ *
+ * All pointers to population data are device pointers owned by the caller; no entry point
+ * in group 1 allocates or frees device memory.
+ */
+#ifndef SPEO_GB300_H
+#define SPEO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SPEO_API __attribute__((visibility("default")))
+#else
+#define SPEO_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------------------ */
+/* Status codes                                                                          */
+/* ------------------------------------------------------------------------------------ */
+#define SPEO_OK                 0
+#define SPEO_ERR_INVALID_ARG    1  /* bad size, null pointer, misaligned stride ...      */
+#define SPEO_ERR_CUDA           2  /* a CUDA runtime call failed (see speo_last_error)   */
+#define SPEO_ERR_UNSUPPORTED    3  /* function id / strategy / shape not implemented     */
+#define SPEO_ERR_DEVICE_FLAG    4  /* a kernel raised its device-side error flag         */
+
+/* Device error flag bits (speo_device_error_bits) */
+#define SPEO_DEVERR_REDRAW_LIMIT  0x1u  /* distinct-index rejection loop hit its bound      */
+#define SPEO_DEVERR_BOUND_LIMIT   0x2u  /* reflection loop hit its bound (non-finite value) */
+#define SPEO_DEVERR_WAIT_TIMEOUT  0x4u  /* a bounded device wait gave up                    */
+#define SPEO_DEVERR_BAD_SEGMENT   0x8u  /* a segment descriptor failed the device check     */
+
+/* Objective ids. 9 is CEC2014 F9 (rotated Rastrigin, scale 0.0512), the reference's
+ * dispatch id (kernel_CEC2014_CUDA.cu:1704-1706). The reference has no GPU rotated sphere;
+ * it gets an id outside the reference's 1..30 range. Both return f(x) - f*. */
+#define SPEO_FUNC_ROTATED_RASTRIGIN  9
+#define SPEO_FUNC_ROTATED_SPHERE     31
+
+/* DE strategy ids, as in DE_CUDA::GetParameters (CUDA_EA_library/DE_CUDA.cc:36-53). */
+#define SPEO_DE_CURRENT_1        0
+#define SPEO_DE_CURRENT_2        1
+#define SPEO_DE_CURRENT_TO_BEST_1 2
+#define SPEO_DE_CURRENT_TO_BEST_2 3
+#define SPEO_DE_RAND_1           4
+#define SPEO_DE_RAND_2           5
+#define SPEO_DE_BEST_1           6
+#define SPEO_DE_BEST_2           7
+#define SPEO_DE_CURRENT_TO_RAND_1 8
+
+#define SPEO_MAX_DIM          256  /* largest D any kernel accepts                          */
+#define SPEO_RNG_STATE_BYTES   64  /* bytes the caller must provide behind speo_rng_state*  */
+
+/* ------------------------------------------------------------------------------------ */
+/* Reference-shaped by-value structs                                                     */
+/* ------------------------------------------------------------------------------------ */
+/* GPU_Population (CUDA_EA_library/EA_CUDA.h:21-25): rows of `np2` elements,
+ * np2 = max(32, next_pow2(dim)) (EA_CUDA.cc:197-206), one fitness per row. */
+typedef struct { double *elements; double *fitness_value; } speo_population_f64;
+typedef struct { float  *elements; float  *fitness_value; } speo_population_f32;
+
+/* GPU_IslandInfo (EA_CUDA.h:26-31). island_size = total rows on the device,
+ * subisland_num partitions, permutated_index maps positions to rows. */
+typedef struct { int island_size; int subisland_num; int *permutated_index; } speo_island_info;
+
+/* DEInfo (EA_CUDA.h:33-38), one per sub-island, in device memory. */
+typedef struct { double CR; double F; int strategy_ID; int pop_size; } speo_de_info_f64;
+typedef struct { float  CR; float  F; int strategy_ID; int pop_size; } speo_de_info_f32;
+
+/* ProblemInfo (config.h:48-59). */
+typedef struct {
+    int dim, function_ID, run_ID, max_base_FEs, seed, running_time, computing_time;
+    double max_bound, min_bound;
+} speo_problem_info_f64;
+typedef struct {
+    int dim, function_ID, run_ID, max_base_FEs, seed, running_time, computing_time;
+    float max_bound, min_bound;
+} speo_problem_info_f32;
+
+/* Opaque Philox-4x32-10 key + generation counter, in device memory, at least
+ * SPEO_RNG_STATE_BYTES bytes, 16-byte aligned. Replaces the reference's curandState array. */
+typedef struct speo_rng_state speo_rng_state;
+
+/* ------------------------------------------------------------------------------------ */
+/* Group 1: drop-in entry points (real = double)                                         */
+/* ------------------------------------------------------------------------------------ */
+/* Replaces API_Initilize (EA_CUDA.h:41-42): seeds the Philox key from problem_info.seed,
+ * resets the generation counter, and fills every row with x = lb + u*(ub-lb), u in (0,1]. */
+SPEO_API int API_Initilize(speo_population_f64 d_population, speo_rng_state *d_rng,
+                  speo_island_info island_info, speo_problem_info_f64 problem_info);
+
+/* Replaces API_CheckCUDAError (EA_CUDA.h:43-44): cudaGetLastError + device sync + device
+ * error flag; returns a status instead of calling exit(-1). */
+SPEO_API int API_CheckCUDAError(void);
+
+/* Replaces API_DE_GenerateNewPopulation (DE_CUDA.cc:2-3): per-sub-island best search
+ * into d_best_individual_ID, then mutation + binomial crossover + reflection into d_candidate. */
+SPEO_API int API_DE_GenerateNewPopulation(speo_population_f64 d_candidate, speo_population_f64 d_population,
+                                 int *d_best_individual_ID, speo_island_info island_info,
+                                 speo_de_info_f64 *d_DE_info, speo_rng_state *d_rng,
+                                 speo_problem_info_f64 problem_info);
+
+/* Replaces API_DE_SelectSurvival (DE_CUDA.cc:4-5): strict `<` greedy replacement per row. */
+SPEO_API int API_DE_SelectSurvival(speo_population_f64 d_population, speo_population_f64 d_candidate,
+                          speo_island_info island_info, speo_problem_info_f64 problem_info);
+
+/* Replaces API_evaluateFitness (CEC2014_CUDA.h:35-37). d_rotated_data is the reference's
+ * padded transposed matrix: d_rotated_data[k*problem_dim + j] = M[j][k] for k < np2
+ * (rows k >= problem_dim zero), d_shift_data holds o in its first problem_dim entries,
+ * rows of d_original_elements have np2 elements. Implemented ids: 9, 31. Scratch
+ * arguments (shuffled, rotated, shuffle, tmp_fitness, wi, sigma) are accepted and unused:
+ * the rotation is fused with the reduction, so no intermediate is written. */
+SPEO_API void API_evaluateFitness(double *d_fitness_value, double *d_shuffled_elements,
+                         double *d_rotated_elements, double *d_original_elements,
+                         double *d_shift_data, double *d_rotated_data, int *d_shuffle_data,
+                         double *d_tmp_fitness, double *d_wi, double *d_sigma,
+                         int pop_size, int problem_dim, double bias, int function_ID);
+
+/* Group 1, real = float. */
+SPEO_API int API_Initilize_f32(speo_population_f32 d_population, speo_rng_state *d_rng,
+                      speo_island_info island_info, speo_problem_info_f32 problem_info);
+SPEO_API int API_DE_GenerateNewPopulation_f32(speo_population_f32 d_candidate, speo_population_f32 d_population,
+                                     int *d_best_individual_ID, speo_island_info island_info,
+                                     speo_de_info_f32 *d_DE_info, speo_rng_state *d_rng,
+                                     speo_problem_info_f32 problem_info);
+SPEO_API int API_DE_SelectSurvival_f32(speo_population_f32 d_population, speo_population_f32 d_candidate,
+                              speo_island_info island_info, speo_problem_info_f32 problem_info);
+SPEO_API void API_evaluateFitness_f32(float *d_fitness_value, float *d_shuffled_elements,
+                             float *d_rotated_elements, float *d_original_elements,
+                             float *d_shift_data, float *d_rotated_data, int *d_shuffle_data,
+                             float *d_tmp_fitness, float *d_wi, float *d_sigma,
+                             int pop_size, int problem_dim, float bias, int function_ID);
+
+/* ------------------------------------------------------------------------------------ */
+/* Library control                                                                       */
+/* ------------------------------------------------------------------------------------ */
+/* Stream used by the group-1 entry points of the calling host thread (default: legacy 0).
+ * `stream` is a cudaStream_t. */
+SPEO_API int speo_set_stream(void *stream);
+/* Message of the last failing call on this host thread ("" if none). */
+SPEO_API const char *speo_last_error(void);
+/* Reads and clears the device error flag bits of the current device (synchronises). */
+SPEO_API int speo_device_error_bits(uint32_t *bits_out);
+/* Library version string. */
+SPEO_API const char *speo_version(void);
+
+/* ------------------------------------------------------------------------------------ */
+/* Group 2: GB300-native extensions                                                      */
+/* ------------------------------------------------------------------------------------ */
+/* One segment = one island of a ring, or one independent run. Rows row0 .. row0+pop_size-1
+ * of the population buffers, `ld` floats apart. The objective instance is (shift, rot):
+ * rot is M^T, rot[k*ld_rot + j] = M[j][k]. Rows are addressed as global row indices, which
+ * also key the Philox counters, so results do not depend on how segments are tiled. */
+typedef struct {
+    int64_t      row0;
+    int32_t      pop_size;   /* P >= 4 */
+    int32_t      dim;        /* 1 <= D <= SPEO_MAX_DIM */
+    int32_t      ld;         /* row stride in floats, >= D, multiple of 4 */
+    int32_t      func_id;    /* SPEO_FUNC_* */
+    int32_t      strategy;   /* SPEO_DE_* */
+    float        F, CR;
+    float        lb, ub;     /* search bounds (reflection) */
+    const float *shift;      /* device, round_up(D, 4) floats, 16-byte aligned, zero past D */
+    const float *rot;        /* device, D rows of ld_rot floats, 16-byte aligned */
+    int32_t      ld_rot;     /* >= D, multiple of 4 */
+    int32_t      ring_next;  /* segment that receives this one's emigrants, -1 = none */
+    uint64_t     seed;       /* Philox key */
+} speo_segment;
+
+#define SPEO_TILE_SIMT  64   /* largest work item of the CUDA-core kernels */
+#define SPEO_TILE_TC   128   /* largest work item of the tcgen05 kernels   */
+
+/* Work item: a tile of up to `tile_rows` consecutive rows of one segment. */
+typedef struct { int32_t segment; int32_t first; int32_t count; int32_t pad; } speo_work_item;
+
+/* Fills `items` (host array of capacity `cap`) with the tiles of `segs` (host copy) for
+ * tiles of `tile_rows` rows; returns the number of items in *n_out. */
+SPEO_API int speo_plan_work(const speo_segment *segs, int n_segs, int tile_rows,
+                   speo_work_item *items, int cap, int *n_out);
+
+/* Initial population of every segment: x = lb + u*(ub-lb), and gen counter untouched. */
+SPEO_API int speo_init_population(const speo_segment *d_segs, int n_segs, const speo_work_item *d_items,
+                         int n_items, float *pop, void *stream);
+
+/* Fitness of every row of every segment (FP32 SIMT evaluation). dim_lo/dim_hi bound the
+ * segments' D (they select which kernel variants are launched). */
+SPEO_API int speo_evaluate(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,
+                  int dim_lo, int dim_hi, const float *pop, float *fit, void *stream);
+
+/* Same, with the rotation on the tcgen05 tensor cores: BF16 hi/lo 3-term split product,
+ * FP32 accumulation in tensor memory, fused shift/scale/objective/row-reduction epilogue.
+ * Tiles are 128 rows; segments need D <= 128 here. */
+SPEO_API int speo_evaluate_tc(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,
+                     int dim_lo, int dim_hi, const float *pop, float *fit, void *stream);
+
+/* One fused DE generation over all work items: for each target row, draw indices and
+ * crossover mask from Philox(key=seed, ctr={block,row,gen,tag}), build the trial
+ * (DE/<strategy>/bin + reflection), evaluate it, and write the winner of the strict-`<`
+ * greedy selection into (pop_out, fit_out). Reads (pop_in, fit_in). *d_gen is read by every
+ * block and advanced by one by the last block to finish (d_gen[1] is its scratch word; both
+ * start at the caller's values, d_gen[1] = 0). `use_tc` selects the tcgen05 evaluation
+ * (tiles of SPEO_TILE_TC rows, D <= 128); otherwise tiles have at most SPEO_TILE_SIMT rows.
+ * trial_out / trial_fit_out (may be NULL) receive every trial vector and its fitness. */
+SPEO_API int speo_generation(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,
+                    int dim_lo, int dim_hi, const float *pop_in, const float *fit_in,
+                    float *pop_out, float *fit_out, uint32_t *d_gen, int use_tc,
+                    float *trial_out, float *trial_fit_out, void *stream);
+
+/* Ring migration: each segment's k best rows (by fitness, then row) replace the k worst
+ * rows (by fitness, then row, from the worst) of segment ring_next. All emigrants are
+ * chosen before any row is replaced. `staging` holds n_segs*k*(max ld + 1) floats. */
+SPEO_API int speo_ring_migrate(const speo_segment *d_segs, int n_segs, int k, float *pop, float *fit,
+                      float *staging, int max_ld, void *stream);
+
+/* Per segment: argmin of fit (ties: lowest row) -> best_row[s]; FP64 re-evaluation of that
+ * row -> best_err[s] = f(x) - f* in double. */
+SPEO_API int speo_best_reeval_f64(const speo_segment *d_segs, int n_segs, const float *pop,
+                         const float *fit, int64_t *best_row, double *best_err, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPEO_GB300_H */

@@ -1,0 +1,439 @@
+/*
+ * speo_oracle.c -- CPU oracle for the island-model DE hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: a plain-C restatement of the reference's algorithm that the
+ * tests, smoke() and the CPU-baseline leg of bench.py use as the checker. It is never
+ * linked into, loaded by or called from libspeo_gb300.so.
+ *
+ * Build: -O2 -ffp-contract=off (every fused multiply-add is an explicit fma/fmaf, so the
+ * results are the same on x86-64 and aarch64).
+ */
+#include "speo_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define SPEO_DEVERR_REDRAW_LIMIT 0x1
+#define SPEO_DEVERR_BOUND_LIMIT 0x2
+#define SPEO_REDRAW_ITERS 4096
+#define SPEO_BOUND_ITERS 64
+#define SPEO_ORACLE_MAX_DIM 256
+
+#define CAT_(a, b) a##b
+#define CAT(a, b) CAT_(a, b)
+
+/* ------------------------------------------------------------------------------------ */
+/* Philox-4x32-10. Restated from the published algorithm (Salmon et al., "Parallel random  */
+/* numbers: as easy as 1, 2, 3", SC'11), Random123 v1.09 constants.                       */
+/* ------------------------------------------------------------------------------------ */
+void speo_oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int round = 0; round < 10; ++round) {
+        if (round) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+float speo_oracle_u01(uint32_t w)
+{
+    return (float)((w >> 8) + 1u) * 5.9604644775390625e-8f; /* 2^-24 */
+}
+
+/* NaN ranks as +inf in every best/worst search. */
+static float nan_as_inf(float f) { return isnan(f) ? INFINITY : f; }
+
+static int next_pow2_dim(int dim)
+{
+    /* EA_CUDA::CalNextPow2Dim, CUDA_EA_library/EA_CUDA.cc:197-206 */
+    int y = 1;
+    while (y < dim) y <<= 1;
+    return y < 32 ? 32 : y;
+}
+
+/* ---- draw source --------------------------------------------------------------------- */
+typedef struct {
+    const speo_oracle_draws *d;
+    int64_t row;          /* Philox row counter */
+    int pos;
+    uint32_t k;           /* next index-draw number (Philox) */
+    uint32_t block[4];
+    uint32_t block_id;
+    int have_block;
+} draw_cursor;
+
+static void cursor_begin(draw_cursor *c, const speo_oracle_draws *d, int pos)
+{
+    c->d = d;
+    c->pos = pos;
+    c->row = d->pos0 + pos;
+    c->k = 0;
+    c->have_block = 0;
+}
+
+static void cursor_end(draw_cursor *c, const speo_oracle_draws *d, int pos)
+{
+    (void)c; (void)d; (void)pos;
+}
+
+static double captured_next(const speo_oracle_draws *d, int stream)
+{
+    const int i = d->cap_pos[stream]++;
+    return d->cap[(size_t)stream * d->cap_len + (i < d->cap_len ? i : d->cap_len - 1)];
+}
+
+/* Uniform for the k-th index draw of this position. */
+static double draw_uniform_idx(draw_cursor *c)
+{
+    const speo_oracle_draws *d = c->d;
+    if (d->kind == 1) return captured_next(d, c->pos * 32);
+    const uint32_t blk = c->k >> 2, w = c->k & 3u;
+    if (!c->have_block || c->block_id != blk) {
+        const uint32_t ctr[4] = {blk, (uint32_t)c->row, d->gen, SPEO_TAG_IDX | d->tag_hi};
+        speo_oracle_philox(ctr, d->key, c->block);
+        c->block_id = blk;
+        c->have_block = 1;
+    }
+    c->k++;
+    return (double)speo_oracle_u01(c->block[w]);
+}
+
+/* (int)(u * n): float arithmetic, except for a captured FP64 stream, which uses the double
+ * arithmetic of the reference's GPU_DOUBLE_PRECISION build (kernel_DE_CUDA.cu:190). */
+static int draw_index(draw_cursor *c, int n, int real_size)
+{
+    const double u = draw_uniform_idx(c);
+    if (c->d->kind == 1 && real_size == 8) return (int)(u * (double)n);
+    return (int)((float)u * (float)n);
+}
+
+static double draw_cr(draw_cursor *c, const speo_oracle_draws *d, int pos, int e, int lane)
+{
+    if (d->kind == 1) return captured_next(d, pos * 32 + lane);
+    const uint32_t ctr[4] = {(uint32_t)(e >> 2), (uint32_t)c->row, d->gen, SPEO_TAG_CR | d->tag_hi};
+    uint32_t out[4];
+    speo_oracle_philox(ctr, d->key, out);
+    (void)lane;
+    return (double)speo_oracle_u01(out[e & 3]);
+}
+
+/* ---- precision-generic DE operators ---------------------------------------------------- */
+#define REAL float
+#define FMA fmaf
+#define SFX _f32
+#include "oracle_de_impl.h"
+#undef REAL
+#undef FMA
+#undef SFX
+#define REAL double
+#define FMA fma
+#define SFX _f64
+#include "oracle_de_impl.h"
+#undef REAL
+#undef FMA
+#undef SFX
+
+int speo_oracle_best_per_subisland_f32(const float *fit, int island_size, int subisland_num,
+                                       const int *perm, int *best_id)
+{
+    /* kernel_DE_CUDA.cu:120-158, reading perm[s*S + i] (the reference omits s*S). */
+    const int S = island_size / subisland_num;
+    for (int s = 0; s < subisland_num; ++s) {
+        int best = perm[s * S];
+        float bf = nan_as_inf(fit[best]);
+        for (int i = 1; i < S; ++i) {
+            const int row = perm[s * S + i];
+            if (bf > nan_as_inf(fit[row])) { bf = nan_as_inf(fit[row]); best = row; }
+        }
+        best_id[s] = best;
+    }
+    return 0;
+}
+
+void speo_oracle_init_population_f32(float *pop, int64_t row0, int n, int ld, int dim,
+                                     float lb, float ub, const uint32_t key[2])
+{
+    /* kernel_EA_CUDA.cu:91-118: x = min + u * (max - min), u from this library's stream */
+    const float range = ub - lb;
+    for (int i = 0; i < n; ++i) {
+        const uint32_t row = (uint32_t)(row0 + i);
+        for (int e = 0; e < dim; ++e) {
+            const uint32_t ctr[4] = {(uint32_t)(e >> 2), row, 0u, SPEO_TAG_INIT};
+            uint32_t out[4];
+            speo_oracle_philox(ctr, key, out);
+            pop[(size_t)i * ld + e] = fmaf(speo_oracle_u01(out[e & 3]), range, lb);
+        }
+    }
+}
+
+/* ---- objectives ---------------------------------------------------------------------- */
+#define ORACLE_PI 3.1415926535897932384626433832795029
+
+double speo_oracle_objective_f64(int func_id, const double *x, const double *o, const double *M, int dim)
+{
+    /* sr_func (CEC2014.cc:1395-1435): ye = (x - o) * rate; z = M * ye (rotatefunc :1382-1393) */
+    double ye[SPEO_ORACLE_MAX_DIM];
+    const double rate = func_id == 9 ? 5.12 / (double)100 : 1.0;
+    for (int i = 0; i < dim; ++i) ye[i] = (x[i] - o[i]) * rate;
+    double f = 0.0;
+    for (int i = 0; i < dim; ++i) {
+        double z = 0;
+        for (int j = 0; j < dim; ++j) z = z + ye[j] * M[i * dim + j];
+        if (func_id == 9)
+            f += (z * z - 10.0 * cos(2.0 * ORACLE_PI * z) + 10.0); /* rastrigin_func :668-683 */
+        else
+            f += z * z;                                             /* sphere_func :462-478 */
+    }
+    return f;
+}
+
+void speo_oracle_evaluate_rows(int func_id, const float *x, int n, int ld, int dim,
+                               const float *o, const float *M, double *f_out)
+{
+    double od[SPEO_ORACLE_MAX_DIM], xd[SPEO_ORACLE_MAX_DIM];
+    double *Md = (double *)malloc(sizeof(double) * (size_t)dim * dim);
+    for (int i = 0; i < dim; ++i) od[i] = o[i];
+    for (int i = 0; i < dim * dim; ++i) Md[i] = M[i];
+    for (int r = 0; r < n; ++r) {
+        for (int i = 0; i < dim; ++i) xd[i] = x[(size_t)r * ld + i];
+        f_out[r] = speo_oracle_objective_f64(func_id, xd, od, Md, dim);
+    }
+    free(Md);
+}
+
+/* ---- fused generation (this library's extended semantics) ------------------------------ */
+static int seg_best_row(const float *fit, int64_t row0, int P)
+{
+    int best = 0;
+    float bf = nan_as_inf(fit[row0]);
+    for (int i = 1; i < P; ++i)
+        if (nan_as_inf(fit[row0 + i]) < bf) { bf = nan_as_inf(fit[row0 + i]); best = i; }
+    return best;
+}
+
+int speo_oracle_generation_f32(int n_segs, const int64_t *row0, const int *P, const int *D,
+                               const int *ld, const int *func, const int *strategy,
+                               const float *F, const float *CR, const float *lb, const float *ub,
+                               const float *const *o, const float *const *M, const uint64_t *seed,
+                               uint32_t gen, const float *pop_in, const float *fit_in,
+                               float *pop_out, float *fit_out, float *trial_out,
+                               const float *trial_fit, uint8_t *sel_out)
+{
+    int err = 0;
+    for (int s = 0; s < n_segs; ++s) {
+        const int n = P[s], dim = D[s], l = ld[s];
+        const int64_t base = row0[s];
+        int *perm = (int *)malloc(sizeof(int) * (size_t)n);
+        for (int i = 0; i < n; ++i) perm[i] = i;
+        float *cand = (float *)calloc((size_t)n * l, sizeof(float));
+        const float *pin = pop_in + (size_t)base * l;
+        int best = seg_best_row(fit_in, base, n);
+        speo_oracle_draws dr;
+        memset(&dr, 0, sizeof dr);
+        dr.kind = 0;
+        dr.key[0] = (uint32_t)seed[s];
+        dr.key[1] = (uint32_t)(seed[s] >> 32);
+        dr.gen = gen;
+        dr.pos0 = base;
+        err |= speo_oracle_de_generate_f32(cand, pin, l, dim, n, 1, perm, &CR[s], &F[s],
+                                           &strategy[s], &best, lb[s], ub[s], &dr);
+        double *fd = (double *)malloc(sizeof(double) * (size_t)n);
+        if (!trial_fit) speo_oracle_evaluate_rows(func[s], cand, n, l, dim, o[s], M[s], fd);
+        for (int i = 0; i < n; ++i) {
+            const int64_t row = base + i;
+            const float tf = trial_fit ? trial_fit[row] : (float)fd[i];
+            const int win = tf < fit_in[row];
+            if (sel_out) sel_out[row] = (uint8_t)win;
+            if (trial_out) memcpy(trial_out + (size_t)row * l, cand + (size_t)i * l, sizeof(float) * (size_t)dim);
+            memcpy(pop_out + (size_t)row * l, win ? cand + (size_t)i * l : pin + (size_t)i * l,
+                   sizeof(float) * (size_t)dim);
+            fit_out[row] = win ? tf : fit_in[row];
+        }
+        free(fd);
+        free(cand);
+        free(perm);
+    }
+    return err;
+}
+
+/* ---- ring migration ------------------------------------------------------------------ */
+
+/* k best (ascending (f,row)) and k worst (descending (f,row)) local indices of a segment. */
+static void seg_extremes(const float *fit, int64_t base, int n, int k, int *best, int *worst)
+{
+    unsigned char *taken = (unsigned char *)calloc((size_t)n, 1);
+    for (int t = 0; t < k; ++t) {
+        int b = -1;
+        for (int i = 0; i < n; ++i) {
+            if (taken[i]) continue;
+            if (b < 0) { b = i; continue; }
+            const float fi = nan_as_inf(fit[base + i]), fb = nan_as_inf(fit[base + b]);
+            if (fi < fb) b = i; /* ties keep the lower row */
+        }
+        taken[b] = 1;
+        best[t] = b;
+    }
+    memset(taken, 0, (size_t)n);
+    for (int t = 0; t < k; ++t) {
+        int w = -1;
+        for (int i = n - 1; i >= 0; --i) {
+            if (taken[i]) continue;
+            if (w < 0) { w = i; continue; }
+            const float fi = nan_as_inf(fit[base + i]), fw = nan_as_inf(fit[base + w]);
+            if (fi > fw) w = i; /* ties keep the higher row */
+        }
+        taken[w] = 1;
+        worst[t] = w;
+    }
+    free(taken);
+}
+
+void speo_oracle_ring_migrate(int n_segs, const int64_t *row0, const int *P, const int *D,
+                              const int *ld, const int *ring_next, int k, float *pop, float *fit)
+{
+    int *best = (int *)malloc(sizeof(int) * (size_t)n_segs * k);
+    int *worst = (int *)malloc(sizeof(int) * (size_t)n_segs * k);
+    float *stage = NULL;
+    int maxld = 0;
+    for (int s = 0; s < n_segs; ++s) if (ld[s] > maxld) maxld = ld[s];
+    stage = (float *)malloc(sizeof(float) * (size_t)n_segs * k * (maxld + 1));
+    for (int s = 0; s < n_segs; ++s) {
+        seg_extremes(fit, row0[s], P[s], k, best + s * k, worst + s * k);
+        for (int t = 0; t < k; ++t) {
+            const int64_t row = row0[s] + best[s * k + t];
+            float *dst = stage + ((size_t)s * k + t) * (maxld + 1);
+            memcpy(dst, pop + (size_t)row * ld[s], sizeof(float) * (size_t)D[s]);
+            dst[maxld] = fit[row];
+        }
+    }
+    for (int s = 0; s < n_segs; ++s) {
+        const int t_seg = ring_next[s];
+        if (t_seg < 0) continue;
+        for (int t = 0; t < k; ++t) {
+            const int64_t row = row0[t_seg] + worst[t_seg * k + t];
+            const float *src = stage + ((size_t)s * k + t) * (maxld + 1);
+            memcpy(pop + (size_t)row * ld[t_seg], src, sizeof(float) * (size_t)D[t_seg]);
+            fit[row] = src[maxld];
+        }
+    }
+    free(stage);
+    free(best);
+    free(worst);
+}
+
+/* ---- CPU baseline (FP64 island loop, threads over islands) ------------------------------ */
+typedef struct {
+    int i0, i1, P, D, ld, func_id, gens;
+    double F, CR, lb, ub;
+    const double *o, *M;
+    uint64_t seed;
+    uint32_t gen0;
+    double *pop, *fit;
+    int err;
+} island_job;
+
+static void *island_worker(void *arg)
+{
+    island_job *j = (island_job *)arg;
+    const int P = j->P, l = j->ld, D = j->D;
+    double *cand = (double *)calloc((size_t)P * l, sizeof(double));
+    double *cfit = (double *)malloc(sizeof(double) * (size_t)P);
+    int *perm = (int *)malloc(sizeof(int) * (size_t)P);
+    for (int i = 0; i < P; ++i) perm[i] = i;
+    const int st = 4;
+    for (int isl = j->i0; isl < j->i1; ++isl) {
+        double *pop = j->pop + (size_t)isl * P * l;
+        double *fit = j->fit + (size_t)isl * P;
+        for (int g = 0; g < j->gens; ++g) {
+            speo_oracle_draws dr;
+            memset(&dr, 0, sizeof dr);
+            dr.key[0] = (uint32_t)j->seed;
+            dr.key[1] = (uint32_t)(j->seed >> 32);
+            dr.gen = j->gen0 + (uint32_t)g;
+            dr.pos0 = (int64_t)isl * P;
+            j->err |= speo_oracle_de_generate_f64(cand, pop, l, D, P, 1, perm, &j->CR, &j->F, &st,
+                                                  NULL, j->lb, j->ub, &dr);
+            for (int i = 0; i < P; ++i)
+                cfit[i] = speo_oracle_objective_f64(j->func_id, cand + (size_t)i * l, j->o, j->M, D);
+            speo_oracle_select_f64(pop, fit, cand, cfit, P, l, D, NULL);
+        }
+    }
+    free(cand);
+    free(cfit);
+    free(perm);
+    return NULL;
+}
+
+static void ring_migrate_f64(int n, int P, int D, int ld, int k, double *pop, double *fit)
+{
+    float *ff = (float *)malloc(sizeof(float) * (size_t)n * P);
+    int *best = (int *)malloc(sizeof(int) * (size_t)n * k), *worst = (int *)malloc(sizeof(int) * (size_t)n * k);
+    double *stage = (double *)malloc(sizeof(double) * (size_t)n * k * (D + 1));
+    for (int i = 0; i < n * P; ++i) ff[i] = (float)fit[i];
+    for (int s = 0; s < n; ++s) {
+        seg_extremes(ff, (int64_t)s * P, P, k, best + s * k, worst + s * k);
+        for (int t = 0; t < k; ++t) {
+            const size_t row = (size_t)s * P + best[s * k + t];
+            memcpy(stage + ((size_t)s * k + t) * (D + 1), pop + row * ld, sizeof(double) * (size_t)D);
+            stage[((size_t)s * k + t) * (D + 1) + D] = fit[row];
+        }
+    }
+    for (int s = 0; s < n; ++s) {
+        const int d = (s + 1) % n;
+        for (int t = 0; t < k; ++t) {
+            const size_t row = (size_t)d * P + worst[d * k + t];
+            memcpy(pop + row * ld, stage + ((size_t)s * k + t) * (D + 1), sizeof(double) * (size_t)D);
+            fit[row] = stage[((size_t)s * k + t) * (D + 1) + D];
+        }
+    }
+    free(ff); free(best); free(worst); free(stage);
+}
+
+int64_t speo_oracle_run_islands_f64(int n_islands, int P, int D, int ld, int func_id,
+                                    double F, double CR, double lb, double ub,
+                                    const double *o, const double *M, uint64_t seed,
+                                    uint32_t gen0, int gens, int interval, int k_migrate,
+                                    double *pop, double *fit, int threads)
+{
+    if (threads < 1) threads = 1;
+    if (threads > n_islands) threads = n_islands;
+    int done = 0;
+    while (done < gens) {
+        /* run up to the next migration point (generation counts are 1-based) */
+        int g_abs = (int)gen0 + done;
+        int until = gens - done;
+        if (interval > 0) {
+            const int to_next = interval - (g_abs % interval);
+            if (to_next < until) until = to_next;
+        }
+        pthread_t *tid = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)threads);
+        island_job *jobs = (island_job *)malloc(sizeof(island_job) * (size_t)threads);
+        for (int t = 0; t < threads; ++t) {
+            island_job *j = &jobs[t];
+            j->i0 = (int)((int64_t)n_islands * t / threads);
+            j->i1 = (int)((int64_t)n_islands * (t + 1) / threads);
+            j->P = P; j->D = D; j->ld = ld; j->func_id = func_id; j->gens = until;
+            j->F = F; j->CR = CR; j->lb = lb; j->ub = ub; j->o = o; j->M = M;
+            j->seed = seed; j->gen0 = (uint32_t)g_abs; j->pop = pop; j->fit = fit; j->err = 0;
+            pthread_create(&tid[t], NULL, island_worker, j);
+        }
+        for (int t = 0; t < threads; ++t) pthread_join(tid[t], NULL);
+        free(tid);
+        free(jobs);
+        done += until;
+        if (interval > 0 && ((int)gen0 + done) % interval == 0 && k_migrate > 0 && n_islands > 1)
+            ring_migrate_f64(n_islands, P, D, ld, k_migrate, pop, fit);
+    }
+    return (int64_t)gens * n_islands * P;
+}

@@ -1,0 +1,204 @@
+// common.cuh -- device helpers shared by the sm_103a kernels of libspeo_gb300.
+//
+// Counter-based Philox-4x32-10 draws, the DE mutation/reflection element rules
+// (reference: CUDA_EA_library/kernel_DE_CUDA.cu:160-276), objective terms and the
+// bounded-loop error flags.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/speo_gb300.h"
+
+namespace speo {
+
+constexpr int kRedrawIters = 4096;  // bound of the distinct-index rejection loop
+constexpr int kBoundIters = 64;     // bound of the reflection loop
+
+constexpr uint32_t kTagIdx = 1u;
+constexpr uint32_t kTagCr = 2u;
+constexpr uint32_t kTagInit = 3u;
+
+// ---------------------------------------------------------------------------------------
+// Philox-4x32-10 (Salmon et al., SC'11). Ten rounds, Weyl key schedule.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox(uint4 c, uint2 k)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k.x += 0x9E3779B9u; k.y += 0xBB67AE85u; }
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    }
+    return c;
+}
+
+__device__ __forceinline__ uint2 seed_key(uint64_t seed)
+{
+    return make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+// u32 -> (0, 1]: ((w >> 8) + 1) * 2^-24, exact in binary32.
+__device__ __forceinline__ float u01(uint32_t w)
+{
+    return __fmul_rn(__uint2float_rn((w >> 8) + 1u), 5.9604644775390625e-8f);
+}
+
+__device__ __forceinline__ uint32_t pick(uint4 v, uint32_t i)
+{
+    return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+
+// Sequential index-draw stream of one target: draw k is word k%4 of
+// philox({k/4, row, gen, tag}, key).
+struct IdxStream {
+    uint2 key;
+    uint32_t row, gen, tag;
+    uint32_t k;
+    uint4 blk;
+    __device__ __forceinline__ IdxStream(uint2 key_, uint32_t row_, uint32_t gen_, uint32_t tag_)
+        : key(key_), row(row_), gen(gen_), tag(tag_), k(0), blk(make_uint4(0, 0, 0, 0)) {}
+    __device__ __forceinline__ float next()
+    {
+        if ((k & 3u) == 0) blk = philox(make_uint4(k >> 2, row, gen, tag), key);
+        const float u = u01(pick(blk, k & 3u));
+        ++k;
+        return u;
+    }
+    // (int)(u * n) in binary32, as kernel_DE_CUDA.cu:193 (GPU_SINGLE_PRECISION build).
+    __device__ __forceinline__ int index(int n) { return (int)__fmul_rn(next(), (float)n); }
+};
+
+// The five donor positions of kernel_DE_CUDA.cu:187-212, in [0, S), including the reference's
+// sequential (not pairwise-complete) distinctness check. Returns false if the bounded
+// rejection loop gave up.
+__device__ __forceinline__ bool draw_donors(IdxStream &s, int S, int r[5])
+{
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        r[i] = s.index(S);
+        if (r[i] == S) r[i]--;
+#pragma unroll
+        for (int j = 0; j < i; ++j) {
+            int guard = 0;
+            while (r[i] == r[j]) {
+                r[i] = s.index(S);
+                if (++guard >= kRedrawIters) { ok = false; break; }
+            }
+        }
+        if (r[i] == S) r[i]--;
+    }
+    return ok;
+}
+
+// device_CheckBound (kernel_DE_CUDA.cu:160-170), bounded.
+template <typename T>
+__device__ __forceinline__ T check_bound(T v, T lb, T ub, bool &ok)
+{
+    int it = 0;
+    while ((v < lb) || (v > ub)) {
+        if (v < lb) v = lb + (lb - v);
+        if (v > ub) v = ub - (v - ub);
+        if (++it >= kBoundIters) { ok = false; v = lb; break; }
+    }
+    return v;
+}
+
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+// Mutant element for strategy st (kernel_DE_CUDA.cu:243-276): terms added left to right,
+// each F*(a-b) fused into the running sum.
+template <typename T>
+__device__ __forceinline__ T mutant(int st, T F, T xi, T xb, const T xr[5])
+{
+    T v;
+    switch (st) {
+    case 0: v = fma_rn(F, sub_rn(xr[0], xr[1]), xi); break;
+    case 1: v = fma_rn(F, sub_rn(xr[2], xr[3]), fma_rn(F, sub_rn(xr[0], xr[1]), xi)); break;
+    case 2: v = fma_rn(F, sub_rn(xr[0], xr[1]), fma_rn(F, sub_rn(xb, xi), xi)); break;
+    case 3:
+        v = fma_rn(F, sub_rn(xr[1], xr[2]), fma_rn(F, sub_rn(xr[0], xr[1]), fma_rn(F, sub_rn(xb, xi), xi)));
+        break;
+    case 4: v = fma_rn(F, sub_rn(xr[1], xr[2]), xr[0]); break;
+    case 5: v = fma_rn(F, sub_rn(xr[3], xr[4]), fma_rn(F, sub_rn(xr[1], xr[2]), xr[0])); break;
+    case 6: v = fma_rn(F, sub_rn(xr[0], xr[1]), xb); break;
+    case 7: v = fma_rn(F, sub_rn(xr[2], xr[3]), fma_rn(F, sub_rn(xr[0], xr[1]), xb)); break;
+    case 8: v = fma_rn(F, sub_rn(xr[1], xr[2]), fma_rn(F, sub_rn(xr[0], xi), xi)); break;
+    default: v = xi; break;
+    }
+    return v;
+}
+
+__host__ __device__ __forceinline__ bool strategy_uses_best(int st)
+{
+    return st == 2 || st == 3 || st == 6 || st == 7;
+}
+
+// Objective scale applied to z = M (x - o): F9 shrinks by 5.12/100 (CEC2014.cc:59-62).
+__host__ __device__ __forceinline__ float func_scale(int func_id)
+{
+    return func_id == SPEO_FUNC_ROTATED_RASTRIGIN ? 0.0512f : 1.0f;
+}
+__host__ __device__ __forceinline__ double func_scale_f64(int func_id)
+{
+    return func_id == SPEO_FUNC_ROTATED_RASTRIGIN ? 5.12 / 100.0 : 1.0;
+}
+
+// Per-coordinate objective term. Rastrigin's z^2 - 10 cos(2 pi z) + 10 (CEC2014.cc:680) is
+// computed as z^2 + 20 sin^2(pi z), the same function without the cancellation at z ~ 0.
+__device__ __forceinline__ float obj_term(int func_id, float z)
+{
+    if (func_id == SPEO_FUNC_ROTATED_RASTRIGIN) {
+        const float s = sinpif(z);
+        return __fmaf_rn(z, z, 20.0f * s * s);
+    }
+    return z * z;
+}
+__device__ __forceinline__ double obj_term(int func_id, double z)
+{
+    if (func_id == SPEO_FUNC_ROTATED_RASTRIGIN) {
+        const double s = sinpi(z);
+        return z * z + 20.0 * s * s;
+    }
+    return z * z;
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// NaN ranks as +inf in every best/worst search.
+__device__ __forceinline__ float rank_key(float f) { return isnan(f) ? __int_as_float(0x7f800000) : f; }
+
+// (f, row) "better" order: smaller f, then smaller row.
+__device__ __forceinline__ bool better(float fa, long long ra, float fb, long long rb)
+{
+    return fa < fb || (fa == fb && ra < rb);
+}
+
+}  // namespace speo
+
+// Per-translation-unit device error word and its host accessor (defined by SPEO_DEVERR_TU).
+#define SPEO_DEFINE_DEVERR(name)                                                         \
+    static __device__ unsigned int s_deverr;                                             \
+    extern "C" unsigned int name(void)                                                   \
+    {                                                                                    \
+        unsigned int v = 0, zero = 0;                                                    \
+        if (cudaMemcpyFromSymbol(&v, s_deverr, sizeof v) != cudaSuccess) return 0x80000000u; \
+        cudaMemcpyToSymbol(s_deverr, &zero, sizeof zero);                               \
+        return v;                                                                        \
+    }

@@ -1,0 +1,37 @@
+// host.h -- host-side helpers shared by the translation units of libspeo_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/speo_gb300.h"
+
+namespace speo {
+
+// Records `msg` as this host thread's last error and returns `status`.
+int fail(int status, const char *fmt, ...);
+// Checks a CUDA runtime result; on failure records it and returns SPEO_ERR_CUDA.
+int check_cuda(cudaError_t e, const char *what);
+// Checks the last launch error (no synchronisation).
+int check_launch(const char *what);
+// Stream of the group-1 (reference-shaped) entry points on this host thread.
+cudaStream_t api_stream();
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+// Opaque Philox state behind speo_rng_state* (SPEO_RNG_STATE_BYTES bytes).
+struct RngState {
+    uint32_t key0, key1;  // Philox key = seed
+    uint32_t gen;         // generation counter, advanced by each generate launch
+    uint32_t done;        // blocks finished in the current launch
+    uint32_t pad[12];
+};
+static_assert(sizeof(RngState) == SPEO_RNG_STATE_BYTES, "rng state size");
+
+}  // namespace speo
+
+// Bit readers of the per-translation-unit device error words.
+extern "C" unsigned int speo_deverr_de_ops(void);
+extern "C" unsigned int speo_deverr_objective(void);
+extern "C" unsigned int speo_deverr_generation(void);
+extern "C" unsigned int speo_deverr_tc(void);

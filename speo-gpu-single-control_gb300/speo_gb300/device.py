@@ -1,0 +1,156 @@
+"""Device-side tables for the extended C ABI, built with torch for device memory.
+
+`SegmentTable` holds the population double buffers, the segment descriptors, the planned
+work items and the per-instance (shift, M^T) data in HBM, and calls the library's entry
+points on them. It is the thin host layer the tests and the benchmark drive; the generation
+loop itself (graph capture, migration cadence, best tracking) is in the library's C++
+island driver.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from .instances import rot_layout, shift_layout
+
+
+@dataclass
+class SegmentSpec:
+    pop_size: int
+    dim: int
+    func_id: int
+    instance: int                 # index into the instance list
+    seed: int
+    F: float = 0.5
+    CR: float = 0.9
+    lb: float = -100.0
+    ub: float = 100.0
+    strategy: int = _lib.DE_RAND_1
+    ring_next: int = -1
+    ld: int | None = None
+
+
+def _bytes_to_device(buf: ctypes.Array, device) -> torch.Tensor:
+    host = torch.frombuffer(bytearray(bytes(buf)), dtype=torch.uint8)
+    return host.to(device)
+
+
+@dataclass
+class SegmentTable:
+    specs: list[SegmentSpec]
+    instances: list[tuple[np.ndarray, np.ndarray]]    # (o, M) float32
+    tile_rows: int = _lib.TILE_SIMT
+    device: str = "cuda"
+    rows: int = field(init=False)
+
+    def __post_init__(self):
+        L = _lib.load()
+        dev = torch.device(self.device)
+        self.inst_shift = []
+        self.inst_rot = []
+        for o, M in self.instances:
+            D = o.shape[0]
+            ldr = (D + 3) // 4 * 4
+            self.inst_shift.append(torch.from_numpy(shift_layout(o)).to(dev))
+            self.inst_rot.append(torch.from_numpy(rot_layout(M, ldr)).to(dev))
+        segs = (_lib.Segment * len(self.specs))()
+        row = 0
+        self.max_ld = 0
+        # rows of every segment share one stride so a flat [rows, ld] buffer can hold them
+        self.ld = max((sp.ld or (sp.dim + 3) // 4 * 4) for sp in self.specs)
+        for i, sp in enumerate(self.specs):
+            s = segs[i]
+            s.row0 = row
+            s.pop_size = sp.pop_size
+            s.dim = sp.dim
+            s.ld = self.ld
+            s.func_id = sp.func_id
+            s.strategy = sp.strategy
+            s.F, s.CR, s.lb, s.ub = sp.F, sp.CR, sp.lb, sp.ub
+            s.shift = self.inst_shift[sp.instance].data_ptr()
+            s.rot = self.inst_rot[sp.instance].data_ptr()
+            s.ld_rot = self.inst_rot[sp.instance].shape[1]
+            s.ring_next = sp.ring_next
+            s.seed = sp.seed
+            row += sp.pop_size
+        self.rows = row
+        self.max_ld = self.ld
+        self.host_segs = segs
+        self.d_segs = _bytes_to_device(segs, dev)
+        n = ctypes.c_int(0)
+        _lib.check(L.speo_plan_work(ctypes.addressof(segs), len(self.specs), self.tile_rows, None, 0, ctypes.byref(n)),
+                   "speo_plan_work")
+        items = (_lib.WorkItem * n.value)()
+        _lib.check(L.speo_plan_work(ctypes.addressof(segs), len(self.specs), self.tile_rows, ctypes.addressof(items),
+                                    n.value, ctypes.byref(n)), "speo_plan_work")
+        self.host_items = items
+        self.n_items = n.value
+        self.d_items = _bytes_to_device(items, dev)
+        self.dim_lo = min(sp.dim for sp in self.specs)
+        self.dim_hi = max(sp.dim for sp in self.specs)
+        self.pop = [torch.zeros(self.rows, self.ld, device=dev), torch.zeros(self.rows, self.ld, device=dev)]
+        self.fit = [torch.zeros(self.rows, device=dev), torch.zeros(self.rows, device=dev)]
+        self.gen = torch.zeros(2, dtype=torch.int32, device=dev)
+        self.cur = 0
+        self.staging = torch.zeros(len(self.specs) * 32 * (self.max_ld + 1), device=dev)
+
+    # -- entry points ------------------------------------------------------------------------
+    @staticmethod
+    def _stream():
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def init_population(self):
+        L = _lib.load()
+        _lib.check(L.speo_init_population(self.d_segs.data_ptr(), len(self.specs), self.d_items.data_ptr(),
+                                          self.n_items, self.pop[self.cur].data_ptr(), self._stream()),
+                   "speo_init_population")
+        self.evaluate()
+
+    def evaluate(self, which: int | None = None, use_tc: bool = False):
+        L = _lib.load()
+        w = self.cur if which is None else which
+        fn = L.speo_evaluate_tc if use_tc else L.speo_evaluate
+        _lib.check(fn(self.d_segs.data_ptr(), self.d_items.data_ptr(), self.n_items, self.dim_lo, self.dim_hi,
+                      self.pop[w].data_ptr(), self.fit[w].data_ptr(), self._stream()), "speo_evaluate")
+
+    def generation(self, use_tc: bool = False, trial_out: torch.Tensor | None = None,
+                   trial_fit_out: torch.Tensor | None = None):
+        L = _lib.load()
+        a, b = self.cur, 1 - self.cur
+        _lib.check(L.speo_generation(self.d_segs.data_ptr(), self.d_items.data_ptr(), self.n_items, self.dim_lo,
+                                     self.dim_hi, self.pop[a].data_ptr(), self.fit[a].data_ptr(),
+                                     self.pop[b].data_ptr(), self.fit[b].data_ptr(), self.gen.data_ptr(),
+                                     int(use_tc), None if trial_out is None else trial_out.data_ptr(),
+                                     None if trial_fit_out is None else trial_fit_out.data_ptr(), self._stream()),
+                   "speo_generation")
+        self.cur = b
+
+    def migrate(self, k: int):
+        L = _lib.load()
+        _lib.check(L.speo_ring_migrate(self.d_segs.data_ptr(), len(self.specs), k, self.pop[self.cur].data_ptr(),
+                                       self.fit[self.cur].data_ptr(), self.staging.data_ptr(), self.max_ld,
+                                       self._stream()), "speo_ring_migrate")
+
+    def best_f64(self):
+        L = _lib.load()
+        n = len(self.specs)
+        rows = torch.zeros(n, dtype=torch.int64, device=self.pop[0].device)
+        errs = torch.zeros(n, dtype=torch.float64, device=self.pop[0].device)
+        _lib.check(L.speo_best_reeval_f64(self.d_segs.data_ptr(), n, self.pop[self.cur].data_ptr(),
+                                          self.fit[self.cur].data_ptr(), rows.data_ptr(), errs.data_ptr(),
+                                          self._stream()), "speo_best_reeval_f64")
+        return rows, errs
+
+    def oracle_segments(self) -> list[dict]:
+        """The segment table as the oracle's dicts (host copies of o and M)."""
+        out = []
+        for i, sp in enumerate(self.specs):
+            o, M = self.instances[sp.instance]
+            out.append(dict(row0=int(self.host_segs[i].row0), P=sp.pop_size, D=sp.dim, ld=self.ld, func=sp.func_id,
+                            strategy=sp.strategy, F=sp.F, CR=sp.CR, lb=sp.lb, ub=sp.ub, o=o, M=M, seed=sp.seed,
+                            ring_next=sp.ring_next))
+        return out

@@ -1,0 +1,64 @@
+"""Generates tests/golden/objective_f9.npz from the reference's own CPU objective.
+
+Run where the reference sources exist (it builds oracle/_ref/libref_cec.so from the
+reference's CUDA_EA_library/CEC2014.cc with `make -C oracle ref`):
+
+    python tests/golden/make_golden.py
+
+For each D the reference supports (CEC2014.cc:318-321) it makes a seeded synthetic instance
+(o, M) in the reference's input_data text format, lets CEC2014::EvaluateFitness (function 9,
+rotated Rastrigin, returns f - f*) evaluate a set of points, and stores inputs and outputs.
+The tests check the oracle's restatement against these values on any machine.
+"""
+from __future__ import annotations
+
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+sys.path.insert(0, str(REPO / "speo-gpu-single-control_gb300"))
+sys.path.insert(0, str(REPO / "oracle"))
+
+from speo_gb300.instances import make_instance, run_seed, write_reference_data  # noqa: E402
+
+DIMS = (10, 30, 50, 100)
+N_POINTS = 24
+
+
+def main() -> None:
+    subprocess.run(["make", "-s", "-C", str(REPO / "oracle"), "ref"], check=True)
+    import speo_oracle
+
+    ref = speo_oracle.ref_lib()
+    assert ref is not None, "oracle/_ref/libref_cec.so was not built"
+    out = {}
+    for D in DIMS:
+        seed = run_seed(1, 9, D)
+        o, M = make_instance(seed, D)
+        rng = np.random.default_rng(seed + 7)
+        X = np.empty((N_POINTS, D), dtype=np.float32)
+        X[0] = o                                                   # f(o) = 0
+        X[1] = np.clip(o + rng.normal(0, 1e-3, D), -100, 100)      # near the optimum
+        X[2] = np.clip(o + rng.normal(0, 0.5, D), -100, 100)
+        X[3:] = rng.uniform(-100, 100, (N_POINTS - 3, D))
+        with tempfile.TemporaryDirectory() as tmp:
+            write_reference_data(tmp, 9, o, M)
+            assert ref.ref_cec_init(9, D, tmp.encode()) == 0
+            Xd = np.ascontiguousarray(X, dtype=np.float64)
+            f = np.zeros(N_POINTS, dtype=np.float64)
+            ref.ref_cec_eval_batch(Xd.ctypes.data, N_POINTS, D, f.ctypes.data)
+        out[f"o_{D}"] = o
+        out[f"M_{D}"] = M
+        out[f"X_{D}"] = X
+        out[f"f_{D}"] = f
+    np.savez_compressed(HERE / "objective_f9.npz", **out)
+    print("wrote", HERE / "objective_f9.npz")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,147 @@
+"""CPU tests of the C ABI: the library loads, exports every declared entry point, its
+by-value structs have the reference's layouts, and host-side logic (work planning, argument
+validation) behaves without a GPU."""
+from __future__ import annotations
+
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+REPO = Path(__file__).resolve().parent.parent
+HEADER = REPO / "include" / "speo_gb300.h"
+REF_LIB_DIR = Path("/root/reference/SPEO-GPU-single-control/CUDA_EA_library")
+
+
+def declared_functions() -> list[str]:
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:SPEO_API\s+)?(?:const\s+)?(?:int|void|char)\s*\*?\s*([A-Za-z_]\w*)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_reference_entry_points():
+    names = declared_functions()
+    for ref_name in ("API_Initilize", "API_CheckCUDAError", "API_DE_GenerateNewPopulation", "API_DE_SelectSurvival",
+                     "API_evaluateFitness"):
+        assert ref_name in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.speo_version()
+
+
+def _segments(P_list, D=30):
+    from speo_gb300 import _lib
+
+    segs = (_lib.Segment * len(P_list))()
+    row = 0
+    for i, P in enumerate(P_list):
+        segs[i].row0, segs[i].pop_size, segs[i].dim, segs[i].ld = row, P, D, 32
+        row += P
+    return segs
+
+
+@pytest.mark.parametrize("tile", [1, 50, 64, 128])
+def test_plan_work_covers_rows_once(lib, tile):
+    from speo_gb300 import _lib
+
+    P_list = [100, 4, 257, 64, 1000]
+    segs = _segments(P_list)
+    n = ctypes.c_int()
+    assert lib.speo_plan_work(ctypes.addressof(segs), len(P_list), tile, None, 0, ctypes.byref(n)) == 0
+    items = (_lib.WorkItem * n.value)()
+    assert lib.speo_plan_work(ctypes.addressof(segs), len(P_list), tile, ctypes.addressof(items), n.value,
+                              ctypes.byref(n)) == 0
+    for s, P in enumerate(P_list):
+        mine = sorted((it.first, it.count) for it in items if it.segment == s)
+        covered = np.zeros(P, dtype=int)
+        for a, c in mine:
+            assert 1 <= c <= tile
+            covered[a:a + c] += 1
+        assert np.all(covered == 1)
+        counts = [c for _, c in mine]
+        assert max(counts) - min(counts) <= 1          # balanced tiles
+
+
+def test_plan_work_rejects_bad_input(lib):
+    segs = _segments([10])
+    n = ctypes.c_int()
+    assert lib.speo_plan_work(ctypes.addressof(segs), 1, 0, None, 0, ctypes.byref(n)) == 1
+    segs[0].pop_size = 0
+    assert lib.speo_plan_work(ctypes.addressof(segs), 1, 8, None, 0, ctypes.byref(n)) == 1
+    assert b"pop_size" in lib.speo_last_error()
+
+
+def test_dropin_validation_happens_before_any_device_work(lib):
+    """Invalid shapes are reported as status codes (the reference exits instead)."""
+    from speo_gb300 import _lib
+
+    pop = _lib.PopulationF32(1, 1)        # never dereferenced: validation fails first
+    ii = _lib.IslandInfo(10, 3, 1)        # 10 not divisible by 3
+    pi = _lib.ProblemInfoF32(30, 9, 1, 0, 1, 0, 0, 100.0, -100.0)
+    assert lib.API_DE_SelectSurvival_f32(pop, pop, ii, pi) == _lib.SPEO_ERR_INVALID_ARG
+    assert b"divisible" in lib.speo_last_error()
+    ii = _lib.IslandInfo(10, 1, 1)
+    pi.dim = 0
+    assert lib.API_Initilize_f32(pop, None, ii, pi) == _lib.SPEO_ERR_INVALID_ARG
+    pi.dim = 300
+    assert lib.API_Initilize_f32(pop, None, ii, pi) == _lib.SPEO_ERR_INVALID_ARG
+
+
+def test_evaluate_rejects_unimplemented_function_id(lib):
+    lib.API_evaluateFitness_f32(*([ctypes.c_void_p(1)] * 10), 100, 30, 0.0, 5)
+    assert b"function_ID 5" in lib.speo_last_error()
+
+
+def test_struct_layouts_match_c(tmp_path):
+    """sizeof/offsetof of the ABI structs from a C compile of the header agree with ctypes."""
+    from speo_gb300 import _lib
+
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "speo_gb300.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(speo_segment), offsetof(speo_segment, shift),
+         offsetof(speo_segment, seed), sizeof(speo_work_item), sizeof(speo_problem_info_f64),
+         offsetof(speo_problem_info_f64, max_bound), sizeof(speo_de_info_f64), sizeof(speo_island_info));
+  return 0; }
+'''
+    build = tmp_path
+    (build / "abi_probe.c").write_text(src)
+    exe = build / "abi_probe"
+    subprocess.run(["gcc", "-I", str(REPO / "include"), str(build / "abi_probe.c"), "-o", str(exe)], check=True)
+    vals = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    expect = [ctypes.sizeof(_lib.Segment), _lib.Segment.shift.offset, _lib.Segment.seed.offset,
+              ctypes.sizeof(_lib.WorkItem), ctypes.sizeof(_lib.ProblemInfoF64), _lib.ProblemInfoF64.max_bound.offset,
+              ctypes.sizeof(_lib.DEInfoF64), ctypes.sizeof(_lib.IslandInfo)]
+    assert vals == expect
+
+
+@pytest.mark.skipif(not (REF_LIB_DIR / "config.h").exists(), reason="reference sources not present")
+def test_problem_info_layout_matches_reference_config(tmp_path):
+    """speo_problem_info_f64 has the layout of the reference's ProblemInfo with real = double
+    (CUDA_EA_library/config.h:31-34,48-59), so by-value calls bind unchanged."""
+    src = r'''
+#include "config.h"
+#include "speo_gb300.h"
+#include <cstddef>
+static_assert(sizeof(ProblemInfo) == sizeof(speo_problem_info_f64), "size");
+static_assert(offsetof(ProblemInfo, max_bound) == offsetof(speo_problem_info_f64, max_bound), "max_bound");
+static_assert(offsetof(ProblemInfo, min_bound) == offsetof(speo_problem_info_f64, min_bound), "min_bound");
+static_assert(offsetof(ProblemInfo, seed) == offsetof(speo_problem_info_f64, seed), "seed");
+int main() { return 0; }
+'''
+    build = tmp_path
+    (build / "abi_ref.cc").write_text(src)
+    subprocess.run(["g++", "-fsyntax-only", "-I", str(REF_LIB_DIR), "-I", str(REPO / "include"),
+                    str(build / "abi_ref.cc")], check=True)

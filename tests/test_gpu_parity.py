@@ -1,0 +1,294 @@
+"""GPU parity tests: every entry point called through the C ABI against the CPU oracle.
+
+Bars: trial vectors, donor/crossover draws, best ids, selection decisions and migrated rows
+bit-exact; FP32 fitness within relative 1e-5 of the FP64 oracle (FP64 entry points 1e-12).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIT_RTOL_F32 = 1e-5      # FP32 fitness vs FP64 oracle
+FIT_ATOL_F32 = 1e-6      # absolute floor for fitness values near 0
+FIT_RTOL_F64 = 1e-12
+
+
+def np2(D):
+    y = 1
+    while y < D:
+        y <<= 1
+    return max(32, y)
+
+
+def _assert_fitness(gpu, ref, rtol=FIT_RTOL_F32, atol=FIT_ATOL_F32):
+    gpu = np.asarray(gpu, dtype=np.float64)
+    err = np.abs(gpu - ref)
+    bad = err > rtol * np.abs(ref) + atol
+    assert not bad.any(), f"max rel err {np.max(err / np.maximum(np.abs(ref), 1e-30)):.3e} at {np.argmax(bad)}"
+
+
+# ---------------------------------------------------------------------------------------------
+# drop-in (reference-shaped) entry points
+# ---------------------------------------------------------------------------------------------
+class DropIn:
+    def __init__(self, lib, cuda, P, D, nsub, f64, seed=1234):
+        import torch
+        from speo_gb300 import _lib
+
+        self.torch, self._lib, self.lib = torch, _lib, lib
+        self.P, self.D, self.nsub, self.f64 = P, D, nsub, f64
+        self.ld = np2(D)
+        self.dt = torch.float64 if f64 else torch.float32
+        self.np_dt = np.float64 if f64 else np.float32
+        z = lambda *s: torch.zeros(*s, dtype=self.dt, device=cuda)
+        self.pop, self.cand = z(P, self.ld), z(P, self.ld)
+        self.pfit, self.cfit = z(P), z(P)
+        self.rng = torch.zeros(16, dtype=torch.int32, device=cuda)
+        self.best = torch.zeros(nsub, dtype=torch.int32, device=cuda)
+        self.perm = torch.arange(P, dtype=torch.int32, device=cuda)
+        self.Pop = _lib.PopulationF64 if f64 else _lib.PopulationF32
+        self.PI = _lib.ProblemInfoF64 if f64 else _lib.ProblemInfoF32
+        self.DI = _lib.DEInfoF64 if f64 else _lib.DEInfoF32
+        self.sfx = "" if f64 else "_f32"
+        self.seed = seed
+        self.problem = self.PI(D, 9, 1, 0, seed, 0, 0, 100.0, -100.0)
+
+    def pops(self):
+        return (self.Pop(self.pop.data_ptr(), self.pfit.data_ptr()), self.Pop(self.cand.data_ptr(),
+                                                                              self.cfit.data_ptr()))
+
+    def island(self):
+        return self._lib.IslandInfo(self.P, self.nsub, self.perm.data_ptr())
+
+    def call(self, name, *args):
+        st = getattr(self.lib, name + self.sfx)(*args)
+        self._lib.check(st, name)
+        self._lib.check(self.lib.API_CheckCUDAError(), "API_CheckCUDAError")
+
+
+@pytest.mark.parametrize("P,D", [(100, 30), (64, 10), (17, 1), (33, 100)])
+def test_dropin_init_matches_oracle(lib, oracle, cuda, P, D):
+    d = DropIn(lib, cuda, P, D, 1, False, seed=99)
+    pop, _ = d.pops()
+    d.call("API_Initilize", pop, d.rng.data_ptr(), d.island(), d.problem)
+    ref = oracle.init_population(P, d.ld, D, -100.0, 100.0, 99)
+    assert np.array_equal(d.pop.cpu().numpy(), ref)       # every row, also past 16*floor(P/16)
+    st = d.rng.cpu().numpy()
+    assert st[0] == 99 and st[1] == 0 and st[2] == 0 and st[3] == 0
+
+
+@pytest.mark.parametrize("f64", [False, True])
+@pytest.mark.parametrize("P,D,nsub", [(100, 30, 4), (64, 10, 1), (96, 100, 3), (8, 1, 2), (40, 33, 10)])
+def test_dropin_generate_matches_oracle(lib, oracle, cuda, f64, P, D, nsub):
+    import torch
+
+    d = DropIn(lib, cuda, P, D, nsub, f64, seed=P * 7 + D)
+    scratch = d.Pop(d.cand.data_ptr(), d.cfit.data_ptr())
+    d.call("API_Initilize", scratch, d.rng.data_ptr(), d.island(), d.problem)     # key + gen = 0
+    rng = np.random.default_rng(P + D)
+    pop = np.zeros((P, d.ld), dtype=d.np_dt)
+    pop[:, :D] = rng.uniform(-100, 100, (P, D)).astype(np.float32)
+    fit = rng.uniform(0, 1000, P).astype(np.float32).astype(d.np_dt)
+    fit[rng.integers(0, P)] = fit[rng.integers(0, P)]          # ties
+    perm = rng.permutation(P).astype(np.int32)
+    S = P // nsub
+    strat = np.array([i % 9 for i in range(nsub)], dtype=np.int32)
+    CR = np.array([0.9 if i % 2 == 0 else 0.1 for i in range(nsub)], dtype=d.np_dt)
+    F = np.full(nsub, 0.5, dtype=d.np_dt)
+    info = (d.DI * nsub)(*[d.DI(float(CR[i]), float(F[i]), int(strat[i]), S) for i in range(nsub)])
+    d_info = torch.frombuffer(bytearray(bytes(info)), dtype=torch.uint8).to(cuda)
+    d.pop.copy_(torch.from_numpy(pop))
+    d.pfit.copy_(torch.from_numpy(fit))
+    d.perm.copy_(torch.from_numpy(perm))
+    d.cand.zero_()
+    pop_s, cand_s = d.pops()
+    for gen in range(2):
+        d.call("API_DE_GenerateNewPopulation", cand_s, pop_s, d.best.data_ptr(), d.island(), d_info.data_ptr(),
+               d.rng.data_ptr(), d.problem)
+        best_ref = oracle.best_per_subisland(fit.astype(np.float32), nsub, perm)
+        assert np.array_equal(d.best.cpu().numpy(), best_ref)
+        cand_ref = np.zeros_like(pop) if gen == 0 else cand_ref
+        err = oracle.de_generate(cand_ref, pop, d.ld, D, perm, CR, F, strat, best_ref, -100.0, 100.0,
+                                 oracle.philox_draws(d.seed, gen), f64=f64)
+        assert err == 0
+        got = d.cand.cpu().numpy()
+        assert np.array_equal(got, cand_ref), f"gen {gen}: {np.argwhere(got != cand_ref)[:5]}"
+        assert int(d.rng.cpu()[2]) == gen + 1                    # generation counter advanced once
+
+
+@pytest.mark.parametrize("f64", [False, True])
+def test_dropin_select_matches_oracle(lib, oracle, cuda, f64):
+    import torch
+
+    P, D = 100, 30
+    d = DropIn(lib, cuda, P, D, 1, f64)
+    rng = np.random.default_rng(4)
+    pop = rng.uniform(-100, 100, (P, d.ld)).astype(d.np_dt)
+    cand = rng.uniform(-100, 100, (P, d.ld)).astype(d.np_dt)
+    pf = rng.uniform(0, 10, P).astype(d.np_dt)
+    cf = rng.uniform(0, 10, P).astype(d.np_dt)
+    cf[::7] = pf[::7]                                   # ties keep the parent
+    cf[3] = np.nan
+    for t, a in ((d.pop, pop), (d.cand, cand), (d.pfit, pf), (d.cfit, cf)):
+        t.copy_(torch.from_numpy(a))
+    pop_s, cand_s = d.pops()
+    d.call("API_DE_SelectSurvival", pop_s, cand_s, d.island(), d.problem)
+    oracle.select(pop, pf, cand, cf, d.ld, D, f64=f64)
+    assert np.array_equal(d.pop.cpu().numpy(), pop)
+    assert np.array_equal(d.pfit.cpu().numpy(), pf)
+
+
+@pytest.mark.parametrize("f64", [False, True])
+@pytest.mark.parametrize("fid", [9, 31])
+@pytest.mark.parametrize("P,D", [(100, 10), (130, 30), (64, 50), (70, 100), (5, 200)])
+def test_dropin_evaluate_matches_oracle(lib, oracle, cuda, f64, fid, P, D):
+    import torch
+    from speo_gb300.instances import make_instance
+
+    o, M = make_instance(P * 31 + D, D)
+    ld = np2(D)
+    rng = np.random.default_rng(D)
+    X = np.zeros((P, ld), dtype=np.float32)
+    X[:, :D] = rng.uniform(-100, 100, (P, D))
+    X[0, :D] = o
+    X[1, :D] = o + rng.normal(0, 1e-3, D).astype(np.float32)
+    dt = torch.float64 if f64 else torch.float32
+    rot = np.zeros((ld, D), dtype=np.float32)        # reference layout: B[k][j] = M[j][k], zero rows k >= D
+    rot[:D, :] = M.T
+    shift = np.zeros(ld, dtype=np.float32)
+    shift[:D] = o
+    tX, trot, tsh = (torch.from_numpy(a).to(cuda, dt) for a in (X, rot, shift))
+    f = torch.zeros(P, dtype=dt, device=cuda)
+    fn = lib.API_evaluateFitness if f64 else lib.API_evaluateFitness_f32
+    fn(f.data_ptr(), None, None, tX.data_ptr(), tsh.data_ptr(), trot.data_ptr(), None, None, None, None, P, D, 0.0,
+       fid)
+    from speo_gb300 import _lib
+    _lib.check(lib.API_CheckCUDAError(), "API_evaluateFitness")
+    ref = oracle.evaluate_rows(fid, X, D, o, M)
+    assert float(f[0]) == 0.0
+    if f64:
+        np.testing.assert_allclose(f.cpu().numpy(), ref, rtol=FIT_RTOL_F64, atol=1e-12)
+    else:
+        _assert_fitness(f.cpu().numpy(), ref)
+
+
+# ---------------------------------------------------------------------------------------------
+# extended entry points: fused generation, migration, FP64 best re-evaluation
+# ---------------------------------------------------------------------------------------------
+def _table(cuda, layout, n_inst=None, ring=False, seed=7):
+    from speo_gb300.device import SegmentSpec, SegmentTable
+    from speo_gb300.instances import make_instance
+
+    dims = sorted({D for (_, D, _, _) in layout})
+    inst = {}
+    instances = []
+    specs = []
+    for i, (P, D, fid, strategy) in enumerate(layout):
+        key = (D, fid if n_inst is None else i % n_inst)
+        if key not in inst:
+            inst[key] = len(instances)
+            instances.append(make_instance(seed * 1000 + D * 10 + len(instances), D))
+        specs.append(SegmentSpec(pop_size=P, dim=D, func_id=fid, instance=inst[key], seed=seed + i,
+                                 strategy=strategy, ring_next=((i + 1) % len(layout)) if ring else -1))
+    return SegmentTable(specs, instances, device=str(cuda))
+
+
+def _check_generations(tab, oracle, n_gen=3):
+    import torch
+
+    segs = tab.oracle_segments()
+    # initial population and its fitness
+    pop0 = tab.pop[tab.cur].cpu().numpy()
+    for s in segs:
+        ref = oracle.init_population(s["P"], tab.ld, s["D"], s["lb"], s["ub"], s["seed"], row0=s["row0"])
+        assert np.array_equal(pop0[s["row0"]:s["row0"] + s["P"]], ref)
+        fref = oracle.evaluate_rows(s["func"], ref, s["D"], s["o"], s["M"])
+        _assert_fitness(tab.fit[tab.cur].cpu().numpy()[s["row0"]:s["row0"] + s["P"]], fref)
+    trial = torch.zeros_like(tab.pop[0])
+    tfit = torch.zeros_like(tab.fit[0])
+    for g in range(n_gen):
+        pin = tab.pop[tab.cur].cpu().numpy()
+        fin = tab.fit[tab.cur].cpu().numpy()
+        tab.generation(trial_out=trial, trial_fit_out=tfit)
+        torch.cuda.synchronize()
+        tf = tfit.cpu().numpy()
+        pout_ref, fout_ref, trials_ref, sel, err = oracle.generation(segs, g, pin, fin, trial_fit=tf)
+        assert err == 0
+        got_trials = trial.cpu().numpy()
+        for s in segs:
+            r = slice(s["row0"], s["row0"] + s["P"])
+            D = s["D"]
+            assert np.array_equal(got_trials[r, :D], trials_ref[r, :D]), f"gen {g} trials differ"
+            _assert_fitness(tf[r], oracle.evaluate_rows(s["func"], trials_ref[r], D, s["o"], s["M"]))
+            assert np.array_equal(tab.pop[tab.cur].cpu().numpy()[r, :D], pout_ref[r, :D])
+        assert np.array_equal(tab.fit[tab.cur].cpu().numpy(), fout_ref)
+        assert int(tab.gen.cpu()[0]) == g + 1 and int(tab.gen.cpu()[1]) == 0
+
+
+@pytest.mark.parametrize("layout", [
+    [(100, 30, 9, 4), (100, 30, 9, 4), (100, 30, 31, 4)],            # config-1 islands, tiles 50 + 50
+    [(128, 100, 9, 4), (128, 100, 31, 5)],                            # config-2 shape
+    [(64, 50, 9, 2), (70, 50, 9, 6), (33, 50, 31, 3)],                # strategies that use the best row
+    [(4, 1, 31, 4), (9, 3, 9, 8), (5, 7, 31, 0)],                     # smallest populations / dims
+    [(40, 200, 9, 4)],                                                # largest column class
+])
+def test_fused_generation_matches_oracle(oracle, cuda, layout):
+    tab = _table(cuda, layout)
+    tab.init_population()
+    _check_generations(tab, oracle)
+
+
+def test_mixed_dims_single_launch_matches_oracle(oracle, cuda):
+    """Batched uneven runs (config-3 shape, scaled down): D and P differ per segment; one
+    kernel launch per generation."""
+    rng = np.random.default_rng(11)
+    layout = [(int(rng.integers(50, 201)), int(rng.choice([10, 30, 50, 100])), int(rng.choice([9, 31])), 4)
+              for _ in range(12)]
+    tab = _table(cuda, layout, n_inst=12)
+    tab.init_population()
+    _check_generations(tab, oracle, n_gen=2)
+
+
+def test_ring_migration_matches_oracle(oracle, cuda):
+    import torch
+
+    tab = _table(cuda, [(100, 30, 9, 4)] * 6, ring=True)
+    tab.init_population()
+    tab.generation()
+    pop = tab.pop[tab.cur].cpu().numpy().copy()
+    fit = tab.fit[tab.cur].cpu().numpy().copy()
+    fit[3] = fit[4]                                     # a tie inside segment 0
+    tab.fit[tab.cur].copy_(torch.from_numpy(fit))
+    tab.migrate(5)
+    torch.cuda.synchronize()
+    oracle.ring_migrate(tab.oracle_segments(), 5, pop, fit)
+    assert np.array_equal(tab.pop[tab.cur].cpu().numpy(), pop)
+    assert np.array_equal(tab.fit[tab.cur].cpu().numpy(), fit)
+
+
+def test_best_reeval_f64_matches_oracle(oracle, cuda):
+    tab = _table(cuda, [(100, 30, 9, 4), (128, 100, 31, 4), (60, 10, 9, 4)])
+    tab.init_population()
+    for _ in range(3):
+        tab.generation()
+    rows, errs = tab.best_f64()
+    fit = tab.fit[tab.cur].cpu().numpy()
+    pop = tab.pop[tab.cur].cpu().numpy()
+    for i, s in enumerate(tab.oracle_segments()):
+        seg_fit = fit[s["row0"]:s["row0"] + s["P"]]
+        assert int(rows[i]) == s["row0"] + int(np.argmin(seg_fit))
+        ref = oracle.objective(s["func"], pop[int(rows[i]), :s["D"]], s["o"], s["M"])
+        assert float(errs[i]) == pytest.approx(ref, rel=1e-12, abs=1e-12)
+
+
+def test_no_device_error_flags(lib, cuda):
+    import ctypes
+
+    tab = _table(cuda, [(100, 30, 9, 4)])
+    tab.init_population()
+    tab.generation()
+    bits = ctypes.c_uint32(0xFFFF)
+    assert lib.speo_device_error_bits(ctypes.byref(bits)) == 0
+    assert bits.value == 0
