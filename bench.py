@@ -225,8 +225,9 @@ def bench_speo(args) -> dict:
         "gpu_launches": epochs * (INTERVAL + 2),
         "clocks": clk.summary(),
     }
-    out["e2e"] = bench_e2e(L, dev, torch, args)
-    if rank == 0:
+    if not args.no_e2e:
+        out["e2e"] = bench_e2e(L, dev, torch, args)
+    if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(sample_s=args.cpu_sample_s)
     return out
 
@@ -353,6 +354,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=500)
     ap.add_argument("--impl", default="speo", choices=["speo", "reference"])
     ap.add_argument("--cpu-sample-s", type=float, default=12.0)
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI leg (profiling runs)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     out = bench_reference(args) if args.impl == "reference" else bench_speo(args)
