@@ -221,9 +221,11 @@ SPEO_API int speo_evaluate(const speo_segment *d_segs, const speo_work_item *d_i
 
 /* Same, with the rotation on the tcgen05 tensor cores: BF16 hi/lo 3-term split product,
  * FP32 accumulation in tensor memory, fused shift/scale/objective/row-reduction epilogue.
- * Tiles are 128 rows; segments need D <= 128 here. */
+ * The population is one flat buffer of n_rows rows, `ld` floats apart, shared by all segments
+ * (it is read with TMA tensor loads); tiles are up to SPEO_TILE_TC rows and D <= 128. */
 SPEO_API int speo_evaluate_tc(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,
-                     int dim_lo, int dim_hi, const float *pop, float *fit, void *stream);
+                     int dim_lo, int dim_hi, const float *pop, int64_t n_rows, int ld, float *fit,
+                     void *stream);
 
 /* One fused DE generation over all work items: for each target row, draw indices and
  * crossover mask from Philox(key=seed, ctr={block,row,gen,tag}), build the trial

@@ -34,6 +34,10 @@ __device__ __forceinline__ uint4 philox(uint4 c, uint2 k)
     return c;
 }
 
+// Out-of-line copy for the rarely refilled index-draw stream: keeps one Philox body in the
+// instruction stream instead of one per draw site.
+__device__ __noinline__ static uint4 philox_block(uint4 c, uint2 k) { return philox(c, k); }
+
 __device__ __forceinline__ uint2 seed_key(uint64_t seed)
 {
     return make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
@@ -61,7 +65,7 @@ struct IdxStream {
         : key(key_), row(row_), gen(gen_), tag(tag_), k(0), blk(make_uint4(0, 0, 0, 0)) {}
     __device__ __forceinline__ float next()
     {
-        if ((k & 3u) == 0) blk = philox(make_uint4(k >> 2, row, gen, tag), key);
+        if ((k & 3u) == 0) blk = philox_block(make_uint4(k >> 2, row, gen, tag), key);
         const float u = u01(pick(blk, k & 3u));
         ++k;
         return u;
@@ -76,11 +80,11 @@ struct IdxStream {
 __device__ __forceinline__ bool draw_donors(IdxStream &s, int S, int r[5])
 {
     bool ok = true;
-#pragma unroll
+#pragma unroll 1
     for (int i = 0; i < 5; ++i) {
         r[i] = s.index(S);
         if (r[i] == S) r[i]--;
-#pragma unroll
+#pragma unroll 1
         for (int j = 0; j < i; ++j) {
             int guard = 0;
             while (r[i] == r[j]) {

@@ -21,7 +21,6 @@ SPEO_DEFINE_DEVERR(speo_deverr_generation)
 namespace speo {
 namespace {
 
-constexpr int kChunk = 32;
 
 __device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 __device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
@@ -79,132 +78,168 @@ struct GenArgs {
 
 __host__ __device__ __forceinline__ int q_class(int D) { return D <= 32 ? 1 : D <= 64 ? 2 : D <= 128 ? 4 : 8; }
 
-// One tile: generate, evaluate, select. Q = accumulator columns per lane (D <= 32Q),
-// QV = float4 chunks per lane (D <= 128 QV). Ys/Ms are this block's shared buffers.
-template <int Q, int QV>
-__device__ __forceinline__ void gen_tile(const GenArgs &a, const speo_work_item &it, const speo_segment &s,
-                                         uint32_t gen, float *Ys, float *Ms, float *s_bf, long long *s_br)
-{
-    constexpr int W = 32 * Q;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const float *__restrict__ pop_in = a.pop_in;
-    const float *__restrict__ fit_in = a.fit_in;
-    float *__restrict__ pop_out = a.pop_out;
-    float *__restrict__ fit_out = a.fit_out;
-    float *trial_out = a.trial_out, *trial_fit_out = a.trial_fit_out;
-    {
-        const int D = s.dim, P = s.pop_size, ld = s.ld;
-        const uint2 key = seed_key(s.seed);
-        const int st = s.strategy;
-        const float F = s.F, CR = s.CR, lb = s.lb, ub = s.ub;
-        const int nch = (D + 3) >> 2;
-        const int ndon = donors_needed(st);
-        __syncthreads();  // previous tile's readers of Ys / Ms are done
-        const long long best_row = strategy_uses_best(st) ? block_seg_best(fit_in, s.row0, P, s_bf, s_br) : -1;
+// Shared-memory plan of one block for column class Q (W = 32Q columns):
+//   Ys[64][W]  (x - o) of the trials      Xs[64][W]  the trials
+//   Ms[KC][W]  rows of M^T                sR[64][8]  donor positions + jrand
+//   sPF[64]    parent fitness             sF[64]     trial fitness
+template <int Q> struct GenPlan {
+    static constexpr int W = 32 * Q;
+    static constexpr int KC = Q <= 2 ? 32 * Q : 32;                 // M^T rows staged at once
+    static constexpr int G = Q == 1 ? 8 : Q == 2 ? 16 : 32;          // lanes per row (float4 chunks)
+    static constexpr int CPL = Q == 8 ? 2 : 1;                       // chunks per lane
+    static constexpr int RPP = 256 / G;                              // rows per pass of the block
+    static constexpr int NPASS = kEvalTile / RPP;
+    static constexpr size_t floats = (size_t)2 * kEvalTile * W + (size_t)KC * W + kEvalTile * 8 + 2 * kEvalTile;
+    static constexpr size_t bytes = floats * sizeof(float);
+};
 
-        // ---- generate: warp w builds rows w*8 .. w*8+7 of the tile --------------------------
-        float4 trial[kRowsPerWarp][QV];
-        bool ok_draw = true, ok_bound = true;
+// One tile: (1) donor indices per row, (2) trials, (3) evaluation, (4) greedy selection.
+template <int Q>
+__device__ __forceinline__ void gen_tile(const GenArgs &a, const speo_work_item &it, const speo_segment &s,
+                                         uint32_t gen, float *smem, float *s_bf, long long *s_br)
+{
+    using Pl = GenPlan<Q>;
+    constexpr int W = Pl::W, G = Pl::G;
+    float *Ys = smem;
+    float *Xs = Ys + kEvalTile * W;
+    float *Ms = Xs + kEvalTile * W;
+    int *sR = reinterpret_cast<int *>(Ms + Pl::KC * W);
+    float *sPF = reinterpret_cast<float *>(sR + kEvalTile * 8);
+    float *sF = sPF + kEvalTile;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int grp = tid / G, gl = tid % G;
+    const float *__restrict__ pop_in = a.pop_in;
+
+    const int D = s.dim, P = s.pop_size, ld = s.ld, count = it.count;
+    const long long row0 = s.row0 + it.first;
+    const uint2 key = seed_key(s.seed);
+    const int st = s.strategy;
+    const float F = s.F, CR = s.CR, lb = s.lb, ub = s.ub;
+    const int nch = (D + 3) >> 2;
+    const int ndon = donors_needed(st);
+
+    __syncthreads();  // the previous tile is done with the shared buffers
+    const long long best_row = strategy_uses_best(st) ? block_seg_best(a.fit_in, s.row0, P, s_bf, s_br) : -1;
+
+    // ---- (1) donor positions and jrand, one thread per row; the rest stage M^T --------------
+    if (tid < count) {
+        IdxStream is(key, (uint32_t)(row0 + tid), gen, kTagIdx);
+        int r[5];
+        if (!draw_donors(is, P, r)) atomicOr(&s_deverr, SPEO_DEVERR_REDRAW_LIMIT);
 #pragma unroll
-        for (int rr = 0; rr < kRowsPerWarp; ++rr) {
-            const int lr = warp * kRowsPerWarp + rr;
-            float *yrow = Ys + lr * W;
-            if (lr < it.count) {
-                const long long row = s.row0 + it.first + lr;
-                IdxStream is(key, (uint32_t)row, gen, kTagIdx);
-                int r[5];
-                ok_draw &= draw_donors(is, P, r);
-                const int jrand = is.index(D);
-                const float *xi = pop_in + row * ld;
-                const float *xb = pop_in + (best_row >= 0 ? best_row : row) * ld;
+        for (int k = 0; k < 5; ++k) sR[tid * 8 + k] = r[k];
+        sR[tid * 8 + 5] = is.index(D);
+        sPF[tid] = a.fit_in[row0 + tid];
+    }
+    load_rot_rows<float, Q>(Ms, s.rot, s.ld_rot, D, 0, min(D, Pl::KC));
+    __syncthreads();
+
+    // ---- (2) trials: G lanes per row, float4 chunks -----------------------------------------
+    bool ok_bound = true;
+#pragma unroll 2
+    for (int p = 0; p < Pl::NPASS; ++p) {
+        const int lr = p * Pl::RPP + grp;
+        float *yrow = Ys + lr * W;
+        float *xrow = Xs + lr * W;
+        if (lr < count) {
+            const long long row = row0 + lr;
+            int r[5];
 #pragma unroll
-                for (int v = 0; v < QV; ++v) {
-                    const int c = lane + 32 * v;
-                    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (c < nch) {
-                        const int e0 = 4 * c;
-                        const float4 ti = ld4(xi + e0);
-                        const float4 tb = best_row >= 0 ? ld4(xb + e0) : ti;
-                        float4 tr[5];
+            for (int k = 0; k < 5; ++k) r[k] = sR[lr * 8 + k];
+            const int jrand = sR[lr * 8 + 5];
+            const float *xi = pop_in + row * ld;
+            const float *xb = pop_in + (best_row >= 0 ? best_row : row) * ld;
 #pragma unroll
-                        for (int k = 0; k < 5; ++k)
-                            tr[k] = k < ndon ? ld4(pop_in + (s.row0 + r[k]) * ld + e0) : ti;
-                        const uint4 w = philox(make_uint4((uint32_t)c, (uint32_t)row, gen, kTagCr), key);
-                        const float4 o4 = ld4(s.shift + e0);
-                        float4 y4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int v = 0; v < Pl::CPL; ++v) {
+                const int c = gl + G * v;
+                if (c >= nch) continue;
+                const int e0 = 4 * c;
+                const float4 ti = ld4(xi + e0);
+                const float4 tb = best_row >= 0 ? ld4(xb + e0) : ti;
+                float4 tr[5];
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            const int e = e0 + q;
-                            if (e < D) {
-                                const float u = u01(pick(w, (uint32_t)q));
-                                float x;
-                                if (e == jrand || u < CR) {
-                                    float xr[5];
+                for (int k = 0; k < 5; ++k) tr[k] = k < ndon ? ld4(pop_in + (s.row0 + r[k]) * ld + e0) : ti;
+                const uint4 w = philox(make_uint4((uint32_t)c, (uint32_t)row, gen, kTagCr), key);
+                const float4 o4 = ld4(s.shift + e0);
+                float4 x4 = make_float4(0.f, 0.f, 0.f, 0.f), y4 = x4;
 #pragma unroll
-                                    for (int k = 0; k < 5; ++k) xr[k] = f4get(tr[k], q);
-                                    x = mutant<float>(st, F, f4get(ti, q), f4get(tb, q), xr);
-                                } else {
-                                    x = f4get(ti, q);
-                                }
-                                x = check_bound<float>(x, lb, ub, ok_bound);
-                                f4set(out, q, x);
-                                f4set(y4, q, __fsub_rn(x, f4get(o4, q)));
-                            }
+                for (int q = 0; q < 4; ++q) {
+                    const int e = e0 + q;
+                    if (e < D) {
+                        const float u = u01(pick(w, (uint32_t)q));
+                        float x;
+                        if (e == jrand || u < CR) {
+                            float xr[5];
+#pragma unroll
+                            for (int k = 0; k < 5; ++k) xr[k] = f4get(tr[k], q);
+                            x = mutant<float>(st, F, f4get(ti, q), f4get(tb, q), xr);
+                        } else {
+                            x = f4get(ti, q);
                         }
-                        st4(yrow + e0, y4);
+                        x = check_bound<float>(x, lb, ub, ok_bound);
+                        f4set(x4, q, x);
+                        f4set(y4, q, __fsub_rn(x, f4get(o4, q)));
                     }
-                    trial[rr][v] = out;
                 }
-            } else {
+                st4(xrow + e0, x4);
+                st4(yrow + e0, y4);
+            }
+        } else if (lr < kEvalTile) {
 #pragma unroll
-                for (int v = 0; v < QV; ++v) {
-                    const int c = lane + 32 * v;
-                    if (c < nch) st4(yrow + 4 * c, make_float4(0.f, 0.f, 0.f, 0.f));
-                    trial[rr][v] = make_float4(0.f, 0.f, 0.f, 0.f);
-                }
+            for (int v = 0; v < Pl::CPL; ++v) {
+                const int c = gl + G * v;
+                if (c < nch) st4(yrow + 4 * c, make_float4(0.f, 0.f, 0.f, 0.f));
             }
         }
-        if (!ok_draw) atomicOr(&s_deverr, SPEO_DEVERR_REDRAW_LIMIT);
-        if (!ok_bound) atomicOr(&s_deverr, SPEO_DEVERR_BOUND_LIMIT);
+    }
+    if (!ok_bound) atomicOr(&s_deverr, SPEO_DEVERR_BOUND_LIMIT);
 
-        // ---- evaluate: z = M (x - o) on CUDA cores ------------------------------------------
-        float acc[kRowsPerWarp][Q];
+    // ---- (3) evaluate: z = M (x - o) on CUDA cores, 8 rows per warp -------------------------
+    float acc[kRowsPerWarp][Q];
 #pragma unroll
-        for (int rr = 0; rr < kRowsPerWarp; ++rr)
+    for (int rr = 0; rr < kRowsPerWarp; ++rr)
 #pragma unroll
-            for (int q = 0; q < Q; ++q) acc[rr][q] = 0.f;
-        for (int kc = 0; kc < D; kc += kChunk) {
-            const int ke = min(kc + kChunk, D);
-            __syncthreads();
+        for (int q = 0; q < Q; ++q) acc[rr][q] = 0.f;
+    for (int kc = 0; kc < D; kc += Pl::KC) {
+        const int ke = min(kc + Pl::KC, D);
+        __syncthreads();
+        if (kc > 0) {
             load_rot_rows<float, Q>(Ms, s.rot, s.ld_rot, D, kc, ke);
             __syncthreads();
-            eval_accumulate<float, Q>(acc, Ys, W, warp * kRowsPerWarp, Ms, W, kc, ke, lane);
         }
-        float f[kRowsPerWarp];
-        eval_reduce<float, Q>(acc, D, s.func_id, func_scale(s.func_id), lane, f);
-
-        // ---- select: strict `<` (kernel_DE_CUDA.cu:312), write the winner ---------------------
+        eval_accumulate<float, Q>(acc, Ys, W, warp * kRowsPerWarp, Ms, W, kc, ke, lane);
+    }
+    float f[kRowsPerWarp];
+    eval_reduce<float, Q>(acc, D, s.func_id, func_scale(s.func_id), lane, f);
+    if (lane == 0) {
 #pragma unroll
         for (int rr = 0; rr < kRowsPerWarp; ++rr) {
             const int lr = warp * kRowsPerWarp + rr;
-            if (lr >= it.count) continue;
-            const long long row = s.row0 + it.first + lr;
-            const float pf = fit_in[row];
-            const bool win = f[rr] < pf;
-#pragma unroll
-            for (int v = 0; v < QV; ++v) {
-                const int c = lane + 32 * v;
-                if (c < nch) {
-                    const float4 w4 = win ? trial[rr][v] : ld4(pop_in + row * ld + 4 * c);
-                    st4(pop_out + row * ld + 4 * c, w4);
-                    if (trial_out) st4(trial_out + row * ld + 4 * c, trial[rr][v]);
-                }
-            }
-            if (lane == 0) {
-                fit_out[row] = win ? f[rr] : pf;
-                if (trial_fit_out) trial_fit_out[row] = f[rr];
+            if (lr < count) {
+                sF[lr] = f[rr];
+                if (a.trial_fit_out) a.trial_fit_out[row0 + lr] = f[rr];
             }
         }
+    }
+    __syncthreads();
+
+    // ---- (4) select: strict `<` (kernel_DE_CUDA.cu:312); write the winner -------------------
+#pragma unroll 2
+    for (int p = 0; p < Pl::NPASS; ++p) {
+        const int lr = p * Pl::RPP + grp;
+        if (lr >= count) continue;
+        const long long row = row0 + lr;
+        const float pf = sPF[lr], tf = sF[lr];
+        const bool win = tf < pf;
+#pragma unroll
+        for (int v = 0; v < Pl::CPL; ++v) {
+            const int c = gl + G * v;
+            if (c >= nch) continue;
+            const float4 t4 = ld4(Xs + lr * W + 4 * c);
+            st4(a.pop_out + row * ld + 4 * c, win ? t4 : ld4(pop_in + row * ld + 4 * c));
+            if (a.trial_out) st4(a.trial_out + row * ld + 4 * c, t4);
+        }
+        if (gl == 0) a.fit_out[row] = win ? tf : pf;
     }
 }
 
@@ -230,12 +265,10 @@ __device__ __forceinline__ void advance_gen(uint32_t *gen_ctr, uint32_t gen)
 }
 
 // All tiles share one column class.
-template <int Q, int QV>
+template <int Q>
 __global__ void __launch_bounds__(256, 2) k_generation(GenArgs a)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *Ys = reinterpret_cast<float *>(smem_raw);  // [kEvalTile][32Q]  (x - o) of the trials
-    float *Ms = Ys + kEvalTile * 32 * Q;               // [kChunk][32Q]     rows of M^T
+    extern __shared__ __align__(16) float smem_f[];
     __shared__ float s_bf[8];
     __shared__ long long s_br[8];
     const uint32_t gen = *(volatile uint32_t *)a.gen_ctr;
@@ -246,7 +279,7 @@ __global__ void __launch_bounds__(256, 2) k_generation(GenArgs a)
             if (threadIdx.x == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
             continue;
         }
-        gen_tile<Q, QV>(a, it, s, gen, Ys, Ms, s_bf, s_br);
+        gen_tile<Q>(a, it, s, gen, smem_f, s_bf, s_br);
     }
     advance_gen(a.gen_ctr, gen);
 }
@@ -255,8 +288,7 @@ __global__ void __launch_bounds__(256, 2) k_generation(GenArgs a)
 // `max_q` is the largest column class the launch's shared memory was sized for.
 __global__ void __launch_bounds__(256, 2) k_generation_mixed(GenArgs a, int max_q)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *Ys = reinterpret_cast<float *>(smem_raw);
+    extern __shared__ __align__(16) float smem_f[];
     __shared__ float s_bf[8];
     __shared__ long long s_br[8];
     const uint32_t gen = *(volatile uint32_t *)a.gen_ctr;
@@ -268,10 +300,10 @@ __global__ void __launch_bounds__(256, 2) k_generation_mixed(GenArgs a, int max_
             continue;
         }
         switch (q_class(s.dim)) {
-        case 1: gen_tile<1, 1>(a, it, s, gen, Ys, Ys + kEvalTile * 32, s_bf, s_br); break;
-        case 2: gen_tile<2, 1>(a, it, s, gen, Ys, Ys + kEvalTile * 64, s_bf, s_br); break;
-        case 4: gen_tile<4, 1>(a, it, s, gen, Ys, Ys + kEvalTile * 128, s_bf, s_br); break;
-        default: gen_tile<8, 2>(a, it, s, gen, Ys, Ys + kEvalTile * 256, s_bf, s_br); break;
+        case 1: gen_tile<1>(a, it, s, gen, smem_f, s_bf, s_br); break;
+        case 2: gen_tile<2>(a, it, s, gen, smem_f, s_bf, s_br); break;
+        case 4: gen_tile<4>(a, it, s, gen, smem_f, s_bf, s_br); break;
+        default: gen_tile<8>(a, it, s, gen, smem_f, s_bf, s_br); break;
         }
     }
     advance_gen(a.gen_ctr, gen);
@@ -408,7 +440,10 @@ int launch_gen(K kernel, size_t smem, const GenArgs &a, cudaStream_t st, Extra..
     return check_launch("k_generation");
 }
 
-size_t gen_smem(int Q) { return sizeof(float) * (size_t)(kEvalTile + kChunk) * 32 * Q; }
+size_t gen_smem(int Q)
+{
+    return Q == 1 ? GenPlan<1>::bytes : Q == 2 ? GenPlan<2>::bytes : Q == 4 ? GenPlan<4>::bytes : GenPlan<8>::bytes;
+}
 
 }  // namespace
 }  // namespace speo
@@ -436,10 +471,10 @@ extern "C" int speo_generation(const speo_segment *segs, const speo_work_item *i
     const int qlo = q_class(dim_lo), qhi = q_class(dim_hi);
     if (qlo != qhi) return launch_gen(k_generation_mixed, gen_smem(qhi), a, st, qhi);
     switch (qhi) {
-    case 1: return launch_gen(k_generation<1, 1>, gen_smem(1), a, st);
-    case 2: return launch_gen(k_generation<2, 1>, gen_smem(2), a, st);
-    case 4: return launch_gen(k_generation<4, 1>, gen_smem(4), a, st);
-    default: return launch_gen(k_generation<8, 2>, gen_smem(8), a, st);
+    case 1: return launch_gen(k_generation<1>, gen_smem(1), a, st);
+    case 2: return launch_gen(k_generation<2>, gen_smem(2), a, st);
+    case 4: return launch_gen(k_generation<4>, gen_smem(4), a, st);
+    default: return launch_gen(k_generation<8>, gen_smem(8), a, st);
     }
 }
 

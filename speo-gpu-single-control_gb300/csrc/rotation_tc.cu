@@ -1,16 +1,332 @@
-// rotation_tc.cu -- tcgen05 evaluation path (BF16 3-term split product, FP32 accumulation in
-// tensor memory). Placeholder until the kernel lands: the entry points report UNSUPPORTED.
+// rotation_tc.cu -- exact evaluation with the rotation on the tcgen05 tensor cores.
+//
+// Replaces global_ShiftAndRotation + global_f8 (CUDA_EA_library/kernel_CEC2014_CUDA.cu:147-181,
+// 557-587), an FP64 16x16 shared-memory GEMM that writes the rotated population back to HBM,
+// with one pass per 128-row tile:
+//   TMA (cp.async.bulk.tensor.2d) brings the FP32 rows into shared memory (two stages, the
+//   next tile in flight while this one is processed); the block subtracts o and splits
+//   y = y_hi + y_lo into BF16 K-major operands; M (B operand, [N][K] = M[n][k]) is split the
+//   same way once per instance; one thread issues, per 16-wide K step, the three products
+//   y_hi*M_hi + y_hi*M_lo + y_lo*M_hi into an FP32 accumulator in tensor memory
+//   (M = 128 rows, N = D rounded up to 16); four warps read their 32 rows back with
+//   tcgen05.ld, apply the scale and the objective term and reduce each row in registers.
+// Nothing but the fitness is written. D <= 128.
+#include <cuda.h>
+
+#include <cmath>
+
 #include "common.cuh"
 #include "host.h"
+#include "tcgen05.cuh"
 
 SPEO_DEFINE_DEVERR(speo_deverr_tc)
 
+namespace speo {
+namespace {
+
+constexpr int kTileM = 128;
+constexpr int kTmemCols = 128;
+constexpr long long kWaitBudget = 2000000000LL;  // ~1 s at 2 GHz: any wait longer is a failure
+
+__host__ __device__ __forceinline__ int round16(int x) { return (x + 15) & ~15; }
+
+// Row stride of a staged tile: ld padded so that 8 consecutive rows start in different banks.
+__host__ __device__ __forceinline__ int stage_ld(int ld) { return (ld & 7) ? ld : ld + 4; }
+
+struct TcLayout {
+    int kmax;         // round16(max D)
+    int box_x;        // staged row stride (floats)
+    int nstage;       // 1 or 2
+    size_t stage_bytes, a_bytes, b_bytes, off_a, off_b, off_o, off_bar, total;
+};
+
+__host__ __device__ inline TcLayout tc_layout(int dim_hi, int ld, int nstage)
+{
+    TcLayout L;
+    L.kmax = round16(dim_hi);
+    L.box_x = stage_ld(ld);
+    L.nstage = nstage;
+    L.stage_bytes = (size_t)kTileM * L.box_x * 4;
+    L.a_bytes = (size_t)kTileM * L.kmax * 2;         // one of hi / lo
+    L.b_bytes = (size_t)L.kmax * L.kmax * 2;
+    L.off_a = ((L.stage_bytes * nstage) + 1023) & ~(size_t)1023;
+    L.off_b = L.off_a + 2 * L.a_bytes;
+    L.off_o = L.off_b + 2 * L.b_bytes;
+    L.off_bar = (L.off_o + (size_t)L.kmax * 4 + 15) & ~(size_t)15;
+    L.total = L.off_bar + 64;
+    return L;
+}
+
+struct EvalTcArgs {
+    const speo_segment *segs;
+    const speo_work_item *items;
+    int n_items;
+    long long n_rows;
+    int ld;
+    int dim_hi;
+    int nstage;
+    float *fit;
+};
+
+// Builds B = split(M) for an instance: B[n][k] = M[n][k] = rot[k*ld_rot + n] (zero past D).
+__device__ __forceinline__ void build_b(const speo_segment &s, int Kp, uint8_t *b_hi, uint8_t *b_lo, float *so)
+{
+    const int D = s.dim;
+    const int pairs = Kp * (Kp / 8);
+    for (int i = threadIdx.x; i < pairs; i += blockDim.x) {
+        const int n = i % Kp, kc = i / Kp;
+        float v[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int k = 8 * kc + e;
+            v[e] = (n < D && k < D) ? s.rot[(size_t)k * s.ld_rot + n] : 0.f;
+        }
+        uint4 h, l;
+        tc::split8(v, h, l);
+        const uint32_t off = tc::kmajor_offset(n, 8 * kc, Kp);
+        *reinterpret_cast<uint4 *>(b_hi + off) = h;
+        *reinterpret_cast<uint4 *>(b_lo + off) = l;
+    }
+    for (int k = threadIdx.x; k < Kp; k += blockDim.x) so[k] = k < D ? s.shift[k] : 0.f;
+}
+
+// Staged FP32 rows -> y = x - o -> BF16 hi/lo K-major A operand. Rows >= count become zero.
+__device__ __forceinline__ void build_a(const float *stage, int box_x, int count, int D, int Kp, const float *so,
+                                        uint8_t *a_hi, uint8_t *a_lo)
+{
+    const int pairs = kTileM * (Kp / 8);
+    for (int i = threadIdx.x; i < pairs; i += blockDim.x) {
+        const int m = i % kTileM, kc = i / kTileM;
+        float v[8];
+        const float *src = stage + (size_t)m * box_x + 8 * kc;
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int k = 8 * kc + e;
+            v[e] = (m < count && k < D) ? __fsub_rn(src[e], so[k]) : 0.f;
+        }
+        uint4 h, l;
+        tc::split8(v, h, l);
+        const uint32_t off = tc::kmajor_offset(m, 8 * kc, Kp);
+        *reinterpret_cast<uint4 *>(a_hi + off) = h;
+        *reinterpret_cast<uint4 *>(a_lo + off) = l;
+    }
+}
+
+// One thread: the 3-term split product over all K steps into the TMEM accumulator.
+__device__ __forceinline__ void issue_split_mma(uint32_t tmem, const uint8_t *a_hi, const uint8_t *a_lo,
+                                                const uint8_t *b_hi, const uint8_t *b_lo, int Kp, int Np)
+{
+    const uint32_t idesc = tc::idesc_bf16_f32(kTileM, Np);
+    const uint32_t sbo = (uint32_t)Kp * 16;  // 8-row groups
+    const uint32_t lbo = 128;                // adjacent core matrices along K
+    const uint32_t ah = tc::smem_u32(a_hi), al = tc::smem_u32(a_lo);
+    const uint32_t bh = tc::smem_u32(b_hi), bl = tc::smem_u32(b_lo);
+    for (int s = 0; s < Kp / 16; ++s) {
+        const uint32_t koff = (uint32_t)s * 256;  // two core matrices per K step
+        tc::mma_bf16(tmem, tc::smem_desc(al + koff, lbo, sbo), tc::smem_desc(bh + koff, lbo, sbo), idesc, s > 0);
+        tc::mma_bf16(tmem, tc::smem_desc(ah + koff, lbo, sbo), tc::smem_desc(bl + koff, lbo, sbo), idesc, 1);
+        tc::mma_bf16(tmem, tc::smem_desc(ah + koff, lbo, sbo), tc::smem_desc(bh + koff, lbo, sbo), idesc, 1);
+    }
+}
+
+// Warps 0..3, one TMEM lane (= tile row) per thread: f = sum_j term(scale * z_j), j < D.
+__device__ __forceinline__ float epilogue_row(uint32_t tmem, int warp, int D, int Np, int func, float scale)
+{
+    float f = 0.f;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int c = 0; c < Np; c += 16) {
+        float z[16];
+        tc::tmem_ld16(lane_base + (uint32_t)c, z);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            if (c + j < D) f += obj_term(func, z[j] * scale);
+    }
+    return f;
+}
+
+__device__ __forceinline__ bool tc_tile_ok(const speo_work_item &it, const speo_segment &s, const EvalTcArgs &a)
+{
+    return it.count >= 1 && it.count <= kTileM && s.dim >= 1 && s.dim <= a.dim_hi && s.dim <= kTmemCols &&
+           s.ld == a.ld && it.first >= 0 && it.first + it.count <= s.pop_size && s.row0 >= 0 &&
+           s.row0 + it.first + it.count <= a.n_rows;
+}
+
+__global__ void __launch_bounds__(256, 1) k_evaluate_tc(const __grid_constant__ CUtensorMap xmap, EvalTcArgs a)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const TcLayout L = tc_layout(a.dim_hi, a.ld, a.nstage);
+    float *stage[2] = {reinterpret_cast<float *>(smem), reinterpret_cast<float *>(smem + L.stage_bytes)};
+    uint8_t *a_hi = smem + L.off_a, *a_lo = a_hi + L.a_bytes;
+    uint8_t *b_hi = smem + L.off_b, *b_lo = b_hi + L.b_bytes;
+    float *so = reinterpret_cast<float *>(smem + L.off_o);
+    uint64_t *bar_tma = reinterpret_cast<uint64_t *>(smem + L.off_bar);  // [2]
+    uint64_t *bar_mma = bar_tma + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_mma + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (warp == 0) {
+        tc::tmem_alloc(tmem_slot, kTmemCols);
+        tc::tmem_relinquish();
+    }
+    if (tid == 32) {
+        tc::mbar_init(&bar_tma[0], 1);
+        tc::mbar_init(&bar_tma[1], 1);
+        tc::mbar_init(bar_mma, 1);
+        tc::fence_mbar_init();
+        tc::prefetch_tensormap(&xmap);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+
+    // this block's items: blockIdx.x + i * gridDim.x, i < my_items
+    const int my_items = a.n_items > (int)blockIdx.x ? (a.n_items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    auto item_of = [&](int i) { return a.items[blockIdx.x + i * gridDim.x]; };
+    auto issue = [&](int i) {  // thread 0: stage the rows of item i
+        if (i >= my_items) return;
+        const speo_work_item it = item_of(i);
+        const speo_segment &sg = a.segs[it.segment];
+        const int sidx = i % a.nstage;
+        tc::mbar_arrive_expect_tx(&bar_tma[sidx], (uint32_t)L.stage_bytes);
+        const long long y = tc_tile_ok(it, sg, a) ? sg.row0 + it.first : 0;
+        tc::tma_load_2d(stage[sidx], &xmap, 0, (int)y, &bar_tma[sidx]);
+    };
+    if (tid == 0)
+        for (int i = 0; i < a.nstage; ++i) issue(i);
+
+    const float *c_rot = nullptr, *c_shift = nullptr;
+    int c_dim = -1, c_ldrot = -1;
+    uint32_t mma_batches = 0;
+    int i = 0;
+    bool failed = false;
+    for (; i < my_items; ++i) {
+        const speo_work_item it = item_of(i);
+        const speo_segment &s = a.segs[it.segment];
+        const bool ok = tc_tile_ok(it, s, a);
+        const int sidx = i % a.nstage;
+        const bool t_out = !tc::mbar_wait(&bar_tma[sidx], (uint32_t)((i / a.nstage) & 1), kWaitBudget);
+        if (__syncthreads_or(t_out)) { failed = true; break; }
+        const int D = s.dim, Kp = round16(D);
+        if (ok) {
+            if (s.rot != c_rot || s.shift != c_shift || D != c_dim || s.ld_rot != c_ldrot) {
+                build_b(s, Kp, b_hi, b_lo, so);  // no MMA is in flight: the previous epilogue waited
+                c_rot = s.rot; c_shift = s.shift; c_dim = D; c_ldrot = s.ld_rot;
+                __syncthreads();
+            }
+            build_a(stage[sidx], L.box_x, it.count, D, Kp, so, a_hi, a_lo);
+        }
+        tc::fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            issue(i + a.nstage);  // the stage just consumed takes the item after next
+            if (ok) {
+                tc::fence_after_sync();
+                issue_split_mma(tmem, a_hi, a_lo, b_hi, b_lo, Kp, Kp);
+                tc::mma_commit(bar_mma);
+            }
+        }
+        if (!ok) {
+            if (tid == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+            continue;
+        }
+        bool m_out = false;
+        if (warp < 4) {
+            m_out = !tc::mbar_wait(bar_mma, mma_batches & 1u, kWaitBudget);
+            tc::fence_after_sync();
+            if (!m_out) {
+                const float f = epilogue_row(tmem, warp, D, Kp, s.func_id, func_scale(s.func_id));
+                const int m = warp * 32 + lane;
+                if (m < it.count) a.fit[s.row0 + it.first + m] = f;
+            }
+        }
+        ++mma_batches;
+        tc::fence_before_sync();
+        if (__syncthreads_or(m_out)) { failed = true; break; }
+    }
+    if (failed) {
+        // Let the copies and products this block started finish (bounded) before its shared and
+        // tensor memory go away.
+        if (tid == 0) {
+            atomicOr(&s_deverr, SPEO_DEVERR_WAIT_TIMEOUT);
+            for (int j = i; j < my_items && j <= i + a.nstage; ++j)
+                tc::mbar_wait(&bar_tma[j % a.nstage], (uint32_t)((j / a.nstage) & 1), kWaitBudget);
+            tc::mbar_wait(bar_mma, mma_batches & 1u, kWaitBudget);
+        }
+        __syncthreads();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+int max_optin_smem()
+{
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return v;
+}
+
+}  // namespace
+}  // namespace speo
+
 using namespace speo;
 
-extern "C" int speo_evaluate_tc(const speo_segment *, const speo_work_item *, int, int, int, const float *, float *,
-                                void *)
+extern "C" int speo_evaluate_tc(const speo_segment *segs, const speo_work_item *items, int n_items, int dim_lo,
+                                int dim_hi, const float *pop, int64_t n_rows, int ld, float *fit, void *stream)
 {
-    return fail(SPEO_ERR_UNSUPPORTED, "speo_evaluate_tc: not built yet");
+    if (!segs || !items || !pop || !fit || n_items < 1 || n_rows < 1)
+        return fail(SPEO_ERR_INVALID_ARG, "speo_evaluate_tc: bad arguments");
+    if (dim_lo < 1 || dim_hi > kTmemCols || dim_lo > dim_hi)
+        return fail(SPEO_ERR_UNSUPPORTED, "speo_evaluate_tc: D in [%d, %d]; the tensor-core path takes D <= %d",
+                    dim_lo, dim_hi, kTmemCols);
+    if (ld < dim_hi || (ld & 3) || stage_ld(ld) > 256 || ((uintptr_t)pop & 15))
+        return fail(SPEO_ERR_INVALID_ARG, "speo_evaluate_tc: ld %d / alignment", ld);
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return fail(SPEO_ERR_CUDA, "speo_evaluate_tc: cuTensorMapEncodeTiled unavailable");
+    CUtensorMap map;
+    const cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)n_rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)stage_ld(ld), (cuuint32_t)kTileM};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(pop), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(SPEO_ERR_CUDA, "speo_evaluate_tc: cuTensorMapEncodeTiled failed (%d)", (int)r);
+    const int limit = max_optin_smem();
+    int nstage = 2;
+    if ((int)tc_layout(dim_hi, ld, 2).total > limit) nstage = 1;
+    const TcLayout Lay = tc_layout(dim_hi, ld, nstage);
+    if ((int)Lay.total > limit) return fail(SPEO_ERR_UNSUPPORTED, "speo_evaluate_tc: needs %zu B of shared memory", Lay.total);
+    // At least half of the SM's shared memory per block: one block (one TMEM allocation) per SM.
+    const size_t smem = Lay.total > (size_t)limit / 2 + 1024 ? Lay.total : (size_t)limit / 2 + 1024;
+    cudaError_t e = cudaFuncSetAttribute(k_evaluate_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_evaluate_tc)");
+    EvalTcArgs a{segs, items, n_items, (long long)n_rows, ld, dim_hi, nstage, fit};
+    const int grid = n_items < sm_count() ? n_items : sm_count();
+    k_evaluate_tc<<<grid, 256, smem, static_cast<cudaStream_t>(stream)>>>(map, a);
+    return check_launch("k_evaluate_tc");
 }
 
 extern "C" int speo_tc_generation(const speo_segment *, const speo_work_item *, int, int, int, const float *,

@@ -93,7 +93,8 @@ SIGNATURES: dict[str, tuple] = {
     "speo_plan_work": (c_int, [c_void_p, c_int, c_int, c_void_p, c_int, POINTER(c_int)]),
     "speo_init_population": (c_int, [c_void_p, c_int, c_void_p, c_int, c_void_p, c_void_p]),
     "speo_evaluate": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
-    "speo_evaluate_tc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "speo_evaluate_tc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_int64, c_int, c_void_p,
+                                 c_void_p]),
     "speo_generation": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                 c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "speo_ring_migrate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),

@@ -110,12 +110,20 @@ class SegmentTable:
                    "speo_init_population")
         self.evaluate()
 
-    def evaluate(self, which: int | None = None, use_tc: bool = False):
+    def evaluate(self, which: int | None = None, use_tc: bool = False, out: torch.Tensor | None = None):
+        """Fitness of population buffer `which` (default: current) into `out` (default: its own
+        fitness buffer). use_tc selects the tcgen05 BF16x3 kernel (tiles of 128 rows)."""
         L = _lib.load()
         w = self.cur if which is None else which
-        fn = L.speo_evaluate_tc if use_tc else L.speo_evaluate
-        _lib.check(fn(self.d_segs.data_ptr(), self.d_items.data_ptr(), self.n_items, self.dim_lo, self.dim_hi,
-                      self.pop[w].data_ptr(), self.fit[w].data_ptr(), self._stream()), "speo_evaluate")
+        fit = self.fit[w] if out is None else out
+        if use_tc:
+            _lib.check(L.speo_evaluate_tc(self.d_segs.data_ptr(), self.d_items.data_ptr(), self.n_items, self.dim_lo,
+                                          self.dim_hi, self.pop[w].data_ptr(), self.rows, self.ld, fit.data_ptr(),
+                                          self._stream()), "speo_evaluate_tc")
+        else:
+            _lib.check(L.speo_evaluate(self.d_segs.data_ptr(), self.d_items.data_ptr(), self.n_items, self.dim_lo,
+                                       self.dim_hi, self.pop[w].data_ptr(), fit.data_ptr(), self._stream()),
+                       "speo_evaluate")
 
     def generation(self, use_tc: bool = False, trial_out: torch.Tensor | None = None,
                    trial_fit_out: torch.Tensor | None = None):

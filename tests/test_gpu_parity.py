@@ -177,7 +177,7 @@ def test_dropin_evaluate_matches_oracle(lib, oracle, cuda, f64, fid, P, D):
 # ---------------------------------------------------------------------------------------------
 # extended entry points: fused generation, migration, FP64 best re-evaluation
 # ---------------------------------------------------------------------------------------------
-def _table(cuda, layout, n_inst=None, ring=False, seed=7):
+def _table(cuda, layout, n_inst=None, ring=False, seed=7, tile_rows=None):
     from speo_gb300.device import SegmentSpec, SegmentTable
     from speo_gb300.instances import make_instance
 
@@ -192,7 +192,9 @@ def _table(cuda, layout, n_inst=None, ring=False, seed=7):
             instances.append(make_instance(seed * 1000 + D * 10 + len(instances), D))
         specs.append(SegmentSpec(pop_size=P, dim=D, func_id=fid, instance=inst[key], seed=seed + i,
                                  strategy=strategy, ring_next=((i + 1) % len(layout)) if ring else -1))
-    return SegmentTable(specs, instances, device=str(cuda))
+    from speo_gb300 import _lib
+
+    return SegmentTable(specs, instances, device=str(cuda), tile_rows=tile_rows or _lib.TILE_SIMT)
 
 
 def _check_generations(tab, oracle, n_gen=3):
@@ -292,3 +294,43 @@ def test_no_device_error_flags(lib, cuda):
     bits = ctypes.c_uint32(0xFFFF)
     assert lib.speo_device_error_bits(ctypes.byref(bits)) == 0
     assert bits.value == 0
+
+
+# ---------------------------------------------------------------------------------------------
+# tcgen05 evaluation (BF16 hi/lo 3-term split, FP32 accumulation)
+# ---------------------------------------------------------------------------------------------
+TC_RTOL = 2e-4      # split-BF16 products carry ~2^-16 relative error per term
+
+
+@pytest.mark.parametrize("layout", [
+    [(100, 30, 9, 4)] * 3,                              # config-1 islands, one 100-row tile each
+    [(128, 100, 9, 4), (128, 100, 31, 4)],              # config-2 islands
+    [(300, 50, 31, 4), (257, 50, 9, 4)],                # several tiles per segment, ragged last tile
+    [(64, 10, 9, 4), (33, 16, 31, 4), (70, 2, 9, 4)],   # mixed small D, one launch
+    [(200, 128, 9, 4)],                                 # largest D of the tensor-core path
+])
+def test_evaluate_tc_matches_oracle(oracle, cuda, layout):
+    import torch
+    from speo_gb300 import _lib
+
+    tab = _table(cuda, layout, n_inst=len(layout), tile_rows=_lib.TILE_TC)
+    tab.init_population()
+    pop = tab.pop[tab.cur].cpu().numpy()
+    pop_dev = tab.pop[tab.cur]
+    for s in tab.oracle_segments()[:1]:           # include x = o (f = 0 exactly) and x ~ o
+        pop[s["row0"], :s["D"]] = s["o"]
+        pop[s["row0"] + 1, :s["D"]] = s["o"] + np.float32(1e-3)
+    pop_dev.copy_(torch.from_numpy(pop))
+    out = torch.full_like(tab.fit[0], float("nan"))
+    tab.evaluate(use_tc=True, out=out)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    worst = 0.0
+    for s in tab.oracle_segments():
+        r = slice(s["row0"], s["row0"] + s["P"])
+        ref = oracle.evaluate_rows(s["func"], pop[r], s["D"], s["o"], s["M"])
+        rel = np.abs(got[r] - ref) / np.maximum(np.abs(ref), 1e-30)
+        worst = max(worst, float(np.max(np.where(ref > 1e-3, rel, 0))))
+        np.testing.assert_allclose(got[r], ref, rtol=TC_RTOL, atol=1e-4)
+    assert got[0] == 0.0
+    print(f"max relative error of the BF16x3 tensor-core fitness: {worst:.2e}")
