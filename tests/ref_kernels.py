@@ -1,0 +1,70 @@
+"""Runs the reference's own DE / EA CUDA kernels (compiled from its sources into
+oracle/_ref/*.fatbin) and this project's XORWOW capture kernel through the CUDA driver API.
+
+Test helper only: it lets the tests pin the oracle's DE restatement against the reference's
+GPU kernel on identical cuRAND streams.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_int, c_uint, c_void_p
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent.parent
+REF_DIR = REPO / "oracle" / "_ref"
+CAPTURE = REPO / "oracle" / "lib" / "xorwow_capture.fatbin"
+
+# Itanium-mangled names of the reference's kernels (host stub names of the same build).
+K_SETUP = b"_Z23global_SetupRandomStateP17curandStateXORWOWi"
+K_INIT = b"_Z22global_InitiPopulation14GPU_PopulationP17curandStateXORWOW11ProblemInfo"
+K_BEST = b"_Z36global_DE_FindBestIndividualInIslandPi14GPU_Population14GPU_IslandInfo11ProblemInfo"
+K_GEN = b"_Z31global_DE_GenerateNewPopulation14GPU_PopulationS_Pi14GPU_IslandInfoP6DEInfoP17curandStateXORWOW11ProblemInfo"
+K_SEL = b"_Z24global_DE_SelectSurvival14GPU_PopulationS_11ProblemInfo"
+CURAND_STATE_BYTES = 48  # sizeof(curandStateXORWOW)
+
+
+def available(precision: str) -> bool:
+    return all((REF_DIR / f"ref_{k}_{precision}.fatbin").exists() for k in ("de", "ea")) and CAPTURE.exists()
+
+
+class Driver:
+    def __init__(self):
+        self.cu = ctypes.CDLL("libcuda.so.1")
+        self._mods = {}
+
+    def check(self, r, what):
+        if r != 0:
+            raise RuntimeError(f"{what}: CUresult {r}")
+
+    def module(self, path: Path):
+        if path not in self._mods:
+            data = path.read_bytes()
+            buf = ctypes.create_string_buffer(data, len(data))
+            mod = c_void_p()
+            self.check(self.cu.cuModuleLoadData(byref(mod), buf), f"cuModuleLoadData({path.name})")
+            self._mods[path] = (mod, buf)
+        return self._mods[path][0]
+
+    def function(self, path: Path, name: bytes):
+        fn = c_void_p()
+        self.check(self.cu.cuModuleGetFunction(byref(fn), self.module(path), name), f"cuModuleGetFunction({name})")
+        return fn
+
+    def launch(self, fn, grid, block, args):
+        """args: ctypes objects (scalars or Structures), passed by value."""
+        ptrs = (c_void_p * len(args))(*[ctypes.cast(ctypes.pointer(a), c_void_p) for a in args])
+        self.check(self.cu.cuLaunchKernel(fn, c_uint(grid[0]), c_uint(grid[1]), c_uint(grid[2]), c_uint(block[0]),
+                                          c_uint(block[1]), c_uint(block[2]), c_uint(0), None, ptrs, None),
+                   "cuLaunchKernel")
+        self.check(self.cu.cuCtxSynchronize(), "cuCtxSynchronize")
+
+
+def de_config(pop_size: int):
+    """CalConfigurations / CalConfigurationsDE (kernel_EA_CUDA.cu:7-21, kernel_DE_CUDA.cu:48-62)."""
+    if pop_size > 16:
+        return (pop_size // 16, 1, 1), (32, 16, 1)
+    return (1, 1, 1), (32, pop_size, 1)
+
+
+def c_int_(v):
+    return c_int(v)
