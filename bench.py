@@ -112,24 +112,47 @@ def island_table(device: str, rank: int):
     return SegmentTable(specs, inst, tile_rows=50, device=device)
 
 
-def capture_epoch(tab, torch):
-    """One CUDA graph = INTERVAL generations (an even number, so the buffers end where they
-    started) + the ring migration."""
-    assert INTERVAL % 2 == 0
+def capture(torch, fn):
+    """CUDA graph of fn() (fn run once outside capture first to set kernel attributes)."""
     g = torch.cuda.CUDAGraph()
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
-        start = tab.cur
-        tab.generation()          # warm the kernel variant (sets its smem attribute) outside capture
-        tab.generation()
-        assert tab.cur == start
+        fn()
         with torch.cuda.graph(g, stream=s):
-            for _ in range(INTERVAL):
-                tab.generation()
-            tab.migrate(MIGRANTS)
+            fn()
     torch.cuda.current_stream().wait_stream(s)
     return g
+
+
+def capture_epoch(tab, torch):
+    """One CUDA graph = INTERVAL generations + the ring migration. Islands that fit one block's
+    shared memory run the epoch as one resident launch; otherwise INTERVAL fused launches (an
+    even number, so the double buffers end where they started)."""
+    assert INTERVAL % 2 == 0
+    if tab.epoch_fits():
+        def epoch():
+            tab.epoch(INTERVAL)
+            tab.migrate(MIGRANTS)
+        return capture(torch, epoch), "resident"
+
+    def epoch():
+        for _ in range(INTERVAL):
+            tab.generation()
+        tab.migrate(MIGRANTS)
+    return capture(torch, epoch), "per-generation"
+
+
+def time_graph(torch, graph, reps, flush):
+    flush_l2(flush)
+    s = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for _ in range(reps):
+        graph.replay()
+    b.record(s)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
 
 
 def bench_speo(args) -> dict:
@@ -149,7 +172,7 @@ def bench_speo(args) -> dict:
     L = _lib.load()
     tab = island_table(dev, rank)
     tab.init_population()
-    graph = capture_epoch(tab, torch)
+    graph, mode = capture_epoch(tab, torch)
     epochs_w = max(1, (args.warmup + INTERVAL - 1) // INTERVAL)
     epochs = max(1, (args.steps + INTERVAL - 1) // INTERVAL)
     steps = epochs * INTERVAL
@@ -178,28 +201,22 @@ def bench_speo(args) -> dict:
     evals_per_step = N_ISLANDS * POP
     value = evals_per_step * steps * world / (ms / 1e3)
 
-    # ---- dominant kernel: average launch time of the fused generation kernel ---------------
-    # (a graph of back-to-back launches, so host launch overhead does not enter the average)
-    kl = 100
-    kg = torch.cuda.CUDAGraph()
-    cs = torch.cuda.Stream()
-    cs.wait_stream(torch.cuda.current_stream())
-    with torch.cuda.stream(cs):
-        with torch.cuda.graph(kg, stream=cs):
-            for _ in range(kl):
-                tab.generation()
-    torch.cuda.current_stream().wait_stream(cs)
-    s = torch.cuda.current_stream()
-    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 20
-    flush_l2(flush)
-    k0.record(s)
-    for _ in range(reps):
-        kg.replay()
-    k1.record(s)
-    torch.cuda.synchronize()
-    launch_ms = k0.elapsed_time(k1) / (kl * reps)
-    alg_bytes = evals_per_step * (5 * DIM * 4 + 2 * 4)       # 4 row reads + 1 row write + 2 fitness
+    # ---- dominant kernel: average duration of one launch (graphs of back-to-back launches) ------
+    alg_bytes_gen = evals_per_step * (5 * DIM * 4 + 2 * 4)   # 4 row reads + 1 row write + 2 fitness
+    reps = 40
+    if mode == "resident":
+        kg = capture(torch, lambda: tab.epoch(INTERVAL))
+        launch_ms = time_graph(torch, kg, reps, flush)
+        kernel = f"k_island_epoch<1> ({INTERVAL} generations per launch, islands resident in shared memory)"
+        alg_bytes = alg_bytes_gen * INTERVAL
+    else:
+        kg = capture(torch, lambda: [tab.generation() for _ in range(INTERVAL)])
+        launch_ms = time_graph(torch, kg, reps, flush) / INTERVAL
+        kernel = "k_generation<1> (fused generate+evaluate+select)"
+        alg_bytes = alg_bytes_gen
+    # the per-generation fused kernel on the same islands, for comparison
+    pg = capture(torch, lambda: [tab.generation() for _ in range(INTERVAL)])
+    per_gen_us = time_graph(torch, pg, 10, flush) / INTERVAL * 1e3
     pk = peaks()
     achieved = alg_bytes / (launch_ms / 1e3) / 1e9
     rows, errs = tab.best_f64()
@@ -215,14 +232,19 @@ def bench_speo(args) -> dict:
                    "migrants": MIGRANTS, "step": "one generation over all islands (6400 exact evaluations)",
                    "l2": "flushed (512 MB write) before each timed 50-generation epoch; the population "
                          "(1.5 MB) stays L2-resident within an epoch as in a real run",
-                   "graph": "one CUDA graph per epoch: 50 fused generation launches + 2 migration launches"},
+                   "graph": "one CUDA graph per epoch: the 50 generations (one island-resident launch, or 50 "
+                            "fused launches when an island does not fit shared memory) + 2 migration launches"},
         "gens_per_s": steps * world / (ms / 1e3) / world,
         "best_error_f64_after_run": best_err,
-        "roofline": {"kernel": "k_generation<1,1> (fused generate+evaluate+select)", "bound": "hbm",
+        "roofline": {"kernel": kernel, "bound": "hbm",
                      "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
                      "traffic": None, "peak_src": pk["src"],
-                     "alg_bytes_per_launch": alg_bytes, "launch_us": launch_ms * 1e3},
-        "gpu_launches": epochs * (INTERVAL + 2),
+                     "alg_bytes_per_launch": alg_bytes, "launch_us": launch_ms * 1e3,
+                     "note": "achieved = algorithmic bytes of a streaming generation (5 D s + 2 s per "
+                             "individual-generation) / launch time"},
+        "per_generation_kernel_us": per_gen_us,
+        "epoch_mode": mode,
+        "gpu_launches": epochs * ((1 if mode == "resident" else INTERVAL) + 2),
         "clocks": clk.summary(),
     }
     if not args.no_e2e:

@@ -240,6 +240,18 @@ SPEO_API int speo_generation(const speo_segment *d_segs, const speo_work_item *d
                     float *pop_out, float *fit_out, uint32_t *d_gen, int use_tc,
                     float *trial_out, float *trial_fit_out, void *stream);
 
+/* `generations` fused DE generations of every segment in one launch, each island held in one
+ * block's shared memory for the whole epoch (read from pop_in/fit_in once, written to
+ * pop_out/fit_out once; in place is allowed). Bit-identical to `generations` calls of
+ * speo_generation. Segments need P <= max_pop and D <= dim_hi with max_pop/dim_hi accepted by
+ * speo_epoch_fits (P <= 512, D <= 64, and the island fits one block's shared memory); all
+ * segments in one column class (D <= 32, or 32 < D <= 64). *d_gen advances by `generations`. */
+SPEO_API int speo_epoch_fits(int max_pop, int dim_hi);
+SPEO_API int speo_generation_epoch(const speo_segment *d_segs, int n_segs, int dim_lo, int dim_hi,
+                                   int max_pop, const float *pop_in, const float *fit_in,
+                                   float *pop_out, float *fit_out, uint32_t *d_gen, int generations,
+                                   void *stream);
+
 /* Ring migration: each segment's k best rows (by fitness, then row) replace the k worst
  * rows (by fitness, then row, from the worst) of segment ring_next. All emigrants are
  * chosen before any row is replaced. `staging` holds n_segs*k*(max ld + 1) floats. */

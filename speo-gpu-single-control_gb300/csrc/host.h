@@ -35,3 +35,4 @@ extern "C" unsigned int speo_deverr_de_ops(void);
 extern "C" unsigned int speo_deverr_objective(void);
 extern "C" unsigned int speo_deverr_generation(void);
 extern "C" unsigned int speo_deverr_tc(void);
+extern "C" unsigned int speo_deverr_resident(void);

@@ -97,6 +97,9 @@ SIGNATURES: dict[str, tuple] = {
                                  c_void_p]),
     "speo_generation": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                 c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "speo_epoch_fits": (c_int, [c_int, c_int]),
+    "speo_generation_epoch": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p, c_int, c_void_p]),
     "speo_ring_migrate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "speo_best_reeval_f64": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
 }

@@ -137,6 +137,20 @@ class SegmentTable:
                    "speo_generation")
         self.cur = b
 
+    def epoch_fits(self) -> bool:
+        L = _lib.load()
+        return bool(L.speo_epoch_fits(max(sp.pop_size for sp in self.specs), self.dim_hi))
+
+    def epoch(self, generations: int):
+        """`generations` generations with every island resident in shared memory (in place)."""
+        L = _lib.load()
+        w = self.cur
+        _lib.check(L.speo_generation_epoch(self.d_segs.data_ptr(), len(self.specs), self.dim_lo, self.dim_hi,
+                                           max(sp.pop_size for sp in self.specs), self.pop[w].data_ptr(),
+                                           self.fit[w].data_ptr(), self.pop[w].data_ptr(), self.fit[w].data_ptr(),
+                                           self.gen.data_ptr(), generations, self._stream()),
+                   "speo_generation_epoch")
+
     def migrate(self, k: int):
         L = _lib.load()
         _lib.check(L.speo_ring_migrate(self.d_segs.data_ptr(), len(self.specs), k, self.pop[self.cur].data_ptr(),

@@ -334,3 +334,42 @@ def test_evaluate_tc_matches_oracle(oracle, cuda, layout):
         np.testing.assert_allclose(got[r], ref, rtol=TC_RTOL, atol=1e-4)
     assert got[0] == 0.0
     print(f"max relative error of the BF16x3 tensor-core fitness: {worst:.2e}")
+
+
+# ---------------------------------------------------------------------------------------------
+# island-resident epochs
+# ---------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("layout,gens", [
+    ([(100, 30, 9, 4)] * 8, 7),                         # config-1 islands
+    ([(256, 50, 9, 4)] * 3, 5),                         # config-4 islands
+    ([(40, 20, 31, 2), (64, 17, 9, 7), (5, 3, 31, 5)], 6),  # best-row strategies, tiny islands
+])
+def test_epoch_equals_per_generation_launches(oracle, cuda, layout, gens):
+    import torch
+
+    a = _table(cuda, layout)
+    b = _table(cuda, layout)
+    a.init_population()
+    b.init_population()
+    assert a.epoch_fits()
+    for _ in range(gens):
+        a.generation()
+    b.epoch(gens)
+    torch.cuda.synchronize()
+    assert np.array_equal(a.pop[a.cur].cpu().numpy(), b.pop[b.cur].cpu().numpy())
+    assert np.array_equal(a.fit[a.cur].cpu().numpy(), b.fit[b.cur].cpu().numpy())
+    assert int(b.gen.cpu()[0]) == gens and int(b.gen.cpu()[1]) == 0
+    # and one more epoch against the oracle, generation by generation
+    segs = b.oracle_segments()
+    pop = b.pop[b.cur].cpu().numpy()
+    fit = b.fit[b.cur].cpu().numpy()
+    b.epoch(2)
+    torch.cuda.synchronize()
+    for g in range(2):
+        pop, fit, trials, _, err = oracle.generation(segs, gens + g, pop, fit)
+        assert err == 0
+    got_pop = b.pop[b.cur].cpu().numpy()
+    got_fit = b.fit[b.cur].cpu().numpy()
+    # the oracle evaluates in FP64: selections can only differ where the two fitness values straddle
+    same = np.mean(got_fit == fit.astype(np.float32))
+    assert same > 0.95, same

@@ -21,6 +21,17 @@ import ref_kernels as rk
 pytestmark = pytest.mark.gpu
 
 
+def fma_exact(a, b, c, dtype):
+    """a*b + c rounded once to `dtype` (what the reference's contracted min + u*(max-min) does)."""
+    from fractions import Fraction
+
+    exact = Fraction(float(a)) * Fraction(float(b)) + Fraction(float(c))
+    if dtype == np.float64:
+        return float(exact)
+    # float32: the exact value fits in a double (24 x 8 bit product), so one more rounding is exact
+    return np.float32(float(exact))
+
+
 def np2(D):
     y = 1
     while y < D:
@@ -94,9 +105,7 @@ def test_reference_kernels_match_oracle(oracle, cuda, prec, P, D, nsub, strategi
     for e in range(D):
         l, c = e % 32, e // 32
         u = cap[np.arange(P) * 32 + l, c].astype(npdt)
-        ref = (np.fma(u, ub - lb, lb) if hasattr(np, "fma") else None)
-        if ref is None:
-            ref = np.array([float(np.float64(ui) * float(ub - lb) + float(lb)) for ui in u], dtype=npdt)
+        ref = np.array([fma_exact(ui, ub - lb, lb, npdt) for ui in u], dtype=npdt)
         assert np.array_equal(got_pop[:, e], ref), f"init element {e}"
 
     rng = np.random.default_rng(D)
