@@ -369,7 +369,7 @@ def test_epoch_equals_per_generation_launches(oracle, cuda, layout, gens):
         pop, fit, trials, _, err = oracle.generation(segs, gens + g, pop, fit)
         assert err == 0
     got_pop = b.pop[b.cur].cpu().numpy()
-    got_fit = b.fit[b.cur].cpu().numpy()
-    # the oracle evaluates in FP64: selections can only differ where the two fitness values straddle
-    same = np.mean(got_fit == fit.astype(np.float32))
-    assert same > 0.95, same
+    # The oracle evaluates in FP64 (its fitness values differ from FP32 in the last bits), so
+    # selections can differ only where the two values straddle a parent's fitness: rows agree.
+    same_rows = np.mean(np.all(got_pop == pop, axis=1))
+    assert same_rows > 0.99, same_rows
