@@ -214,8 +214,8 @@ SPEO_API int speo_plan_work(const speo_segment *segs, int n_segs, int tile_rows,
 SPEO_API int speo_init_population(const speo_segment *d_segs, int n_segs, const speo_work_item *d_items,
                          int n_items, float *pop, void *stream);
 
-/* Fitness of every row of every segment (FP32 SIMT evaluation). dim_lo/dim_hi bound the
- * segments' D (they select which kernel variants are launched). */
+/* Fitness of every row of every segment (FP32 SIMT evaluation; work items of any size).
+ * dim_lo/dim_hi bound the segments' D (they select which kernel variants are launched). */
 SPEO_API int speo_evaluate(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,
                   int dim_lo, int dim_hi, const float *pop, float *fit, void *stream);
 

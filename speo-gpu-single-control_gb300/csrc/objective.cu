@@ -42,16 +42,19 @@ __device__ __forceinline__ TileDesc ref_tile(int t, const T *X, int ldx, int P, 
     return d;
 }
 
-__device__ __forceinline__ bool seg_tile(int t, const speo_segment *segs, const speo_work_item *items, const float *pop,
-                                         float *fit, TileDesc &d)
+// Piece `sub` (64 rows) of work item t; work items may be any size.
+__device__ __forceinline__ bool seg_tile(int t, int sub, const speo_segment *segs, const speo_work_item *items,
+                                         const float *pop, float *fit, TileDesc &d)
 {
     const speo_work_item it = items[t];
     const speo_segment &s = segs[it.segment];
-    if (it.count > kEvalTile || it.count < 0 || s.dim < 1 || s.dim > SPEO_MAX_DIM) return false;
-    const long long row = s.row0 + it.first;
+    if (it.count < 1 || it.first < 0 || it.first + it.count > s.pop_size || s.dim < 1 || s.dim > SPEO_MAX_DIM ||
+        s.ld < s.dim)
+        return false;
+    const long long row = s.row0 + it.first + (long long)sub * kEvalTile;
     d.x = pop + row * s.ld;
     d.ldx = s.ld;
-    d.count = it.count;
+    d.count = min(kEvalTile, it.count - sub * kEvalTile);
     d.D = s.dim;
     d.func = s.func_id;
     d.ld_rot = s.ld_rot;
@@ -119,14 +122,17 @@ __global__ void __launch_bounds__(256) k_eval_seg(const speo_segment *segs, cons
     float *Ys = reinterpret_cast<float *>(smem_raw);
     float *Ms = Ys + kEvalTile * 32 * Q;
     for (int t = blockIdx.x; t < n_items; t += gridDim.x) {
-        TileDesc d;
-        if (!seg_tile(t, segs, items, pop, fit, d)) {
-            if (threadIdx.x == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
-            continue;
+        const int pieces = (items[t].count + kEvalTile - 1) / kEvalTile;
+        for (int sub = 0; sub < pieces; ++sub) {
+            TileDesc d;
+            if (!seg_tile(t, sub, segs, items, pop, fit, d)) {
+                if (threadIdx.x == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+                break;
+            }
+            if ((d.D + 31) / 32 > Q) break;  // handled by the launch for its own Q
+            if (Q > 1 && (d.D + 31) / 32 <= Q / 2) break;
+            eval_one_tile<float, Q>(d, Ys, Ms);
         }
-        if ((d.D + 31) / 32 > Q) continue;  // handled by the launch for its own Q
-        if (Q > 1 && (d.D + 31) / 32 <= Q / 2) continue;
-        eval_one_tile<float, Q>(d, Ys, Ms);
     }
 }
 

@@ -39,3 +39,23 @@ def cuda():
     if not torch.cuda.is_available():
         pytest.fail("GPU test run without a CUDA device")
     return torch.device("cuda:0")
+
+
+@pytest.fixture(autouse=True)
+def _device_error_flags_clean(request):
+    """After every GPU test: the library's device error flags must be clear (read and reset)."""
+    yield
+    if request.node.get_closest_marker("gpu") is None:
+        return
+    import ctypes
+
+    import torch
+
+    if not torch.cuda.is_available():
+        return
+    from speo_gb300 import _lib
+
+    bits = ctypes.c_uint32(0)
+    st = _lib.load().speo_device_error_bits(ctypes.byref(bits))
+    assert st == 0, f"speo_device_error_bits failed: {st}"
+    assert bits.value == 0, f"device error flags 0x{bits.value:x} set by {request.node.nodeid}"
