@@ -258,6 +258,21 @@ SPEO_API int speo_generation_epoch(const speo_segment *d_segs, int n_segs, int d
 SPEO_API int speo_ring_migrate(const speo_segment *d_segs, int n_segs, int k, float *pop, float *fit,
                       float *staging, int max_ld, void *stream);
 
+/* speo_ring_migrate without a caller staging buffer, for callers that cannot allocate device
+ * memory themselves (for instance a plugin whose host process owns and pre-reserves all device
+ * memory through its own allocator, or a loop that must not allocate once it has started).
+ * No counterpart in the reference (its migration is host MPI, src/migrate.cc:46-136).
+ * The staging lives in a fixed array of SPEO_NOALLOC_STAGING_FLOATS floats (4 MiB) inside the
+ * library, held by every GPU that loads the library until the process exits;
+ * n_segs * k * (max_ld + 1) beyond that is rejected with SPEO_ERR_INVALID_ARG. The function
+ * allocates nothing: the first call on a device (with that device current) looks up the array's
+ * device address once, so make that first call before any stream capture. Every call shares
+ * the one array, each call writes every staging slot it reads (nothing needs clearing), and
+ * calls that overlap on the GPU (other streams, other threads) race on it. */
+#define SPEO_NOALLOC_STAGING_FLOATS (1 << 20)
+SPEO_API int speo_ring_migrate_noalloc(const speo_segment *d_segs, int n_segs, int k, float *pop,
+                                       float *fit, int max_ld, void *stream);
+
 /* Per segment: argmin of fit (ties: lowest row) -> best_row[s]; FP64 re-evaluation of that
  * row -> best_err[s] = f(x) - f* in double. */
 SPEO_API int speo_best_reeval_f64(const speo_segment *d_segs, int n_segs, const float *pop,

@@ -13,6 +13,8 @@
 //
 // Migration replaces src/migrate.cc:46-136 (host MPI exchange of random individuals) with the
 // ring of best-k -> neighbour's worst-k on the device.
+#include <mutex>
+
 #include "eval_simt.cuh"
 #include "host.h"
 
@@ -500,4 +502,49 @@ extern "C" int speo_init_population(const speo_segment *segs, int n_segs, const 
     const int grid = n_items < 4 * sm_count() ? n_items : 4 * sm_count();
     k_init_segments<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(segs, items, n_items, pop);
     return check_launch("k_init_segments");
+}
+
+// ---- ring migration without caller-provided scratch -----------------------------------------
+// Staging for callers that cannot allocate device memory: a fixed array in the library's own
+// device image. Every GPU that loads the library holds it until the process exits.
+namespace {
+static __device__ __align__(256) float g_migration_staging[SPEO_NOALLOC_STAGING_FLOATS];
+std::mutex g_staging_mu;
+float *g_staging_addr[64] = {};  // device address of g_migration_staging, per device
+}  // namespace
+
+extern "C" int speo_ring_migrate_noalloc(const speo_segment *segs, int n_segs, int k, float *pop, float *fit,
+                                         int max_ld, void *stream)
+{
+    if (!segs || !pop || !fit || n_segs < 1 || max_ld < 1)
+        return fail(SPEO_ERR_INVALID_ARG, "speo_ring_migrate_noalloc: bad arguments");
+    if (k < 1 || k > kMaxMigrants)
+        return fail(SPEO_ERR_INVALID_ARG, "speo_ring_migrate_noalloc: k = %d outside [1, %d]", k, kMaxMigrants);
+    const unsigned long long need = (unsigned long long)n_segs * (unsigned long long)k * (unsigned long long)(max_ld + 1);
+    if (need > SPEO_NOALLOC_STAGING_FLOATS)
+        return fail(SPEO_ERR_INVALID_ARG,
+                    "speo_ring_migrate_noalloc: %d segments x %d migrants x (max_ld %d + 1) = %llu staging floats "
+                    "exceed the fixed %d; use speo_ring_migrate with a caller buffer",
+                    n_segs, k, max_ld, need, SPEO_NOALLOC_STAGING_FLOATS);
+    int dev = 0;
+    if (int e = check_cuda(cudaGetDevice(&dev), "speo_ring_migrate_noalloc: cudaGetDevice")) return e;
+    if (dev < 0 || dev >= 64) return fail(SPEO_ERR_INVALID_ARG, "speo_ring_migrate_noalloc: device %d", dev);
+    float *staging = nullptr;
+    {
+        // first call on this device (with it current): look up the array's device address once
+        std::lock_guard<std::mutex> lock(g_staging_mu);
+        if (!g_staging_addr[dev]) {
+            void *addr = nullptr;
+            if (int e = check_cuda(cudaGetSymbolAddress(&addr, g_migration_staging),
+                                   "speo_ring_migrate_noalloc: cudaGetSymbolAddress"))
+                return e;
+            g_staging_addr[dev] = static_cast<float *>(addr);
+        }
+        staging = g_staging_addr[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    k_emigrate<<<n_segs, 256, 0, st>>>(segs, k, pop, fit, staging, max_ld);
+    if (int e = check_launch("k_emigrate")) return e;
+    k_immigrate<<<n_segs, 256, 0, st>>>(segs, n_segs, k, pop, fit, staging, max_ld);
+    return check_launch("k_immigrate");
 }

@@ -24,6 +24,7 @@ MAX_DIM = 256
 RNG_STATE_BYTES = 64
 TILE_SIMT = 64
 TILE_TC = 128
+NOALLOC_STAGING_FLOATS = 1 << 20
 
 
 class Segment(ctypes.Structure):
@@ -101,6 +102,7 @@ SIGNATURES: dict[str, tuple] = {
     "speo_generation_epoch": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_int, c_void_p]),
     "speo_ring_migrate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "speo_ring_migrate_noalloc": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p]),
     "speo_best_reeval_f64": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
