@@ -247,10 +247,92 @@ def bench_speo(args) -> dict:
         "gpu_launches": epochs * ((1 if mode == "resident" else INTERVAL) + 2),
         "clocks": clk.summary(),
     }
+    if not args.no_ops:
+        out["operators_bandwidth_scale"] = bench_operators(L, dev, torch, pk)
     if not args.no_e2e:
         out["e2e"] = bench_e2e(L, dev, torch, args)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(sample_s=args.cpu_sample_s)
+    return out
+
+
+def bench_operators(L, dev, torch, pk) -> dict:
+    """Operator kernels on a bandwidth-scale population (measurement-only variant): 16384 islands
+    x P = 128, D = 100 = 2^21 rows, 0.84 GB per FP32 buffer (> 6x L2), so every launch streams
+    from HBM. Each kernel is timed alone with CUDA events (median of several launches, L2
+    flushed before each); achieved = algorithmic bytes / time."""
+    from speo_gb300 import _lib
+    from speo_gb300.device import SegmentSpec, SegmentTable
+    from speo_gb300.instances import make_instance
+
+    n_isl, P, D = 16384, 128, 100
+    inst = [make_instance(run_seed() + 1, D)]
+    specs = [SegmentSpec(pop_size=P, dim=D, func_id=FUNC, instance=0, seed=77 + i) for i in range(n_isl)]
+    tab = SegmentTable(specs, inst, tile_rows=_lib.TILE_SIMT, device=dev)
+    tab_tc = SegmentTable(specs, inst, tile_rows=_lib.TILE_TC, device=dev)
+    tab.init_population()
+    rows = tab.rows
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
+    s = 4
+
+    def timed(fn, reps=7):
+        fn()
+        ts = []
+        for _ in range(reps):
+            flush_l2(flush)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts)) / 1e3
+
+    out = {"workload": f"{n_isl} islands x P={P}, D={D} ({rows} rows, {rows * D * s / 1e9:.2f} GB per buffer)",
+           "peak_gbs": pk["hbm_gbs"], "kernels": {}}
+
+    def rec(name, sec, bytes_):
+        gbs = bytes_ / sec / 1e9
+        out["kernels"][name] = {"us": sec * 1e6, "alg_bytes": bytes_, "achieved_gbs": gbs,
+                                "frac": gbs / pk["hbm_gbs"]}
+
+    # fused generation (CUDA-core rotation), segment layout ld = 100
+    rec("k_generation<4> fused generate+evaluate+select", timed(lambda: tab.generation()), rows * (5 * D * s + 2 * s))
+    # tcgen05 evaluation: read D floats, write 1
+    tab_tc.pop[0].copy_(tab.pop[tab.cur])
+    out_fit = torch.empty(rows, device=dev)
+    rec("k_evaluate_tc (TMA + tcgen05 BF16x3)", timed(lambda: tab_tc.evaluate(which=0, use_tc=True, out=out_fit)),
+        rows * (D * s + s))
+    rec("k_eval_seg<4> (CUDA-core evaluation)", timed(lambda: tab.evaluate(which=tab.cur, out=out_fit)),
+        rows * (D * s + s))
+    # drop-in operators in the reference layout (ld = np2 = 128), FP32
+    ld = 128
+    pop = torch.zeros(rows, ld, device=dev)
+    pop[:, :D] = tab.pop[tab.cur][:, :D]
+    cand = torch.zeros(rows, ld, device=dev)
+    pfit = tab.fit[tab.cur].clone()
+    cfit = torch.empty(rows, device=dev)
+    rng_state = torch.zeros(16, dtype=torch.int32, device=dev)
+    perm = torch.arange(rows, dtype=torch.int32, device=dev)
+    best = torch.zeros(n_isl, dtype=torch.int32, device=dev)
+    info = (_lib.DEInfoF32 * n_isl)(*[_lib.DEInfoF32(0.9, 0.5, 4, P) for _ in range(n_isl)])
+    d_info = torch.frombuffer(bytearray(bytes(info)), dtype=torch.uint8).to(dev)
+    ii = _lib.IslandInfo(rows, n_isl, perm.data_ptr())
+    pi = _lib.ProblemInfoF32(D, FUNC, 1, 0, 5, 0, 0, 100.0, -100.0)
+    Pp = _lib.PopulationF32(pop.data_ptr(), pfit.data_ptr())
+    Cp = _lib.PopulationF32(cand.data_ptr(), cfit.data_ptr())
+    L.speo_set_stream(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(L.API_Initilize_f32(Cp, rng_state.data_ptr(), ii, pi), "API_Initilize_f32")
+    rec("API_DE_GenerateNewPopulation_f32 (best search + generate)",
+        timed(lambda: L.API_DE_GenerateNewPopulation_f32(Cp, Pp, best.data_ptr(), ii, d_info.data_ptr(),
+                                                         rng_state.data_ptr(), pi)),
+        rows * (4 * D * s + D * s) + rows * s)
+    rec("API_DE_SelectSurvival_f32", timed(lambda: L.API_DE_SelectSurvival_f32(Pp, Cp, ii, pi)),
+        rows * (2 * D * s + 3 * s))
+    L.speo_set_stream(None)
+    _lib.check(L.API_CheckCUDAError(), "operators")
+    del tab, tab_tc, pop, cand
+    torch.cuda.empty_cache()
     return out
 
 
@@ -378,8 +460,17 @@ def main() -> None:
     ap.add_argument("--cpu-sample-s", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI leg (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
+    ap.add_argument("--no-ops", action="store_true", help="skip the bandwidth-scale operator measurements")
+    ap.add_argument("--ops-only", action="store_true", help="only the bandwidth-scale operator measurements")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.ops_only:
+        import torch
+        from speo_gb300 import _lib
+
+        torch.cuda.set_device(0)
+        print(json.dumps(bench_operators(_lib.load(), "cuda:0", torch, peaks())))
+        return
     out = bench_reference(args) if args.impl == "reference" else bench_speo(args)
     if out is not None and int(os.environ.get("RANK", "0")) == 0:
         print(json.dumps(out))
