@@ -25,7 +25,8 @@ namespace speo {
 namespace {
 
 constexpr int kTileM = 128;
-constexpr int kTmemCols = 128;
+constexpr int kTmemCols = 128;   // one accumulator (N <= 128)
+constexpr int kTmemAlloc = 256;  // two accumulators: MMA of tile i+1 overlaps the epilogue of tile i
 constexpr long long kWaitBudget = 2000000000LL;  // ~1 s at 2 GHz: any wait longer is a failure
 
 __host__ __device__ __forceinline__ int round16(int x) { return (x + 15) & ~15; }
@@ -53,7 +54,7 @@ __host__ __device__ inline TcLayout tc_layout(int dim_hi, int ld, int nstage)
     L.off_b = L.off_a + 2 * L.a_bytes;
     L.off_o = L.off_b + 2 * L.b_bytes;
     L.off_bar = (L.off_o + (size_t)L.kmax * 4 + 15) & ~(size_t)15;
-    L.total = L.off_bar + 64;
+    L.total = L.off_bar + 128;
     return L;
 }
 
@@ -68,12 +69,14 @@ struct EvalTcArgs {
     float *fit;
 };
 
-// Builds B = split(M) for an instance: B[n][k] = M[n][k] = rot[k*ld_rot + n] (zero past D).
-__device__ __forceinline__ void build_b(const speo_segment &s, int Kp, uint8_t *b_hi, uint8_t *b_lo, float *so)
+// Builds B = split(M) for an instance with `nthr` threads (index t): B[n][k] = M[n][k] =
+// rot[k*ld_rot + n] (zero past D), and the shift o.
+__device__ __forceinline__ void build_b(const speo_segment &s, int Kp, uint8_t *b_hi, uint8_t *b_lo, float *so, int t,
+                                        int nthr)
 {
     const int D = s.dim;
     const int pairs = Kp * (Kp / 8);
-    for (int i = threadIdx.x; i < pairs; i += blockDim.x) {
+    for (int i = t; i < pairs; i += nthr) {
         const int n = i % Kp, kc = i / Kp;
         float v[8];
 #pragma unroll
@@ -87,15 +90,16 @@ __device__ __forceinline__ void build_b(const speo_segment &s, int Kp, uint8_t *
         *reinterpret_cast<uint4 *>(b_hi + off) = h;
         *reinterpret_cast<uint4 *>(b_lo + off) = l;
     }
-    for (int k = threadIdx.x; k < Kp; k += blockDim.x) so[k] = k < D ? s.shift[k] : 0.f;
+    for (int k = t; k < Kp; k += nthr) so[k] = k < D ? s.shift[k] : 0.f;
 }
 
-// Staged FP32 rows -> y = x - o -> BF16 hi/lo K-major A operand. Rows >= count become zero.
+// Staged FP32 rows -> y = x - o -> BF16 hi/lo K-major A operand, `nthr` threads. Rows >= count
+// become zero.
 __device__ __forceinline__ void build_a(const float *stage, int box_x, int count, int D, int Kp, const float *so,
-                                        uint8_t *a_hi, uint8_t *a_lo)
+                                        uint8_t *a_hi, uint8_t *a_lo, int t, int nthr)
 {
     const int pairs = kTileM * (Kp / 8);
-    for (int i = threadIdx.x; i < pairs; i += blockDim.x) {
+    for (int i = t; i < pairs; i += nthr) {
         const int m = i % kTileM, kc = i / kTileM;
         float v[8];
         const float *src = stage + (size_t)m * box_x + 8 * kc;
@@ -151,6 +155,11 @@ __device__ __forceinline__ bool tc_tile_ok(const speo_work_item &it, const speo_
            s.row0 + it.first + it.count <= a.n_rows;
 }
 
+// Warp roles: warps 4..7 stage-convert tile i (thread 128 also issues TMA loads and the MMAs);
+// warps 0..3 run the epilogue of tile i-1 from the other TMEM accumulator meanwhile.
+//   bar_tma[s]  stage s holds the rows of its tile         (TMA transaction bytes)
+//   bar_mma[b]  accumulator b holds a finished product     (tcgen05.commit)
+//   bar_epi[b]  the epilogue is done reading accumulator b (128 arrivals)
 __global__ void __launch_bounds__(256, 1) k_evaluate_tc(const __grid_constant__ CUtensorMap xmap, EvalTcArgs a)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -159,19 +168,25 @@ __global__ void __launch_bounds__(256, 1) k_evaluate_tc(const __grid_constant__ 
     uint8_t *a_hi = smem + L.off_a, *a_lo = a_hi + L.a_bytes;
     uint8_t *b_hi = smem + L.off_b, *b_lo = b_hi + L.b_bytes;
     float *so = reinterpret_cast<float *>(smem + L.off_o);
-    uint64_t *bar_tma = reinterpret_cast<uint64_t *>(smem + L.off_bar);  // [2]
-    uint64_t *bar_mma = bar_tma + 2;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_mma + 1);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
+    uint64_t *bar_tma = bars, *bar_mma = bars + 2, *bar_epi = bars + 4;
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 6);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 7);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ns = a.nstage;
 
     if (warp == 0) {
-        tc::tmem_alloc(tmem_slot, kTmemCols);
+        tc::tmem_alloc(tmem_slot, kTmemAlloc);
         tc::tmem_relinquish();
     }
     if (tid == 32) {
         tc::mbar_init(&bar_tma[0], 1);
         tc::mbar_init(&bar_tma[1], 1);
-        tc::mbar_init(bar_mma, 1);
+        tc::mbar_init(&bar_mma[0], 1);
+        tc::mbar_init(&bar_mma[1], 1);
+        tc::mbar_init(&bar_epi[0], 128);
+        tc::mbar_init(&bar_epi[1], 128);
+        *abort_flag = 0;
         tc::fence_mbar_init();
         tc::prefetch_tensormap(&xmap);
     }
@@ -180,85 +195,96 @@ __global__ void __launch_bounds__(256, 1) k_evaluate_tc(const __grid_constant__ 
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
 
-    // this block's items: blockIdx.x + i * gridDim.x, i < my_items
     const int my_items = a.n_items > (int)blockIdx.x ? (a.n_items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     auto item_of = [&](int i) { return a.items[blockIdx.x + i * gridDim.x]; };
-    auto issue = [&](int i) {  // thread 0: stage the rows of item i
+    int tma_issued = 0, mma_issued = 0;   // issuer bookkeeping (thread 128)
+    auto issue_tma = [&](int i) {
         if (i >= my_items) return;
         const speo_work_item it = item_of(i);
         const speo_segment &sg = a.segs[it.segment];
-        const int sidx = i % a.nstage;
+        const int sidx = i % ns;
         tc::mbar_arrive_expect_tx(&bar_tma[sidx], (uint32_t)L.stage_bytes);
         const long long y = tc_tile_ok(it, sg, a) ? sg.row0 + it.first : 0;
         tc::tma_load_2d(stage[sidx], &xmap, 0, (int)y, &bar_tma[sidx]);
+        tma_issued = i + 1;
     };
-    if (tid == 0)
-        for (int i = 0; i < a.nstage; ++i) issue(i);
 
-    const float *c_rot = nullptr, *c_shift = nullptr;
-    int c_dim = -1, c_ldrot = -1;
-    uint32_t mma_batches = 0;
-    int i = 0;
-    bool failed = false;
-    for (; i < my_items; ++i) {
-        const speo_work_item it = item_of(i);
-        const speo_segment &s = a.segs[it.segment];
-        const bool ok = tc_tile_ok(it, s, a);
-        const int sidx = i % a.nstage;
-        const bool t_out = !tc::mbar_wait(&bar_tma[sidx], (uint32_t)((i / a.nstage) & 1), kWaitBudget);
-        if (__syncthreads_or(t_out)) { failed = true; break; }
-        const int D = s.dim, Kp = round16(D);
-        if (ok) {
-            if (s.rot != c_rot || s.shift != c_shift || D != c_dim || s.ld_rot != c_ldrot) {
-                build_b(s, Kp, b_hi, b_lo, so);  // no MMA is in flight: the previous epilogue waited
-                c_rot = s.rot; c_shift = s.shift; c_dim = D; c_ldrot = s.ld_rot;
-                __syncthreads();
-            }
-            build_a(stage[sidx], L.box_x, it.count, D, Kp, so, a_hi, a_lo);
-        }
-        tc::fence_proxy_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            issue(i + a.nstage);  // the stage just consumed takes the item after next
+    if (warp >= 4) {
+        // ---- conversion group ---------------------------------------------------------------------
+        const int ct = tid - 128;
+        const bool issuer = ct == 0;
+        if (issuer)
+            for (int i = 0; i < ns; ++i) issue_tma(i);
+        const float *c_rot = nullptr, *c_shift = nullptr;
+        int c_dim = -1, c_ldrot = -1;
+        for (int i = 0; i < my_items; ++i) {
+            const speo_work_item it = item_of(i);
+            const speo_segment &s = a.segs[it.segment];
+            const bool ok = tc_tile_ok(it, s, a);
+            const int D = ok ? s.dim : 16, Kp = round16(D);
+            bool to = !tc::mbar_wait(&bar_tma[i % ns], (uint32_t)((i / ns) & 1), kWaitBudget);
+            if (i >= 1) to |= !tc::mbar_wait(&bar_mma[(i - 1) & 1], (uint32_t)(((i - 1) >> 1) & 1), kWaitBudget);
+            if (tc::named_bar_or(1, 128, to || *abort_flag != 0)) { *abort_flag = 1; break; }
             if (ok) {
-                tc::fence_after_sync();
-                issue_split_mma(tmem, a_hi, a_lo, b_hi, b_lo, Kp, Kp);
-                tc::mma_commit(bar_mma);
+                if (s.rot != c_rot || s.shift != c_shift || D != c_dim || s.ld_rot != c_ldrot) {
+                    build_b(s, Kp, b_hi, b_lo, so, ct, 128);
+                    c_rot = s.rot; c_shift = s.shift; c_dim = D; c_ldrot = s.ld_rot;
+                    tc::named_bar_sync(1, 128);
+                }
+                build_a(stage[i % ns], L.box_x, it.count, D, Kp, so, a_hi, a_lo, ct, 128);
+            } else if (ct == 0) {
+                atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+            }
+            tc::fence_proxy_async_smem();
+            tc::named_bar_sync(1, 128);
+            if (issuer) {
+                issue_tma(i + ns);  // the stage just converted takes the tile after next
+                bool free_acc = true;
+                if (i >= 2) free_acc = tc::mbar_wait(&bar_epi[i & 1], (uint32_t)(((i - 2) >> 1) & 1), kWaitBudget);
+                if (!free_acc) {
+                    *abort_flag = 1;
+                } else {
+                    tc::fence_after_sync();
+                    issue_split_mma(tmem + (uint32_t)((i & 1) * kTmemCols), a_hi, a_lo, b_hi, b_lo, Kp, Kp);
+                    tc::mma_commit(&bar_mma[i & 1]);
+                    mma_issued = i + 1;
+                }
             }
         }
-        if (!ok) {
-            if (tid == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
-            continue;
-        }
-        bool m_out = false;
-        if (warp < 4) {
-            m_out = !tc::mbar_wait(bar_mma, mma_batches & 1u, kWaitBudget);
+    } else {
+        // ---- epilogue group: one TMEM lane (= tile row) per thread ----------------------------------
+        for (int i = 0; i < my_items; ++i) {
+            if (__any_sync(0xffffffffu, *abort_flag != 0)) break;
+            const speo_work_item it = item_of(i);
+            const speo_segment &s = a.segs[it.segment];
+            const bool ok = tc_tile_ok(it, s, a);
+            const int D = ok ? s.dim : 16, Kp = round16(D);
+            // warp-uniform decision: tcgen05.ld below is warp-collective
+            const bool got = tc::mbar_wait(&bar_mma[i & 1], (uint32_t)((i >> 1) & 1), kWaitBudget);
+            if (!__all_sync(0xffffffffu, got)) { *abort_flag = 1; break; }
             tc::fence_after_sync();
-            if (!m_out) {
-                const float f = epilogue_row(tmem, warp, D, Kp, s.func_id, func_scale(s.func_id));
-                const int m = warp * 32 + lane;
-                if (m < it.count) a.fit[s.row0 + it.first + m] = f;
-            }
+            const float f = epilogue_row(tmem + (uint32_t)((i & 1) * kTmemCols), warp, D, Kp, s.func_id,
+                                         func_scale(s.func_id));
+            const int m = warp * 32 + lane;
+            if (ok && m < it.count) a.fit[s.row0 + it.first + m] = f;
+            tc::fence_before_sync();
+            tc::mbar_arrive(&bar_epi[i & 1]);
         }
-        ++mma_batches;
-        tc::fence_before_sync();
-        if (__syncthreads_or(m_out)) { failed = true; break; }
     }
-    if (failed) {
+    __syncthreads();
+    if (*abort_flag && tid == 128) {
         // Let the copies and products this block started finish (bounded) before its shared and
-        // tensor memory go away.
-        if (tid == 0) {
-            atomicOr(&s_deverr, SPEO_DEVERR_WAIT_TIMEOUT);
-            for (int j = i; j < my_items && j <= i + a.nstage; ++j)
-                tc::mbar_wait(&bar_tma[j % a.nstage], (uint32_t)((j / a.nstage) & 1), kWaitBudget);
-            tc::mbar_wait(bar_mma, mma_batches & 1u, kWaitBudget);
-        }
-        __syncthreads();
+        // tensor memory are released.
+        atomicOr(&s_deverr, SPEO_DEVERR_WAIT_TIMEOUT);
+        for (int j = (tma_issued > ns ? tma_issued - ns : 0); j < tma_issued; ++j)
+            tc::mbar_wait(&bar_tma[j % ns], (uint32_t)((j / ns) & 1), kWaitBudget);
+        for (int j = (mma_issued > 2 ? mma_issued - 2 : 0); j < mma_issued; ++j)
+            tc::mbar_wait(&bar_mma[j & 1], (uint32_t)((j >> 1) & 1), kWaitBudget);
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+    if (warp == 0) tc::tmem_dealloc(tmem, kTmemAlloc);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
