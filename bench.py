@@ -256,7 +256,7 @@ def bench_speo(args) -> dict:
     return out
 
 
-def bench_operators(L, dev, torch, pk) -> dict:
+def bench_operators(L, dev, torch, pk, n_isl: int = 16384) -> dict:
     """Operator kernels on a bandwidth-scale population (measurement-only variant): 16384 islands
     x P = 128, D = 100 = 2^21 rows, 0.84 GB per FP32 buffer (> 6x L2), so every launch streams
     from HBM. Each kernel is timed alone with CUDA events (median of several launches, L2
@@ -265,7 +265,7 @@ def bench_operators(L, dev, torch, pk) -> dict:
     from speo_gb300.device import SegmentSpec, SegmentTable
     from speo_gb300.instances import make_instance
 
-    n_isl, P, D = 16384, 128, 100
+    P, D = 128, 100
     inst = [make_instance(run_seed() + 1, D)]
     specs = [SegmentSpec(pop_size=P, dim=D, func_id=FUNC, instance=0, seed=77 + i) for i in range(n_isl)]
     tab = SegmentTable(specs, inst, tile_rows=_lib.TILE_SIMT, device=dev)
@@ -462,6 +462,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     ap.add_argument("--no-ops", action="store_true", help="skip the bandwidth-scale operator measurements")
     ap.add_argument("--ops-only", action="store_true", help="only the bandwidth-scale operator measurements")
+    ap.add_argument("--ops-islands", type=int, default=16384, help="islands of 128 rows in the operator variant")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.ops_only:
@@ -469,7 +470,7 @@ def main() -> None:
         from speo_gb300 import _lib
 
         torch.cuda.set_device(0)
-        print(json.dumps(bench_operators(_lib.load(), "cuda:0", torch, peaks())))
+        print(json.dumps(bench_operators(_lib.load(), "cuda:0", torch, peaks(), args.ops_islands)))
         return
     out = bench_reference(args) if args.impl == "reference" else bench_speo(args)
     if out is not None and int(os.environ.get("RANK", "0")) == 0:
