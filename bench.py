@@ -327,8 +327,22 @@ def bench_operators(L, dev, torch, pk, n_isl: int = 16384) -> dict:
         timed(lambda: L.API_DE_GenerateNewPopulation_f32(Cp, Pp, best.data_ptr(), ii, d_info.data_ptr(),
                                                          rng_state.data_ptr(), pi)),
         rows * (4 * D * s + D * s) + rows * s)
-    rec("API_DE_SelectSurvival_f32", timed(lambda: L.API_DE_SelectSurvival_f32(Pp, Cp, ii, pi)),
-        rows * (2 * D * s + 3 * s))
+    # selection moves a row only where the trial wins: bytes = both fitness values for every row
+    # + (read trial row + write it + write fitness) for each winner, counted from this state
+    L.API_evaluateFitness_f32(cfit.data_ptr(), None, None, cand.data_ptr(), tab.inst_shift[0].data_ptr(),
+                              tab.inst_rot[0].data_ptr(), None, None, None, None, rows, D, 0.0, FUNC)
+    torch.cuda.synchronize()
+    pfit0 = pfit.clone()
+    winners = int((cfit < pfit0).sum().item())
+
+    def select_once():
+        pfit.copy_(pfit0)
+        L.API_DE_SelectSurvival_f32(Pp, Cp, ii, pi)
+
+    t_copy = timed(lambda: pfit.copy_(pfit0))
+    rec("API_DE_SelectSurvival_f32", max(timed(select_once) - t_copy, 1e-9),
+        rows * 2 * s + winners * (2 * D * s + s))
+    out["kernels"]["API_DE_SelectSurvival_f32"]["winners"] = winners
     L.speo_set_stream(None)
     _lib.check(L.API_CheckCUDAError(), "operators")
     del tab, tab_tc, pop, cand

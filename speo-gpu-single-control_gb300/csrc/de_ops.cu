@@ -93,49 +93,113 @@ __global__ void k_best(const T *fit, const int *perm, int S, int nsub, int *best
     if (lane == 0) best_id[s] = perm[s * S + bp];
 }
 
-// global_DE_GenerateNewPopulation (kernel_DE_CUDA.cu:172-289): one warp per position.
+// global_DE_GenerateNewPopulation (kernel_DE_CUDA.cu:172-289). A block takes 64 positions:
+// (1) one thread per position draws the donors and jrand (the reference recomputes them on all
+// 32 lanes), (2) G lanes per row build the trial from 16-byte vector loads of the target and
+// donor rows with one Philox block per 4 elements, and store it with vector stores.
+constexpr int kGenRows = 64;
+
+template <typename T> struct Vec;
+template <> struct Vec<float> { using type = float4; static constexpr int n = 4; };
+template <> struct Vec<double> { using type = double2; static constexpr int n = 2; };
+
 template <typename T>
+__device__ __forceinline__ T vget(const typename Vec<T>::type &v, int q)
+{
+    if constexpr (Vec<T>::n == 4) return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w;
+    else return q == 0 ? v.x : v.y;
+}
+template <typename T>
+__device__ __forceinline__ void vset(typename Vec<T>::type &v, int q, T x)
+{
+    if constexpr (Vec<T>::n == 4) { if (q == 0) v.x = x; else if (q == 1) v.y = x; else if (q == 2) v.z = x; else v.w = x; }
+    else { if (q == 0) v.x = x; else v.y = x; }
+}
+
+__device__ __forceinline__ int ndonors(int st)
+{
+    switch (st) {
+    case 0: case 2: case 6: return 2;
+    case 3: case 4: case 8: return 3;
+    case 1: case 7: return 4;
+    default: return 5;
+    }
+}
+
+template <typename T, int G>
 __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld, int dim, int island_size, int S,
                                                   const int *perm, const typename DeInfoT<T>::type *info,
                                                   const int *best_id, T lb, T ub, RngState *rng)
 {
+    using V = typename Vec<T>::type;
+    constexpr int VN = Vec<T>::n;
+    __shared__ int sR[kGenRows][8];  // donor rows (through perm), jrand, target row, sub-island
     const uint32_t gen = *(volatile uint32_t *)&rng->gen;
     const uint2 key = make_uint2(rng->key0, rng->key1);
-    const int pos = blockIdx.x * kWarps + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (pos < island_size) {
-        const int sel = perm[pos];
+    const int tid = threadIdx.x;
+    const int pos0 = blockIdx.x * kGenRows;
+    bool ok_bound = true;
+    if (tid < kGenRows && pos0 + tid < island_size) {
+        const int pos = pos0 + tid;
         const int isl = pos / S;
         IdxStream s(key, (uint32_t)pos, gen, kTagIdx);
         int r[5];
-        const bool ok_draw = draw_donors(s, S, r);
-        bool ok_bound = true;
+        if (!draw_donors(s, S, r)) atomicOr(&s_deverr, SPEO_DEVERR_REDRAW_LIMIT);
 #pragma unroll
-        for (int i = 0; i < 5; ++i) r[i] = perm[r[i] + isl * S];
-        const int jrand = s.index(dim);
+        for (int i = 0; i < 5; ++i) sR[tid][i] = perm[r[i] + isl * S];
+        sR[tid][5] = s.index(dim);
+        sR[tid][6] = perm[pos];
+        sR[tid][7] = isl;
+    }
+    __syncthreads();
+    const int grp = tid / G, gl = tid % G;
+    const int nch = (dim + VN - 1) / VN;
+    for (int lr = grp; lr < kGenRows; lr += 256 / G) {
+        const int pos = pos0 + lr;
+        if (pos >= island_size) break;
+        const int sel = sR[lr][6], isl = sR[lr][7], jrand = sR[lr][5];
         const T F = info[isl].F, CR = info[isl].CR;
         const int st = info[isl].strategy_ID;
+        const int nd = ndonors(st);
         const int b = strategy_uses_best(st) ? best_id[isl] : sel;
         const T *xi = pop + (size_t)sel * ld;
         const T *xb = pop + (size_t)b * ld;
-        for (int e = lane; e < dim; e += 32) {
-            const uint4 w = philox(make_uint4((uint32_t)(e >> 2), (uint32_t)pos, gen, kTagCr), key);
-            const float u = u01(pick(w, (uint32_t)(e & 3)));
-            T v;
-            if (e == jrand || (T)u < CR) {
-                T xr[5];
+        T *out = cand + (size_t)sel * ld;
+        for (int c = gl; c < nch; c += G) {
+            const int e0 = VN * c;
+            const V ti = *reinterpret_cast<const V *>(xi + e0);
+            const V tb = strategy_uses_best(st) ? *reinterpret_cast<const V *>(xb + e0) : ti;
+            V tr[5];
 #pragma unroll
-                for (int i = 0; i < 5; ++i) xr[i] = pop[(size_t)r[i] * ld + e];
-                v = mutant<T>(st, F, xi[e], xb[e], xr);
-            } else {
-                v = xi[e];
+            for (int k = 0; k < 5; ++k)
+                tr[k] = k < nd ? *reinterpret_cast<const V *>(pop + (size_t)sR[lr][k] * ld + e0) : ti;
+            const uint4 w = philox(make_uint4((uint32_t)(e0 >> 2), (uint32_t)pos, gen, kTagCr), key);
+            V o = ti;
+#pragma unroll
+            for (int q = 0; q < VN; ++q) {
+                const int e = e0 + q;
+                const float u = u01(pick(w, (uint32_t)(e & 3)));
+                T v;
+                if (e == jrand || (T)u < CR) {
+                    T xr[5];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) xr[k] = vget<T>(tr[k], q);
+                    v = mutant<T>(st, F, vget<T>(ti, q), vget<T>(tb, q), xr);
+                } else {
+                    v = vget<T>(ti, q);
+                }
+                vset<T>(o, q, check_bound<T>(v, lb, ub, ok_bound));
             }
-            v = check_bound<T>(v, lb, ub, ok_bound);
-            cand[(size_t)sel * ld + e] = v;
+            if (e0 + VN <= dim) {
+                *reinterpret_cast<V *>(out + e0) = o;
+            } else {  // ragged last chunk: elements past D are never written (as in the reference)
+#pragma unroll
+                for (int q = 0; q < VN; ++q)
+                    if (e0 + q < dim) out[e0 + q] = vget<T>(o, q);
+            }
         }
-        if (!ok_draw && lane == 0) atomicOr(&s_deverr, SPEO_DEVERR_REDRAW_LIMIT);
-        if (!ok_bound) atomicOr(&s_deverr, SPEO_DEVERR_BOUND_LIMIT);
     }
+    if (!ok_bound) atomicOr(&s_deverr, SPEO_DEVERR_BOUND_LIMIT);
     finish_launch(rng, gen);
 }
 
@@ -193,10 +257,23 @@ int generate(Pop cand, Pop pop, int *d_best, speo_island_info ii, Info *d_info, 
     k_best<T><<<(ii.subisland_num + kWarps - 1) / kWarps, 32 * kWarps, 0, st>>>(
         pop.fitness_value, ii.permutated_index, S, ii.subisland_num, d_best);
     if (int e = check_launch("global_DE_FindBestIndividualInIsland")) return e;
-    k_generate<T><<<(ii.island_size + kWarps - 1) / kWarps, 32 * kWarps, 0, st>>>(
-        cand.elements, pop.elements, ld, pi.dim, ii.island_size, S, ii.permutated_index,
-        reinterpret_cast<const typename DeInfoT<T>::type *>(d_info), d_best, (T)pi.min_bound, (T)pi.max_bound,
-        reinterpret_cast<RngState *>(d_rng));
+    // lanes per row: enough 16-byte chunks to cover D (np2 rows keep every chunk in bounds)
+    const int vn = 16 / (int)sizeof(T), nch = (pi.dim + vn - 1) / vn;
+    const int grid = (ii.island_size + kGenRows - 1) / kGenRows;
+    const auto *inf = reinterpret_cast<const typename DeInfoT<T>::type *>(d_info);
+    RngState *rs = reinterpret_cast<RngState *>(d_rng);
+    if (nch <= 4)
+        k_generate<T, 4><<<grid, 256, 0, st>>>(cand.elements, pop.elements, ld, pi.dim, ii.island_size, S,
+                                                 ii.permutated_index, inf, d_best, (T)pi.min_bound, (T)pi.max_bound, rs);
+    else if (nch <= 8)
+        k_generate<T, 8><<<grid, 256, 0, st>>>(cand.elements, pop.elements, ld, pi.dim, ii.island_size, S,
+                                                 ii.permutated_index, inf, d_best, (T)pi.min_bound, (T)pi.max_bound, rs);
+    else if (nch <= 16)
+        k_generate<T, 16><<<grid, 256, 0, st>>>(cand.elements, pop.elements, ld, pi.dim, ii.island_size, S,
+                                                  ii.permutated_index, inf, d_best, (T)pi.min_bound, (T)pi.max_bound, rs);
+    else
+        k_generate<T, 32><<<grid, 256, 0, st>>>(cand.elements, pop.elements, ld, pi.dim, ii.island_size, S,
+                                                  ii.permutated_index, inf, d_best, (T)pi.min_bound, (T)pi.max_bound, rs);
     return check_launch("global_DE_GenerateNewPopulation");
 }
 

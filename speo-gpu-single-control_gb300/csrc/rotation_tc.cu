@@ -94,7 +94,9 @@ __device__ __forceinline__ void build_b(const speo_segment &s, int Kp, uint8_t *
 }
 
 // Staged FP32 rows -> y = x - o -> BF16 hi/lo K-major A operand, `nthr` threads. Rows >= count
-// become zero.
+// become zero. Thread (m, kc) reads 8 consecutive floats of row m with two 16-byte loads (the
+// staged row stride keeps 8 consecutive rows on distinct banks) and writes one 16-byte chunk of
+// each operand.
 __device__ __forceinline__ void build_a(const float *stage, int box_x, int count, int D, int Kp, const float *so,
                                         uint8_t *a_hi, uint8_t *a_lo, int t, int nthr)
 {
@@ -102,15 +104,22 @@ __device__ __forceinline__ void build_a(const float *stage, int box_x, int count
     for (int i = t; i < pairs; i += nthr) {
         const int m = i % kTileM, kc = i / kTileM;
         float v[8];
-        const float *src = stage + (size_t)m * box_x + 8 * kc;
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            const int k = 8 * kc + e;
-            v[e] = (m < count && k < D) ? __fsub_rn(src[e], so[k]) : 0.f;
-        }
+        const float4 *src = reinterpret_cast<const float4 *>(stage + (size_t)m * box_x + 8 * kc);
+        const float4 *o4 = reinterpret_cast<const float4 *>(so + 8 * kc);
+        const float4 x0 = src[0], x1 = src[1], s0 = o4[0], s1 = o4[1];
+        const bool live = m < count;
+        const int kb = 8 * kc;
+        v[0] = (live && kb + 0 < D) ? __fsub_rn(x0.x, s0.x) : 0.f;
+        v[1] = (live && kb + 1 < D) ? __fsub_rn(x0.y, s0.y) : 0.f;
+        v[2] = (live && kb + 2 < D) ? __fsub_rn(x0.z, s0.z) : 0.f;
+        v[3] = (live && kb + 3 < D) ? __fsub_rn(x0.w, s0.w) : 0.f;
+        v[4] = (live && kb + 4 < D) ? __fsub_rn(x1.x, s1.x) : 0.f;
+        v[5] = (live && kb + 5 < D) ? __fsub_rn(x1.y, s1.y) : 0.f;
+        v[6] = (live && kb + 6 < D) ? __fsub_rn(x1.z, s1.z) : 0.f;
+        v[7] = (live && kb + 7 < D) ? __fsub_rn(x1.w, s1.w) : 0.f;
         uint4 h, l;
         tc::split8(v, h, l);
-        const uint32_t off = tc::kmajor_offset(m, 8 * kc, Kp);
+        const uint32_t off = tc::kmajor_offset(m, kb, Kp);
         *reinterpret_cast<uint4 *>(a_hi + off) = h;
         *reinterpret_cast<uint4 *>(a_lo + off) = l;
     }
@@ -133,19 +142,49 @@ __device__ __forceinline__ void issue_split_mma(uint32_t tmem, const uint8_t *a_
     }
 }
 
-// Warps 0..3, one TMEM lane (= tile row) per thread: f = sum_j term(scale * z_j), j < D.
+// Two objective terms at once (f32x2); per element the same operations as obj_term: z - rint(z)
+// (rint by adding and subtracting 1.5 * 2^23, exact for |z| < 2^22), the Taylor sine, and
+// z*z + (20 s) s.
+__device__ __forceinline__ uint64_t obj_term2(int func, uint64_t z)
+{
+    using namespace tc;
+    if (func != SPEO_FUNC_ROTATED_RASTRIGIN) return mul2(z, z);
+    const uint64_t C = pk2(12582912.0f, 12582912.0f);
+    const uint64_t r = sub2(z, sub2(add2(z, C), C));
+    const uint64_t r2 = mul2(r, r);
+    uint64_t p = pk2(-7.3704309762e-03f, -7.3704309762e-03f);
+    p = fma2(p, r2, pk2(8.2145884633e-02f, 8.2145884633e-02f));
+    p = fma2(p, r2, pk2(-5.9926450253e-01f, -5.9926450253e-01f));
+    p = fma2(p, r2, pk2(2.5501639843e+00f, 2.5501639843e+00f));
+    p = fma2(p, r2, pk2(-5.1677126884e+00f, -5.1677126884e+00f));
+    p = fma2(p, r2, pk2(3.1415927410e+00f, 3.1415927410e+00f));
+    const uint64_t sn = mul2(r, p);
+    return fma2(z, z, mul2(mul2(pk2(20.0f, 20.0f), sn), sn));
+}
+
+// Warps of one TMEM lane quarter (warp % 4), one lane (= tile row) per thread:
+// f = sum_j term(scale * z_j), j < D, two columns per packed op, 32 columns per TMEM load.
 __device__ __forceinline__ float epilogue_row(uint32_t tmem, int warp, int D, int Np, int func, float scale)
 {
-    float f = 0.f;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int c = 0; c < Np; c += 16) {
-        float z[16];
-        tc::tmem_ld16(lane_base + (uint32_t)c, z);
+    using namespace tc;
+    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    const uint64_t sc = pk2(scale, scale);
+    uint64_t acc = pk2(0.f, 0.f);
+    for (int c = 0; c < Np; c += 32) {
+        uint32_t r[32];
+        tmem_ld32_nowait(lane_base + (uint32_t)c, r);
+        tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-            if (c + j < D) f += obj_term(func, z[j] * scale);
+        for (int j = 0; j < 32; j += 2) {
+            if (c + j < D) {
+                const float z1 = (c + j + 1 < D) ? __uint_as_float(r[j + 1]) : 0.f;
+                acc = add2(acc, obj_term2(func, mul2(pk2(__uint_as_float(r[j]), z1), sc)));
+            }
+        }
     }
-    return f;
+    float a, b;
+    upk2(acc, a, b);
+    return a + b;
 }
 
 __device__ __forceinline__ bool tc_tile_ok(const speo_work_item &it, const speo_segment &s, const EvalTcArgs &a)
@@ -160,6 +199,29 @@ __device__ __forceinline__ bool tc_tile_ok(const speo_work_item &it, const speo_
 //   bar_tma[s]  stage s holds the rows of its tile         (TMA transaction bytes)
 //   bar_mma[b]  accumulator b holds a finished product     (tcgen05.commit)
 //   bar_epi[b]  the epilogue is done reading accumulator b (128 arrivals)
+// Everything a role needs about one tile, loaded ahead of use (two-stage register prefetch:
+// the work item two tiles ahead, its segment one tile ahead).
+struct TileInfo {
+    int ok, count, D, func, ld_rot;
+    long long row;
+    const float *rot, *shift;
+};
+
+__device__ __forceinline__ TileInfo tile_info(const EvalTcArgs &a, const speo_work_item &it)
+{
+    const speo_segment &s = a.segs[it.segment];
+    TileInfo t;
+    t.ok = tc_tile_ok(it, s, a);
+    t.count = it.count;
+    t.D = t.ok ? s.dim : 16;
+    t.func = s.func_id;
+    t.ld_rot = s.ld_rot;
+    t.row = s.row0 + it.first;
+    t.rot = s.rot;
+    t.shift = s.shift;
+    return t;
+}
+
 __global__ void __launch_bounds__(256, 1) k_evaluate_tc(const __grid_constant__ CUtensorMap xmap, EvalTcArgs a)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -217,21 +279,24 @@ __global__ void __launch_bounds__(256, 1) k_evaluate_tc(const __grid_constant__ 
             for (int i = 0; i < ns; ++i) issue_tma(i);
         const float *c_rot = nullptr, *c_shift = nullptr;
         int c_dim = -1, c_ldrot = -1;
+        speo_work_item it_next = item_of(my_items > 1 ? 1 : 0);
+        TileInfo cur = tile_info(a, item_of(0));
         for (int i = 0; i < my_items; ++i) {
-            const speo_work_item it = item_of(i);
-            const speo_segment &s = a.segs[it.segment];
-            const bool ok = tc_tile_ok(it, s, a);
-            const int D = ok ? s.dim : 16, Kp = round16(D);
+            const speo_work_item it_nn = item_of(i + 2 < my_items ? i + 2 : i);
+            const TileInfo nxt = tile_info(a, it_next);
+            const int D = cur.D, Kp = round16(D);
             bool to = !tc::mbar_wait(&bar_tma[i % ns], (uint32_t)((i / ns) & 1), kWaitBudget);
             if (i >= 1) to |= !tc::mbar_wait(&bar_mma[(i - 1) & 1], (uint32_t)(((i - 1) >> 1) & 1), kWaitBudget);
             if (tc::named_bar_or(1, 128, to || *abort_flag != 0)) { *abort_flag = 1; break; }
-            if (ok) {
-                if (s.rot != c_rot || s.shift != c_shift || D != c_dim || s.ld_rot != c_ldrot) {
-                    build_b(s, Kp, b_hi, b_lo, so, ct, 128);
-                    c_rot = s.rot; c_shift = s.shift; c_dim = D; c_ldrot = s.ld_rot;
+            if (cur.ok) {
+                if (cur.rot != c_rot || cur.shift != c_shift || D != c_dim || cur.ld_rot != c_ldrot) {
+                    speo_segment sb;
+                    sb.dim = D; sb.rot = cur.rot; sb.shift = cur.shift; sb.ld_rot = cur.ld_rot;
+                    build_b(sb, Kp, b_hi, b_lo, so, ct, 128);
+                    c_rot = cur.rot; c_shift = cur.shift; c_dim = D; c_ldrot = cur.ld_rot;
                     tc::named_bar_sync(1, 128);
                 }
-                build_a(stage[i % ns], L.box_x, it.count, D, Kp, so, a_hi, a_lo, ct, 128);
+                build_a(stage[i % ns], L.box_x, cur.count, D, Kp, so, a_hi, a_lo, ct, 128);
             } else if (ct == 0) {
                 atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
             }
@@ -250,25 +315,29 @@ __global__ void __launch_bounds__(256, 1) k_evaluate_tc(const __grid_constant__ 
                     mma_issued = i + 1;
                 }
             }
+            cur = nxt;
+            it_next = it_nn;
         }
     } else {
         // ---- epilogue group: one TMEM lane (= tile row) per thread ----------------------------------
+        speo_work_item it_next = item_of(my_items > 1 ? 1 : 0);
+        TileInfo cur = tile_info(a, item_of(0));
         for (int i = 0; i < my_items; ++i) {
             if (__any_sync(0xffffffffu, *abort_flag != 0)) break;
-            const speo_work_item it = item_of(i);
-            const speo_segment &s = a.segs[it.segment];
-            const bool ok = tc_tile_ok(it, s, a);
-            const int D = ok ? s.dim : 16, Kp = round16(D);
+            const speo_work_item it_nn = item_of(i + 2 < my_items ? i + 2 : i);
+            const TileInfo nxt = tile_info(a, it_next);
             // warp-uniform decision: tcgen05.ld below is warp-collective
             const bool got = tc::mbar_wait(&bar_mma[i & 1], (uint32_t)((i >> 1) & 1), kWaitBudget);
             if (!__all_sync(0xffffffffu, got)) { *abort_flag = 1; break; }
             tc::fence_after_sync();
-            const float f = epilogue_row(tmem + (uint32_t)((i & 1) * kTmemCols), warp, D, Kp, s.func_id,
-                                         func_scale(s.func_id));
+            const float f = epilogue_row(tmem + (uint32_t)((i & 1) * kTmemCols), warp, cur.D, round16(cur.D),
+                                         cur.func, func_scale(cur.func));
             const int m = warp * 32 + lane;
-            if (ok && m < it.count) a.fit[s.row0 + it.first + m] = f;
+            if (cur.ok && m < cur.count) a.fit[cur.row + m] = f;
             tc::fence_before_sync();
             tc::mbar_arrive(&bar_epi[i & 1]);
+            cur = nxt;
+            it_next = it_nn;
         }
     }
     __syncthreads();
