@@ -97,7 +97,6 @@ __global__ void k_best(const T *fit, const int *perm, int S, int nsub, int *best
 // (1) one thread per position draws the donors and jrand (the reference recomputes them on all
 // 32 lanes), (2) G lanes per row build the trial from 16-byte vector loads of the target and
 // donor rows with one Philox block per 4 elements, and store it with vector stores.
-constexpr int kGenRows = 64;
 
 template <typename T> struct Vec;
 template <> struct Vec<float> { using type = float4; static constexpr int n = 4; };
@@ -126,6 +125,9 @@ __device__ __forceinline__ int ndonors(int st)
     }
 }
 
+// One warp owns 32 consecutive positions: lane l draws the donors and jrand of position l
+// (Philox on all lanes at once), then the warp walks its rows R = 32/G at a time, G lanes per
+// row, two steps in flight, broadcasting each row's draws with shuffles.
 template <typename T, int G>
 __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld, int dim, int island_size, int S,
                                                   const int *perm, const typename DeInfoT<T>::type *info,
@@ -133,38 +135,46 @@ __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld,
 {
     using V = typename Vec<T>::type;
     constexpr int VN = Vec<T>::n;
-    __shared__ int sR[kGenRows][8];  // donor rows (through perm), jrand, target row, sub-island
+    constexpr int R = 32 / G;
     const uint32_t gen = *(volatile uint32_t *)&rng->gen;
     const uint2 key = make_uint2(rng->key0, rng->key1);
-    const int tid = threadIdx.x;
-    const int pos0 = blockIdx.x * kGenRows;
-    bool ok_bound = true;
-    if (tid < kGenRows && pos0 + tid < island_size) {
-        const int pos = pos0 + tid;
-        const int isl = pos / S;
-        IdxStream s(key, (uint32_t)pos, gen, kTagIdx);
-        int r[5];
-        if (!draw_donors(s, S, r)) atomicOr(&s_deverr, SPEO_DEVERR_REDRAW_LIMIT);
-#pragma unroll
-        for (int i = 0; i < 5; ++i) sR[tid][i] = perm[r[i] + isl * S];
-        sR[tid][5] = s.index(dim);
-        sR[tid][6] = perm[pos];
-        sR[tid][7] = isl;
+    const int lane = threadIdx.x & 31;
+    const int wbase = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
+    // ---- draws of position wbase + lane ------------------------------------------------------
+    int d0 = 0, d1 = 0, d2 = 0, d3 = 0, d4 = 0, jr = 0, sel = 0, isl = 0;
+    {
+        const int pos = wbase + lane;
+        if (pos < island_size) {
+            isl = pos / S;
+            IdxStream s(key, (uint32_t)pos, gen, kTagIdx);
+            int r[5];
+            if (!draw_donors(s, S, r)) atomicOr(&s_deverr, SPEO_DEVERR_REDRAW_LIMIT);
+            d0 = perm[r[0] + isl * S]; d1 = perm[r[1] + isl * S]; d2 = perm[r[2] + isl * S];
+            d3 = perm[r[3] + isl * S]; d4 = perm[r[4] + isl * S];
+            jr = s.index(dim);
+            sel = perm[pos];
+        }
     }
-    __syncthreads();
-    const int grp = tid / G, gl = tid % G;
     const int nch = (dim + VN - 1) / VN;
-    for (int lr = grp; lr < kGenRows; lr += 256 / G) {
-        const int pos = pos0 + lr;
-        if (pos >= island_size) break;
-        const int sel = sR[lr][6], isl = sR[lr][7], jrand = sR[lr][5];
-        const T F = info[isl].F, CR = info[isl].CR;
-        const int st = info[isl].strategy_ID;
+    const int gl = lane % G;
+    bool ok_bound = true;
+#pragma unroll 2
+    for (int step = 0; step < 32; step += R) {
+        const int src = step + lane / G;  // lane holding this group's row
+        const int pos = wbase + src;
+        const int rsel = __shfl_sync(0xffffffffu, sel, src), risl = __shfl_sync(0xffffffffu, isl, src);
+        const int rjr = __shfl_sync(0xffffffffu, jr, src);
+        const int rd[5] = {__shfl_sync(0xffffffffu, d0, src), __shfl_sync(0xffffffffu, d1, src),
+                           __shfl_sync(0xffffffffu, d2, src), __shfl_sync(0xffffffffu, d3, src),
+                           __shfl_sync(0xffffffffu, d4, src)};
+        if (pos >= island_size) continue;
+        const T F = info[risl].F, CR = info[risl].CR;
+        const int st = info[risl].strategy_ID;
         const int nd = ndonors(st);
-        const int b = strategy_uses_best(st) ? best_id[isl] : sel;
-        const T *xi = pop + (size_t)sel * ld;
+        const int b = strategy_uses_best(st) ? best_id[risl] : rsel;
+        const T *xi = pop + (size_t)rsel * ld;
         const T *xb = pop + (size_t)b * ld;
-        T *out = cand + (size_t)sel * ld;
+        T *out = cand + (size_t)rsel * ld;
         for (int c = gl; c < nch; c += G) {
             const int e0 = VN * c;
             const V ti = *reinterpret_cast<const V *>(xi + e0);
@@ -172,7 +182,7 @@ __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld,
             V tr[5];
 #pragma unroll
             for (int k = 0; k < 5; ++k)
-                tr[k] = k < nd ? *reinterpret_cast<const V *>(pop + (size_t)sR[lr][k] * ld + e0) : ti;
+                tr[k] = k < nd ? *reinterpret_cast<const V *>(pop + (size_t)rd[k] * ld + e0) : ti;
             const uint4 w = philox(make_uint4((uint32_t)(e0 >> 2), (uint32_t)pos, gen, kTagCr), key);
             V o = ti;
 #pragma unroll
@@ -180,7 +190,7 @@ __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld,
                 const int e = e0 + q;
                 const float u = u01(pick(w, (uint32_t)(e & 3)));
                 T v;
-                if (e == jrand || (T)u < CR) {
+                if (e == rjr || (T)u < CR) {
                     T xr[5];
 #pragma unroll
                     for (int k = 0; k < 5; ++k) xr[k] = vget<T>(tr[k], q);
@@ -203,18 +213,26 @@ __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld,
     finish_launch(rng, gen);
 }
 
-// global_DE_SelectSurvival (kernel_DE_CUDA.cu:305-327): strict `<`, one warp per row.
+// global_DE_SelectSurvival (kernel_DE_CUDA.cu:305-327): strict `<`. One thread per 16-byte
+// chunk of a row: rows whose trial loses move no data.
 template <typename T>
 __global__ void k_select(T *pop, T *pop_fit, const T *cand, const T *cand_fit, int n, int ld, int dim)
 {
-    const int i = blockIdx.x * kWarps + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (i >= n) return;
+    using V = typename Vec<T>::type;
+    constexpr int VN = Vec<T>::n;
+    const int nch = (dim + VN - 1) / VN;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * nch) return;
+    const int i = (int)(t / nch), c = (int)(t - (long long)i * nch);
     const T fc = cand_fit[i];
-    if (fc < pop_fit[i]) {
-        for (int e = lane; e < dim; e += 32) pop[(size_t)i * ld + e] = cand[(size_t)i * ld + e];
-        if (lane == 0) pop_fit[i] = fc;
+    if (!(fc < pop_fit[i])) return;
+    const int e0 = VN * c;
+    if (e0 + VN <= dim) {
+        *reinterpret_cast<V *>(pop + (size_t)i * ld + e0) = *reinterpret_cast<const V *>(cand + (size_t)i * ld + e0);
+    } else {
+        for (int q = 0; q < VN && e0 + q < dim; ++q) pop[(size_t)i * ld + e0 + q] = cand[(size_t)i * ld + e0 + q];
     }
+    if (c == 0) pop_fit[i] = fc;
 }
 
 template <typename T>
@@ -259,7 +277,7 @@ int generate(Pop cand, Pop pop, int *d_best, speo_island_info ii, Info *d_info, 
     if (int e = check_launch("global_DE_FindBestIndividualInIsland")) return e;
     // lanes per row: enough 16-byte chunks to cover D (np2 rows keep every chunk in bounds)
     const int vn = 16 / (int)sizeof(T), nch = (pi.dim + vn - 1) / vn;
-    const int grid = (ii.island_size + kGenRows - 1) / kGenRows;
+    const int grid = (ii.island_size + 255) / 256;  // 8 warps x 32 positions per block
     const auto *inf = reinterpret_cast<const typename DeInfoT<T>::type *>(d_info);
     RngState *rs = reinterpret_cast<RngState *>(d_rng);
     if (nch <= 4)
@@ -284,7 +302,9 @@ int select(Pop pop, Pop cand, speo_island_info ii, Prob pi)
     if (!cand.elements || !pop.fitness_value || !cand.fitness_value)
         return fail(SPEO_ERR_INVALID_ARG, "API_DE_SelectSurvival: null pointer argument");
     const int ld = np2_of(pi.dim);
-    k_select<T><<<(ii.island_size + kWarps - 1) / kWarps, 32 * kWarps, 0, api_stream()>>>(
+    const int vn = 16 / (int)sizeof(T);
+    const long long threads = (long long)ii.island_size * ((pi.dim + vn - 1) / vn);
+    k_select<T><<<(unsigned)((threads + 255) / 256), 256, 0, api_stream()>>>(
         pop.elements, pop.fitness_value, cand.elements, cand.fitness_value, ii.island_size, ld, pi.dim);
     return check_launch("global_DE_SelectSurvival");
 }
