@@ -185,20 +185,32 @@ __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld,
                 tr[k] = k < nd ? *reinterpret_cast<const V *>(pop + (size_t)rd[k] * ld + e0) : ti;
             const uint4 w = philox(make_uint4((uint32_t)(e0 >> 2), (uint32_t)pos, gen, kTagCr), key);
             V o = ti;
+            if (st == SPEO_DE_RAND_1) {  // rand/1, the default strategy (DE_CUDA.cc:63): no switch
 #pragma unroll
-            for (int q = 0; q < VN; ++q) {
-                const int e = e0 + q;
-                const float u = u01(pick(w, (uint32_t)(e & 3)));
-                T v;
-                if (e == rjr || (T)u < CR) {
-                    T xr[5];
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) xr[k] = vget<T>(tr[k], q);
-                    v = mutant<T>(st, F, vget<T>(ti, q), vget<T>(tb, q), xr);
-                } else {
-                    v = vget<T>(ti, q);
+                for (int q = 0; q < VN; ++q) {
+                    const int e = e0 + q;
+                    const float u = u01(pick(w, (uint32_t)(e & 3)));
+                    T v = vget<T>(ti, q);
+                    if (e == rjr || (T)u < CR)
+                        v = fma_rn(F, sub_rn(vget<T>(tr[1], q), vget<T>(tr[2], q)), vget<T>(tr[0], q));
+                    vset<T>(o, q, check_bound<T>(v, lb, ub, ok_bound));
                 }
-                vset<T>(o, q, check_bound<T>(v, lb, ub, ok_bound));
+            } else {
+#pragma unroll
+                for (int q = 0; q < VN; ++q) {
+                    const int e = e0 + q;
+                    const float u = u01(pick(w, (uint32_t)(e & 3)));
+                    T v;
+                    if (e == rjr || (T)u < CR) {
+                        T xr[5];
+#pragma unroll
+                        for (int k = 0; k < 5; ++k) xr[k] = vget<T>(tr[k], q);
+                        v = mutant<T>(st, F, vget<T>(ti, q), vget<T>(tb, q), xr);
+                    } else {
+                        v = vget<T>(ti, q);
+                    }
+                    vset<T>(o, q, check_bound<T>(v, lb, ub, ok_bound));
+                }
             }
             if (e0 + VN <= dim) {
                 *reinterpret_cast<V *>(out + e0) = o;
@@ -213,26 +225,46 @@ __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld,
     finish_launch(rng, gen);
 }
 
-// global_DE_SelectSurvival (kernel_DE_CUDA.cu:305-327): strict `<`. One thread per 16-byte
-// chunk of a row: rows whose trial loses move no data.
+// global_DE_SelectSurvival (kernel_DE_CUDA.cu:305-327): strict `<`. Grid-stride over 16-byte
+// chunks of rows, four independent chunks in flight per thread; rows whose trial loses move no
+// data.
 template <typename T>
-__global__ void k_select(T *pop, T *pop_fit, const T *cand, const T *cand_fit, int n, int ld, int dim)
+__global__ void __launch_bounds__(256) k_select(T *pop, T *pop_fit, const T *cand, const T *cand_fit, int n, int ld,
+                                                int dim)
 {
     using V = typename Vec<T>::type;
-    constexpr int VN = Vec<T>::n;
+    constexpr int VN = Vec<T>::n, U = 4;
     const int nch = (dim + VN - 1) / VN;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)n * nch) return;
-    const int i = (int)(t / nch), c = (int)(t - (long long)i * nch);
-    const T fc = cand_fit[i];
-    if (!(fc < pop_fit[i])) return;
-    const int e0 = VN * c;
-    if (e0 + VN <= dim) {
-        *reinterpret_cast<V *>(pop + (size_t)i * ld + e0) = *reinterpret_cast<const V *>(cand + (size_t)i * ld + e0);
-    } else {
-        for (int q = 0; q < VN && e0 + q < dim; ++q) pop[(size_t)i * ld + e0 + q] = cand[(size_t)i * ld + e0 + q];
+    const long long total = (long long)n * nch;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; t0 < total; t0 += stride * U) {
+        int row[U], c[U];
+        bool win[U];
+        T fc[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long long t = t0 + u * stride;
+            row[u] = (int)(t / nch);
+            c[u] = (int)(t - (long long)row[u] * nch);
+            win[u] = false;
+            if (t < total) {
+                fc[u] = cand_fit[row[u]];
+                win[u] = fc[u] < pop_fit[row[u]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (!win[u]) continue;
+            const size_t base = (size_t)row[u] * ld;
+            const int e0 = VN * c[u];
+            if (e0 + VN <= dim) {
+                *reinterpret_cast<V *>(pop + base + e0) = *reinterpret_cast<const V *>(cand + base + e0);
+            } else {
+                for (int q = 0; q < VN && e0 + q < dim; ++q) pop[base + e0 + q] = cand[base + e0 + q];
+            }
+            if (c[u] == 0) pop_fit[row[u]] = fc[u];
+        }
     }
-    if (c == 0) pop_fit[i] = fc;
 }
 
 template <typename T>
@@ -304,7 +336,9 @@ int select(Pop pop, Pop cand, speo_island_info ii, Prob pi)
     const int ld = np2_of(pi.dim);
     const int vn = 16 / (int)sizeof(T);
     const long long threads = (long long)ii.island_size * ((pi.dim + vn - 1) / vn);
-    k_select<T><<<(unsigned)((threads + 255) / 256), 256, 0, api_stream()>>>(
+    const long long want = (threads + 4 * 256 - 1) / (4 * 256);
+    const int grid = (int)(want < 16LL * sm_count() ? (want > 0 ? want : 1) : 16LL * sm_count());
+    k_select<T><<<grid, 256, 0, api_stream()>>>(
         pop.elements, pop.fitness_value, cand.elements, cand.fitness_value, ii.island_size, ld, pi.dim);
     return check_launch("global_DE_SelectSurvival");
 }
