@@ -273,6 +273,38 @@ SPEO_API int speo_ring_migrate(const speo_segment *d_segs, int n_segs, int k, fl
 SPEO_API int speo_ring_migrate_noalloc(const speo_segment *d_segs, int n_segs, int k, float *pop,
                                        float *fit, int max_ld, void *stream);
 
+/* ---- Online MLP surrogate (no counterpart in the reference) -------------------------------
+ * din -> hidden -> hidden -> 1 with ReLU, FP32 parameters in one flat vector
+ * (W1[h][din], b1[h], W2[h][h], b2[h], w3[h], b3), inputs scaled by in_scale, trained by Adam
+ * (beta1 0.9, beta2 0.999, eps 1e-8) on the mean squared error of log(f + 1e-8) over batches
+ * sampled from a ring-buffer archive of exact evaluations. The object owns its device memory. */
+typedef struct speo_surrogate speo_surrogate;
+SPEO_API int speo_surrogate_create(speo_surrogate **out, int din, int hidden, long long archive_cap, int batch,
+                                   float lr, float in_scale, uint64_t seed);
+SPEO_API int speo_surrogate_destroy(speo_surrogate *s);
+SPEO_API int speo_surrogate_params(speo_surrogate *s, float **d_theta, float **d_grad, int *n_params);
+SPEO_API int speo_surrogate_forward(speo_surrogate *s, const float *X, int n, int ldx, float *y, void *stream);
+/* Gradient of the batch MSE w.r.t. theta into the object's gradient buffer; mean loss out. */
+SPEO_API int speo_surrogate_grad(speo_surrogate *s, const float *X, int n, int ldx, const float *T,
+                                 float *loss_out, void *stream);
+SPEO_API int speo_surrogate_adam_step(speo_surrogate *s, void *stream);
+SPEO_API int speo_surrogate_archive_append(speo_surrogate *s, const float *X, int n, int ldx, const float *f,
+                                           void *stream);
+SPEO_API int speo_surrogate_train(speo_surrogate *s, int steps, float *loss_out, void *stream);
+/* k trial vectors per target: trial t of row r is written to T[(r*k + t)*ld ...]; its donor and
+ * crossover draws use Philox tags (1 | (t+1) << 8) and (2 | (t+1) << 8). */
+SPEO_API int speo_make_trials(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,
+                              int dim_hi, int k, const float *pop, const float *fit, float *T,
+                              const uint32_t *d_gen, void *stream);
+/* One screened generation over a flat population (rows x ld): k trials per target, the MLP
+ * picks one, exact evaluation, strict-`<` selection into (pop_out, fit_out), archive append,
+ * `train_steps` Adam steps; *d_gen advances by one. */
+SPEO_API int speo_surrogate_generation(speo_surrogate *s, const speo_segment *d_segs,
+                                       const speo_work_item *d_items, int n_items, int dim_lo, int dim_hi,
+                                       long long rows, int ld, int k, const float *pop_in,
+                                       const float *fit_in, float *pop_out, float *fit_out,
+                                       uint32_t *d_gen, int train_steps, void *stream);
+
 /* Per segment: argmin of fit (ties: lowest row) -> best_row[s]; FP64 re-evaluation of that
  * row -> best_err[s] = f(x) - f* in double. */
 SPEO_API int speo_best_reeval_f64(const speo_segment *d_segs, int n_segs, const float *pop,

@@ -437,3 +437,101 @@ int64_t speo_oracle_run_islands_f64(int n_islands, int P, int D, int ld, int fun
     }
     return (int64_t)gens * n_islands * P;
 }
+
+/* ---- surrogate MLP --------------------------------------------------------------------- */
+int speo_oracle_mlp_nparams(int din, int h) { return h * din + h + h * h + h + h + 1; }
+
+typedef struct { const float *W1, *b1, *W2, *b2, *w3, *b3; } mlp_view;
+
+static mlp_view mlp_split(const float *theta, int din, int h)
+{
+    mlp_view v;
+    v.W1 = theta;
+    v.b1 = v.W1 + (size_t)h * din;
+    v.W2 = v.b1 + h;
+    v.b2 = v.W2 + (size_t)h * h;
+    v.w3 = v.b2 + h;
+    v.b3 = v.w3 + h;
+    return v;
+}
+
+/* forward of one row; keeps pre-activations z1, z2 (length h) */
+static double mlp_row(mlp_view p, int din, int h, float in_scale, const float *x, double *z1, double *z2)
+{
+    for (int j = 0; j < h; ++j) {
+        double a = p.b1[j];
+        for (int k = 0; k < din; ++k) a += (double)p.W1[(size_t)j * din + k] * ((double)x[k] * (double)in_scale);
+        z1[j] = a;
+    }
+    for (int j = 0; j < h; ++j) {
+        double a = p.b2[j];
+        for (int k = 0; k < h; ++k) a += (double)p.W2[(size_t)j * h + k] * (z1[k] > 0 ? z1[k] : 0.0);
+        z2[j] = a;
+    }
+    double y = p.b3[0];
+    for (int j = 0; j < h; ++j) y += (double)p.w3[j] * (z2[j] > 0 ? z2[j] : 0.0);
+    return y;
+}
+
+void speo_oracle_mlp_forward(const float *theta, int din, int h, float in_scale, const float *X, int n, int ldx,
+                             double *y)
+{
+    mlp_view p = mlp_split(theta, din, h);
+    double *z1 = (double *)malloc(sizeof(double) * (size_t)h), *z2 = (double *)malloc(sizeof(double) * (size_t)h);
+    for (int i = 0; i < n; ++i) y[i] = mlp_row(p, din, h, in_scale, X + (size_t)i * ldx, z1, z2);
+    free(z1);
+    free(z2);
+}
+
+double speo_oracle_mlp_loss_grad(const float *theta, int din, int h, float in_scale, const float *X, int n, int ldx,
+                                 const float *t, double *grad)
+{
+    mlp_view p = mlp_split(theta, din, h);
+    const int np = speo_oracle_mlp_nparams(din, h);
+    double *gW1 = grad, *gb1 = gW1 + (size_t)h * din, *gW2 = gb1 + h, *gb2 = gW2 + (size_t)h * h, *gw3 = gb2 + h,
+           *gb3 = gw3 + h;
+    memset(grad, 0, sizeof(double) * (size_t)np);
+    double *z1 = (double *)malloc(sizeof(double) * (size_t)h), *z2 = (double *)malloc(sizeof(double) * (size_t)h);
+    double *dz2 = (double *)malloc(sizeof(double) * (size_t)h), *dz1 = (double *)malloc(sizeof(double) * (size_t)h);
+    double loss = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const float *x = X + (size_t)i * ldx;
+        const double y = mlp_row(p, din, h, in_scale, x, z1, z2);
+        const double e = y - (double)t[i];
+        loss += e * e;
+        const double dy = 2.0 * e / n;
+        gb3[0] += dy;
+        for (int j = 0; j < h; ++j) {
+            const double a2 = z2[j] > 0 ? z2[j] : 0.0;
+            gw3[j] += dy * a2;
+            dz2[j] = z2[j] > 0 ? dy * p.w3[j] : 0.0;
+        }
+        for (int j = 0; j < h; ++j) {
+            gb2[j] += dz2[j];
+            for (int k = 0; k < h; ++k) gW2[(size_t)j * h + k] += dz2[j] * (z1[k] > 0 ? z1[k] : 0.0);
+        }
+        for (int k = 0; k < h; ++k) {
+            double a = 0.0;
+            for (int j = 0; j < h; ++j) a += dz2[j] * (double)p.W2[(size_t)j * h + k];
+            dz1[k] = z1[k] > 0 ? a : 0.0;
+        }
+        for (int j = 0; j < h; ++j) {
+            gb1[j] += dz1[j];
+            for (int k = 0; k < din; ++k) gW1[(size_t)j * din + k] += dz1[j] * ((double)x[k] * (double)in_scale);
+        }
+    }
+    free(z1); free(z2); free(dz1); free(dz2);
+    return loss / n;
+}
+
+void speo_oracle_adam(float *theta, float *m, float *v, const float *g, int n, float lr, float beta1, float beta2,
+                      float eps, int step)
+{
+    const float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
+    for (int i = 0; i < n; ++i) {
+        m[i] = beta1 * m[i] + (1.0f - beta1) * g[i];
+        v[i] = beta2 * v[i] + (1.0f - beta2) * g[i] * g[i];
+        const float mh = m[i] / c1, vh = v[i] / c2;
+        theta[i] -= lr * mh / (sqrtf(vh) + eps);
+    }
+}

@@ -125,6 +125,20 @@ int64_t speo_oracle_run_islands_f64(int n_islands, int P, int D, int ld, int fun
                                     uint32_t gen0, int gens, int interval, int k_migrate,
                                     double *pop, double *fit, int threads);
 
+/* ---- Surrogate MLP (this library's learned pre-screen; no reference counterpart) -----------
+ * din -> h (ReLU) -> h (ReLU) -> 1. Flat FP32 parameter vector, in order:
+ *   W1[h][din], b1[h], W2[h][h], b2[h], w3[h], b3[1]   (din=50, h=256: 79105 values).
+ * Inputs are scaled by `in_scale` before the first layer. Forward and backward in FP64. */
+int speo_oracle_mlp_nparams(int din, int h);
+void speo_oracle_mlp_forward(const float *theta, int din, int h, float in_scale, const float *X, int n, int ldx,
+                             double *y);
+/* Mean-squared-error loss sum_i (y_i - t_i)^2 / n and its gradient w.r.t. theta (FP64). */
+double speo_oracle_mlp_loss_grad(const float *theta, int din, int h, float in_scale, const float *X, int n, int ldx,
+                                 const float *t, double *grad);
+/* One Adam step (Kingma & Ba, 2015) with bias correction; `step` counts from 1. */
+void speo_oracle_adam(float *theta, float *m, float *v, const float *g, int n, float lr, float beta1, float beta2,
+                      float eps, int step);
+
 #ifdef __cplusplus
 }
 #endif

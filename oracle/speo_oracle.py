@@ -53,6 +53,13 @@ def lib() -> ctypes.CDLL:
                                                   c_double, c_void_p, c_void_p, c_uint64, c_uint32, c_int, c_int,
                                                   c_int, c_void_p, c_void_p, c_int]
         L.speo_oracle_run_islands_f64.restype = c_int64
+        L.speo_oracle_mlp_nparams.argtypes = [c_int, c_int]
+        L.speo_oracle_mlp_forward.argtypes = [c_void_p, c_int, c_int, c_float, c_void_p, c_int, c_int, c_void_p]
+        L.speo_oracle_mlp_loss_grad.argtypes = [c_void_p, c_int, c_int, c_float, c_void_p, c_int, c_int, c_void_p,
+                                                c_void_p]
+        L.speo_oracle_mlp_loss_grad.restype = c_double
+        L.speo_oracle_adam.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float, c_float, c_float,
+                                       c_float, c_int]
         _lib = L
     return _lib
 
@@ -209,3 +216,30 @@ def ref_lib():
         L.ref_cec_eval_batch.argtypes = [c_void_p, c_int, c_int, c_void_p]
         _ref = L
     return _ref
+
+
+# ---- surrogate MLP ------------------------------------------------------------------------------
+def mlp_nparams(din, h):
+    return lib().speo_oracle_mlp_nparams(din, h)
+
+
+def mlp_forward(theta, din, h, in_scale, X):
+    theta = np.ascontiguousarray(theta, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    y = np.zeros(X.shape[0], dtype=np.float64)
+    lib().speo_oracle_mlp_forward(_p(theta), din, h, in_scale, _p(X), X.shape[0], X.shape[1], _p(y))
+    return y
+
+
+def mlp_loss_grad(theta, din, h, in_scale, X, t):
+    theta = np.ascontiguousarray(theta, dtype=np.float32)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    t = np.ascontiguousarray(t, dtype=np.float32)
+    g = np.zeros(mlp_nparams(din, h), dtype=np.float64)
+    loss = lib().speo_oracle_mlp_loss_grad(_p(theta), din, h, in_scale, _p(X), X.shape[0], X.shape[1], _p(t), _p(g))
+    return loss, g
+
+
+def adam(theta, m, v, g, lr, beta1, beta2, eps, step):
+    g = np.ascontiguousarray(g, dtype=np.float32)
+    lib().speo_oracle_adam(_p(theta), _p(m), _p(v), _p(g), len(theta), lr, beta1, beta2, eps, step)

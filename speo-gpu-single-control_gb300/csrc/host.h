@@ -36,3 +36,4 @@ extern "C" unsigned int speo_deverr_objective(void);
 extern "C" unsigned int speo_deverr_generation(void);
 extern "C" unsigned int speo_deverr_tc(void);
 extern "C" unsigned int speo_deverr_resident(void);
+extern "C" unsigned int speo_deverr_surrogate(void);

@@ -103,6 +103,18 @@ SIGNATURES: dict[str, tuple] = {
                                       c_void_p, c_int, c_void_p]),
     "speo_ring_migrate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "speo_ring_migrate_noalloc": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p]),
+    "speo_surrogate_create": (c_int, [c_void_p, c_int, c_int, ctypes.c_longlong, c_int, c_float, c_float, c_uint64]),
+    "speo_surrogate_destroy": (c_int, [c_void_p]),
+    "speo_surrogate_params": (c_int, [c_void_p, c_void_p, c_void_p, POINTER(c_int)]),
+    "speo_surrogate_forward": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p]),
+    "speo_surrogate_grad": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, POINTER(c_float), c_void_p]),
+    "speo_surrogate_adam_step": (c_int, [c_void_p, c_void_p]),
+    "speo_surrogate_archive_append": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p]),
+    "speo_surrogate_train": (c_int, [c_void_p, c_int, POINTER(c_float), c_void_p]),
+    "speo_make_trials": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                 c_void_p]),
+    "speo_surrogate_generation": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, ctypes.c_longlong, c_int,
+                                          c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "speo_best_reeval_f64": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 

@@ -196,3 +196,22 @@ def test_cpu_baseline_loop_improves(oracle):
                                    threads=2)
     assert evals == 60 * n * P
     assert fit.min() < f0 * 1e-2
+
+
+def test_mlp_gradient_matches_finite_differences(oracle):
+    """The oracle's analytic MLP gradient against central differences (FP64)."""
+    din, h, scale = 5, 7, 0.01
+    rng = np.random.default_rng(0)
+    theta = rng.normal(0, 0.5, oracle.mlp_nparams(din, h)).astype(np.float32)
+    X = rng.uniform(-100, 100, (9, din)).astype(np.float32)
+    t = rng.normal(0, 1, 9).astype(np.float32)
+    loss, g = oracle.mlp_loss_grad(theta, din, h, scale, X, t)
+    eps = 1e-3
+    for i in rng.choice(len(theta), 25, replace=False):
+        tp, tm = theta.copy(), theta.copy()
+        tp[i] += eps
+        tm[i] -= eps
+        lp = np.mean((oracle.mlp_forward(tp, din, h, scale, X) - t) ** 2)
+        lm = np.mean((oracle.mlp_forward(tm, din, h, scale, X) - t) ** 2)
+        fd = (lp - lm) / (float(tp[i]) - float(tm[i]))
+        assert fd == pytest.approx(g[i], rel=2e-3, abs=1e-5)
