@@ -13,63 +13,49 @@ pytestmark = pytest.mark.gpu
 DIN, H, SCALE = 50, 256, 0.01
 
 
+def _cu():
+    return ctypes.CDLL("libcuda.so.1")
+
+
+def dev_to_np(ptr, n):
+    """float32[n] from a device pointer owned by the library (driver API copy, synchronous)."""
+    out = np.empty(n, dtype=np.float32)
+    cu = _cu()
+    assert cu.cuCtxSynchronize() == 0
+    assert cu.cuMemcpyDtoH_v2(ctypes.c_void_p(out.ctypes.data), ctypes.c_uint64(ptr), ctypes.c_size_t(4 * n)) == 0
+    return out
+
+
+def np_to_dev(ptr, arr):
+    arr = np.ascontiguousarray(arr, dtype=np.float32)
+    cu = _cu()
+    assert cu.cuCtxSynchronize() == 0
+    assert cu.cuMemcpyHtoD_v2(ctypes.c_uint64(ptr), ctypes.c_void_p(arr.ctypes.data), ctypes.c_size_t(4 * arr.size)) == 0
+
+
 class Surr:
+    """An speo_surrogate object and raw views of its parameter and gradient buffers."""
+
     def __init__(self, lib, din=DIN, h=H, cap=1 << 16, batch=4096, lr=1e-3, seed=5):
         from speo_gb300 import _lib
 
-        self.lib, self._lib = lib, _lib
+        self.lib = lib
         self.p = ctypes.c_void_p()
         _lib.check(lib.speo_surrogate_create(ctypes.byref(self.p), din, h, cap, batch, lr, SCALE, seed),
                    "speo_surrogate_create")
         th, gr, n = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_int()
-        lib.speo_surrogate_params(self.p, ctypes.byref(th), ctypes.byref(gr), ctypes.byref(n))
+        _lib.check(lib.speo_surrogate_params(self.p, ctypes.byref(th), ctypes.byref(gr), ctypes.byref(n)), "params")
         self.theta_ptr, self.grad_ptr, self.n = th.value, gr.value, n.value
         self.din, self.h = din, h
 
     def theta(self):
-        import torch
+        return dev_to_np(self.theta_ptr, self.n)
 
-        buf = (ctypes.c_float * self.n)()
-        torch.cuda.synchronize()
-        from speo_gb300 import _lib as L  # noqa: F401
-        import ctypes as C
-
-        cudart = torch.cuda  # noqa: F841
-        t = torch.empty(self.n, dtype=torch.float32, device="cuda")
-        # copy device -> tensor through a raw pointer view
-        src = torch.cuda.FloatTensor  # noqa: F841
-        ctypes.memmove(ctypes.addressof(buf), 0, 0)
-        return self._dev_to_np(self.theta_ptr)
-
-    def _dev_to_np(self, ptr):
-        import torch
-
-        out = torch.empty(self.n, dtype=torch.float32)
-        dev = torch.empty(self.n, dtype=torch.float32, device="cuda")
-        # view the library's buffer by copying it into a tensor with cudaMemcpy via torch's storage
-        cuda = ctypes.CDLL("libcudart.so") if False else None  # noqa: F841
-        self.lib.speo_surrogate_params  # keep the library alive
-        _copy_dev(dev.data_ptr(), ptr, self.n * 4)
-        out.copy_(dev.cpu())
-        return out.numpy().copy()
+    def grad(self):
+        return dev_to_np(self.grad_ptr, self.n)
 
     def close(self):
         self.lib.speo_surrogate_destroy(self.p)
-
-
-def _copy_dev(dst, src, nbytes):
-    """Device-to-device copy between raw pointers, through the CUDA driver."""
-    cu = ctypes.CDLL("libcuda.so.1")
-    r = cu.cuMemcpyDtoD_v2(ctypes.c_uint64(dst), ctypes.c_uint64(src), ctypes.c_size_t(nbytes))
-    assert r == 0, r
-    cu.cuCtxSynchronize()
-
-
-def _to_dev_ptr(dst_ptr, arr):
-    import torch
-
-    t = torch.from_numpy(np.ascontiguousarray(arr, dtype=np.float32)).cuda()
-    _copy_dev(dst_ptr, t.data_ptr(), arr.size * 4)
 
 
 def test_forward_matches_oracle(lib, oracle, cuda):
@@ -77,7 +63,7 @@ def test_forward_matches_oracle(lib, oracle, cuda):
 
     s = Surr(lib)
     try:
-        theta = s._dev_to_np(s.theta_ptr)
+        theta = s.theta()
         rng = np.random.default_rng(1)
         X = np.zeros((300, 52), dtype=np.float32)
         X[:, :DIN] = rng.uniform(-100, 100, (300, DIN))
@@ -98,7 +84,7 @@ def test_gradients_match_oracle(lib, oracle, cuda):
 
     s = Surr(lib, batch=128)
     try:
-        theta = s._dev_to_np(s.theta_ptr)
+        theta = s.theta()
         rng = np.random.default_rng(2)
         n = 96
         X = np.zeros((n, 52), dtype=np.float32)
@@ -107,7 +93,7 @@ def test_gradients_match_oracle(lib, oracle, cuda):
         tX, tt = torch.from_numpy(X).cuda(), torch.from_numpy(t).cuda()
         loss = ctypes.c_float()
         _lib.check(lib.speo_surrogate_grad(s.p, tX.data_ptr(), n, 52, tt.data_ptr(), ctypes.byref(loss), None), "grad")
-        g = s._dev_to_np(s.grad_ptr)
+        g = s.grad()
         ref_loss, ref = oracle.mlp_loss_grad(theta, DIN, H, SCALE, X[:, :DIN], t)
         assert loss.value == pytest.approx(ref_loss, rel=1e-4)
         # per parameter block: |g - ref| <= 1e-3 * max|ref in block| + 1e-7
@@ -127,15 +113,15 @@ def test_adam_matches_oracle(lib, oracle, cuda):
     s = Surr(lib, din=8, h=16, lr=1e-3)
     try:
         rng = np.random.default_rng(3)
-        theta = s._dev_to_np(s.theta_ptr)
+        theta = s.theta()
         m = np.zeros_like(theta)
         v = np.zeros_like(theta)
         for step in range(1, 4):
             g = rng.normal(0, 1, s.n).astype(np.float32)
-            _to_dev_ptr(s.grad_ptr, g)
+            np_to_dev(s.grad_ptr, g)
             _lib.check(lib.speo_surrogate_adam_step(s.p, None), "adam")
             oracle.adam(theta, m, v, g, 1e-3, 0.9, 0.999, 1e-8, step)
-        got = s._dev_to_np(s.theta_ptr)
+        got = s.theta()
         np.testing.assert_allclose(got, theta, rtol=2e-6, atol=1e-7)
     finally:
         s.close()
