@@ -288,6 +288,11 @@ SPEO_API int speo_surrogate_forward(speo_surrogate *s, const float *X, int n, in
 SPEO_API int speo_surrogate_grad(speo_surrogate *s, const float *X, int n, int ldx, const float *T,
                                  float *loss_out, void *stream);
 SPEO_API int speo_surrogate_adam_step(speo_surrogate *s, void *stream);
+/* Standardise the MLP's inputs by the per-dimension mean and standard deviation of `rows` rows of
+ * pop (stride ld) from now on (until then x' = x * in_scale). speo_surrogate_generation calls it
+ * with its parents every generation, so the network sees the population's region at unit scale. */
+SPEO_API int speo_surrogate_standardize(speo_surrogate *s, const float *pop, long long rows, int ld,
+                                        void *stream);
 SPEO_API int speo_surrogate_archive_append(speo_surrogate *s, const float *X, int n, int ldx, const float *f,
                                            void *stream);
 SPEO_API int speo_surrogate_train(speo_surrogate *s, int steps, float *loss_out, void *stream);
@@ -297,13 +302,15 @@ SPEO_API int speo_make_trials(const speo_segment *d_segs, const speo_work_item *
                               int dim_hi, int k, const float *pop, const float *fit, float *T,
                               const uint32_t *d_gen, void *stream);
 /* One screened generation over a flat population (rows x ld): k trials per target, the MLP
- * picks one, exact evaluation, strict-`<` selection into (pop_out, fit_out), archive append,
+ * picks one (an `explore` fraction of targets, chosen by Philox, takes a uniformly drawn trial
+ * instead, so the archive also holds unbiased labels), exact evaluation, strict-`<` selection
+ * into (pop_out, fit_out), archive append (the first call also archives the parents),
  * `train_steps` Adam steps; *d_gen advances by one. */
 SPEO_API int speo_surrogate_generation(speo_surrogate *s, const speo_segment *d_segs,
                                        const speo_work_item *d_items, int n_items, int dim_lo, int dim_hi,
                                        long long rows, int ld, int k, const float *pop_in,
                                        const float *fit_in, float *pop_out, float *fit_out,
-                                       uint32_t *d_gen, int train_steps, void *stream);
+                                       uint32_t *d_gen, int train_steps, float explore, void *stream);
 
 /* Per segment: argmin of fit (ties: lowest row) -> best_row[s]; FP64 re-evaluation of that
  * row -> best_err[s] = f(x) - f* in double. */

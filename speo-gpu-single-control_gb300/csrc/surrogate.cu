@@ -283,7 +283,14 @@ __global__ void __launch_bounds__(256) k_make_trials(const speo_segment *segs, c
 }
 
 // Per row: the trial with the lowest prediction (NaN as +inf, ties lowest trial) -> sel row.
-__global__ void k_pick(const float *T, const float *pred, int k, float *sel, long long rows, int ld, int max_dim)
+// An `explore` fraction of rows instead takes a uniformly drawn trial: those exact evaluations are
+// an unbiased sample of the trial distribution, which keeps the archive from holding only the
+// points the model under-predicts. Draw for row r at generation g:
+// u = u01(philox({0, r, g, PICK}, key)[0]); explore if u < explore, trial = word 1 mod k.
+constexpr uint32_t kTagPick = 5u;
+
+__global__ void k_pick(const float *T, const float *pred, int k, float *sel, long long rows, int ld, int max_dim,
+                       float explore, uint2 key, const uint32_t *gen_ctr)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int nch = (max_dim + 3) >> 2;
@@ -291,10 +298,15 @@ __global__ void k_pick(const float *T, const float *pred, int k, float *sel, lon
     const long long row = t / nch;
     const int c = (int)(t - row * nch);
     int bt = 0;
-    float bp = rank_key(pred[row * k]);
-    for (int q = 1; q < k; ++q) {
-        const float v = rank_key(pred[row * k + q]);
-        if (v < bp) { bp = v; bt = q; }
+    const uint4 w = philox(make_uint4(0u, (uint32_t)row, *gen_ctr, kTagPick), key);
+    if (u01(w.x) < explore) {
+        bt = (int)(w.y % (uint32_t)k);
+    } else {
+        float bp = rank_key(pred[row * k]);
+        for (int q = 1; q < k; ++q) {
+            const float v = rank_key(pred[row * k + q]);
+            if (v < bp) { bp = v; bt = q; }
+        }
     }
     if (4 * c < ld)
         *reinterpret_cast<float4 *>(sel + row * ld + 4 * c) =
@@ -318,6 +330,45 @@ __global__ void k_select_flat(const float *pop_in, const float *fit_in, const fl
 
 __global__ void k_advance_gen(uint32_t *gen, uint32_t n) { gen[0] += n; }
 
+// Per input dimension d: mean and 1/std over `rows` rows of pop (stride ld), FP64 sums; one block
+// per dimension. The MLP then sees the population's region at unit scale.
+__global__ void k_input_stats(const float *pop, long long rows, int ld, int din, float *mu, float *isig)
+{
+    __shared__ double s1[256], s2[256];
+    const int d = blockIdx.x;
+    double a = 0.0, b = 0.0;
+    for (long long i = threadIdx.x; i < rows; i += blockDim.x) {
+        const double x = pop[i * ld + d];
+        a += x;
+        b += x * x;
+    }
+    s1[threadIdx.x] = a;
+    s2[threadIdx.x] = b;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) { s1[threadIdx.x] += s1[threadIdx.x + o]; s2[threadIdx.x] += s2[threadIdx.x + o]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double m = s1[0] / (double)rows;
+        const double var = fmax(s2[0] / (double)rows - m * m, 0.0);
+        mu[d] = (float)m;
+        isig[d] = (float)(1.0 / (sqrt(var) + 1e-6));
+        (void)din;
+    }
+}
+
+// Y[i][d] = (X[i][d] - mu[d]) * isig[d] for d < din (zero in the padding up to ldy).
+__global__ void k_normalize(const float *X, int ldx, long long n, int din, const float *mu, const float *isig, float *Y,
+                            int ldy)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * ldy) return;
+    const long long i = t / ldy;
+    const int d = (int)(t - i * ldy);
+    Y[t] = d < din ? (X[i * ldx + d] - mu[d]) * isig[d] : 0.f;
+}
+
 }  // namespace
 
 // ---- host object --------------------------------------------------------------------------------
@@ -332,6 +383,10 @@ struct Surrogate {
     float *Xb = nullptr, *Tb = nullptr;       // training batch
     float *Z1 = nullptr, *H1 = nullptr, *Z2 = nullptr, *H2 = nullptr, *yb = nullptr, *dy = nullptr;
     float *dZ2 = nullptr, *dZ1 = nullptr, *loss = nullptr, *one = nullptr;
+    float *mu = nullptr, *isig = nullptr;     // input standardisation (default: 0 and in_scale)
+    float *Xbn = nullptr;                     // standardised training batch
+    long long nrm_rows = 0;
+    float *Xn = nullptr;                      // standardised screening inputs
     // screening scratch (grown on demand)
     long long scr_rows = 0;
     float *sH1 = nullptr, *sH2 = nullptr;
@@ -348,20 +403,32 @@ struct Surrogate {
 
 namespace {
 
+// Inputs standardised into `Xn` (n x lda) first: x' = (x - mu) * isig.
+int standardise(Surrogate *S, cudaStream_t st, const float *X, int n, int ldx, float *Xn)
+{
+    const long long total = (long long)n * S->lda;
+    k_normalize<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(X, ldx, n, S->din, S->mu, S->isig, Xn, S->lda);
+    return check_launch("k_normalize");
+}
+
+// Forward on standardised inputs Xn (stride lda).
 int mlp_forward(Surrogate *S, cudaStream_t st, const float *X, int n, int ldx, float *y, float *Z1, float *H1, float *Z2,
                 float *H2)
 {
     const int h = S->h;
-    if (int e = gemm<1>(st, X, ldx, 1, S->W1(), 1, S->din, S->b1(), H1, h, Z1, n, h, S->din, S->in_scale)) return e;
+    if (int e = gemm<1>(st, X, ldx, 1, S->W1(), 1, S->din, S->b1(), H1, h, Z1, n, h, S->din, 1.f)) return e;
     if (int e = gemm<1>(st, H1, h, 1, S->W2(), 1, h, S->b2(), H2, h, Z2, n, h, h, 1.f)) return e;
     k_head<<<(n + 7) / 8, 256, 0, st>>>(H2, h, S->w3(), S->b3(), y, n);
     return check_launch("k_head");
 }
 
-// Gradient of the mean squared error over the batch (Xb, Tb) into S->grad; loss into S->loss.
-int mlp_grad(Surrogate *S, cudaStream_t st, const float *X, int n, int ldx, const float *T)
+// Gradient of the mean squared error over the batch (X raw, T) into S->grad; loss into S->loss.
+int mlp_grad(Surrogate *S, cudaStream_t st, const float *Xraw, int n, int ldxraw, const float *T)
 {
     const int h = S->h, din = S->din;
+    if (int e = standardise(S, st, Xraw, n, ldxraw, S->Xbn)) return e;
+    const float *X = S->Xbn;
+    const int ldx = S->lda;
     if (int e = mlp_forward(S, st, X, n, ldx, S->yb, S->Z1, S->H1, S->Z2, S->H2)) return e;
     if (int e = check_cuda(cudaMemsetAsync(S->loss, 0, sizeof(float), st), "memset loss")) return e;
     k_mse<<<(n + 255) / 256, 256, 0, st>>>(S->yb, T, n, S->dy, S->loss);
@@ -376,8 +443,8 @@ int mlp_grad(Surrogate *S, cudaStream_t st, const float *X, int n, int ldx, cons
     if (int e = gemm<0>(st, S->dZ2, 1, h, S->H1, h, 1, nullptr, gW2, h, nullptr, h, h, n, 1.f)) return e;
     if (int e = gemm<0>(st, S->one, 0, 0, S->dZ2, h, 1, nullptr, gb2, h, nullptr, 1, h, n, 1.f)) return e;
     if (int e = gemm<2>(st, S->dZ2, h, 1, S->W2(), h, 1, nullptr, S->dZ1, h, S->Z1, n, h, h, 1.f)) return e;
-    // layer 1: gW1 = dZ1^T (s X), gb1 = 1^T dZ1
-    if (int e = gemm<0>(st, S->dZ1, 1, h, X, ldx, 1, nullptr, gW1, din, nullptr, h, din, n, S->in_scale)) return e;
+    // layer 1: gW1 = dZ1^T X', gb1 = 1^T dZ1 (X' standardised)
+    if (int e = gemm<0>(st, S->dZ1, 1, h, X, ldx, 1, nullptr, gW1, din, nullptr, h, din, n, 1.f)) return e;
     return gemm<0>(st, S->one, 0, 0, S->dZ1, h, 1, nullptr, gb1, h, nullptr, 1, h, n, 1.f);
 }
 
@@ -416,6 +483,9 @@ extern "C" int speo_surrogate_create(speo_surrogate **out, int din, int hidden, 
     e = e ? e : dalloc(&S->dy, (size_t)batch);
     e = e ? e : dalloc(&S->loss, 1);
     e = e ? e : dalloc(&S->one, 1);
+    e = e ? e : dalloc(&S->mu, (size_t)S->lda);
+    e = e ? e : dalloc(&S->isig, (size_t)S->lda);
+    e = e ? e : dalloc(&S->Xbn, (size_t)batch * S->lda);
     if (e) { speo_surrogate_destroy(reinterpret_cast<speo_surrogate *>(S)); return e; }
     // He-style initialisation from Philox on the host side of the stream: uniform(-a, a)
     float *h_theta = new float[S->np];
@@ -442,6 +512,14 @@ extern "C" int speo_surrogate_create(speo_surrogate **out, int din, int hidden, 
     e = e ? e : check_cuda(cudaMemset(S->m, 0, sizeof(float) * S->np), "memset m");
     e = e ? e : check_cuda(cudaMemset(S->v, 0, sizeof(float) * S->np), "memset v");
     e = e ? e : check_cuda(cudaMemcpy(S->one, &one, sizeof(float), cudaMemcpyHostToDevice), "one");
+    {   // default standardisation: x' = x * in_scale
+        float *h_mu = new float[S->lda], *h_is = new float[S->lda];
+        for (int d = 0; d < S->lda; ++d) { h_mu[d] = 0.f; h_is[d] = in_scale; }
+        e = e ? e : check_cuda(cudaMemcpy(S->mu, h_mu, sizeof(float) * S->lda, cudaMemcpyHostToDevice), "mu");
+        e = e ? e : check_cuda(cudaMemcpy(S->isig, h_is, sizeof(float) * S->lda, cudaMemcpyHostToDevice), "isig");
+        delete[] h_mu;
+        delete[] h_is;
+    }
     if (e) { speo_surrogate_destroy(reinterpret_cast<speo_surrogate *>(S)); return e; }
     *out = reinterpret_cast<speo_surrogate *>(S);
     return SPEO_OK;
@@ -452,7 +530,8 @@ extern "C" int speo_surrogate_destroy(speo_surrogate *sp)
     Surrogate *S = reinterpret_cast<Surrogate *>(sp);
     if (!S) return SPEO_OK;
     for (float *p : {S->theta, S->m, S->v, S->grad, S->AX, S->AT, S->Xb, S->Tb, S->Z1, S->H1, S->Z2, S->H2, S->yb,
-                     S->dy, S->dZ2, S->dZ1, S->loss, S->one, S->sH1, S->sH2, S->T, S->pred, S->sel, S->fsel})
+                     S->dy, S->dZ2, S->dZ1, S->loss, S->one, S->sH1, S->sH2, S->T, S->pred, S->sel, S->fsel, S->mu,
+                     S->isig, S->Xbn, S->Xn})
         if (p) cudaFree(p);
     delete S;
     return SPEO_OK;
@@ -482,7 +561,26 @@ extern "C" int speo_surrogate_forward(speo_surrogate *sp, const float *X, int n,
         if (int e = dalloc(&S->sH2, (size_t)n * S->h)) return e;
         S->scr_rows = n;
     }
-    return mlp_forward(S, static_cast<cudaStream_t>(stream), X, n, ldx, y, nullptr, S->sH1, nullptr, S->sH2);
+    if (S->nrm_rows < n) {
+        if (S->Xn) cudaFree(S->Xn);
+        S->Xn = nullptr;
+        S->nrm_rows = 0;
+        if (int e = dalloc(&S->Xn, (size_t)n * S->lda)) return e;
+        S->nrm_rows = n;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (int e = standardise(S, st, X, n, ldx, S->Xn)) return e;
+    return mlp_forward(S, st, S->Xn, n, S->lda, y, nullptr, S->sH1, nullptr, S->sH2);
+}
+
+// Standardise the MLP's inputs by the per-dimension mean and standard deviation of `rows` rows of
+// pop (stride ld); later forward passes and training batches use these statistics.
+extern "C" int speo_surrogate_standardize(speo_surrogate *sp, const float *pop, long long rows, int ld, void *stream)
+{
+    Surrogate *S = reinterpret_cast<Surrogate *>(sp);
+    if (!S || !pop || rows < 1 || ld < S->din) return fail(SPEO_ERR_INVALID_ARG, "speo_surrogate_standardize: bad arguments");
+    k_input_stats<<<S->din, 256, 0, static_cast<cudaStream_t>(stream)>>>(pop, rows, ld, S->din, S->mu, S->isig);
+    return check_launch("k_input_stats");
 }
 
 extern "C" int speo_surrogate_grad(speo_surrogate *sp, const float *X, int n, int ldx, const float *T, float *loss_out,
@@ -576,7 +674,7 @@ extern "C" int speo_make_trials(const speo_segment *segs, const speo_work_item *
 extern "C" int speo_surrogate_generation(speo_surrogate *sp, const speo_segment *segs, const speo_work_item *items,
                                          int n_items, int dim_lo, int dim_hi, long long rows, int ld, int k,
                                          const float *pop_in, const float *fit_in, float *pop_out, float *fit_out,
-                                         uint32_t *d_gen, int train_steps, void *stream)
+                                         uint32_t *d_gen, int train_steps, float explore, void *stream)
 {
     Surrogate *S = reinterpret_cast<Surrogate *>(sp);
     if (!S || !segs || !items || !pop_in || !fit_in || !pop_out || !fit_out || !d_gen || rows < 1 || k < 1 ||
@@ -596,10 +694,16 @@ extern "C" int speo_surrogate_generation(speo_surrogate *sp, const speo_segment 
         if (int e = check_cuda(cudaMemsetAsync(S->sel, 0, sizeof(float) * (size_t)rows * ld, st), "memset sel")) return e;
         S->trial_cap = rows * k;
     }
+    if (S->count == 0) {  // first screened generation: the exact-evaluated parents seed the archive
+        if (int e = speo_surrogate_archive_append(sp, pop_in, (int)rows, ld, fit_in, stream)) return e;
+    }
+    if (int e = speo_surrogate_standardize(sp, pop_in, rows, ld, stream)) return e;
     if (int e = speo_make_trials(segs, items, n_items, dim_hi, k, pop_in, fit_in, S->T, d_gen, stream)) return e;
     if (int e = speo_surrogate_forward(sp, S->T, (int)(rows * k), ld, S->pred, stream)) return e;
     const int nch = (dim_hi + 3) / 4;
-    k_pick<<<(unsigned)((rows * nch + 255) / 256), 256, 0, st>>>(S->T, S->pred, k, S->sel, rows, ld, dim_hi);
+    k_pick<<<(unsigned)((rows * nch + 255) / 256), 256, 0, st>>>(
+        S->T, S->pred, k, S->sel, rows, ld, dim_hi, explore, make_uint2((uint32_t)S->seed, (uint32_t)(S->seed >> 32)),
+        d_gen);
     if (int e = check_launch("k_pick")) return e;
     if (int e = speo_evaluate(segs, items, n_items, dim_lo, dim_hi, S->sel, S->fsel, stream)) return e;
     const int nchl = ld / 4;

@@ -109,12 +109,14 @@ SIGNATURES: dict[str, tuple] = {
     "speo_surrogate_forward": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p]),
     "speo_surrogate_grad": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, POINTER(c_float), c_void_p]),
     "speo_surrogate_adam_step": (c_int, [c_void_p, c_void_p]),
+    "speo_surrogate_standardize": (c_int, [c_void_p, c_void_p, ctypes.c_longlong, c_int, c_void_p]),
     "speo_surrogate_archive_append": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p]),
     "speo_surrogate_train": (c_int, [c_void_p, c_int, POINTER(c_float), c_void_p]),
     "speo_make_trials": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_void_p]),
     "speo_surrogate_generation": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, ctypes.c_longlong, c_int,
-                                          c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+                                          c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float,
+                                          c_void_p]),
     "speo_best_reeval_f64": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 

@@ -192,12 +192,15 @@ def test_training_reduces_loss(lib, cuda):
 
 
 def _run(lib, cuda, use_surrogate, gens, seed, D=10, n_isl=8, P=64, k=8, func=31):
+    """Best FP64 error after `gens` generations of n_isl x P islands (ring migration every 25).
+    Screened runs: MLP D -> 64 -> 64 -> 1, archive of the last 8 generations, 32 Adam steps
+    (lr 3e-3, batch 1024) per generation, 25 % of targets take a random trial."""
     import torch
     from speo_gb300 import _lib
 
     tab = _islands(cuda, n_isl, P, D, func=func, seed=seed)
     tab.init_population()
-    s = Surr(lib, din=D, h=64, cap=1 << 16, batch=1024, lr=2e-3, seed=seed) if use_surrogate else None
+    s = Surr(lib, din=D, h=64, cap=8 * n_isl * P, batch=1024, lr=3e-3, seed=seed) if use_surrogate else None
     try:
         for g in range(gens):
             if use_surrogate:
@@ -206,7 +209,7 @@ def _run(lib, cuda, use_surrogate, gens, seed, D=10, n_isl=8, P=64, k=8, func=31
                                                          tab.n_items, tab.dim_lo, tab.dim_hi, tab.rows, tab.ld, k,
                                                          tab.pop[a].data_ptr(), tab.fit[a].data_ptr(),
                                                          tab.pop[b].data_ptr(), tab.fit[b].data_ptr(),
-                                                         tab.gen.data_ptr(), 4, None), "surrogate generation")
+                                                         tab.gen.data_ptr(), 32, 0.25, None), "surrogate generation")
                 tab.cur = b
             else:
                 tab.generation()
@@ -222,9 +225,9 @@ def _run(lib, cuda, use_surrogate, gens, seed, D=10, n_isl=8, P=64, k=8, func=31
 
 def test_surrogate_beats_plain_de_at_equal_exact_evaluations(lib, cuda):
     """Rotated sphere, D = 10, 8 islands x 64: both variants spend exactly 512 exact evaluations
-    per generation; after the same number of generations the screened run must be clearly ahead
+    per generation; after the same number of generations the screened run must be far ahead
     (median over seeds). The rotated Rastrigin figures are printed for information."""
-    gens = 150
+    gens = 100
     ratios = []
     for seed in (21, 22, 23):
         plain = _run(lib, cuda, False, gens, seed)
@@ -234,4 +237,4 @@ def test_surrogate_beats_plain_de_at_equal_exact_evaluations(lib, cuda):
     for seed in (21,):
         print(f"rastrigin seed {seed}: plain {_run(lib, cuda, False, gens, seed, func=9):.3e}, "
               f"screened {_run(lib, cuda, True, gens, seed, func=9):.3e}")
-    assert np.median(ratios) > 3.0, ratios
+    assert np.median(ratios) > 10.0, ratios
