@@ -249,6 +249,10 @@ def bench_speo(args) -> dict:
     }
     if not args.no_ops:
         out["operators_bandwidth_scale"] = bench_operators(L, dev, torch, pk)
+    if not args.no_configs:
+        out["config2_precision"] = bench_config2(L, dev, torch, flush)
+        out["config3_batched"] = bench_config3(L, dev, torch, flush)
+        out["config4_surrogate_vs_plain"] = bench_config4(L, dev, torch, args.c4_gens)
     if not args.no_e2e:
         out["e2e"] = bench_e2e(L, dev, torch, args)
     if rank == 0 and not args.no_cpu:
@@ -347,6 +351,135 @@ def bench_operators(L, dev, torch, pk, n_isl: int = 16384) -> dict:
     _lib.check(L.API_CheckCUDAError(), "operators")
     del tab, tab_tc, pop, cand
     torch.cuda.empty_cache()
+    return out
+
+
+def bench_config2(L, dev, torch, flush) -> dict:
+    """Config 2: 256 islands x 128, D = 100, mixed objectives; the rotation runs on the tcgen05
+    tensor cores in BF16x3 (trial generation, tensor-core evaluation and selection per generation,
+    20 generations per CUDA graph). Precision: tensor-core and CUDA-core FP32 fitness of 4096
+    sampled rows against the FP64 oracle; FP64 re-evaluation of every island's best."""
+    import speo_oracle
+    from speo_gb300 import _lib
+    from speo_gb300 import workloads as w
+
+    specs, inst = w.config2_specs(256)
+    tab = w.table(specs, inst, device=dev, tile_rows=_lib.TILE_TC)
+    tab.init_population()
+    trial = torch.zeros(tab.rows, tab.ld, device=dev)
+    tfit = torch.zeros(tab.rows, device=dev)
+    G = 20
+    g = capture(torch, lambda: [tab.tc_generation(trial, tfit) for _ in range(G)])
+    for _ in range(2):
+        g.replay()
+    ms = time_graph(torch, g, 5, flush) / G
+    fit_tc = torch.empty(tab.rows, device=dev)
+    fit_cc = torch.empty(tab.rows, device=dev)
+    tab.evaluate(use_tc=True, out=fit_tc)
+    tab.evaluate(out=fit_cc)
+    torch.cuda.synchronize()
+    pop = tab.pop[tab.cur].cpu().numpy()
+    rng = np.random.default_rng(2)
+    sample = rng.choice(tab.rows, 4096, replace=False)
+    ref = np.empty(len(sample))
+    owner = np.repeat(np.arange(len(specs)), [sp.pop_size for sp in specs])
+    for j, r in enumerate(sample):
+        sp = specs[owner[r]]
+        o, M = inst[sp.instance]
+        ref[j] = speo_oracle.evaluate_rows(sp.func_id, pop[r:r + 1], sp.dim, o, M)[0]
+    rel_tc = np.abs(fit_tc.cpu().numpy()[sample] - ref) / np.maximum(np.abs(ref), 1e-30)
+    rel_cc = np.abs(fit_cc.cpu().numpy()[sample] - ref) / np.maximum(np.abs(ref), 1e-30)
+    rows, errs = tab.best_f64()
+    return {"workload": "256 islands x P=128, D=100, per island rotated sphere or rotated Rastrigin (seeded), "
+                        "BF16x3 tcgen05 evaluation",
+            "ms_per_generation": ms, "gens_per_s": 1e3 / ms, "evals_per_s": tab.rows / (ms / 1e3),
+            "launches_per_generation": 3,
+            "fitness_rel_err_vs_fp64": {"tcgen05_bf16x3": {"max": float(rel_tc.max()), "median": float(np.median(rel_tc)),
+                                                           "p99": float(np.quantile(rel_tc, 0.99))},
+                                        "cuda_core_fp32": {"max": float(rel_cc.max()), "median": float(np.median(rel_cc)),
+                                                           "p99": float(np.quantile(rel_cc, 0.99))},
+                                        "rows_sampled": int(len(sample))},
+            "best_error_f64_min_over_islands": float(errs.min().item())}
+
+
+def bench_config3(L, dev, torch, flush) -> dict:
+    """Config 3: 1024 independent runs with D ~ U{10,30,50,100}, P ~ U[50,200], each with its own
+    instance and objective; one launch per generation (the mixed-class kernel), 20 generations per
+    CUDA graph. The tile size is tuned by measurement over the candidates."""
+    from speo_gb300 import workloads as w
+
+    specs, inst = w.config3_specs(1024)
+    evals = sum(sp.pop_size for sp in specs)
+    tuned = {}
+    for tile in (32, 48, 64):
+        tab = w.table(specs, inst, device=dev, tile_rows=tile)
+        tab.init_population()
+        g = capture(torch, lambda: [tab.generation() for _ in range(20)])
+        g.replay()
+        tuned[tile] = time_graph(torch, g, 5, flush) / 20
+    best = min(tuned, key=tuned.get)
+    ms = tuned[best]
+    return {"workload": f"1024 runs, D in {{10,30,50,100}}, P in [50,200] ({evals} rows), mixed objectives",
+            "ms_per_generation": ms, "gens_per_s": 1e3 / ms, "evals_per_s": evals / (ms / 1e3),
+            "launches_per_generation": 1, "autotune_tile_rows_ms": {str(k): v for k, v in tuned.items()},
+            "tile_rows": best}
+
+
+def bench_config4(L, dev, torch, gens: int) -> dict:
+    """Config 4: 128 islands x 256, D = 50, rotated Rastrigin. Plain DE against the surrogate-
+    screened DE (MLP 50-256-256-1, archive 2^20, Adam lr 1e-3, batch 4096, k = 8 trials per
+    target, 16 Adam steps per generation, 25 % exploration picks); ring migration of 5 every 50
+    generations in both. Both spend 32768 exact evaluations per generation. Best FP64 error every
+    10 generations; wall time from CUDA events around the generations only."""
+    import ctypes as C
+
+    from speo_gb300 import _lib
+    from speo_gb300 import workloads as w
+
+    specs, inst = w.config4_specs()
+    out = {"workload": "128 islands x P=256, D=50, rotated Rastrigin; surrogate MLP 50-256-256-1", "generations": gens}
+    for mode in ("plain", "surrogate"):
+        tab = w.table(specs, inst, device=dev)
+        tab.init_population()
+        surr = None
+        if mode == "surrogate":
+            surr = C.c_void_p()
+            _lib.check(L.speo_surrogate_create(C.byref(surr), 50, 256, 1 << 20, 4096, 1e-3, 0.01, 4242),
+                       "speo_surrogate_create")
+        curve, t_total = [], 0.0
+        try:
+            for g0 in range(0, gens, 10):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                for g in range(g0, g0 + 10):
+                    if mode == "plain":
+                        if tab.epoch_fits():
+                            tab.epoch(1)
+                        else:
+                            tab.generation()
+                    else:
+                        tab.surrogate_generation(surr, k=8, train_steps=16, explore=0.25)
+                    if (g + 1) % 50 == 0:
+                        tab.migrate(5)
+                b.record()
+                torch.cuda.synchronize()
+                t_total += a.elapsed_time(b) / 1e3
+                rows, errs = tab.best_f64()
+                curve.append({"gen": g0 + 10, "exact_evals": (g0 + 10) * tab.rows, "wall_s": t_total,
+                              "best_err": float(errs.min().item())})
+        finally:
+            if surr is not None:
+                L.speo_surrogate_destroy(surr)
+        out[mode] = {"curve": curve, "final_err": curve[-1]["best_err"], "wall_s": t_total,
+                     "gens_per_s": gens / t_total, "exact_evals_per_s": gens * tab.rows / t_total}
+    target = out["plain"]["final_err"]
+    hit = next((c for c in out["surrogate"]["curve"] if c["best_err"] <= target), None)
+    out["surrogate_reaches_plain_final_error"] = None if hit is None else {
+        "at_gen": hit["gen"], "exact_evals_ratio_plain_over_surrogate": out["plain"]["curve"][-1]["exact_evals"]
+        / hit["exact_evals"], "wall_ratio_plain_over_surrogate": out["plain"]["wall_s"] / hit["wall_s"]}
+    for mode in ("plain", "surrogate"):
+        hit8 = next((c for c in out[mode]["curve"] if c["best_err"] <= 1e-8), None)
+        out[mode]["exact_evals_to_1e-8"] = None if hit8 is None else hit8["exact_evals"]
     return out
 
 
@@ -477,8 +610,22 @@ def main() -> None:
     ap.add_argument("--no-ops", action="store_true", help="skip the bandwidth-scale operator measurements")
     ap.add_argument("--ops-only", action="store_true", help="only the bandwidth-scale operator measurements")
     ap.add_argument("--ops-islands", type=int, default=16384, help="islands of 128 rows in the operator variant")
+    ap.add_argument("--no-configs", action="store_true", help="skip the config 2 / 3 / 4 sections")
+    ap.add_argument("--c4-gens", type=int, default=200, help="generations of each config-4 run")
+    ap.add_argument("--configs-only", action="store_true", help="only the config 2 / 3 / 4 sections")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.configs_only:
+        import torch
+        from speo_gb300 import _lib
+
+        torch.cuda.set_device(0)
+        L = _lib.load()
+        flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda:0")
+        print(json.dumps({"config2_precision": bench_config2(L, "cuda:0", torch, flush),
+                          "config3_batched": bench_config3(L, "cuda:0", torch, flush),
+                          "config4_surrogate_vs_plain": bench_config4(L, "cuda:0", torch, args.c4_gens)}))
+        return
     if args.ops_only:
         import torch
         from speo_gb300 import _lib

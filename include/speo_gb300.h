@@ -312,6 +312,13 @@ SPEO_API int speo_surrogate_generation(speo_surrogate *s, const speo_segment *d_
                                        const float *fit_in, float *pop_out, float *fit_out,
                                        uint32_t *d_gen, int train_steps, float explore, void *stream);
 
+/* Strict-`<` greedy selection over a flat buffer of `rows` rows (stride ld, a multiple of 4):
+ * row r of (pop_out, fit_out) = trial r if trial_fit[r] < fit_in[r], else parent r
+ * (kernel_DE_CUDA.cu:305-327 over double buffers). */
+SPEO_API int speo_select_rows(const float *pop_in, const float *fit_in, const float *trial,
+                              const float *trial_fit, float *pop_out, float *fit_out, long long rows, int ld,
+                              void *stream);
+
 /* Per segment: argmin of fit (ties: lowest row) -> best_row[s]; FP64 re-evaluation of that
  * row -> best_err[s] = f(x) - f* in double. */
 SPEO_API int speo_best_reeval_f64(const speo_segment *d_segs, int n_segs, const float *pop,

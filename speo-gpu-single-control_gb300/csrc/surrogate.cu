@@ -716,3 +716,14 @@ extern "C" int speo_surrogate_generation(speo_surrogate *sp, const speo_segment 
     if (int e = speo_surrogate_archive_append(sp, S->sel, (int)rows, ld, S->fsel, stream)) return e;
     return speo_surrogate_train(sp, train_steps, nullptr, stream);
 }
+
+extern "C" int speo_select_rows(const float *pop_in, const float *fit_in, const float *trial, const float *trial_fit,
+                                float *pop_out, float *fit_out, long long rows, int ld, void *stream)
+{
+    if (!pop_in || !fit_in || !trial || !trial_fit || !pop_out || !fit_out || rows < 1 || ld < 4 || (ld & 3))
+        return fail(SPEO_ERR_INVALID_ARG, "speo_select_rows: bad arguments");
+    const int nchl = ld / 4;
+    k_select_flat<<<(unsigned)((rows * nchl + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        pop_in, fit_in, trial, trial_fit, pop_out, fit_out, rows, ld, nchl);
+    return check_launch("k_select_flat");
+}

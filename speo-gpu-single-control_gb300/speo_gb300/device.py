@@ -151,6 +151,40 @@ class SegmentTable:
                                            self.gen.data_ptr(), generations, self._stream()),
                    "speo_generation_epoch")
 
+    def tc_generation(self, trial: torch.Tensor, trial_fit: torch.Tensor):
+        """One generation with the rotation on the tensor cores: one DE trial per target
+        (speo_make_trials, k = 1), tcgen05 BF16x3 evaluation, strict-`<` selection. The table must
+        be planned with tiles of at most 128 rows."""
+        L = _lib.load()
+        a, b = self.cur, 1 - self.cur
+        st = self._stream()
+        _lib.check(L.speo_make_trials(self.d_segs.data_ptr(), self.d_items.data_ptr(), self.n_items, self.dim_hi, 1,
+                                      self.pop[a].data_ptr(), self.fit[a].data_ptr(), trial.data_ptr(),
+                                      self.gen.data_ptr(), st), "speo_make_trials")
+        _lib.check(L.speo_evaluate_tc(self.d_segs.data_ptr(), self.d_items.data_ptr(), self.n_items, self.dim_lo,
+                                      self.dim_hi, trial.data_ptr(), self.rows, self.ld, trial_fit.data_ptr(), st),
+                   "speo_evaluate_tc")
+        _lib.check(L.speo_select_rows(self.pop[a].data_ptr(), self.fit[a].data_ptr(), trial.data_ptr(),
+                                      trial_fit.data_ptr(), self.pop[b].data_ptr(), self.fit[b].data_ptr(), self.rows,
+                                      self.ld, st), "speo_select_rows")
+        self._advance_gen()
+        self.cur = b
+
+    def _advance_gen(self):
+        self.gen[0] += 1
+
+    def surrogate_generation(self, surrogate, k: int = 8, train_steps: int = 16, explore: float = 0.25):
+        """One surrogate-screened generation (speo_surrogate_generation); `surrogate` is an
+        speo_surrogate handle (ctypes.c_void_p)."""
+        L = _lib.load()
+        a, b = self.cur, 1 - self.cur
+        _lib.check(L.speo_surrogate_generation(surrogate, self.d_segs.data_ptr(), self.d_items.data_ptr(),
+                                               self.n_items, self.dim_lo, self.dim_hi, self.rows, self.ld, k,
+                                               self.pop[a].data_ptr(), self.fit[a].data_ptr(), self.pop[b].data_ptr(),
+                                               self.fit[b].data_ptr(), self.gen.data_ptr(), train_steps, explore,
+                                               self._stream()), "speo_surrogate_generation")
+        self.cur = b
+
     def migrate(self, k: int):
         L = _lib.load()
         _lib.check(L.speo_ring_migrate(self.d_segs.data_ptr(), len(self.specs), k, self.pop[self.cur].data_ptr(),
