@@ -23,36 +23,43 @@ namespace {
 
 constexpr uint32_t kTagSample = 4u;
 constexpr float kTargetFloor = 1e-8f;  // target = log(f + floor)
+constexpr int kSplitRows = 128;        // batch rows per split-K chunk of the weight gradients
 
 // ---- generic strided SIMT GEMM ---------------------------------------------------------------
 // C[m][n] = epi(alpha * sum_k A(m,k) B(k,n) + bias[n]),  A(m,k) = A[m*sam + k*sak],
 // B(k,n) = B[k*sbk + n*sbn]. epi: 0 = identity, 1 = ReLU (Z receives the pre-activation when
 // non-null), 2 = multiply by 1[Z[m][n] > 0] (ReLU backward). 64x64 tiles, 4x4 per thread.
+// Split-K: blockIdx.z sums k in [z*kc, (z+1)*kc) into C + z*cz (partial sums, reduced later in a
+// fixed order, so the result does not depend on scheduling).
 constexpr int BM = 64, BN = 64, BK = 16;
 
 template <int EPI>
 __global__ void __launch_bounds__(256) k_gemm(const float *__restrict__ A, long long sam, long long sak,
                                               const float *__restrict__ B, long long sbk, long long sbn,
                                               const float *__restrict__ bias, float *__restrict__ C, int ldc,
-                                              float *__restrict__ Z, int M, int N, int K, float alpha)
+                                              float *__restrict__ Z, int M, int N, int K, float alpha, int kc,
+                                              long long cz)
 {
     __shared__ float As[BK][BM + 4];
     __shared__ float Bs[BK][BN + 4];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    const int kbeg = blockIdx.z * kc;
+    const int kend = min(K, kbeg + kc);
+    C += blockIdx.z * cz;
     float acc[4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += BK) {
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
         for (int i = threadIdx.x; i < BK * BM; i += 256) {
             int kk, mm;
             if (sak == 1) { kk = i % BK; mm = i / BK; } else { mm = i % BM; kk = i / BM; }
             const int m = m0 + mm, k = k0 + kk;
-            As[kk][mm] = (m < M && k < K) ? A[m * sam + k * sak] : 0.f;
+            As[kk][mm] = (m < M && k < kend) ? A[m * sam + k * sak] : 0.f;
         }
         for (int i = threadIdx.x; i < BK * BN; i += 256) {
             int kk, nn;
             if (sbn == 1) { nn = i % BN; kk = i / BN; } else { kk = i % BK; nn = i / BK; }
             const int n = n0 + nn, k = k0 + kk;
-            Bs[kk][nn] = (n < N && k < K) ? B[k * sbk + n * sbn] : 0.f;
+            Bs[kk][nn] = (n < N && k < kend) ? B[k * sbk + n * sbn] : 0.f;
         }
         __syncthreads();
 #pragma unroll
@@ -92,11 +99,23 @@ __global__ void __launch_bounds__(256) k_gemm(const float *__restrict__ A, long 
 
 template <int EPI>
 int gemm(cudaStream_t st, const float *A, long long sam, long long sak, const float *B, long long sbk, long long sbn,
-         const float *bias, float *C, int ldc, float *Z, int M, int N, int K, float alpha)
+         const float *bias, float *C, int ldc, float *Z, int M, int N, int K, float alpha, int splits = 1,
+         long long cz = 0)
 {
-    const dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-    k_gemm<EPI><<<grid, 256, 0, st>>>(A, sam, sak, B, sbk, sbn, bias, C, ldc, Z, M, N, K, alpha);
+    const int kc = (((K + splits - 1) / splits) + BK - 1) / BK * BK;
+    const dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, splits);
+    k_gemm<EPI><<<grid, 256, 0, st>>>(A, sam, sak, B, sbk, sbn, bias, C, ldc, Z, M, N, K, alpha, kc, cz);
     return check_launch("k_gemm");
+}
+
+// out[i] = sum_z P[z * n + i], z ascending.
+__global__ void k_reduce_splits(const float *P, int splits, int n, float *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.f;
+    for (int z = 0; z < splits; ++z) s += P[(size_t)z * n + i];
+    out[i] = s;
 }
 
 // y[i] = b3 + sum_j H2[i][j] w3[j]: one warp per row.
@@ -383,6 +402,7 @@ struct Surrogate {
     float *Xb = nullptr, *Tb = nullptr;       // training batch
     float *Z1 = nullptr, *H1 = nullptr, *Z2 = nullptr, *H2 = nullptr, *yb = nullptr, *dy = nullptr;
     float *dZ2 = nullptr, *dZ1 = nullptr, *loss = nullptr, *one = nullptr;
+    float *gpart = nullptr;                   // split-K partial gradients, ceil(batch / 128) x np
     float *mu = nullptr, *isig = nullptr;     // input standardisation (default: 0 and in_scale)
     float *Xbn = nullptr;                     // standardised training batch
     long long nrm_rows = 0;
@@ -432,20 +452,26 @@ int mlp_grad(Surrogate *S, cudaStream_t st, const float *Xraw, int n, int ldxraw
     if (int e = mlp_forward(S, st, X, n, ldx, S->yb, S->Z1, S->H1, S->Z2, S->H2)) return e;
     if (int e = check_cuda(cudaMemsetAsync(S->loss, 0, sizeof(float), st), "memset loss")) return e;
     k_mse<<<(n + 255) / 256, 256, 0, st>>>(S->yb, T, n, S->dy, S->loss);
-    float *g = S->grad;
+    // Weight and bias gradients are sums over the batch rows: split-K over chunks of kSplitRows
+    // rows into the partial buffer (one full gradient vector per chunk), then one fixed-order sum.
+    const int splits = (n + kSplitRows - 1) / kSplitRows;
+    const long long np = S->np;
+    float *g = S->gpart;
     float *gW1 = g, *gb1 = gW1 + (size_t)h * din, *gW2 = gb1 + h, *gb2 = gW2 + (size_t)h * h, *gw3 = gb2 + h,
           *gb3 = gw3 + h;
     // head: gw3 = dy^T H2, gb3 = sum dy, dZ2 = 1[Z2>0] dy w3
-    if (int e = gemm<0>(st, S->dy, 0, 1, S->H2, h, 1, nullptr, gw3, h, nullptr, 1, h, n, 1.f)) return e;
-    if (int e = gemm<0>(st, S->one, 0, 0, S->dy, 1, 0, nullptr, gb3, 1, nullptr, 1, 1, n, 1.f)) return e;
+    if (int e = gemm<0>(st, S->dy, 0, 1, S->H2, h, 1, nullptr, gw3, h, nullptr, 1, h, n, 1.f, splits, np)) return e;
+    if (int e = gemm<0>(st, S->one, 0, 0, S->dy, 1, 0, nullptr, gb3, 1, nullptr, 1, 1, n, 1.f, splits, np)) return e;
     k_head_back<<<(unsigned)(((long long)n * h + 255) / 256), 256, 0, st>>>(S->dy, S->w3(), S->Z2, S->dZ2, n, h);
     // layer 2: gW2 = dZ2^T H1, gb2 = 1^T dZ2, dZ1 = (dZ2 W2) * 1[Z1 > 0]
-    if (int e = gemm<0>(st, S->dZ2, 1, h, S->H1, h, 1, nullptr, gW2, h, nullptr, h, h, n, 1.f)) return e;
-    if (int e = gemm<0>(st, S->one, 0, 0, S->dZ2, h, 1, nullptr, gb2, h, nullptr, 1, h, n, 1.f)) return e;
+    if (int e = gemm<0>(st, S->dZ2, 1, h, S->H1, h, 1, nullptr, gW2, h, nullptr, h, h, n, 1.f, splits, np)) return e;
+    if (int e = gemm<0>(st, S->one, 0, 0, S->dZ2, h, 1, nullptr, gb2, h, nullptr, 1, h, n, 1.f, splits, np)) return e;
     if (int e = gemm<2>(st, S->dZ2, h, 1, S->W2(), h, 1, nullptr, S->dZ1, h, S->Z1, n, h, h, 1.f)) return e;
     // layer 1: gW1 = dZ1^T X', gb1 = 1^T dZ1 (X' standardised)
-    if (int e = gemm<0>(st, S->dZ1, 1, h, X, ldx, 1, nullptr, gW1, din, nullptr, h, din, n, 1.f)) return e;
-    return gemm<0>(st, S->one, 0, 0, S->dZ1, h, 1, nullptr, gb1, h, nullptr, 1, h, n, 1.f);
+    if (int e = gemm<0>(st, S->dZ1, 1, h, X, ldx, 1, nullptr, gW1, din, nullptr, h, din, n, 1.f, splits, np)) return e;
+    if (int e = gemm<0>(st, S->one, 0, 0, S->dZ1, h, 1, nullptr, gb1, h, nullptr, 1, h, n, 1.f, splits, np)) return e;
+    k_reduce_splits<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(S->gpart, splits, (int)np, S->grad);
+    return check_launch("k_reduce_splits");
 }
 
 template <typename T>
@@ -474,6 +500,7 @@ extern "C" int speo_surrogate_create(speo_surrogate **out, int din, int hidden, 
     e = e ? e : dalloc(&S->m, S->np);
     e = e ? e : dalloc(&S->v, S->np);
     e = e ? e : dalloc(&S->grad, S->np);
+    e = e ? e : dalloc(&S->gpart, (size_t)S->np * ((batch + kSplitRows - 1) / kSplitRows));
     e = e ? e : dalloc(&S->AX, (size_t)archive_cap * S->lda);
     e = e ? e : dalloc(&S->AT, (size_t)archive_cap);
     e = e ? e : dalloc(&S->Xb, (size_t)batch * S->lda);
@@ -529,7 +556,7 @@ extern "C" int speo_surrogate_destroy(speo_surrogate *sp)
 {
     Surrogate *S = reinterpret_cast<Surrogate *>(sp);
     if (!S) return SPEO_OK;
-    for (float *p : {S->theta, S->m, S->v, S->grad, S->AX, S->AT, S->Xb, S->Tb, S->Z1, S->H1, S->Z2, S->H2, S->yb,
+    for (float *p : {S->theta, S->m, S->v, S->grad, S->gpart, S->AX, S->AT, S->Xb, S->Tb, S->Z1, S->H1, S->Z2, S->H2, S->yb,
                      S->dy, S->dZ2, S->dZ1, S->loss, S->one, S->sH1, S->sH2, S->T, S->pred, S->sel, S->fsel, S->mu,
                      S->isig, S->Xbn, S->Xn})
         if (p) cudaFree(p);
