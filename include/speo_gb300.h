@@ -284,6 +284,12 @@ SPEO_API int speo_surrogate_create(speo_surrogate **out, int din, int hidden, lo
 SPEO_API int speo_surrogate_destroy(speo_surrogate *s);
 SPEO_API int speo_surrogate_params(speo_surrogate *s, float **d_theta, float **d_grad, int *n_params);
 SPEO_API int speo_surrogate_forward(speo_surrogate *s, const float *X, int n, int ldx, float *y, void *stream);
+/* The same forward pass on the tcgen05 tensor cores: inputs standardised in FP32 and rounded to
+ * BF16, weights and hidden activations in BF16, FP32 accumulation and head. Takes din <= 64 and
+ * hidden 64, 128 or 256 (SPEO_ERR_UNSUPPORTED otherwise). speo_surrogate_generation screens with
+ * this pass whenever the shape allows it. */
+SPEO_API int speo_surrogate_forward_bf16(speo_surrogate *s, const float *X, long long n, int ldx, float *y,
+                                         void *stream);
 /* Gradient of the batch MSE w.r.t. theta into the object's gradient buffer; mean loss out. */
 SPEO_API int speo_surrogate_grad(speo_surrogate *s, const float *X, int n, int ldx, const float *T,
                                  float *loss_out, void *stream);

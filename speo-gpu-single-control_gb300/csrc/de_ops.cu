@@ -125,17 +125,29 @@ __device__ __forceinline__ int ndonors(int st)
     }
 }
 
+// Crossover test `(T)u01(w) < CR` as an integer compare: u01(w) = k * 2^-24 with
+// k = (w >> 8) + 1, so u < CR  <=>  k < CR * 2^24  <=>  k < ceil(CR * 2^24) for integer k (the
+// scaling by 2^24 is exact). NaN CR takes no element, as the float compare does.
+template <typename T>
+__device__ __forceinline__ uint32_t cr_threshold(T CR)
+{
+    const T x = ceil(CR * (T)16777216.0);
+    if (!(x > (T)0)) return 0u;               // also NaN
+    return x >= (T)33554432.0 ? 33554432u : (uint32_t)x;
+}
+__device__ __forceinline__ bool cr_take(uint32_t w, uint32_t thr) { return (w >> 8) + 1u < thr; }
+
 // One warp owns 32 consecutive positions: lane l draws the donors and jrand of position l
-// (Philox on all lanes at once), then the warp walks its rows R = 32/G at a time, G lanes per
-// row, two steps in flight, broadcasting each row's draws with shuffles.
-template <typename T, int G>
+// (Philox on all lanes at once). The warp's 32 x nch (row, 16-byte chunk) tasks are then dealt
+// to the lanes in order, task t = it * 32 + lane, so no lane idles whatever D is; each task reads
+// its row's draws from the drawing lane with shuffles. Two tasks in flight per lane.
+template <typename T>
 __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld, int dim, int island_size, int S,
                                                   const int *perm, const typename DeInfoT<T>::type *info,
                                                   const int *best_id, T lb, T ub, RngState *rng)
 {
     using V = typename Vec<T>::type;
     constexpr int VN = Vec<T>::n;
-    constexpr int R = 32 / G;
     const uint32_t gen = *(volatile uint32_t *)&rng->gen;
     const uint2 key = make_uint2(rng->key0, rng->key1);
     const int lane = threadIdx.x & 31;
@@ -156,113 +168,127 @@ __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld,
         }
     }
     const int nch = (dim + VN - 1) / VN;
-    const int gl = lane % G;
+    const int q32 = 32 / nch, r32 = 32 % nch;  // task t -> t + 32 advances (row, chunk) by these
+    int src = lane / nch, c = lane - src * nch;
     bool ok_bound = true;
 #pragma unroll 2
-    for (int step = 0; step < 32; step += R) {
-        const int src = step + lane / G;  // lane holding this group's row
+    for (int it = 0; it < nch; ++it) {          // uniform trip count: every lane takes nch tasks
         const int pos = wbase + src;
         const int rsel = __shfl_sync(0xffffffffu, sel, src), risl = __shfl_sync(0xffffffffu, isl, src);
         const int rjr = __shfl_sync(0xffffffffu, jr, src);
         const int rd[5] = {__shfl_sync(0xffffffffu, d0, src), __shfl_sync(0xffffffffu, d1, src),
                            __shfl_sync(0xffffffffu, d2, src), __shfl_sync(0xffffffffu, d3, src),
                            __shfl_sync(0xffffffffu, d4, src)};
+        const int e0 = VN * c;
+        src += q32;
+        c += r32;
+        if (c >= nch) { c -= nch; ++src; }
         if (pos >= island_size) continue;
-        const T F = info[risl].F, CR = info[risl].CR;
+        const T F = info[risl].F;
+        const uint32_t thr = cr_threshold<T>(info[risl].CR);
         const int st = info[risl].strategy_ID;
         const int nd = ndonors(st);
         const int b = strategy_uses_best(st) ? best_id[risl] : rsel;
         const T *xi = pop + (size_t)rsel * ld;
         const T *xb = pop + (size_t)b * ld;
         T *out = cand + (size_t)rsel * ld;
-        for (int c = gl; c < nch; c += G) {
-            const int e0 = VN * c;
-            const V ti = *reinterpret_cast<const V *>(xi + e0);
-            const V tb = strategy_uses_best(st) ? *reinterpret_cast<const V *>(xb + e0) : ti;
-            V tr[5];
+        const V ti = *reinterpret_cast<const V *>(xi + e0);
+        const V tb = strategy_uses_best(st) ? *reinterpret_cast<const V *>(xb + e0) : ti;
+        V tr[5];
 #pragma unroll
-            for (int k = 0; k < 5; ++k)
-                tr[k] = k < nd ? *reinterpret_cast<const V *>(pop + (size_t)rd[k] * ld + e0) : ti;
-            const uint4 w = philox(make_uint4((uint32_t)(e0 >> 2), (uint32_t)pos, gen, kTagCr), key);
-            V o = ti;
-            if (st == SPEO_DE_RAND_1) {  // rand/1, the default strategy (DE_CUDA.cc:63): no switch
+        for (int k = 0; k < 5; ++k)
+            tr[k] = k < nd ? *reinterpret_cast<const V *>(pop + (size_t)rd[k] * ld + e0) : ti;
+        const uint4 w = philox(make_uint4((uint32_t)(e0 >> 2), (uint32_t)pos, gen, kTagCr), key);
+        V o = ti;
+        if (st == SPEO_DE_RAND_1) {  // rand/1, the default strategy (DE_CUDA.cc:63): no switch
 #pragma unroll
-                for (int q = 0; q < VN; ++q) {
-                    const int e = e0 + q;
-                    const float u = u01(pick(w, (uint32_t)(e & 3)));
-                    T v = vget<T>(ti, q);
-                    if (e == rjr || (T)u < CR)
-                        v = fma_rn(F, sub_rn(vget<T>(tr[1], q), vget<T>(tr[2], q)), vget<T>(tr[0], q));
-                    vset<T>(o, q, check_bound<T>(v, lb, ub, ok_bound));
-                }
-            } else {
-#pragma unroll
-                for (int q = 0; q < VN; ++q) {
-                    const int e = e0 + q;
-                    const float u = u01(pick(w, (uint32_t)(e & 3)));
-                    T v;
-                    if (e == rjr || (T)u < CR) {
-                        T xr[5];
-#pragma unroll
-                        for (int k = 0; k < 5; ++k) xr[k] = vget<T>(tr[k], q);
-                        v = mutant<T>(st, F, vget<T>(ti, q), vget<T>(tb, q), xr);
-                    } else {
-                        v = vget<T>(ti, q);
-                    }
-                    vset<T>(o, q, check_bound<T>(v, lb, ub, ok_bound));
-                }
+            for (int q = 0; q < VN; ++q) {
+                const int e = e0 + q;
+                T v = vget<T>(ti, q);
+                if (e == rjr || cr_take(pick(w, (uint32_t)(e & 3)), thr))
+                    v = fma_rn(F, sub_rn(vget<T>(tr[1], q), vget<T>(tr[2], q)), vget<T>(tr[0], q));
+                vset<T>(o, q, check_bound<T>(v, lb, ub, ok_bound));
             }
-            if (e0 + VN <= dim) {
-                *reinterpret_cast<V *>(out + e0) = o;
-            } else {  // ragged last chunk: elements past D are never written (as in the reference)
+        } else {
 #pragma unroll
-                for (int q = 0; q < VN; ++q)
-                    if (e0 + q < dim) out[e0 + q] = vget<T>(o, q);
+            for (int q = 0; q < VN; ++q) {
+                const int e = e0 + q;
+                T v;
+                if (e == rjr || cr_take(pick(w, (uint32_t)(e & 3)), thr)) {
+                    T xr[5];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) xr[k] = vget<T>(tr[k], q);
+                    v = mutant<T>(st, F, vget<T>(ti, q), vget<T>(tb, q), xr);
+                } else {
+                    v = vget<T>(ti, q);
+                }
+                vset<T>(o, q, check_bound<T>(v, lb, ub, ok_bound));
             }
+        }
+        if (e0 + VN <= dim) {
+            *reinterpret_cast<V *>(out + e0) = o;
+        } else {  // ragged last chunk: elements past D are never written (as in the reference)
+#pragma unroll
+            for (int q = 0; q < VN; ++q)
+                if (e0 + q < dim) out[e0 + q] = vget<T>(o, q);
         }
     }
     if (!ok_bound) atomicOr(&s_deverr, SPEO_DEVERR_BOUND_LIMIT);
     finish_launch(rng, gen);
 }
 
-// global_DE_SelectSurvival (kernel_DE_CUDA.cu:305-327): strict `<`. Grid-stride over 16-byte
-// chunks of rows, four independent chunks in flight per thread; rows whose trial loses move no
-// data.
+// global_DE_SelectSurvival (kernel_DE_CUDA.cu:305-327): strict `<`. One warp per group of 32
+// rows: a coalesced compare of the two fitness arrays, a ballot, then the winning rows copied up
+// to kBatch at a time with every load issued before the first store (bytes in flight, not
+// instruction count, bound a sparse row copy). Rows whose trial loses move no data.
 template <typename T>
 __global__ void __launch_bounds__(256) k_select(T *pop, T *pop_fit, const T *cand, const T *cand_fit, int n, int ld,
                                                 int dim)
 {
     using V = typename Vec<T>::type;
-    constexpr int VN = Vec<T>::n, U = 4;
+    constexpr int VN = Vec<T>::n, kBatch = 8;
+    const int lane = threadIdx.x & 31;
     const int nch = (dim + VN - 1) / VN;
-    const long long total = (long long)n * nch;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; t0 < total; t0 += stride * U) {
-        int row[U], c[U];
-        bool win[U];
-        T fc[U];
+    const bool ragged = (dim % VN) != 0;
+    const long long groups = ((long long)n + 31) / 32;
+    const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+    long long g = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    T fc = 0, fp = 0;  // this group's fitness pair, loaded one group ahead
+    if (g < groups && g * 32 + lane < n) { fc = cand_fit[g * 32 + lane]; fp = pop_fit[g * 32 + lane]; }
+    for (; g < groups; g += nwarps) {
+        const long long row = g * 32 + lane;
+        const bool win = row < n && fc < fp;
+        if (win) pop_fit[row] = fc;
+        const long long gn = g + nwarps;
+        if (gn < groups && gn * 32 + lane < n) { fc = cand_fit[gn * 32 + lane]; fp = pop_fit[gn * 32 + lane]; }
+        unsigned m = __ballot_sync(0xffffffffu, win);
+        while (m) {
+            int rr[kBatch];
+            int cnt = 0;
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const long long t = t0 + u * stride;
-            row[u] = (int)(t / nch);
-            c[u] = (int)(t - (long long)row[u] * nch);
-            win[u] = false;
-            if (t < total) {
-                fc[u] = cand_fit[row[u]];
-                win[u] = fc[u] < pop_fit[row[u]];
+            for (int q = 0; q < kBatch; ++q) {
+                rr[q] = 0;
+                if (m) {
+                    rr[q] = (int)(g * 32) + (__ffs(m) - 1);
+                    m &= m - 1;
+                    ++cnt;
+                }
             }
-        }
+            for (int c0 = 0; c0 < nch; c0 += 32) {
+                const int c = c0 + lane;
+                const bool full = c < nch && (!ragged || c < nch - 1);
+                V v[kBatch];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            if (!win[u]) continue;
-            const size_t base = (size_t)row[u] * ld;
-            const int e0 = VN * c[u];
-            if (e0 + VN <= dim) {
-                *reinterpret_cast<V *>(pop + base + e0) = *reinterpret_cast<const V *>(cand + base + e0);
-            } else {
-                for (int q = 0; q < VN && e0 + q < dim; ++q) pop[base + e0 + q] = cand[base + e0 + q];
+                for (int q = 0; q < kBatch; ++q)
+                    if (q < cnt && full) v[q] = *reinterpret_cast<const V *>(cand + (size_t)rr[q] * ld + VN * c);
+#pragma unroll
+                for (int q = 0; q < kBatch; ++q)
+                    if (q < cnt && full) *reinterpret_cast<V *>(pop + (size_t)rr[q] * ld + VN * c) = v[q];
+                if (c < nch && !full) {  // ragged last chunk: elements past D are never written
+                    for (int q = 0; q < cnt; ++q)
+                        for (int e = VN * c; e < dim; ++e) pop[(size_t)rr[q] * ld + e] = cand[(size_t)rr[q] * ld + e];
+                }
             }
-            if (c[u] == 0) pop_fit[row[u]] = fc[u];
         }
     }
 }
@@ -307,23 +333,12 @@ int generate(Pop cand, Pop pop, int *d_best, speo_island_info ii, Info *d_info, 
     k_best<T><<<(ii.subisland_num + kWarps - 1) / kWarps, 32 * kWarps, 0, st>>>(
         pop.fitness_value, ii.permutated_index, S, ii.subisland_num, d_best);
     if (int e = check_launch("global_DE_FindBestIndividualInIsland")) return e;
-    // lanes per row: enough 16-byte chunks to cover D (np2 rows keep every chunk in bounds)
-    const int vn = 16 / (int)sizeof(T), nch = (pi.dim + vn - 1) / vn;
+    // 16-byte chunks cover D (np2 rows keep every chunk in bounds)
     const int grid = (ii.island_size + 255) / 256;  // 8 warps x 32 positions per block
     const auto *inf = reinterpret_cast<const typename DeInfoT<T>::type *>(d_info);
     RngState *rs = reinterpret_cast<RngState *>(d_rng);
-    if (nch <= 4)
-        k_generate<T, 4><<<grid, 256, 0, st>>>(cand.elements, pop.elements, ld, pi.dim, ii.island_size, S,
-                                                 ii.permutated_index, inf, d_best, (T)pi.min_bound, (T)pi.max_bound, rs);
-    else if (nch <= 8)
-        k_generate<T, 8><<<grid, 256, 0, st>>>(cand.elements, pop.elements, ld, pi.dim, ii.island_size, S,
-                                                 ii.permutated_index, inf, d_best, (T)pi.min_bound, (T)pi.max_bound, rs);
-    else if (nch <= 16)
-        k_generate<T, 16><<<grid, 256, 0, st>>>(cand.elements, pop.elements, ld, pi.dim, ii.island_size, S,
-                                                  ii.permutated_index, inf, d_best, (T)pi.min_bound, (T)pi.max_bound, rs);
-    else
-        k_generate<T, 32><<<grid, 256, 0, st>>>(cand.elements, pop.elements, ld, pi.dim, ii.island_size, S,
-                                                  ii.permutated_index, inf, d_best, (T)pi.min_bound, (T)pi.max_bound, rs);
+    k_generate<T><<<grid, 256, 0, st>>>(cand.elements, pop.elements, ld, pi.dim, ii.island_size, S,
+                                        ii.permutated_index, inf, d_best, (T)pi.min_bound, (T)pi.max_bound, rs);
     return check_launch("global_DE_GenerateNewPopulation");
 }
 
@@ -334,10 +349,8 @@ int select(Pop pop, Pop cand, speo_island_info ii, Prob pi)
     if (!cand.elements || !pop.fitness_value || !cand.fitness_value)
         return fail(SPEO_ERR_INVALID_ARG, "API_DE_SelectSurvival: null pointer argument");
     const int ld = np2_of(pi.dim);
-    const int vn = 16 / (int)sizeof(T);
-    const long long threads = (long long)ii.island_size * ((pi.dim + vn - 1) / vn);
-    const long long want = (threads + 4 * 256 - 1) / (4 * 256);
-    const int grid = (int)(want < 16LL * sm_count() ? (want > 0 ? want : 1) : 16LL * sm_count());
+    const long long want = ((long long)ii.island_size + 32 * 8 - 1) / (32 * 8);  // 8 warps of 32 rows
+    const int grid = (int)(want < 8LL * sm_count() ? want : 8LL * sm_count());
     k_select<T><<<grid, 256, 0, api_stream()>>>(
         pop.elements, pop.fitness_value, cand.elements, cand.fitness_value, ii.island_size, ld, pi.dim);
     return check_launch("global_DE_SelectSurvival");

@@ -28,6 +28,14 @@ struct RngState {
 };
 static_assert(sizeof(RngState) == SPEO_RNG_STATE_BYTES, "rng state size");
 
+// Surrogate MLP forward on the tensor cores (BF16 operands, FP32 accumulation), mlp_tc.cu.
+// theta: W1 (h x din) | b1 | W2 (h x h) | b2 | w3 | b3; img: mlp_bf16_image_bytes(h) bytes of
+// device scratch for the packed weights.
+bool mlp_bf16_supported(int din, int h);
+size_t mlp_bf16_image_bytes(int h);
+int mlp_forward_bf16(const float *theta, int din, int h, const float *mu, const float *isig, const float *X,
+                     long long n, int ldx, float *y, uint8_t *img, cudaStream_t st);
+
 }  // namespace speo
 
 // Bit readers of the per-translation-unit device error words.
@@ -37,3 +45,4 @@ extern "C" unsigned int speo_deverr_generation(void);
 extern "C" unsigned int speo_deverr_tc(void);
 extern "C" unsigned int speo_deverr_resident(void);
 extern "C" unsigned int speo_deverr_surrogate(void);
+extern "C" unsigned int speo_deverr_mlp(void);

@@ -407,6 +407,7 @@ struct Surrogate {
     float *Xbn = nullptr;                     // standardised training batch
     long long nrm_rows = 0;
     float *Xn = nullptr;                      // standardised screening inputs
+    uint8_t *wimg = nullptr;                  // packed BF16 weights of the tensor-core forward
     // screening scratch (grown on demand)
     long long scr_rows = 0;
     float *sH1 = nullptr, *sH2 = nullptr;
@@ -513,6 +514,7 @@ extern "C" int speo_surrogate_create(speo_surrogate **out, int din, int hidden, 
     e = e ? e : dalloc(&S->mu, (size_t)S->lda);
     e = e ? e : dalloc(&S->isig, (size_t)S->lda);
     e = e ? e : dalloc(&S->Xbn, (size_t)batch * S->lda);
+    if (mlp_bf16_supported(din, hidden)) e = e ? e : dalloc(&S->wimg, mlp_bf16_image_bytes(hidden));
     if (e) { speo_surrogate_destroy(reinterpret_cast<speo_surrogate *>(S)); return e; }
     // He-style initialisation from Philox on the host side of the stream: uniform(-a, a)
     float *h_theta = new float[S->np];
@@ -560,6 +562,7 @@ extern "C" int speo_surrogate_destroy(speo_surrogate *sp)
                      S->dy, S->dZ2, S->dZ1, S->loss, S->one, S->sH1, S->sH2, S->T, S->pred, S->sel, S->fsel, S->mu,
                      S->isig, S->Xbn, S->Xn})
         if (p) cudaFree(p);
+    if (S->wimg) cudaFree(S->wimg);
     delete S;
     return SPEO_OK;
 }
@@ -598,6 +601,21 @@ extern "C" int speo_surrogate_forward(speo_surrogate *sp, const float *X, int n,
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (int e = standardise(S, st, X, n, ldx, S->Xn)) return e;
     return mlp_forward(S, st, S->Xn, n, S->lda, y, nullptr, S->sH1, nullptr, S->sH2);
+}
+
+// The same network on the tensor cores: BF16 operands (inputs standardised in FP32 first, weights
+// and hidden activations rounded to BF16), FP32 accumulation, FP32 head.
+extern "C" int speo_surrogate_forward_bf16(speo_surrogate *sp, const float *X, long long n, int ldx, float *y,
+                                           void *stream)
+{
+    Surrogate *S = reinterpret_cast<Surrogate *>(sp);
+    if (!S || !X || !y || n < 0 || ldx < S->din)
+        return fail(SPEO_ERR_INVALID_ARG, "speo_surrogate_forward_bf16: bad arguments");
+    if (!S->wimg)
+        return fail(SPEO_ERR_UNSUPPORTED, "speo_surrogate_forward_bf16: din %d, hidden %d (takes din <= 64, hidden "
+                                          "64 / 128 / 256)", S->din, S->h);
+    return mlp_forward_bf16(S->theta, S->din, S->h, S->mu, S->isig, X, n, ldx, y, S->wimg,
+                            static_cast<cudaStream_t>(stream));
 }
 
 // Standardise the MLP's inputs by the per-dimension mean and standard deviation of `rows` rows of
@@ -726,7 +744,11 @@ extern "C" int speo_surrogate_generation(speo_surrogate *sp, const speo_segment 
     }
     if (int e = speo_surrogate_standardize(sp, pop_in, rows, ld, stream)) return e;
     if (int e = speo_make_trials(segs, items, n_items, dim_hi, k, pop_in, fit_in, S->T, d_gen, stream)) return e;
-    if (int e = speo_surrogate_forward(sp, S->T, (int)(rows * k), ld, S->pred, stream)) return e;
+    if (S->wimg) {  // screening on the tensor cores where the shape allows it
+        if (int e = speo_surrogate_forward_bf16(sp, S->T, rows * k, ld, S->pred, stream)) return e;
+    } else {
+        if (int e = speo_surrogate_forward(sp, S->T, (int)(rows * k), ld, S->pred, stream)) return e;
+    }
     const int nch = (dim_hi + 3) / 4;
     k_pick<<<(unsigned)((rows * nch + 255) / 256), 256, 0, st>>>(
         S->T, S->pred, k, S->sel, rows, ld, dim_hi, explore, make_uint2((uint32_t)S->seed, (uint32_t)(S->seed >> 32)),

@@ -58,6 +58,80 @@ class Surr:
         self.lib.speo_surrogate_destroy(self.p)
 
 
+def _bf16(x):
+    """Round float32 to the nearest BF16, ties to even, returned as float32."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def _forward_bf16_emulated(theta, din, h, X, scale):
+    """The tensor-core forward pass with its roundings made explicit: standardise in FP32, round
+    inputs, weights and hidden activations to BF16, accumulate exactly (FP64) and round the sums
+    to FP32 before each bias add."""
+    f32 = np.float32
+    W1 = theta[: h * din].reshape(h, din)
+    o = h * din
+    b1 = theta[o:o + h]; o += h
+    W2 = theta[o:o + h * h].reshape(h, h); o += h * h
+    b2 = theta[o:o + h]; o += h
+    w3 = theta[o:o + h]; b3 = theta[o + h]
+    xn = _bf16((X[:, :din] - f32(0)) * f32(scale)).astype(np.float64)
+    a1 = (xn @ _bf16(W1).astype(np.float64).T).astype(f32)
+    h1 = _bf16(np.maximum(a1 + b1, f32(0))).astype(np.float64)
+    a2 = (h1 @ _bf16(W2).astype(np.float64).T).astype(f32)
+    h2 = np.maximum(a2 + b2, f32(0)).astype(np.float64)
+    return h2 @ w3.astype(np.float64) + float(b3)
+
+
+@pytest.mark.parametrize("din,h,n,ldx", [(50, 256, 1000, 52), (50, 256, 128, 50), (10, 64, 777, 12),
+                                         (64, 128, 300, 64)])
+def test_forward_bf16_matches_emulation(lib, cuda, din, h, n, ldx):
+    """tcgen05 forward (BF16 operands, FP32 accumulation) against the same roundings in numpy:
+    only the order of the FP32 accumulation differs."""
+    import torch
+    from speo_gb300 import _lib
+
+    s = Surr(lib, din=din, h=h)
+    try:
+        rng = np.random.default_rng(din + h)
+        theta = (rng.normal(0, 1, s.n) * np.sqrt(2.0 / np.where(np.arange(s.n) < h * din, din, h))).astype(np.float32)
+        np_to_dev(s.theta_ptr, theta)
+        X = np.zeros((n, ldx), dtype=np.float32)
+        X[:, :din] = rng.uniform(-100, 100, (n, din))
+        if ldx > din:
+            X[:, din:] = 1e30        # padding must never reach the network
+        tX = torch.from_numpy(X).cuda()
+        y = torch.full((n + 1,), -7.0, device="cuda")
+        _lib.check(lib.speo_surrogate_forward_bf16(s.p, tX.data_ptr(), n, ldx, y.data_ptr(), None), "forward_bf16")
+        torch.cuda.synchronize()
+        got = y.cpu().numpy()
+        assert got[n] == -7.0        # nothing written past n rows
+        ref = _forward_bf16_emulated(theta, din, h, X, SCALE)
+        scale = np.abs(ref).max() + 1.0
+        np.testing.assert_allclose(got[:n], ref, rtol=0, atol=2e-4 * scale)
+        # and close to the FP32 network: BF16 rounding only
+        y32 = torch.zeros(n, device="cuda")
+        _lib.check(lib.speo_surrogate_forward(s.p, tX.data_ptr(), n, ldx, y32.data_ptr(), None), "forward")
+        torch.cuda.synchronize()
+        assert np.corrcoef(got[:n], y32.cpu().numpy())[0, 1] > 0.999
+    finally:
+        s.close()
+
+
+def test_forward_bf16_rejects_unsupported_shapes(lib, cuda):
+    from speo_gb300 import _lib
+
+    s = Surr(lib, din=100, h=256)
+    try:
+        import torch
+        X = torch.zeros(4, 100, device="cuda")
+        y = torch.zeros(4, device="cuda")
+        assert lib.speo_surrogate_forward_bf16(s.p, X.data_ptr(), 4, 100, y.data_ptr(), None) == _lib.SPEO_ERR_UNSUPPORTED
+    finally:
+        s.close()
+
+
 def test_forward_matches_oracle(lib, oracle, cuda):
     import torch
 
