@@ -425,61 +425,89 @@ def bench_config3(L, dev, torch, flush) -> dict:
             "tile_rows": best}
 
 
-def bench_config4(L, dev, torch, gens: int) -> dict:
-    """Config 4: 128 islands x 256, D = 50, rotated Rastrigin. Plain DE against the surrogate-
-    screened DE (MLP 50-256-256-1, archive 2^20, Adam lr 1e-3, batch 4096, k = 8 trials per
-    target, 16 Adam steps per generation, 25 % exploration picks); ring migration of 5 every 50
-    generations in both. Both spend 32768 exact evaluations per generation. Best FP64 error every
-    10 generations; wall time from CUDA events around the generations only."""
+def _c4_run(L, dev, torch, func: int, mode: str, max_gens: int, log_every: int = 10, stop_at: float | None = None):
+    """One config-4 run (plain or surrogate-screened) logging the FP64 best error every
+    `log_every` generations; stops early once the error reaches `stop_at`."""
     import ctypes as C
 
     from speo_gb300 import _lib
     from speo_gb300 import workloads as w
 
-    specs, inst = w.config4_specs()
-    out = {"workload": "128 islands x P=256, D=50, rotated Rastrigin; surrogate MLP 50-256-256-1", "generations": gens}
-    for mode in ("plain", "surrogate"):
-        tab = w.table(specs, inst, device=dev)
-        tab.init_population()
-        surr = None
-        if mode == "surrogate":
-            surr = C.c_void_p()
-            _lib.check(L.speo_surrogate_create(C.byref(surr), 50, 256, 1 << 20, 4096, 1e-3, 0.01, 4242),
-                       "speo_surrogate_create")
-        curve, t_total = [], 0.0
-        try:
-            for g0 in range(0, gens, 10):
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record()
-                for g in range(g0, g0 + 10):
-                    if mode == "plain":
-                        if tab.epoch_fits():
-                            tab.epoch(1)
-                        else:
-                            tab.generation()
+    specs, inst = w.config4_specs(func)
+    tab = w.table(specs, inst, device=dev)
+    tab.init_population()
+    surr = None
+    if mode == "surrogate":
+        surr = C.c_void_p()
+        _lib.check(L.speo_surrogate_create(C.byref(surr), 50, 256, 1 << 20, 4096, 1e-3, 0.01, 4242),
+                   "speo_surrogate_create")
+    curve, t_total = [], 0.0
+    try:
+        for g0 in range(0, max_gens, log_every):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for g in range(g0, g0 + log_every):
+                if mode == "plain":
+                    if tab.epoch_fits():
+                        tab.epoch(1)
                     else:
-                        tab.surrogate_generation(surr, k=8, train_steps=16, explore=0.25)
-                    if (g + 1) % 50 == 0:
-                        tab.migrate(5)
-                b.record()
-                torch.cuda.synchronize()
-                t_total += a.elapsed_time(b) / 1e3
-                rows, errs = tab.best_f64()
-                curve.append({"gen": g0 + 10, "exact_evals": (g0 + 10) * tab.rows, "wall_s": t_total,
-                              "best_err": float(errs.min().item())})
-        finally:
-            if surr is not None:
-                L.speo_surrogate_destroy(surr)
-        out[mode] = {"curve": curve, "final_err": curve[-1]["best_err"], "wall_s": t_total,
-                     "gens_per_s": gens / t_total, "exact_evals_per_s": gens * tab.rows / t_total}
-    target = out["plain"]["final_err"]
-    hit = next((c for c in out["surrogate"]["curve"] if c["best_err"] <= target), None)
-    out["surrogate_reaches_plain_final_error"] = None if hit is None else {
-        "at_gen": hit["gen"], "exact_evals_ratio_plain_over_surrogate": out["plain"]["curve"][-1]["exact_evals"]
-        / hit["exact_evals"], "wall_ratio_plain_over_surrogate": out["plain"]["wall_s"] / hit["wall_s"]}
+                        tab.generation()
+                else:
+                    tab.surrogate_generation(surr, k=8, train_steps=16, explore=0.25)
+                if (g + 1) % 50 == 0:
+                    tab.migrate(5)
+            b.record()
+            torch.cuda.synchronize()
+            t_total += a.elapsed_time(b) / 1e3
+            rows, errs = tab.best_f64()
+            curve.append({"gen": g0 + log_every, "exact_evals": (g0 + log_every) * tab.rows, "wall_s": t_total,
+                          "best_err": float(errs.min().item())})
+            if stop_at is not None and curve[-1]["best_err"] <= stop_at:
+                break
+    finally:
+        if surr is not None:
+            L.speo_surrogate_destroy(surr)
+    gens = curve[-1]["gen"]
+    hit = next((c for c in curve if c["best_err"] <= 1e-8), None)
+    kept = curve[:: max(1, len(curve) // 40)]
+    if kept[-1] is not curve[-1]:
+        kept.append(curve[-1])
+    return {"curve": kept, "final_err": curve[-1]["best_err"], "generations": gens, "wall_s": t_total,
+            "gens_per_s": gens / t_total, "exact_evals_per_s": gens * tab.rows / t_total,
+            "exact_evals_to_1e-8": None if hit is None else hit["exact_evals"],
+            "wall_s_to_1e-8": None if hit is None else hit["wall_s"]}, curve
+
+
+def bench_config4(L, dev, torch, gens: int) -> dict:
+    """Config 4: 128 islands x 256, D = 50. Plain DE against the surrogate-screened DE (MLP
+    50-256-256-1 screening on the tensor cores in BF16, archive 2^20, Adam lr 1e-3, batch 4096,
+    k = 8 trials per target, 16 Adam steps per generation, 25 % exploration picks); ring migration
+    of 5 every 50 generations in both, both spend 32768 exact evaluations per generation. Best
+    FP64 error every 10 generations; wall time from CUDA events around the generations only.
+    (a) rotated Rastrigin for `gens` generations; (b) the rotated sphere of the same shape run to
+    an error of 1e-8 (capped), which gives the exact evaluations each method needs to get there."""
+    from speo_gb300 import _lib
+
+    out = {"workload": "128 islands x P=256, D=50; surrogate MLP 50-256-256-1 (BF16 tcgen05 screening, "
+                       "FP32 training), k=8"}
+    ras = {"objective": "rotated Rastrigin", "generations": gens}
+    curves = {}
     for mode in ("plain", "surrogate"):
-        hit8 = next((c for c in out[mode]["curve"] if c["best_err"] <= 1e-8), None)
-        out[mode]["exact_evals_to_1e-8"] = None if hit8 is None else hit8["exact_evals"]
+        ras[mode], curves[mode] = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, mode, gens)
+    target = ras["plain"]["final_err"]
+    hit = next((c for c in curves["surrogate"] if c["best_err"] <= target), None)
+    ras["surrogate_reaches_plain_final_error"] = None if hit is None else {
+        "at_gen": hit["gen"], "exact_evals_ratio_plain_over_surrogate": curves["plain"][-1]["exact_evals"]
+        / hit["exact_evals"], "wall_ratio_plain_over_surrogate": ras["plain"]["wall_s"] / hit["wall_s"]}
+    out["rastrigin"] = ras
+    sph = {"objective": "rotated sphere", "target_err": 1e-8}
+    sph["plain"], _ = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "plain", 4000, stop_at=1e-8)
+    sph["surrogate"], _ = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8)
+    ep, es = sph["plain"]["exact_evals_to_1e-8"], sph["surrogate"]["exact_evals_to_1e-8"]
+    wp, ws = sph["plain"]["wall_s_to_1e-8"], sph["surrogate"]["wall_s_to_1e-8"]
+    sph["exact_evals_ratio_plain_over_surrogate"] = ep / es if ep and es else None
+    sph["wall_ratio_plain_over_surrogate"] = wp / ws if wp and ws else None
+    out["sphere_to_1e-8"] = sph
     return out
 
 
@@ -613,8 +641,16 @@ def main() -> None:
     ap.add_argument("--no-configs", action="store_true", help="skip the config 2 / 3 / 4 sections")
     ap.add_argument("--c4-gens", type=int, default=200, help="generations of each config-4 run")
     ap.add_argument("--configs-only", action="store_true", help="only the config 2 / 3 / 4 sections")
+    ap.add_argument("--c4-only", action="store_true", help="only the config 4 section")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.c4_only:
+        import torch
+        from speo_gb300 import _lib
+
+        torch.cuda.set_device(0)
+        print(json.dumps({"config4_surrogate_vs_plain": bench_config4(_lib.load(), "cuda:0", torch, args.c4_gens)}))
+        return
     if args.configs_only:
         import torch
         from speo_gb300 import _lib
