@@ -290,6 +290,18 @@ SPEO_API int speo_surrogate_forward(speo_surrogate *s, const float *X, int n, in
  * this pass whenever the shape allows it. */
 SPEO_API int speo_surrogate_forward_bf16(speo_surrogate *s, const float *X, long long n, int ldx, float *y,
                                          void *stream);
+/* Gradient of the batch loss on the tcgen05 tensor cores into the gradient buffer: BF16 operands
+ * (standardised inputs, weights, hidden activations and back-propagated deltas), FP32
+ * accumulation. The weight gradients are sums over 128-row chunks added in a fixed order, so the
+ * result is deterministic. Same shapes as speo_surrogate_forward_bf16. */
+SPEO_API int speo_surrogate_grad_bf16(speo_surrogate *s, const float *X, int n, int ldx, const float *T,
+                                      float *loss_out, void *stream);
+/* Which passes run on the tensor cores in speo_surrogate_generation / speo_surrogate_train:
+ * SPEO_SURROGATE_BF16_SCREEN (screening forward) and SPEO_SURROGATE_BF16_TRAIN (training
+ * gradient); 0 = FP32 CUDA-core passes throughout. Default: both where the shape allows. */
+#define SPEO_SURROGATE_BF16_SCREEN 1
+#define SPEO_SURROGATE_BF16_TRAIN 2
+SPEO_API int speo_surrogate_set_mode(speo_surrogate *s, int mode);
 /* Gradient of the batch MSE w.r.t. theta into the object's gradient buffer; mean loss out. */
 SPEO_API int speo_surrogate_grad(speo_surrogate *s, const float *X, int n, int ldx, const float *T,
                                  float *loss_out, void *stream);

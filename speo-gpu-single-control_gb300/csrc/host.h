@@ -35,6 +35,18 @@ bool mlp_bf16_supported(int din, int h);
 size_t mlp_bf16_image_bytes(int h);
 int mlp_forward_bf16(const float *theta, int din, int h, const float *mu, const float *isig, const float *X,
                      long long n, int ldx, float *y, uint8_t *img, cudaStream_t st);
+// Gradient of the mean squared error of one batch (n rows of X, targets T) on the tensor cores:
+// chunk z of 128 rows writes its partial gradient vector to gpart + z * round_up(n_params, 4) (summed over
+// chunks by the caller); the squared-error sum is added to *loss. Scratch: BF16 [features][rp]
+// transposes of the layer inputs and deltas, dy [rp]; rp = batch rounded up to 128.
+struct MlpTrainBufs {
+    uint16_t *xnT, *h1T, *h2T, *dz2T, *dz1T;
+    float *dy;
+    long long rp;
+};
+int mlp_grad_bf16(const float *theta, int din, int h, const float *mu, const float *isig, const float *X, int n,
+                  int ldx, const float *T, uint8_t *img, const MlpTrainBufs &b, float *gpart, float *loss,
+                  cudaStream_t st);
 
 }  // namespace speo
 

@@ -108,13 +108,13 @@ int gemm(cudaStream_t st, const float *A, long long sam, long long sak, const fl
     return check_launch("k_gemm");
 }
 
-// out[i] = sum_z P[z * n + i], z ascending.
-__global__ void k_reduce_splits(const float *P, int splits, int n, float *out)
+// out[i] = sum_z P[z * stride + i], z ascending.
+__global__ void k_reduce_splits(const float *P, int splits, int n, long long stride, float *out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float s = 0.f;
-    for (int z = 0; z < splits; ++z) s += P[(size_t)z * n + i];
+    for (int z = 0; z < splits; ++z) s += P[(size_t)z * stride + i];
     out[i] = s;
 }
 
@@ -407,13 +407,16 @@ struct Surrogate {
     float *Xbn = nullptr;                     // standardised training batch
     long long nrm_rows = 0;
     float *Xn = nullptr;                      // standardised screening inputs
-    uint8_t *wimg = nullptr;                  // packed BF16 weights of the tensor-core forward
+    uint8_t *wimg = nullptr;                  // packed BF16 weight images of the tensor-core passes
+    MlpTrainBufs tb{};                        // tensor-core training scratch
+    int mode = 0;                             // SPEO_SURROGATE_BF16_SCREEN | SPEO_SURROGATE_BF16_TRAIN
     // screening scratch (grown on demand)
     long long scr_rows = 0;
     float *sH1 = nullptr, *sH2 = nullptr;
     long long trial_cap = 0;
     float *T = nullptr, *pred = nullptr, *sel = nullptr, *fsel = nullptr;
 
+    long long gstride() const { return (np + 3) & ~3; }  // partial-gradient vector stride (16-byte rows)
     float *W1() { return theta; }
     float *b1() { return theta + (size_t)h * din; }
     float *W2() { return b1() + h; }
@@ -456,7 +459,7 @@ int mlp_grad(Surrogate *S, cudaStream_t st, const float *Xraw, int n, int ldxraw
     // Weight and bias gradients are sums over the batch rows: split-K over chunks of kSplitRows
     // rows into the partial buffer (one full gradient vector per chunk), then one fixed-order sum.
     const int splits = (n + kSplitRows - 1) / kSplitRows;
-    const long long np = S->np;
+    const long long np = S->gstride();
     float *g = S->gpart;
     float *gW1 = g, *gb1 = gW1 + (size_t)h * din, *gW2 = gb1 + h, *gb2 = gW2 + (size_t)h * h, *gw3 = gb2 + h,
           *gb3 = gw3 + h;
@@ -471,7 +474,20 @@ int mlp_grad(Surrogate *S, cudaStream_t st, const float *Xraw, int n, int ldxraw
     // layer 1: gW1 = dZ1^T X', gb1 = 1^T dZ1 (X' standardised)
     if (int e = gemm<0>(st, S->dZ1, 1, h, X, ldx, 1, nullptr, gW1, din, nullptr, h, din, n, 1.f, splits, np)) return e;
     if (int e = gemm<0>(st, S->one, 0, 0, S->dZ1, h, 1, nullptr, gb1, h, nullptr, 1, h, n, 1.f, splits, np)) return e;
-    k_reduce_splits<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(S->gpart, splits, (int)np, S->grad);
+    k_reduce_splits<<<(unsigned)((S->np + 255) / 256), 256, 0, st>>>(S->gpart, splits, S->np, np, S->grad);
+    return check_launch("k_reduce_splits");
+}
+
+// One batch's gradient into S->grad: tensor cores (BF16 operands, FP32 accumulation) or FP32 SIMT.
+int grad_step(Surrogate *S, cudaStream_t st, const float *X, int n, int ldx, const float *T, bool bf16)
+{
+    if (!bf16) return mlp_grad(S, st, X, n, ldx, T);
+    if (int e = check_cuda(cudaMemsetAsync(S->loss, 0, sizeof(float), st), "memset loss")) return e;
+    if (int e = mlp_grad_bf16(S->theta, S->din, S->h, S->mu, S->isig, X, n, ldx, T, S->wimg, S->tb, S->gpart, S->loss,
+                              st))
+        return e;
+    const int splits = (n + kSplitRows - 1) / kSplitRows;
+    k_reduce_splits<<<(unsigned)((S->np + 255) / 256), 256, 0, st>>>(S->gpart, splits, S->np, S->gstride(), S->grad);
     return check_launch("k_reduce_splits");
 }
 
@@ -501,7 +517,7 @@ extern "C" int speo_surrogate_create(speo_surrogate **out, int din, int hidden, 
     e = e ? e : dalloc(&S->m, S->np);
     e = e ? e : dalloc(&S->v, S->np);
     e = e ? e : dalloc(&S->grad, S->np);
-    e = e ? e : dalloc(&S->gpart, (size_t)S->np * ((batch + kSplitRows - 1) / kSplitRows));
+    e = e ? e : dalloc(&S->gpart, (size_t)S->gstride() * ((batch + kSplitRows - 1) / kSplitRows));
     e = e ? e : dalloc(&S->AX, (size_t)archive_cap * S->lda);
     e = e ? e : dalloc(&S->AT, (size_t)archive_cap);
     e = e ? e : dalloc(&S->Xb, (size_t)batch * S->lda);
@@ -514,7 +530,15 @@ extern "C" int speo_surrogate_create(speo_surrogate **out, int din, int hidden, 
     e = e ? e : dalloc(&S->mu, (size_t)S->lda);
     e = e ? e : dalloc(&S->isig, (size_t)S->lda);
     e = e ? e : dalloc(&S->Xbn, (size_t)batch * S->lda);
-    if (mlp_bf16_supported(din, hidden)) e = e ? e : dalloc(&S->wimg, mlp_bf16_image_bytes(hidden));
+    if (mlp_bf16_supported(din, hidden)) {
+        const long long rp = ((long long)batch + 127) / 128 * 128;
+        S->tb.rp = rp;
+        e = e ? e : dalloc(&S->wimg, mlp_bf16_image_bytes(hidden));
+        e = e ? e : dalloc(&S->tb.xnT, (size_t)64 * rp);
+        for (uint16_t **p : {&S->tb.h1T, &S->tb.h2T, &S->tb.dz2T, &S->tb.dz1T}) e = e ? e : dalloc(p, (size_t)hidden * rp);
+        e = e ? e : dalloc(&S->tb.dy, (size_t)rp);
+        S->mode = SPEO_SURROGATE_BF16_SCREEN | SPEO_SURROGATE_BF16_TRAIN;
+    }
     if (e) { speo_surrogate_destroy(reinterpret_cast<speo_surrogate *>(S)); return e; }
     // He-style initialisation from Philox on the host side of the stream: uniform(-a, a)
     float *h_theta = new float[S->np];
@@ -563,6 +587,9 @@ extern "C" int speo_surrogate_destroy(speo_surrogate *sp)
                      S->isig, S->Xbn, S->Xn})
         if (p) cudaFree(p);
     if (S->wimg) cudaFree(S->wimg);
+    for (void *p : {(void *)S->tb.xnT, (void *)S->tb.h1T, (void *)S->tb.h2T, (void *)S->tb.dz2T, (void *)S->tb.dz1T,
+                    (void *)S->tb.dy})
+        if (p) cudaFree(p);
     delete S;
     return SPEO_OK;
 }
@@ -645,6 +672,36 @@ extern "C" int speo_surrogate_grad(speo_surrogate *sp, const float *X, int n, in
     return SPEO_OK;
 }
 
+extern "C" int speo_surrogate_grad_bf16(speo_surrogate *sp, const float *X, int n, int ldx, const float *T,
+                                        float *loss_out, void *stream)
+{
+    Surrogate *S = reinterpret_cast<Surrogate *>(sp);
+    if (!S || !X || !T || n < 1 || n > S->batch || ldx < S->din)
+        return fail(SPEO_ERR_INVALID_ARG, "speo_surrogate_grad_bf16: bad arguments");
+    if (!S->wimg) return fail(SPEO_ERR_UNSUPPORTED, "speo_surrogate_grad_bf16: din %d, hidden %d", S->din, S->h);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (int e = grad_step(S, st, X, n, ldx, T, true)) return e;
+    if (loss_out) {
+        float l = 0.f;
+        if (int e = check_cuda(cudaMemcpyAsync(&l, S->loss, sizeof(float), cudaMemcpyDeviceToHost, st), "loss")) return e;
+        if (int e = check_cuda(cudaStreamSynchronize(st), "loss sync")) return e;
+        *loss_out = l / n;
+    }
+    return SPEO_OK;
+}
+
+extern "C" int speo_surrogate_set_mode(speo_surrogate *sp, int mode)
+{
+    Surrogate *S = reinterpret_cast<Surrogate *>(sp);
+    if (!S || (mode & ~(SPEO_SURROGATE_BF16_SCREEN | SPEO_SURROGATE_BF16_TRAIN)))
+        return fail(SPEO_ERR_INVALID_ARG, "speo_surrogate_set_mode: bad arguments");
+    if (mode && !S->wimg)
+        return fail(SPEO_ERR_UNSUPPORTED, "speo_surrogate_set_mode: the tensor-core passes take din <= 64 and hidden "
+                                          "64 / 128 / 256 (din %d, hidden %d)", S->din, S->h);
+    S->mode = mode;
+    return SPEO_OK;
+}
+
 extern "C" int speo_surrogate_adam_step(speo_surrogate *sp, void *stream)
 {
     Surrogate *S = reinterpret_cast<Surrogate *>(sp);
@@ -686,7 +743,7 @@ extern "C" int speo_surrogate_train(speo_surrogate *sp, int steps, float *loss_o
             S->AX, S->lda, S->AT, S->count, n, make_uint2((uint32_t)S->seed, (uint32_t)(S->seed >> 32)),
             (uint32_t)S->step, S->Xb, S->Tb);
         if (int e = check_launch("k_archive_sample")) return e;
-        if (int e = mlp_grad(S, st, S->Xb, n, S->lda, S->Tb)) return e;
+        if (int e = grad_step(S, st, S->Xb, n, S->lda, S->Tb, (S->mode & SPEO_SURROGATE_BF16_TRAIN) != 0)) return e;
         if (int e = speo_surrogate_adam_step(sp, stream)) return e;
     }
     if (loss_out) {
@@ -744,7 +801,7 @@ extern "C" int speo_surrogate_generation(speo_surrogate *sp, const speo_segment 
     }
     if (int e = speo_surrogate_standardize(sp, pop_in, rows, ld, stream)) return e;
     if (int e = speo_make_trials(segs, items, n_items, dim_hi, k, pop_in, fit_in, S->T, d_gen, stream)) return e;
-    if (S->wimg) {  // screening on the tensor cores where the shape allows it
+    if (S->mode & SPEO_SURROGATE_BF16_SCREEN) {  // screening on the tensor cores
         if (int e = speo_surrogate_forward_bf16(sp, S->T, rows * k, ld, S->pred, stream)) return e;
     } else {
         if (int e = speo_surrogate_forward(sp, S->T, (int)(rows * k), ld, S->pred, stream)) return e;

@@ -108,6 +108,8 @@ SIGNATURES: dict[str, tuple] = {
     "speo_surrogate_params": (c_int, [c_void_p, c_void_p, c_void_p, POINTER(c_int)]),
     "speo_surrogate_forward": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, c_void_p]),
     "speo_surrogate_forward_bf16": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_void_p]),
+    "speo_surrogate_grad_bf16": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, POINTER(c_float), c_void_p]),
+    "speo_surrogate_set_mode": (c_int, [c_void_p, c_int]),
     "speo_surrogate_grad": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p, POINTER(c_float), c_void_p]),
     "speo_surrogate_adam_step": (c_int, [c_void_p, c_void_p]),
     "speo_surrogate_standardize": (c_int, [c_void_p, c_void_p, ctypes.c_longlong, c_int, c_void_p]),

@@ -181,6 +181,72 @@ def test_gradients_match_oracle(lib, oracle, cuda):
         s.close()
 
 
+def _grad_bf16_emulated(theta, din, h, X, t, scale):
+    """The tensor-core gradient with its roundings made explicit (BF16 at every tensor-core operand,
+    exact sums rounded to FP32 before each bias add); returns (mean loss, gradient)."""
+    f32, f64 = np.float32, np.float64
+    n = X.shape[0]
+    W1 = theta[: h * din].reshape(h, din)
+    o = h * din
+    b1 = theta[o:o + h]; o += h
+    W2 = theta[o:o + h * h].reshape(h, h); o += h * h
+    b2 = theta[o:o + h]; o += h
+    w3 = theta[o:o + h]; b3 = theta[o + h]
+    W1b, W2b = _bf16(W1).astype(f64), _bf16(W2).astype(f64)
+    xn = _bf16((X[:, :din] - f32(0)) * f32(scale)).astype(f64)
+    z1 = (xn @ W1b.T).astype(f32) + b1
+    h1f = np.maximum(z1, f32(0))
+    h1 = _bf16(h1f).astype(f64)
+    z2 = (h1 @ W2b.T).astype(f32) + b2
+    h2 = np.maximum(z2, f32(0))
+    y = h2.astype(f64) @ w3.astype(f64) + float(b3)
+    e = (y - t.astype(f64)).astype(f32)
+    dy = (e * f32(2.0 / n)).astype(f32)
+    dz2 = _bf16(np.where(z2 > 0, dy[:, None] * w3[None, :], f32(0)).astype(f32)).astype(f64)
+    dz1 = _bf16(np.where(h1f > 0, (dz2 @ W2b).astype(f32), f32(0))).astype(f64)
+    h2b = _bf16(h2).astype(f64)
+    g = np.concatenate([(dz1.T @ xn).ravel(), dz1.sum(0), (dz2.T @ h1).ravel(), dz2.sum(0),
+                        (dy.astype(f64)[:, None] * h2b).sum(0), [dy.astype(f64).sum()]])
+    return float(np.mean(e.astype(f64) ** 2)), g
+
+
+@pytest.mark.parametrize("din,h,n", [(50, 256, 1000), (50, 256, 4096), (10, 64, 300), (64, 128, 128)])
+def test_gradients_bf16_match_emulation(lib, oracle, cuda, din, h, n):
+    """tcgen05 gradient (BF16 operands, FP32 accumulation) against the same roundings in numpy,
+    and close to the FP64 oracle's exact gradient."""
+    import torch
+    from speo_gb300 import _lib
+
+    s = Surr(lib, din=din, h=h, batch=4096)
+    try:
+        rng = np.random.default_rng(n + h)
+        theta = (rng.normal(0, 1, s.n) * np.sqrt(2.0 / np.where(np.arange(s.n) < h * din, din, h))).astype(np.float32)
+        np_to_dev(s.theta_ptr, theta)
+        ldx = (din + 3) // 4 * 4
+        X = np.zeros((n, ldx), dtype=np.float32)
+        X[:, :din] = rng.uniform(-100, 100, (n, din))
+        t = rng.normal(2.0, 1.0, n).astype(np.float32)
+        tX, tt = torch.from_numpy(X).cuda(), torch.from_numpy(t).cuda()
+        loss = ctypes.c_float()
+        _lib.check(lib.speo_surrogate_grad_bf16(s.p, tX.data_ptr(), n, ldx, tt.data_ptr(), ctypes.byref(loss), None),
+                   "grad_bf16")
+        g = s.grad()
+        ref_loss, ref = _grad_bf16_emulated(theta, din, h, X, t, SCALE)
+        exact_loss, exact = oracle.mlp_loss_grad(theta, din, h, SCALE, X[:, :din], t)
+        assert loss.value == pytest.approx(ref_loss, rel=1e-4)
+        o = 0
+        for name, size in [("W1", h * din), ("b1", h), ("W2", h * h), ("b2", h), ("w3", h), ("b3", 1)]:
+            gb, rb, xb = g[o:o + size], ref[o:o + size], exact[o:o + size]
+            tol = 5e-3 * np.abs(rb).max() + 1e-7
+            assert np.abs(gb - rb).max() <= tol, (name, np.abs(gb - rb).max(), tol)
+            # BF16 rounding only: the direction of each block agrees with the exact gradient
+            cos = float(np.dot(gb, xb) / (np.linalg.norm(gb) * np.linalg.norm(xb) + 1e-30))
+            assert cos > 0.99, (name, cos)
+            o += size
+    finally:
+        s.close()
+
+
 def test_adam_matches_oracle(lib, oracle, cuda):
     from speo_gb300 import _lib
 
