@@ -425,9 +425,15 @@ def bench_config3(L, dev, torch, flush) -> dict:
             "tile_rows": best}
 
 
-def _c4_run(L, dev, torch, func: int, mode: str, max_gens: int, log_every: int = 10, stop_at: float | None = None):
+C4_TRAIN_STEPS = 48   # Adam steps per generation: 48 x 4096 = 6 passes over a generation's 32768 new rows
+C4_EXPLORE = 0.05     # fraction of targets that take a uniformly drawn trial instead of the screened one
+
+
+def _c4_run(L, dev, torch, func: int, mode: str, max_gens: int, log_every: int = 10, stop_at: float | None = None,
+            train_steps: int = 16, explore: float = 0.25, train_k: int = 8, use_graph: bool = True):
     """One config-4 run (plain or surrogate-screened) logging the FP64 best error every
-    `log_every` generations; stops early once the error reaches `stop_at`."""
+    `log_every` generations; stops early once the error reaches `stop_at`. Blocks of `log_every`
+    generations replay one CUDA graph after the first (eager) block."""
     import ctypes as C
 
     from speo_gb300 import _lib
@@ -441,24 +447,40 @@ def _c4_run(L, dev, torch, func: int, mode: str, max_gens: int, log_every: int =
         surr = C.c_void_p()
         _lib.check(L.speo_surrogate_create(C.byref(surr), 50, 256, 1 << 20, 4096, 1e-3, 0.01, 4242),
                    "speo_surrogate_create")
-    curve, t_total = [], 0.0
+    assert log_every % 2 == 0 and 50 % log_every == 0
+
+    def block():  # log_every generations (an even number: the double buffers end where they began)
+        if mode == "plain":
+            if tab.epoch_fits():
+                tab.epoch(log_every)
+            else:
+                for _ in range(log_every):
+                    tab.generation()
+        else:
+            for _ in range(log_every):
+                tab.surrogate_generation(surr, k=train_k, train_steps=train_steps, explore=explore)
+
+    curve, t_total, graph = [], 0.0, None
     try:
         for g0 in range(0, max_gens, log_every):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record()
-            for g in range(g0, g0 + log_every):
-                if mode == "plain":
-                    if tab.epoch_fits():
-                        tab.epoch(1)
-                    else:
-                        tab.generation()
-                else:
-                    tab.surrogate_generation(surr, k=8, train_steps=16, explore=0.25)
-                if (g + 1) % 50 == 0:
-                    tab.migrate(5)
+            if graph is None:
+                block()   # first block eagerly: scratch allocation, archive seeding
+            else:
+                graph.replay()
+            if (g0 + log_every) % 50 == 0:
+                tab.migrate(5)
             b.record()
             torch.cuda.synchronize()
             t_total += a.elapsed_time(b) / 1e3
+            if graph is None and use_graph:  # later blocks replay one CUDA graph (not executed by capture)
+                graph = torch.cuda.CUDAGraph()
+                cs = torch.cuda.Stream()
+                cs.wait_stream(torch.cuda.current_stream())
+                with torch.cuda.stream(cs), torch.cuda.graph(graph, stream=cs):
+                    block()
+                torch.cuda.current_stream().wait_stream(cs)
             rows, errs = tab.best_f64()
             curve.append({"gen": g0 + log_every, "exact_evals": (g0 + log_every) * tab.rows, "wall_s": t_total,
                           "best_err": float(errs.min().item())})
@@ -480,20 +502,22 @@ def _c4_run(L, dev, torch, func: int, mode: str, max_gens: int, log_every: int =
 
 def bench_config4(L, dev, torch, gens: int) -> dict:
     """Config 4: 128 islands x 256, D = 50. Plain DE against the surrogate-screened DE (MLP
-    50-256-256-1 screening on the tensor cores in BF16, archive 2^20, Adam lr 1e-3, batch 4096,
-    k = 8 trials per target, 16 Adam steps per generation, 25 % exploration picks); ring migration
+    50-256-256-1, screening and training on the tensor cores in BF16 with FP32 accumulation,
+    archive 2^20, Adam lr 1e-3, batch 4096, k = 8 trials per target, C4_TRAIN_STEPS Adam steps per
+    generation, C4_EXPLORE exploration picks; blocks of 10 generations replay a CUDA graph); ring migration
     of 5 every 50 generations in both, both spend 32768 exact evaluations per generation. Best
     FP64 error every 10 generations; wall time from CUDA events around the generations only.
     (a) rotated Rastrigin for `gens` generations; (b) the rotated sphere of the same shape run to
     an error of 1e-8 (capped), which gives the exact evaluations each method needs to get there."""
     from speo_gb300 import _lib
 
-    out = {"workload": "128 islands x P=256, D=50; surrogate MLP 50-256-256-1 (BF16 tcgen05 screening, "
-                       "FP32 training), k=8"}
+    out = {"workload": "128 islands x P=256, D=50; surrogate MLP 50-256-256-1 (BF16 tcgen05 screening and "
+                       "training), k=8", "train_steps_per_gen": C4_TRAIN_STEPS, "explore": C4_EXPLORE}
     ras = {"objective": "rotated Rastrigin", "generations": gens}
     curves = {}
     for mode in ("plain", "surrogate"):
-        ras[mode], curves[mode] = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, mode, gens)
+        ras[mode], curves[mode] = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, mode, gens,
+                                          train_steps=C4_TRAIN_STEPS, explore=C4_EXPLORE)
     target = ras["plain"]["final_err"]
     hit = next((c for c in curves["surrogate"] if c["best_err"] <= target), None)
     ras["surrogate_reaches_plain_final_error"] = None if hit is None else {
@@ -502,7 +526,11 @@ def bench_config4(L, dev, torch, gens: int) -> dict:
     out["rastrigin"] = ras
     sph = {"objective": "rotated sphere", "target_err": 1e-8}
     sph["plain"], _ = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "plain", 4000, stop_at=1e-8)
-    sph["surrogate"], _ = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8)
+    sph["surrogate"], _ = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8,
+                                  train_steps=C4_TRAIN_STEPS, explore=C4_EXPLORE)
+    light, _ = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8, train_steps=16,
+                       explore=C4_EXPLORE)
+    sph["surrogate_16_steps"] = {k: v for k, v in light.items() if k != "curve"}
     ep, es = sph["plain"]["exact_evals_to_1e-8"], sph["surrogate"]["exact_evals_to_1e-8"]
     wp, ws = sph["plain"]["wall_s_to_1e-8"], sph["surrogate"]["wall_s_to_1e-8"]
     sph["exact_evals_ratio_plain_over_surrogate"] = ep / es if ep and es else None

@@ -18,6 +18,7 @@ constexpr int kBoundIters = 64;     // bound of the reflection loop
 constexpr uint32_t kTagIdx = 1u;
 constexpr uint32_t kTagCr = 2u;
 constexpr uint32_t kTagInit = 3u;
+constexpr uint32_t kTagSample = 4u;  // surrogate training batches
 
 // ---------------------------------------------------------------------------------------
 // Philox-4x32-10 (Salmon et al., SC'11). Ten rounds, Weyl key schedule.

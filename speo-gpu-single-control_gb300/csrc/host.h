@@ -28,6 +28,22 @@ struct RngState {
 };
 static_assert(sizeof(RngState) == SPEO_RNG_STATE_BYTES, "rng state size");
 
+// Mutable surrogate state kept on the device, so that captured generations replay correctly.
+struct SurrDev {
+    long long head, count;  // archive ring head and fill
+    uint32_t step;          // Adam steps taken
+    uint32_t done;          // blocks of the running Adam launch that have finished
+    float c1, c2;           // bias corrections 1 - beta^t of the next step, t = step + 1
+};
+// Training batch drawn from the archive inside the gradient kernel: row i of the batch is archive
+// slot philox({i/4, step, 0, 4}, key)[i%4] mod count (rows AX[slot][0..din), target AT[slot]).
+struct MlpArchive {
+    const float *AX, *AT;
+    int lda;
+    const SurrDev *st;
+    uint32_t key0, key1;
+};
+
 // Surrogate MLP forward on the tensor cores (BF16 operands, FP32 accumulation), mlp_tc.cu.
 // theta: W1 (h x din) | b1 | W2 (h x h) | b2 | w3 | b3; img: mlp_bf16_image_bytes(h) bytes of
 // device scratch for the packed weights.
@@ -44,9 +60,14 @@ struct MlpTrainBufs {
     float *dy;
     long long rp;
 };
+// X/T: the batch rows, or null with `arch` set to draw them from the archive. pack_weights: refresh
+// the BF16 weight images from theta first (the Adam kernel keeps them current between steps).
 int mlp_grad_bf16(const float *theta, int din, int h, const float *mu, const float *isig, const float *X, int n,
-                  int ldx, const float *T, uint8_t *img, const MlpTrainBufs &b, float *gpart, float *loss,
-                  cudaStream_t st);
+                  int ldx, const float *T, const MlpArchive *arch, uint8_t *img, bool pack_weights,
+                  const MlpTrainBufs &b, float *gpart, float *loss, cudaStream_t st);
+// Byte offsets of the BF16 weight images inside `img`: W1 (h x 64), W2 (h x h), W2^T (h x h).
+size_t mlp_img_w2_offset(int h);
+size_t mlp_img_w2t_offset(int h);
 
 }  // namespace speo
 

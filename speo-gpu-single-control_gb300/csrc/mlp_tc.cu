@@ -275,7 +275,8 @@ int pack(const float *theta, int din, uint8_t *img, cudaStream_t st, int with_t 
 struct TrainArgs {
     const uint8_t *img;  // W1 | W2 | W2^T images
     const float *b1, *b2, *w3, *b3, *mu, *isig;
-    const float *X, *T;
+    const float *X, *T;  // batch rows, or null: drawn from the archive (arch)
+    MlpArchive arch;
     int n, ldx, din, vec;
     long long rp;
     float two_over_n;
@@ -325,6 +326,23 @@ __global__ void __launch_bounds__(256, 1) k_mlp_train_tc(TrainArgs a)
     }
     const long long r0 = (long long)blockIdx.x * kRows;
     const long long rp = a.rp;
+    // this thread's batch row (tid % 128) and, when drawn from the archive, its slot
+    const float *xrow = nullptr, *trow = nullptr;
+    {
+        const long long gr = r0 + (tid % kRows);
+        if (gr < a.n) {
+            if (a.X) {
+                xrow = a.X + gr * a.ldx;
+                trow = a.T + gr;
+            } else {
+                const uint4 w = philox(make_uint4((uint32_t)(gr >> 2), a.arch.st->step, 0u, kTagSample),
+                                       make_uint2(a.arch.key0, a.arch.key1));
+                const long long slot = (long long)(pick(w, (uint32_t)(gr & 3)) % (uint32_t)a.arch.st->count);
+                xrow = a.arch.AX + slot * a.arch.lda;
+                trow = a.arch.AT + slot;
+            }
+        }
+    }
     // ---- A1 and x'^T (lanes = consecutive rows: coalesced transposed writes) --------------------
 #pragma unroll
     for (int j = 0; j < kRows * (kK1 / 8) / 256; ++j) {
@@ -335,7 +353,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_train_tc(TrainArgs a)
 #pragma unroll
         for (int e = 0; e < 8; ++e) v[e] = 0.f;
         if (gr < a.n) {
-            const float *xr = a.X + gr * a.ldx;
+            const float *xr = xrow;
             if (a.vec && k0 + 8 <= a.din) {
                 const float4 p = *reinterpret_cast<const float4 *>(xr + k0);
                 const float4 q = *reinterpret_cast<const float4 *>(xr + k0 + 4);
@@ -445,7 +463,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_train_tc(TrainArgs a)
         if (tid < kRows) {
             const long long gr = r0 + tid;
             float e = 0.f;
-            if (gr < a.n) e = __fsub_rn(__fadd_rn(__fadd_rn(red[tid], red[kRows + tid]), a.b3[0]), a.T[gr]);
+            if (gr < a.n) e = __fsub_rn(__fadd_rn(__fadd_rn(red[tid], red[kRows + tid]), a.b3[0]), *trow);
             const float d = __fmul_rn(e, a.two_over_n);
             dys[tid] = d;
             a.dy[gr] = d;
@@ -744,10 +762,14 @@ int mlp_forward_bf16(const float *theta, int din, int h, const float *mu, const 
     }
 }
 
+size_t mlp_img_w2_offset(int h) { return w1_bytes(h); }
+size_t mlp_img_w2t_offset(int h) { return w1_bytes(h) + w2_bytes(h); }
+
 int mlp_grad_bf16(const float *theta, int din, int h, const float *mu, const float *isig, const float *X, int n,
-                  int ldx, const float *T, uint8_t *img, const MlpTrainBufs &b, float *gpart, float *loss,
-                  cudaStream_t st)
+                  int ldx, const float *T, const MlpArchive *arch, uint8_t *img, bool pack_weights,
+                  const MlpTrainBufs &b, float *gpart, float *loss, cudaStream_t st)
 {
+    if (!X && !arch) return fail(SPEO_ERR_INVALID_ARG, "mlp gradient: no batch");
     if (!mlp_bf16_supported(din, h)) return fail(SPEO_ERR_UNSUPPORTED, "mlp gradient: din %d, hidden %d", din, h);
     if (n < 1 || (long long)n > b.rp || (b.rp % kRows) != 0)
         return fail(SPEO_ERR_INVALID_ARG, "mlp gradient: %d rows, %lld padded", n, b.rp);
@@ -757,15 +779,17 @@ int mlp_grad_bf16(const float *theta, int din, int h, const float *mu, const flo
     const float *b2 = b1 + h + (size_t)h * h;
     const float *w3 = b2 + h;
     const int splits = (int)((n + kRows - 1) / kRows);
-    TrainArgs ta{img, b1, b2, w3, w3 + h, mu, isig, X, T, n, ldx, din,
-                 (((uintptr_t)X & 15) == 0 && (ldx & 3) == 0) ? 1 : 0, b.rp, 2.f / (float)n,
+    const MlpArchive none{nullptr, nullptr, 0, nullptr, 0u, 0u};
+    const int vec = X ? ((((uintptr_t)X & 15) == 0 && (ldx & 3) == 0) ? 1 : 0)
+                      : ((((uintptr_t)arch->AX & 15) == 0 && (arch->lda & 3) == 0) ? 1 : 0);
+    TrainArgs ta{img, b1, b2, w3, w3 + h, mu, isig, X, T, X ? none : *arch, n, ldx, din, vec, b.rp, 2.f / (float)n,
                  b.xnT, b.h1T, b.h2T, b.dz2T, b.dz1T, b.dy, loss};
     WgradArgs wa{b.xnT, b.h1T, b.dz2T, b.dz1T, b.rp, din, gs, gpart};
     int e = 0;
     switch (h) {
-    case 64: e = pack<64>(theta, din, img, st, 1); return e ? e : launch_train<64>(ta, wa, splits, st);
-    case 128: e = pack<128>(theta, din, img, st, 1); return e ? e : launch_train<128>(ta, wa, splits, st);
-    default: e = pack<256>(theta, din, img, st, 1); return e ? e : launch_train<256>(ta, wa, splits, st);
+    case 64: e = pack_weights ? pack<64>(theta, din, img, st, 1) : 0; return e ? e : launch_train<64>(ta, wa, splits, st);
+    case 128: e = pack_weights ? pack<128>(theta, din, img, st, 1) : 0; return e ? e : launch_train<128>(ta, wa, splits, st);
+    default: e = pack_weights ? pack<256>(theta, din, img, st, 1) : 0; return e ? e : launch_train<256>(ta, wa, splits, st);
     }
 }
 

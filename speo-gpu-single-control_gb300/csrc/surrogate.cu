@@ -15,13 +15,13 @@
 
 #include "eval_simt.cuh"
 #include "host.h"
+#include "tcgen05.cuh"
 
 SPEO_DEFINE_DEVERR(speo_deverr_surrogate)
 
 namespace speo {
 namespace {
 
-constexpr uint32_t kTagSample = 4u;
 constexpr float kTargetFloor = 1e-8f;  // target = log(f + floor)
 constexpr int kSplitRows = 128;        // batch rows per split-K chunk of the weight gradients
 
@@ -153,42 +153,80 @@ __global__ void k_head_back(const float *dy, const float *w3, const float *Z2, f
     dZ2[t] = Z2[t] > 0.f ? dy[i] * w3[j] : 0.f;
 }
 
-// Adam (Kingma & Ba, 2015); c1 = 1 - beta1^t, c2 = 1 - beta2^t computed on the host.
-__global__ void k_adam(float *theta, float *m, float *v, const float *g, int n, float lr, float b1, float b2, float eps,
-                       float c1, float c2)
+__global__ void k_archive_advance(SurrDev *st, long long n, long long cap)
+{
+    st->head = (st->head + n) % cap;
+    st->count = st->count + n < cap ? st->count + n : cap;
+}
+
+// Adam (Kingma & Ba, 2015) at step t = st->step + 1 with the bias corrections st->c1, st->c2.
+// The gradient is the fixed-order sum of `splits` partial vectors (stride pstride). With `img`,
+// the BF16 weight images of the tensor-core passes are refreshed from the new parameters. The last
+// block to finish advances the step and the next step's bias corrections, so a captured sequence
+// of steps replays correctly.
+__global__ void k_adam(float *theta, float *m, float *v, const float *P, int splits, long long pstride, int n,
+                       float lr, float b1, float b2, float eps, SurrDev *st, uint8_t *img, int din, int h)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float gi = g[i];
-    const float mi = b1 * m[i] + (1.f - b1) * gi;
-    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
-    m[i] = mi;
-    v[i] = vi;
-    theta[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    const float c1 = st->c1, c2 = st->c2;
+    if (i < n) {
+        float gi = 0.f;
+        for (int z = 0; z < splits; ++z) gi += P[(size_t)z * pstride + i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float th = theta[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        theta[i] = th;
+        if (img) {
+            const long long o2 = (long long)h * din + h;
+            const __nv_bfloat16 hb = __float2bfloat16_rn(th);
+            if (i < h * din) {
+                *reinterpret_cast<__nv_bfloat16 *>(img + tc::kmajor_offset(i / din, i % din, 64)) = hb;
+            } else if (i >= o2 && i < o2 + (long long)h * h) {
+                const int a = (int)((i - o2) / h), b = (int)((i - o2) % h);
+                *reinterpret_cast<__nv_bfloat16 *>(img + (size_t)h * 64 * 2 + tc::kmajor_offset(a, b, h)) = hb;
+                *reinterpret_cast<__nv_bfloat16 *>(img + (size_t)h * 64 * 2 + (size_t)h * h * 2 +
+                                                   tc::kmajor_offset(b, a, h)) = hb;
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&st->done, 1u) == gridDim.x - 1) {
+            const uint32_t s = st->step + 1u;
+            st->step = s;
+            st->c1 = (float)(1.0 - pow((double)b1, (double)s + 1.0));
+            st->c2 = (float)(1.0 - pow((double)b2, (double)s + 1.0));
+            st->done = 0u;
+        }
+    }
 }
+
 
 // Archive append: rows [0, n) of X (stride ldx, din used) and their exact fitness at slots
 // (head + i) mod cap, target = log(f + floor).
 __global__ void k_archive_append(const float *X, int ldx, const float *f, int n, int din, float *AX, int lda, float *AT,
-                                 long long head, long long cap)
+                                 const SurrDev *st, long long cap)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)n * lda) return;
     const int i = (int)(t / lda), d = (int)(t - (long long)i * lda);
-    const long long slot = (head + i) % cap;
+    const long long slot = (st->head + i) % cap;
     AX[slot * lda + d] = d < din ? X[(size_t)i * ldx + d] : 0.f;
     if (d == 0) AT[slot] = logf(fmaxf(f[i], 0.f) + kTargetFloor);
 }
 
-// Batch sampling: index i of step `step` is philox({i/4, step, 0, SAMPLE})[i%4] mod count.
-__global__ void k_archive_sample(const float *AX, int lda, const float *AT, long long count, int batch, uint2 key,
-                                 uint32_t step, float *X, float *T)
+// Batch sampling: index i at Adam step `step` is philox({i/4, step, 0, SAMPLE})[i%4] mod count.
+__global__ void k_archive_sample(const float *AX, int lda, const float *AT, const SurrDev *st, int batch, uint2 key,
+                                 float *X, float *T)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)batch * lda) return;
     const int i = (int)(t / lda), d = (int)(t - (long long)i * lda);
-    const uint4 w = philox(make_uint4((uint32_t)(i >> 2), step, 0u, kTagSample), key);
-    const long long slot = (long long)(pick(w, (uint32_t)(i & 3)) % (uint32_t)count);
+    const uint4 w = philox(make_uint4((uint32_t)(i >> 2), st->step, 0u, kTagSample), key);
+    const long long slot = (long long)(pick(w, (uint32_t)(i & 3)) % (uint32_t)st->count);
     X[t] = AX[slot * lda + d];
     if (d == 0) T[i] = AT[slot];
 }
@@ -396,7 +434,9 @@ struct Surrogate {
     long long cap, count = 0, head = 0;
     float lr, in_scale, beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
     uint64_t seed;
-    int step = 0;
+    int step = 0;                             // host mirrors of the device state (exact: advanced in
+                                              // the same order); used for sizes and first-call checks
+    SurrDev *dst = nullptr;                   // device state: archive head / count, Adam step
     float *theta = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr;
     float *AX = nullptr, *AT = nullptr;       // archive
     float *Xb = nullptr, *Tb = nullptr;       // training batch
@@ -478,17 +518,31 @@ int mlp_grad(Surrogate *S, cudaStream_t st, const float *Xraw, int n, int ldxraw
     return check_launch("k_reduce_splits");
 }
 
-// One batch's gradient into S->grad: tensor cores (BF16 operands, FP32 accumulation) or FP32 SIMT.
-int grad_step(Surrogate *S, cudaStream_t st, const float *X, int n, int ldx, const float *T, bool bf16)
+// One batch's gradient on the tensor cores: partial vectors per 128-row chunk into S->gpart, summed
+// into S->grad when `reduce` (the training loop lets the Adam kernel sum them instead). The batch is
+// X/T, or drawn from the archive inside the kernel when X is null.
+int grad_bf16(Surrogate *S, cudaStream_t st, const float *X, int n, int ldx, const float *T, bool pack_weights,
+              bool reduce)
 {
-    if (!bf16) return mlp_grad(S, st, X, n, ldx, T);
     if (int e = check_cuda(cudaMemsetAsync(S->loss, 0, sizeof(float), st), "memset loss")) return e;
-    if (int e = mlp_grad_bf16(S->theta, S->din, S->h, S->mu, S->isig, X, n, ldx, T, S->wimg, S->tb, S->gpart, S->loss,
-                              st))
+    const MlpArchive arch{S->AX, S->AT, S->lda, S->dst, (uint32_t)S->seed, (uint32_t)(S->seed >> 32)};
+    if (int e = mlp_grad_bf16(S->theta, S->din, S->h, S->mu, S->isig, X, n, ldx, T, X ? nullptr : &arch, S->wimg,
+                              pack_weights, S->tb, S->gpart, S->loss, st))
         return e;
+    if (!reduce) return SPEO_OK;
     const int splits = (n + kSplitRows - 1) / kSplitRows;
     k_reduce_splits<<<(unsigned)((S->np + 255) / 256), 256, 0, st>>>(S->gpart, splits, S->np, S->gstride(), S->grad);
     return check_launch("k_reduce_splits");
+}
+
+// One Adam step from `splits` partial gradient vectors (stride pstride); refreshes the BF16 weight
+// images when `img` is set.
+int adam(Surrogate *S, cudaStream_t st, const float *P, int splits, long long pstride, uint8_t *img)
+{
+    k_adam<<<(S->np + 255) / 256, 256, 0, st>>>(S->theta, S->m, S->v, P, splits, pstride, S->np, S->lr, S->beta1,
+                                                S->beta2, S->eps, S->dst, img, S->din, S->h);
+    S->step += 1;
+    return check_launch("k_adam");
 }
 
 template <typename T>
@@ -517,6 +571,13 @@ extern "C" int speo_surrogate_create(speo_surrogate **out, int din, int hidden, 
     e = e ? e : dalloc(&S->m, S->np);
     e = e ? e : dalloc(&S->v, S->np);
     e = e ? e : dalloc(&S->grad, S->np);
+    e = e ? e : dalloc(&S->dst, 1);
+    if (!e) {
+        SurrDev d0{};
+        d0.c1 = (float)(1.0 - (double)S->beta1);
+        d0.c2 = (float)(1.0 - (double)S->beta2);
+        e = check_cuda(cudaMemcpy(S->dst, &d0, sizeof d0, cudaMemcpyHostToDevice), "surrogate state");
+    }
     e = e ? e : dalloc(&S->gpart, (size_t)S->gstride() * ((batch + kSplitRows - 1) / kSplitRows));
     e = e ? e : dalloc(&S->AX, (size_t)archive_cap * S->lda);
     e = e ? e : dalloc(&S->AT, (size_t)archive_cap);
@@ -587,6 +648,7 @@ extern "C" int speo_surrogate_destroy(speo_surrogate *sp)
                      S->isig, S->Xbn, S->Xn})
         if (p) cudaFree(p);
     if (S->wimg) cudaFree(S->wimg);
+    if (S->dst) cudaFree(S->dst);
     for (void *p : {(void *)S->tb.xnT, (void *)S->tb.h1T, (void *)S->tb.h2T, (void *)S->tb.dz2T, (void *)S->tb.dz1T,
                     (void *)S->tb.dy})
         if (p) cudaFree(p);
@@ -680,7 +742,7 @@ extern "C" int speo_surrogate_grad_bf16(speo_surrogate *sp, const float *X, int 
         return fail(SPEO_ERR_INVALID_ARG, "speo_surrogate_grad_bf16: bad arguments");
     if (!S->wimg) return fail(SPEO_ERR_UNSUPPORTED, "speo_surrogate_grad_bf16: din %d, hidden %d", S->din, S->h);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (int e = grad_step(S, st, X, n, ldx, T, true)) return e;
+    if (int e = grad_bf16(S, st, X, n, ldx, T, true, true)) return e;
     if (loss_out) {
         float l = 0.f;
         if (int e = check_cuda(cudaMemcpyAsync(&l, S->loss, sizeof(float), cudaMemcpyDeviceToHost, st), "loss")) return e;
@@ -706,12 +768,7 @@ extern "C" int speo_surrogate_adam_step(speo_surrogate *sp, void *stream)
 {
     Surrogate *S = reinterpret_cast<Surrogate *>(sp);
     if (!S) return fail(SPEO_ERR_INVALID_ARG, "speo_surrogate_adam_step: null");
-    S->step += 1;
-    const float c1 = (float)(1.0 - std::pow((double)S->beta1, S->step));
-    const float c2 = (float)(1.0 - std::pow((double)S->beta2, S->step));
-    k_adam<<<(S->np + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(S->theta, S->m, S->v, S->grad, S->np,
-                                                                              S->lr, S->beta1, S->beta2, S->eps, c1, c2);
-    return check_launch("k_adam");
+    return adam(S, static_cast<cudaStream_t>(stream), S->grad, 1, 0, S->wimg);
 }
 
 extern "C" int speo_surrogate_archive_append(speo_surrogate *sp, const float *X, int n, int ldx, const float *f,
@@ -721,15 +778,20 @@ extern "C" int speo_surrogate_archive_append(speo_surrogate *sp, const float *X,
     if (!S || !X || !f || n < 0 || ldx < S->din) return fail(SPEO_ERR_INVALID_ARG, "speo_surrogate_archive_append: bad arguments");
     if (n == 0) return SPEO_OK;
     const long long total = (long long)n * S->lda;
-    k_archive_append<<<(unsigned)((total + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        X, ldx, f, n, S->din, S->AX, S->lda, S->AT, S->head, S->cap);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    k_archive_append<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(X, ldx, f, n, S->din, S->AX, S->lda, S->AT,
+                                                                      S->dst, S->cap);
+    if (int e = check_launch("k_archive_append")) return e;
+    k_archive_advance<<<1, 1, 0, st>>>(S->dst, n, S->cap);
     S->head = (S->head + n) % S->cap;
     S->count = S->count + n < S->cap ? S->count + n : S->cap;
-    return check_launch("k_archive_append");
+    return check_launch("k_archive_advance");
 }
 
 // `steps` Adam steps on batches sampled from the archive; the mean batch loss of the last step
-// goes to *loss_out when non-null (synchronises).
+// goes to *loss_out when non-null (synchronises). The batch holds min(archive rows, batch) rows
+// (drawn with replacement from the rows present when the step runs); under stream capture that
+// size is the one at capture time.
 extern "C" int speo_surrogate_train(speo_surrogate *sp, int steps, float *loss_out, void *stream)
 {
     Surrogate *S = reinterpret_cast<Surrogate *>(sp);
@@ -737,14 +799,20 @@ extern "C" int speo_surrogate_train(speo_surrogate *sp, int steps, float *loss_o
     if (S->count == 0 || steps == 0) return SPEO_OK;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int n = (int)(S->count < S->batch ? S->count : S->batch);
+    const bool bf16 = (S->mode & SPEO_SURROGATE_BF16_TRAIN) != 0;
     for (int i = 0; i < steps; ++i) {
-        const long long total = (long long)n * S->lda;
-        k_archive_sample<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(
-            S->AX, S->lda, S->AT, S->count, n, make_uint2((uint32_t)S->seed, (uint32_t)(S->seed >> 32)),
-            (uint32_t)S->step, S->Xb, S->Tb);
-        if (int e = check_launch("k_archive_sample")) return e;
-        if (int e = grad_step(S, st, S->Xb, n, S->lda, S->Tb, (S->mode & SPEO_SURROGATE_BF16_TRAIN) != 0)) return e;
-        if (int e = speo_surrogate_adam_step(sp, stream)) return e;
+        if (bf16) {  // batch drawn inside the gradient kernel; Adam sums the chunk partials
+            if (int e = grad_bf16(S, st, nullptr, n, S->lda, nullptr, i == 0, false)) return e;
+            if (int e = adam(S, st, S->gpart, (n + kSplitRows - 1) / kSplitRows, S->gstride(), S->wimg)) return e;
+        } else {
+            const long long total = (long long)n * S->lda;
+            k_archive_sample<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(
+                S->AX, S->lda, S->AT, S->dst, n, make_uint2((uint32_t)S->seed, (uint32_t)(S->seed >> 32)), S->Xb,
+                S->Tb);
+            if (int e = check_launch("k_archive_sample")) return e;
+            if (int e = mlp_grad(S, st, S->Xb, n, S->lda, S->Tb)) return e;
+            if (int e = adam(S, st, S->grad, 1, 0, nullptr)) return e;
+        }
     }
     if (loss_out) {
         float l = 0.f;

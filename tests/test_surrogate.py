@@ -378,3 +378,46 @@ def test_surrogate_beats_plain_de_at_equal_exact_evaluations(lib, cuda):
         print(f"rastrigin seed {seed}: plain {_run(lib, cuda, False, gens, seed, func=9):.3e}, "
               f"screened {_run(lib, cuda, True, gens, seed, func=9):.3e}")
     assert np.median(ratios) > 10.0, ratios
+
+
+def test_surrogate_generation_replays_from_a_cuda_graph(lib, cuda):
+    """The archive ring head and fill and the Adam step counter live on the device, so generations
+    captured once in a CUDA graph and replayed give bit-identical populations, fitness and network
+    parameters to the same generations run eagerly (the archive wraps during the run)."""
+    import torch
+
+    tabs, surrs = [], []
+    for _ in range(2):
+        tab = _islands(cuda, 8, 64, 10, func=31, seed=5)
+        tab.init_population()
+        tabs.append(tab)
+        surrs.append(Surr(lib, din=10, h=64, cap=4096, batch=1024, lr=3e-3, seed=5))
+    try:
+        def gen(i):
+            tabs[i].surrogate_generation(surrs[i].p, k=8, train_steps=4, explore=0.25)
+
+        for i in range(2):       # eager: scratch sizing and archive seeding
+            gen(i)
+            gen(i)
+        for _ in range(6):
+            gen(0)
+        g = torch.cuda.CUDAGraph()
+        cs = torch.cuda.Stream()
+        cs.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(cs), torch.cuda.graph(g, stream=cs):
+            gen(1)
+            gen(1)
+        torch.cuda.current_stream().wait_stream(cs)
+        for _ in range(3):
+            g.replay()
+        torch.cuda.synchronize()
+        a, b = tabs[0], tabs[1]
+        assert a.cur == b.cur
+        assert torch.equal(a.pop[a.cur], b.pop[b.cur])
+        assert torch.equal(a.fit[a.cur], b.fit[b.cur])
+        assert np.array_equal(surrs[0].theta(), surrs[1].theta())
+        assert int(a.gen[0].item()) == int(b.gen[0].item())
+    finally:
+        for s_ in surrs:
+            s_.close()
+
