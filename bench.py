@@ -253,6 +253,7 @@ def bench_speo(args) -> dict:
         out["config2_precision"] = bench_config2(L, dev, torch, flush)
         out["config3_batched"] = bench_config3(L, dev, torch, flush)
         out["config4_surrogate_vs_plain"] = bench_config4(L, dev, torch, args.c4_gens)
+        out["surrogate_mlp"] = bench_mlp(L, dev, torch)
     if not args.no_e2e:
         out["e2e"] = bench_e2e(L, dev, torch, args)
     if rank == 0 and not args.no_cpu:
@@ -539,6 +540,56 @@ def bench_config4(L, dev, torch, gens: int) -> dict:
     return out
 
 
+def bench_mlp(L, dev, torch, steps: int = 16) -> dict:
+    """The surrogate network's kernels at config 4's shapes (MLP 50-256-256-1): the tcgen05 screening
+    forward over 262,144 trials (8 per target, 32,768 targets) and `steps` tcgen05 training steps on
+    batches of 4096 drawn from an archive holding 32,768 rows; CUDA events, medians of 5."""
+    import ctypes as C
+
+    from speo_gb300 import _lib
+
+    s = C.c_void_p()
+    _lib.check(L.speo_surrogate_create(C.byref(s), 50, 256, 1 << 20, 4096, 1e-3, 0.01, 4242), "speo_surrogate_create")
+    st = torch.cuda.current_stream().cuda_stream
+    try:
+        g = torch.Generator(device=dev).manual_seed(7)
+        X = (torch.rand(32768, 52, device=dev, generator=g) * 200 - 100)
+        X[:, 50:] = 0
+        f = torch.rand(32768, device=dev, generator=g) * 1e4
+        _lib.check(L.speo_surrogate_archive_append(s, X.data_ptr(), 32768, 52, f.data_ptr(), st), "append")
+        T = (torch.rand(262144, 52, device=dev, generator=g) * 200 - 100)
+        T[:, 50:] = 0
+        y = torch.empty(262144, device=dev)
+
+        def timed(fn, reps=5):
+            fn()
+            ts = []
+            for _ in range(reps):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                fn()
+                b.record()
+                torch.cuda.synchronize()
+                ts.append(a.elapsed_time(b) / 1e3)
+            return float(np.median(ts))
+
+        t_fwd = timed(lambda: _lib.check(L.speo_surrogate_forward_bf16(s, T.data_ptr(), 262144, 52, y.data_ptr(), st),
+                                         "forward_bf16"))
+        t_train = timed(lambda: _lib.check(L.speo_surrogate_train(s, steps, None, st), "train"))
+        _lib.check(L.speo_surrogate_set_mode(s, 0), "set_mode")
+        t_fwd32 = timed(lambda: _lib.check(L.speo_surrogate_forward(s, T.data_ptr(), 262144, 52, y.data_ptr(), st),
+                                           "forward"))
+        t_train32 = timed(lambda: _lib.check(L.speo_surrogate_train(s, steps, None, st), "train"))
+    finally:
+        L.speo_surrogate_destroy(s)
+    flop_fwd = 262144 * 2 * (50 * 256 + 256 * 256 + 256)
+    return {"workload": "MLP 50-256-256-1: screening forward of 262,144 trials; training steps of batch 4096",
+            "forward_bf16_us": t_fwd * 1e6, "forward_bf16_tflops": flop_fwd / t_fwd / 1e12,
+            "forward_fp32_simt_us": t_fwd32 * 1e6,
+            "train_step_bf16_us": t_train / steps * 1e6, "train_step_fp32_simt_us": t_train32 / steps * 1e6,
+            "train_steps_timed": steps}
+
+
 def bench_e2e(L, dev, torch, args) -> dict:
     """Reference-shaped C ABI with host buffers: initial population + instance uploaded from
     pinned host memory, then per generation generate / evaluate / select and a read-back of
@@ -577,13 +628,23 @@ def bench_e2e(L, dev, torch, args) -> dict:
     _lib.check(L.API_Initilize_f32(C, rng_state.data_ptr(), ii, pi), "API_Initilize_f32")
     steps = max(100, min(args.steps, 2000))
 
-    def run(nsteps):
+    def upload():
         pop.copy_(h_pop, non_blocking=True)
         d_rot.copy_(h_rot, non_blocking=True)
         d_sh.copy_(h_sh, non_blocking=True)
         d_info.copy_(h_info, non_blocking=True)
         L.API_evaluateFitness_f32(pfit.data_ptr(), None, None, pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(),
                                   None, None, None, None, n, DIM, 0.0, FUNC)
+
+    def run_native(nsteps):  # the reference's DE_CUDA::Run loop as one library call (C++ host loop)
+        upload()
+        _lib.check(L.speo_de_run_f32(P, C, rng_state.data_ptr(), ii, d_info.data_ptr(), best.data_ptr(), pi,
+                                     d_sh.data_ptr(), d_rot.data_ptr(), nsteps, h_fit.data_ptr(),
+                                     stream.cuda_stream), "speo_de_run_f32")
+        stream.synchronize()
+
+    def run_python(nsteps):  # the same calls issued one by one from Python (ctypes)
+        upload()
         for _ in range(nsteps):
             L.API_DE_GenerateNewPopulation_f32(C, P, best.data_ptr(), ii, d_info.data_ptr(), rng_state.data_ptr(),
                                                pi)
@@ -593,17 +654,22 @@ def bench_e2e(L, dev, torch, args) -> dict:
             h_fit.copy_(pfit, non_blocking=True)
         stream.synchronize()
 
-    run(20)
-    t0 = time.perf_counter()
-    run(steps)
-    dt = time.perf_counter() - t0
+    out = {}
+    for name, fn in (("native", run_native), ("python", run_python)):
+        fn(20)
+        t0 = time.perf_counter()
+        fn(steps)
+        out[name] = n * steps / (time.perf_counter() - t0)
     _lib.check(L.API_CheckCUDAError(), "e2e")
     L.speo_set_stream(None)
     h2d = (n * ld + ld * DIM + ld) * 4 + len(bytes(info))
-    return {"value": n * steps / dt, "unit": "evals/s", "h2d_bytes_per_step": h2d / steps,
+    return {"value": out["native"], "unit": "evals/s", "h2d_bytes_per_step": h2d / steps,
             "d2h_bytes_per_step": n * 4, "steps": steps,
-            "path": "API_DE_GenerateNewPopulation_f32 + API_evaluateFitness_f32 + API_DE_SelectSurvival_f32, "
-                    "64 sub-islands of 100"}
+            "path": "speo_de_run_f32: per generation API_DE_GenerateNewPopulation_f32 + API_evaluateFitness_f32 + "
+                    "API_DE_SelectSurvival_f32 + fitness read-back to pinned host memory (64 sub-islands of 100), "
+                    "blocks of 10 generations replayed as a CUDA graph",
+            "python_loop_value": out["python"],
+            "python_loop_path": "the same entry points called one by one from Python (ctypes), per-call host cost"}
 
 
 def cpu_workload_sample(sample_s: float, threads: int):
@@ -670,8 +736,16 @@ def main() -> None:
     ap.add_argument("--c4-gens", type=int, default=200, help="generations of each config-4 run")
     ap.add_argument("--configs-only", action="store_true", help="only the config 2 / 3 / 4 sections")
     ap.add_argument("--c4-only", action="store_true", help="only the config 4 section")
+    ap.add_argument("--mlp-case", action="store_true", help="only the surrogate network's kernels at config-4 shapes")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.mlp_case:
+        import torch
+        from speo_gb300 import _lib
+
+        torch.cuda.set_device(0)
+        print(json.dumps({"surrogate_mlp": bench_mlp(_lib.load(), "cuda:0", torch)}))
+        return
     if args.c4_only:
         import torch
         from speo_gb300 import _lib

@@ -34,6 +34,8 @@ int check_launch(const char *what) { return check_cuda(cudaGetLastError(), what)
 
 cudaStream_t api_stream() { return t_stream; }
 
+int sticky_status() { return t_sticky; }
+
 int sm_count()
 {
     int dev = 0;

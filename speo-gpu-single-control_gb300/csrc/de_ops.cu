@@ -137,26 +137,27 @@ __device__ __forceinline__ uint32_t cr_threshold(T CR)
 }
 __device__ __forceinline__ bool cr_take(uint32_t w, uint32_t thr) { return (w >> 8) + 1u < thr; }
 
-// One warp owns 32 consecutive positions: lane l draws the donors and jrand of position l
-// (Philox on all lanes at once). The warp's 32 x nch (row, 16-byte chunk) tasks are then dealt
-// to the lanes in order, task t = it * 32 + lane, so no lane idles whatever D is; each task reads
-// its row's draws from the drawing lane with shuffles. Two tasks in flight per lane.
+// One warp owns ppw (4 .. 32) consecutive positions: lane l < ppw draws the donors and jrand of
+// position l (Philox on those lanes at once). The warp's ppw x nch (row, 16-byte chunk) tasks are
+// then dealt to the lanes in order, task t = it * 32 + lane, so no lane idles whatever D is; each
+// task reads its row's draws from the drawing lane with shuffles. Two tasks in flight per lane.
+// Small populations take small ppw so that enough warps cover the GPU.
 template <typename T>
 __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld, int dim, int island_size, int S,
                                                   const int *perm, const typename DeInfoT<T>::type *info,
-                                                  const int *best_id, T lb, T ub, RngState *rng)
+                                                  const int *best_id, T lb, T ub, RngState *rng, int ppw)
 {
     using V = typename Vec<T>::type;
     constexpr int VN = Vec<T>::n;
     const uint32_t gen = *(volatile uint32_t *)&rng->gen;
     const uint2 key = make_uint2(rng->key0, rng->key1);
     const int lane = threadIdx.x & 31;
-    const int wbase = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
+    const int wbase = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * ppw;
     // ---- draws of position wbase + lane ------------------------------------------------------
     int d0 = 0, d1 = 0, d2 = 0, d3 = 0, d4 = 0, jr = 0, sel = 0, isl = 0;
     {
         const int pos = wbase + lane;
-        if (pos < island_size) {
+        if (lane < ppw && pos < island_size) {
             isl = pos / S;
             IdxStream s(key, (uint32_t)pos, gen, kTagIdx);
             int r[5];
@@ -170,20 +171,23 @@ __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld,
     const int nch = (dim + VN - 1) / VN;
     const int q32 = 32 / nch, r32 = 32 % nch;  // task t -> t + 32 advances (row, chunk) by these
     int src = lane / nch, c = lane - src * nch;
+    const int iters = (ppw * nch + 31) / 32;   // uniform trip count
     bool ok_bound = true;
 #pragma unroll 2
-    for (int it = 0; it < nch; ++it) {          // uniform trip count: every lane takes nch tasks
+    for (int it = 0; it < iters; ++it) {
+        const int s_lane = src < 32 ? src : 31;
         const int pos = wbase + src;
-        const int rsel = __shfl_sync(0xffffffffu, sel, src), risl = __shfl_sync(0xffffffffu, isl, src);
-        const int rjr = __shfl_sync(0xffffffffu, jr, src);
-        const int rd[5] = {__shfl_sync(0xffffffffu, d0, src), __shfl_sync(0xffffffffu, d1, src),
-                           __shfl_sync(0xffffffffu, d2, src), __shfl_sync(0xffffffffu, d3, src),
-                           __shfl_sync(0xffffffffu, d4, src)};
+        const int rsel = __shfl_sync(0xffffffffu, sel, s_lane), risl = __shfl_sync(0xffffffffu, isl, s_lane);
+        const int rjr = __shfl_sync(0xffffffffu, jr, s_lane);
+        const int rd[5] = {__shfl_sync(0xffffffffu, d0, s_lane), __shfl_sync(0xffffffffu, d1, s_lane),
+                           __shfl_sync(0xffffffffu, d2, s_lane), __shfl_sync(0xffffffffu, d3, s_lane),
+                           __shfl_sync(0xffffffffu, d4, s_lane)};
         const int e0 = VN * c;
+        const bool live = src < ppw && pos < island_size;
         src += q32;
         c += r32;
         if (c >= nch) { c -= nch; ++src; }
-        if (pos >= island_size) continue;
+        if (!live) continue;
         const T F = info[risl].F;
         const uint32_t thr = cr_threshold<T>(info[risl].CR);
         const int st = info[risl].strategy_ID;
@@ -252,15 +256,14 @@ __global__ void __launch_bounds__(256) k_select(T *pop, T *pop_fit, const T *can
     const bool ragged = (dim % VN) != 0;
     const long long groups = ((long long)n + 31) / 32;
     const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
-    long long g = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    T fc = 0, fp = 0;  // this group's fitness pair, loaded one group ahead
-    if (g < groups && g * 32 + lane < n) { fc = cand_fit[g * 32 + lane]; fp = pop_fit[g * 32 + lane]; }
-    for (; g < groups; g += nwarps) {
+    for (long long g = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < groups; g += nwarps) {
         const long long row = g * 32 + lane;
-        const bool win = row < n && fc < fp;
-        if (win) pop_fit[row] = fc;
-        const long long gn = g + nwarps;
-        if (gn < groups && gn * 32 + lane < n) { fc = cand_fit[gn * 32 + lane]; fp = pop_fit[gn * 32 + lane]; }
+        bool win = false;
+        if (row < n) {
+            const T fc = cand_fit[row];
+            win = fc < pop_fit[row];
+            if (win) pop_fit[row] = fc;
+        }
         unsigned m = __ballot_sync(0xffffffffu, win);
         while (m) {
             int rr[kBatch];
@@ -333,12 +336,15 @@ int generate(Pop cand, Pop pop, int *d_best, speo_island_info ii, Info *d_info, 
     k_best<T><<<(ii.subisland_num + kWarps - 1) / kWarps, 32 * kWarps, 0, st>>>(
         pop.fitness_value, ii.permutated_index, S, ii.subisland_num, d_best);
     if (int e = check_launch("global_DE_FindBestIndividualInIsland")) return e;
-    // 16-byte chunks cover D (np2 rows keep every chunk in bounds)
-    const int grid = (ii.island_size + 255) / 256;  // 8 warps x 32 positions per block
+    // 16-byte chunks cover D (np2 rows keep every chunk in bounds). Positions per warp: the
+    // largest of 32, 16, 8, 4 that still gives about 16 warps per SM.
+    int ppw = 32;
+    while (ppw > 4 && (long long)ii.island_size < (long long)ppw * 16 * sm_count()) ppw >>= 1;
+    const int grid = (ii.island_size + 8 * ppw - 1) / (8 * ppw);  // 8 warps per block
     const auto *inf = reinterpret_cast<const typename DeInfoT<T>::type *>(d_info);
     RngState *rs = reinterpret_cast<RngState *>(d_rng);
     k_generate<T><<<grid, 256, 0, st>>>(cand.elements, pop.elements, ld, pi.dim, ii.island_size, S,
-                                        ii.permutated_index, inf, d_best, (T)pi.min_bound, (T)pi.max_bound, rs);
+                                        ii.permutated_index, inf, d_best, (T)pi.min_bound, (T)pi.max_bound, rs, ppw);
     return check_launch("global_DE_GenerateNewPopulation");
 }
 

@@ -1,0 +1,109 @@
+// driver.cu -- the reference's host generation loop, natively.
+//
+// DE_CUDA::Run (CUDA_EA_library/DE_CUDA.cc:200-216) calls, per generation,
+// API_DE_GenerateNewPopulation, CEC2014_CUDA::EvaluateFitness (-> API_evaluateFitness) and
+// API_DE_SelectSurvival, with a device synchronisation after each launch; the island driver then
+// reads results back to the host (src/island_EA.cc:78-113). speo_de_run_f32 runs that loop over
+// this library's drop-in entry points on a private stream, ordered after the caller's stream:
+// blocks of kBlock generations (each with its read-back of the fitness vector into pinned host
+// memory) are captured once as a CUDA graph and replayed, so the per-generation host cost is one
+// graph launch per block instead of a synchronisation per kernel.
+#include "host.h"
+
+namespace speo {
+namespace {
+
+constexpr int kBlock = 10;  // generations per captured graph
+
+struct DriverStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t in = nullptr, out = nullptr;
+};
+thread_local DriverStream t_drv;
+
+int driver_stream(DriverStream **out)
+{
+    DriverStream &d = t_drv;
+    if (!d.s) {
+        if (int e = check_cuda(cudaStreamCreateWithFlags(&d.s, cudaStreamNonBlocking), "driver stream")) return e;
+        if (int e = check_cuda(cudaEventCreateWithFlags(&d.in, cudaEventDisableTiming), "driver event")) return e;
+        if (int e = check_cuda(cudaEventCreateWithFlags(&d.out, cudaEventDisableTiming), "driver event")) return e;
+    }
+    *out = &d;
+    return SPEO_OK;
+}
+
+bool is_pinned(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+}  // namespace
+}  // namespace speo
+
+using namespace speo;
+
+extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand, speo_rng_state *rng,
+                               speo_island_info ii, speo_de_info_f32 *d_info, int *d_best, speo_problem_info_f32 pi,
+                               const float *d_shift, const float *d_rot, int generations, float *h_fitness,
+                               void *stream)
+{
+    if (!pop.elements || !pop.fitness_value || !cand.elements || !cand.fitness_value || !rng || !d_info || !d_best ||
+        !d_shift || !d_rot || generations < 0 || ii.island_size <= 0)
+        return fail(SPEO_ERR_INVALID_ARG, "speo_de_run_f32: bad arguments");
+    if (generations == 0) return SPEO_OK;
+    DriverStream *d = nullptr;
+    if (int e = driver_stream(&d)) return e;
+    const int n = ii.island_size;
+    cudaStream_t caller = static_cast<cudaStream_t>(stream);
+    if (int e = check_cuda(cudaEventRecord(d->in, caller), "driver: record")) return e;
+    if (int e = check_cuda(cudaStreamWaitEvent(d->s, d->in, 0), "driver: wait")) return e;
+    const cudaStream_t prev = api_stream();
+    speo_set_stream(d->s);
+
+    auto one_generation = [&]() -> int {
+        if (int e = API_DE_GenerateNewPopulation_f32(cand, pop, d_best, ii, d_info, rng, pi)) return e;
+        const int before = sticky_status();
+        API_evaluateFitness_f32(cand.fitness_value, nullptr, nullptr, cand.elements, const_cast<float *>(d_shift),
+                                const_cast<float *>(d_rot), nullptr, nullptr, nullptr, nullptr, n, pi.dim, 0.f,
+                                pi.function_ID);
+        if (sticky_status() != before) return sticky_status();
+        if (int e = API_DE_SelectSurvival_f32(pop, cand, ii, pi)) return e;
+        if (h_fitness)
+            return check_cuda(cudaMemcpyAsync(h_fitness, pop.fitness_value, sizeof(float) * (size_t)n,
+                                              cudaMemcpyDeviceToHost, d->s),
+                              "driver: fitness read-back");
+        return SPEO_OK;
+    };
+
+    int e = SPEO_OK, done = 0;
+    if (generations >= 2 * kBlock && (!h_fitness || is_pinned(h_fitness))) {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t x = nullptr;
+        e = check_cuda(cudaStreamBeginCapture(d->s, cudaStreamCaptureModeThreadLocal), "driver: begin capture");
+        if (!e) {
+            for (int i = 0; !e && i < kBlock; ++i) e = one_generation();
+            const cudaError_t ce = cudaStreamEndCapture(d->s, &g);  // always ends the capture
+            if (!e) e = check_cuda(ce, "driver: end capture");
+        }
+        if (!e) e = check_cuda(cudaGraphInstantiate(&x, g, 0), "driver: instantiate");
+        for (; !e && done + kBlock <= generations; done += kBlock)
+            e = check_cuda(cudaGraphLaunch(x, d->s), "driver: graph launch");
+        const int es = check_cuda(cudaStreamSynchronize(d->s), "driver: sync");
+        if (!e) e = es;
+        if (x) cudaGraphExecDestroy(x);
+        if (g) cudaGraphDestroy(g);
+    }
+    for (; !e && done < generations; ++done) e = one_generation();
+    speo_set_stream(prev);
+    const int es = check_cuda(cudaStreamSynchronize(d->s), "driver: sync");
+    if (!e) e = es;
+    if (!e) e = check_cuda(cudaEventRecord(d->out, d->s), "driver: record");
+    if (!e) e = check_cuda(cudaStreamWaitEvent(caller, d->out, 0), "driver: wait");
+    return e;
+}

@@ -16,6 +16,8 @@ int check_cuda(cudaError_t e, const char *what);
 int check_launch(const char *what);
 // Stream of the group-1 (reference-shaped) entry points on this host thread.
 cudaStream_t api_stream();
+// First failure status recorded on this host thread since the last API_CheckCUDAError.
+int sticky_status();
 // Number of SMs of the current device (cached per device).
 int sm_count();
 

@@ -42,17 +42,25 @@ __device__ __forceinline__ int donors_for(int st)
 __host__ __device__ __forceinline__ int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
 // Shared memory of one island with population bound Pmax and column class Q (W = 32Q):
-//   pop[Pmax][W] fit[Pmax] | Xs[Pt][W] Ys[Pt][W] | Ms[D<=32Q][W] | sR[Pmax][8] sF[Pt] | o[W]
+//   pop[Pmax][W] fit[Pmax] | Xs[Pt][W] Ys[Pt][W] | Ms[D<=32Q][W] | sR[GB][Pmax][8] sF[Pt] | o[W]
+// The donor draws depend only on (seed, row, generation), so the block draws them for the next GB
+// generations at once (GB x P rows over all threads, instead of P rows per generation).
 template <int Q> struct ResPlan {
     static constexpr int W = 32 * Q;
     static constexpr int G = Q == 1 ? 8 : 16;     // lanes per row
     static constexpr int RPP = kThreads / G;      // rows per pass of the block
 };
 
+__host__ __device__ inline int draw_gens(int Pmax)
+{
+    const int g = kThreads / Pmax;
+    return g < 1 ? 1 : g > 8 ? 8 : g;
+}
+
 __host__ __device__ inline size_t res_smem_floats(int Q, int Pmax)
 {
     const int W = 32 * Q, Pt = round_up(Pmax, kEvalRows);
-    return (size_t)Pmax * W + Pmax + 2 * (size_t)Pt * W + (size_t)W * W + (size_t)Pmax * 8 + Pt + W;
+    return (size_t)Pmax * W + Pmax + 2 * (size_t)Pt * W + (size_t)W * W + (size_t)draw_gens(Pmax) * Pmax * 8 + Pt + W;
 }
 
 template <int Q>
@@ -69,8 +77,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     float *Xs = fit + Pmax;
     float *Ys = Xs + (size_t)Pt * W;
     float *Ms = Ys + (size_t)Pt * W;
+    const int GB = draw_gens(Pmax);
     int *sR = reinterpret_cast<int *>(Ms + W * W);
-    float *sF = reinterpret_cast<float *>(sR + Pmax * 8);
+    float *sF = reinterpret_cast<float *>(sR + GB * Pmax * 8);
     float *so = sF + Pt;
     __shared__ float s_bf[kWarpsR];
     __shared__ int s_bi[kWarpsR];
@@ -123,22 +132,28 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (s_bf[w] < bf || (s_bf[w] == bf && s_bi[w] < bi)) { bf = s_bf[w]; bi = s_bi[w]; }
                 best = bi;
             }
-            // (1) donor positions + jrand, one thread per row
-            for (int r = tid; r < P; r += kThreads) {
-                IdxStream is(key, (uint32_t)(row0 + r), gen, kTagIdx);
-                int rr[5];
-                ok_draw &= draw_donors(is, P, rr);
+            // (1) donor positions + jrand of generations g .. g + GB - 1, one thread per (gen, row)
+            if (g % GB == 0) {
+                const int nb = generations - g < GB ? generations - g : GB;
+                for (int t = tid; t < nb * P; t += kThreads) {
+                    const int gi = t / P, r = t - gi * P;
+                    IdxStream is(key, (uint32_t)(row0 + r), gen + (uint32_t)gi, kTagIdx);
+                    int rr[5];
+                    ok_draw &= draw_donors(is, P, rr);
+                    int *o = sR + (gi * Pmax + r) * 8;
 #pragma unroll
-                for (int k = 0; k < 5; ++k) sR[r * 8 + k] = rr[k];
-                sR[r * 8 + 5] = is.index(D);
+                    for (int k = 0; k < 5; ++k) o[k] = rr[k];
+                    o[5] = is.index(D);
+                }
+                __syncthreads();
             }
-            __syncthreads();
+            const int *sRg = sR + (g % GB) * Pmax * 8;
             // (2) trials from the shared-memory population
             for (int r = grp; r < P; r += Pl::RPP) {
-                const int jrand = sR[r * 8 + 5];
+                const int jrand = sRg[r * 8 + 5];
                 int dr[5];
 #pragma unroll
-                for (int k = 0; k < 5; ++k) dr[k] = sR[r * 8 + k];
+                for (int k = 0; k < 5; ++k) dr[k] = sRg[r * 8 + k];
                 const float *xi = pop + r * W;
                 const float *xb = pop + (best >= 0 ? best : r) * W;
                 for (int c = gl; c < nch; c += G) {

@@ -118,6 +118,59 @@ def test_dropin_generate_matches_oracle(lib, oracle, cuda, f64, P, D, nsub):
         assert int(d.rng.cpu()[2]) == gen + 1                    # generation counter advanced once
 
 
+@pytest.mark.parametrize("gens,pinned", [(25, True), (7, False)])
+def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned):
+    """speo_de_run_f32 (the reference's DE_CUDA::Run loop, natively; CUDA-graph blocks when the
+    fitness buffer is pinned) gives the same populations as the drop-in calls issued one by one."""
+    import torch
+    from speo_gb300.instances import make_instance
+
+    P, D, nsub = 200, 30, 2
+    o, M = make_instance(77, D)
+    ld = np2(D)
+    rot = np.zeros((ld, D), dtype=np.float32)
+    rot[:D] = M.T
+    shift = np.zeros(ld, dtype=np.float32)
+    shift[:D] = o
+    d_rot, d_sh = torch.from_numpy(rot).to(cuda), torch.from_numpy(shift).to(cuda)
+    rng = np.random.default_rng(9)
+    pop0 = np.zeros((P, ld), dtype=np.float32)
+    pop0[:, :D] = rng.uniform(-100, 100, (P, D))
+    runs = []
+    for mode in ("calls", "driver"):
+        d = DropIn(lib, cuda, P, D, nsub, False, seed=4321)
+        info = (d.DI * nsub)(*[d.DI(0.9, 0.5, 4 if i == 0 else 6, P // nsub) for i in range(nsub)])
+        d_info = torch.frombuffer(bytearray(bytes(info)), dtype=torch.uint8).to(cuda)
+        pop_s, cand_s = d.pops()
+        d.call("API_Initilize", cand_s, d.rng.data_ptr(), d.island(), d.problem)
+        d.pop.copy_(torch.from_numpy(pop0))
+        args = (None, None, d.pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(), None, None, None, None, P, D, 0.0, 9)
+        d.lib.API_evaluateFitness_f32(d.pfit.data_ptr(), *args)
+        if mode == "calls":
+            for _ in range(gens):
+                d.call("API_DE_GenerateNewPopulation", cand_s, pop_s, d.best.data_ptr(), d.island(),
+                       d_info.data_ptr(), d.rng.data_ptr(), d.problem)
+                d.lib.API_evaluateFitness_f32(d.cfit.data_ptr(), None, None, d.cand.data_ptr(), d_sh.data_ptr(),
+                                              d_rot.data_ptr(), None, None, None, None, P, D, 0.0, 9)
+                d.call("API_DE_SelectSurvival", pop_s, cand_s, d.island(), d.problem)
+            h = None
+        else:
+            h = torch.zeros(P, dtype=torch.float32)
+            if pinned:
+                h = h.pin_memory()
+            d._lib.check(d.lib.speo_de_run_f32(pop_s, cand_s, d.rng.data_ptr(), d.island(), d_info.data_ptr(),
+                                               d.best.data_ptr(), d.problem, d_sh.data_ptr(), d_rot.data_ptr(), gens,
+                                               h.data_ptr(), None), "speo_de_run_f32")
+        d._lib.check(d.lib.API_CheckCUDAError(), "API_CheckCUDAError")
+        runs.append((d.pop.cpu().numpy(), d.pfit.cpu().numpy(), None if h is None else h.numpy().copy(),
+                     int(d.rng.cpu()[2])))
+    (pa, fa, _, ga), (pb, fb, hb, gb) = runs
+    assert np.array_equal(pa, pb)
+    assert np.array_equal(fa, fb)
+    assert np.array_equal(hb, fb)          # the last generation's fitness read back
+    assert ga == gb == gens
+
+
 @pytest.mark.parametrize("f64", [False, True])
 def test_dropin_select_matches_oracle(lib, oracle, cuda, f64):
     import torch
