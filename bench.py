@@ -737,8 +737,16 @@ def main() -> None:
     ap.add_argument("--configs-only", action="store_true", help="only the config 2 / 3 / 4 sections")
     ap.add_argument("--c4-only", action="store_true", help="only the config 4 section")
     ap.add_argument("--mlp-case", action="store_true", help="only the surrogate network's kernels at config-4 shapes")
+    ap.add_argument("--e2e-only", action="store_true", help="only the end-to-end drop-in measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.e2e_only:
+        import torch
+        from speo_gb300 import _lib
+
+        torch.cuda.set_device(0)
+        print(json.dumps({"e2e": bench_e2e(_lib.load(), "cuda:0", torch, args)}))
+        return
     if args.mlp_case:
         import torch
         from speo_gb300 import _lib

@@ -134,34 +134,52 @@ __global__ void __launch_bounds__(256, 1) k_mlp_fwd_tc(MlpArgs a)
     uint32_t phase = 0;
     int mma_pending = 0;  // a commit whose wait gave up
 
-    for (long long tile = blockIdx.x; tile < ntiles && !abort; tile += gridDim.x) {
-        const long long r0 = tile * kRows;
-        // ---- A1 = bf16((x - mu) * isig), zero past din and past n ----------------------------
+    // This thread's share of a tile's inputs: rows r = tid % 128 (lanes = consecutive rows, so
+    // each 8-lane phase of the shared-memory stores covers 128 contiguous bytes), 16-byte chunks
+    // k0 = 8 ((tid + 256 j) / 128). The next tile's rows are loaded into registers before the
+    // current tile's products start, so their latency overlaps the tensor-core work.
+    constexpr int kItems = kRows * (kK1 / 8) / 256;
+    float xin[kItems][8];
+    auto load_rows = [&](long long r0) {
 #pragma unroll
-        for (int j = 0; j < kRows * (kK1 / 8) / 256; ++j) {
+        for (int j = 0; j < kItems; ++j) {
             const int item = tid + 256 * j;
-            const int r = item / (kK1 / 8), k0 = (item % (kK1 / 8)) * 8;
+            const int r = item % kRows, k0 = (item / kRows) * 8;
             const long long gr = r0 + r;
-            float v[8];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) v[e] = 0.f;
+            for (int e = 0; e < 8; ++e) xin[j][e] = 0.f;
             if (gr < a.n) {
                 const float *xr = a.X + gr * a.ldx;
                 if (a.vec && k0 + 8 <= a.din) {
                     const float4 p = *reinterpret_cast<const float4 *>(xr + k0);
-                    const float4 s = *reinterpret_cast<const float4 *>(xr + k0 + 4);
-                    v[0] = p.x; v[1] = p.y; v[2] = p.z; v[3] = p.w; v[4] = s.x; v[5] = s.y; v[6] = s.z; v[7] = s.w;
+                    const float4 q = *reinterpret_cast<const float4 *>(xr + k0 + 4);
+                    xin[j][0] = p.x; xin[j][1] = p.y; xin[j][2] = p.z; xin[j][3] = p.w;
+                    xin[j][4] = q.x; xin[j][5] = q.y; xin[j][6] = q.z; xin[j][7] = q.w;
                 } else {
 #pragma unroll
-                    for (int e = 0; e < 8; ++e) v[e] = k0 + e < a.din ? xr[k0 + e] : 0.f;
+                    for (int e = 0; e < 8; ++e) xin[j][e] = k0 + e < a.din ? xr[k0 + e] : 0.f;
                 }
-#pragma unroll
-                for (int e = 0; e < 8; ++e)
-                    v[e] = k0 + e < a.din ? __fmul_rn(__fsub_rn(v[e], a.mu[k0 + e]), a.isig[k0 + e]) : 0.f;
             }
+        }
+    };
+    if (blockIdx.x < ntiles) load_rows((long long)blockIdx.x * kRows);
+
+    for (long long tile = blockIdx.x; tile < ntiles && !abort; tile += gridDim.x) {
+        const long long r0 = tile * kRows;
+        // ---- A1 = bf16((x - mu) * isig), zero past din and past n ----------------------------
+#pragma unroll
+        for (int j = 0; j < kItems; ++j) {
+            const int item = tid + 256 * j;
+            const int r = item % kRows, k0 = (item / kRows) * 8;
+            float v[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+                v[e] = (k0 + e < a.din && r0 + r < a.n) ? __fmul_rn(__fsub_rn(xin[j][e], a.mu[k0 + e]), a.isig[k0 + e])
+                                                        : 0.f;
             *reinterpret_cast<uint4 *>(sa + tc::kmajor_offset(r, k0, kK1)) =
                 make_uint4(bf2(v[0], v[1]), bf2(v[2], v[3]), bf2(v[4], v[5]), bf2(v[6], v[7]));
         }
+        if (tile + gridDim.x < ntiles) load_rows((tile + gridDim.x) * kRows);
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
         __syncthreads();
