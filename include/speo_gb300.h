@@ -263,6 +263,14 @@ SPEO_API int speo_generation_epoch(const speo_segment *d_segs, int n_segs, int d
                                    int max_pop, const float *pop_in, const float *fit_in,
                                    float *pop_out, float *fit_out, uint32_t *d_gen, int generations,
                                    void *stream);
+/* speo_generation_epoch with the block shape chosen explicitly: cluster = 1 runs one block per
+ * island; cluster = 2 runs each island on a two-block cluster (each block holds a replica of the
+ * island, computes half of the rows and writes them into both replicas through distributed
+ * shared memory; one cluster barrier per generation), bit-identical to cluster = 1;
+ * cluster = 0 picks 2 when there are SMs for two blocks per island and the replicas fit. */
+SPEO_API int speo_generation_epoch_ex(const speo_segment *d_segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
+                                      const float *pop_in, const float *fit_in, float *pop_out, float *fit_out,
+                                      uint32_t *d_gen, int generations, int cluster, void *stream);
 
 /* Ring migration: each segment's k best rows (by fitness, then row) replace the k worst
  * rows (by fitness, then row, from the worst) of segment ring_next. All emigrants are

@@ -15,12 +15,12 @@ constexpr int kRowsPerWarp = 8;
 constexpr int kEvalWarps = 8;
 constexpr int kEvalTile = kRowsPerWarp * kEvalWarps;  // 64 rows per 256-thread block
 
-// acc[rr][q] += sum_k Y[row0+rr][k] * Ms[(k-kbeg)*ms_ld + lane + 32q], k in [kbeg, kend).
-// Ys rows are ys_ld apart (multiple of 4 for float); columns >= D of Ms must be zero or unused.
-template <typename T, int Q>
-__device__ __forceinline__ void eval_accumulate(T (&acc)[kRowsPerWarp][Q], const T *__restrict__ Ys, int ys_ld,
-                                                int row0, const T *__restrict__ Ms, int ms_ld, int kbeg, int kend,
-                                                int lane)
+// acc[rr][q] += sum_k Y[row0+rr][k] * Ms[(k-kbeg)*ms_ld + lane + 32q], k in [kbeg, kend), for the
+// RPW rows of the warp. Ys rows are ys_ld apart (multiple of 4 for float); columns >= D of Ms must
+// be zero or unused. The order of the FMAs of one row does not depend on RPW.
+template <typename T, int Q, int RPW>
+__device__ __forceinline__ void eval_accumulate(T (&acc)[RPW][Q], const T *__restrict__ Ys, int ys_ld, int row0,
+                                                const T *__restrict__ Ms, int ms_ld, int kbeg, int kend, int lane)
 {
     int k = kbeg;
     if constexpr (sizeof(T) == 4) {
@@ -31,7 +31,7 @@ __device__ __forceinline__ void eval_accumulate(T (&acc)[kRowsPerWarp][Q], const
 #pragma unroll
                 for (int q = 0; q < Q; ++q) m[kk][q] = Ms[(k + kk - kbeg) * ms_ld + lane + 32 * q];
 #pragma unroll
-            for (int rr = 0; rr < kRowsPerWarp; ++rr) {
+            for (int rr = 0; rr < RPW; ++rr) {
                 const float4 y = *reinterpret_cast<const float4 *>(Ys + (row0 + rr) * ys_ld + k);
 #pragma unroll
                 for (int q = 0; q < Q; ++q) {
@@ -48,7 +48,7 @@ __device__ __forceinline__ void eval_accumulate(T (&acc)[kRowsPerWarp][Q], const
 #pragma unroll
         for (int q = 0; q < Q; ++q) m[q] = Ms[(k - kbeg) * ms_ld + lane + 32 * q];
 #pragma unroll
-        for (int rr = 0; rr < kRowsPerWarp; ++rr) {
+        for (int rr = 0; rr < RPW; ++rr) {
             const T y = Ys[(row0 + rr) * ys_ld + k];
 #pragma unroll
             for (int q = 0; q < Q; ++q) acc[rr][q] = fma_rn(y, m[q], acc[rr][q]);
@@ -57,12 +57,11 @@ __device__ __forceinline__ void eval_accumulate(T (&acc)[kRowsPerWarp][Q], const
 }
 
 // f[rr] = sum over columns j < D of term(scale * acc[rr][j]); result valid on every lane.
-template <typename T, int Q>
-__device__ __forceinline__ void eval_reduce(const T (&acc)[kRowsPerWarp][Q], int D, int func_id, T scale, int lane,
-                                            T (&f)[kRowsPerWarp])
+template <typename T, int Q, int RPW>
+__device__ __forceinline__ void eval_reduce(const T (&acc)[RPW][Q], int D, int func_id, T scale, int lane, T (&f)[RPW])
 {
 #pragma unroll
-    for (int rr = 0; rr < kRowsPerWarp; ++rr) {
+    for (int rr = 0; rr < RPW; ++rr) {
         T s = T(0);
 #pragma unroll
         for (int q = 0; q < Q; ++q)

@@ -239,6 +239,256 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
+// ---- two-block clusters: one island per cluster of 2 -------------------------------------------
+// Each block of the pair keeps a full replica of the island in shared memory, double-buffered
+// (pop[g % 2] is generation g), and runs the trials, evaluation and selection of one half of the
+// rows. Its new rows (winner or parent) go to the next buffer of both replicas: its own, and the
+// peer's through distributed shared memory. One cluster barrier per generation then makes both
+// replicas whole. Donor reads are local; the per-row arithmetic is the single-block kernel's, so
+// the result is bit-identical.
+__device__ __forceinline__ uint32_t cluster_rank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t map_peer(const void *p, uint32_t peer)
+{
+    uint32_t out;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+                 : "=r"(out)
+                 : "r"((uint32_t)__cvta_generic_to_shared(p)), "r"(peer));
+    return out;
+}
+__device__ __forceinline__ void st_peer4(uint32_t addr, float4 v)
+{
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(v.x), "f"(v.y), "f"(v.z),
+                 "f"(v.w)
+                 : "memory");
+}
+__device__ __forceinline__ void st_peer1(uint32_t addr, float v)
+{
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+// All threads of both blocks: writes before it (local and remote) are visible after it.
+__device__ __forceinline__ void cluster_sync()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+constexpr int kRowsPerWarp2 = 4;
+constexpr int kEvalRows2 = kWarpsR * kRowsPerWarp2;  // 64 rows per evaluation pass
+
+__host__ __device__ inline int half_rows(int Pmax) { return (Pmax + 1) / 2; }
+__host__ __device__ inline int draw_gens2(int Pmax) { return draw_gens(half_rows(Pmax)); }
+
+//   pop[2][Pmax][W] fit[2][Pmax] | Xs[Ph][W] Ys[Ph][W] | Ms[W][W] | sR[GB][h][8] sF[Ph] | o[W]
+__host__ __device__ inline size_t res2_smem_floats(int Q, int Pmax)
+{
+    const int W = 32 * Q, h = half_rows(Pmax), Ph = round_up(h, kEvalRows2);
+    return 2 * ((size_t)Pmax * W + Pmax) + 2 * (size_t)Ph * W + (size_t)W * W + (size_t)draw_gens2(Pmax) * h * 8 + Ph +
+           W;
+}
+
+template <int Q>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
+    k_island_epoch2(const speo_segment *__restrict__ segs, int Pmax, const float *pop_in, const float *fit_in,
+                    float *pop_out, float *fit_out, uint32_t *gen_ctr, int generations)
+{
+    using Pl = ResPlan<Q>;
+    constexpr int W = Pl::W, G = Pl::G;
+    extern __shared__ __align__(16) float sm[];
+    const int hmax = half_rows(Pmax), Ph = round_up(hmax, kEvalRows2), GB = draw_gens2(Pmax);
+    float *const pop0 = sm;                               // pop buffer b at pop0 + b * Pmax * W
+    float *const fit0 = sm + 2 * (size_t)Pmax * W;        // fit buffer b at fit0 + b * Pmax
+    float *Xs = fit0 + 2 * Pmax;
+    float *Ys = Xs + (size_t)Ph * W;
+    float *Ms = Ys + (size_t)Ph * W;
+    int *sR = reinterpret_cast<int *>(Ms + W * W);
+    float *sF = reinterpret_cast<float *>(sR + GB * hmax * 8);
+    float *so = sF + Ph;
+    __shared__ float s_bf[kWarpsR];
+    __shared__ int s_bi[kWarpsR];
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int grp = tid / G, gl = tid % G;
+    const uint32_t me = cluster_rank(), peer = me ^ 1u;
+    const speo_segment &s = segs[blockIdx.x >> 1];
+    const int D = s.dim, P = s.pop_size, ld = s.ld, nch = (D + 3) >> 2;
+    const uint32_t gen0 = *(volatile uint32_t *)gen_ctr;
+    // both blocks of a cluster read the same segment, so they take the same branch and pass the
+    // same number of cluster barriers
+    const bool seg_ok = P >= 2 && P <= Pmax && D >= 1 && D <= W && (ld & 3) == 0 && ld >= D;
+    if (seg_ok) {
+        const long long row0 = s.row0;
+        const uint2 key = seed_key(s.seed);
+        const int st = s.strategy, ndon = donors_for(st);
+        const float F = s.F, CR = s.CR, lb = s.lb, ub = s.ub;
+        const float scale = func_scale(s.func_id);
+        const int h = half_rows(P);
+        const int rb = (int)me * h, nr = (P - rb < h ? P - rb : h);  // this block's rows [rb, rb + nr)
+
+        for (int i = tid; i < P * nch; i += kThreads) {
+            const int r = i / nch, c = i - r * nch;
+            st4s(pop0 + r * W + 4 * c, *reinterpret_cast<const float4 *>(pop_in + (row0 + r) * ld + 4 * c));
+        }
+        for (int r = tid; r < P; r += kThreads) fit0[r] = fit_in[row0 + r];
+        load_rot_rows<float, Q>(Ms, s.rot, s.ld_rot, D, 0, D);
+        for (int k = tid; k < W; k += kThreads) so[k] = k < 4 * nch ? s.shift[k] : 0.f;
+        for (int i = tid; i < Ph * W; i += kThreads) Ys[i] = 0.f;
+        const uint32_t peer_pop0 = map_peer(pop0, peer), peer_fit0 = map_peer(fit0, peer);
+        cluster_sync();
+
+        bool ok_draw = true, ok_bound = true;
+        for (int g = 0; g < generations; ++g) {
+            const uint32_t gen = gen0 + (uint32_t)g;
+            const int cur = g & 1, nxt = cur ^ 1;
+            const float *pop = pop0 + (size_t)cur * Pmax * W;
+            const float *fit = fit0 + cur * Pmax;
+            __syncthreads();
+            int best = -1;
+            if (strategy_uses_best(st)) {
+                float bf = __int_as_float(0x7f800000);
+                int bi = 0x7fffffff;
+                for (int r = tid; r < P; r += kThreads) {
+                    const float f = rank_key(fit[r]);
+                    if (f < bf || (f == bf && r < bi)) { bf = f; bi = r; }
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float of = __shfl_xor_sync(0xffffffffu, bf, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (of < bf || (of == bf && oi < bi)) { bf = of; bi = oi; }
+                }
+                if (lane == 0) { s_bf[warp] = bf; s_bi[warp] = bi; }
+                __syncthreads();
+                bf = s_bf[0]; bi = s_bi[0];
+                for (int w = 1; w < kWarpsR; ++w)
+                    if (s_bf[w] < bf || (s_bf[w] == bf && s_bi[w] < bi)) { bf = s_bf[w]; bi = s_bi[w]; }
+                best = bi;
+            }
+            // (1) donor positions + jrand of this block's rows for generations g .. g + GB - 1
+            if (g % GB == 0) {
+                const int nb = generations - g < GB ? generations - g : GB;
+                for (int t = tid; t < nb * nr; t += kThreads) {
+                    const int gi = t / nr, lr = t - gi * nr;
+                    IdxStream is(key, (uint32_t)(row0 + rb + lr), gen + (uint32_t)gi, kTagIdx);
+                    int rr[5];
+                    ok_draw &= draw_donors(is, P, rr);
+                    int *o = sR + (gi * hmax + lr) * 8;
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) o[k] = rr[k];
+                    o[5] = is.index(D);
+                }
+                __syncthreads();
+            }
+            const int *sRg = sR + (g % GB) * hmax * 8;
+            // (2) trials of this block's rows
+            for (int lr = grp; lr < nr; lr += Pl::RPP) {
+                const int r = rb + lr;
+                const int jrand = sRg[lr * 8 + 5];
+                int dr[5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) dr[k] = sRg[lr * 8 + k];
+                const float *xi = pop + r * W;
+                const float *xb = pop + (best >= 0 ? best : r) * W;
+                for (int c = gl; c < nch; c += G) {
+                    const int e0 = 4 * c;
+                    const float4 ti = ld4s(xi + e0);
+                    const float4 tb = best >= 0 ? ld4s(xb + e0) : ti;
+                    float4 tr[5];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) tr[k] = k < ndon ? ld4s(pop + dr[k] * W + e0) : ti;
+                    const uint4 w = philox(make_uint4((uint32_t)c, (uint32_t)(row0 + r), gen, kTagCr), key);
+                    const float4 o4 = ld4s(so + e0);
+                    float4 x4 = make_float4(0.f, 0.f, 0.f, 0.f), y4 = x4;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int e = e0 + q;
+                        if (e < D) {
+                            const float u = u01(pick(w, (uint32_t)q));
+                            float x;
+                            if (e == jrand || u < CR) {
+                                float xr[5];
+#pragma unroll
+                                for (int k = 0; k < 5; ++k) xr[k] = f4g(tr[k], q);
+                                x = mutant<float>(st, F, f4g(ti, q), f4g(tb, q), xr);
+                            } else {
+                                x = f4g(ti, q);
+                            }
+                            x = check_bound<float>(x, lb, ub, ok_bound);
+                            f4s(x4, q, x);
+                            f4s(y4, q, __fsub_rn(x, f4g(o4, q)));
+                        }
+                    }
+                    st4s(Xs + lr * W + e0, x4);
+                    st4s(Ys + lr * W + e0, y4);
+                }
+            }
+            __syncthreads();
+            // (3) evaluate this block's rows, 64 per pass
+            for (int pb = 0; pb < nr; pb += kEvalRows2) {
+                float acc[kRowsPerWarp2][Q];
+#pragma unroll
+                for (int rr = 0; rr < kRowsPerWarp2; ++rr)
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) acc[rr][q] = 0.f;
+                eval_accumulate<float, Q>(acc, Ys, W, pb + warp * kRowsPerWarp2, Ms, W, 0, D, lane);
+                float f[kRowsPerWarp2];
+                eval_reduce<float, Q>(acc, D, s.func_id, scale, lane, f);
+                if (lane == 0)
+#pragma unroll
+                    for (int rr = 0; rr < kRowsPerWarp2; ++rr) sF[pb + warp * kRowsPerWarp2 + rr] = f[rr];
+            }
+            __syncthreads();
+            // (4) greedy selection (strict `<`, kernel_DE_CUDA.cu:312) into the next buffer of both
+            // replicas
+            float *npop = pop0 + (size_t)nxt * Pmax * W;
+            float *nfit = fit0 + nxt * Pmax;
+            const uint32_t ppop = peer_pop0 + (uint32_t)(nxt * Pmax * W * sizeof(float));
+            const uint32_t pfit = peer_fit0 + (uint32_t)(nxt * Pmax * sizeof(float));
+            for (int lr = grp; lr < nr; lr += Pl::RPP) {
+                const int r = rb + lr;
+                const float tf = sF[lr];
+                const bool win = tf < fit[r];
+                const float *src = win ? Xs + lr * W : pop + r * W;
+                for (int c = gl; c < nch; c += G) {
+                    const float4 v = ld4s(src + 4 * c);
+                    st4s(npop + r * W + 4 * c, v);
+                    st_peer4(ppop + (uint32_t)((r * W + 4 * c) * sizeof(float)), v);
+                }
+                if (gl == 0) {
+                    const float nf = win ? tf : fit[r];
+                    nfit[r] = nf;
+                    st_peer1(pfit + (uint32_t)(r * sizeof(float)), nf);
+                }
+            }
+            cluster_sync();
+        }
+        if (!ok_draw) atomicOr(&s_deverr, SPEO_DEVERR_REDRAW_LIMIT);
+        if (!ok_bound) atomicOr(&s_deverr, SPEO_DEVERR_BOUND_LIMIT);
+        // ---- write this block's rows back --------------------------------------------------------
+        const float *pop = pop0 + (size_t)(generations & 1) * Pmax * W;
+        const float *fit = fit0 + (generations & 1) * Pmax;
+        for (int i = tid; i < nr * nch; i += kThreads) {
+            const int lr = i / nch, c = i - lr * nch, r = rb + lr;
+            *reinterpret_cast<float4 *>(pop_out + (row0 + r) * ld + 4 * c) = ld4s(pop + r * W + 4 * c);
+        }
+        for (int lr = tid; lr < nr; lr += kThreads) fit_out[row0 + rb + lr] = fit[rb + lr];
+    } else if (tid == 0) {
+        atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        const unsigned done = atomicAdd(gen_ctr + 1, 1u);
+        if (done == gridDim.x - 1) {
+            gen_ctr[1] = 0;
+            gen_ctr[0] = gen0 + (uint32_t)generations;
+            __threadfence();
+        }
+    }
+}
+
 int max_optin()
 {
     int dev = 0, v = 0;
@@ -259,10 +509,11 @@ extern "C" int speo_epoch_fits(int max_pop, int dim_hi)
     return res_smem_floats(Q, max_pop) * sizeof(float) <= (size_t)max_optin() ? 1 : 0;
 }
 
-extern "C" int speo_generation_epoch(const speo_segment *segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
-                                     const float *pop_in, const float *fit_in, float *pop_out, float *fit_out,
-                                     uint32_t *d_gen, int generations, void *stream)
+extern "C" int speo_generation_epoch_ex(const speo_segment *segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
+                                        const float *pop_in, const float *fit_in, float *pop_out, float *fit_out,
+                                        uint32_t *d_gen, int generations, int cluster, void *stream)
 {
+    if (cluster < 0 || cluster > 2) return fail(SPEO_ERR_INVALID_ARG, "speo_generation_epoch_ex: cluster %d", cluster);
     if (!segs || !pop_in || !fit_in || !pop_out || !fit_out || !d_gen || n_segs < 1 || generations < 1)
         return fail(SPEO_ERR_INVALID_ARG, "speo_generation_epoch: bad arguments");
     if (dim_lo < 1 || dim_lo > dim_hi) return fail(SPEO_ERR_INVALID_ARG, "speo_generation_epoch: dim range");
@@ -273,9 +524,28 @@ extern "C" int speo_generation_epoch(const speo_segment *segs, int n_segs, int d
     const int Q = dim_hi <= 32 ? 1 : 2;
     if (dim_lo <= 32 && Q == 2)
         return fail(SPEO_ERR_UNSUPPORTED, "speo_generation_epoch: segments must share one column class");
-    const size_t smem = res_smem_floats(Q, max_pop) * sizeof(float);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e;
+    // two-block clusters when there are SMs for two blocks per island
+    const size_t smem2 = res2_smem_floats(Q, max_pop) * sizeof(float);
+    const bool pair = cluster != 1 && (cluster == 2 || 2LL * n_segs <= sm_count()) && smem2 <= (size_t)max_optin();
+    if (cluster == 2 && !pair)
+        return fail(SPEO_ERR_UNSUPPORTED, "speo_generation_epoch_ex: two-block islands need %zu B of shared memory", smem2);
+    if (pair) {
+        if (Q == 1) {
+            e = cudaFuncSetAttribute(k_island_epoch2<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+            if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_island_epoch2)");
+            k_island_epoch2<1><<<2 * n_segs, kThreads, smem2, st>>>(segs, max_pop, pop_in, fit_in, pop_out, fit_out,
+                                                                     d_gen, generations);
+        } else {
+            e = cudaFuncSetAttribute(k_island_epoch2<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2);
+            if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_island_epoch2)");
+            k_island_epoch2<2><<<2 * n_segs, kThreads, smem2, st>>>(segs, max_pop, pop_in, fit_in, pop_out, fit_out,
+                                                                     d_gen, generations);
+        }
+        return check_launch("k_island_epoch2");
+    }
+    const size_t smem = res_smem_floats(Q, max_pop) * sizeof(float);
     if (Q == 1) {
         e = cudaFuncSetAttribute(k_island_epoch<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_island_epoch)");
@@ -288,4 +558,12 @@ extern "C" int speo_generation_epoch(const speo_segment *segs, int n_segs, int d
                                                           generations);
     }
     return check_launch("k_island_epoch");
+}
+
+extern "C" int speo_generation_epoch(const speo_segment *segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
+                                     const float *pop_in, const float *fit_in, float *pop_out, float *fit_out,
+                                     uint32_t *d_gen, int generations, void *stream)
+{
+    return speo_generation_epoch_ex(segs, n_segs, dim_lo, dim_hi, max_pop, pop_in, fit_in, pop_out, fit_out, d_gen,
+                                    generations, 0, stream);
 }

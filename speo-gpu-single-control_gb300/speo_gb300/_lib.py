@@ -103,6 +103,8 @@ SIGNATURES: dict[str, tuple] = {
     "speo_epoch_fits": (c_int, [c_int, c_int]),
     "speo_generation_epoch": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_int, c_void_p]),
+    "speo_generation_epoch_ex": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                         c_void_p, c_void_p, c_int, c_int, c_void_p]),
     "speo_ring_migrate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "speo_ring_migrate_noalloc": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p]),
     "speo_surrogate_create": (c_int, [c_void_p, c_int, c_int, ctypes.c_longlong, c_int, c_float, c_float, c_uint64]),

@@ -141,15 +141,16 @@ class SegmentTable:
         L = _lib.load()
         return bool(L.speo_epoch_fits(max(sp.pop_size for sp in self.specs), self.dim_hi))
 
-    def epoch(self, generations: int):
-        """`generations` generations with every island resident in shared memory (in place)."""
+    def epoch(self, generations: int, cluster: int = 0):
+        """`generations` generations with every island resident in shared memory (in place);
+        cluster: 0 = library's choice, 1 = one block per island, 2 = two-block clusters."""
         L = _lib.load()
         w = self.cur
-        _lib.check(L.speo_generation_epoch(self.d_segs.data_ptr(), len(self.specs), self.dim_lo, self.dim_hi,
-                                           max(sp.pop_size for sp in self.specs), self.pop[w].data_ptr(),
-                                           self.fit[w].data_ptr(), self.pop[w].data_ptr(), self.fit[w].data_ptr(),
-                                           self.gen.data_ptr(), generations, self._stream()),
-                   "speo_generation_epoch")
+        _lib.check(L.speo_generation_epoch_ex(self.d_segs.data_ptr(), len(self.specs), self.dim_lo, self.dim_hi,
+                                              max(sp.pop_size for sp in self.specs), self.pop[w].data_ptr(),
+                                              self.fit[w].data_ptr(), self.pop[w].data_ptr(), self.fit[w].data_ptr(),
+                                              self.gen.data_ptr(), generations, cluster, self._stream()),
+                   "speo_generation_epoch_ex")
 
     def tc_generation(self, trial: torch.Tensor, trial_fit: torch.Tensor):
         """One generation with the rotation on the tensor cores: one DE trial per target

@@ -392,12 +392,15 @@ def test_evaluate_tc_matches_oracle(oracle, cuda, layout):
 # ---------------------------------------------------------------------------------------------
 # island-resident epochs
 # ---------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("cluster", [1, 2])
 @pytest.mark.parametrize("layout,gens", [
     ([(100, 30, 9, 4)] * 8, 7),                         # config-1 islands
     ([(256, 50, 9, 4)] * 3, 5),                         # config-4 islands
     ([(40, 20, 31, 2), (64, 17, 9, 7), (5, 3, 31, 5)], 6),  # best-row strategies, tiny islands
 ])
-def test_epoch_equals_per_generation_launches(oracle, cuda, layout, gens):
+def test_epoch_equals_per_generation_launches(oracle, cuda, layout, gens, cluster):
+    """Island-resident epochs, one block or a two-block cluster per island, bit-identical to the
+    same number of per-generation launches."""
     import torch
 
     a = _table(cuda, layout)
@@ -407,7 +410,7 @@ def test_epoch_equals_per_generation_launches(oracle, cuda, layout, gens):
     assert a.epoch_fits()
     for _ in range(gens):
         a.generation()
-    b.epoch(gens)
+    b.epoch(gens, cluster)
     torch.cuda.synchronize()
     assert np.array_equal(a.pop[a.cur].cpu().numpy(), b.pop[b.cur].cpu().numpy())
     assert np.array_equal(a.fit[a.cur].cpu().numpy(), b.fit[b.cur].cpu().numpy())
@@ -416,7 +419,7 @@ def test_epoch_equals_per_generation_launches(oracle, cuda, layout, gens):
     segs = b.oracle_segments()
     pop = b.pop[b.cur].cpu().numpy()
     fit = b.fit[b.cur].cpu().numpy()
-    b.epoch(2)
+    b.epoch(2, cluster)
     torch.cuda.synchronize()
     for g in range(2):
         pop, fit, trials, _, err = oracle.generation(segs, gens + g, pop, fit)
