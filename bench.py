@@ -207,7 +207,11 @@ def bench_speo(args) -> dict:
     if mode == "resident":
         kg = capture(torch, lambda: tab.epoch(INTERVAL))
         launch_ms = time_graph(torch, kg, reps, flush)
-        kernel = f"k_island_epoch<1> ({INTERVAL} generations per launch, islands resident in shared memory)"
+        if 2 * N_ISLANDS <= torch.cuda.get_device_properties(dev).multi_processor_count:
+            kernel = (f"k_island_epoch2<1> ({INTERVAL} generations per launch, each island resident in the "
+                      f"shared memory of a two-block cluster: {2 * N_ISLANDS} blocks)")
+        else:
+            kernel = f"k_island_epoch<1> ({INTERVAL} generations per launch, islands resident in shared memory)"
         alg_bytes = alg_bytes_gen * INTERVAL
     else:
         kg = capture(torch, lambda: [tab.generation() for _ in range(INTERVAL)])
@@ -238,7 +242,11 @@ def bench_speo(args) -> dict:
         "best_error_f64_after_run": best_err,
         "roofline": {"kernel": kernel, "bound": "hbm",
                      "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
-                     "traffic": None, "peak_src": pk["src"],
+                     "traffic": EPOCH_TRAFFIC_BYTES if mode == "resident" else None,
+                     "traffic_src": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_island_epoch2 launch "
+                                    "at this workload (the island is read once per launch; its writes stay in L2)"
+                     if mode == "resident" else None,
+                     "peak_src": pk["src"],
                      "alg_bytes_per_launch": alg_bytes, "launch_us": launch_ms * 1e3,
                      "note": "achieved = algorithmic bytes of a streaming generation (5 D s + 2 s per "
                              "individual-generation) / launch time"},
@@ -426,6 +434,10 @@ def bench_config3(L, dev, torch, flush) -> dict:
             "tile_rows": best}
 
 
+# DRAM bytes of one 50-generation island-resident launch of this workload (64 x 100, D = 30), from
+# an ncu capture (dram__bytes_read.sum 932,352 + dram__bytes_write.sum 0): the algorithmic bytes of
+# the same 50 streaming generations are 194.6 MB.
+EPOCH_TRAFFIC_BYTES = 932352
 C4_TRAIN_STEPS = 48   # Adam steps per generation: 48 x 4096 = 6 passes over a generation's 32768 new rows
 C4_EXPLORE = 0.05     # fraction of targets that take a uniformly drawn trial instead of the screened one
 
