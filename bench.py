@@ -100,16 +100,36 @@ def flush_l2(buf) -> None:
     buf.add_(1.0)   # writes 512 MB, > 4x the 129 MB L2
 
 
-def island_table(device: str, rank: int):
-    from speo_gb300.device import SegmentSpec, SegmentTable
+def island_specs(rank: int):
+    """Config 1's island ring for one rank: under torchrun each rank runs an independent replica
+    of the ring (its own Philox seeds, the same instance), so per-GPU work is fixed as N grows."""
+    from speo_gb300.device import SegmentSpec
     from speo_gb300.instances import make_instance
 
     seed = run_seed()
     inst = [make_instance(seed, DIM)]
     specs = [SegmentSpec(pop_size=POP, dim=DIM, func_id=FUNC, instance=0, seed=seed * 1000003 + rank,
                          ring_next=(i + 1) % N_ISLANDS) for i in range(N_ISLANDS)]
+    return specs, inst
+
+
+def island_table(device: str, rank: int):
+    from speo_gb300.device import SegmentTable
+
+    specs, inst = island_specs(rank)
     # tiles of 50 rows: two balanced tiles per island
     return SegmentTable(specs, inst, tile_rows=50, device=device)
+
+
+def max_over_ranks(value: float, device: str, world: int) -> float:
+    """The largest of the ranks' values (the job's time is its slowest rank's)."""
+    if world <= 1:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
 
 
 def capture(torch, fn):
@@ -193,11 +213,7 @@ def bench_speo(args) -> dict:
         torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    ms = sum(a.elapsed_time(b) for a, b in ev)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), dev, world)
     evals_per_step = N_ISLANDS * POP
     value = evals_per_step * steps * world / (ms / 1e3)
 
@@ -255,6 +271,8 @@ def bench_speo(args) -> dict:
         "gpu_launches": epochs * ((1 if mode == "resident" else INTERVAL) + 2),
         "clocks": clk.summary(),
     }
+    if rank != 0:  # the remaining sections are single-GPU measurements: rank 0 alone
+        return out
     if not args.no_ops:
         out["operators_bandwidth_scale"] = bench_operators(L, dev, torch, pk)
     if not args.no_configs:
