@@ -178,24 +178,155 @@ void speo_oracle_init_population_f32(float *pop, int64_t row0, int n, int ld, in
 }
 
 /* ---- objectives ---------------------------------------------------------------------- */
+/* CEC2014 functions 1-16 and the rotated sphere (31), restated from the reference's CPU code
+ * (CUDA_EA_library/CEC2014.cc): EvaluateFitness dispatch :14-144 (id, rate, rotation, fixed
+ * shift), sr_func :1395-1435 (ye = (x - o) * rate, z = M ye), the function bodies :462-953.
+ * Returns f(x) - f*, the reference's convention. */
 #define ORACLE_PI 3.1415926535897932384626433832795029
+#define ORACLE_E 2.7182818284590452353602874713526625
+
+double speo_oracle_func_rate(int fid)
+{
+    switch (fid) {
+    case 4: return 2.048 / (double)100;
+    case 6: return 0.5 / (double)100;
+    case 7: return 6.0;
+    case 8: case 9: return 5.12 / (double)100;
+    case 10: case 11: return 10.0;
+    case 12: case 13: case 14: case 15: return 5 / (double)100;
+    default: return 1.0;
+    }
+}
+int speo_oracle_func_rotated(int fid) { return fid != 8 && fid != 10; }
+static double fixed_shift(int fid) { return (fid == 4 || fid == 15) ? 1.0 : 0.0; }
+
+/* f from z (after rate, rotation and the fixed shift), in the reference's order of operations. */
+double speo_oracle_cec_from_z(int fid, const double *z, int nx)
+{
+    double f = 0.0;
+    switch (fid) {
+    case 1: /* ellips_func :481-497 */
+        for (int i = 0; i < nx; i++) f += pow(10.0, 6.0 * i / (nx - 1)) * z[i] * z[i];
+        return f;
+    case 2: /* bent_cigar_func :499-516 */
+        f = z[0] * z[0];
+        for (int i = 1; i < nx; i++) f += pow(10.0, 6.0) * z[i] * z[i];
+        return f;
+    case 3: /* discus_func :518-531 */
+        f = pow(10.0, 6.0) * z[0] * z[0];
+        for (int i = 1; i < nx; i++) f += z[i] * z[i];
+        return f;
+    case 4: /* rosenbrock_func :552-567 */
+        for (int i = 0; i < nx - 1; i++) {
+            const double t1 = z[i] * z[i] - z[i + 1], t2 = z[i] - 1.0;
+            f += 100.0 * t1 * t1 + t2 * t2;
+        }
+        return f;
+    case 5: { /* ackley_func :590-613 */
+        double s1 = 0.0, s2 = 0.0;
+        for (int i = 0; i < nx; i++) { s1 += z[i] * z[i]; s2 += cos(2.0 * ORACLE_PI * z[i]); }
+        s1 = -0.2 * sqrt(s1 / (double)nx);
+        s2 /= (double)nx;
+        return ORACLE_E - 20.0 * exp(s1) + 20.0 - exp(s2);
+    }
+    case 6: { /* weierstrass_func :615-644 */
+        double sum2 = 0.0;
+        for (int i = 0; i < nx; i++) {
+            double sum = 0.0;
+            sum2 = 0.0;
+            for (int j = 0; j <= 20; j++) {
+                sum += pow(0.5, j) * cos(2.0 * ORACLE_PI * pow(3.0, j) * (z[i] + 0.5));
+                sum2 += pow(0.5, j) * cos(2.0 * ORACLE_PI * pow(3.0, j) * 0.5);
+            }
+            f += sum;
+        }
+        return f - nx * sum2;
+    }
+    case 7: { /* griewank_func :646-666 */
+        double s = 0.0, p = 1.0;
+        for (int i = 0; i < nx; i++) { s += z[i] * z[i]; p *= cos(z[i] / sqrt(1.0 + i)); }
+        return 1.0 + s / 4000.0 - p;
+    }
+    case 8: case 9: /* rastrigin_func :668-683 */
+        for (int i = 0; i < nx; i++) f += (z[i] * z[i] - 10.0 * cos(2.0 * ORACLE_PI * z[i]) + 10.0);
+        return f;
+    case 10: case 11: /* schwefel_func :705-737 */
+        for (int i = 0; i < nx; i++) {
+            const double zi = z[i] + 4.209687462275036e+002;
+            if (zi > 500) {
+                f -= (500.0 - fmod(zi, 500)) * sin(pow(500.0 - fmod(zi, 500), 0.5));
+                const double t = (zi - 500.0) / 100;
+                f += t * t / nx;
+            } else if (zi < -500) {
+                f -= (-500.0 + fmod(fabs(zi), 500)) * sin(pow(500.0 - fmod(fabs(zi), 500), 0.5));
+                const double t = (zi + 500.0) / 100;
+                f += t * t / nx;
+            } else {
+                f -= zi * sin(pow(fabs(zi), 0.5));
+            }
+        }
+        return f + 4.189828872724338e+002 * nx;
+    case 12: { /* katsuura_func :739-763 */
+        double p = 1.0;
+        const double e3 = pow(1.0 * nx, 1.2);
+        for (int i = 0; i < nx; i++) {
+            double t = 0.0;
+            for (int j = 1; j <= 32; j++) {
+                const double a = pow(2.0, j), b = a * z[i];
+                t += fabs(b - floor(b + 0.5)) / a;
+            }
+            p *= pow(1.0 + (i + 1) * t, 10.0 / e3);
+        }
+        const double c = 10.0 / nx / nx;
+        return p * c - c;
+    }
+    case 13: case 14: { /* happycat_func :907-929, hgbat_func :931-953 */
+        double r2 = 0.0, sz = 0.0;
+        for (int i = 0; i < nx; i++) { const double zi = z[i] - 1.0; r2 += zi * zi; sz += zi; }
+        if (fid == 13) return pow(fabs(r2 - nx), 2 * (1.0 / 8.0)) + (0.5 * r2 + sz) / nx + 0.5;
+        return pow(fabs(pow(r2, 2.0) - pow(sz, 2.0)), 2 * (1.0 / 4.0)) + (0.5 * r2 + sz) / nx + 0.5;
+    }
+    case 15: /* grie_rosen_func :842-868 */
+        for (int i = 0; i < nx; i++) {
+            const int k = i + 1 < nx ? i + 1 : 0;
+            const double t1 = z[i] * z[i] - z[k], t2 = z[i] - 1.0;
+            const double t = 100.0 * t1 * t1 + t2 * t2;
+            f += (t * t) / 4000.0 - cos(t) + 1.0;
+        }
+        return f;
+    case 16: /* escaffer6_func :870-905 */
+        if (nx == 1) {
+            const double t1 = sin(z[0]), t2 = 1.0 + 0.001 * (z[0] * z[0]);
+            return 0.5 + (t1 * t1 - 0.5) / (t2 * t2);
+        }
+        for (int i = 0; i < nx; i++) {
+            const int k = i + 1 < nx ? i + 1 : 0;
+            const double s2 = z[i] * z[i] + z[k] * z[k];
+            const double t1 = sin(sqrt(s2)), t2 = 1.0 + 0.001 * s2;
+            f += 0.5 + (t1 * t1 - 0.5) / (t2 * t2);
+        }
+        return f;
+    default: /* 31: sphere_func :462-478 */
+        for (int i = 0; i < nx; i++) f += z[i] * z[i];
+        return f;
+    }
+}
 
 double speo_oracle_objective_f64(int func_id, const double *x, const double *o, const double *M, int dim)
 {
     /* sr_func (CEC2014.cc:1395-1435): ye = (x - o) * rate; z = M * ye (rotatefunc :1382-1393) */
-    double ye[SPEO_ORACLE_MAX_DIM];
-    const double rate = func_id == 9 ? 5.12 / (double)100 : 1.0;
+    double ye[SPEO_ORACLE_MAX_DIM], z[SPEO_ORACLE_MAX_DIM];
+    const double rate = speo_oracle_func_rate(func_id), fs = fixed_shift(func_id);
     for (int i = 0; i < dim; ++i) ye[i] = (x[i] - o[i]) * rate;
-    double f = 0.0;
     for (int i = 0; i < dim; ++i) {
-        double z = 0;
-        for (int j = 0; j < dim; ++j) z = z + ye[j] * M[i * dim + j];
-        if (func_id == 9)
-            f += (z * z - 10.0 * cos(2.0 * ORACLE_PI * z) + 10.0); /* rastrigin_func :668-683 */
-        else
-            f += z * z;                                             /* sphere_func :462-478 */
+        double zi = ye[i];
+        if (speo_oracle_func_rotated(func_id)) {
+            zi = 0;
+            for (int j = 0; j < dim; ++j) zi = zi + ye[j] * M[i * dim + j];
+        }
+        z[i] = zi + fs;
     }
-    return f;
+    return speo_oracle_cec_from_z(func_id, z, dim);
 }
 
 void speo_oracle_evaluate_rows(int func_id, const float *x, int n, int ld, int dim,

@@ -85,10 +85,14 @@ void speo_oracle_init_population_f32(float *pop, int64_t row0, int n, int ld, in
                                      float lb, float ub, const uint32_t key[2]);
 
 /* ---- Objectives in FP64. o has D entries; M is row-major D x D (file layout,
- * CEC2014.cc:354-369), z = M * (rate * (x - o)) as in sr_func (CEC2014.cc:1395-1435).
- *   9  rastrigin_func (CEC2014.cc:668-683): rate 0.0512, sum(z^2 - 10 cos(2 pi z) + 10)
- *  31  sphere_func    (CEC2014.cc:462-478): rate 1,      sum(z^2)
- * Both return f - f* (the reference's convention, CEC2014.cc:144). */
+ * CEC2014.cc:354-369), z = M * (rate * (x - o)) as in sr_func (CEC2014.cc:1395-1435), no
+ * rotation for ids 8 and 10, plus the fixed shift 1 of ids 4 and 15. Ids 1-16 follow the
+ * reference's EvaluateFitness dispatch (CEC2014.cc:14-144); 31 is sphere_func
+ * (CEC2014.cc:462-478), which the reference never dispatches. All return f - f*. */
+double speo_oracle_func_rate(int fid);
+int speo_oracle_func_rotated(int fid);
+/* f from the transformed vector z (rate, rotation and fixed shift already applied). */
+double speo_oracle_cec_from_z(int fid, const double *z, int nx);
 double speo_oracle_objective_f64(int func_id, const double *x, const double *o, const double *M, int dim);
 /* Batch helper for float rows: x rows are `ld` floats apart, o/M given as float (exactly
  * upcast to double). */

@@ -144,15 +144,28 @@ __host__ __device__ __forceinline__ bool strategy_uses_best(int st)
     return st == 2 || st == 3 || st == 6 || st == 7;
 }
 
-// Objective scale applied to z = M (x - o): F9 shrinks by 5.12/100 (CEC2014.cc:59-62).
-__host__ __device__ __forceinline__ float func_scale(int func_id)
+// ---- CEC2014 functions 1-16 and the rotated sphere (31) -------------------------------------
+// The reference's EvaluateFitness dispatch (CUDA_EA_library/CEC2014.cc:14-144): each id shifts,
+// scales by a rate, rotates (all but 8 and 10) and, for 4 and 15, adds a fixed shift of 1 before
+// the function body. z = rate * M (x - o) here (the same value as the reference's M (rate (x - o))
+// up to rounding).
+__host__ __device__ __forceinline__ bool func_supported(int f) { return (f >= 1 && f <= 16) || f == 31; }
+__host__ __device__ __forceinline__ bool func_rotated(int f) { return f != 8 && f != 10; }
+__host__ __device__ __forceinline__ double func_scale_f64(int f)
 {
-    return func_id == SPEO_FUNC_ROTATED_RASTRIGIN ? 0.0512f : 1.0f;
+    switch (f) {
+    case 4: return 2.048 / 100.0;
+    case 6: return 0.5 / 100.0;
+    case 7: return 6.0;
+    case 8: case 9: return 5.12 / 100.0;
+    case 10: case 11: return 10.0;
+    case 12: case 13: case 14: case 15: return 5.0 / 100.0;
+    default: return 1.0;
+    }
 }
-__host__ __device__ __forceinline__ double func_scale_f64(int func_id)
-{
-    return func_id == SPEO_FUNC_ROTATED_RASTRIGIN ? 5.12 / 100.0 : 1.0;
-}
+__host__ __device__ __forceinline__ float func_scale(int f) { return (float)func_scale_f64(f); }
+template <typename T>
+__host__ __device__ __forceinline__ T func_fixed_shift(int f) { return (f == 4 || f == 15) ? T(1) : T(0); }
 
 // sin(pi r) for |r| <= 1/2 from its Taylor series, odd terms through r^11 (truncation
 // (pi/2)^13 / 13! < 6e-8 relative at |r| = 1/2, exact limit r -> 0), Horner in r^2.
@@ -173,7 +186,7 @@ __device__ __forceinline__ float sin_pi_reduced(float r)
 // sine is reduced exactly (z - rint(z), exact in binary32 for |z| < 2^23; sin^2 has period 1).
 __device__ __forceinline__ float obj_term(int func_id, float z)
 {
-    if (func_id == SPEO_FUNC_ROTATED_RASTRIGIN) {
+    if (func_id == SPEO_FUNC_ROTATED_RASTRIGIN || func_id == 8) {
         const float s = sin_pi_reduced(__fsub_rn(z, rintf(z)));
         return __fmaf_rn(z, z, 20.0f * s * s);
     }
@@ -181,11 +194,123 @@ __device__ __forceinline__ float obj_term(int func_id, float z)
 }
 __device__ __forceinline__ double obj_term(int func_id, double z)
 {
-    if (func_id == SPEO_FUNC_ROTATED_RASTRIGIN) {
+    if (func_id == SPEO_FUNC_ROTATED_RASTRIGIN || func_id == 8) {
         const double s = sinpi(z);
         return z * z + 20.0 * s * s;
     }
     return z * z;
+}
+
+// Row objective as a streaming accumulator: push(j, z_j, z_next) for each coordinate (z_next =
+// z_{j+1}, or z_0 for the last coordinate), partial states combine by sum / product, finish(D)
+// applies the function's outer formula. Function bodies follow CEC2014.cc: ellips :481-497, bent
+// cigar :499-516, discus :518-531, Rosenbrock :552-567, Ackley :590-613, Weierstrass :615-644,
+// Griewank :646-666, Rastrigin :668-683, Schwefel :705-737, Katsuura :739-763, Griewank-Rosenbrock
+// :842-868, expanded Scaffer F6 :870-905, HappyCat :907-929, HGBat :931-953, sphere :462-478.
+// Weierstrass and Katsuura terms are evaluated in FP64 in both precisions (their high harmonics
+// amplify the argument by up to 3^20 and 2^32).
+template <typename T> struct RowAcc {
+    T s1 = T(0), s2 = T(0), p = T(1);
+};
+
+__device__ __forceinline__ float cos2pi(float z) { return cospif(2.f * z); }
+__device__ __forceinline__ double cos2pi(double z) { return cospi(2.0 * z); }
+
+template <typename T>
+__device__ __forceinline__ void row_push(RowAcc<T> &a, int f, int j, T z, T zn, int D)
+{
+    switch (f) {
+    case 1: {
+        const T w = sizeof(T) == 4 ? (T)exp10f(6.f * (float)j / (float)(D - 1)) : (T)pow(10.0, 6.0 * j / (D - 1));
+        a.s1 += w * z * z;
+        break;
+    }
+    case 2: a.s1 += (j == 0 ? T(1) : T(1e6)) * z * z; break;
+    case 3: a.s1 += (j == 0 ? T(1e6) : T(1)) * z * z; break;
+    case 4:
+        if (j < D - 1) {
+            const T t1 = z * z - zn, t2 = z - T(1);
+            a.s1 += T(100) * t1 * t1 + t2 * t2;
+        }
+        break;
+    case 5: a.s1 += z * z; a.s2 += cos2pi(z); break;
+    case 6: {
+        double s = 0.0, ak = 1.0, bk = 1.0;
+        for (int k = 0; k <= 20; ++k) {
+            s += ak * cospi(2.0 * bk * ((double)z + 0.5));
+            ak *= 0.5;
+            bk *= 3.0;
+        }
+        a.s1 += (T)s;
+        break;
+    }
+    case 7: a.s1 += z * z; a.p *= cos(z / sqrt(T(j + 1))); break;
+    case 10: case 11: {
+        const T zi = z + T(4.209687462275036e+002);
+        if (zi > T(500)) {
+            const T m = T(500) - fmod(zi, T(500));
+            a.s1 -= m * sin(sqrt(m));
+            const T t = (zi - T(500)) / T(100);
+            a.s1 += t * t / T(D);
+        } else if (zi < T(-500)) {
+            const T m = fmod(fabs(zi), T(500));
+            a.s1 -= (T(-500) + m) * sin(sqrt(T(500) - m));
+            const T t = (zi + T(500)) / T(100);
+            a.s1 += t * t / T(D);
+        } else {
+            a.s1 -= zi * sin(sqrt(fabs(zi)));
+        }
+        break;
+    }
+    case 12: {
+        double t = 0.0, p2 = 1.0;
+        for (int k = 1; k <= 32; ++k) {
+            p2 *= 2.0;
+            const double b = p2 * (double)z;
+            t += fabs(b - floor(b + 0.5)) / p2;
+        }
+        a.p *= (T)pow(1.0 + (j + 1) * t, 10.0 / pow((double)D, 1.2));
+        break;
+    }
+    case 13: case 14: {
+        const T zz = z - T(1);
+        a.s1 += zz * zz;
+        a.s2 += zz;
+        break;
+    }
+    case 15: {
+        const T t1 = z * z - zn, t2 = z - T(1);
+        const T t = T(100) * t1 * t1 + t2 * t2;
+        a.s1 += (t * t) / T(4000) - cos(t) + T(1);
+        break;
+    }
+    case 16: {
+        const T s2 = D == 1 ? z * z : z * z + zn * zn;
+        const T t1 = sin(sqrt(s2)), t2 = T(1) + T(0.001) * s2;
+        a.s1 += T(0.5) + (t1 * t1 - T(0.5)) / (t2 * t2);
+        break;
+    }
+    default: a.s1 += obj_term(f, z); break;  // 8, 9, 31: sum of per-coordinate terms
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T row_finish(const RowAcc<T> &a, int f, int D)
+{
+    switch (f) {
+    case 5:
+        return T(2.7182818284590452354) - T(20) * exp(T(-0.2) * sqrt(a.s1 / T(D))) + T(20) - exp(a.s2 / T(D));
+    case 6: return a.s1 + T(D) * (T(2) - T(9.5367431640625e-07));  // - D sum_k 0.5^k cos(pi 3^k)
+    case 7: return T(1) + a.s1 / T(4000) - a.p;
+    case 10: case 11: return a.s1 + T(4.189828872724338e+002) * T(D);
+    case 12: {
+        const T c = T(10) / T(D) / T(D);
+        return a.p * c - c;
+    }
+    case 13: return pow(fabs(a.s1 - T(D)), T(0.25)) + (T(0.5) * a.s1 + a.s2) / T(D) + T(0.5);
+    case 14: return sqrt(fabs(a.s1 * a.s1 - a.s2 * a.s2)) + (T(0.5) * a.s1 + a.s2) / T(D) + T(0.5);
+    default: return a.s1;
+    }
 }
 
 __device__ __forceinline__ float warp_sum(float v)
@@ -198,6 +323,14 @@ __device__ __forceinline__ double warp_sum(double v)
 {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_prod(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v *= __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 

@@ -56,17 +56,66 @@ __device__ __forceinline__ void eval_accumulate(T (&acc)[RPW][Q], const T *__res
     }
 }
 
-// f[rr] = sum over columns j < D of term(scale * acc[rr][j]); result valid on every lane.
+// The unrotated functions (8, 10): acc[rr][q] = Y[row0+rr][lane + 32q] (0 past D).
+template <typename T, int Q, int RPW>
+__device__ __forceinline__ void eval_identity(T (&acc)[RPW][Q], const T *__restrict__ Ys, int ys_ld, int row0, int D,
+                                              int lane)
+{
+#pragma unroll
+    for (int rr = 0; rr < RPW; ++rr)
+#pragma unroll
+        for (int q = 0; q < Q; ++q) acc[rr][q] = lane + 32 * q < D ? Ys[(row0 + rr) * ys_ld + lane + 32 * q] : T(0);
+}
+
+// One row's objective, z_j in lane j % 32 of element j / 32 (all lanes call it together). Out of
+// line, so that the kernels' per-coordinate-sum path carries none of its registers or stack.
+template <typename T, int Q> struct ZRow {
+    T v[Q];
+};
+template <typename T, int Q>
+__device__ __noinline__ T row_objective_warp(ZRow<T, Q> z, int D, int func_id, int lane)
+{
+    const T z0 = __shfl_sync(0xffffffffu, z.v[0], 0);
+    RowAcc<T> a;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const T dn = __shfl_down_sync(0xffffffffu, z.v[q], 1);
+        const T up = q + 1 < Q ? __shfl_sync(0xffffffffu, z.v[q + 1 < Q ? q + 1 : q], 0) : z0;
+        const int j = lane + 32 * q;
+        const T zn = j == D - 1 ? z0 : (lane < 31 ? dn : up);
+        if (j < D) row_push(a, func_id, j, z.v[q], zn, D);
+    }
+    a.s1 = warp_sum(a.s1);
+    a.s2 = warp_sum(a.s2);
+    a.p = warp_prod(a.p);
+    return row_finish(a, func_id, D);
+}
+
+// f[rr] = objective of the row whose column j = lane + 32q holds scale * acc[rr][q] (+ the fixed
+// shift); result valid on every lane. Sums of per-coordinate terms (8, 9, 31) add each lane's
+// columns in order and then reduce across the warp; the other functions run the row accumulator
+// per lane, with the next coordinate fetched from the neighbouring lane.
 template <typename T, int Q, int RPW>
 __device__ __forceinline__ void eval_reduce(const T (&acc)[RPW][Q], int D, int func_id, T scale, int lane, T (&f)[RPW])
 {
+    if (func_id == SPEO_FUNC_ROTATED_RASTRIGIN || func_id == SPEO_FUNC_ROTATED_SPHERE || func_id == 8) {
+#pragma unroll
+        for (int rr = 0; rr < RPW; ++rr) {
+            T s = T(0);
+#pragma unroll
+            for (int q = 0; q < Q; ++q)
+                if (lane + 32 * q < D) s += obj_term(func_id, acc[rr][q] * scale);
+            f[rr] = warp_sum(s);
+        }
+        return;
+    }
+    const T fs = func_fixed_shift<T>(func_id);
 #pragma unroll
     for (int rr = 0; rr < RPW; ++rr) {
-        T s = T(0);
+        ZRow<T, Q> z;
 #pragma unroll
-        for (int q = 0; q < Q; ++q)
-            if (lane + 32 * q < D) s += obj_term(func_id, acc[rr][q] * scale);
-        f[rr] = warp_sum(s);
+        for (int q = 0; q < Q; ++q) z.v[q] = acc[rr][q] * scale + fs;
+        f[rr] = row_objective_warp<T, Q>(z, D, func_id, lane);
     }
 }
 

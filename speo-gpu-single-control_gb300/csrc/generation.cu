@@ -202,14 +202,19 @@ __device__ __forceinline__ void gen_tile(const GenArgs &a, const speo_work_item 
     for (int rr = 0; rr < kRowsPerWarp; ++rr)
 #pragma unroll
         for (int q = 0; q < Q; ++q) acc[rr][q] = 0.f;
-    for (int kc = 0; kc < D; kc += Pl::KC) {
-        const int ke = min(kc + Pl::KC, D);
-        __syncthreads();
-        if (kc > 0) {
-            load_rot_rows<float, Q>(Ms, s.rot, s.ld_rot, D, kc, ke);
+    if (func_rotated(s.func_id)) {
+        for (int kc = 0; kc < D; kc += Pl::KC) {
+            const int ke = min(kc + Pl::KC, D);
             __syncthreads();
+            if (kc > 0) {
+                load_rot_rows<float, Q>(Ms, s.rot, s.ld_rot, D, kc, ke);
+                __syncthreads();
+            }
+            eval_accumulate<float, Q>(acc, Ys, W, warp * kRowsPerWarp, Ms, W, kc, ke, lane);
         }
-        eval_accumulate<float, Q>(acc, Ys, W, warp * kRowsPerWarp, Ms, W, kc, ke, lane);
+    } else {  // ids 8 and 10: no rotation
+        __syncthreads();
+        eval_identity<float, Q>(acc, Ys, W, warp * kRowsPerWarp, D, lane);
     }
     float f[kRowsPerWarp];
     eval_reduce<float, Q>(acc, D, s.func_id, func_scale(s.func_id), lane, f);

@@ -82,12 +82,17 @@ __device__ void eval_one_tile(const TileDesc &d, T *Ys, T *Ms)
     for (int rr = 0; rr < kRowsPerWarp; ++rr)
 #pragma unroll
         for (int q = 0; q < Q; ++q) acc[rr][q] = T(0);
-    for (int kc = 0; kc < d.D; kc += kChunk) {
-        const int ke = min(kc + kChunk, d.D);
+    if (func_rotated(d.func)) {
+        for (int kc = 0; kc < d.D; kc += kChunk) {
+            const int ke = min(kc + kChunk, d.D);
+            __syncthreads();
+            load_rot_rows<T, Q>(Ms, rot, d.ld_rot, d.D, kc, ke);
+            __syncthreads();
+            eval_accumulate<T, Q>(acc, Ys, W, warp * kRowsPerWarp, Ms, W, kc, ke, lane);
+        }
+    } else {  // ids 8 and 10: no rotation
         __syncthreads();
-        load_rot_rows<T, Q>(Ms, rot, d.ld_rot, d.D, kc, ke);
-        __syncthreads();
-        eval_accumulate<T, Q>(acc, Ys, W, warp * kRowsPerWarp, Ms, W, kc, ke, lane);
+        eval_identity<T, Q>(acc, Ys, W, warp * kRowsPerWarp, d.D, lane);
     }
     T f[kRowsPerWarp];
     const T scale = sizeof(T) == 4 ? (T)func_scale(d.func) : (T)func_scale_f64(d.func);
@@ -140,10 +145,9 @@ __global__ void __launch_bounds__(256) k_eval_seg(const speo_segment *segs, cons
 __global__ void __launch_bounds__(256) k_best_reeval(const speo_segment *segs, const float *pop, const float *fit,
                                                      int64_t *best_row, double *best_err)
 {
-    __shared__ double ys[SPEO_MAX_DIM];
+    __shared__ double ys[SPEO_MAX_DIM], zs[SPEO_MAX_DIM];
     __shared__ float bfs[8];
     __shared__ long long brs[8];
-    __shared__ double parts[8];
     const speo_segment &s = segs[blockIdx.x];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (s.pop_size < 1 || s.dim < 1 || s.dim > SPEO_MAX_DIM) {
@@ -177,21 +181,27 @@ __global__ void __launch_bounds__(256) k_best_reeval(const speo_segment *segs, c
     for (int k = threadIdx.x; k < D; k += blockDim.x)
         ys[k] = (double)pop[row * s.ld + k] - (double)s.shift[k];
     __syncthreads();
-    const double scale = func_scale_f64(s.func_id);
-    double part = 0.0;
+    const int fid = s.func_id;
+    const double scale = func_scale_f64(fid), fs = func_fixed_shift<double>(fid);
     for (int j = threadIdx.x; j < D; j += blockDim.x) {
-        double z = 0.0;
-        for (int k = 0; k < D; ++k) z = __fma_rn(ys[k], (double)s.rot[(size_t)k * s.ld_rot + j], z);
-        part += obj_term(s.func_id, z * scale);
+        double z = ys[j];
+        if (func_rotated(fid)) {
+            z = 0.0;
+            for (int k = 0; k < D; ++k) z = __fma_rn(ys[k], (double)s.rot[(size_t)k * s.ld_rot + j], z);
+        }
+        zs[j] = z * scale + fs;
     }
-    part = warp_sum(part);
-    if (lane == 0) parts[warp] = part;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < blockDim.x / 32; ++w) t += parts[w];
-        best_err[blockIdx.x] = t;
-        best_row[blockIdx.x] = row;
+    if (warp == 0) {
+        RowAcc<double> a;
+        for (int j = lane; j < D; j += 32) row_push(a, fid, j, zs[j], zs[j + 1 < D ? j + 1 : 0], D);
+        a.s1 = warp_sum(a.s1);
+        a.s2 = warp_sum(a.s2);
+        a.p = warp_prod(a.p);
+        if (lane == 0) {
+            best_err[blockIdx.x] = row_finish(a, fid, D);
+            best_row[blockIdx.x] = row;
+        }
     }
 }
 
@@ -210,8 +220,8 @@ int launch_ref(const T *X, int ldx, int P, int D, int func, const T *shift, cons
 template <typename T>
 int eval_ref(T *fit, T *X, T *shift, T *rot, int P, int D, int func)
 {
-    if (func != SPEO_FUNC_ROTATED_RASTRIGIN && func != SPEO_FUNC_ROTATED_SPHERE)
-        return fail(SPEO_ERR_UNSUPPORTED, "API_evaluateFitness: function_ID %d is not implemented", func);
+    if (!func_supported(func))
+        return fail(SPEO_ERR_UNSUPPORTED, "API_evaluateFitness: function_ID %d is not implemented (1-16, 31)", func);
     if (!fit || !X || !shift || !rot) return fail(SPEO_ERR_INVALID_ARG, "API_evaluateFitness: null pointer");
     if (P <= 0 || D < 1 || D > SPEO_MAX_DIM)
         return fail(SPEO_ERR_INVALID_ARG, "API_evaluateFitness: pop_size %d, dim %d", P, D);

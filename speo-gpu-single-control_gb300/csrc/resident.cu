@@ -42,7 +42,7 @@ __device__ __forceinline__ int donors_for(int st)
 __host__ __device__ __forceinline__ int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
 // Shared memory of one island with population bound Pmax and column class Q (W = 32Q):
-//   pop[Pmax][W] fit[Pmax] | Xs[Pt][W] Ys[Pt][W] | Ms[D<=32Q][W] | sR[GB][Pmax][8] sF[Pt] | o[W]
+//   pop[Pmax][W] fit[round_up(Pmax, 4)] | Xs[Pt][W] Ys[Pt][W] | Ms[D<=32Q][W] | sR[GB][Pmax][8] sF[Pt] | o[W]
 // The donor draws depend only on (seed, row, generation), so the block draws them for the next GB
 // generations at once (GB x P rows over all threads, instead of P rows per generation).
 template <int Q> struct ResPlan {
@@ -60,7 +60,8 @@ __host__ __device__ inline int draw_gens(int Pmax)
 __host__ __device__ inline size_t res_smem_floats(int Q, int Pmax)
 {
     const int W = 32 * Q, Pt = round_up(Pmax, kEvalRows);
-    return (size_t)Pmax * W + Pmax + 2 * (size_t)Pt * W + (size_t)W * W + (size_t)draw_gens(Pmax) * Pmax * 8 + Pt + W;
+    return (size_t)Pmax * W + round_up(Pmax, 4) + 2 * (size_t)Pt * W + (size_t)W * W + (size_t)draw_gens(Pmax) * Pmax * 8 +
+           Pt + W;
 }
 
 template <int Q>
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int Pt = round_up(Pmax, kEvalRows);
     float *pop = sm;
     float *fit = pop + (size_t)Pmax * W;
-    float *Xs = fit + Pmax;
+    float *Xs = fit + round_up(Pmax, 4);  // 16-byte aligned: Xs / Ys rows are read as float4
     float *Ys = Xs + (size_t)Pt * W;
     float *Ms = Ys + (size_t)Pt * W;
     const int GB = draw_gens(Pmax);
@@ -197,7 +198,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 for (int rr = 0; rr < kRowsPerWarp; ++rr)
 #pragma unroll
                     for (int q = 0; q < Q; ++q) acc[rr][q] = 0.f;
-                eval_accumulate<float, Q>(acc, Ys, W, pb + warp * kRowsPerWarp, Ms, W, 0, D, lane);
+                if (func_rotated(s.func_id))
+                    eval_accumulate<float, Q>(acc, Ys, W, pb + warp * kRowsPerWarp, Ms, W, 0, D, lane);
+                else
+                    eval_identity<float, Q>(acc, Ys, W, pb + warp * kRowsPerWarp, D, lane);
                 float f[kRowsPerWarp];
                 eval_reduce<float, Q>(acc, D, s.func_id, scale, lane, f);
                 if (lane == 0)
@@ -282,11 +286,12 @@ constexpr int kEvalRows2 = kWarpsR * kRowsPerWarp2;  // 64 rows per evaluation p
 __host__ __device__ inline int half_rows(int Pmax) { return (Pmax + 1) / 2; }
 __host__ __device__ inline int draw_gens2(int Pmax) { return draw_gens(half_rows(Pmax)); }
 
-//   pop[2][Pmax][W] fit[2][Pmax] | Xs[Ph][W] Ys[Ph][W] | Ms[W][W] | sR[GB][h][8] sF[Ph] | o[W]
+//   pop[2][Pmax][W] fit[2][round_up(Pmax, 4)] | Xs[Ph][W] Ys[Ph][W] | Ms[W][W] | sR[GB][h][8] sF[Ph] | o[W]
 __host__ __device__ inline size_t res2_smem_floats(int Q, int Pmax)
 {
     const int W = 32 * Q, h = half_rows(Pmax), Ph = round_up(h, kEvalRows2);
-    return 2 * ((size_t)Pmax * W + Pmax) + 2 * (size_t)Ph * W + (size_t)W * W + (size_t)draw_gens2(Pmax) * h * 8 + Ph +
+    return 2 * ((size_t)Pmax * W + round_up(Pmax, 4)) + 2 * (size_t)Ph * W + (size_t)W * W +
+           (size_t)draw_gens2(Pmax) * h * 8 + Ph +
            W;
 }
 
@@ -300,8 +305,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
     extern __shared__ __align__(16) float sm[];
     const int hmax = half_rows(Pmax), Ph = round_up(hmax, kEvalRows2), GB = draw_gens2(Pmax);
     float *const pop0 = sm;                               // pop buffer b at pop0 + b * Pmax * W
-    float *const fit0 = sm + 2 * (size_t)Pmax * W;        // fit buffer b at fit0 + b * Pmax
-    float *Xs = fit0 + 2 * Pmax;
+    const int Pf = round_up(Pmax, 4);                     // fit buffers padded: Xs stays 16-byte aligned
+    float *const fit0 = sm + 2 * (size_t)Pmax * W;        // fit buffer b at fit0 + b * Pf
+    float *Xs = fit0 + 2 * Pf;
     float *Ys = Xs + (size_t)Ph * W;
     float *Ms = Ys + (size_t)Ph * W;
     int *sR = reinterpret_cast<int *>(Ms + W * W);
@@ -344,7 +350,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
             const uint32_t gen = gen0 + (uint32_t)g;
             const int cur = g & 1, nxt = cur ^ 1;
             const float *pop = pop0 + (size_t)cur * Pmax * W;
-            const float *fit = fit0 + cur * Pmax;
+            const float *fit = fit0 + cur * Pf;
             __syncthreads();
             int best = -1;
             if (strategy_uses_best(st)) {
@@ -432,7 +438,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
                 for (int rr = 0; rr < kRowsPerWarp2; ++rr)
 #pragma unroll
                     for (int q = 0; q < Q; ++q) acc[rr][q] = 0.f;
-                eval_accumulate<float, Q>(acc, Ys, W, pb + warp * kRowsPerWarp2, Ms, W, 0, D, lane);
+                if (func_rotated(s.func_id))
+                    eval_accumulate<float, Q>(acc, Ys, W, pb + warp * kRowsPerWarp2, Ms, W, 0, D, lane);
+                else
+                    eval_identity<float, Q>(acc, Ys, W, pb + warp * kRowsPerWarp2, D, lane);
                 float f[kRowsPerWarp2];
                 eval_reduce<float, Q>(acc, D, s.func_id, scale, lane, f);
                 if (lane == 0)
@@ -443,9 +452,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
             // (4) greedy selection (strict `<`, kernel_DE_CUDA.cu:312) into the next buffer of both
             // replicas
             float *npop = pop0 + (size_t)nxt * Pmax * W;
-            float *nfit = fit0 + nxt * Pmax;
+            float *nfit = fit0 + nxt * Pf;
             const uint32_t ppop = peer_pop0 + (uint32_t)(nxt * Pmax * W * sizeof(float));
-            const uint32_t pfit = peer_fit0 + (uint32_t)(nxt * Pmax * sizeof(float));
+            const uint32_t pfit = peer_fit0 + (uint32_t)(nxt * Pf * sizeof(float));
             for (int lr = grp; lr < nr; lr += Pl::RPP) {
                 const int r = rb + lr;
                 const float tf = sF[lr];
@@ -468,7 +477,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
         if (!ok_bound) atomicOr(&s_deverr, SPEO_DEVERR_BOUND_LIMIT);
         // ---- write this block's rows back --------------------------------------------------------
         const float *pop = pop0 + (size_t)(generations & 1) * Pmax * W;
-        const float *fit = fit0 + (generations & 1) * Pmax;
+        const float *fit = fit0 + (generations & 1) * Pf;
         for (int i = tid; i < nr * nch; i += kThreads) {
             const int lr = i / nch, c = i - lr * nch, r = rb + lr;
             *reinterpret_cast<float4 *>(pop_out + (row0 + r) * ld + 4 * c) = ld4s(pop + r * W + 4 * c);

@@ -189,7 +189,9 @@ __device__ __forceinline__ float epilogue_row(uint32_t tmem, int warp, int D, in
 
 __device__ __forceinline__ bool tc_tile_ok(const speo_work_item &it, const speo_segment &s, const EvalTcArgs &a)
 {
-    return it.count >= 1 && it.count <= kTileM && s.dim >= 1 && s.dim <= a.dim_hi && s.dim <= kTmemCols &&
+    // the tensor-core epilogue implements the sums of per-coordinate terms: ids 9 and 31
+    return (s.func_id == SPEO_FUNC_ROTATED_RASTRIGIN || s.func_id == SPEO_FUNC_ROTATED_SPHERE) && it.count >= 1 &&
+           it.count <= kTileM && s.dim >= 1 && s.dim <= a.dim_hi && s.dim <= kTmemCols &&
            s.ld == a.ld && it.first >= 0 && it.first + it.count <= s.pop_size && s.row0 >= 0 &&
            s.row0 + it.first + it.count <= a.n_rows;
 }

@@ -16,6 +16,10 @@ SPEO_ERR_INVALID_ARG = 1
 SPEO_ERR_CUDA = 2
 SPEO_ERR_UNSUPPORTED = 3
 SPEO_ERR_DEVICE_FLAG = 4
+SPEO_DEVERR_REDRAW_LIMIT = 0x1
+SPEO_DEVERR_BOUND_LIMIT = 0x2
+SPEO_DEVERR_WAIT_TIMEOUT = 0x4
+SPEO_DEVERR_BAD_SEGMENT = 0x8
 
 FUNC_ROTATED_RASTRIGIN = 9
 FUNC_ROTATED_SPHERE = 31

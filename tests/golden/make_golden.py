@@ -1,4 +1,5 @@
-"""Generates tests/golden/objective_f9.npz from the reference's own CPU objective.
+"""Generates tests/golden/objective_f9.npz and tests/golden/objective_cec.npz from the
+reference's own CPU objective.
 
 Run where the reference sources exist (it builds oracle/_ref/libref_cec.so from the
 reference's CUDA_EA_library/CEC2014.cc with `make -C oracle ref`):
@@ -9,6 +10,7 @@ For each D the reference supports (CEC2014.cc:318-321) it makes a seeded synthet
 (o, M) in the reference's input_data text format, lets CEC2014::EvaluateFitness (function 9,
 rotated Rastrigin, returns f - f*) evaluate a set of points, and stores inputs and outputs.
 The tests check the oracle's restatement against these values on any machine.
+objective_cec.npz holds the same for functions 1-16 at D = 10 and 30 (keys "<fid>_<D>_<o|M|X|f>").
 """
 from __future__ import annotations
 
@@ -58,6 +60,28 @@ def main() -> None:
         out[f"f_{D}"] = f
     np.savez_compressed(HERE / "objective_f9.npz", **out)
     print("wrote", HERE / "objective_f9.npz")
+
+    cec = {}
+    for fid in range(1, 17):
+        for D in (10, 30):
+            seed = run_seed(1, fid, D)
+            o, M = make_instance(seed, D)
+            rng = np.random.default_rng(seed + 11)
+            n = 12
+            X = np.empty((n, D), dtype=np.float32)
+            X[0] = o
+            X[1] = np.clip(o + rng.normal(0, 1e-2, D), -100, 100)
+            X[2] = np.clip(o + rng.normal(0, 1.0, D), -100, 100)
+            X[3:] = rng.uniform(-100, 100, (n - 3, D))
+            with tempfile.TemporaryDirectory() as tmp:
+                write_reference_data(tmp, fid, o, M)
+                assert ref.ref_cec_init(fid, D, tmp.encode()) == 0
+                Xd = np.ascontiguousarray(X, dtype=np.float64)
+                f = np.zeros(n, dtype=np.float64)
+                ref.ref_cec_eval_batch(Xd.ctypes.data, n, D, f.ctypes.data)
+            cec.update({f"{fid}_{D}_o": o, f"{fid}_{D}_M": M, f"{fid}_{D}_X": X, f"{fid}_{D}_f": f})
+    np.savez_compressed(HERE / "objective_cec.npz", **cec)
+    print("wrote", HERE / "objective_cec.npz")
 
 
 if __name__ == "__main__":

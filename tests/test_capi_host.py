@@ -97,9 +97,12 @@ def test_dropin_validation_happens_before_any_device_work(lib):
     assert lib.API_Initilize_f32(pop, None, ii, pi) == _lib.SPEO_ERR_INVALID_ARG
 
 
-def test_evaluate_rejects_unimplemented_function_id(lib):
-    lib.API_evaluateFitness_f32(*([ctypes.c_void_p(1)] * 10), 100, 30, 0.0, 5)
-    assert b"function_ID 5" in lib.speo_last_error()
+@pytest.mark.parametrize("fid", [0, 17, 23, 30, 32])
+def test_evaluate_rejects_unimplemented_function_id(lib, fid):
+    """Ids 1-16 (CEC2014) and 31 (rotated sphere) are implemented; the hybrid (17-22) and
+    composition (23-30) functions are not, and are refused before any device work."""
+    lib.API_evaluateFitness_f32(*([ctypes.c_void_p(1)] * 10), 100, 30, 0.0, fid)
+    assert f"function_ID {fid}".encode() in lib.speo_last_error()
 
 
 def test_struct_layouts_match_c(tmp_path):

@@ -193,10 +193,30 @@ def test_dropin_select_matches_oracle(lib, oracle, cuda, f64):
     assert np.array_equal(d.pfit.cpu().numpy(), pf)
 
 
+# Per-function fitness bars (rtol, atol) against the FP64 oracle. The defaults are the FP32 /
+# FP64 bars above; the exceptions are ill-conditioned in the input: the elliptic, bent-cigar and
+# discus functions (1-3) weight single coordinates up to 1e6 times the rest, so the FP32 rounding
+# of one rotated coordinate can dominate a row's error; Weierstrass (6) and Katsuura
+# (12) amplify z by up to 3^20 and 2^32 in their high harmonics, Schwefel (10, 11) and Ackley (5)
+# cancel terms of size ~400 D and ~20 near the optimum, and HappyCat / HGBat (13, 14) take
+# |r2 - D|^(1/4) and |r2^2 - s^2|^(1/2), which turn an FP32 rounding of r2 near the optimum into
+# a visible absolute error.
+ALL_FUNCS = list(range(1, 17)) + [31]
+TOL32 = {1: (1e-4, 1e-6), 2: (1e-4, 1e-6), 3: (1e-4, 1e-6), 5: (1e-5, 2e-5), 6: (2e-3, 5e-2), 10: (2e-4, 5e-2),
+         11: (2e-4, 5e-2), 12: (2e-4, 1e-5), 13: (1e-5, 5e-3), 14: (1e-5, 5e-3)}
+TOL64 = {5: (1e-12, 1e-12), 6: (1e-10, 1e-10), 10: (1e-11, 1e-8), 11: (1e-11, 1e-8), 12: (1e-10, 1e-12),
+         13: (1e-12, 1e-9), 14: (1e-12, 1e-9)}
+
+
+def _tol(fid, f64):
+    return (TOL64 if f64 else TOL32).get(fid, (FIT_RTOL_F64, 1e-12) if f64 else (FIT_RTOL_F32, FIT_ATOL_F32))
+
+
 @pytest.mark.parametrize("f64", [False, True])
-@pytest.mark.parametrize("fid", [9, 31])
+@pytest.mark.parametrize("fid", ALL_FUNCS)
 @pytest.mark.parametrize("P,D", [(100, 10), (130, 30), (64, 50), (70, 100), (5, 200)])
 def test_dropin_evaluate_matches_oracle(lib, oracle, cuda, f64, fid, P, D):
+    """API_evaluateFitness for every implemented function id (CEC2014 1-16, rotated sphere 31)."""
     import torch
     from speo_gb300.instances import make_instance
 
@@ -220,11 +240,46 @@ def test_dropin_evaluate_matches_oracle(lib, oracle, cuda, f64, fid, P, D):
     from speo_gb300 import _lib
     _lib.check(lib.API_CheckCUDAError(), "API_evaluateFitness")
     ref = oracle.evaluate_rows(fid, X, D, o, M)
-    assert float(f[0]) == 0.0
-    if f64:
-        np.testing.assert_allclose(f.cpu().numpy(), ref, rtol=FIT_RTOL_F64, atol=1e-12)
-    else:
-        _assert_fitness(f.cpu().numpy(), ref)
+    rtol, atol = _tol(fid, f64)
+    assert abs(float(f[0])) <= atol                    # f(o) - f* = 0
+    _assert_fitness(f.cpu().numpy(), ref, rtol=rtol, atol=atol)
+
+
+def test_segment_evaluate_all_functions(oracle, cuda):
+    """speo_evaluate on one table holding a segment of every function id (D = 30, one launch)."""
+    import torch
+
+    layout = [(40, 30, fid, 4) for fid in ALL_FUNCS]
+    tab = _table(cuda, layout)
+    tab.init_population()
+    out = torch.zeros_like(tab.fit[0])
+    tab.evaluate(which=tab.cur, out=out)
+    torch.cuda.synchronize()
+    pop, got = tab.pop[tab.cur].cpu().numpy(), out.cpu().numpy()
+    for s in tab.oracle_segments():
+        r = slice(s["row0"], s["row0"] + s["P"])
+        rtol, atol = _tol(s["func"], False)
+        _assert_fitness(got[r], oracle.evaluate_rows(s["func"], pop[r], s["D"], s["o"], s["M"]), rtol=rtol,
+                        atol=atol)
+
+
+def test_evaluate_tc_flags_functions_it_does_not_implement(lib, cuda):
+    """The tensor-core evaluation implements ids 9 and 31; a tile of another id is skipped and
+    raises SPEO_DEVERR_BAD_SEGMENT."""
+    import ctypes
+
+    import torch
+    from speo_gb300 import _lib
+
+    tab = _table(cuda, [(64, 30, 4, 4)], tile_rows=_lib.TILE_TC)
+    tab.init_population()
+    bits = ctypes.c_uint32()
+    _lib.check(lib.speo_device_error_bits(ctypes.byref(bits)), "clear flags")
+    out = torch.full_like(tab.fit[0], -1.0)
+    tab.evaluate(which=tab.cur, use_tc=True, out=out)
+    _lib.check(lib.speo_device_error_bits(ctypes.byref(bits)), "read flags")
+    assert bits.value & _lib.SPEO_DEVERR_BAD_SEGMENT
+    assert torch.all(out == -1.0)
 
 
 # ---------------------------------------------------------------------------------------------
@@ -288,6 +343,7 @@ def _check_generations(tab, oracle, n_gen=3):
     [(64, 50, 9, 2), (70, 50, 9, 6), (33, 50, 31, 3)],                # strategies that use the best row
     [(4, 1, 31, 4), (9, 3, 9, 8), (5, 7, 31, 0)],                     # smallest populations / dims
     [(40, 200, 9, 4)],                                                # largest column class
+    [(40, 30, 4, 4), (40, 30, 8, 4), (40, 20, 15, 6), (33, 20, 16, 4), (40, 10, 1, 2)],  # other CEC2014 ids
 ])
 def test_fused_generation_matches_oracle(oracle, cuda, layout):
     tab = _table(cuda, layout)
@@ -397,6 +453,8 @@ def test_evaluate_tc_matches_oracle(oracle, cuda, layout):
     ([(100, 30, 9, 4)] * 8, 7),                         # config-1 islands
     ([(256, 50, 9, 4)] * 3, 5),                         # config-4 islands
     ([(40, 20, 31, 2), (64, 17, 9, 7), (5, 3, 31, 5)], 6),  # best-row strategies, tiny islands
+    ([(50, 30, 10, 4), (50, 30, 4, 4), (50, 30, 12, 6), (50, 30, 16, 4)], 4),  # other CEC2014 ids
+    ([(37, 30, 9, 4), (23, 30, 31, 6), (37, 30, 9, 2)], 3),  # odd populations (shared-memory padding)
 ])
 def test_epoch_equals_per_generation_launches(oracle, cuda, layout, gens, cluster):
     """Island-resident epochs, one block or a two-block cluster per island, bit-identical to the

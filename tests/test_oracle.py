@@ -45,6 +45,21 @@ def test_objective_matches_reference_golden(oracle, D):
     np.testing.assert_allclose(mine, f_ref, rtol=0, atol=_bias_ulps(9))
 
 
+GOLDEN_CEC = Path(__file__).resolve().parent / "golden" / "objective_cec.npz"
+
+
+@pytest.mark.parametrize("fid", range(1, 17))
+@pytest.mark.parametrize("D", [10, 30])
+def test_cec_objectives_match_reference_golden(oracle, fid, D):
+    """CEC2014 functions 1-16: the oracle against the reference's own CEC2014::EvaluateFitness
+    (golden vectors from tests/golden/make_golden.py), at the optimum, near it and at random points."""
+    g = np.load(GOLDEN_CEC)
+    o, M, X, f_ref = (g[f"{fid}_{D}_{k}"] for k in "oMXf")
+    mine = np.array([oracle.objective(fid, x, o, M) for x in X])
+    # the reference adds and subtracts f* = 100 fid (CEC2014.cc:144): its values carry that rounding
+    np.testing.assert_allclose(mine, f_ref, rtol=1e-12, atol=_bias_ulps(fid))
+
+
 @pytest.mark.skipif(not REF_DATA.exists(), reason="reference suite data not present")
 @pytest.mark.parametrize("D", [10, 30, 100])
 def test_objective_matches_reference_on_suite_data(oracle, D):
