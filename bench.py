@@ -657,6 +657,7 @@ def bench_e2e(L, dev, torch, args) -> dict:
     L.speo_set_stream(ctypes.c_void_p(stream.cuda_stream))
     _lib.check(L.API_Initilize_f32(C, rng_state.data_ptr(), ii, pi), "API_Initilize_f32")
     steps = max(100, min(args.steps, 2000))
+    h_hist = torch.zeros(steps * n, dtype=torch.float32).pin_memory()  # every generation's fitness
 
     def upload():
         pop.copy_(h_pop, non_blocking=True)
@@ -669,7 +670,7 @@ def bench_e2e(L, dev, torch, args) -> dict:
     def run_native(nsteps):  # the reference's DE_CUDA::Run loop as one library call (C++ host loop)
         upload()
         _lib.check(L.speo_de_run_f32(P, C, rng_state.data_ptr(), ii, d_info.data_ptr(), best.data_ptr(), pi,
-                                     d_sh.data_ptr(), d_rot.data_ptr(), nsteps, h_fit.data_ptr(),
+                                     d_sh.data_ptr(), d_rot.data_ptr(), nsteps, h_hist.data_ptr(), 1,
                                      stream.cuda_stream), "speo_de_run_f32")
         stream.synchronize()
 
@@ -695,9 +696,10 @@ def bench_e2e(L, dev, torch, args) -> dict:
     h2d = (n * ld + ld * DIM + ld) * 4 + len(bytes(info))
     return {"value": out["native"], "unit": "evals/s", "h2d_bytes_per_step": h2d / steps,
             "d2h_bytes_per_step": n * 4, "steps": steps,
-            "path": "speo_de_run_f32: per generation API_DE_GenerateNewPopulation_f32 + API_evaluateFitness_f32 + "
-                    "API_DE_SelectSurvival_f32 + fitness read-back to pinned host memory (64 sub-islands of 100), "
-                    "blocks of 10 generations replayed as a CUDA graph",
+            "path": "speo_de_run_f32 (64 sub-islands of 100): the generations of API_DE_GenerateNewPopulation_f32 + "
+                    "API_evaluateFitness_f32 + API_DE_SelectSurvival_f32, bit-identical, with the sub-islands "
+                    "resident in shared memory for 25 generations per launch; every generation's fitness vector "
+                    "read back to pinned host memory (one copy per launch)",
             "python_loop_value": out["python"],
             "python_loop_path": "the same entry points called one by one from Python (ctypes), per-call host cost"}
 

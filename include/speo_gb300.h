@@ -165,15 +165,19 @@ SPEO_API void API_evaluateFitness_f32(float *d_fitness_value, float *d_shuffled_
 
 /* The reference's host generation loop (DE_CUDA::Run, CUDA_EA_library/DE_CUDA.cc:200-216),
  * natively: `generations` x (API_DE_GenerateNewPopulation_f32, API_evaluateFitness_f32 on
- * (d_shift, d_rot, problem_info.function_ID), API_DE_SelectSurvival_f32), each generation's
- * fitness vector copied to h_fitness (island_size floats, overwritten every generation; may be
- * null). Runs on a private stream ordered after `stream`; blocks of generations replay a CUDA graph
- * when h_fitness is pinned (or null). Synchronous: returns when the generations are done. No
- * counterpart function in the reference (it is the reference's caller loop, as a library call). */
+ * (d_shift, d_rot, problem_info.function_ID), API_DE_SelectSurvival_f32), with the same results
+ * as those calls issued one by one. When a sub-island fits one block's shared memory, blocks of
+ * generations run in one launch with the sub-island resident on chip; otherwise the three entry
+ * points run in turn (replayed as a CUDA graph when h_fitness is pinned or null). h_fitness (may
+ * be null): with history = 0, island_size floats that receive the last generation's fitness;
+ * with history != 0, generations x island_size floats that receive every generation's fitness
+ * (generation g at h_fitness + g * island_size). Runs on a private stream ordered after
+ * `stream`. Synchronous: returns when the generations are done. No counterpart function in the
+ * reference (it is the reference's caller loop, as a library call). */
 SPEO_API int speo_de_run_f32(speo_population_f32 d_population, speo_population_f32 d_candidate,
                              speo_rng_state *d_rng, speo_island_info island_info, speo_de_info_f32 *d_DE_info,
                              int *d_best_individual_ID, speo_problem_info_f32 problem_info, const float *d_shift,
-                             const float *d_rotated, int generations, float *h_fitness, void *stream);
+                             const float *d_rotated, int generations, float *h_fitness, int history, void *stream);
 
 /* ------------------------------------------------------------------------------------ */
 /* Library control                                                                       */

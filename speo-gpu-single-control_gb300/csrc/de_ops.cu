@@ -8,8 +8,7 @@
 // per target row, lanes over elements, draws from Philox instead of per-lane XORWOW states.
 #include <cmath>
 
-#include "common.cuh"
-#include "host.h"
+#include "dropin.cuh"
 
 SPEO_DEFINE_DEVERR(speo_deverr_de_ops)
 
@@ -23,25 +22,6 @@ int np2_of(int dim)
     int y = 1;
     while (y < dim) y <<= 1;
     return y < 32 ? 32 : y;
-}
-
-template <typename T> struct DeInfoT;
-template <> struct DeInfoT<float> { using type = speo_de_info_f32; };
-template <> struct DeInfoT<double> { using type = speo_de_info_f64; };
-
-// Advances the generation counter once every block of this launch has read it.
-__device__ __forceinline__ void finish_launch(RngState *rng, uint32_t gen)
-{
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned t = atomicAdd(&rng->done, 1u);
-        if (t == gridDim.x - 1) {
-            rng->done = 0;
-            rng->gen = gen + 1;
-            __threadfence();
-        }
-    }
 }
 
 // global_SetupRandomState + global_InitiPopulation (kernel_EA_CUDA.cu:85-118): one thread per
@@ -71,9 +51,6 @@ __global__ void k_init(T *elems, int n, int ld, int dim, T lb, T ub, uint2 key, 
 // global_DE_FindBestIndividualInIsland (kernel_DE_CUDA.cu:120-158), one warp per sub-island,
 // positions s*S .. s*S+S-1 (the reference reads the first sub-island's positions for all s).
 template <typename T>
-__device__ __forceinline__ T rank_t(T f) { return isnan(f) ? T(INFINITY) : f; }
-
-template <typename T>
 __global__ void k_best(const T *fit, const int *perm, int S, int nsub, int *best_id)
 {
     const int s = blockIdx.x * kWarps + (threadIdx.x >> 5);
@@ -93,50 +70,7 @@ __global__ void k_best(const T *fit, const int *perm, int S, int nsub, int *best
     if (lane == 0) best_id[s] = perm[s * S + bp];
 }
 
-// global_DE_GenerateNewPopulation (kernel_DE_CUDA.cu:172-289). A block takes 64 positions:
-// (1) one thread per position draws the donors and jrand (the reference recomputes them on all
-// 32 lanes), (2) G lanes per row build the trial from 16-byte vector loads of the target and
-// donor rows with one Philox block per 4 elements, and store it with vector stores.
-
-template <typename T> struct Vec;
-template <> struct Vec<float> { using type = float4; static constexpr int n = 4; };
-template <> struct Vec<double> { using type = double2; static constexpr int n = 2; };
-
-template <typename T>
-__device__ __forceinline__ T vget(const typename Vec<T>::type &v, int q)
-{
-    if constexpr (Vec<T>::n == 4) return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w;
-    else return q == 0 ? v.x : v.y;
-}
-template <typename T>
-__device__ __forceinline__ void vset(typename Vec<T>::type &v, int q, T x)
-{
-    if constexpr (Vec<T>::n == 4) { if (q == 0) v.x = x; else if (q == 1) v.y = x; else if (q == 2) v.z = x; else v.w = x; }
-    else { if (q == 0) v.x = x; else v.y = x; }
-}
-
-__device__ __forceinline__ int ndonors(int st)
-{
-    switch (st) {
-    case 0: case 2: case 6: return 2;
-    case 3: case 4: case 8: return 3;
-    case 1: case 7: return 4;
-    default: return 5;
-    }
-}
-
-// Crossover test `(T)u01(w) < CR` as an integer compare: u01(w) = k * 2^-24 with
-// k = (w >> 8) + 1, so u < CR  <=>  k < CR * 2^24  <=>  k < ceil(CR * 2^24) for integer k (the
-// scaling by 2^24 is exact). NaN CR takes no element, as the float compare does.
-template <typename T>
-__device__ __forceinline__ uint32_t cr_threshold(T CR)
-{
-    const T x = ceil(CR * (T)16777216.0);
-    if (!(x > (T)0)) return 0u;               // also NaN
-    return x >= (T)33554432.0 ? 33554432u : (uint32_t)x;
-}
-__device__ __forceinline__ bool cr_take(uint32_t w, uint32_t thr) { return (w >> 8) + 1u < thr; }
-
+// global_DE_GenerateNewPopulation (kernel_DE_CUDA.cu:172-289).
 // One warp owns ppw (4 .. 32) consecutive positions: lane l < ppw draws the donors and jrand of
 // position l (Philox on those lanes at once). The warp's ppw x nch (row, 16-byte chunk) tasks are
 // then dealt to the lanes in order, task t = it * 32 + lane, so no lane idles whatever D is; each

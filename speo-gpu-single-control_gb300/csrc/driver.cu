@@ -3,17 +3,45 @@
 // DE_CUDA::Run (CUDA_EA_library/DE_CUDA.cc:200-216) calls, per generation,
 // API_DE_GenerateNewPopulation, CEC2014_CUDA::EvaluateFitness (-> API_evaluateFitness) and
 // API_DE_SelectSurvival, with a device synchronisation after each launch; the island driver then
-// reads results back to the host (src/island_EA.cc:78-113). speo_de_run_f32 runs that loop over
-// this library's drop-in entry points on a private stream, ordered after the caller's stream:
-// blocks of kBlock generations (each with its read-back of the fitness vector into pinned host
-// memory) are captured once as a CUDA graph and replayed, so the per-generation host cost is one
-// graph launch per block instead of a synchronisation per kernel.
+// reads results back to the host (src/island_EA.cc:78-113). speo_de_run_f32 runs that loop on a
+// private stream, ordered after the caller's stream:
+//   * when a sub-island fits a block, kStepGens generations per launch of the fused kernel
+//     (dropin_step.cu, bit-identical to the three calls), each generation's fitness vector
+//     collected in a device history buffer and copied to the host once per launch;
+//   * otherwise over this library's drop-in entry points, where blocks of kBlock generations
+//     (each with its read-back of the fitness vector into pinned host memory) are captured once as
+//     a CUDA graph and replayed, so the per-generation host cost is one graph launch per block
+//     instead of a synchronisation per kernel.
 #include "host.h"
 
 namespace speo {
 namespace {
 
-constexpr int kBlock = 10;  // generations per captured graph
+constexpr int kBlock = 10;     // generations per captured graph (three-call path)
+constexpr int kStepGens = 25;  // generations per fused launch
+
+struct DriverHistory {
+    float *p = nullptr;
+    size_t cap = 0;  // floats
+};
+thread_local DriverHistory t_hist;
+
+// The device history buffer of this host thread, grown on demand (the previous call has
+// synchronised its stream, so nothing is using the old one).
+int history_buffer(size_t floats, float **out)
+{
+    DriverHistory &h = t_hist;
+    if (h.cap < floats) {
+        if (h.p) cudaFree(h.p);
+        h.p = nullptr;
+        h.cap = 0;
+        if (int e = check_cuda(cudaMalloc(reinterpret_cast<void **>(&h.p), sizeof(float) * floats), "driver: history"))
+            return e;
+        h.cap = floats;
+    }
+    *out = h.p;
+    return SPEO_OK;
+}
 
 struct DriverStream {
     cudaStream_t s = nullptr;
@@ -51,10 +79,10 @@ using namespace speo;
 extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand, speo_rng_state *rng,
                                speo_island_info ii, speo_de_info_f32 *d_info, int *d_best, speo_problem_info_f32 pi,
                                const float *d_shift, const float *d_rot, int generations, float *h_fitness,
-                               void *stream)
+                               int history, void *stream)
 {
     if (!pop.elements || !pop.fitness_value || !cand.elements || !cand.fitness_value || !rng || !d_info || !d_best ||
-        !d_shift || !d_rot || generations < 0 || ii.island_size <= 0)
+        !d_shift || !d_rot || !ii.permutated_index || generations < 0 || ii.island_size <= 0)
         return fail(SPEO_ERR_INVALID_ARG, "speo_de_run_f32: bad arguments");
     if (generations == 0) return SPEO_OK;
     DriverStream *d = nullptr;
@@ -66,28 +94,50 @@ extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand
     const cudaStream_t prev = api_stream();
     speo_set_stream(d->s);
 
-    auto one_generation = [&]() -> int {
-        if (int e = API_DE_GenerateNewPopulation_f32(cand, pop, d_best, ii, d_info, rng, pi)) return e;
+    const bool fused = dropin_step_fits_f32(ii.island_size, ii.subisland_num, pi.dim, pi.function_ID);
+    const bool hist = h_fitness && history;
+    int e = SPEO_OK, done = 0;
+    if (fused) {
+        float *d_hist = nullptr;
+        if (hist) e = history_buffer((size_t)kStepGens * n, &d_hist);
+        for (; !e && done < generations; done += kStepGens) {
+            const int k = generations - done < kStepGens ? generations - done : kStepGens;
+            e = dropin_step_f32(pop, cand, d_best, ii, d_info, rng, pi, d_shift, d_rot, k, d_hist, d->s);
+            if (!e && hist)
+                e = check_cuda(cudaMemcpyAsync(h_fitness + (size_t)done * n, d_hist, sizeof(float) * (size_t)k * n,
+                                               cudaMemcpyDeviceToHost, d->s),
+                               "driver: fitness read-back");
+        }
+        if (!e && h_fitness && !hist)
+            e = check_cuda(cudaMemcpyAsync(h_fitness, pop.fitness_value, sizeof(float) * (size_t)n,
+                                           cudaMemcpyDeviceToHost, d->s),
+                           "driver: fitness read-back");
+    }
+
+    // the three entry points in turn; generation g's fitness goes to h_fitness (+ g n with history)
+    int g_next = 0;
+    auto one_generation = [&](bool in_graph) -> int {
+        if (int e2 = API_DE_GenerateNewPopulation_f32(cand, pop, d_best, ii, d_info, rng, pi)) return e2;
         const int before = sticky_status();
         API_evaluateFitness_f32(cand.fitness_value, nullptr, nullptr, cand.elements, const_cast<float *>(d_shift),
                                 const_cast<float *>(d_rot), nullptr, nullptr, nullptr, nullptr, n, pi.dim, 0.f,
                                 pi.function_ID);
         if (sticky_status() != before) return sticky_status();
-        if (int e = API_DE_SelectSurvival_f32(pop, cand, ii, pi)) return e;
+        if (int e2 = API_DE_SelectSurvival_f32(pop, cand, ii, pi)) return e2;
+        float *dst = h_fitness + (hist && !in_graph ? (size_t)g_next * n : 0);
+        ++g_next;
         if (h_fitness)
-            return check_cuda(cudaMemcpyAsync(h_fitness, pop.fitness_value, sizeof(float) * (size_t)n,
+            return check_cuda(cudaMemcpyAsync(dst, pop.fitness_value, sizeof(float) * (size_t)n,
                                               cudaMemcpyDeviceToHost, d->s),
                               "driver: fitness read-back");
         return SPEO_OK;
     };
-
-    int e = SPEO_OK, done = 0;
-    if (generations >= 2 * kBlock && (!h_fitness || is_pinned(h_fitness))) {
+    if (!fused && !hist && generations >= 2 * kBlock && (!h_fitness || is_pinned(h_fitness))) {
         cudaGraph_t g = nullptr;
         cudaGraphExec_t x = nullptr;
         e = check_cuda(cudaStreamBeginCapture(d->s, cudaStreamCaptureModeThreadLocal), "driver: begin capture");
         if (!e) {
-            for (int i = 0; !e && i < kBlock; ++i) e = one_generation();
+            for (int i = 0; !e && i < kBlock; ++i) e = one_generation(true);
             const cudaError_t ce = cudaStreamEndCapture(d->s, &g);  // always ends the capture
             if (!e) e = check_cuda(ce, "driver: end capture");
         }
@@ -99,7 +149,8 @@ extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand
         if (x) cudaGraphExecDestroy(x);
         if (g) cudaGraphDestroy(g);
     }
-    for (; !e && done < generations; ++done) e = one_generation();
+    g_next = done;
+    for (; !e && done < generations; ++done) e = one_generation(false);
     speo_set_stream(prev);
     const int es = check_cuda(cudaStreamSynchronize(d->s), "driver: sync");
     if (!e) e = es;

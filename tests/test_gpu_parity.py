@@ -118,14 +118,23 @@ def test_dropin_generate_matches_oracle(lib, oracle, cuda, f64, P, D, nsub):
         assert int(d.rng.cpu()[2]) == gen + 1                    # generation counter advanced once
 
 
-@pytest.mark.parametrize("gens,pinned", [(25, True), (7, False)])
-def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned):
-    """speo_de_run_f32 (the reference's DE_CUDA::Run loop, natively; CUDA-graph blocks when the
-    fitness buffer is pinned) gives the same populations as the drop-in calls issued one by one."""
+@pytest.mark.parametrize("gens,pinned,history,P,D,nsub,fid,strats", [
+    (60, True, True, 200, 30, 2, 9, (4, 6)),         # config-1 sub-islands, several fused launches
+    (7, False, False, 200, 30, 2, 9, (4, 6)),        # pageable buffer, last generation only
+    (21, True, True, 111, 50, 3, 4, (2, 4, 7)),      # odd sub-islands of 37, best-row strategies, Rosenbrock
+    (6, True, True, 256, 100, 4, 31, (5, 3, 8, 0)),  # D = 100
+    (5, True, False, 64, 10, 1, 10, (1,)),           # unrotated Schwefel, one sub-island
+    (22, True, False, 4096, 100, 1, 9, (4,)),        # too large for one block: three calls, graph blocks
+    (4, True, True, 4096, 100, 1, 9, (4,)),          # the same with every generation's fitness
+])
+def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned, history, P, D, nsub, fid, strats):
+    """speo_de_run_f32 (the reference's DE_CUDA::Run loop, natively: sub-islands resident in shared
+    memory for blocks of generations, or the three calls replayed as a CUDA graph) gives the same
+    populations, candidates, best ids, generation counter and per-generation fitness as the drop-in
+    calls issued one by one."""
     import torch
     from speo_gb300.instances import make_instance
 
-    P, D, nsub = 200, 30, 2
     o, M = make_instance(77, D)
     ld = np2(D)
     rot = np.zeros((ld, D), dtype=np.float32)
@@ -137,38 +146,49 @@ def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned):
     pop0 = np.zeros((P, ld), dtype=np.float32)
     pop0[:, :D] = rng.uniform(-100, 100, (P, D))
     runs = []
+    perm = np.random.default_rng(P + D).permutation(P).astype(np.int32)
     for mode in ("calls", "driver"):
         d = DropIn(lib, cuda, P, D, nsub, False, seed=4321)
-        info = (d.DI * nsub)(*[d.DI(0.9, 0.5, 4 if i == 0 else 6, P // nsub) for i in range(nsub)])
+        d.problem.function_ID = fid
+        d.perm.copy_(torch.from_numpy(perm))
+        info = (d.DI * nsub)(*[d.DI(0.9 if i % 2 == 0 else 0.1, 0.5, strats[i % len(strats)], P // nsub)
+                               for i in range(nsub)])
         d_info = torch.frombuffer(bytearray(bytes(info)), dtype=torch.uint8).to(cuda)
         pop_s, cand_s = d.pops()
         d.call("API_Initilize", cand_s, d.rng.data_ptr(), d.island(), d.problem)
         d.pop.copy_(torch.from_numpy(pop0))
-        args = (None, None, d.pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(), None, None, None, None, P, D, 0.0, 9)
+        args = (None, None, d.pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(), None, None, None, None, P, D, 0.0, fid)
         d.lib.API_evaluateFitness_f32(d.pfit.data_ptr(), *args)
         if mode == "calls":
+            per_gen = []
             for _ in range(gens):
                 d.call("API_DE_GenerateNewPopulation", cand_s, pop_s, d.best.data_ptr(), d.island(),
                        d_info.data_ptr(), d.rng.data_ptr(), d.problem)
                 d.lib.API_evaluateFitness_f32(d.cfit.data_ptr(), None, None, d.cand.data_ptr(), d_sh.data_ptr(),
-                                              d_rot.data_ptr(), None, None, None, None, P, D, 0.0, 9)
+                                              d_rot.data_ptr(), None, None, None, None, P, D, 0.0, fid)
                 d.call("API_DE_SelectSurvival", pop_s, cand_s, d.island(), d.problem)
-            h = None
+                per_gen.append(d.pfit.cpu().numpy())
+            h = np.stack(per_gen)
         else:
-            h = torch.zeros(P, dtype=torch.float32)
+            h = torch.zeros((gens if history else 1) * P, dtype=torch.float32)
             if pinned:
                 h = h.pin_memory()
             d._lib.check(d.lib.speo_de_run_f32(pop_s, cand_s, d.rng.data_ptr(), d.island(), d_info.data_ptr(),
                                                d.best.data_ptr(), d.problem, d_sh.data_ptr(), d_rot.data_ptr(), gens,
-                                               h.data_ptr(), None), "speo_de_run_f32")
+                                               h.data_ptr(), int(history), None), "speo_de_run_f32")
+            h = h.numpy().reshape(-1, P)
         d._lib.check(d.lib.API_CheckCUDAError(), "API_CheckCUDAError")
-        runs.append((d.pop.cpu().numpy(), d.pfit.cpu().numpy(), None if h is None else h.numpy().copy(),
-                     int(d.rng.cpu()[2])))
-    (pa, fa, _, ga), (pb, fb, hb, gb) = runs
+        runs.append((d.pop.cpu().numpy(), d.pfit.cpu().numpy(), h.copy(),
+                     int(d.rng.cpu()[2]), d.cand.cpu().numpy(), d.cfit.cpu().numpy(), d.best.cpu().numpy()))
+    (pa, fa, ha, ga, ca, cfa, ba), (pb, fb, hb, gb, cb, cfb, bb) = runs
     assert np.array_equal(pa, pb)
     assert np.array_equal(fa, fb)
-    assert np.array_equal(hb, fb)          # the last generation's fitness read back
+    if history:
+        assert np.array_equal(hb, ha)      # every generation's fitness read back
+    else:
+        assert np.array_equal(hb[0], fb)   # the last generation's fitness read back
     assert ga == gb == gens
+    assert np.array_equal(ca, cb) and np.array_equal(cfa, cfb) and np.array_equal(ba, bb)
 
 
 @pytest.mark.parametrize("f64", [False, True])
