@@ -151,6 +151,9 @@ __host__ __device__ __forceinline__ bool strategy_uses_best(int st)
 // up to rounding).
 __host__ __device__ __forceinline__ bool func_supported(int f) { return (f >= 1 && f <= 16) || f == 31; }
 __host__ __device__ __forceinline__ bool func_rotated(int f) { return f != 8 && f != 10; }
+// Sums of one term per coordinate (8, 9, 31): the kernels' fast path; the others take the row
+// accumulator below.
+__host__ __device__ __forceinline__ bool func_sum_form(int f) { return f == 8 || f == 9 || f == 31; }
 __host__ __device__ __forceinline__ double func_scale_f64(int f)
 {
     switch (f) {

@@ -58,7 +58,8 @@ __host__ __device__ inline size_t step_smem_bytes(int Q, int S, int D)
            sizeof(int) * (size_t)step_draw_gens(S) * S * 8;
 }
 
-template <typename T, int Q>
+// G: the generic objective variant (ids other than 8, 9, 31).
+template <typename T, int Q, bool G>
 __global__ void __launch_bounds__(kThreadsS) k_de_step(StepArgs<T> a)
 {
     using V = typename Vec<T>::type;
@@ -215,7 +216,7 @@ __global__ void __launch_bounds__(kThreadsS) k_de_step(StepArgs<T> a)
             else
                 eval_identity<T, Q>(acc, Yt, W, pb + warp * kRowsPerWarp, D, lane);
             T f[kRowsPerWarp];
-            eval_reduce<T, Q>(acc, D, a.func, scale, lane, f);
+            eval_reduce<T, Q, kRowsPerWarp, G>(acc, D, a.func, scale, lane, f);
             if (lane == 0)
 #pragma unroll
                 for (int rr = 0; rr < kRowsPerWarp; ++rr) sF[pb + warp * kRowsPerWarp + rr] = f[rr];
@@ -268,14 +269,20 @@ __global__ void __launch_bounds__(kThreadsS) k_de_step(StepArgs<T> a)
     }
 }
 
+template <typename T, int Q, bool G>
+int launch_step_v(const StepArgs<T> &a, int nsub, cudaStream_t st)
+{
+    const size_t smem = step_smem_bytes<T>(Q, a.S, a.D);
+    cudaError_t e = cudaFuncSetAttribute(k_de_step<T, Q, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_de_step)");
+    k_de_step<T, Q, G><<<nsub, kThreadsS, smem, st>>>(a);
+    return check_launch("k_de_step");
+}
+
 template <typename T, int Q>
 int launch_step(const StepArgs<T> &a, int nsub, cudaStream_t st)
 {
-    const size_t smem = step_smem_bytes<T>(Q, a.S, a.D);
-    cudaError_t e = cudaFuncSetAttribute(k_de_step<T, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_de_step)");
-    k_de_step<T, Q><<<nsub, kThreadsS, smem, st>>>(a);
-    return check_launch("k_de_step");
+    return func_sum_form(a.func) ? launch_step_v<T, Q, false>(a, nsub, st) : launch_step_v<T, Q, true>(a, nsub, st);
 }
 
 int q_of(int D) { return D <= 32 ? 1 : D <= 64 ? 2 : D <= 128 ? 4 : 8; }

@@ -95,10 +95,12 @@ __device__ __noinline__ T row_objective_warp(ZRow<T, Q> z, int D, int func_id, i
 // shift); result valid on every lane. Sums of per-coordinate terms (8, 9, 31) add each lane's
 // columns in order and then reduce across the warp; the other functions run the row accumulator
 // per lane, with the next coordinate fetched from the neighbouring lane.
-template <typename T, int Q, int RPW>
+// kGeneric = false compiles the per-coordinate-sum path alone (the caller guarantees such an id), so
+// the hot kernels carry none of the row accumulator's code.
+template <typename T, int Q, int RPW, bool kGeneric = true>
 __device__ __forceinline__ void eval_reduce(const T (&acc)[RPW][Q], int D, int func_id, T scale, int lane, T (&f)[RPW])
 {
-    if (func_id == SPEO_FUNC_ROTATED_RASTRIGIN || func_id == SPEO_FUNC_ROTATED_SPHERE || func_id == 8) {
+    if (!kGeneric || func_sum_form(func_id)) {
 #pragma unroll
         for (int rr = 0; rr < RPW; ++rr) {
             T s = T(0);
@@ -109,13 +111,15 @@ __device__ __forceinline__ void eval_reduce(const T (&acc)[RPW][Q], int D, int f
         }
         return;
     }
-    const T fs = func_fixed_shift<T>(func_id);
+    if constexpr (kGeneric) {
+        const T fs = func_fixed_shift<T>(func_id);
 #pragma unroll
-    for (int rr = 0; rr < RPW; ++rr) {
-        ZRow<T, Q> z;
+        for (int rr = 0; rr < RPW; ++rr) {
+            ZRow<T, Q> z;
 #pragma unroll
-        for (int q = 0; q < Q; ++q) z.v[q] = acc[rr][q] * scale + fs;
-        f[rr] = row_objective_warp<T, Q>(z, D, func_id, lane);
+            for (int q = 0; q < Q; ++q) z.v[q] = acc[rr][q] * scale + fs;
+            f[rr] = row_objective_warp<T, Q>(z, D, func_id, lane);
+        }
     }
 }
 

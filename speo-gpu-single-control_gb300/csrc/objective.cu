@@ -64,7 +64,8 @@ __device__ __forceinline__ bool seg_tile(int t, int sub, const speo_segment *seg
     return true;
 }
 
-template <typename T, int Q>
+// G: the generic variant (ids other than 8, 9, 31); G = false: per-coordinate sums only.
+template <typename T, int Q, bool G>
 __device__ void eval_one_tile(const TileDesc &d, T *Ys, T *Ms)
 {
     constexpr int W = 32 * Q;
@@ -96,7 +97,7 @@ __device__ void eval_one_tile(const TileDesc &d, T *Ys, T *Ms)
     }
     T f[kRowsPerWarp];
     const T scale = sizeof(T) == 4 ? (T)func_scale(d.func) : (T)func_scale_f64(d.func);
-    eval_reduce<T, Q>(acc, d.D, d.func, scale, lane, f);
+    eval_reduce<T, Q, kRowsPerWarp, G>(acc, d.D, d.func, scale, lane, f);
     if (lane == 0) {
         T *fit = static_cast<T *>(d.fit);
 #pragma unroll
@@ -107,7 +108,7 @@ __device__ void eval_one_tile(const TileDesc &d, T *Ys, T *Ms)
     }
 }
 
-template <typename T, int Q>
+template <typename T, int Q, bool G>
 __global__ void __launch_bounds__(256) k_eval_ref(const T *X, int ldx, int P, int D, int func, const T *shift,
                                                   const T *rot, T *fit)
 {
@@ -116,11 +117,12 @@ __global__ void __launch_bounds__(256) k_eval_ref(const T *X, int ldx, int P, in
     T *Ms = Ys + kEvalTile * 32 * Q;
     const int tiles = (P + kEvalTile - 1) / kEvalTile;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x)
-        eval_one_tile<T, Q>(ref_tile<T>(t, X, ldx, P, D, func, shift, rot, fit), Ys, Ms);
+        eval_one_tile<T, Q, G>(ref_tile<T>(t, X, ldx, P, D, func, shift, rot, fit), Ys, Ms);
 }
 
-template <int Q>
-__global__ void __launch_bounds__(256) k_eval_seg(const speo_segment *segs, const speo_work_item *items, int n_items,
+// Four blocks per SM where that fits 64 registers without spilling (per-coordinate sums, Q = 1, 4).
+template <int Q, bool G>
+__global__ void __launch_bounds__(256, (!G && (Q == 1 || Q == 4)) ? 4 : 1) k_eval_seg(const speo_segment *segs, const speo_work_item *items, int n_items,
                                                   const float *pop, float *fit)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -136,7 +138,8 @@ __global__ void __launch_bounds__(256) k_eval_seg(const speo_segment *segs, cons
             }
             if ((d.D + 31) / 32 > Q) break;  // handled by the launch for its own Q
             if (Q > 1 && (d.D + 31) / 32 <= Q / 2) break;
-            eval_one_tile<float, Q>(d, Ys, Ms);
+            if (func_sum_form(d.func) == G) break;  // handled by the other variant's launch
+            eval_one_tile<float, Q, G>(d, Ys, Ms);
         }
     }
 }
@@ -209,11 +212,16 @@ template <typename T, int Q>
 int launch_ref(const T *X, int ldx, int P, int D, int func, const T *shift, const T *rot, T *fit, cudaStream_t st)
 {
     const size_t smem = sizeof(T) * (size_t)(kEvalTile + kChunk) * 32 * Q;
-    cudaError_t e = cudaFuncSetAttribute(k_eval_ref<T, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const bool generic = !func_sum_form(func);
+    cudaError_t e = cudaFuncSetAttribute(generic ? k_eval_ref<T, Q, true> : k_eval_ref<T, Q, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_eval_ref)");
     const int tiles = (P + kEvalTile - 1) / kEvalTile;
     const int grid = tiles < 4 * sm_count() ? tiles : 4 * sm_count();
-    k_eval_ref<T, Q><<<grid, 256, smem, st>>>(X, ldx, P, D, func, shift, rot, fit);
+    if (generic)
+        k_eval_ref<T, Q, true><<<grid, 256, smem, st>>>(X, ldx, P, D, func, shift, rot, fit);
+    else
+        k_eval_ref<T, Q, false><<<grid, 256, smem, st>>>(X, ldx, P, D, func, shift, rot, fit);
     return check_launch("k_eval_ref");
 }
 
@@ -242,10 +250,15 @@ int launch_seg(const speo_segment *segs, const speo_work_item *items, int n_item
                cudaStream_t st)
 {
     const size_t smem = sizeof(float) * (size_t)(kEvalTile + kChunk) * 32 * Q;
-    cudaError_t e = cudaFuncSetAttribute(k_eval_seg<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // two variants: the per-coordinate sums (8, 9, 31) and the other ids; each skips the other's tiles
+    cudaError_t e = cudaFuncSetAttribute(k_eval_seg<Q, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_eval_seg<Q, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_eval_seg)");
     const int grid = n_items < 4 * sm_count() ? n_items : 4 * sm_count();
-    k_eval_seg<Q><<<grid, 256, smem, st>>>(segs, items, n_items, pop, fit);
+    k_eval_seg<Q, false><<<grid, 256, smem, st>>>(segs, items, n_items, pop, fit);
+    if (int r = check_launch("k_eval_seg")) return r;
+    k_eval_seg<Q, true><<<grid, 256, smem, st>>>(segs, items, n_items, pop, fit);
     return check_launch("k_eval_seg");
 }
 
