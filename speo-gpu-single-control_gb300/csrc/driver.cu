@@ -102,7 +102,7 @@ extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand
         if (hist) e = history_buffer((size_t)kStepGens * n, &d_hist);
         for (; !e && done < generations; done += kStepGens) {
             const int k = generations - done < kStepGens ? generations - done : kStepGens;
-            e = dropin_step_f32(pop, cand, d_best, ii, d_info, rng, pi, d_shift, d_rot, k, d_hist, d->s);
+            e = dropin_step_f32(pop, cand, d_best, ii, d_info, rng, pi, d_shift, d_rot, k, d_hist, 0, d->s);
             if (!e && hist)
                 e = check_cuda(cudaMemcpyAsync(h_fitness + (size_t)done * n, d_hist, sizeof(float) * (size_t)k * n,
                                                cudaMemcpyDeviceToHost, d->s),

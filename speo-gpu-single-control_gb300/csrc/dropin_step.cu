@@ -11,6 +11,7 @@
 // block writes what the three calls leave behind -- the last trials and their fitness (candidate
 // buffers), the selected rows and fitness, the best ids -- and the generation counter advances by
 // K, so the results are bit-identical to K rounds of the three calls.
+#include "cluster.cuh"
 #include "dropin.cuh"
 #include "eval_simt.cuh"
 
@@ -285,6 +286,264 @@ int launch_step(const StepArgs<T> &a, int nsub, cudaStream_t st)
     return func_sum_form(a.func) ? launch_step_v<T, Q, false>(a, nsub, st) : launch_step_v<T, Q, true>(a, nsub, st);
 }
 
+// ---- two-block clusters: one sub-island per cluster of 2 -----------------------------------------
+// Each block of the pair keeps a replica of the sub-island, double-buffered (generation g reads
+// buffer g % 2), and runs the draws, trials, evaluation and selection of half of the positions. Its
+// new rows (winner or parent) go to the next buffer of both replicas, the peer's through
+// distributed shared memory; one cluster barrier per generation makes both replicas whole. The
+// per-row arithmetic is k_de_step's, so the results are bit-identical. FP32.
+constexpr int kRowsPerWarp2 = 4;
+constexpr int kPassRows2 = kWarpsS * kRowsPerWarp2;  // 64 rows per evaluation pass
+
+__host__ __device__ inline int half_pos(int S) { return (S + 1) / 2; }
+
+//   Xp[2][S][W] fp[2][round_up(S,4)] | Xt[h][W] | Yt[hp][W] | Ms[D][W] | sF[hp] | o[W] | sR[GB][h][8]
+__host__ __device__ inline size_t step2_smem_bytes(int Q, int S, int D)
+{
+    const size_t W = 32 * (size_t)Q, h = half_pos(S), hp = round_up_i((int)h, kPassRows2);
+    return sizeof(float) * (2 * ((size_t)S * W + round_up_i(S, 4)) + h * W + hp * W + (size_t)D * W + hp + W) +
+           sizeof(int) * (size_t)step_draw_gens((int)h) * h * 8;
+}
+
+template <int Q, bool G>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_step2(StepArgs<float> a)
+{
+    using V = float4;
+    constexpr int VN = 4, W = 32 * Q;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int S = a.S, D = a.D, h = half_pos(S), hp = round_up_i(h, kPassRows2), Sf = round_up_i(S, 4);
+    float *const Xp0 = reinterpret_cast<float *>(smem_raw);  // buffer b at Xp0 + b * S * W
+    float *const fp0 = Xp0 + 2 * (size_t)S * W;              // buffer b at fp0 + b * Sf
+    float *Xt = fp0 + 2 * Sf;
+    float *Yt = Xt + (size_t)h * W;
+    float *Ms = Yt + (size_t)hp * W;
+    float *sF = Ms + (size_t)D * W;
+    float *so = sF + hp;
+    int *sR = reinterpret_cast<int *>(so + W);
+    __shared__ float s_bf[kWarpsS];
+    __shared__ int s_bp[kWarpsS];
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t me = cluster_rank(), peer = me ^ 1u;
+    const int isl = blockIdx.x >> 1;
+    const int base = isl * S;
+    const int pb0 = (int)me * h, np = (S - pb0 < h ? S - pb0 : h);  // this block's positions [pb0, pb0 + np)
+    const uint32_t gen0 = *(volatile uint32_t *)&a.rng->gen;
+    const uint2 key = make_uint2(a.rng->key0, a.rng->key1);
+    const int nch = (D + VN - 1) / VN;
+    const int GB = step_draw_gens(h);
+    const float F = a.info[isl].F;
+    const uint32_t thr = cr_threshold<float>(a.info[isl].CR);
+    const int st = a.info[isl].strategy_ID;
+    const int nd = ndonors(st);
+    const float scale = func_scale(a.func);
+
+    for (int i = tid; i < S * (W / VN); i += kThreadsS) {
+        const int p = i / (W / VN), c = i - p * (W / VN);
+        reinterpret_cast<V *>(Xp0 + (size_t)p * W)[c] =
+            reinterpret_cast<const V *>(a.pop + (size_t)a.perm[base + p] * W)[c];
+    }
+    for (int p = tid; p < S; p += kThreadsS) fp0[p] = a.pfit[a.perm[base + p]];
+    load_rot_rows<float, Q>(Ms, a.rot, D, D, 0, D);
+    for (int k = tid; k < W; k += kThreadsS) so[k] = k < D ? a.shift[k] : 0.f;
+    for (int i = tid; i < (hp - np) * W; i += kThreadsS) Yt[(size_t)np * W + i] = 0.f;
+    if (nch * VN < W) {
+        const int tail = W - nch * VN;
+        for (int i = tid; i < np * tail; i += kThreadsS) {
+            const int p = i / tail, k = nch * VN + (i - p * tail);
+            Xt[(size_t)p * W + k] = 0.f;
+            Yt[(size_t)p * W + k] = 0.f;
+        }
+        for (int i = tid; i < S * tail; i += kThreadsS) {  // and in the second population buffer
+            const int p = i / tail, k = nch * VN + (i - p * tail);
+            Xp0[(size_t)S * W + (size_t)p * W + k] = 0.f;
+        }
+    }
+    const uint32_t peer_xp = map_peer(Xp0, peer), peer_fp = map_peer(fp0, peer);
+    cluster_sync();
+
+    bool ok_draw = true, ok_bound = true;
+    for (int g = 0; g < a.gens; ++g) {
+        const uint32_t gen = gen0 + (uint32_t)g;
+        const bool last = g == a.gens - 1;
+        const int cur = g & 1, nxt = cur ^ 1;
+        const float *Xp = Xp0 + (size_t)cur * S * W;
+        const float *fp = fp0 + cur * Sf;
+        __syncthreads();
+        {
+            float bf = INFINITY;
+            int bp = 0x7fffffff;
+            for (int p = tid; p < S; p += kThreadsS) {
+                const float f = rank_t(fp[p]);
+                if (f < bf || (f == bf && p < bp)) { bf = f; bp = p; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const float of = __shfl_xor_sync(0xffffffffu, bf, o);
+                const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+                if (of < bf || (of == bf && op < bp)) { bf = of; bp = op; }
+            }
+            if (lane == 0) { s_bf[warp] = bf; s_bp[warp] = bp; }
+        }
+        if (g % GB == 0) {
+            const int nb = a.gens - g < GB ? a.gens - g : GB;
+            for (int t = tid; t < nb * np; t += kThreadsS) {
+                const int gi = t / np, lp = t - gi * np;
+                IdxStream s(key, (uint32_t)(base + pb0 + lp), gen + (uint32_t)gi, kTagIdx);
+                int r[5];
+                ok_draw &= draw_donors(s, S, r);
+                int *o = sR + (gi * h + lp) * 8;
+#pragma unroll
+                for (int k = 0; k < 5; ++k) o[k] = r[k];
+                o[5] = s.index(D);
+            }
+        }
+        __syncthreads();
+        int bp = s_bp[0];
+        {
+            float bf = s_bf[0];
+            for (int w = 1; w < kWarpsS; ++w)
+                if (s_bf[w] < bf || (s_bf[w] == bf && s_bp[w] < bp)) { bf = s_bf[w]; bp = s_bp[w]; }
+        }
+        if (last && me == 0 && tid == 0) a.best_id[isl] = a.perm[base + bp];
+        const int *sRg = sR + (g % GB) * h * 8;
+
+        for (int t = tid; t < np * nch; t += kThreadsS) {
+            const int lp = t / nch, c = t - lp * nch;
+            const int p = pb0 + lp, pos = base + p;
+            const int e0 = VN * c;
+            const float *xi = Xp + (size_t)p * W;
+            const float *xb = Xp + (size_t)(strategy_uses_best(st) ? bp : p) * W;
+            const V ti = *reinterpret_cast<const V *>(xi + e0);
+            const V tb = strategy_uses_best(st) ? *reinterpret_cast<const V *>(xb + e0) : ti;
+            V tr[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k)
+                tr[k] = k < nd ? *reinterpret_cast<const V *>(Xp + (size_t)sRg[lp * 8 + k] * W + e0) : ti;
+            const int jr = sRg[lp * 8 + 5];
+            const uint4 w = philox(make_uint4((uint32_t)(e0 >> 2), (uint32_t)pos, gen, kTagCr), key);
+            V x = ti;
+#pragma unroll
+            for (int q = 0; q < VN; ++q) {
+                const int e = e0 + q;
+                float v;
+                if (e == jr || cr_take(pick(w, (uint32_t)(e & 3)), thr)) {
+                    float xr[5];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) xr[k] = vget<float>(tr[k], q);
+                    v = mutant<float>(st, F, vget<float>(ti, q), vget<float>(tb, q), xr);
+                } else {
+                    v = vget<float>(ti, q);
+                }
+                vset<float>(x, q, check_bound<float>(v, a.lb, a.ub, ok_bound));
+            }
+            *reinterpret_cast<V *>(Xt + (size_t)lp * W + e0) = x;
+            V y;
+#pragma unroll
+            for (int q = 0; q < VN; ++q) {
+                const int e = e0 + q;
+                vset<float>(y, q, e < D ? sub_rn(vget<float>(x, q), so[e]) : 0.f);
+            }
+            *reinterpret_cast<V *>(Yt + (size_t)lp * W + e0) = y;
+            if (last) {
+                float *out = a.cand + (size_t)a.perm[pos] * W;
+                if (e0 + VN <= D) {
+                    *reinterpret_cast<V *>(out + e0) = x;
+                } else {
+#pragma unroll
+                    for (int q = 0; q < VN; ++q)
+                        if (e0 + q < D) out[e0 + q] = vget<float>(x, q);
+                }
+            }
+        }
+        __syncthreads();
+
+        for (int pb = 0; pb < np; pb += kPassRows2) {
+            float acc[kRowsPerWarp2][Q];
+#pragma unroll
+            for (int rr = 0; rr < kRowsPerWarp2; ++rr)
+#pragma unroll
+                for (int q = 0; q < Q; ++q) acc[rr][q] = 0.f;
+            if (func_rotated(a.func))
+                eval_accumulate<float, Q>(acc, Yt, W, pb + warp * kRowsPerWarp2, Ms, W, 0, D, lane);
+            else
+                eval_identity<float, Q>(acc, Yt, W, pb + warp * kRowsPerWarp2, D, lane);
+            float f[kRowsPerWarp2];
+            eval_reduce<float, Q, kRowsPerWarp2, G>(acc, D, a.func, scale, lane, f);
+            if (lane == 0)
+#pragma unroll
+                for (int rr = 0; rr < kRowsPerWarp2; ++rr) sF[pb + warp * kRowsPerWarp2 + rr] = f[rr];
+        }
+        __syncthreads();
+
+        // selection into the next buffer of both replicas
+        float *nXp = Xp0 + (size_t)nxt * S * W;
+        float *nfp = fp0 + nxt * Sf;
+        const uint32_t pxp = peer_xp + (uint32_t)((size_t)nxt * S * W * sizeof(float));
+        const uint32_t pfp = peer_fp + (uint32_t)(nxt * Sf * sizeof(float));
+        for (int t = tid; t < np * nch; t += kThreadsS) {
+            const int lp = t / nch, c = t - lp * nch, p = pb0 + lp;
+            const bool win = sF[lp] < fp[p];
+            const V v = *reinterpret_cast<const V *>((win ? Xt + (size_t)lp * W : Xp + (size_t)p * W) + VN * c);
+            *reinterpret_cast<V *>(nXp + (size_t)p * W + VN * c) = v;
+            st_peer4(pxp + (uint32_t)(((size_t)p * W + VN * c) * sizeof(float)), v);
+        }
+        for (int lp = tid; lp < np; lp += kThreadsS) {
+            const int p = pb0 + lp, row = a.perm[base + p];
+            const float tf = sF[lp];
+            const float nf = tf < fp[p] ? tf : fp[p];
+            nfp[p] = nf;
+            st_peer1(pfp + (uint32_t)(p * sizeof(float)), nf);
+            if (last) a.cfit[row] = tf;
+            if (a.hist) a.hist[(size_t)g * a.P + row] = nf;
+        }
+        cluster_sync();
+    }
+    // this block's rows and fitness back (elements past D are never written)
+    const float *Xp = Xp0 + (size_t)(a.gens & 1) * S * W;
+    const float *fp = fp0 + (a.gens & 1) * Sf;
+    for (int t = tid; t < np * nch; t += kThreadsS) {
+        const int lp = t / nch, c = t - lp * nch, e0 = VN * c, p = pb0 + lp;
+        float *dst = a.pop + (size_t)a.perm[base + p] * W;
+        const V v = *reinterpret_cast<const V *>(Xp + (size_t)p * W + e0);
+        if (e0 + VN <= D) {
+            *reinterpret_cast<V *>(dst + e0) = v;
+        } else {
+#pragma unroll
+            for (int q = 0; q < VN; ++q)
+                if (e0 + q < D) dst[e0 + q] = vget<float>(v, q);
+        }
+    }
+    for (int lp = tid; lp < np; lp += kThreadsS) a.pfit[a.perm[base + pb0 + lp]] = fp[pb0 + lp];
+    if (!ok_draw) atomicOr(&s_deverr, SPEO_DEVERR_REDRAW_LIMIT);
+    if (!ok_bound) atomicOr(&s_deverr, SPEO_DEVERR_BOUND_LIMIT);
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        const unsigned done = atomicAdd(&a.rng->done, 1u);
+        if (done == gridDim.x - 1) {
+            a.rng->done = 0;
+            a.rng->gen = gen0 + (uint32_t)a.gens;
+            __threadfence();
+        }
+    }
+}
+
+template <int Q, bool G>
+int launch_step2_v(const StepArgs<float> &a, int nsub, cudaStream_t st)
+{
+    const size_t smem = step2_smem_bytes(Q, a.S, a.D);
+    cudaError_t e = cudaFuncSetAttribute(k_de_step2<Q, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_de_step2)");
+    k_de_step2<Q, G><<<2 * nsub, kThreadsS, smem, st>>>(a);
+    return check_launch("k_de_step2");
+}
+
+template <int Q>
+int launch_step2(const StepArgs<float> &a, int nsub, cudaStream_t st)
+{
+    return func_sum_form(a.func) ? launch_step2_v<Q, false>(a, nsub, st) : launch_step2_v<Q, true>(a, nsub, st);
+}
+
 int q_of(int D) { return D <= 32 ? 1 : D <= 64 ? 2 : D <= 128 ? 4 : 8; }
 
 }  // namespace
@@ -303,14 +562,29 @@ bool dropin_step_fits_f32(int island_size, int subisland_num, int dim, int func)
 
 int dropin_step_f32(speo_population_f32 pop, speo_population_f32 cand, int *d_best, speo_island_info ii,
                     speo_de_info_f32 *d_info, speo_rng_state *rng, speo_problem_info_f32 pi, const float *shift,
-                    const float *rot, int generations, float *d_hist, cudaStream_t st)
+                    const float *rot, int generations, float *d_hist, int pair_mode, cudaStream_t st)
 {
     if (generations < 1) return SPEO_OK;
     StepArgs<float> a{pop.elements, pop.fitness_value, cand.elements, cand.fitness_value, pi.dim,
                       ii.island_size / ii.subisland_num, ii.permutated_index, d_info, d_best,
                       (float)pi.min_bound, (float)pi.max_bound, reinterpret_cast<RngState *>(rng), shift, rot,
                       pi.function_ID, generations, ii.island_size, d_hist};
-    switch (q_of(pi.dim)) {
+    // two-block clusters when there are SMs for two blocks per sub-island and the replicas fit
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const int S = ii.island_size / ii.subisland_num, Q = q_of(pi.dim);
+    const bool pair = pair_mode != 1 && S >= 4 && (pair_mode == 2 || 2LL * ii.subisland_num <= sm_count()) &&
+                      step2_smem_bytes(Q, S, pi.dim) <= (size_t)optin;
+    if (pair) {
+        switch (Q) {
+        case 1: return launch_step2<1>(a, ii.subisland_num, st);
+        case 2: return launch_step2<2>(a, ii.subisland_num, st);
+        case 4: return launch_step2<4>(a, ii.subisland_num, st);
+        default: return launch_step2<8>(a, ii.subisland_num, st);
+        }
+    }
+    switch (Q) {
     case 1: return launch_step<float, 1>(a, ii.subisland_num, st);
     case 2: return launch_step<float, 2>(a, ii.subisland_num, st);
     case 4: return launch_step<float, 4>(a, ii.subisland_num, st);

@@ -71,11 +71,13 @@ int mlp_grad_bf16(const float *theta, int din, int h, const float *mu, const flo
 // search, generate, evaluate and select, bit-identical to as many rounds of
 // API_DE_GenerateNewPopulation_f32 + API_evaluateFitness_f32 + API_DE_SelectSurvival_f32.
 // d_hist (generations x island_size, may be null) receives the fitness after each generation.
-// Fits when a sub-island's rows, trials and M^T fit one block's shared memory.
+// pair_mode: 0 = two-block clusters per sub-island when 2 x sub-islands <= SMs, 1 = one block,
+// 2 = two-block clusters (bit-identical to one block). Fits when a sub-island's rows, trials and
+// M^T fit one block's shared memory.
 bool dropin_step_fits_f32(int island_size, int subisland_num, int dim, int func);
 int dropin_step_f32(speo_population_f32 pop, speo_population_f32 cand, int *d_best, speo_island_info ii,
                     speo_de_info_f32 *d_info, speo_rng_state *rng, speo_problem_info_f32 pi, const float *shift,
-                    const float *rot, int generations, float *d_hist, cudaStream_t st);
+                    const float *rot, int generations, float *d_hist, int pair_mode, cudaStream_t st);
 
 // Byte offsets of the BF16 weight images inside `img`: W1 (h x 64), W2 (h x h), W2^T (h x h).
 size_t mlp_img_w2_offset(int h);

@@ -8,6 +8,7 @@
 // from HBM once, evolved in shared memory, and written back once. Each generation is the same
 // computation as speo_generation (same Philox counters, same FMA order in the mutant and in the
 // rotation), so the result is bit-identical to `generations` launches of it.
+#include "cluster.cuh"
 #include "eval_simt.cuh"
 #include "host.h"
 
@@ -250,36 +251,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 // peer's through distributed shared memory. One cluster barrier per generation then makes both
 // replicas whole. Donor reads are local; the per-row arithmetic is the single-block kernel's, so
 // the result is bit-identical.
-__device__ __forceinline__ uint32_t cluster_rank()
-{
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-__device__ __forceinline__ uint32_t map_peer(const void *p, uint32_t peer)
-{
-    uint32_t out;
-    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
-                 : "=r"(out)
-                 : "r"((uint32_t)__cvta_generic_to_shared(p)), "r"(peer));
-    return out;
-}
-__device__ __forceinline__ void st_peer4(uint32_t addr, float4 v)
-{
-    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(v.x), "f"(v.y), "f"(v.z),
-                 "f"(v.w)
-                 : "memory");
-}
-__device__ __forceinline__ void st_peer1(uint32_t addr, float v)
-{
-    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
-}
-// All threads of both blocks: writes before it (local and remote) are visible after it.
-__device__ __forceinline__ void cluster_sync()
-{
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
 constexpr int kRowsPerWarp2 = 4;
 constexpr int kEvalRows2 = kWarpsR * kRowsPerWarp2;  // 64 rows per evaluation pass
 

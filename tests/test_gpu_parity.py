@@ -120,6 +120,7 @@ def test_dropin_generate_matches_oracle(lib, oracle, cuda, f64, P, D, nsub):
 
 @pytest.mark.parametrize("gens,pinned,history,P,D,nsub,fid,strats", [
     (60, True, True, 200, 30, 2, 9, (4, 6)),         # config-1 sub-islands, several fused launches
+    (30, True, True, 4000, 30, 80, 9, (4, 6)),       # 80 sub-islands of 50: one block each (2 x 80 > SMs)
     (7, False, False, 200, 30, 2, 9, (4, 6)),        # pageable buffer, last generation only
     (21, True, True, 111, 50, 3, 4, (2, 4, 7)),      # odd sub-islands of 37, best-row strategies, Rosenbrock
     (6, True, True, 256, 100, 4, 31, (5, 3, 8, 0)),  # D = 100
@@ -129,7 +130,8 @@ def test_dropin_generate_matches_oracle(lib, oracle, cuda, f64, P, D, nsub):
 ])
 def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned, history, P, D, nsub, fid, strats):
     """speo_de_run_f32 (the reference's DE_CUDA::Run loop, natively: sub-islands resident in shared
-    memory for blocks of generations, or the three calls replayed as a CUDA graph) gives the same
+    memory for blocks of generations, on two-block clusters when the GPU has SMs for two blocks per
+    sub-island, or the three calls replayed as a CUDA graph) gives the same
     populations, candidates, best ids, generation counter and per-generation fitness as the drop-in
     calls issued one by one."""
     import torch
