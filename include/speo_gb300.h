@@ -179,6 +179,18 @@ SPEO_API int speo_de_run_f32(speo_population_f32 d_population, speo_population_f
                              int *d_best_individual_ID, speo_problem_info_f32 problem_info, const float *d_shift,
                              const float *d_rotated, int generations, float *h_fitness, int history, void *stream);
 
+/* Per-sub-island DE parameters, as DE_CUDA::ConfigureEA (CUDA_EA_library/DE_CUDA.cc:89-118)
+ * fills them before copying them to the device: `dynamic` = 0 ("constant") gives every
+ * sub-island (CR, F, strategy); `dynamic` = 1 gives each sub-island CR in {0.1, 0.9} and strategy
+ * in {4, 6}, chosen independently with probability 1/2 each, and F. pop_size = island_size /
+ * subisland_num. The reference draws the choices from its host RNG (random.cc); here sub-island i
+ * takes word 0 (CR) and word 1 (strategy) of Philox-4x32-10({i, 0, 0, 6}, seed), low bit. Host
+ * arrays of subisland_num entries; nothing on the device. */
+SPEO_API int speo_configure_de_f32(speo_de_info_f32 *h_info, int subisland_num, int island_size, float F, float CR,
+                                   int strategy, int dynamic, uint64_t seed);
+SPEO_API int speo_configure_de_f64(speo_de_info_f64 *h_info, int subisland_num, int island_size, double F, double CR,
+                                   int strategy, int dynamic, uint64_t seed);
+
 /* ------------------------------------------------------------------------------------ */
 /* Library control                                                                       */
 /* ------------------------------------------------------------------------------------ */

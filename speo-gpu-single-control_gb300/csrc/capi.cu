@@ -119,3 +119,57 @@ extern "C" int speo_plan_work(const speo_segment *segs, int n_segs, int tile_row
     if (items && n > cap) return fail(SPEO_ERR_INVALID_ARG, "speo_plan_work: %d items exceed capacity %d", n, cap);
     return SPEO_OK;
 }
+
+// ---- DE_CUDA::ConfigureEA (CUDA_EA_library/DE_CUDA.cc:89-118) ------------------------------------
+namespace {
+
+// Philox-4x32-10 on the host (Salmon et al., SC'11; the same rounds as the device copy).
+void philox_host(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0; c1 = (uint32_t)p1; c2 = n2; c3 = (uint32_t)p0;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+template <typename T, typename Info>
+int configure_de(Info *h, int nsub, int island_size, T F, T CR, int strategy, int dynamic, uint64_t seed,
+                 const char *who)
+{
+    if (!h || nsub < 1 || island_size < 1 || island_size % nsub || (dynamic != 0 && dynamic != 1) ||
+        (!dynamic && (strategy < 0 || strategy > 8)))
+        return speo::fail(SPEO_ERR_INVALID_ARG, "%s: bad arguments", who);
+    for (int i = 0; i < nsub; ++i) {
+        h[i].F = F;
+        h[i].pop_size = island_size / nsub;
+        if (dynamic) {
+            const uint32_t ctr[4] = {(uint32_t)i, 0u, 0u, 6u};
+            uint32_t w[4];
+            philox_host(ctr, (uint32_t)seed, (uint32_t)(seed >> 32), w);
+            h[i].CR = (w[0] & 1u) ? (T)0.9 : (T)0.1;
+            h[i].strategy_ID = (w[1] & 1u) ? 6 : 4;
+        } else {
+            h[i].CR = CR;
+            h[i].strategy_ID = strategy;
+        }
+    }
+    return SPEO_OK;
+}
+
+}  // namespace
+
+extern "C" int speo_configure_de_f32(speo_de_info_f32 *h, int nsub, int island_size, float F, float CR, int strategy,
+                                     int dynamic, uint64_t seed)
+{
+    return configure_de<float>(h, nsub, island_size, F, CR, strategy, dynamic, seed, "speo_configure_de_f32");
+}
+
+extern "C" int speo_configure_de_f64(speo_de_info_f64 *h, int nsub, int island_size, double F, double CR,
+                                     int strategy, int dynamic, uint64_t seed)
+{
+    return configure_de<double>(h, nsub, island_size, F, CR, strategy, dynamic, seed, "speo_configure_de_f64");
+}

@@ -148,3 +148,29 @@ int main() { return 0; }
     (build / "abi_ref.cc").write_text(src)
     subprocess.run(["g++", "-fsyntax-only", "-I", str(REF_LIB_DIR), "-I", str(REPO / "include"),
                     str(build / "abi_ref.cc")], check=True)
+
+
+@pytest.mark.parametrize("f64", [False, True])
+def test_configure_de_constant_and_dynamic(lib, oracle, f64):
+    """DE_CUDA::ConfigureEA (DE_CUDA.cc:89-118): "constant" repeats one setting; "dynamic" picks CR
+    in {0.1, 0.9} and strategy in {4, 6} per sub-island, here from Philox({i, 0, 0, 6}, seed)."""
+    from speo_gb300 import _lib
+
+    DI = _lib.DEInfoF64 if f64 else _lib.DEInfoF32
+    fn = lib.speo_configure_de_f64 if f64 else lib.speo_configure_de_f32
+    n = 256
+    info = (DI * n)()
+    assert fn(ctypes.addressof(info), n, n * 100, 0.5, 0.8, 5, 0, 1) == 0
+    assert all((x.CR, x.strategy_ID, x.pop_size) == (pytest.approx(0.8), 5, 100) for x in info)
+    assert fn(ctypes.addressof(info), n, n * 100, 0.5, 0.8, 5, 1, 1234) == 0
+    crs = np.array([x.CR for x in info])
+    sts = np.array([x.strategy_ID for x in info])
+    assert set(np.round(crs, 6)) == {0.1, 0.9} and set(sts) == {4, 6}
+    assert all(x.F == pytest.approx(0.5) and x.pop_size == 100 for x in info)
+    key = oracle.key_of(1234)
+    for i in range(n):
+        w = oracle.philox([i, 0, 0, 6], key)
+        assert (crs[i] > 0.5) == bool(w[0] & 1) and (sts[i] == 6) == bool(w[1] & 1)
+    assert 60 < (crs > 0.5).sum() < 196 and 60 < (sts == 6).sum() < 196
+    assert fn(ctypes.addressof(info), n, n * 100 + 1, 0.5, 0.8, 5, 0, 1) == _lib.SPEO_ERR_INVALID_ARG
+
