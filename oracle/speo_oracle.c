@@ -343,6 +343,153 @@ void speo_oracle_evaluate_rows(int func_id, const float *x, int n, int ld, int d
     free(Md);
 }
 
+/* ---- CEC2014 hybrid (17-22) and composition (23-30) functions ---------------------------
+ * Hybrid functions hf01..hf06 (CEC2014.cc:954-1206): z = M (x - o) (rate 1), y_i = z[S_i - 1]
+ * (S 1-based), y cut into groups of ceil(gp_g * D) coordinates (the last takes the rest); group g
+ * is body fid_g on y_g * rate(fid_g) + its fixed shift, with the group's own length; f = sum of
+ * the groups in order.
+ * Composition functions cf01..cf08 (CEC2014.cc:1209-1369): component c evaluates its body on
+ * rate * M_c (x - o_c) (or without M_c) and is rescaled as num * f / den; cf07 / cf08 take the
+ * hybrids hf01-03 / hf04-06 on (o_c, M_c, S_c). cf_cal (:1481-1520) adds bias_c = 100 c, weights
+ * w_c = (1 / S_c)^0.5 exp(-S_c / (2 D delta_c^2)), S_c = sum (x - o_c)^2 (1e99 at S_c = 0; all 1
+ * when every weight is 0) and returns sum w_c / w_sum * fit_c. Bodies are chosen by the ids 1-16
+ * whose code they share (schwefel = 10, rastrigin = 8), with those ids' rates and fixed shifts. */
+typedef struct { int n; double gp[5]; int fid[5]; } oracle_hybrid;
+static const oracle_hybrid k_hybrid[6] = {
+    {3, {0.3, 0.3, 0.4}, {10, 8, 1}},                        /* hf01 :954-991  */
+    {3, {0.3, 0.3, 0.4}, {2, 14, 8}},                        /* hf02 :993-1032 */
+    {4, {0.2, 0.2, 0.3, 0.3}, {7, 6, 4, 16}},                /* hf03 :1034-1075 */
+    {4, {0.2, 0.2, 0.3, 0.3}, {14, 3, 15, 8}},               /* hf04 :1077-1117 */
+    {5, {0.1, 0.2, 0.2, 0.2, 0.3}, {16, 14, 4, 10, 1}},      /* hf05 :1119-1162 */
+    {5, {0.1, 0.2, 0.2, 0.2, 0.2}, {12, 13, 15, 10, 5}},     /* hf06 :1164-1207 */
+};
+typedef struct { int fid, rotated; double num, den; } oracle_piece; /* den 0: no rescale */
+typedef struct { int n, hybrid0; double delta[5]; oracle_piece c[5]; } oracle_comp;
+static const oracle_comp k_comp[8] = {
+    {5, -1, {10, 20, 30, 40, 50},                           /* cf01 :1209-1233 */
+     {{4, 1, 10000, 1e+4}, {1, 1, 10000, 1e+10}, {2, 1, 10000, 1e+30}, {3, 1, 10000, 1e+10}, {1, 0, 10000, 1e+10}}},
+    {3, -1, {20, 20, 20}, {{10, 0, 0, 0}, {8, 1, 0, 0}, {14, 1, 0, 0}}},                    /* cf02 :1235-1249 */
+    {3, -1, {10, 30, 50}, {{10, 1, 1000, 4e+3}, {8, 1, 1000, 1e+3}, {1, 1, 1000, 1e+10}}}, /* cf03 :1251-1267 */
+    {5, -1, {10, 10, 10, 10, 10},                           /* cf04 :1269-1291 */
+     {{10, 1, 1000, 4e+3}, {13, 1, 1000, 1e+3}, {1, 1, 1000, 1e+10}, {6, 1, 1000, 400}, {7, 1, 1000, 100}}},
+    {5, -1, {10, 10, 10, 20, 20},                           /* cf05 :1293-1315 */
+     {{14, 1, 10000, 1000}, {8, 1, 10000, 1e+3}, {10, 1, 10000, 4e+3}, {6, 1, 10000, 400}, {1, 1, 10000, 1e+10}}},
+    {5, -1, {10, 20, 30, 40, 50},                           /* cf06 :1317-1339 */
+     {{15, 1, 10000, 4e+3}, {13, 1, 10000, 1e+3}, {10, 1, 10000, 4e+3}, {16, 1, 10000, 2e+7}, {1, 1, 10000, 1e+10}}},
+    {3, 0, {10, 30, 50}, {{0}}},                            /* cf07 :1341-1354: hf01, hf02, hf03 */
+    {3, 3, {10, 30, 50}, {{0}}},                            /* cf08 :1356-1369: hf04, hf05, hf06 */
+};
+
+int speo_oracle_cec_components(int fid)
+{
+    return (fid >= 23 && fid <= 30) ? k_comp[fid - 23].n : 1;
+}
+
+int speo_oracle_hybrid_groups(int fid, int nx, int *G, int *G_nx)
+{
+    if (fid < 17 || fid > 22) return 0;
+    const oracle_hybrid *h = &k_hybrid[fid - 17];
+    int tmp = 0;
+    for (int i = 0; i < h->n - 1; i++) {
+        G_nx[i] = (int)ceil(h->gp[i] * nx);
+        tmp += G_nx[i];
+    }
+    G_nx[h->n - 1] = nx - tmp;
+    G[0] = 0;
+    for (int i = 1; i < h->n; i++) G[i] = G[i - 1] + G_nx[i - 1];
+    return h->n;
+}
+
+static double hybrid_f64(int hi, const double *x, const double *o, const double *M, const int *S, int nx)
+{
+    double ze[SPEO_ORACLE_MAX_DIM], ye[SPEO_ORACLE_MAX_DIM], zg[SPEO_ORACLE_MAX_DIM];
+    int G[5], G_nx[5];
+    const oracle_hybrid *h = &k_hybrid[hi];
+    speo_oracle_hybrid_groups(17 + hi, nx, G, G_nx);
+    for (int i = 0; i < nx; ++i) ye[i] = (x[i] - o[i]) * 1.0;
+    for (int i = 0; i < nx; ++i) {
+        double zi = 0;
+        for (int j = 0; j < nx; ++j) zi = zi + ye[j] * M[i * nx + j];
+        ze[i] = zi;
+    }
+    for (int i = 0; i < nx; ++i) ye[i] = ze[S[i] - 1];
+    double f = 0.0;
+    for (int g = 0; g < h->n; ++g) {
+        const int fid = h->fid[g];
+        const double rate = speo_oracle_func_rate(fid), fs = fixed_shift(fid);
+        for (int i = 0; i < G_nx[g]; ++i) zg[i] = ye[G[g] + i] * rate + fs;
+        f += speo_oracle_cec_from_z(fid, zg, G_nx[g]);
+    }
+    return f;
+}
+
+static double piece_f64(const oracle_piece *pc, const double *x, const double *o, const double *M, int nx)
+{
+    double ye[SPEO_ORACLE_MAX_DIM], z[SPEO_ORACLE_MAX_DIM];
+    const double rate = speo_oracle_func_rate(pc->fid), fs = fixed_shift(pc->fid);
+    for (int i = 0; i < nx; ++i) ye[i] = (x[i] - o[i]) * rate;
+    for (int i = 0; i < nx; ++i) {
+        double zi = ye[i];
+        if (pc->rotated) {
+            zi = 0;
+            for (int j = 0; j < nx; ++j) zi = zi + ye[j] * M[i * nx + j];
+        }
+        z[i] = zi + fs;
+    }
+    double f = speo_oracle_cec_from_z(pc->fid, z, nx);
+    if (pc->den != 0) f = pc->num * f / pc->den;
+    return f;
+}
+
+double speo_oracle_objective_multi_f64(int fid, const double *x, const double *o, const double *M, const int *S,
+                                       int nx)
+{
+    if (fid >= 17 && fid <= 22) return hybrid_f64(fid - 17, x, o, M, S, nx);
+    if (fid < 23 || fid > 30) return speo_oracle_objective_f64(fid, x, o, M, nx);
+    const oracle_comp *cp = &k_comp[fid - 23];
+    double fit[5], w[5], w_max = 0, w_sum = 0;
+    for (int c = 0; c < cp->n; ++c) {
+        const double *oc = o + (size_t)c * nx, *Mc = M + (size_t)c * nx * nx;
+        fit[c] = cp->hybrid0 >= 0 ? hybrid_f64(cp->hybrid0 + c, x, oc, Mc, S + (size_t)c * nx, nx)
+                                  : piece_f64(&cp->c[c], x, oc, Mc, nx);
+    }
+    for (int c = 0; c < cp->n; ++c) {   /* cf_cal :1481-1520 */
+        fit[c] += 100.0 * c;
+        w[c] = 0;
+        for (int j = 0; j < nx; ++j) w[c] += pow(x[j] - o[(size_t)c * nx + j], 2.0);
+        if (w[c] != 0)
+            w[c] = pow(1.0 / w[c], 0.5) * exp(-w[c] / 2.0 / nx / pow(cp->delta[c], 2.0));
+        else
+            w[c] = 1.0e99;
+        if (w[c] > w_max) w_max = w[c];
+    }
+    for (int c = 0; c < cp->n; ++c) w_sum = w_sum + w[c];
+    if (w_max == 0) {
+        for (int c = 0; c < cp->n; ++c) w[c] = 1;
+        w_sum = cp->n;
+    }
+    double f = 0.0;
+    for (int c = 0; c < cp->n; ++c) f = f + w[c] / w_sum * fit[c];
+    return f;
+}
+
+void speo_oracle_evaluate_rows_multi(int fid, const float *x, int n, int ld, int dim, const float *o,
+                                     const float *M, const int *S, double *f_out)
+{
+    const int nc = speo_oracle_cec_components(fid);
+    double xd[SPEO_ORACLE_MAX_DIM];
+    double *od = (double *)malloc(sizeof(double) * (size_t)nc * dim);
+    double *Md = (double *)malloc(sizeof(double) * (size_t)nc * dim * dim);
+    for (int i = 0; i < nc * dim; ++i) od[i] = o[i];
+    for (int i = 0; i < nc * dim * dim; ++i) Md[i] = M[i];
+    for (int r = 0; r < n; ++r) {
+        for (int i = 0; i < dim; ++i) xd[i] = x[(size_t)r * ld + i];
+        f_out[r] = speo_oracle_objective_multi_f64(fid, xd, od, Md, S, dim);
+    }
+    free(od);
+    free(Md);
+}
+
 /* ---- fused generation (this library's extended semantics) ------------------------------ */
 static int seg_best_row(const float *fit, int64_t row0, int P)
 {

@@ -99,6 +99,18 @@ double speo_oracle_objective_f64(int func_id, const double *x, const double *o, 
 void speo_oracle_evaluate_rows(int func_id, const float *x, int n, int ld, int dim,
                                const float *o, const float *M, double *f_out);
 
+/* Hybrid (17-22) and composition (23-30) functions (CEC2014.cc:954-1369, cf_cal :1481-1520).
+ * o: nc x D (component-major), M: nc row-major D x D blocks, S: nc x D 1-based shuffles (used by
+ * 17-22, 29, 30; may be NULL otherwise); nc = speo_oracle_cec_components(fid). Other ids forward to
+ * speo_oracle_objective_f64. */
+int speo_oracle_cec_components(int fid);
+/* Group starts / lengths of hybrid fid (17-22) at dimension nx; returns the group count. */
+int speo_oracle_hybrid_groups(int fid, int nx, int *G, int *G_nx);
+double speo_oracle_objective_multi_f64(int fid, const double *x, const double *o, const double *M, const int *S,
+                                       int nx);
+void speo_oracle_evaluate_rows_multi(int fid, const float *x, int n, int ld, int dim, const float *o,
+                                     const float *M, const int *S, double *f_out);
+
 /* ---- Extended (this library's) semantics ------------------------------------------- */
 /* Fused generation over segments of identity-permuted rows: what speo_generation computes.
  * Segment arrays are parallel host arrays. pop_in/fit_in -> pop_out/fit_out. fit values of

@@ -46,6 +46,12 @@ def lib() -> ctypes.CDLL:
         L.speo_oracle_objective_f64.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_int]
         L.speo_oracle_objective_f64.restype = c_double
         L.speo_oracle_evaluate_rows.argtypes = [c_int, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p]
+        L.speo_oracle_cec_components.argtypes = [c_int]
+        L.speo_oracle_hybrid_groups.argtypes = [c_int, c_int, c_void_p, c_void_p]
+        L.speo_oracle_objective_multi_f64.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_int]
+        L.speo_oracle_objective_multi_f64.restype = c_double
+        L.speo_oracle_evaluate_rows_multi.argtypes = [c_int, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p,
+                                                      c_void_p, c_void_p]
         L.speo_oracle_generation_f32.argtypes = [c_int] + [c_void_p] * 13 + [c_uint32] + [c_void_p] * 7
         L.speo_oracle_ring_migrate.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
                                                c_void_p, c_void_p]
@@ -147,6 +153,37 @@ def evaluate_rows(func_id, X, dim, o, M) -> np.ndarray:
     lib().speo_oracle_evaluate_rows(func_id, _p(X), X.shape[0], X.shape[1], dim,
                                     _p(np.ascontiguousarray(o, dtype=np.float32)),
                                     _p(np.ascontiguousarray(M, dtype=np.float32)), _p(out))
+    return out
+
+
+def cec_components(func_id) -> int:
+    return lib().speo_oracle_cec_components(func_id)
+
+
+def hybrid_groups(func_id, dim) -> list[tuple[int, int]]:
+    """[(start, length)] of the groups of hybrid func_id (17-22) at dimension dim."""
+    G = (ctypes.c_int * 5)()
+    n = (ctypes.c_int * 5)()
+    k = lib().speo_oracle_hybrid_groups(func_id, dim, G, n)
+    return [(G[i], n[i]) for i in range(k)]
+
+
+def objective_multi(func_id, x, o, M, S=None) -> float:
+    """Any id 1-31; o (nc, D), M (nc, D, D), S (nc, D) 1-based (hybrids and 29/30)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    o = np.ascontiguousarray(o, dtype=np.float64)
+    M = np.ascontiguousarray(M, dtype=np.float64)
+    S = None if S is None else np.ascontiguousarray(S, dtype=np.int32)
+    return lib().speo_oracle_objective_multi_f64(func_id, _p(x), _p(o), _p(M), _p(S), x.shape[-1])
+
+
+def evaluate_rows_multi(func_id, X, dim, o, M, S=None) -> np.ndarray:
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    S = None if S is None else np.ascontiguousarray(S, dtype=np.int32)
+    out = np.zeros(X.shape[0], dtype=np.float64)
+    lib().speo_oracle_evaluate_rows_multi(func_id, _p(X), X.shape[0], X.shape[1], dim,
+                                          _p(np.ascontiguousarray(o, dtype=np.float32)),
+                                          _p(np.ascontiguousarray(M, dtype=np.float32)), _p(S), _p(out))
     return out
 
 

@@ -60,3 +60,57 @@ def write_reference_data(directory: str, func_id: int, o: np.ndarray, M: np.ndar
             f.write(" ".join(f"{float(v):.17g}" for v in M[i]) + "\n")
     with open(os.path.join(directory, "input_data", f"shift_data_{func_id}.txt"), "w") as f:
         f.write(" ".join(f"{float(v):.17g}" for v in o) + "\n")
+
+
+def cec_components(function_id: int) -> int:
+    """Components of a composition function (CUDA_EA_library/CEC2014.cc:306-333); 1 otherwise."""
+    return {23: 5, 24: 3, 25: 3, 26: 5, 27: 5, 28: 5, 29: 3, 30: 3}.get(function_id, 1)
+
+
+def uses_shuffle(function_id: int) -> bool:
+    """Hybrid functions (17-22) and the compositions of hybrids (29, 30) read a shuffle."""
+    return 17 <= function_id <= 22 or function_id in (29, 30)
+
+
+def make_instance_multi(seed: int, dim: int, function_id: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """(o, M, S) for any id: o (nc, D) and M (nc, D, D) as float32, component c drawn like
+    make_instance(seed + 1000003 c) (so component 0 is make_instance(seed)); S (nc, D) int32,
+    each row a 1-based permutation of 1..D (the reference's shuffle_data convention)."""
+    nc = cec_components(function_id)
+    o = np.empty((nc, dim), dtype=np.float32)
+    M = np.empty((nc, dim, dim), dtype=np.float32)
+    for c in range(nc):
+        o[c], M[c] = make_instance(seed + 1000003 * c, dim)
+    rng = np.random.default_rng(seed + 7919)
+    S = np.stack([rng.permutation(dim) + 1 for _ in range(nc)]).astype(np.int32)
+    return o, M, S
+
+
+def write_reference_data_multi(directory: str, func_id: int, o: np.ndarray, M: np.ndarray,
+                               S: np.ndarray | None) -> None:
+    """Writes (o, M, S) in the reference's text format for any id: M_<f>_D<d>.txt holds the nc
+    D x D blocks one after another; shift_data_<f>.txt one line per component, padded to 100
+    values (CEC2014.cc:385-418 reads D values and skips the rest of the line;
+    CEC2014_CUDA.cc:198-224 reads 100 values per component); shuffle_data_<f>_D<d>.txt one line
+    of D 1-based indices per component (CEC2014.cc:423-460)."""
+    import os
+
+    o = np.atleast_2d(o)
+    nc, D = o.shape
+    M = M.reshape(nc, D, D)
+    d = os.path.join(directory, "input_data")
+    os.makedirs(d, exist_ok=True)
+    with open(os.path.join(d, f"M_{func_id}_D{D}.txt"), "w") as f:
+        for c in range(nc):
+            for i in range(D):
+                f.write(" ".join(f"{float(v):.17g}" for v in M[c, i]) + "\n")
+    with open(os.path.join(d, f"shift_data_{func_id}.txt"), "w") as f:
+        for c in range(nc):
+            row = list(o[c]) + [0.0] * max(0, 100 - D)
+            f.write(" ".join(f"{float(v):.17g}" for v in row) + "\n")
+    if S is not None:
+        S = np.atleast_2d(S)
+        with open(os.path.join(d, f"shuffle_data_{func_id}_D{D}.txt"), "w") as f:
+            for c in range(S.shape[0]):
+                f.write(" ".join(str(int(v)) for v in S[c]) + "\n")
+

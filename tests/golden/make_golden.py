@@ -10,7 +10,9 @@ For each D the reference supports (CEC2014.cc:318-321) it makes a seeded synthet
 (o, M) in the reference's input_data text format, lets CEC2014::EvaluateFitness (function 9,
 rotated Rastrigin, returns f - f*) evaluate a set of points, and stores inputs and outputs.
 The tests check the oracle's restatement against these values on any machine.
-objective_cec.npz holds the same for functions 1-16 at D = 10 and 30 (keys "<fid>_<D>_<o|M|X|f>").
+objective_cec.npz holds the same for functions 1-16 at D = 10 and 30 (keys "<fid>_<D>_<o|M|X|f>"),
+objective_multi.npz for the hybrid and composition functions 17-30 at D = 10 and 30 (keys
+"<fid>_<D>_<o|M|S|X|f>", o / M / S with one row / block per component).
 """
 from __future__ import annotations
 
@@ -26,7 +28,8 @@ REPO = HERE.parent.parent
 sys.path.insert(0, str(REPO / "speo-gpu-single-control_gb300"))
 sys.path.insert(0, str(REPO / "oracle"))
 
-from speo_gb300.instances import make_instance, run_seed, write_reference_data  # noqa: E402
+from speo_gb300.instances import (make_instance, make_instance_multi, run_seed, uses_shuffle,  # noqa: E402
+                                  write_reference_data, write_reference_data_multi)
 
 DIMS = (10, 30, 50, 100)
 N_POINTS = 24
@@ -82,6 +85,29 @@ def main() -> None:
             cec.update({f"{fid}_{D}_o": o, f"{fid}_{D}_M": M, f"{fid}_{D}_X": X, f"{fid}_{D}_f": f})
     np.savez_compressed(HERE / "objective_cec.npz", **cec)
     print("wrote", HERE / "objective_cec.npz")
+
+    multi = {}
+    for fid in range(17, 31):
+        for D in (10, 30):
+            seed = run_seed(1, fid, D)
+            o, M, S = make_instance_multi(seed, D, fid)
+            rng = np.random.default_rng(seed + 13)
+            n = 12
+            X = np.empty((n, D), dtype=np.float32)
+            X[0] = o[0]                                                  # optimum (component 0)
+            X[1] = np.clip(o[0] + rng.normal(0, 1e-2, D), -100, 100)
+            X[2] = np.clip(o[-1] + rng.normal(0, 1.0, D), -100, 100)    # near the last component
+            X[3:] = rng.uniform(-100, 100, (n - 3, D))
+            with tempfile.TemporaryDirectory() as tmp:
+                write_reference_data_multi(tmp, fid, o, M, S if uses_shuffle(fid) else None)
+                assert ref.ref_cec_init(fid, D, tmp.encode()) == 0
+                Xd = np.ascontiguousarray(X, dtype=np.float64)
+                f = np.zeros(n, dtype=np.float64)
+                ref.ref_cec_eval_batch(Xd.ctypes.data, n, D, f.ctypes.data)
+            multi.update({f"{fid}_{D}_o": o, f"{fid}_{D}_M": M, f"{fid}_{D}_S": S, f"{fid}_{D}_X": X,
+                          f"{fid}_{D}_f": f})
+    np.savez_compressed(HERE / "objective_multi.npz", **multi)
+    print("wrote", HERE / "objective_multi.npz")
 
 
 if __name__ == "__main__":

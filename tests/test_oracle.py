@@ -60,6 +60,66 @@ def test_cec_objectives_match_reference_golden(oracle, fid, D):
     np.testing.assert_allclose(mine, f_ref, rtol=1e-12, atol=_bias_ulps(fid))
 
 
+GOLDEN_MULTI = Path(__file__).resolve().parent / "golden" / "objective_multi.npz"
+
+
+@pytest.mark.parametrize("fid", range(17, 31))
+@pytest.mark.parametrize("D", [10, 30])
+def test_hybrid_composition_match_reference_golden(oracle, fid, D):
+    """CEC2014 hybrid (17-22) and composition (23-30) functions: the oracle against the reference's
+    CEC2014::EvaluateFitness on multi-component instances (one shift / matrix / shuffle per component)."""
+    g = np.load(GOLDEN_MULTI)
+    o, M, S, X, f_ref = (g[f"{fid}_{D}_{k}"] for k in "oMSXf")
+    assert o.shape[0] == oracle.cec_components(fid)
+    mine = np.array([oracle.objective_multi(fid, x, o, M, S) for x in X])
+    np.testing.assert_allclose(mine, f_ref, rtol=1e-12, atol=_bias_ulps(fid))
+
+
+def test_hybrid_groups_follow_reference_split(oracle):
+    """G_nx[g] = ceil(gp_g * D) in double for all but the last group (CEC2014.cc:961-972)."""
+    assert oracle.hybrid_groups(17, 10) == [(0, 3), (3, 3), (6, 4)]
+    assert oracle.hybrid_groups(21, 10) == [(0, 1), (1, 2), (3, 2), (5, 2), (7, 3)]
+    assert oracle.hybrid_groups(22, 100) == [(0, 10), (10, 20), (30, 20), (50, 20), (70, 30)]
+    assert oracle.hybrid_groups(19, 30) == [(0, 6), (6, 6), (12, 9), (21, 9)]
+
+
+def _suite_instance(fid, D):
+    """The reference suite's own (o, M, S) for fid at D, read as CEC2014::Initilize reads them
+    (CEC2014.cc:354-460): M = the first nc*D*D values, o = the first D values of each of the first
+    nc lines, S = the first nc*D integers."""
+    nc = {23: 5, 24: 3, 25: 3, 26: 5, 27: 5, 28: 5, 29: 3, 30: 3}.get(fid, 1)
+    M = np.array(open(REF_DATA / f"M_{fid}_D{D}.txt").read().split(), dtype=np.float64)[: nc * D * D]
+    lines = open(REF_DATA / f"shift_data_{fid}.txt").read().splitlines()
+    if nc == 1:
+        o = np.array(" ".join(lines).split(), dtype=np.float64)[:D][None]
+    else:
+        o = np.stack([np.array(lines[c].split(), dtype=np.float64)[:D] for c in range(nc)])
+    S = None
+    shuf = REF_DATA / f"shuffle_data_{fid}_D{D}.txt"
+    if 17 <= fid <= 22 or fid in (29, 30):
+        S = np.array(open(shuf).read().split(), dtype=np.int32)[: nc * D].reshape(nc, D)
+    return o, M.reshape(nc, D, D), S
+
+
+@pytest.mark.skipif(not REF_DATA.exists(), reason="reference suite data not present")
+@pytest.mark.parametrize("fid", range(17, 31))
+@pytest.mark.parametrize("D", [10, 30])
+def test_hybrid_composition_on_suite_data(oracle, fid, D):
+    """The reference's own instances of 17-30 (read in place), evaluated by the reference's CEC2014.cc
+    and by the oracle."""
+    ref = oracle.ref_lib()
+    if ref is None:
+        pytest.skip("oracle/_ref not built")
+    o, M, S = _suite_instance(fid, D)
+    assert ref.ref_cec_init(fid, D, str(REF_DATA.parent).encode()) == 0
+    rng = np.random.default_rng(fid * 100 + D)
+    X = np.concatenate([o[:1], o[-1:] + rng.normal(0, 0.5, (1, D)), rng.uniform(-100, 100, (6, D))])
+    f_ref = np.zeros(len(X))
+    ref.ref_cec_eval_batch(np.ascontiguousarray(X).ctypes.data, len(X), D, f_ref.ctypes.data)
+    mine = np.array([oracle.objective_multi(fid, x, o, M, S) for x in X])
+    np.testing.assert_allclose(mine, f_ref, rtol=1e-12, atol=_bias_ulps(fid))
+
+
 @pytest.mark.skipif(not REF_DATA.exists(), reason="reference suite data not present")
 @pytest.mark.parametrize("D", [10, 30, 100])
 def test_objective_matches_reference_on_suite_data(oracle, D):
