@@ -670,7 +670,7 @@ def bench_e2e(L, dev, torch, args) -> dict:
     def run_native(nsteps):  # the reference's DE_CUDA::Run loop as one library call (C++ host loop)
         upload()
         _lib.check(L.speo_de_run_f32(P, C, rng_state.data_ptr(), ii, d_info.data_ptr(), best.data_ptr(), pi,
-                                     d_sh.data_ptr(), d_rot.data_ptr(), nsteps, h_hist.data_ptr(), 1,
+                                     d_sh.data_ptr(), d_rot.data_ptr(), None, nsteps, h_hist.data_ptr(), 1,
                                      stream.cuda_stream), "speo_de_run_f32")
         stream.synchronize()
 

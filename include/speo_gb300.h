@@ -139,9 +139,14 @@ SPEO_API int API_DE_SelectSurvival(speo_population_f64 d_population, speo_popula
 /* Replaces API_evaluateFitness (CEC2014_CUDA.h:35-37). d_rotated_data is the reference's
  * padded transposed matrix: d_rotated_data[k*problem_dim + j] = M[j][k] for k < np2
  * (rows k >= problem_dim zero), d_shift_data holds o in its first problem_dim entries,
- * rows of d_original_elements have np2 elements. Implemented ids: 9, 31. Scratch
- * arguments (shuffled, rotated, shuffle, tmp_fitness, wi, sigma) are accepted and unused:
- * the rotation is fused with the reduction, so no intermediate is written. */
+ * rows of d_original_elements have np2 elements. Implemented ids: 1-30 (CEC2014) and 31
+ * (rotated sphere). Ids 23-30 read one block per component: shift c at d_shift_data + c*np2,
+ * matrix c at d_rotated_data + c*np2*problem_dim (CEC2014_CUDA.cc:160-281); ids 17-22, 29, 30
+ * read d_shuffle_data (1-based, component c at + c*np2). The composition deltas are the
+ * reference's fixed tables (the values CEC2014_CUDA.cc:336-390 puts in d_sigma). Scratch
+ * arguments (shuffled, rotated, tmp_fitness, wi, sigma) are accepted and unused: each
+ * component's rotation is fused with its reduction and the mixing, so no intermediate is
+ * written. */
 SPEO_API void API_evaluateFitness(double *d_fitness_value, double *d_shuffled_elements,
                          double *d_rotated_elements, double *d_original_elements,
                          double *d_shift_data, double *d_rotated_data, int *d_shuffle_data,
@@ -165,7 +170,7 @@ SPEO_API void API_evaluateFitness_f32(float *d_fitness_value, float *d_shuffled_
 
 /* The reference's host generation loop (DE_CUDA::Run, CUDA_EA_library/DE_CUDA.cc:200-216),
  * natively: `generations` x (API_DE_GenerateNewPopulation_f32, API_evaluateFitness_f32 on
- * (d_shift, d_rot, problem_info.function_ID), API_DE_SelectSurvival_f32), with the same results
+ * (d_shift, d_rot, d_shuffle, problem_info.function_ID), API_DE_SelectSurvival_f32), with the same results
  * as those calls issued one by one. When a sub-island fits one block's shared memory, blocks of
  * generations run in one launch with the sub-island resident on chip; otherwise the three entry
  * points run in turn (replayed as a CUDA graph when h_fitness is pinned or null). h_fitness (may
@@ -177,7 +182,8 @@ SPEO_API void API_evaluateFitness_f32(float *d_fitness_value, float *d_shuffled_
 SPEO_API int speo_de_run_f32(speo_population_f32 d_population, speo_population_f32 d_candidate,
                              speo_rng_state *d_rng, speo_island_info island_info, speo_de_info_f32 *d_DE_info,
                              int *d_best_individual_ID, speo_problem_info_f32 problem_info, const float *d_shift,
-                             const float *d_rotated, int generations, float *h_fitness, int history, void *stream);
+                             const float *d_rotated, const int *d_shuffle, int generations, float *h_fitness,
+                             int history, void *stream);
 
 /* Per-sub-island DE parameters, as DE_CUDA::ConfigureEA (CUDA_EA_library/DE_CUDA.cc:89-118)
  * fills them before copying them to the device: `dynamic` = 0 ("constant") gives every
@@ -225,7 +231,13 @@ typedef struct {
     int32_t      ld_rot;     /* >= D, multiple of 4 */
     int32_t      ring_next;  /* segment that receives this one's emigrants, -1 = none */
     uint64_t     seed;       /* Philox key */
+    const int32_t *shuffle;  /* ids 17-22, 29, 30: device, 1-based shuffles; else unused (NULL) */
 } speo_segment;
+/* Ids 17-30 (CEC2014 hybrid and composition functions) carry one shift / matrix / shuffle per
+ * component (5 for 23, 26-28; 3 for 24, 25, 29, 30; 1 for 17-22): component c's shift starts at
+ * shift + c*ld_rot, its D rows of M^T at rot + c*dim*ld_rot, its shuffle at shuffle + c*ld_rot.
+ * speo_evaluate evaluates them; the fused generation, epoch and tensor-core kernels flag them
+ * (SPEO_DEVERR_BAD_SEGMENT / SPEO_ERR_UNSUPPORTED). */
 
 #define SPEO_TILE_SIMT  64   /* largest work item of the CUDA-core kernels */
 #define SPEO_TILE_TC   128   /* largest work item of the tcgen05 kernels   */

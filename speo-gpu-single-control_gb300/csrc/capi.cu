@@ -68,7 +68,7 @@ extern "C" int speo_device_error_bits(uint32_t *bits_out)
     if (int e = check_cuda(cudaDeviceSynchronize(), "speo_device_error_bits: sync")) return e;
     const unsigned bits = speo_deverr_de_ops() | speo_deverr_objective() | speo_deverr_generation() | speo_deverr_tc() |
                           speo_deverr_resident() | speo_deverr_surrogate() | speo_deverr_mlp() |
-                          speo_deverr_dropin_step();
+                          speo_deverr_dropin_step() | speo_deverr_objective_multi();
     if (bits & 0x80000000u) return fail(SPEO_ERR_CUDA, "speo_device_error_bits: cannot read the device flags");
     if (bits_out) *bits_out = bits;
     return SPEO_OK;

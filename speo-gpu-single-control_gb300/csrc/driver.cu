@@ -78,8 +78,8 @@ using namespace speo;
 
 extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand, speo_rng_state *rng,
                                speo_island_info ii, speo_de_info_f32 *d_info, int *d_best, speo_problem_info_f32 pi,
-                               const float *d_shift, const float *d_rot, int generations, float *h_fitness,
-                               int history, void *stream)
+                               const float *d_shift, const float *d_rot, const int *d_shuffle, int generations,
+                               float *h_fitness, int history, void *stream)
 {
     if (!pop.elements || !pop.fitness_value || !cand.elements || !cand.fitness_value || !rng || !d_info || !d_best ||
         !d_shift || !d_rot || !ii.permutated_index || generations < 0 || ii.island_size <= 0)
@@ -120,7 +120,8 @@ extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand
         if (int e2 = API_DE_GenerateNewPopulation_f32(cand, pop, d_best, ii, d_info, rng, pi)) return e2;
         const int before = sticky_status();
         API_evaluateFitness_f32(cand.fitness_value, nullptr, nullptr, cand.elements, const_cast<float *>(d_shift),
-                                const_cast<float *>(d_rot), nullptr, nullptr, nullptr, nullptr, n, pi.dim, 0.f,
+                                const_cast<float *>(d_rot), const_cast<int *>(d_shuffle), nullptr, nullptr, nullptr, n,
+                                pi.dim, 0.f,
                                 pi.function_ID);
         if (sticky_status() != before) return sticky_status();
         if (int e2 = API_DE_SelectSurvival_f32(pop, cand, ii, pi)) return e2;

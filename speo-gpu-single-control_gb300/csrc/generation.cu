@@ -253,7 +253,8 @@ __device__ __forceinline__ void gen_tile(const GenArgs &a, const speo_work_item 
 __device__ __forceinline__ bool tile_ok(const speo_work_item &it, const speo_segment &s)
 {
     return it.count >= 1 && it.count <= kEvalTile && s.pop_size >= 2 && s.dim >= 1 && s.dim <= SPEO_MAX_DIM &&
-           (s.ld & 3) == 0 && s.ld >= s.dim && it.first >= 0 && it.first + it.count <= s.pop_size;
+           (s.ld & 3) == 0 && s.ld >= s.dim && it.first >= 0 && it.first + it.count <= s.pop_size &&
+           func_supported(s.func_id);
 }
 
 // Advances the generation counter once every block of the launch has read it.

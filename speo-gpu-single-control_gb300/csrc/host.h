@@ -75,6 +75,11 @@ int mlp_grad_bf16(const float *theta, int din, int h, const float *mu, const flo
 // 2 = two-block clusters (bit-identical to one block). Fits when a sub-island's rows, trials and
 // M^T fit one block's shared memory.
 bool dropin_step_fits_f32(int island_size, int subisland_num, int dim, int func);
+// API_evaluateFitness(_f32) for ids 17-30 (objective_multi.cu); arguments already checked.
+template <typename T>
+int eval_ref_multi(T *fit, const T *X, const T *shift, const T *rot, const int *shuf, int P, int D, int func,
+                   cudaStream_t st);
+
 int dropin_step_f32(speo_population_f32 pop, speo_population_f32 cand, int *d_best, speo_island_info ii,
                     speo_de_info_f32 *d_info, speo_rng_state *rng, speo_problem_info_f32 pi, const float *shift,
                     const float *rot, int generations, float *d_hist, int pair_mode, cudaStream_t st);
@@ -94,3 +99,4 @@ extern "C" unsigned int speo_deverr_resident(void);
 extern "C" unsigned int speo_deverr_surrogate(void);
 extern "C" unsigned int speo_deverr_mlp(void);
 extern "C" unsigned int speo_deverr_dropin_step(void);
+extern "C" unsigned int speo_deverr_objective_multi(void);

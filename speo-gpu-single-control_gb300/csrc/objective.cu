@@ -1,46 +1,18 @@
 // objective.cu -- exact objective evaluation on CUDA cores:
 //   * API_evaluateFitness / API_evaluateFitness_f32: the reference-shaped entry point
-//     (CUDA_EA_library/CEC2014_CUDA.h:35-37, kernel_CEC2014_CUDA.cu:1672-1797) for ids 9
-//     (F9, rotated Rastrigin) and 31 (rotated sphere), reference data layout;
-//   * speo_evaluate: the same evaluation over the segment/work-item tables (FP32);
+//     (CUDA_EA_library/CEC2014_CUDA.h:35-37, kernel_CEC2014_CUDA.cu:1672-1797) for ids 1-16
+//     and 31 (rotated sphere), reference data layout; ids 17-30 in objective_multi.cu;
+//   * speo_evaluate: the same evaluation over the segment/work-item tables (FP32), ids 1-31;
 //   * speo_best_reeval_f64: per segment argmin + FP64 re-evaluation of the best row.
 #include <cmath>
 
-#include "eval_simt.cuh"
+#include "eval_tile.cuh"
 #include "host.h"
 
 SPEO_DEFINE_DEVERR(speo_deverr_objective)
 
 namespace speo {
 namespace {
-
-constexpr int kChunk = 32;  // rows of M^T staged per step
-
-struct TileDesc {
-    const void *x;        // first row of the tile
-    long long ldx;        // row stride (elements)
-    int count;            // rows in the tile (<= kEvalTile)
-    int D, func, ld_rot;
-    const void *shift, *rot;
-    void *fit;            // fitness of the first row of the tile
-};
-
-template <typename T>
-__device__ __forceinline__ TileDesc ref_tile(int t, const T *X, int ldx, int P, int D, int func, const T *shift,
-                                             const T *rot, T *fit)
-{
-    TileDesc d;
-    d.x = X + (size_t)t * kEvalTile * ldx;
-    d.ldx = ldx;
-    d.count = min(kEvalTile, P - t * kEvalTile);
-    d.D = D;
-    d.func = func;
-    d.ld_rot = D;
-    d.shift = shift;
-    d.rot = rot;
-    d.fit = fit + (size_t)t * kEvalTile;
-    return d;
-}
 
 // Piece `sub` (64 rows) of work item t; work items may be any size.
 __device__ __forceinline__ bool seg_tile(int t, int sub, const speo_segment *segs, const speo_work_item *items,
@@ -61,6 +33,9 @@ __device__ __forceinline__ bool seg_tile(int t, int sub, const speo_segment *seg
     d.shift = s.shift;
     d.rot = s.rot;
     d.fit = fit + row;
+    d.shift_cs = d.shuf_cs = s.ld_rot;
+    d.rot_cs = (long long)s.dim * s.ld_rot;
+    d.shuf = s.shuffle;
     return true;
 }
 
@@ -139,6 +114,21 @@ __global__ void __launch_bounds__(256, (!G && (Q == 1 || Q == 4)) ? 4 : 1) k_eva
             if ((d.D + 31) / 32 > Q) break;  // handled by the launch for its own Q
             if (Q > 1 && (d.D + 31) / 32 <= Q / 2) break;
             if (func_sum_form(d.func) == G) break;  // handled by the other variant's launch
+            if (G && func_multi(d.func)) {
+                if (!multi_dim_ok(d.func, d.D) || (d.ld_rot & 3) || d.ld_rot < d.D) {
+                    if (threadIdx.x == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+                    break;
+                }
+                float *fbuf, *sbuf;
+                int *Ss;
+                multi_smem<float, Q>(smem_raw, Ys, Ms, fbuf, sbuf, Ss);
+                eval_multi_tile<float, Q>(d, Ys, Ms, Ss, fbuf, sbuf, &s_deverr);
+                continue;
+            }
+            if (!func_supported(d.func)) {
+                if (threadIdx.x == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+                break;
+            }
             eval_one_tile<float, Q, G>(d, Ys, Ms);
         }
     }
@@ -153,7 +143,7 @@ __global__ void __launch_bounds__(256) k_best_reeval(const speo_segment *segs, c
     __shared__ long long brs[8];
     const speo_segment &s = segs[blockIdx.x];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (s.pop_size < 1 || s.dim < 1 || s.dim > SPEO_MAX_DIM) {
+    if (s.pop_size < 1 || s.dim < 1 || s.dim > SPEO_MAX_DIM || !func_any(s.func_id)) {
         if (threadIdx.x == 0) {
             atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
             best_err[blockIdx.x] = __longlong_as_double(0x7ff8000000000000LL);
@@ -180,31 +170,72 @@ __global__ void __launch_bounds__(256) k_best_reeval(const speo_segment *segs, c
     }
     __syncthreads();
     const long long row = brs[0];
-    const int D = s.dim;
-    for (int k = threadIdx.x; k < D; k += blockDim.x)
-        ys[k] = (double)pop[row * s.ld + k] - (double)s.shift[k];
-    __syncthreads();
-    const int fid = s.func_id;
-    const double scale = func_scale_f64(fid), fs = func_fixed_shift<double>(fid);
-    for (int j = threadIdx.x; j < D; j += blockDim.x) {
-        double z = ys[j];
-        if (func_rotated(fid)) {
-            z = 0.0;
-            for (int k = 0; k < D; ++k) z = __fma_rn(ys[k], (double)s.rot[(size_t)k * s.ld_rot + j], z);
-        }
-        zs[j] = z * scale + fs;
-    }
-    __syncthreads();
-    if (warp == 0) {
-        RowAcc<double> a;
-        for (int j = lane; j < D; j += 32) row_push(a, fid, j, zs[j], zs[j + 1 < D ? j + 1 : 0], D);
-        a.s1 = warp_sum(a.s1);
-        a.s2 = warp_sum(a.s2);
-        a.p = warp_prod(a.p);
-        if (lane == 0) {
-            best_err[blockIdx.x] = row_finish(a, fid, D);
+    const int D = s.dim, fid = s.func_id;
+    // ids 17-30: each component in turn (shift / matrix / shuffle c), then the mixing
+    const bool multi = func_multi(fid);
+    if (multi && (!multi_dim_ok(fid, D) || (s.ld_rot & 3) || s.ld_rot < D)) {
+        if (threadIdx.x == 0) {
+            atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+            best_err[blockIdx.x] = __longlong_as_double(0x7ff8000000000000LL);
             best_row[blockIdx.x] = row;
         }
+        return;
+    }
+    __shared__ int ss[SPEO_MAX_DIM];
+    __shared__ double cfit[kMaxComp], csq[kMaxComp];
+    const int nc = func_components(fid);
+    for (int c = 0; c < nc; ++c) {
+        const int h = multi_hybrid(fid, c);
+        const CompPiece pc = func_composition(fid) ? comp_piece(fid, c) : CompPiece{fid, func_rotated(fid), 0.0, 0.0};
+        const float *o = s.shift + (size_t)c * s.ld_rot;
+        const float *rot = s.rot + (size_t)c * D * s.ld_rot;
+        __syncthreads();
+        for (int k = threadIdx.x; k < D; k += blockDim.x) {
+            ys[k] = (double)pop[row * s.ld + k] - (double)o[k];
+            if (h >= 0) {
+                int v = s.shuffle ? s.shuffle[(size_t)c * s.ld_rot + k] - 1 : -1;
+                if (v < 0 || v >= D) {
+                    atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+                    v = 0;
+                }
+                ss[k] = v;
+            }
+        }
+        __syncthreads();
+        const double scale = h >= 0 ? 1.0 : func_scale_f64(pc.fid);
+        const double fs = h >= 0 ? 0.0 : func_fixed_shift<double>(pc.fid);
+        for (int j = threadIdx.x; j < D; j += blockDim.x) {
+            double z = ys[j];
+            if (h >= 0 || pc.rotated) {
+                z = 0.0;
+                for (int k = 0; k < D; ++k) z = __fma_rn(ys[k], (double)rot[(size_t)k * s.ld_rot + j], z);
+            }
+            zs[j] = z * scale + fs;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            double f;
+            if (h >= 0) {
+                f = hybrid_row_warp<double>(zs, ss, h, D, lane);
+            } else {
+                RowAcc<double> a;
+                for (int j = lane; j < D; j += 32) row_push(a, pc.fid, j, zs[j], zs[j + 1 < D ? j + 1 : 0], D);
+                a.s1 = warp_sum(a.s1);
+                a.s2 = warp_sum(a.s2);
+                a.p = warp_prod(a.p);
+                f = row_finish(a, pc.fid, D);
+                if (pc.den != 0.0) f = pc.num * f / pc.den;
+            }
+            double sq = 0.0;
+            for (int k = lane; k < D; k += 32) sq += ys[k] * ys[k];
+            sq = warp_sum(sq);
+            if (lane == 0) { cfit[c] = f; csq[c] = sq; }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        best_err[blockIdx.x] = func_composition(fid) ? comp_combine<double>(fid, D, cfit, csq) : cfit[0];
+        best_row[blockIdx.x] = row;
     }
 }
 
@@ -226,17 +257,22 @@ int launch_ref(const T *X, int ldx, int P, int D, int func, const T *shift, cons
 }
 
 template <typename T>
-int eval_ref(T *fit, T *X, T *shift, T *rot, int P, int D, int func)
+int eval_ref(T *fit, T *X, T *shift, T *rot, const int *shuf, int P, int D, int func)
 {
-    if (!func_supported(func))
-        return fail(SPEO_ERR_UNSUPPORTED, "API_evaluateFitness: function_ID %d is not implemented (1-16, 31)", func);
+    if (!func_any(func))
+        return fail(SPEO_ERR_UNSUPPORTED, "API_evaluateFitness: function_ID %d is not implemented (1-31)", func);
     if (!fit || !X || !shift || !rot) return fail(SPEO_ERR_INVALID_ARG, "API_evaluateFitness: null pointer");
     if (P <= 0 || D < 1 || D > SPEO_MAX_DIM)
         return fail(SPEO_ERR_INVALID_ARG, "API_evaluateFitness: pop_size %d, dim %d", P, D);
+    if (func_uses_shuffle(func) && !shuf)
+        return fail(SPEO_ERR_INVALID_ARG, "API_evaluateFitness: function_ID %d needs the shuffle data", func);
+    if (func_multi(func) && !multi_dim_ok(func, D))
+        return fail(SPEO_ERR_INVALID_ARG, "API_evaluateFitness: function_ID %d is not defined for dim %d", func, D);
     int ldx = 1;
     while (ldx < D) ldx <<= 1;
     if (ldx < 32) ldx = 32;
     cudaStream_t st = api_stream();
+    if (func_multi(func)) return eval_ref_multi<T>(fit, X, shift, rot, shuf, P, D, func, st);
     switch ((D + 31) / 32) {
     case 1: return launch_ref<T, 1>(X, ldx, P, D, func, shift, rot, fit, st);
     case 2: return launch_ref<T, 2>(X, ldx, P, D, func, shift, rot, fit, st);
@@ -250,15 +286,16 @@ int launch_seg(const speo_segment *segs, const speo_work_item *items, int n_item
                cudaStream_t st)
 {
     const size_t smem = sizeof(float) * (size_t)(kEvalTile + kChunk) * 32 * Q;
+    constexpr size_t smem_g = multi_smem_bytes<float, Q>();  // the generic variant also runs ids 17-30
     // two variants: the per-coordinate sums (8, 9, 31) and the other ids; each skips the other's tiles
     cudaError_t e = cudaFuncSetAttribute(k_eval_seg<Q, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_eval_seg<Q, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(k_eval_seg<Q, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_eval_seg)");
     const int grid = n_items < 4 * sm_count() ? n_items : 4 * sm_count();
     k_eval_seg<Q, false><<<grid, 256, smem, st>>>(segs, items, n_items, pop, fit);
     if (int r = check_launch("k_eval_seg")) return r;
-    k_eval_seg<Q, true><<<grid, 256, smem, st>>>(segs, items, n_items, pop, fit);
+    k_eval_seg<Q, true><<<grid, 256, smem_g, st>>>(segs, items, n_items, pop, fit);
     return check_launch("k_eval_seg");
 }
 
@@ -267,16 +304,16 @@ int launch_seg(const speo_segment *segs, const speo_work_item *items, int n_item
 
 using namespace speo;
 
-extern "C" void API_evaluateFitness(double *f, double *, double *, double *X, double *shift, double *M, int *, double *,
-                                    double *, double *, int P, int D, double, int fid)
+extern "C" void API_evaluateFitness(double *f, double *, double *, double *X, double *shift, double *M, int *shuffle,
+                                    double *, double *, double *, int P, int D, double, int fid)
 {
-    eval_ref<double>(f, X, shift, M, P, D, fid);
+    eval_ref<double>(f, X, shift, M, shuffle, P, D, fid);
 }
 
-extern "C" void API_evaluateFitness_f32(float *f, float *, float *, float *X, float *shift, float *M, int *, float *,
-                                        float *, float *, int P, int D, float, int fid)
+extern "C" void API_evaluateFitness_f32(float *f, float *, float *, float *X, float *shift, float *M, int *shuffle,
+                                        float *, float *, float *, int P, int D, float, int fid)
 {
-    eval_ref<float>(f, X, shift, M, P, D, fid);
+    eval_ref<float>(f, X, shift, M, shuffle, P, D, fid);
 }
 
 extern "C" int speo_evaluate(const speo_segment *segs, const speo_work_item *items, int n_items, int dim_lo,

@@ -1,0 +1,63 @@
+// objective_multi.cu -- API_evaluateFitness for the CEC2014 hybrid (17-22) and composition
+// (23-30) functions (CUDA_EA_library/kernel_CEC2014_CUDA.cu:1204-1670, HybirdFunc1-6 and
+// CompFunc1-8; CPU definitions CEC2014.cc:954-1520) on the reference's device data layout: one
+// launch per call, every component's shift + rotation + body fused per 64-row tile, the
+// composition weights and mixing in the same kernel.
+#include "eval_tile.cuh"
+#include "host.h"
+
+SPEO_DEFINE_DEVERR(speo_deverr_objective_multi)
+
+namespace speo {
+namespace {
+
+template <typename T, int Q>
+__global__ void __launch_bounds__(256) k_eval_ref_multi(const T *X, int ldx, int P, int D, int func, const T *shift,
+                                                        const T *rot, const int *shuf, T *fit)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *Ys, *Ms, *fbuf, *sbuf;
+    int *Ss;
+    multi_smem<T, Q>(smem_raw, Ys, Ms, fbuf, sbuf, Ss);
+    const int tiles = (P + kEvalTile - 1) / kEvalTile;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x)
+        eval_multi_tile<T, Q>(ref_tile_multi<T>(t, X, ldx, P, D, func, shift, rot, shuf, fit), Ys, Ms, Ss, fbuf,
+                              sbuf, &s_deverr);
+}
+
+template <typename T, int Q>
+int launch_ref_multi(const T *X, int ldx, int P, int D, int func, const T *shift, const T *rot, const int *shuf, T *fit,
+                     cudaStream_t st)
+{
+    constexpr size_t smem = multi_smem_bytes<T, Q>();
+    cudaError_t e = cudaFuncSetAttribute(k_eval_ref_multi<T, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_eval_ref_multi)");
+    const int tiles = (P + kEvalTile - 1) / kEvalTile;
+    const int per_sm = sizeof(T) == 8 && Q == 8 ? 1 : 2;
+    const int grid = tiles < per_sm * sm_count() ? tiles : per_sm * sm_count();
+    k_eval_ref_multi<T, Q><<<grid, 256, smem, st>>>(X, ldx, P, D, func, shift, rot, shuf, fit);
+    return check_launch("k_eval_ref_multi");
+}
+
+}  // namespace
+
+template <typename T>
+int eval_ref_multi(T *fit, const T *X, const T *shift, const T *rot, const int *shuf, int P, int D, int func,
+                   cudaStream_t st)
+{
+    int ldx = 1;
+    while (ldx < D) ldx <<= 1;
+    if (ldx < 32) ldx = 32;
+    switch ((D + 31) / 32) {
+    case 1: return launch_ref_multi<T, 1>(X, ldx, P, D, func, shift, rot, shuf, fit, st);
+    case 2: return launch_ref_multi<T, 2>(X, ldx, P, D, func, shift, rot, shuf, fit, st);
+    case 3: case 4: return launch_ref_multi<T, 4>(X, ldx, P, D, func, shift, rot, shuf, fit, st);
+    default: return launch_ref_multi<T, 8>(X, ldx, P, D, func, shift, rot, shuf, fit, st);
+    }
+}
+template int eval_ref_multi<float>(float *, const float *, const float *, const float *, const int *, int, int, int,
+                                   cudaStream_t);
+template int eval_ref_multi<double>(double *, const double *, const double *, const double *, const int *, int, int,
+                                    int, cudaStream_t);
+
+}  // namespace speo

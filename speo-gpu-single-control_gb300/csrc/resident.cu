@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const speo_segment &s = segs[blockIdx.x];
     const int D = s.dim, P = s.pop_size, ld = s.ld, nch = (D + 3) >> 2;
     const uint32_t gen0 = *(volatile uint32_t *)gen_ctr;
-    const bool seg_ok = P >= 2 && P <= Pmax && D >= 1 && D <= W && (ld & 3) == 0 && ld >= D;
+    const bool seg_ok = P >= 2 && P <= Pmax && D >= 1 && D <= W && (ld & 3) == 0 && ld >= D && func_supported(s.func_id);
     if (seg_ok) {
         const long long row0 = s.row0;
         const uint2 key = seed_key(s.seed);
@@ -295,7 +295,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
     const uint32_t gen0 = *(volatile uint32_t *)gen_ctr;
     // both blocks of a cluster read the same segment, so they take the same branch and pass the
     // same number of cluster barriers
-    const bool seg_ok = P >= 2 && P <= Pmax && D >= 1 && D <= W && (ld & 3) == 0 && ld >= D;
+    const bool seg_ok = P >= 2 && P <= Pmax && D >= 1 && D <= W && (ld & 3) == 0 && ld >= D && func_supported(s.func_id);
     if (seg_ok) {
         const long long row0 = s.row0;
         const uint2 key = seed_key(s.seed);

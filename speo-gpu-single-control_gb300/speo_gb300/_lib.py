@@ -37,7 +37,7 @@ class Segment(ctypes.Structure):
         ("row0", c_int64), ("pop_size", c_int32), ("dim", c_int32), ("ld", c_int32),
         ("func_id", c_int32), ("strategy", c_int32), ("F", c_float), ("CR", c_float),
         ("lb", c_float), ("ub", c_float), ("shift", c_void_p), ("rot", c_void_p),
-        ("ld_rot", c_int32), ("ring_next", c_int32), ("seed", c_uint64),
+        ("ld_rot", c_int32), ("ring_next", c_int32), ("seed", c_uint64), ("shuffle", c_void_p),
     ]
 
 
@@ -92,7 +92,7 @@ SIGNATURES: dict[str, tuple] = {
     "speo_configure_de_f32": (c_int, [c_void_p, c_int, c_int, c_float, c_float, c_int, c_int, c_uint64]),
     "speo_configure_de_f64": (c_int, [c_void_p, c_int, c_int, c_double, c_double, c_int, c_int, c_uint64]),
     "speo_de_run_f32": (c_int, [PopulationF32, PopulationF32, c_void_p, IslandInfo, c_void_p, c_void_p, ProblemInfoF32,
-                                c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p]),
+                                c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p]),
     "API_evaluateFitness": (None, [c_void_p] * 10 + [c_int, c_int, c_double, c_int]),
     "API_evaluateFitness_f32": (None, [c_void_p] * 10 + [c_int, c_int, c_float, c_int]),
     "speo_set_stream": (c_int, [c_void_p]),

@@ -42,7 +42,8 @@ def _bytes_to_device(buf: ctypes.Array, device) -> torch.Tensor:
 @dataclass
 class SegmentTable:
     specs: list[SegmentSpec]
-    instances: list[tuple[np.ndarray, np.ndarray]]    # (o, M) float32
+    # (o, M) float32, or (o, M, S) for ids 17-30: o (nc, D), M (nc, D, D), S (nc, D) 1-based int32
+    instances: list[tuple]
     tile_rows: int = _lib.TILE_SIMT
     device: str = "cuda"
     rows: int = field(init=False)
@@ -52,11 +53,22 @@ class SegmentTable:
         dev = torch.device(self.device)
         self.inst_shift = []
         self.inst_rot = []
-        for o, M in self.instances:
-            D = o.shape[0]
+        self.inst_shuf = []
+        for inst in self.instances:
+            # component c: shift at c*ldr, D rows of M^T at c*D*ldr, shuffle at c*ldr
+            o = np.atleast_2d(inst[0])
+            nc, D = o.shape
+            M = np.asarray(inst[1]).reshape(nc, D, D)
             ldr = (D + 3) // 4 * 4
-            self.inst_shift.append(torch.from_numpy(shift_layout(o)).to(dev))
-            self.inst_rot.append(torch.from_numpy(rot_layout(M, ldr)).to(dev))
+            self.inst_shift.append(torch.from_numpy(np.concatenate([shift_layout(o[c], ldr) for c in range(nc)])).to(dev))
+            self.inst_rot.append(torch.from_numpy(np.concatenate([rot_layout(M[c], ldr) for c in range(nc)])).to(dev))
+            shuf = None
+            if len(inst) > 2 and inst[2] is not None:
+                S = np.atleast_2d(inst[2]).astype(np.int32)
+                pad = np.zeros((nc, ldr), dtype=np.int32)
+                pad[:, :D] = S
+                shuf = torch.from_numpy(pad.reshape(-1)).to(dev)
+            self.inst_shuf.append(shuf)
         segs = (_lib.Segment * len(self.specs))()
         row = 0
         self.max_ld = 0
@@ -74,6 +86,8 @@ class SegmentTable:
             s.shift = self.inst_shift[sp.instance].data_ptr()
             s.rot = self.inst_rot[sp.instance].data_ptr()
             s.ld_rot = self.inst_rot[sp.instance].shape[1]
+            shuf = self.inst_shuf[sp.instance]
+            s.shuffle = shuf.data_ptr() if shuf is not None else None
             s.ring_next = sp.ring_next
             s.seed = sp.seed
             row += sp.pop_size
@@ -206,8 +220,10 @@ class SegmentTable:
         """The segment table as the oracle's dicts (host copies of o and M)."""
         out = []
         for i, sp in enumerate(self.specs):
-            o, M = self.instances[sp.instance]
+            inst = self.instances[sp.instance]
+            o, M = inst[0], inst[1]
+            S = inst[2] if len(inst) > 2 else None
             out.append(dict(row0=int(self.host_segs[i].row0), P=sp.pop_size, D=sp.dim, ld=self.ld, func=sp.func_id,
-                            strategy=sp.strategy, F=sp.F, CR=sp.CR, lb=sp.lb, ub=sp.ub, o=o, M=M, seed=sp.seed,
+                            strategy=sp.strategy, F=sp.F, CR=sp.CR, lb=sp.lb, ub=sp.ub, o=o, M=M, S=S, seed=sp.seed,
                             ring_next=sp.ring_next))
         return out

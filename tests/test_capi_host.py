@@ -97,12 +97,30 @@ def test_dropin_validation_happens_before_any_device_work(lib):
     assert lib.API_Initilize_f32(pop, None, ii, pi) == _lib.SPEO_ERR_INVALID_ARG
 
 
-@pytest.mark.parametrize("fid", [0, 17, 23, 30, 32])
+@pytest.mark.parametrize("fid", [-1, 0, 32, 33])
 def test_evaluate_rejects_unimplemented_function_id(lib, fid):
-    """Ids 1-16 (CEC2014) and 31 (rotated sphere) are implemented; the hybrid (17-22) and
-    composition (23-30) functions are not, and are refused before any device work."""
+    """Ids 1-30 (CEC2014) and 31 (rotated sphere) are implemented; any other id is refused
+    before any device work."""
     lib.API_evaluateFitness_f32(*([ctypes.c_void_p(1)] * 10), 100, 30, 0.0, fid)
-    assert f"function_ID {fid}".encode() in lib.speo_last_error()
+    assert f"function_ID {fid} is not implemented".encode() in lib.speo_last_error()
+
+
+@pytest.mark.parametrize("fid", [17, 22, 29, 30])
+def test_evaluate_hybrids_need_shuffle(lib, fid):
+    """The hybrid functions and the compositions of hybrids read the shuffle data; without it the
+    call is refused before any device work."""
+    args = [ctypes.c_void_p(1)] * 10
+    args[6] = None
+    lib.API_evaluateFitness_f32(*args, 100, 30, 0.0, fid)
+    assert f"function_ID {fid} needs the shuffle data".encode() in lib.speo_last_error()
+
+
+@pytest.mark.parametrize("fid,D", [(17, 2), (21, 3), (22, 4), (29, 2), (30, 3)])
+def test_evaluate_hybrids_refuse_dims_without_every_group(lib, fid, D):
+    """A hybrid is defined only where each of its groups gets a coordinate (CEC2014.cc:350 excludes
+    D = 2); such dimensions are refused."""
+    lib.API_evaluateFitness_f32(*([ctypes.c_void_p(1)] * 10), 100, D, 0.0, fid)
+    assert f"function_ID {fid} is not defined for dim {D}".encode() in lib.speo_last_error()
 
 
 def test_struct_layouts_match_c(tmp_path):

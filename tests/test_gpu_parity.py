@@ -127,6 +127,9 @@ def test_dropin_generate_matches_oracle(lib, oracle, cuda, f64, P, D, nsub):
     (5, True, False, 64, 10, 1, 10, (1,)),           # unrotated Schwefel, one sub-island
     (22, True, False, 4096, 100, 1, 9, (4,)),        # too large for one block: three calls, graph blocks
     (4, True, True, 4096, 100, 1, 9, (4,)),          # the same with every generation's fitness
+    (9, True, True, 200, 30, 2, 23, (4, 6)),         # composition: three calls, every generation's fitness
+    (24, True, False, 300, 50, 3, 30, (4, 6, 2)),    # composition of hybrids: graph blocks
+    (5, False, True, 120, 20, 2, 21, (6,)),          # hybrid, pageable buffer
 ])
 def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned, history, P, D, nsub, fid, strats):
     """speo_de_run_f32 (the reference's DE_CUDA::Run loop, natively: sub-islands resident in shared
@@ -135,15 +138,18 @@ def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned, history, P, D, 
     populations, candidates, best ids, generation counter and per-generation fitness as the drop-in
     calls issued one by one."""
     import torch
-    from speo_gb300.instances import make_instance
+    from speo_gb300.instances import make_instance_multi
 
-    o, M = make_instance(77, D)
-    ld = np2(D)
-    rot = np.zeros((ld, D), dtype=np.float32)
-    rot[:D] = M.T
-    shift = np.zeros(ld, dtype=np.float32)
-    shift[:D] = o
+    o, M, S = make_instance_multi(77, D, fid)       # component 0 = make_instance(77, D)
+    nc, ld = o.shape[0], np2(D)
+    rot = np.zeros((nc, ld, D), dtype=np.float32)
+    rot[:, :D] = M.transpose(0, 2, 1)
+    shift = np.zeros((nc, ld), dtype=np.float32)
+    shift[:, :D] = o
+    shuf = np.zeros((nc, ld), dtype=np.int32)
+    shuf[:, :D] = S
     d_rot, d_sh = torch.from_numpy(rot).to(cuda), torch.from_numpy(shift).to(cuda)
+    d_sf = torch.from_numpy(shuf).to(cuda)
     rng = np.random.default_rng(9)
     pop0 = np.zeros((P, ld), dtype=np.float32)
     pop0[:, :D] = rng.uniform(-100, 100, (P, D))
@@ -159,7 +165,8 @@ def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned, history, P, D, 
         pop_s, cand_s = d.pops()
         d.call("API_Initilize", cand_s, d.rng.data_ptr(), d.island(), d.problem)
         d.pop.copy_(torch.from_numpy(pop0))
-        args = (None, None, d.pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(), None, None, None, None, P, D, 0.0, fid)
+        args = (None, None, d.pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(), d_sf.data_ptr(), None, None, None, P,
+                D, 0.0, fid)
         d.lib.API_evaluateFitness_f32(d.pfit.data_ptr(), *args)
         if mode == "calls":
             per_gen = []
@@ -167,7 +174,7 @@ def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned, history, P, D, 
                 d.call("API_DE_GenerateNewPopulation", cand_s, pop_s, d.best.data_ptr(), d.island(),
                        d_info.data_ptr(), d.rng.data_ptr(), d.problem)
                 d.lib.API_evaluateFitness_f32(d.cfit.data_ptr(), None, None, d.cand.data_ptr(), d_sh.data_ptr(),
-                                              d_rot.data_ptr(), None, None, None, None, P, D, 0.0, fid)
+                                              d_rot.data_ptr(), d_sf.data_ptr(), None, None, None, P, D, 0.0, fid)
                 d.call("API_DE_SelectSurvival", pop_s, cand_s, d.island(), d.problem)
                 per_gen.append(d.pfit.cpu().numpy())
             h = np.stack(per_gen)
@@ -176,7 +183,8 @@ def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned, history, P, D, 
             if pinned:
                 h = h.pin_memory()
             d._lib.check(d.lib.speo_de_run_f32(pop_s, cand_s, d.rng.data_ptr(), d.island(), d_info.data_ptr(),
-                                               d.best.data_ptr(), d.problem, d_sh.data_ptr(), d_rot.data_ptr(), gens,
+                                               d.best.data_ptr(), d.problem, d_sh.data_ptr(), d_rot.data_ptr(),
+                                               d_sf.data_ptr(), gens,
                                                h.data_ptr(), int(history), None), "speo_de_run_f32")
             h = h.numpy().reshape(-1, P)
         d._lib.check(d.lib.API_CheckCUDAError(), "API_CheckCUDAError")
@@ -302,6 +310,124 @@ def test_evaluate_tc_flags_functions_it_does_not_implement(lib, cuda):
     _lib.check(lib.speo_device_error_bits(ctypes.byref(bits)), "read flags")
     assert bits.value & _lib.SPEO_DEVERR_BAD_SEGMENT
     assert torch.all(out == -1.0)
+
+
+# ---- hybrid (17-22) and composition (23-30) functions -------------------------------------
+# FP32 tolerances: the hybrids sum groups of the bodies above (Schwefel, Weierstrass and Katsuura
+# groups carry their own FP32 error), and the compositions mix components whose FP32 errors are
+# those of their bodies, rescaled; the FP32 mixing weights come from logarithms (relative error
+# ~|l| 2^-24 for |l| up to ~200).
+MULTI_FUNCS = list(range(17, 31))
+TOL32_MULTI = (2e-3, 5e-2)
+TOL64_MULTI = (1e-9, 1e-8)
+
+
+def _multi_points(rng, o, P, D):
+    X = rng.uniform(-100, 100, (P, D)).astype(np.float32)
+    X[0] = o[0]                                                       # the optimum (component 0)
+    X[1] = o[0] + rng.normal(0, 1e-3, D).astype(np.float32)
+    X[2] = np.clip(o[-1] + rng.normal(0, 1.0, D), -100, 100).astype(np.float32)
+    return X
+
+
+@pytest.mark.parametrize("f64", [False, True])
+@pytest.mark.parametrize("fid", MULTI_FUNCS)
+@pytest.mark.parametrize("P,D", [(100, 10), (90, 20), (130, 30), (64, 50), (70, 100)])
+def test_dropin_evaluate_multi_matches_oracle(lib, oracle, cuda, f64, fid, P, D):
+    """API_evaluateFitness for the hybrid and composition functions on the reference's device layout
+    (component c's shift at c*np2, M^T at c*np2*D, shuffle at c*np2; CEC2014_CUDA.cc:160-281)."""
+    import torch
+    from speo_gb300 import _lib
+    from speo_gb300.instances import make_instance_multi
+
+    o, M, S = make_instance_multi(P * 31 + D, D, fid)
+    nc, ld = o.shape[0], np2(D)
+    rng = np.random.default_rng(fid * 1000 + D)
+    X = np.zeros((P, ld), dtype=np.float32)
+    X[:, :D] = _multi_points(rng, o, P, D)
+    rot = np.zeros((nc, ld, D), dtype=np.float32)
+    rot[:, :D, :] = M.transpose(0, 2, 1)
+    shift = np.zeros((nc, ld), dtype=np.float32)
+    shift[:, :D] = o
+    shuf = np.zeros((nc, ld), dtype=np.int32)
+    shuf[:, :D] = S
+    dt = torch.float64 if f64 else torch.float32
+    tX, trot, tsh = (torch.from_numpy(a).to(cuda, dt) for a in (X, rot, shift))
+    tsf = torch.from_numpy(shuf).to(cuda)
+    f = torch.full((P,), -1.0, dtype=dt, device=cuda)
+    fn = lib.API_evaluateFitness if f64 else lib.API_evaluateFitness_f32
+    fn(f.data_ptr(), None, None, tX.data_ptr(), tsh.data_ptr(), trot.data_ptr(), tsf.data_ptr(), None, None, None, P, D,
+       0.0, fid)
+    _lib.check(lib.API_CheckCUDAError(), "API_evaluateFitness")
+    ref = oracle.evaluate_rows_multi(fid, X, D, o, M, S)
+    rtol, atol = TOL64_MULTI if f64 else TOL32_MULTI
+    assert abs(float(f[0])) <= atol                    # f(o_1) - f* = 0
+    _assert_fitness(f.cpu().numpy(), ref, rtol=rtol, atol=atol)
+
+
+def _table_multi(cuda, layout, seed=11):
+    """layout: (P, D, fid); one multi-component instance (o, M, S) per entry."""
+    from speo_gb300 import _lib
+    from speo_gb300.device import SegmentSpec, SegmentTable
+    from speo_gb300.instances import make_instance_multi
+
+    instances, specs = [], []
+    for i, (P, D, fid) in enumerate(layout):
+        instances.append(make_instance_multi(seed * 1000 + D * 37 + fid, D, fid))
+        specs.append(SegmentSpec(pop_size=P, dim=D, func_id=fid, instance=i, seed=seed + i))
+    return SegmentTable(specs, instances, device=str(cuda), tile_rows=_lib.TILE_SIMT)
+
+
+def test_segment_evaluate_multi_functions(oracle, cuda):
+    """speo_evaluate on one table holding every hybrid / composition id next to ids 1-16 and 31, at
+    D = 10, 30 (one column group) and 50 (the next); each segment against the oracle."""
+    import torch
+
+    layout = [(40 + fid, D, fid) for fid in MULTI_FUNCS for D in (10, 30)] + [(70, 50, 23), (66, 50, 30)]
+    layout += [(50, 30, 9), (50, 30, 4)]
+    tab = _table_multi(cuda, layout)
+    tab.init_population()
+    out = torch.zeros_like(tab.fit[0])
+    tab.evaluate(which=tab.cur, out=out)
+    torch.cuda.synchronize()
+    pop, got = tab.pop[tab.cur].cpu().numpy(), out.cpu().numpy()
+    for s in tab.oracle_segments():
+        r = slice(s["row0"], s["row0"] + s["P"])
+        ref = oracle.evaluate_rows_multi(s["func"], pop[r], s["D"], s["o"], s["M"], s["S"])
+        rtol, atol = TOL32_MULTI if s["func"] in MULTI_FUNCS else _tol(s["func"], False)
+        _assert_fitness(got[r], ref, rtol=rtol, atol=atol)
+
+
+def test_best_reeval_f64_multi_functions(oracle, cuda):
+    """speo_best_reeval_f64 on hybrid / composition segments: argmin row and its FP64 value."""
+    layout = [(64, 30, fid) for fid in MULTI_FUNCS] + [(48, 10, 29), (48, 50, 26)]
+    tab = _table_multi(cuda, layout)
+    tab.init_population()
+    rows, errs = tab.best_f64()
+    fit = tab.fit[tab.cur].cpu().numpy()
+    pop = tab.pop[tab.cur].cpu().numpy()
+    for i, s in enumerate(tab.oracle_segments()):
+        seg_fit = fit[s["row0"]:s["row0"] + s["P"]]
+        assert int(rows[i]) == s["row0"] + int(np.argmin(seg_fit))
+        ref = oracle.objective_multi(s["func"], pop[int(rows[i]), :s["D"]], s["o"], s["M"], s["S"])
+        assert float(errs[i]) == pytest.approx(ref, rel=1e-10, abs=1e-9)
+
+
+def test_fused_generation_flags_multi_functions(lib, cuda):
+    """The fused generation kernels implement ids 1-16 and 31: a hybrid / composition segment is
+    skipped and raises SPEO_DEVERR_BAD_SEGMENT (the drop-in loop evaluates those ids instead)."""
+    import ctypes
+
+    from speo_gb300 import _lib
+
+    tab = _table_multi(cuda, [(64, 30, 23)])
+    tab.init_population()
+    bits = ctypes.c_uint32()
+    _lib.check(lib.speo_device_error_bits(ctypes.byref(bits)), "clear flags")
+    assert bits.value == 0
+    tab.generation()
+    _lib.check(lib.speo_device_error_bits(ctypes.byref(bits)), "read flags")
+    assert bits.value & _lib.SPEO_DEVERR_BAD_SEGMENT
 
 
 # ---------------------------------------------------------------------------------------------
