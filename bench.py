@@ -704,6 +704,104 @@ def bench_e2e(L, dev, torch, args) -> dict:
             "python_loop_path": "the same entry points called one by one from Python (ctypes), per-call host cost"}
 
 
+# The reference's published runs (CEC2014 composition functions, D = 100, 4096 individuals per
+# GPU, FP64, DE/rand/1/bin CR = 0.9 F = 0.5): per-GPU Mevals/s of its 2-GPU runs, whole loop with
+# its host-staged migration (R/bin/Results/SPEO_GPU.csv).
+PUBLISHED_2GPU_MEVALS = {23: 2.94, 24: 3.84, 25: 3.61, 26: 2.25, 27: 2.30, 28: 2.71, 29: 2.87, 30: 2.43}
+
+
+def bench_published(L, dev, torch, gens: int = 300, gens64: int = 60) -> dict:
+    """F23-F30 at D = 100, one island of 4096 rows (one sub-island), through the drop-in entry
+    points on device-resident data: the FP32 loop as one speo_de_run_f32 call (last fitness read
+    back), and the FP64 loop (the reference's precision) as API_DE_GenerateNewPopulation +
+    API_evaluateFitness + API_DE_SelectSurvival called one by one; plus the evaluation kernel alone
+    (CUDA events). No migration (one island per GPU; the reference's numbers include its MPI
+    migration, 19-38% of its wall time at 2 GPUs)."""
+    from speo_gb300 import _lib
+    from speo_gb300.instances import make_instance_multi
+
+    n, D, ld = 4096, 100, 128
+    out = {"workload": "CEC2014 F23-F30, D=100, island of 4096, DE/rand/1/bin CR=0.9 F=0.5, synthetic instances",
+           "functions": {}}
+    stream = torch.cuda.current_stream()
+    L.speo_set_stream(ctypes.c_void_p(stream.cuda_stream))
+    for fid in range(23, 31):
+        o, M, S = make_instance_multi(run_seed() + fid, D, fid)
+        nc = o.shape[0]
+        rot = np.zeros((nc, ld, D), dtype=np.float32)
+        rot[:, :D] = M.transpose(0, 2, 1)
+        sh = np.zeros((nc, ld), dtype=np.float32)
+        sh[:, :D] = o
+        sf = np.zeros((nc, ld), dtype=np.int32)
+        sf[:, :D] = S
+        rec = {}
+        for f64 in (False, True):
+            dt = torch.float64 if f64 else torch.float32
+            sfx = "" if f64 else "_f32"
+            Pop = _lib.PopulationF64 if f64 else _lib.PopulationF32
+            PI = _lib.ProblemInfoF64 if f64 else _lib.ProblemInfoF32
+            DI = _lib.DEInfoF64 if f64 else _lib.DEInfoF32
+            pop, cand = torch.zeros(n, ld, dtype=dt, device=dev), torch.zeros(n, ld, dtype=dt, device=dev)
+            pfit, cfit = torch.zeros(n, dtype=dt, device=dev), torch.zeros(n, dtype=dt, device=dev)
+            d_rot, d_sh = torch.from_numpy(rot).to(dev, dt), torch.from_numpy(sh).to(dev, dt)
+            d_sf = torch.from_numpy(sf).to(dev)
+            rng_state = torch.zeros(16, dtype=torch.int32, device=dev)
+            perm = torch.arange(n, dtype=torch.int32, device=dev)
+            best = torch.zeros(1, dtype=torch.int32, device=dev)
+            info = (DI * 1)(DI(0.9, 0.5, 4, n))
+            d_info = torch.frombuffer(bytearray(bytes(info)), dtype=torch.uint8).to(dev)
+            ii = _lib.IslandInfo(n, 1, perm.data_ptr())
+            pi = PI(D, fid, 1, 0, run_seed(), 0, 0, 100.0, -100.0)
+            P, C = Pop(pop.data_ptr(), pfit.data_ptr()), Pop(cand.data_ptr(), cfit.data_ptr())
+            _lib.check(getattr(L, "API_Initilize" + sfx)(P, rng_state.data_ptr(), ii, pi), "API_Initilize")
+            ev = getattr(L, "API_evaluateFitness" + sfx)
+            eargs = (d_sh.data_ptr(), d_rot.data_ptr(), d_sf.data_ptr(), None, None, None, n, D, 0.0, fid)
+            ev(pfit.data_ptr(), None, None, pop.data_ptr(), *eargs)
+            # the evaluation kernel alone
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            for _ in range(3):
+                ev(cfit.data_ptr(), None, None, pop.data_ptr(), *eargs)
+            reps = 20
+            e0.record(stream)
+            for _ in range(reps):
+                ev(cfit.data_ptr(), None, None, pop.data_ptr(), *eargs)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            eval_us = e0.elapsed_time(e1) * 1e3 / reps
+            if not f64:
+                h = torch.zeros(n, dtype=torch.float32).pin_memory()
+
+                def run(k):
+                    _lib.check(L.speo_de_run_f32(P, C, rng_state.data_ptr(), ii, d_info.data_ptr(), best.data_ptr(),
+                                                 pi, d_sh.data_ptr(), d_rot.data_ptr(), d_sf.data_ptr(), k,
+                                                 h.data_ptr(), 0, stream.cuda_stream), "speo_de_run_f32")
+                    stream.synchronize()
+                k = gens
+            else:
+                def run(k):
+                    for _ in range(k):
+                        L.API_DE_GenerateNewPopulation(C, P, best.data_ptr(), ii, d_info.data_ptr(),
+                                                       rng_state.data_ptr(), pi)
+                        ev(cfit.data_ptr(), None, None, cand.data_ptr(), *eargs)
+                        L.API_DE_SelectSurvival(P, C, ii, pi)
+                    stream.synchronize()
+                k = gens64
+            run(10)
+            t0 = time.perf_counter()
+            run(k)
+            dt_s = time.perf_counter() - t0
+            _lib.check(L.API_CheckCUDAError(), "published")
+            v = n * k / dt_s
+            rec["fp64" if f64 else "fp32"] = {
+                "evals_per_s": v, "us_per_gen": dt_s / k * 1e6, "eval_kernel_us": eval_us,
+                "vs_published_per_gpu": v / (PUBLISHED_2GPU_MEVALS[fid] * 1e6),
+                "best_error": float(pfit.min())}
+        out["functions"][str(fid)] = rec
+    L.speo_set_stream(None)
+    out["published_per_gpu_mevals"] = PUBLISHED_2GPU_MEVALS
+    return out
+
+
 def cpu_workload_sample(sample_s: float, threads: int):
     """FP64 island loop of the oracle port on the host cores: (evals/s, gens done)."""
     import speo_oracle
@@ -770,6 +868,8 @@ def main() -> None:
     ap.add_argument("--c4-only", action="store_true", help="only the config 4 section")
     ap.add_argument("--mlp-case", action="store_true", help="only the surrogate network's kernels at config-4 shapes")
     ap.add_argument("--e2e-only", action="store_true", help="only the end-to-end drop-in measurement")
+    ap.add_argument("--published-only", action="store_true",
+                    help="only the reference's published configuration (F23-F30, D=100, 4096 rows)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.e2e_only:
@@ -778,6 +878,13 @@ def main() -> None:
 
         torch.cuda.set_device(0)
         print(json.dumps({"e2e": bench_e2e(_lib.load(), "cuda:0", torch, args)}))
+        return
+    if args.published_only:
+        import torch
+        from speo_gb300 import _lib
+
+        torch.cuda.set_device(0)
+        print(json.dumps({"published_config": bench_published(_lib.load(), "cuda:0", torch)}))
         return
     if args.mlp_case:
         import torch

@@ -210,8 +210,34 @@ __device__ __forceinline__ double obj_term(int func_id, double z)
 // cigar :499-516, discus :518-531, Rosenbrock :552-567, Ackley :590-613, Weierstrass :615-644,
 // Griewank :646-666, Rastrigin :668-683, Schwefel :705-737, Katsuura :739-763, Griewank-Rosenbrock
 // :842-868, expanded Scaffer F6 :870-905, HappyCat :907-929, HGBat :931-953, sphere :462-478.
-// Weierstrass and Katsuura terms are evaluated in FP64 in both precisions (their high harmonics
-// amplify the argument by up to 3^20 and 2^32).
+// Weierstrass and Katsuura reduce their high harmonics (arguments amplified by up to 3^20 and
+// 2^32) exactly: in integer arithmetic (FP32) or in FP64.
+// Weierstrass' inner sum for a binary32 z: sum_{k=0}^{20} 0.5^k cos(2 pi 3^k (z + 1/2)) =
+// -sum_k 0.5^k cos(2 pi frac(3^k |z|)) (3^k is odd and cos is even). frac(3^k |z|) is exact:
+// |z| = m 2^e with m < 2^24, and 3^k m < 2^56 is an exact 64-bit product whose bits below the
+// binary point are the fraction; only the cosine of the reduced argument is rounded.
+__device__ __forceinline__ float weierstrass_sum_f32(float z)
+{
+    const float az = fabsf(z);
+    if (!(az < __int_as_float(0x7f800000))) return z - z;  // inf / NaN -> NaN
+    if (az == 0.f) return -(2.f - 9.5367431640625e-07f);
+    int e;
+    const float mf = frexpf(az, &e);                              // az = mf 2^e, mf in [0.5, 1)
+    unsigned long long p = (unsigned long long)(mf * 16777216.f); // exact, < 2^24
+    e -= 24;                                                      // az = p 2^e
+    if (e >= 0) return -(2.f - 9.5367431640625e-07f);             // an integer: every cosine is 1
+    const unsigned long long mask = -e >= 64 ? ~0ull : (1ull << -e) - 1ull;
+    float s = 0.f, ak = 1.f;
+#pragma unroll 1
+    for (int k = 0; k <= 20; ++k) {
+        const float fr = ldexpf(__ull2float_rn(p & mask), e);    // frac(3^k |z|)
+        s = __fmaf_rn(ak, cospif(2.f * fr), s);
+        ak *= 0.5f;
+        p *= 3ull;
+    }
+    return -s;
+}
+
 template <typename T> struct RowAcc {
     T s1 = T(0), s2 = T(0), p = T(1);
 };
@@ -237,16 +263,19 @@ __device__ __forceinline__ void row_push(RowAcc<T> &a, int f, int j, T z, T zn, 
         }
         break;
     case 5: a.s1 += z * z; a.s2 += cos2pi(z); break;
-    case 6: {
-        double s = 0.0, ak = 1.0, bk = 1.0;
-        for (int k = 0; k <= 20; ++k) {
-            s += ak * cospi(2.0 * bk * ((double)z + 0.5));
-            ak *= 0.5;
-            bk *= 3.0;
+    case 6:
+        if constexpr (sizeof(T) == 4) {
+            a.s1 += weierstrass_sum_f32(z);
+        } else {
+            double s = 0.0, ak = 1.0, bk = 1.0;
+            for (int k = 0; k <= 20; ++k) {
+                s += ak * cospi(2.0 * bk * ((double)z + 0.5));
+                ak *= 0.5;
+                bk *= 3.0;
+            }
+            a.s1 += (T)s;
         }
-        a.s1 += (T)s;
         break;
-    }
     case 7: a.s1 += z * z; a.p *= cos(z / sqrt(T(j + 1))); break;
     case 10: case 11: {
         const T zi = z + T(4.209687462275036e+002);
@@ -265,16 +294,25 @@ __device__ __forceinline__ void row_push(RowAcc<T> &a, int f, int j, T z, T zn, 
         }
         break;
     }
-    case 12: {
-        double t = 0.0, p2 = 1.0;
-        for (int k = 1; k <= 32; ++k) {
-            p2 *= 2.0;
-            const double b = p2 * (double)z;
-            t += fabs(b - floor(b + 0.5)) / p2;
+    case 12:
+        if constexpr (sizeof(T) == 4) {
+            // 2^k z, its distance to the nearest integer and the division by 2^k are exact in binary32
+            float t = 0.f;
+            for (int k = 1; k <= 32; ++k) {
+                const float b = ldexpf(z, k);
+                t += ldexpf(fabsf(b - rintf(b)), -k);
+            }
+            a.p *= powf(1.f + (float)(j + 1) * t, 10.f / powf((float)D, 1.2f));
+        } else {
+            double t = 0.0, p2 = 1.0;
+            for (int k = 1; k <= 32; ++k) {
+                p2 *= 2.0;
+                const double b = p2 * (double)z;
+                t += fabs(b - floor(b + 0.5)) / p2;
+            }
+            a.p *= (T)pow(1.0 + (j + 1) * t, 10.0 / pow((double)D, 1.2));
         }
-        a.p *= (T)pow(1.0 + (j + 1) * t, 10.0 / pow((double)D, 1.2));
         break;
-    }
     case 13: case 14: {
         const T zz = z - T(1);
         a.s1 += zz * zz;

@@ -21,20 +21,20 @@ struct TileDesc {
     const int *shuf;      // 1-based shuffles (ids 17-22, 29, 30)
 };
 
-template <typename T>
+template <typename T, int TILE = kEvalTile>
 __device__ __forceinline__ TileDesc ref_tile(int t, const T *X, int ldx, int P, int D, int func, const T *shift,
                                              const T *rot, T *fit)
 {
     TileDesc d;
-    d.x = X + (size_t)t * kEvalTile * ldx;
+    d.x = X + (size_t)t * TILE * ldx;
     d.ldx = ldx;
-    d.count = min(kEvalTile, P - t * kEvalTile);
+    d.count = min(TILE, P - t * TILE);
     d.D = D;
     d.func = func;
     d.ld_rot = D;
     d.shift = shift;
     d.rot = rot;
-    d.fit = fit + (size_t)t * kEvalTile;
+    d.fit = fit + (size_t)t * TILE;
     d.shift_cs = d.rot_cs = d.shuf_cs = 0;
     d.shuf = nullptr;
     return d;
@@ -43,11 +43,11 @@ __device__ __forceinline__ TileDesc ref_tile(int t, const T *X, int ldx, int P, 
 // The reference's device layout of the multi-component data (CUDA_EA_library/CEC2014_CUDA.cc:
 // 160-281): component c's shift at c * np2, its M^T (np2 rows of D) at c * np2 * D, its shuffle
 // at c * np2, np2 = max(32, next power of two >= D).
-template <typename T>
+template <typename T, int TILE>
 __device__ __forceinline__ TileDesc ref_tile_multi(int t, const T *X, int ldx, int P, int D, int func,
                                                    const T *shift, const T *rot, const int *shuf, T *fit)
 {
-    TileDesc d = ref_tile<T>(t, X, ldx, P, D, func, shift, rot, fit);
+    TileDesc d = ref_tile<T, TILE>(t, X, ldx, P, D, func, shift, rot, fit);
     d.shift_cs = ldx;
     d.rot_cs = (long long)ldx * D;
     d.shuf_cs = ldx;
@@ -60,12 +60,12 @@ __device__ __forceinline__ TileDesc ref_tile_multi(int t, const T *X, int ldx, i
 // the component's body (a hybrid reads its rotated row back from the warp's own rows of Ys,
 // gathered through the shuffle) and keep the result per row in shared memory; then mix.
 constexpr int kMaxComp = 5;
-template <typename T, int Q>
+template <typename T, int Q, int RPW = kRowsPerWarp>
 __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, int *Ss, T *fbuf, T *sbuf,
                                              unsigned int *err)
 {
     constexpr int W = 32 * Q;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row0 = warp * kRowsPerWarp;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row0 = warp * RPW;
     const T *X = static_cast<const T *>(d.x);
     const int nc = func_components(d.func), D = d.D;
     const bool comp = func_composition(d.func);
@@ -74,7 +74,7 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, in
         const T *o = static_cast<const T *>(d.shift) + c * d.shift_cs;
         const T *rot = static_cast<const T *>(d.rot) + c * d.rot_cs;
         __syncthreads();  // previous component (or tile) done with Ys / Ss / Ms
-        for (int i = threadIdx.x; i < kEvalTile * W; i += blockDim.x) {
+        for (int i = threadIdx.x; i < 8 * RPW * W; i += blockDim.x) {
             const int r = i / W, k = i - r * W;
             Ys[i] = (r < d.count && k < D) ? X[(size_t)r * d.ldx + k] - o[k] : T(0);
         }
@@ -94,7 +94,7 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, in
         __syncthreads();
         if (comp) {
 #pragma unroll 1
-            for (int rr = 0; rr < kRowsPerWarp; ++rr) {
+            for (int rr = 0; rr < RPW; ++rr) {
                 T sq = T(0);
 #pragma unroll
                 for (int q = 0; q < Q; ++q) {
@@ -106,9 +106,9 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, in
             }
         }
         const bool rotated = h >= 0 || comp_piece(d.func, c).rotated;
-        T acc[kRowsPerWarp][Q];
+        T acc[RPW][Q];
 #pragma unroll
-        for (int rr = 0; rr < kRowsPerWarp; ++rr)
+        for (int rr = 0; rr < RPW; ++rr)
 #pragma unroll
             for (int q = 0; q < Q; ++q) acc[rr][q] = T(0);
         if (rotated) {
@@ -125,12 +125,12 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, in
         if (h >= 0) {
             __syncwarp();
 #pragma unroll
-            for (int rr = 0; rr < kRowsPerWarp; ++rr)
+            for (int rr = 0; rr < RPW; ++rr)
 #pragma unroll
                 for (int q = 0; q < Q; ++q) Ys[(row0 + rr) * W + lane + 32 * q] = acc[rr][q];
             __syncwarp();
 #pragma unroll 1
-            for (int rr = 0; rr < kRowsPerWarp; ++rr) {
+            for (int rr = 0; rr < RPW; ++rr) {
                 const T f = hybrid_row_warp<T>(Ys + (row0 + rr) * W, Ss, h, D, lane);
                 if (lane == 0) fbuf[(row0 + rr) * kMaxComp + c] = f;
             }
@@ -138,7 +138,7 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, in
             const CompPiece pc = comp_piece(d.func, c);
             const T scale = rate_of<T>(pc.fid), fs = func_fixed_shift<T>(pc.fid);
 #pragma unroll 1
-            for (int rr = 0; rr < kRowsPerWarp; ++rr) {
+            for (int rr = 0; rr < RPW; ++rr) {
                 ZRow<T, Q> z;
 #pragma unroll
                 for (int q = 0; q < Q; ++q) z.v[q] = acc[rr][q] * scale + fs;
@@ -151,7 +151,7 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, in
     if (lane == 0) {
         T *fit = static_cast<T *>(d.fit);
 #pragma unroll 1
-        for (int rr = 0; rr < kRowsPerWarp; ++rr) {
+        for (int rr = 0; rr < RPW; ++rr) {
             const int r = row0 + rr;
             if (r < d.count)
                 fit[r] = comp ? comp_combine<T>(d.func, D, fbuf + r * kMaxComp, sbuf + r * kMaxComp)
@@ -160,20 +160,21 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, in
     }
 }
 
-template <typename T, int Q>
+// Tiles of 8 * RPW rows (one warp per RPW rows, 256 threads).
+template <typename T, int Q, int RPW = kRowsPerWarp>
 constexpr size_t multi_smem_bytes()
 {
-    return sizeof(T) * ((size_t)(kEvalTile + kChunk) * 32 * Q + 2 * kEvalTile * kMaxComp) + sizeof(int) * 32 * Q;
+    return sizeof(T) * ((size_t)(8 * RPW + kChunk) * 32 * Q + 2 * 8 * RPW * kMaxComp) + sizeof(int) * 32 * Q;
 }
 
-template <typename T, int Q>
+template <typename T, int Q, int RPW = kRowsPerWarp>
 __device__ __forceinline__ void multi_smem(unsigned char *raw, T *&Ys, T *&Ms, T *&fbuf, T *&sbuf, int *&Ss)
 {
     Ys = reinterpret_cast<T *>(raw);
-    Ms = Ys + kEvalTile * 32 * Q;
+    Ms = Ys + 8 * RPW * 32 * Q;
     fbuf = Ms + kChunk * 32 * Q;
-    sbuf = fbuf + kEvalTile * kMaxComp;
-    Ss = reinterpret_cast<int *>(sbuf + kEvalTile * kMaxComp);
+    sbuf = fbuf + 8 * RPW * kMaxComp;
+    Ss = reinterpret_cast<int *>(sbuf + 8 * RPW * kMaxComp);
 }
 
 }  // namespace speo

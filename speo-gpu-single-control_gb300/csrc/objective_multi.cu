@@ -11,32 +11,45 @@ SPEO_DEFINE_DEVERR(speo_deverr_objective_multi)
 namespace speo {
 namespace {
 
-template <typename T, int Q>
+// Tiles of 8 * RPW rows: RPW = 2 while 64-row tiles would leave SMs idle (the reference's
+// islands of a few thousand rows), RPW = 8 above that.
+template <typename T, int Q, int RPW>
 __global__ void __launch_bounds__(256) k_eval_ref_multi(const T *X, int ldx, int P, int D, int func, const T *shift,
                                                         const T *rot, const int *shuf, T *fit)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *Ys, *Ms, *fbuf, *sbuf;
     int *Ss;
-    multi_smem<T, Q>(smem_raw, Ys, Ms, fbuf, sbuf, Ss);
-    const int tiles = (P + kEvalTile - 1) / kEvalTile;
+    multi_smem<T, Q, RPW>(smem_raw, Ys, Ms, fbuf, sbuf, Ss);
+    constexpr int kTile = 8 * RPW;
+    const int tiles = (P + kTile - 1) / kTile;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x)
-        eval_multi_tile<T, Q>(ref_tile_multi<T>(t, X, ldx, P, D, func, shift, rot, shuf, fit), Ys, Ms, Ss, fbuf,
-                              sbuf, &s_deverr);
+        eval_multi_tile<T, Q, RPW>(ref_tile_multi<T, kTile>(t, X, ldx, P, D, func, shift, rot, shuf, fit), Ys, Ms, Ss,
+                                   fbuf, sbuf, &s_deverr);
+}
+
+template <typename T, int Q, int RPW>
+int launch_ref_multi_rpw(const T *X, int ldx, int P, int D, int func, const T *shift, const T *rot, const int *shuf,
+                         T *fit, cudaStream_t st)
+{
+    constexpr size_t smem = multi_smem_bytes<T, Q, RPW>();
+    cudaError_t e =
+        cudaFuncSetAttribute(k_eval_ref_multi<T, Q, RPW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_eval_ref_multi)");
+    const int tiles = (P + 8 * RPW - 1) / (8 * RPW);
+    const int per_sm = (int)((200u * 1024u) / smem) < 2 ? 1 : 2;
+    const int grid = tiles < per_sm * sm_count() ? tiles : per_sm * sm_count();
+    k_eval_ref_multi<T, Q, RPW><<<grid, 256, smem, st>>>(X, ldx, P, D, func, shift, rot, shuf, fit);
+    return check_launch("k_eval_ref_multi");
 }
 
 template <typename T, int Q>
 int launch_ref_multi(const T *X, int ldx, int P, int D, int func, const T *shift, const T *rot, const int *shuf, T *fit,
                      cudaStream_t st)
 {
-    constexpr size_t smem = multi_smem_bytes<T, Q>();
-    cudaError_t e = cudaFuncSetAttribute(k_eval_ref_multi<T, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_eval_ref_multi)");
-    const int tiles = (P + kEvalTile - 1) / kEvalTile;
-    const int per_sm = sizeof(T) == 8 && Q == 8 ? 1 : 2;
-    const int grid = tiles < per_sm * sm_count() ? tiles : per_sm * sm_count();
-    k_eval_ref_multi<T, Q><<<grid, 256, smem, st>>>(X, ldx, P, D, func, shift, rot, shuf, fit);
-    return check_launch("k_eval_ref_multi");
+    if ((P + kEvalTile - 1) / kEvalTile < 2 * sm_count())
+        return launch_ref_multi_rpw<T, Q, 2>(X, ldx, P, D, func, shift, rot, shuf, fit, st);
+    return launch_ref_multi_rpw<T, Q, kRowsPerWarp>(X, ldx, P, D, func, shift, rot, shuf, fit, st);
 }
 
 }  // namespace

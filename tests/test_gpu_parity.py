@@ -316,10 +316,12 @@ def test_evaluate_tc_flags_functions_it_does_not_implement(lib, cuda):
 # FP32 tolerances: the hybrids sum groups of the bodies above (Schwefel, Weierstrass and Katsuura
 # groups carry their own FP32 error), and the compositions mix components whose FP32 errors are
 # those of their bodies, rescaled; the FP32 mixing weights come from logarithms (relative error
-# ~|l| 2^-24 for |l| up to ~200).
+# ~|l| 2^-24 for |l| up to ~200). Measured on GB300 over D = 10-100 and points at, near and far
+# from every component's optimum: relative error <= 1e-5 above 5e-2; the absolute floor covers
+# the unrotated Schwefel component of 24 (418.98 D - sum cancels in FP32 near its optimum).
 MULTI_FUNCS = list(range(17, 31))
-TOL32_MULTI = (2e-3, 5e-2)
-TOL64_MULTI = (1e-9, 1e-8)
+TOL32_MULTI = (2e-5, 5e-2)
+TOL64_MULTI = (1e-11, 1e-8)
 
 
 def _multi_points(rng, o, P, D):
