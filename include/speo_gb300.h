@@ -321,6 +321,67 @@ SPEO_API int speo_ring_migrate(const speo_segment *d_segs, int n_segs, int k, fl
 SPEO_API int speo_ring_migrate_noalloc(const speo_segment *d_segs, int n_segs, int k, float *pop,
                                        float *fit, int max_ld, void *stream);
 
+/* ---- Archipelago migration policies (src/migrate.cc:34-186, src/buffer_manage.cc:36-313) ----
+ * The reference runs one island per MPI rank and migrates through host buffers; here n_islands
+ * islands share one device: island i is rows [i*island_size, (i+1)*island_size) of pop / fit
+ * (ld floats apart), with its own sub-island permutation d_perm + i*island_size (island-local
+ * rows, the drop-in permutated_index) and sub-island count d_subisland_num[i]. Per generation g
+ * the caller runs its DE generation on every island, then speo_migrate_out when g % interval
+ * == 0, then speo_migrate_in (the order of IslandEA::Execute, src/island_EA.cc:86-105).
+ *  - destinations (dynamicConnect, migrate.cc:34-44): when an island's list is used up, every
+ *    other island joins it with probability migration_rate, in island order;
+ *  - migrate_in (SendEmigrations + CheckAndRecvEmigrations, migrate.cc:71-144): every island
+ *    whose list is not used up sends migration_size distinct random rows (with fitness) to the
+ *    head of its list and drops that head; each island takes the messages sent to it this
+ *    generation in source-island order into its immigrant buffer (buffer_policy);
+ *  - migrate_out (UpdateDestination + UpdatePopulation + RegroupIslands, migrate.cc:46-69,
+ *    147-186): refill used-up lists, take the buffer's selection (OnlineCluster: every entry
+ *    updated since the last selection; the others: up to migration_size) into distinct random
+ *    rows, then regroup (regroup_option).
+ * Draws (Philox-4x32-10 keyed by `seed`, in place of the reference's host rand() and partial
+ * Fisher-Yates, random.cc:14-53), for island s at generation g:
+ *   destination t joins:  u01(word 0 of philox({t, s, g, 7})) < migration_rate
+ *   emigrant rows:        perm_{P}(philox({s, g, 0, 8}))[0 .. migration_size)
+ *   import rows:          perm_{P}(philox({s, g, 0, 9}))[0 .. count)
+ *   regroup size index:   (word 0 of philox({s, g, 0, 10}) * (max_index + 1)) >> 32
+ *   regroup permutation:  perm_{P}(philox({s, g, 1, 10}))
+ *   RandomSelect draw q:  (word 0 of philox({q, s, g, 11}) * buffer size) >> 32
+ * perm_n(k)[x] is a 4-round Feistel network on 2h bits (h = max(1, ceil(ceil(log2 n) / 2))),
+ * round r: (L, R) <- (R, L ^ (fmix32(R * 0x9E3779B1 ^ k_r) & (2^h - 1))), fmix32 the MurmurHash3
+ * finaliser, walked until the value is below n. MPI's asynchronous delivery becomes delivery
+ * in the generation the message is sent. */
+#define SPEO_BUFFER_ONLINE_CLUSTER 0  /* OnlineCluster (buffer_manage.cc:36-131), the reference driver's buffer */
+#define SPEO_BUFFER_BEST           1  /* BestSelect (:169-212): largest fitness first, as the reference's */
+#define SPEO_BUFFER_RANDOM         2  /* RandomSelect (:214-245) */
+#define SPEO_BUFFER_FIFO           3  /* FIFO (:247-278) */
+#define SPEO_BUFFER_LIFO           4  /* LIFO (:280-313) */
+#define SPEO_REGROUP_STATIC_ORDERED  0  /* static_and_ordered: no regroup */
+#define SPEO_REGROUP_STATIC_RANDOM   1  /* new random permutation */
+#define SPEO_REGROUP_DYNAMIC_ORDERED 2  /* new sub-island size 4 << U{0..log2(P/4)} */
+#define SPEO_REGROUP_DYNAMIC_RANDOM  3  /* both (the reference's published runs) */
+#define SPEO_ARCHIPELAGO_MAX_CAPACITY 64
+typedef struct {
+    int32_t  n_islands;        /* >= 1 */
+    int32_t  island_size;      /* rows per island, >= 4, < 2^30 */
+    int32_t  dim, ld;          /* 1 <= dim <= SPEO_MAX_DIM, ld >= dim */
+    int32_t  migration_size;   /* rows per message, 1..island_size */
+    int32_t  buffer_capacity;  /* 1..SPEO_ARCHIPELAGO_MAX_CAPACITY, <= island_size */
+    int32_t  buffer_policy;    /* SPEO_BUFFER_* */
+    int32_t  regroup_option;   /* SPEO_REGROUP_* */
+    float    migration_rate;   /* [0, 1] */
+    int32_t  reserved;         /* 0 */
+    uint64_t seed;             /* Philox key of every draw */
+} speo_archipelago;
+/* Device bytes of the migration state (destination lists and immigrant buffers of every island). */
+SPEO_API size_t speo_archipelago_state_bytes(const speo_archipelago *a);
+/* Empty lists and buffers; d_perm = identity per island; d_subisland_num[i] = subisland_num. */
+SPEO_API int speo_archipelago_init(const speo_archipelago *a, void *d_state, int32_t *d_perm,
+                                   int32_t *d_subisland_num, int subisland_num, void *stream);
+SPEO_API int speo_migrate_out(const speo_archipelago *a, void *d_state, float *pop, float *fit, int32_t *d_perm,
+                              int32_t *d_subisland_num, uint32_t generation, void *stream);
+SPEO_API int speo_migrate_in(const speo_archipelago *a, void *d_state, const float *pop, const float *fit,
+                             uint32_t generation, void *stream);
+
 /* ---- Online MLP surrogate (no counterpart in the reference) -------------------------------
  * din -> hidden -> hidden -> 1 with ReLU, FP32 parameters in one flat vector
  * (W1[h][din], b1[h], W2[h][h], b2[h], w3[h], b3), inputs scaled by in_scale, trained by Adam

@@ -490,6 +490,240 @@ void speo_oracle_evaluate_rows_multi(int fid, const float *x, int n, int ld, int
     free(Md);
 }
 
+/* ---- archipelago migration policies ------------------------------------------------------
+ * The reference's migration (src/migrate.cc:34-186) and immigrant buffers
+ * (src/buffer_manage.cc:36-313) for n islands held together, with this library's draws: Philox
+ * tags 7-11 and keyed Feistel permutations in place of rand() and the partial Fisher-Yates of
+ * random.cc:29-53. Same state layout as the library, so states compare byte for byte:
+ * ints per island [0] list length, [1] head, [2] buffer size, [3] 0, list[N], member[C], flag[C],
+ * order[C] (padded to 4); floats per island entry[C][D+1], centre[C][D] (padded to 4). */
+static int arch_istride(const speo_oracle_arch *a) { return (4 + a->n_islands + 3 * a->buffer_capacity + 3) / 4 * 4; }
+static int arch_fstride(const speo_oracle_arch *a) { return (a->buffer_capacity * (2 * a->dim + 1) + 3) / 4 * 4; }
+
+size_t speo_oracle_arch_state_bytes(const speo_oracle_arch *a)
+{
+    return 4 * (size_t)a->n_islands * (size_t)(arch_istride(a) + arch_fstride(a));
+}
+
+typedef struct { int *ints; float *flts; int N, C, D, is, fs; } arch_view;
+static arch_view arch_of(const speo_oracle_arch *a, uint8_t *state)
+{
+    arch_view v;
+    v.N = a->n_islands; v.C = a->buffer_capacity; v.D = a->dim;
+    v.is = arch_istride(a); v.fs = arch_fstride(a);
+    v.ints = (int *)state;
+    v.flts = (float *)(v.ints + (size_t)v.N * v.is);
+    return v;
+}
+static int *a_hdr(const arch_view *v, int i) { return v->ints + (size_t)i * v->is; }
+static int *a_list(const arch_view *v, int i) { return a_hdr(v, i) + 4; }
+static int *a_member(const arch_view *v, int i) { return a_hdr(v, i) + 4 + v->N; }
+static int *a_flag(const arch_view *v, int i) { return a_member(v, i) + v->C; }
+static int *a_order(const arch_view *v, int i) { return a_flag(v, i) + v->C; }
+static float *a_entry(const arch_view *v, int i, int c) { return v->flts + (size_t)i * v->fs + (size_t)c * (v->D + 1); }
+static float *a_centre(const arch_view *v, int i, int c)
+{
+    return v->flts + (size_t)i * v->fs + (size_t)v->C * (v->D + 1) + (size_t)c * v->D;
+}
+
+static uint32_t fmix32(uint32_t v)
+{
+    v ^= v >> 16; v *= 0x85EBCA6Bu; v ^= v >> 13; v *= 0xC2B2AE35u; v ^= v >> 16;
+    return v;
+}
+
+uint32_t speo_oracle_fperm(uint32_t n, const uint32_t key[4], uint32_t x)
+{
+    uint32_t bits = 0;
+    while (bits < 30 && (1u << bits) < n) ++bits;
+    uint32_t h = (bits + 1) / 2;
+    if (h == 0) h = 1;
+    const uint32_t mask = (1u << h) - 1u;
+    for (uint64_t it = 0; it < (1ull << (2 * h)); ++it) {
+        uint32_t L = x >> h, R = x & mask;
+        for (int r = 0; r < 4; ++r) {
+            const uint32_t t = L ^ (fmix32(R * 0x9E3779B1u ^ key[r]) & mask);
+            L = R;
+            R = t;
+        }
+        x = (L << h) | R;
+        if (x < n) return x;
+    }
+    return 0u;
+}
+
+static void arch_draw(const speo_oracle_arch *a, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t tag, uint32_t out[4])
+{
+    const uint32_t ctr[4] = {c0, c1, c2, tag};
+    const uint32_t key[2] = {(uint32_t)a->seed, (uint32_t)(a->seed >> 32)};
+    speo_oracle_philox(ctr, key, out);
+}
+static uint32_t below(uint32_t w, uint32_t n) { return (uint32_t)(((uint64_t)w * n) >> 32); }
+
+/* vector::erase(begin + pos) on the live order, the freed slot kept behind it */
+static void order_erase(int *order, int size, int pos)
+{
+    const int slot = order[pos];
+    for (int i = pos; i < size - 1; ++i) order[i] = order[i + 1];
+    order[size - 1] = slot;
+}
+
+void speo_oracle_arch_init(const speo_oracle_arch *a, uint8_t *state, int *perm, int *subisland_num, int nsub)
+{
+    arch_view v = arch_of(a, state);
+    memset(state, 0, speo_oracle_arch_state_bytes(a));
+    for (int i = 0; i < v.N; ++i) {
+        for (int c = 0; c < v.C; ++c) a_order(&v, i)[c] = c;
+        for (int r = 0; r < a->island_size; ++r) perm[(size_t)i * a->island_size + r] = r;
+        subisland_num[i] = nsub;
+    }
+}
+
+void speo_oracle_migrate_out(const speo_oracle_arch *a, uint8_t *state, float *pop, float *fit, int *perm,
+                             int *subisland_num, uint32_t g)
+{
+    arch_view v = arch_of(a, state);
+    const int P = a->island_size, D = a->dim;
+    for (int s = 0; s < v.N; ++s) {
+        int *h = a_hdr(&v, s);
+        /* UpdateDestination (migrate.cc:34-44): each other island with probability migration_rate */
+        if (h[1] >= h[0]) {
+            int cnt = 0;
+            for (int t = 0; t < v.N; ++t) {
+                uint32_t w[4];
+                if (t == s) continue;
+                arch_draw(a, (uint32_t)t, (uint32_t)s, g, 7u, w);
+                if (speo_oracle_u01(w[0]) < a->migration_rate) a_list(&v, s)[cnt++] = t;
+            }
+            h[0] = cnt;
+            h[1] = 0;
+        }
+        /* UpdatePopulation (migrate.cc:46-62): SelectFromBuffer, then distinct random rows */
+        int sel[64], n = 0, size = h[2];
+        int *order = a_order(&v, s), *flag = a_flag(&v, s);
+        if (a->buffer_policy == 0) {            /* OnlineCluster::SelectFromBuffer :105-117 */
+            for (int c = 0; c < size; ++c)
+                if (flag[c]) { sel[n++] = c; flag[c] = 0; }
+        } else {
+            for (int q = 0; q < a->migration_size && size > 0; ++q) {
+                int pos = 0;
+                if (a->buffer_policy == 1) {    /* BestSelect::FindBestBufferMember :178-191 */
+                    float bf = a_entry(&v, s, order[0])[D];
+                    for (int i = 1; i < size; ++i)
+                        if (bf < a_entry(&v, s, order[i])[D]) { bf = a_entry(&v, s, order[i])[D]; pos = i; }
+                } else if (a->buffer_policy == 2) { /* RandomSelect :235-245 */
+                    uint32_t w[4];
+                    arch_draw(a, (uint32_t)q, (uint32_t)s, g, 11u, w);
+                    pos = (int)below(w[0], (uint32_t)size);
+                } else if (a->buffer_policy == 4) { /* LIFO :303-313: the newest */
+                    pos = size - 1;
+                }                                   /* FIFO :268-278: the oldest */
+                sel[n++] = order[pos];
+                order_erase(order, size, pos);
+                --size;
+            }
+        }
+        h[2] = size;
+        if (n > 0) {
+            uint32_t key[4];
+            arch_draw(a, (uint32_t)s, g, 0u, 9u, key);
+            for (int q = 0; q < n; ++q) {
+                const size_t row = (size_t)s * P + speo_oracle_fperm((uint32_t)P, key, (uint32_t)q);
+                const float *e = a_entry(&v, s, sel[q]);
+                for (int j = 0; j < D; ++j) pop[row * a->ld + j] = e[j];
+                fit[row] = e[D];
+            }
+        }
+        /* RegroupIslands (migrate.cc:147-186) */
+        const int opt = a->regroup_option;
+        if (opt == 2 || opt == 3) {
+            int max_index = 0, q = P / 4;
+            uint32_t w[4];
+            while (q > 1) { q /= 2; max_index++; }
+            arch_draw(a, (uint32_t)s, g, 0u, 10u, w);
+            subisland_num[s] = P / (4 << below(w[0], (uint32_t)(max_index + 1)));
+        }
+        if (opt == 1 || opt == 3) {
+            uint32_t key[4];
+            arch_draw(a, (uint32_t)s, g, 1u, 10u, key);
+            for (int r = 0; r < P; ++r) perm[(size_t)s * P + r] = (int)speo_oracle_fperm((uint32_t)P, key, (uint32_t)r);
+        }
+    }
+}
+
+void speo_oracle_migrate_in(const speo_oracle_arch *a, uint8_t *state, const float *pop, const float *fit, uint32_t g)
+{
+    arch_view v = arch_of(a, state);
+    const int P = a->island_size, D = a->dim, C = v.C;
+    for (int d = 0; d < v.N; ++d) {
+        int *h = a_hdr(&v, d);
+        for (int src = 0; src < v.N; ++src) {
+            const int *hs = a_hdr(&v, src);
+            if (hs[1] >= hs[0] || a_list(&v, src)[hs[1]] != d) continue;
+            /* SendEmigrations (migrate.cc:105-136): migration_size distinct random rows */
+            uint32_t key[4];
+            arch_draw(a, (uint32_t)src, g, 0u, 8u, key);
+            for (int q = 0; q < a->migration_size; ++q) {
+                const size_t row = (size_t)src * P + speo_oracle_fperm((uint32_t)P, key, (uint32_t)q);
+                const float *x = pop + row * a->ld;
+                const float fx = fit[row];
+                if (a->buffer_policy == 0) {    /* OnlineCluster::UpdateBuffer :119-131 */
+                    const int size = h[2];
+                    if (size < C) {             /* CreatCluster :51-58 */
+                        memcpy(a_entry(&v, d, size), x, sizeof(float) * D);
+                        a_entry(&v, d, size)[D] = fx;
+                        memcpy(a_centre(&v, d, size), x, sizeof(float) * D);
+                        a_member(&v, d)[size] = 1;
+                        a_flag(&v, d)[size] = 1;
+                        h[2] = size + 1;
+                        continue;
+                    }
+                    int best = 0;               /* FindNearestIndividual :134-150, CalDistance :38-49 */
+                    float bv = 0.f;
+                    for (int c = 0; c < C; ++c) {
+                        const float *cc = a_centre(&v, d, c);
+                        float acc = 0.f;
+                        for (int j = 0; j < D; ++j) {
+                            const float df = x[j] - cc[j];
+                            acc = acc + df * df;
+                        }
+                        const float dist = sqrtf(acc);
+                        if (c == 0 || bv > dist) { bv = dist; best = c; }
+                    }
+                    /* ReplaceMemberToCluster :60-76 */
+                    const int m = a_member(&v, d)[best];
+                    float *cc = a_centre(&v, d, best);
+                    for (int j = 0; j < D; ++j) {
+                        const float t = (float)m * cc[j] + x[j];
+                        cc[j] = (float)((double)t / ((double)m + 1.0));
+                    }
+                    memcpy(a_entry(&v, d, best), x, sizeof(float) * D);
+                    a_entry(&v, d, best)[D] = fx;
+                    a_member(&v, d)[best] = m + 1;
+                    a_flag(&v, d)[best] = 1;
+                } else {                        /* push_back, then erase(begin) past capacity */
+                    int *order = a_order(&v, d);
+                    const int size = h[2];
+                    int slot;
+                    if (size < C) {
+                        slot = order[size];
+                        h[2] = size + 1;
+                    } else {
+                        slot = order[0];
+                        order_erase(order, size, 0);
+                    }
+                    memcpy(a_entry(&v, d, slot), x, sizeof(float) * D);
+                    a_entry(&v, d, slot)[D] = fx;
+                }
+            }
+        }
+    }
+    for (int s = 0; s < v.N; ++s) {
+        int *h = a_hdr(&v, s);
+        if (h[1] < h[0]) h[1] += 1;
+    }
+}
+
 /* ---- fused generation (this library's extended semantics) ------------------------------ */
 static int seg_best_row(const float *fit, int64_t row0, int P)
 {

@@ -11,6 +11,7 @@
  */
 #ifndef SPEO_ORACLE_H
 #define SPEO_ORACLE_H
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -110,6 +111,22 @@ double speo_oracle_objective_multi_f64(int fid, const double *x, const double *o
                                        int nx);
 void speo_oracle_evaluate_rows_multi(int fid, const float *x, int n, int ld, int dim, const float *o,
                                      const float *M, const int *S, double *f_out);
+
+/* Archipelago migration policies: the reference's migrate.cc / buffer_manage.cc for n islands
+ * held together, with this library's draws (layout of speo_archipelago in speo_gb300.h). */
+typedef struct {
+    int n_islands, island_size, dim, ld, migration_size, buffer_capacity, buffer_policy, regroup_option;
+    float migration_rate;
+    int reserved;
+    uint64_t seed;
+} speo_oracle_arch;
+size_t speo_oracle_arch_state_bytes(const speo_oracle_arch *a);
+uint32_t speo_oracle_fperm(uint32_t n, const uint32_t key[4], uint32_t x);
+void speo_oracle_arch_init(const speo_oracle_arch *a, uint8_t *state, int *perm, int *subisland_num, int nsub);
+void speo_oracle_migrate_out(const speo_oracle_arch *a, uint8_t *state, float *pop, float *fit, int *perm,
+                             int *subisland_num, uint32_t g);
+void speo_oracle_migrate_in(const speo_oracle_arch *a, uint8_t *state, const float *pop, const float *fit,
+                            uint32_t g);
 
 /* ---- Extended (this library's) semantics ------------------------------------------- */
 /* Fused generation over segments of identity-permuted rows: what speo_generation computes.

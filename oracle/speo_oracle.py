@@ -52,6 +52,13 @@ def lib() -> ctypes.CDLL:
         L.speo_oracle_objective_multi_f64.restype = c_double
         L.speo_oracle_evaluate_rows_multi.argtypes = [c_int, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p,
                                                       c_void_p, c_void_p]
+        L.speo_oracle_arch_state_bytes.argtypes = [c_void_p]
+        L.speo_oracle_arch_state_bytes.restype = ctypes.c_size_t
+        L.speo_oracle_fperm.argtypes = [c_uint32, c_void_p, c_uint32]
+        L.speo_oracle_fperm.restype = c_uint32
+        L.speo_oracle_arch_init.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int]
+        L.speo_oracle_migrate_out.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_uint32]
+        L.speo_oracle_migrate_in.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_uint32]
         L.speo_oracle_generation_f32.argtypes = [c_int] + [c_void_p] * 13 + [c_uint32] + [c_void_p] * 7
         L.speo_oracle_ring_migrate.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
                                                c_void_p, c_void_p]
@@ -185,6 +192,40 @@ def evaluate_rows_multi(func_id, X, dim, o, M, S=None) -> np.ndarray:
                                           _p(np.ascontiguousarray(o, dtype=np.float32)),
                                           _p(np.ascontiguousarray(M, dtype=np.float32)), _p(S), _p(out))
     return out
+
+
+class Archipelago:
+    """Host restatement of the archipelago migration ops on numpy arrays (same state layout as the
+    library). `desc` is a ctypes speo_archipelago (speo_gb300._lib.Archipelago)."""
+
+    def __init__(self, desc, subisland_num: int):
+        self.desc = desc
+        n = lib().speo_oracle_arch_state_bytes(ctypes.addressof(desc))
+        self.state = np.zeros(n, dtype=np.uint8)
+        self.perm = np.zeros(desc.n_islands * desc.island_size, dtype=np.int32)
+        self.subisland_num = np.zeros(desc.n_islands, dtype=np.int32)
+        lib().speo_oracle_arch_init(ctypes.addressof(desc), _p(self.state), _p(self.perm), _p(self.subisland_num),
+                                    subisland_num)
+
+    def migrate_out(self, pop, fit, gen):
+        lib().speo_oracle_migrate_out(ctypes.addressof(self.desc), _p(self.state), _p(pop), _p(fit), _p(self.perm),
+                                      _p(self.subisland_num), gen)
+
+    def migrate_in(self, pop, fit, gen):
+        lib().speo_oracle_migrate_in(ctypes.addressof(self.desc), _p(self.state), _p(pop), _p(fit), gen)
+
+    def view(self):
+        """(ints, floats) per island: ints (N, istride), floats (N, fstride)."""
+        d = self.desc
+        istride = (4 + d.n_islands + 3 * d.buffer_capacity + 3) // 4 * 4
+        ints = self.state[: 4 * d.n_islands * istride].view(np.int32).reshape(d.n_islands, istride)
+        flts = self.state[4 * d.n_islands * istride:].view(np.float32).reshape(d.n_islands, -1)
+        return ints, flts
+
+
+def fperm(n: int, key, x: int) -> int:
+    k = np.asarray(key, dtype=np.uint32)
+    return lib().speo_oracle_fperm(n, _p(k), x)
 
 
 def generation(segs: list[dict], gen: int, pop_in, fit_in, trial_fit=None):

@@ -41,6 +41,19 @@ class Segment(ctypes.Structure):
     ]
 
 
+class Archipelago(ctypes.Structure):
+    """speo_archipelago: islands of one device and the reference's migration parameters."""
+    _fields_ = [
+        ("n_islands", c_int32), ("island_size", c_int32), ("dim", c_int32), ("ld", c_int32),
+        ("migration_size", c_int32), ("buffer_capacity", c_int32), ("buffer_policy", c_int32),
+        ("regroup_option", c_int32), ("migration_rate", c_float), ("reserved", c_int32), ("seed", c_uint64),
+    ]
+
+
+BUFFER_ONLINE_CLUSTER, BUFFER_BEST, BUFFER_RANDOM, BUFFER_FIFO, BUFFER_LIFO = range(5)
+REGROUP_STATIC_ORDERED, REGROUP_STATIC_RANDOM, REGROUP_DYNAMIC_ORDERED, REGROUP_DYNAMIC_RANDOM = range(4)
+
+
 class WorkItem(ctypes.Structure):
     """speo_work_item."""
     _fields_ = [("segment", c_int32), ("first", c_int32), ("count", c_int32), ("pad", c_int32)]
@@ -113,6 +126,10 @@ SIGNATURES: dict[str, tuple] = {
                                          c_void_p, c_void_p, c_int, c_int, c_void_p]),
     "speo_ring_migrate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "speo_ring_migrate_noalloc": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p]),
+    "speo_archipelago_state_bytes": (ctypes.c_size_t, [c_void_p]),
+    "speo_archipelago_init": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
+    "speo_migrate_out": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p]),
+    "speo_migrate_in": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p]),
     "speo_surrogate_create": (c_int, [c_void_p, c_int, c_int, ctypes.c_longlong, c_int, c_float, c_float, c_uint64]),
     "speo_surrogate_destroy": (c_int, [c_void_p]),
     "speo_surrogate_params": (c_int, [c_void_p, c_void_p, c_void_p, POINTER(c_int)]),

@@ -132,9 +132,11 @@ def test_struct_layouts_match_c(tmp_path):
 #include <stddef.h>
 #include "speo_gb300.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(speo_segment), offsetof(speo_segment, shift),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(speo_segment), offsetof(speo_segment, shift),
          offsetof(speo_segment, seed), sizeof(speo_work_item), sizeof(speo_problem_info_f64),
-         offsetof(speo_problem_info_f64, max_bound), sizeof(speo_de_info_f64), sizeof(speo_island_info));
+         offsetof(speo_problem_info_f64, max_bound), sizeof(speo_de_info_f64), sizeof(speo_island_info),
+         offsetof(speo_segment, shuffle), sizeof(speo_archipelago), offsetof(speo_archipelago, migration_rate),
+         offsetof(speo_archipelago, seed));
   return 0; }
 '''
     build = tmp_path
@@ -144,7 +146,8 @@ int main(void) {
     vals = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     expect = [ctypes.sizeof(_lib.Segment), _lib.Segment.shift.offset, _lib.Segment.seed.offset,
               ctypes.sizeof(_lib.WorkItem), ctypes.sizeof(_lib.ProblemInfoF64), _lib.ProblemInfoF64.max_bound.offset,
-              ctypes.sizeof(_lib.DEInfoF64), ctypes.sizeof(_lib.IslandInfo)]
+              ctypes.sizeof(_lib.DEInfoF64), ctypes.sizeof(_lib.IslandInfo), _lib.Segment.shuffle.offset,
+              ctypes.sizeof(_lib.Archipelago), _lib.Archipelago.migration_rate.offset, _lib.Archipelago.seed.offset]
     assert vals == expect
 
 
