@@ -73,6 +73,25 @@ def build_library(verbose: bool = False, jobs: int | None = None) -> Path:
     return LIB_PATH
 
 
+CLI_SRC = PKG_ROOT / "app" / "speo_gpu.cc"
+CLI_PATH = LIB_DIR / "speo_gpu"
+
+
+def build_cli() -> Path:
+    """Builds lib/speo_gpu, the reference driver's command line (src/main.cc flags, Results/SPEO_GPU.csv)
+    over libspeo_gb300.so; host C++ compiled and linked by nvcc."""
+    lib = build_library()
+    deps = [CLI_SRC, lib, INCLUDE / "speo_gb300.h"]
+    if CLI_PATH.exists() and CLI_PATH.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return CLI_PATH
+    cmd = [nvcc(), "-O2", "-std=c++17", "-I", str(INCLUDE), str(CLI_SRC), "-o", str(CLI_PATH), "-L", str(LIB_DIR),
+           "-lspeo_gb300", "-Xlinker", "-rpath,$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"speo_gpu build failed:\n{res.stdout}\n{res.stderr}")
+    return CLI_PATH
+
+
 def build_oracle() -> Path:
     """Builds oracle/lib/libspeo_oracle.so (test infrastructure) with make."""
     res = subprocess.run(["make", "-s", "-C", str(REPO_ROOT / "oracle")], capture_output=True, text=True)
