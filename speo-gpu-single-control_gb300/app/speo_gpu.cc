@@ -109,7 +109,8 @@ int set_parameters(Params &p, int argc, char **argv)
     }
     if (p.dim < 1 || p.dim > SPEO_MAX_DIM) return usage("-dim out of range");
     if (p.GPU_num < 1 || p.island_size < 4 || p.interval < 1 || p.max_base_FEs < 1) return usage("bad sizes");
-    if (p.subisland_num < 1 || p.island_size % p.subisland_num) return usage("island_size must split into sub-islands");
+    if (p.subisland_num < 1 || p.island_size % p.subisland_num || p.island_size / p.subisland_num < 4)
+        return usage("island_size must split into sub-islands of at least 4 rows (MIN_SUBISLAND_SIZE)");
     if (p.migration_size < 1 || p.migration_size > p.island_size) return usage("bad -migration_size");
     if (p.buffer_capacity < 1 || p.buffer_capacity > SPEO_ARCHIPELAGO_MAX_CAPACITY ||
         p.buffer_capacity > p.island_size)

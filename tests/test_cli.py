@@ -25,7 +25,8 @@ def _cli():
 
 @pytest.mark.parametrize("args", [["-dim", "0"], ["-configure_EA", "sometimes"], ["-total_functions", "5"],
                                   ["-regroup_option", "shuffle"], ["-buffer_capacity", "65"], ["-dim"],
-                                  ["-island_size", "64", "-subisland_size", "128"]])
+                                  ["-island_size", "64", "-subisland_size", "128"],
+                                  ["-island_size", "64", "-subisland_size", "2"]])
 def test_cli_rejects_bad_flags_before_touching_the_gpu(tmp_path, args):
     res = subprocess.run([str(_cli()), *args], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert res.returncode == 2 and "speo_gpu:" in res.stderr
