@@ -70,8 +70,36 @@ __global__ void k_best(const T *fit, const int *perm, int S, int nsub, int *best
     if (lane == 0) best_id[s] = perm[s * S + bp];
 }
 
+// The same search for large sub-islands: one 512-thread block per sub-island. The (fitness,
+// position) minimum is order-independent, so the result equals the warp version's.
+template <typename T>
+__global__ void __launch_bounds__(512) k_best_block(const T *fit, const int *perm, int S, int *best_id)
+{
+    __shared__ T wf[16];
+    __shared__ int wp[16];
+    const int s = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T bf = T(INFINITY);
+    int bp = 0x7fffffff;
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+        const T f = rank_t(fit[perm[(size_t)s * S + i]]);
+        if (f < bf || (f == bf && i < bp)) { bf = f; bp = i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const T of = __shfl_xor_sync(0xffffffffu, bf, o);
+        const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+        if (of < bf || (of == bf && op < bp)) { bf = of; bp = op; }
+    }
+    if (lane == 0) { wf[warp] = bf; wp[warp] = bp; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            if (wf[w] < bf || (wf[w] == bf && wp[w] < bp)) { bf = wf[w]; bp = wp[w]; }
+        best_id[s] = perm[(size_t)s * S + bp];
+    }
+}
+
 // global_DE_GenerateNewPopulation (kernel_DE_CUDA.cu:172-289).
-// One warp owns ppw (4 .. 32) consecutive positions: lane l < ppw draws the donors and jrand of
+// One warp owns ppw (1 .. 32) consecutive positions: lane l < ppw draws the donors and jrand of
 // position l (Philox on those lanes at once). The warp's ppw x nch (row, 16-byte chunk) tasks are
 // then dealt to the lanes in order, task t = it * 32 + lane, so no lane idles whatever D is; each
 // task reads its row's draws from the drawing lane with shuffles. Two tasks in flight per lane.
@@ -267,13 +295,16 @@ int generate(Pop cand, Pop pop, int *d_best, speo_island_info ii, Info *d_info, 
     if (S < 2) return fail(SPEO_ERR_INVALID_ARG, "API_DE_GenerateNewPopulation: sub-island size %d < 2", S);
     const int ld = np2_of(pi.dim);
     cudaStream_t st = api_stream();
-    k_best<T><<<(ii.subisland_num + kWarps - 1) / kWarps, 32 * kWarps, 0, st>>>(
-        pop.fitness_value, ii.permutated_index, S, ii.subisland_num, d_best);
+    if (S >= 1024)
+        k_best_block<T><<<ii.subisland_num, 512, 0, st>>>(pop.fitness_value, ii.permutated_index, S, d_best);
+    else
+        k_best<T><<<(ii.subisland_num + kWarps - 1) / kWarps, 32 * kWarps, 0, st>>>(
+            pop.fitness_value, ii.permutated_index, S, ii.subisland_num, d_best);
     if (int e = check_launch("global_DE_FindBestIndividualInIsland")) return e;
     // 16-byte chunks cover D (np2 rows keep every chunk in bounds). Positions per warp: the
-    // largest of 32, 16, 8, 4 that still gives about 16 warps per SM.
+    // largest of 32, 16, 8, 4, 2, 1 that still gives about 16 warps per SM.
     int ppw = 32;
-    while (ppw > 4 && (long long)ii.island_size < (long long)ppw * 16 * sm_count()) ppw >>= 1;
+    while (ppw > 1 && (long long)ii.island_size < (long long)ppw * 16 * sm_count()) ppw >>= 1;
     const int grid = (ii.island_size + 8 * ppw - 1) / (8 * ppw);  // 8 warps per block
     const auto *inf = reinterpret_cast<const typename DeInfoT<T>::type *>(d_info);
     RngState *rs = reinterpret_cast<RngState *>(d_rng);

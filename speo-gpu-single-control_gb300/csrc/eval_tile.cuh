@@ -60,23 +60,98 @@ __device__ __forceinline__ TileDesc ref_tile_multi(int t, const T *X, int ldx, i
 // the component's body (a hybrid reads its rotated row back from the warp's own rows of Ys,
 // gathered through the shuffle) and keep the result per row in shared memory; then mix.
 constexpr int kMaxComp = 5;
-template <typename T, int Q, int RPW = kRowsPerWarp>
-__device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, int *Ss, T *fbuf, T *sbuf,
-                                             unsigned int *err)
+
+// Ampere-style asynchronous global -> shared copies (cp.async), element-sized.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *smem, const T *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// The chunks of M_c^T the tile consumes, in order: (component, first row) for every rotated
+// component, kChunk rows at a time. Returns false past the last one.
+__device__ __forceinline__ bool multi_next_chunk(int func, int D, int &c, int &kc)
+{
+    const int nc = func_components(func);
+    if (c >= 0 && kc + kChunk < D) {
+        kc += kChunk;
+        return true;
+    }
+    for (int n = c + 1; n < nc; ++n)
+        if (multi_hybrid(func, n) >= 0 || comp_piece(func, n).rotated) {
+            c = n;
+            kc = 0;
+            return true;
+        }
+    return false;
+}
+
+template <typename T, int Q>
+__device__ __forceinline__ void issue_chunk(const TileDesc &d, int c, int kc, T *Mb)
 {
     constexpr int W = 32 * Q;
+    const T *rot = static_cast<const T *>(d.rot) + c * d.rot_cs;
+    const int D = d.D, rows = min(kc + kChunk, D) - kc, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = warp; r < rows; r += blockDim.x >> 5) {
+        const T *src = rot + (size_t)(kc + r) * d.ld_rot;
+        for (int j = lane; j < D; j += 32) cp_async_elem<T>(Mb + r * W + j, src + j);
+    }
+    cp_async_commit();
+}
+
+// Ids 17-30 on one tile of 8 * RPW rows: the x rows are staged once (cp.async); per component,
+// x - o_c is formed in shared memory, the squared distance for the composition weights is
+// accumulated, M_c^T streams through two shared-memory chunk buffers (the next chunk, of this or
+// the next rotated component, is in flight while the current one is used), the component's body
+// runs (a hybrid reads its rotated row back from the warp's own rows of Ys, gathered through the
+// shuffle), and the result per row stays in shared memory; then the components are mixed.
+template <typename T, int Q, int RPW = kRowsPerWarp>
+__device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, T *Xs, int *Ss, T *fbuf, T *sbuf,
+                                             unsigned int *err)
+{
+    constexpr int W = 32 * Q, kRows = 8 * RPW;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row0 = warp * RPW;
     const T *X = static_cast<const T *>(d.x);
     const int nc = func_components(d.func), D = d.D;
     const bool comp = func_composition(d.func);
+    T *Mbuf[2] = {Ms, Ms + kChunk * W};
+    __syncthreads();  // the previous tile is done with every buffer
+    for (int r = warp; r < kChunk; r += blockDim.x >> 5)  // zero columns D..W-1
+        for (int j = D + lane; j < W; j += 32) {
+            Mbuf[0][r * W + j] = T(0);
+            Mbuf[1][r * W + j] = T(0);
+        }
+    for (int i = threadIdx.x; i < kRows * W; i += blockDim.x) {
+        const int r = i / W, k = i - r * W;
+        if (r < d.count && k < D) cp_async_elem<T>(Xs + i, X + (size_t)r * d.ldx + k);
+        else Xs[i] = T(0);
+    }
+    cp_async_commit();
+    int cc = -1, ck = 0;
+    bool pending = multi_next_chunk(d.func, D, cc, ck);
+    if (pending) issue_chunk<T, Q>(d, cc, ck, Mbuf[0]);
+    int buf = 0;
     for (int c = 0; c < nc; ++c) {
         const int h = multi_hybrid(d.func, c);
         const T *o = static_cast<const T *>(d.shift) + c * d.shift_cs;
-        const T *rot = static_cast<const T *>(d.rot) + c * d.rot_cs;
-        __syncthreads();  // previous component (or tile) done with Ys / Ss / Ms
-        for (int i = threadIdx.x; i < 8 * RPW * W; i += blockDim.x) {
-            const int r = i / W, k = i - r * W;
-            Ys[i] = (r < d.count && k < D) ? X[(size_t)r * d.ldx + k] - o[k] : T(0);
+        if (c == 0) {
+            if (pending) cp_async_wait<1>();
+            else cp_async_wait<0>();
+        }
+        __syncthreads();  // x rows arrived; the previous component is done with Ys / Ss
+        for (int i = threadIdx.x; i < kRows * W; i += blockDim.x) {
+            const int k = i % W;
+            Ys[i] = k < D ? Xs[i] - o[k] : T(0);
         }
         if (h >= 0) {
             for (int k = threadIdx.x; k < W; k += blockDim.x) {
@@ -112,12 +187,21 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, in
 #pragma unroll
             for (int q = 0; q < Q; ++q) acc[rr][q] = T(0);
         if (rotated) {
-            for (int kc = 0; kc < D; kc += kChunk) {
-                const int ke = min(kc + kChunk, D);
-                __syncthreads();
-                load_rot_rows<T, Q>(Ms, rot, d.ld_rot, D, kc, ke);
-                __syncthreads();
-                eval_accumulate<T, Q>(acc, Ys, W, row0, Ms, W, kc, ke, lane);
+            for (int kc = 0; kc < D; kc += kChunk) {  // (cc, ck) == (c, kc) here
+                int nc2 = cc, nk = ck;
+                const bool more = multi_next_chunk(d.func, D, nc2, nk);
+                if (more) {
+                    issue_chunk<T, Q>(d, nc2, nk, Mbuf[buf ^ 1]);
+                    cp_async_wait<1>();
+                } else {
+                    cp_async_wait<0>();
+                }
+                __syncthreads();  // chunk (c, kc) visible to every thread
+                eval_accumulate<T, Q>(acc, Ys, W, row0, Mbuf[buf], W, kc, min(kc + kChunk, D), lane);
+                __syncthreads();  // everyone is done with this buffer before it is refilled
+                buf ^= 1;
+                cc = nc2;
+                ck = nk;
             }
         } else {
             eval_identity<T, Q>(acc, Ys, W, row0, D, lane);
@@ -160,19 +244,23 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, in
     }
 }
 
-// Tiles of 8 * RPW rows (one warp per RPW rows, 256 threads).
+// Tiles of 8 * RPW rows (one warp per RPW rows, 256 threads). Layout: Ys (tile), Ms (two chunk
+// buffers; the first is where the single-matrix kernels keep their chunk), Xs (tile), fbuf,
+// sbuf (per row and component), Ss (shuffle).
 template <typename T, int Q, int RPW = kRowsPerWarp>
 constexpr size_t multi_smem_bytes()
 {
-    return sizeof(T) * ((size_t)(8 * RPW + kChunk) * 32 * Q + 2 * 8 * RPW * kMaxComp) + sizeof(int) * 32 * Q;
+    return sizeof(T) * ((size_t)(2 * 8 * RPW + 2 * kChunk) * 32 * Q + 2 * 8 * RPW * kMaxComp) +
+           sizeof(int) * 32 * Q;
 }
 
 template <typename T, int Q, int RPW = kRowsPerWarp>
-__device__ __forceinline__ void multi_smem(unsigned char *raw, T *&Ys, T *&Ms, T *&fbuf, T *&sbuf, int *&Ss)
+__device__ __forceinline__ void multi_smem(unsigned char *raw, T *&Ys, T *&Ms, T *&Xs, T *&fbuf, T *&sbuf, int *&Ss)
 {
     Ys = reinterpret_cast<T *>(raw);
     Ms = Ys + 8 * RPW * 32 * Q;
-    fbuf = Ms + kChunk * 32 * Q;
+    Xs = Ms + 2 * kChunk * 32 * Q;
+    fbuf = Xs + 8 * RPW * 32 * Q;
     sbuf = fbuf + 8 * RPW * kMaxComp;
     Ss = reinterpret_cast<int *>(sbuf + 8 * RPW * kMaxComp);
 }

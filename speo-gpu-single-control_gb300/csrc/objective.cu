@@ -119,10 +119,10 @@ __global__ void __launch_bounds__(256, (!G && (Q == 1 || Q == 4)) ? 4 : 1) k_eva
                     if (threadIdx.x == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
                     break;
                 }
-                float *fbuf, *sbuf;
+                float *Xs, *fbuf, *sbuf;
                 int *Ss;
-                multi_smem<float, Q>(smem_raw, Ys, Ms, fbuf, sbuf, Ss);
-                eval_multi_tile<float, Q>(d, Ys, Ms, Ss, fbuf, sbuf, &s_deverr);
+                multi_smem<float, Q>(smem_raw, Ys, Ms, Xs, fbuf, sbuf, Ss);
+                eval_multi_tile<float, Q>(d, Ys, Ms, Xs, Ss, fbuf, sbuf, &s_deverr);
                 continue;
             }
             if (!func_supported(d.func)) {
@@ -287,6 +287,7 @@ int launch_seg(const speo_segment *segs, const speo_work_item *items, int n_item
 {
     const size_t smem = sizeof(float) * (size_t)(kEvalTile + kChunk) * 32 * Q;
     constexpr size_t smem_g = multi_smem_bytes<float, Q>();  // the generic variant also runs ids 17-30
+    static_assert(smem_g <= 227 * 1024, "tile buffers exceed the shared memory of one block");
     // two variants: the per-coordinate sums (8, 9, 31) and the other ids; each skips the other's tiles
     cudaError_t e = cudaFuncSetAttribute(k_eval_seg<Q, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess)

@@ -18,14 +18,14 @@ __global__ void __launch_bounds__(256) k_eval_ref_multi(const T *X, int ldx, int
                                                         const T *rot, const int *shuf, T *fit)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *Ys, *Ms, *fbuf, *sbuf;
+    T *Ys, *Ms, *Xs, *fbuf, *sbuf;
     int *Ss;
-    multi_smem<T, Q, RPW>(smem_raw, Ys, Ms, fbuf, sbuf, Ss);
+    multi_smem<T, Q, RPW>(smem_raw, Ys, Ms, Xs, fbuf, sbuf, Ss);
     constexpr int kTile = 8 * RPW;
     const int tiles = (P + kTile - 1) / kTile;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x)
-        eval_multi_tile<T, Q, RPW>(ref_tile_multi<T, kTile>(t, X, ldx, P, D, func, shift, rot, shuf, fit), Ys, Ms, Ss,
-                                   fbuf, sbuf, &s_deverr);
+        eval_multi_tile<T, Q, RPW>(ref_tile_multi<T, kTile>(t, X, ldx, P, D, func, shift, rot, shuf, fit), Ys, Ms, Xs,
+                                   Ss, fbuf, sbuf, &s_deverr);
 }
 
 template <typename T, int Q, int RPW>
@@ -33,11 +33,12 @@ int launch_ref_multi_rpw(const T *X, int ldx, int P, int D, int func, const T *s
                          T *fit, cudaStream_t st)
 {
     constexpr size_t smem = multi_smem_bytes<T, Q, RPW>();
+    static_assert(smem <= 227 * 1024, "tile buffers exceed the shared memory of one block");
     cudaError_t e =
         cudaFuncSetAttribute(k_eval_ref_multi<T, Q, RPW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_eval_ref_multi)");
     const int tiles = (P + 8 * RPW - 1) / (8 * RPW);
-    const int per_sm = (int)((200u * 1024u) / smem) < 2 ? 1 : 2;
+    const int fit_sm = (int)((220u * 1024u) / smem), per_sm = fit_sm < 1 ? 1 : fit_sm > 4 ? 4 : fit_sm;
     const int grid = tiles < per_sm * sm_count() ? tiles : per_sm * sm_count();
     k_eval_ref_multi<T, Q, RPW><<<grid, 256, smem, st>>>(X, ldx, P, D, func, shift, rot, shuf, fit);
     return check_launch("k_eval_ref_multi");
@@ -47,9 +48,14 @@ template <typename T, int Q>
 int launch_ref_multi(const T *X, int ldx, int P, int D, int func, const T *shift, const T *rot, const int *shuf, T *fit,
                      cudaStream_t st)
 {
-    if ((P + kEvalTile - 1) / kEvalTile < 2 * sm_count())
+    // FP64 with D > 128 keeps 16-row tiles: a 64-row tile's buffers would not fit in shared memory
+    if constexpr (sizeof(T) == 8 && Q == 8) {
         return launch_ref_multi_rpw<T, Q, 2>(X, ldx, P, D, func, shift, rot, shuf, fit, st);
-    return launch_ref_multi_rpw<T, Q, kRowsPerWarp>(X, ldx, P, D, func, shift, rot, shuf, fit, st);
+    } else {
+        if ((P + kEvalTile - 1) / kEvalTile < 2 * sm_count())
+            return launch_ref_multi_rpw<T, Q, 2>(X, ldx, P, D, func, shift, rot, shuf, fit, st);
+        return launch_ref_multi_rpw<T, Q, kRowsPerWarp>(X, ldx, P, D, func, shift, rot, shuf, fit, st);
+    }
 }
 
 }  // namespace

@@ -80,7 +80,8 @@ def test_dropin_init_matches_oracle(lib, oracle, cuda, P, D):
 
 
 @pytest.mark.parametrize("f64", [False, True])
-@pytest.mark.parametrize("P,D,nsub", [(100, 30, 4), (64, 10, 1), (96, 100, 3), (8, 1, 2), (40, 33, 10)])
+@pytest.mark.parametrize("P,D,nsub", [(100, 30, 4), (64, 10, 1), (96, 100, 3), (8, 1, 2), (40, 33, 10), (2048, 10, 1),
+                                      (3000, 30, 2)])
 def test_dropin_generate_matches_oracle(lib, oracle, cuda, f64, P, D, nsub):
     import torch
 
