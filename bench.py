@@ -280,6 +280,7 @@ def bench_speo(args) -> dict:
         out["config3_batched"] = bench_config3(L, dev, torch, flush)
         out["config4_surrogate_vs_plain"] = bench_config4(L, dev, torch, args.c4_gens)
         out["surrogate_mlp"] = bench_mlp(L, dev, torch)
+        out["published_config"] = bench_published(L, dev, torch)
     if not args.no_e2e:
         out["e2e"] = bench_e2e(L, dev, torch, args)
     if rank == 0 and not args.no_cpu:
@@ -710,7 +711,7 @@ def bench_e2e(L, dev, torch, args) -> dict:
 PUBLISHED_2GPU_MEVALS = {23: 2.94, 24: 3.84, 25: 3.61, 26: 2.25, 27: 2.30, 28: 2.71, 29: 2.87, 30: 2.43}
 
 
-def bench_published(L, dev, torch, gens: int = 300, gens64: int = 60) -> dict:
+def bench_published(L, dev, torch, gens: int = 300, gens64: int = 60, fids=range(23, 31), fp64: bool = True) -> dict:
     """F23-F30 at D = 100, one island of 4096 rows (one sub-island), through the drop-in entry
     points on device-resident data: the FP32 loop as one speo_de_run_f32 call (last fitness read
     back), and the FP64 loop (the reference's precision) as API_DE_GenerateNewPopulation +
@@ -725,7 +726,7 @@ def bench_published(L, dev, torch, gens: int = 300, gens64: int = 60) -> dict:
            "functions": {}}
     stream = torch.cuda.current_stream()
     L.speo_set_stream(ctypes.c_void_p(stream.cuda_stream))
-    for fid in range(23, 31):
+    for fid in fids:
         o, M, S = make_instance_multi(run_seed() + fid, D, fid)
         nc = o.shape[0]
         rot = np.zeros((nc, ld, D), dtype=np.float32)
@@ -735,7 +736,7 @@ def bench_published(L, dev, torch, gens: int = 300, gens64: int = 60) -> dict:
         sf = np.zeros((nc, ld), dtype=np.int32)
         sf[:, :D] = S
         rec = {}
-        for f64 in (False, True):
+        for f64 in (False, True) if fp64 else (False,):
             dt = torch.float64 if f64 else torch.float32
             sfx = "" if f64 else "_f32"
             Pop = _lib.PopulationF64 if f64 else _lib.PopulationF32
@@ -870,6 +871,8 @@ def main() -> None:
     ap.add_argument("--e2e-only", action="store_true", help="only the end-to-end drop-in measurement")
     ap.add_argument("--published-only", action="store_true",
                     help="only the reference's published configuration (F23-F30, D=100, 4096 rows)")
+    ap.add_argument("--published-fids", default="23-30", help="function ids a-b of the published configuration")
+    ap.add_argument("--published-fp32-only", action="store_true", help="skip the FP64 leg of the published configuration")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.e2e_only:
@@ -884,7 +887,9 @@ def main() -> None:
         from speo_gb300 import _lib
 
         torch.cuda.set_device(0)
-        print(json.dumps({"published_config": bench_published(_lib.load(), "cuda:0", torch)}))
+        a, b = (int(v) for v in args.published_fids.split("-"))
+        print(json.dumps({"published_config": bench_published(_lib.load(), "cuda:0", torch, fids=range(a, b + 1),
+                                                               fp64=not args.published_fp32_only)}))
         return
     if args.mlp_case:
         import torch

@@ -79,15 +79,14 @@ __device__ __forceinline__ void cp_async_wait()
 }
 
 // The chunks of M_c^T the tile consumes, in order: (component, first row) for every rotated
-// component, kChunk rows at a time. Returns false past the last one.
-__device__ __forceinline__ bool multi_next_chunk(int func, int D, int &c, int &kc)
+// component below cend, kChunk rows at a time. Returns false past the last one.
+__device__ __forceinline__ bool multi_next_chunk(int func, int D, int cend, int &c, int &kc, bool started)
 {
-    const int nc = func_components(func);
-    if (c >= 0 && kc + kChunk < D) {
+    if (started && kc + kChunk < D) {
         kc += kChunk;
         return true;
     }
-    for (int n = c + 1; n < nc; ++n)
+    for (int n = started ? c + 1 : c; n < cend; ++n)
         if (multi_hybrid(func, n) >= 0 || comp_piece(func, n).rotated) {
             c = n;
             kc = 0;
@@ -109,20 +108,22 @@ __device__ __forceinline__ void issue_chunk(const TileDesc &d, int c, int kc, T 
     cp_async_commit();
 }
 
-// Ids 17-30 on one tile of 8 * RPW rows: the x rows are staged once (cp.async); per component,
+// Ids 17-30 on one tile of 8 * RPW rows, components [cbeg, cend): the x rows are staged once
+// (cp.async); per component,
 // x - o_c is formed in shared memory, the squared distance for the composition weights is
 // accumulated, M_c^T streams through two shared-memory chunk buffers (the next chunk, of this or
 // the next rotated component, is in flight while the current one is used), the component's body
 // runs (a hybrid reads its rotated row back from the warp's own rows of Ys, gathered through the
-// shuffle), and the result per row stays in shared memory; then the components are mixed.
+// shuffle), and the result per row stays in shared memory (fbuf / sbuf [row][component], on lane 0
+// of the row's warp); with `finish` the components are then mixed and the fitness written.
 template <typename T, int Q, int RPW = kRowsPerWarp>
 __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, T *Xs, int *Ss, T *fbuf, T *sbuf,
-                                             unsigned int *err)
+                                             unsigned int *err, int cbeg, int cend, bool finish)
 {
     constexpr int W = 32 * Q, kRows = 8 * RPW;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row0 = warp * RPW;
     const T *X = static_cast<const T *>(d.x);
-    const int nc = func_components(d.func), D = d.D;
+    const int D = d.D;
     const bool comp = func_composition(d.func);
     T *Mbuf[2] = {Ms, Ms + kChunk * W};
     __syncthreads();  // the previous tile is done with every buffer
@@ -137,14 +138,14 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, T 
         else Xs[i] = T(0);
     }
     cp_async_commit();
-    int cc = -1, ck = 0;
-    bool pending = multi_next_chunk(d.func, D, cc, ck);
+    int cc = cbeg, ck = 0;
+    bool pending = multi_next_chunk(d.func, D, cend, cc, ck, false);
     if (pending) issue_chunk<T, Q>(d, cc, ck, Mbuf[0]);
     int buf = 0;
-    for (int c = 0; c < nc; ++c) {
+    for (int c = cbeg; c < cend; ++c) {
         const int h = multi_hybrid(d.func, c);
         const T *o = static_cast<const T *>(d.shift) + c * d.shift_cs;
-        if (c == 0) {
+        if (c == cbeg) {
             if (pending) cp_async_wait<1>();
             else cp_async_wait<0>();
         }
@@ -189,7 +190,7 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, T 
         if (rotated) {
             for (int kc = 0; kc < D; kc += kChunk) {  // (cc, ck) == (c, kc) here
                 int nc2 = cc, nk = ck;
-                const bool more = multi_next_chunk(d.func, D, nc2, nk);
+                const bool more = multi_next_chunk(d.func, D, cend, nc2, nk, true);
                 if (more) {
                     issue_chunk<T, Q>(d, nc2, nk, Mbuf[buf ^ 1]);
                     cp_async_wait<1>();
@@ -232,7 +233,7 @@ __device__ __noinline__ void eval_multi_tile(const TileDesc &d, T *Ys, T *Ms, T 
             }
         }
     }
-    if (lane == 0) {
+    if (finish && lane == 0) {
         T *fit = static_cast<T *>(d.fit);
 #pragma unroll 1
         for (int rr = 0; rr < RPW; ++rr) {

@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(256, (!G && (Q == 1 || Q == 4)) ? 4 : 1) k_eva
                 float *Xs, *fbuf, *sbuf;
                 int *Ss;
                 multi_smem<float, Q>(smem_raw, Ys, Ms, Xs, fbuf, sbuf, Ss);
-                eval_multi_tile<float, Q>(d, Ys, Ms, Xs, Ss, fbuf, sbuf, &s_deverr);
+                eval_multi_tile<float, Q>(d, Ys, Ms, Xs, Ss, fbuf, sbuf, &s_deverr, 0, func_components(d.func), true);
                 continue;
             }
             if (!func_supported(d.func)) {

@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(256) k_eval_ref_multi(const T *X, int ldx, int
     const int tiles = (P + kTile - 1) / kTile;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x)
         eval_multi_tile<T, Q, RPW>(ref_tile_multi<T, kTile>(t, X, ldx, P, D, func, shift, rot, shuf, fit), Ys, Ms, Xs,
-                                   Ss, fbuf, sbuf, &s_deverr);
+                                   Ss, fbuf, sbuf, &s_deverr, 0, func_components(func), true);
 }
 
 template <typename T, int Q, int RPW>

@@ -368,6 +368,38 @@ def test_dropin_evaluate_multi_matches_oracle(lib, oracle, cuda, f64, fid, P, D)
     _assert_fitness(f.cpu().numpy(), ref, rtol=rtol, atol=atol)
 
 
+@pytest.mark.parametrize("fid", [23, 24, 29, 30, 17])
+def test_multi_tiles_do_not_change_results(lib, cuda, fid):
+    """A row's fitness does not depend on how the rows are tiled: a 4096-row call (16-row tiles)
+    and a 20000-row call (64-row tiles) agree bit for bit on their common rows, in both precisions."""
+    import torch
+    from speo_gb300 import _lib
+    from speo_gb300.instances import make_instance_multi
+
+    D, ld, n_big, n_small = 50, 64, 20000, 4096
+    o, M, S = make_instance_multi(fid + 5, D, fid)
+    nc = o.shape[0]
+    rot = np.zeros((nc, ld, D), dtype=np.float32)
+    rot[:, :D] = M.transpose(0, 2, 1)
+    shift = np.zeros((nc, ld), dtype=np.float32)
+    shift[:, :D] = o
+    shuf = np.zeros((nc, ld), dtype=np.int32)
+    shuf[:, :D] = S
+    X = np.zeros((n_big, ld), dtype=np.float32)
+    X[:, :D] = np.random.default_rng(fid).uniform(-100, 100, (n_big, D))
+    for dt, fn in ((torch.float32, lib.API_evaluateFitness_f32), (torch.float64, lib.API_evaluateFitness)):
+        tX, tr, ts = (torch.from_numpy(a).to(cuda, dt) for a in (X, rot, shift))
+        tsf = torch.from_numpy(shuf).to(cuda)
+        outs = []
+        for n in (n_big, n_small):
+            f = torch.full((n,), -1.0, dtype=dt, device=cuda)
+            fn(f.data_ptr(), None, None, tX.data_ptr(), ts.data_ptr(), tr.data_ptr(), tsf.data_ptr(), None, None, None,
+               n, D, 0.0, fid)
+            _lib.check(lib.API_CheckCUDAError(), "API_evaluateFitness")
+            outs.append(f.cpu().numpy())
+        assert np.array_equal(outs[0][:n_small], outs[1])
+
+
 def _table_multi(cuda, layout, seed=11):
     """layout: (P, D, fid); one multi-component instance (o, M, S) per entry."""
     from speo_gb300 import _lib
