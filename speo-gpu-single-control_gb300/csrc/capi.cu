@@ -3,6 +3,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "host.h"
 
@@ -12,6 +13,54 @@ thread_local char t_msg[512] = "";
 thread_local int t_sticky = SPEO_OK;  // first failure since the last API_CheckCUDAError
 thread_local cudaStream_t t_stream = nullptr;
 int g_sm_count[64] = {0};
+
+// The device error words of every translation unit, gathered (read and cleared) by one kernel
+// into a mapped host word: one launch and one synchronisation per read instead of a copy per unit.
+constexpr int kErrUnits = 9;
+struct DevErr {
+    bool ready = false;
+    unsigned int **d_addrs = nullptr;
+    unsigned int *h_out = nullptr, *d_out = nullptr;
+};
+DevErr g_deverr[64];
+std::mutex g_deverr_mu;
+
+__global__ void k_gather_errors(unsigned int *const *addrs, int n, unsigned int *out)
+{
+    unsigned int v = 0;
+    for (int i = 0; i < n; ++i) v |= atomicExch(addrs[i], 0u);
+    *out = v;
+}
+
+int deverr_state(DevErr **out)
+{
+    int dev = 0;
+    if (int e = check_cuda(cudaGetDevice(&dev), "speo_device_error_bits: device")) return e;
+    if (dev < 0 || dev >= 64) return fail(SPEO_ERR_CUDA, "speo_device_error_bits: device %d", dev);
+    std::lock_guard<std::mutex> lock(g_deverr_mu);
+    DevErr &s = g_deverr[dev];
+    if (!s.ready) {
+        void *addrs[kErrUnits] = {speo_deverr_de_ops(),  speo_deverr_objective(),  speo_deverr_generation(),
+                                  speo_deverr_tc(),      speo_deverr_resident(),   speo_deverr_surrogate(),
+                                  speo_deverr_mlp(),     speo_deverr_dropin_step(), speo_deverr_objective_multi()};
+        for (void *a : addrs)
+            if (!a) return fail(SPEO_ERR_CUDA, "speo_device_error_bits: cannot locate the device flags");
+        if (int e = check_cuda(cudaMalloc(reinterpret_cast<void **>(&s.d_addrs), sizeof addrs), "deverr: alloc"))
+            return e;
+        if (int e = check_cuda(cudaMemcpy(s.d_addrs, addrs, sizeof addrs, cudaMemcpyHostToDevice), "deverr: copy"))
+            return e;
+        if (int e = check_cuda(cudaHostAlloc(reinterpret_cast<void **>(&s.h_out), sizeof(unsigned int),
+                                             cudaHostAllocMapped),
+                               "deverr: host word"))
+            return e;
+        if (int e = check_cuda(cudaHostGetDevicePointer(reinterpret_cast<void **>(&s.d_out), s.h_out, 0),
+                               "deverr: mapped word"))
+            return e;
+        s.ready = true;
+    }
+    *out = &s;
+    return SPEO_OK;
+}
 }  // namespace
 
 int fail(int status, const char *fmt, ...)
@@ -66,10 +115,13 @@ extern "C" const char *speo_version(void) { return "speo_gb300 0.1 (sm_103a)"; }
 extern "C" int speo_device_error_bits(uint32_t *bits_out)
 {
     if (int e = check_cuda(cudaDeviceSynchronize(), "speo_device_error_bits: sync")) return e;
-    const unsigned bits = speo_deverr_de_ops() | speo_deverr_objective() | speo_deverr_generation() | speo_deverr_tc() |
-                          speo_deverr_resident() | speo_deverr_surrogate() | speo_deverr_mlp() |
-                          speo_deverr_dropin_step() | speo_deverr_objective_multi();
-    if (bits & 0x80000000u) return fail(SPEO_ERR_CUDA, "speo_device_error_bits: cannot read the device flags");
+    DevErr *s = nullptr;
+    if (int e = deverr_state(&s)) return e;
+    *const_cast<volatile unsigned int *>(s->h_out) = 0u;
+    k_gather_errors<<<1, 1>>>(s->d_addrs, kErrUnits, s->d_out);
+    if (int e = check_launch("k_gather_errors")) return e;
+    if (int e = check_cuda(cudaDeviceSynchronize(), "speo_device_error_bits: sync")) return e;
+    const unsigned bits = *const_cast<volatile unsigned int *>(s->h_out);
     if (bits_out) *bits_out = bits;
     return SPEO_OK;
 }

@@ -386,13 +386,16 @@ __device__ __forceinline__ bool better(float fa, long long ra, float fb, long lo
 
 }  // namespace speo
 
-// Per-translation-unit device error word and its host accessor (defined by SPEO_DEVERR_TU).
+// Per-translation-unit device error word; the host accessor returns its device address (on the
+// current device), which speo_device_error_bits reads and clears with one gather kernel.
 #define SPEO_DEFINE_DEVERR(name)                                                         \
     static __device__ unsigned int s_deverr;                                             \
-    extern "C" unsigned int name(void)                                                   \
+    extern "C" void *name(void)                                                          \
     {                                                                                    \
-        unsigned int v = 0, zero = 0;                                                    \
-        if (cudaMemcpyFromSymbol(&v, s_deverr, sizeof v) != cudaSuccess) return 0x80000000u; \
-        cudaMemcpyToSymbol(s_deverr, &zero, sizeof zero);                               \
-        return v;                                                                        \
+        void *p = nullptr;                                                               \
+        if (cudaGetSymbolAddress(&p, s_deverr) != cudaSuccess) {                          \
+            cudaGetLastError();                                                          \
+            return nullptr;                                                              \
+        }                                                                                \
+        return p;                                                                        \
     }

@@ -91,12 +91,12 @@ size_t mlp_img_w2t_offset(int h);
 }  // namespace speo
 
 // Bit readers of the per-translation-unit device error words.
-extern "C" unsigned int speo_deverr_de_ops(void);
-extern "C" unsigned int speo_deverr_objective(void);
-extern "C" unsigned int speo_deverr_generation(void);
-extern "C" unsigned int speo_deverr_tc(void);
-extern "C" unsigned int speo_deverr_resident(void);
-extern "C" unsigned int speo_deverr_surrogate(void);
-extern "C" unsigned int speo_deverr_mlp(void);
-extern "C" unsigned int speo_deverr_dropin_step(void);
-extern "C" unsigned int speo_deverr_objective_multi(void);
+extern "C" void *speo_deverr_de_ops(void);
+extern "C" void *speo_deverr_objective(void);
+extern "C" void *speo_deverr_generation(void);
+extern "C" void *speo_deverr_tc(void);
+extern "C" void *speo_deverr_resident(void);
+extern "C" void *speo_deverr_surrogate(void);
+extern "C" void *speo_deverr_mlp(void);
+extern "C" void *speo_deverr_dropin_step(void);
+extern "C" void *speo_deverr_objective_multi(void);

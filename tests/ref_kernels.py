@@ -21,10 +21,13 @@ K_BEST = b"_Z36global_DE_FindBestIndividualInIslandPi14GPU_Population14GPU_Islan
 K_GEN = b"_Z31global_DE_GenerateNewPopulation14GPU_PopulationS_Pi14GPU_IslandInfoP6DEInfoP17curandStateXORWOW11ProblemInfo"
 K_SEL = b"_Z24global_DE_SelectSurvival14GPU_PopulationS_11ProblemInfo"
 CURAND_STATE_BYTES = 48  # sizeof(curandStateXORWOW)
+# kernel_CEC2014_CUDA.cu: global_ShiftAndRotation (:147-181) and global_f8 (:557-587), per precision
+K_SR = {"f64": b"_Z23global_ShiftAndRotationPdS_S_S_iiiiiii", "f32": b"_Z23global_ShiftAndRotationPfS_S_S_iiiiiii"}
+K_F8 = {"f64": b"_Z9global_f8PdS_iidddd", "f32": b"_Z9global_f8PfS_iiffff"}
 
 
-def available(precision: str) -> bool:
-    return all((REF_DIR / f"ref_{k}_{precision}.fatbin").exists() for k in ("de", "ea")) and CAPTURE.exists()
+def available(precision: str, kinds=("de", "ea")) -> bool:
+    return all((REF_DIR / f"ref_{k}_{precision}.fatbin").exists() for k in kinds) and CAPTURE.exists()
 
 
 class Driver:
@@ -50,13 +53,15 @@ class Driver:
         self.check(self.cu.cuModuleGetFunction(byref(fn), self.module(path), name), f"cuModuleGetFunction({name})")
         return fn
 
-    def launch(self, fn, grid, block, args):
-        """args: ctypes objects (scalars or Structures), passed by value."""
+    def launch(self, fn, grid, block, args, smem=0, sync=True):
+        """args: ctypes objects (scalars or Structures), passed by value. sync: a context
+        synchronisation after the launch (the reference's CudaCheckError does one)."""
         ptrs = (c_void_p * len(args))(*[ctypes.cast(ctypes.pointer(a), c_void_p) for a in args])
         self.check(self.cu.cuLaunchKernel(fn, c_uint(grid[0]), c_uint(grid[1]), c_uint(grid[2]), c_uint(block[0]),
-                                          c_uint(block[1]), c_uint(block[2]), c_uint(0), None, ptrs, None),
+                                          c_uint(block[1]), c_uint(block[2]), c_uint(smem), None, ptrs, None),
                    "cuLaunchKernel")
-        self.check(self.cu.cuCtxSynchronize(), "cuCtxSynchronize")
+        if sync:
+            self.check(self.cu.cuCtxSynchronize(), "cuCtxSynchronize")
 
 
 def de_config(pop_size: int):
