@@ -24,6 +24,13 @@ CURAND_STATE_BYTES = 48  # sizeof(curandStateXORWOW)
 # kernel_CEC2014_CUDA.cu: global_ShiftAndRotation (:147-181) and global_f8 (:557-587), per precision
 K_SR = {"f64": b"_Z23global_ShiftAndRotationPdS_S_S_iiiiiii", "f32": b"_Z23global_ShiftAndRotationPfS_S_S_iiiiiii"}
 K_F8 = {"f64": b"_Z9global_f8PdS_iidddd", "f32": b"_Z9global_f8PfS_iiffff"}
+# the elementwise bodies global_f1..f4 (:254-387), global_Shift (:183-195), global_CalW (:74-122),
+# global_CombineFitness (:197-206): what CompFunc1 (F23, :1416-1451) launches
+K_FN = {p: {n: f"_Z9global_f{n}{'PdS_iidddd' if p == 'f64' else 'PfS_iiffff'}".encode() for n in (1, 2, 3, 4)}
+        for p in ("f64", "f32")}
+K_SHIFT = {"f64": b"_Z12global_ShiftPdS_S_iii", "f32": b"_Z12global_ShiftPfS_S_iii"}
+K_CALW = {"f64": b"_Z11global_CalWPdS_S_S_ii", "f32": b"_Z11global_CalWPfS_S_S_ii"}
+K_COMBINE = {"f64": b"_Z21global_CombineFitnessPdS_iS_idd", "f32": b"_Z21global_CombineFitnessPfS_iS_iff"}
 
 
 def available(precision: str, kinds=("de", "ea")) -> bool:
