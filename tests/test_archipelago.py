@@ -149,7 +149,10 @@ def test_regroup_options(oracle, regroup):
 @pytest.mark.parametrize("policy", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("regroup", [0, 3, 1, 2])
 @pytest.mark.parametrize("N,P,D,k,C,rate,interval", [(6, 64, 30, 8, 16, 0.5, 3), (3, 100, 10, 32, 32, 1.0, 2),
-                                                     (17, 40, 50, 5, 7, 0.3, 1)])
+                                                     (17, 40, 50, 5, 7, 0.3, 1),
+                                                     (1, 16, 1, 16, 1, 1.0, 1),      # one island: nobody to send to
+                                                     (2, 4, 3, 4, 4, 1.0, 1),        # the smallest islands, k = P
+                                                     (4, 33, 100, 1, 32, 0.0, 1)])   # rate 0: lists stay empty
 def test_archipelago_matches_oracle(lib, oracle, cuda, policy, regroup, N, P, D, k, C, rate, interval):
     import torch
     from speo_gb300 import _lib
