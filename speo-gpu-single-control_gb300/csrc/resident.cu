@@ -322,7 +322,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
             const int cur = g & 1, nxt = cur ^ 1;
             const float *pop = pop0 + (size_t)cur * Pmax * W;
             const float *fit = fit0 + cur * Pf;
-            __syncthreads();
             int best = -1;
             if (strategy_uses_best(st)) {
                 float bf = __int_as_float(0x7f800000);
@@ -359,16 +358,25 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
                 __syncthreads();
             }
             const int *sRg = sR + (g % GB) * hmax * 8;
-            // (2) trials of this block's rows
-            for (int lr = grp; lr < nr; lr += Pl::RPP) {
-                const int r = rb + lr;
-                const int jrand = sRg[lr * 8 + 5];
-                int dr[5];
+            float *npop = pop0 + (size_t)nxt * Pmax * W;
+            float *nfit = fit0 + nxt * Pf;
+            const uint32_t ppop = peer_pop0 + (uint32_t)(nxt * Pmax * W * sizeof(float));
+            const uint32_t pfit = peer_fit0 + (uint32_t)(nxt * Pf * sizeof(float));
+            // (2)-(4) per warp, for its kRowsPerWarp2 rows of each 64-row pass: trials, evaluation,
+            // greedy selection (strict `<`, kernel_DE_CUDA.cu:312) into the next buffer of both
+            // replicas. A row's trial, fitness and selection stay in its warp: no block barrier.
+            for (int pb = 0; pb < nr; pb += kEvalRows2) {
+                const int lr0 = pb + warp * kRowsPerWarp2;
+                if (lr0 >= nr) break;  // warp-uniform
+                const int nrw = nr - lr0 < kRowsPerWarp2 ? nr - lr0 : kRowsPerWarp2;
+                for (int t = lane; t < nrw * nch; t += 32) {
+                    const int lr = lr0 + t / nch, c = t % nch, r = rb + lr;
+                    const int jrand = sRg[lr * 8 + 5];
+                    int dr[5];
 #pragma unroll
-                for (int k = 0; k < 5; ++k) dr[k] = sRg[lr * 8 + k];
-                const float *xi = pop + r * W;
-                const float *xb = pop + (best >= 0 ? best : r) * W;
-                for (int c = gl; c < nch; c += G) {
+                    for (int k = 0; k < 5; ++k) dr[k] = sRg[lr * 8 + k];
+                    const float *xi = pop + r * W;
+                    const float *xb = pop + (best >= 0 ? best : r) * W;
                     const int e0 = 4 * c;
                     const float4 ti = ld4s(xi + e0);
                     const float4 tb = best >= 0 ? ld4s(xb + e0) : ti;
@@ -400,46 +408,34 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreads, 1)
                     st4s(Xs + lr * W + e0, x4);
                     st4s(Ys + lr * W + e0, y4);
                 }
-            }
-            __syncthreads();
-            // (3) evaluate this block's rows, 64 per pass
-            for (int pb = 0; pb < nr; pb += kEvalRows2) {
+                __syncwarp();
                 float acc[kRowsPerWarp2][Q];
 #pragma unroll
                 for (int rr = 0; rr < kRowsPerWarp2; ++rr)
 #pragma unroll
                     for (int q = 0; q < Q; ++q) acc[rr][q] = 0.f;
                 if (func_rotated(s.func_id))
-                    eval_accumulate<float, Q>(acc, Ys, W, pb + warp * kRowsPerWarp2, Ms, W, 0, D, lane);
+                    eval_accumulate<float, Q>(acc, Ys, W, lr0, Ms, W, 0, D, lane);
                 else
-                    eval_identity<float, Q>(acc, Ys, W, pb + warp * kRowsPerWarp2, D, lane);
+                    eval_identity<float, Q>(acc, Ys, W, lr0, D, lane);
                 float f[kRowsPerWarp2];
                 eval_reduce<float, Q>(acc, D, s.func_id, scale, lane, f);
                 if (lane == 0)
 #pragma unroll
-                    for (int rr = 0; rr < kRowsPerWarp2; ++rr) sF[pb + warp * kRowsPerWarp2 + rr] = f[rr];
-            }
-            __syncthreads();
-            // (4) greedy selection (strict `<`, kernel_DE_CUDA.cu:312) into the next buffer of both
-            // replicas
-            float *npop = pop0 + (size_t)nxt * Pmax * W;
-            float *nfit = fit0 + nxt * Pf;
-            const uint32_t ppop = peer_pop0 + (uint32_t)(nxt * Pmax * W * sizeof(float));
-            const uint32_t pfit = peer_fit0 + (uint32_t)(nxt * Pf * sizeof(float));
-            for (int lr = grp; lr < nr; lr += Pl::RPP) {
-                const int r = rb + lr;
-                const float tf = sF[lr];
-                const bool win = tf < fit[r];
-                const float *src = win ? Xs + lr * W : pop + r * W;
-                for (int c = gl; c < nch; c += G) {
-                    const float4 v = ld4s(src + 4 * c);
+                    for (int rr = 0; rr < kRowsPerWarp2; ++rr) sF[lr0 + rr] = f[rr];
+                __syncwarp();
+                for (int t = lane; t < nrw * nch; t += 32) {
+                    const int lr = lr0 + t / nch, c = t % nch, r = rb + lr;
+                    const float tf = sF[lr];
+                    const bool win = tf < fit[r];
+                    const float4 v = ld4s((win ? Xs + lr * W : pop + r * W) + 4 * c);
                     st4s(npop + r * W + 4 * c, v);
                     st_peer4(ppop + (uint32_t)((r * W + 4 * c) * sizeof(float)), v);
-                }
-                if (gl == 0) {
-                    const float nf = win ? tf : fit[r];
-                    nfit[r] = nf;
-                    st_peer1(pfit + (uint32_t)(r * sizeof(float)), nf);
+                    if (c == 0) {
+                        const float nf = win ? tf : fit[r];
+                        nfit[r] = nf;
+                        st_peer1(pfit + (uint32_t)(r * sizeof(float)), nf);
+                    }
                 }
             }
             cluster_sync();
