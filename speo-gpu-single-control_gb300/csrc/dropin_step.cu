@@ -369,8 +369,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
         const int cur = g & 1, nxt = cur ^ 1;
         const float *Xp = Xp0 + (size_t)cur * S * W;
         const float *fp = fp0 + cur * Sf;
-        __syncthreads();
-        {
+        {  // (the previous generation's cluster barrier ordered every access before this point)
             float bf = INFINITY;
             int bp = 0x7fffffff;
             for (int p = tid; p < S; p += kThreadsS) {
@@ -406,95 +405,97 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
         }
         if (last && me == 0 && tid == 0) a.best_id[isl] = a.perm[base + bp];
         const int *sRg = sR + (g % GB) * h * 8;
-
-        for (int t = tid; t < np * nch; t += kThreadsS) {
-            const int lp = t / nch, c = t - lp * nch;
-            const int p = pb0 + lp, pos = base + p;
-            const int e0 = VN * c;
-            const float *xi = Xp + (size_t)p * W;
-            const float *xb = Xp + (size_t)(strategy_uses_best(st) ? bp : p) * W;
-            const V ti = *reinterpret_cast<const V *>(xi + e0);
-            const V tb = strategy_uses_best(st) ? *reinterpret_cast<const V *>(xb + e0) : ti;
-            V tr[5];
-#pragma unroll
-            for (int k = 0; k < 5; ++k)
-                tr[k] = k < nd ? *reinterpret_cast<const V *>(Xp + (size_t)sRg[lp * 8 + k] * W + e0) : ti;
-            const int jr = sRg[lp * 8 + 5];
-            const uint4 w = philox(make_uint4((uint32_t)(e0 >> 2), (uint32_t)pos, gen, kTagCr), key);
-            V x = ti;
-#pragma unroll
-            for (int q = 0; q < VN; ++q) {
-                const int e = e0 + q;
-                float v;
-                if (e == jr || cr_take(pick(w, (uint32_t)(e & 3)), thr)) {
-                    float xr[5];
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) xr[k] = vget<float>(tr[k], q);
-                    v = mutant<float>(st, F, vget<float>(ti, q), vget<float>(tb, q), xr);
-                } else {
-                    v = vget<float>(ti, q);
-                }
-                vset<float>(x, q, check_bound<float>(v, a.lb, a.ub, ok_bound));
-            }
-            *reinterpret_cast<V *>(Xt + (size_t)lp * W + e0) = x;
-            V y;
-#pragma unroll
-            for (int q = 0; q < VN; ++q) {
-                const int e = e0 + q;
-                vset<float>(y, q, e < D ? sub_rn(vget<float>(x, q), so[e]) : 0.f);
-            }
-            *reinterpret_cast<V *>(Yt + (size_t)lp * W + e0) = y;
-            if (last) {
-                float *out = a.cand + (size_t)a.perm[pos] * W;
-                if (e0 + VN <= D) {
-                    *reinterpret_cast<V *>(out + e0) = x;
-                } else {
-#pragma unroll
-                    for (int q = 0; q < VN; ++q)
-                        if (e0 + q < D) out[e0 + q] = vget<float>(x, q);
-                }
-            }
-        }
-        __syncthreads();
-
+        float *nXp = Xp0 + (size_t)nxt * S * W;
+        float *nfp = fp0 + nxt * Sf;
+        const uint32_t pxp = peer_xp + (uint32_t)((size_t)nxt * S * W * sizeof(float));
+        const uint32_t pfp = peer_fp + (uint32_t)(nxt * Sf * sizeof(float));
+        // trials, evaluation and selection per warp, for its kRowsPerWarp2 positions of each
+        // 64-position pass: a position's trial, fitness and selection stay in its warp
         for (int pb = 0; pb < np; pb += kPassRows2) {
+            const int lr0 = pb + warp * kRowsPerWarp2;
+            if (lr0 >= np) break;  // warp-uniform
+            const int nrw = np - lr0 < kRowsPerWarp2 ? np - lr0 : kRowsPerWarp2;
+            for (int t = lane; t < nrw * nch; t += 32) {
+                const int lp = lr0 + t / nch, c = t % nch;
+                const int p = pb0 + lp, pos = base + p;
+                const int e0 = VN * c;
+                const float *xi = Xp + (size_t)p * W;
+                const float *xb = Xp + (size_t)(strategy_uses_best(st) ? bp : p) * W;
+                const V ti = *reinterpret_cast<const V *>(xi + e0);
+                const V tb = strategy_uses_best(st) ? *reinterpret_cast<const V *>(xb + e0) : ti;
+                V tr[5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k)
+                    tr[k] = k < nd ? *reinterpret_cast<const V *>(Xp + (size_t)sRg[lp * 8 + k] * W + e0) : ti;
+                const int jr = sRg[lp * 8 + 5];
+                const uint4 w = philox(make_uint4((uint32_t)(e0 >> 2), (uint32_t)pos, gen, kTagCr), key);
+                V x = ti;
+#pragma unroll
+                for (int q = 0; q < VN; ++q) {
+                    const int e = e0 + q;
+                    float v;
+                    if (e == jr || cr_take(pick(w, (uint32_t)(e & 3)), thr)) {
+                        float xr[5];
+#pragma unroll
+                        for (int k = 0; k < 5; ++k) xr[k] = vget<float>(tr[k], q);
+                        v = mutant<float>(st, F, vget<float>(ti, q), vget<float>(tb, q), xr);
+                    } else {
+                        v = vget<float>(ti, q);
+                    }
+                    vset<float>(x, q, check_bound<float>(v, a.lb, a.ub, ok_bound));
+                }
+                *reinterpret_cast<V *>(Xt + (size_t)lp * W + e0) = x;
+                V y;
+#pragma unroll
+                for (int q = 0; q < VN; ++q) {
+                    const int e = e0 + q;
+                    vset<float>(y, q, e < D ? sub_rn(vget<float>(x, q), so[e]) : 0.f);
+                }
+                *reinterpret_cast<V *>(Yt + (size_t)lp * W + e0) = y;
+                if (last) {
+                    float *out = a.cand + (size_t)a.perm[pos] * W;
+                    if (e0 + VN <= D) {
+                        *reinterpret_cast<V *>(out + e0) = x;
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < VN; ++q)
+                            if (e0 + q < D) out[e0 + q] = vget<float>(x, q);
+                    }
+                }
+            }
+            __syncwarp();
             float acc[kRowsPerWarp2][Q];
 #pragma unroll
             for (int rr = 0; rr < kRowsPerWarp2; ++rr)
 #pragma unroll
                 for (int q = 0; q < Q; ++q) acc[rr][q] = 0.f;
             if (func_rotated(a.func))
-                eval_accumulate<float, Q>(acc, Yt, W, pb + warp * kRowsPerWarp2, Ms, W, 0, D, lane);
+                eval_accumulate<float, Q>(acc, Yt, W, lr0, Ms, W, 0, D, lane);
             else
-                eval_identity<float, Q>(acc, Yt, W, pb + warp * kRowsPerWarp2, D, lane);
+                eval_identity<float, Q>(acc, Yt, W, lr0, D, lane);
             float f[kRowsPerWarp2];
             eval_reduce<float, Q, kRowsPerWarp2, G>(acc, D, a.func, scale, lane, f);
             if (lane == 0)
 #pragma unroll
-                for (int rr = 0; rr < kRowsPerWarp2; ++rr) sF[pb + warp * kRowsPerWarp2 + rr] = f[rr];
-        }
-        __syncthreads();
-
-        // selection into the next buffer of both replicas
-        float *nXp = Xp0 + (size_t)nxt * S * W;
-        float *nfp = fp0 + nxt * Sf;
-        const uint32_t pxp = peer_xp + (uint32_t)((size_t)nxt * S * W * sizeof(float));
-        const uint32_t pfp = peer_fp + (uint32_t)(nxt * Sf * sizeof(float));
-        for (int t = tid; t < np * nch; t += kThreadsS) {
-            const int lp = t / nch, c = t - lp * nch, p = pb0 + lp;
-            const bool win = sF[lp] < fp[p];
-            const V v = *reinterpret_cast<const V *>((win ? Xt + (size_t)lp * W : Xp + (size_t)p * W) + VN * c);
-            *reinterpret_cast<V *>(nXp + (size_t)p * W + VN * c) = v;
-            st_peer4(pxp + (uint32_t)(((size_t)p * W + VN * c) * sizeof(float)), v);
-        }
-        for (int lp = tid; lp < np; lp += kThreadsS) {
-            const int p = pb0 + lp, row = a.perm[base + p];
-            const float tf = sF[lp];
-            const float nf = tf < fp[p] ? tf : fp[p];
-            nfp[p] = nf;
-            st_peer1(pfp + (uint32_t)(p * sizeof(float)), nf);
-            if (last) a.cfit[row] = tf;
-            if (a.hist) a.hist[(size_t)g * a.P + row] = nf;
+                for (int rr = 0; rr < kRowsPerWarp2; ++rr) sF[lr0 + rr] = f[rr];
+            __syncwarp();
+            // selection into the next buffer of both replicas
+            for (int t = lane; t < nrw * nch; t += 32) {
+                const int lp = lr0 + t / nch, c = t % nch, p = pb0 + lp;
+                const float tf = sF[lp];
+                const bool win = tf < fp[p];
+                const V v = *reinterpret_cast<const V *>((win ? Xt + (size_t)lp * W : Xp + (size_t)p * W) + VN * c);
+                *reinterpret_cast<V *>(nXp + (size_t)p * W + VN * c) = v;
+                st_peer4(pxp + (uint32_t)(((size_t)p * W + VN * c) * sizeof(float)), v);
+                if (c == 0) {
+                    const int row = a.perm[base + p];
+                    const float nf = win ? tf : fp[p];
+                    nfp[p] = nf;
+                    st_peer1(pfp + (uint32_t)(p * sizeof(float)), nf);
+                    if (last) a.cfit[row] = tf;
+                    if (a.hist) a.hist[(size_t)g * a.P + row] = nf;
+                }
+            }
         }
         cluster_sync();
     }
