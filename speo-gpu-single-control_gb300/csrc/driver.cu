@@ -7,7 +7,8 @@
 // private stream, ordered after the caller's stream:
 //   * when a sub-island fits a block, kStepGens generations per launch of the fused kernel
 //     (dropin_step.cu, bit-identical to the three calls), each generation's fitness vector
-//     collected in a device history buffer and copied to the host once per launch;
+//     collected in one of two device history buffers and copied to the host on a second stream
+//     while the next launch runs;
 //   * otherwise over this library's drop-in entry points, where blocks of kBlock generations
 //     (each with its read-back of the fitness vector into pinned host memory) are captured once as
 //     a CUDA graph and replayed, so the per-generation host cost is one graph launch per block
@@ -44,8 +45,10 @@ int history_buffer(size_t floats, float **out)
 }
 
 struct DriverStream {
-    cudaStream_t s = nullptr;
+    cudaStream_t s = nullptr, copy = nullptr;   // generations; fitness read-backs
     cudaEvent_t in = nullptr, out = nullptr;
+    cudaEvent_t made[2] = {nullptr, nullptr};    // history buffer b written
+    cudaEvent_t read[2] = {nullptr, nullptr};    // history buffer b copied to the host
 };
 thread_local DriverStream t_drv;
 
@@ -56,6 +59,13 @@ int driver_stream(DriverStream **out)
         if (int e = check_cuda(cudaStreamCreateWithFlags(&d.s, cudaStreamNonBlocking), "driver stream")) return e;
         if (int e = check_cuda(cudaEventCreateWithFlags(&d.in, cudaEventDisableTiming), "driver event")) return e;
         if (int e = check_cuda(cudaEventCreateWithFlags(&d.out, cudaEventDisableTiming), "driver event")) return e;
+        if (int e = check_cuda(cudaStreamCreateWithFlags(&d.copy, cudaStreamNonBlocking), "driver stream")) return e;
+        for (int b = 0; b < 2; ++b) {
+            if (int e = check_cuda(cudaEventCreateWithFlags(&d.made[b], cudaEventDisableTiming), "driver event"))
+                return e;
+            if (int e = check_cuda(cudaEventCreateWithFlags(&d.read[b], cudaEventDisableTiming), "driver event"))
+                return e;
+        }
     }
     *out = &d;
     return SPEO_OK;
@@ -98,15 +108,28 @@ extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand
     const bool hist = h_fitness && history;
     int e = SPEO_OK, done = 0;
     if (fused) {
+        // two history buffers: launch i writes buffer i % 2 while the copy stream reads the other
+        // one back, so the read-back of a block of generations overlaps the next block
         float *d_hist = nullptr;
-        if (hist) e = history_buffer((size_t)kStepGens * n, &d_hist);
-        for (; !e && done < generations; done += kStepGens) {
-            const int k = generations - done < kStepGens ? generations - done : kStepGens;
-            e = dropin_step_f32(pop, cand, d_best, ii, d_info, rng, pi, d_shift, d_rot, k, d_hist, 0, d->s);
-            if (!e && hist)
-                e = check_cuda(cudaMemcpyAsync(h_fitness + (size_t)done * n, d_hist, sizeof(float) * (size_t)k * n,
-                                               cudaMemcpyDeviceToHost, d->s),
-                               "driver: fitness read-back");
+        if (hist) e = history_buffer(2 * (size_t)kStepGens * n, &d_hist);
+        for (int i = 0; !e && done < generations; done += kStepGens, ++i) {
+            const int k = generations - done < kStepGens ? generations - done : kStepGens, b = i & 1;
+            float *hb = hist ? d_hist + (size_t)b * kStepGens * n : nullptr;
+            if (hist && i >= 2) e = check_cuda(cudaStreamWaitEvent(d->s, d->read[b], 0), "driver: wait");
+            if (!e) e = dropin_step_f32(pop, cand, d_best, ii, d_info, rng, pi, d_shift, d_rot, k, hb, 0, d->s);
+            if (!e && hist) {
+                e = check_cuda(cudaEventRecord(d->made[b], d->s), "driver: record");
+                if (!e) e = check_cuda(cudaStreamWaitEvent(d->copy, d->made[b], 0), "driver: wait");
+                if (!e)
+                    e = check_cuda(cudaMemcpyAsync(h_fitness + (size_t)done * n, hb, sizeof(float) * (size_t)k * n,
+                                                   cudaMemcpyDeviceToHost, d->copy),
+                                   "driver: fitness read-back");
+                if (!e) e = check_cuda(cudaEventRecord(d->read[b], d->copy), "driver: record");
+            }
+        }
+        if (hist) {  // the generation stream (synchronised below) also covers the last read-backs
+            for (int b = 0; b < 2; ++b)
+                if (int e2 = check_cuda(cudaStreamWaitEvent(d->s, d->read[b], 0), "driver: wait"); e2 && !e) e = e2;
         }
         if (!e && h_fitness && !hist)
             e = check_cuda(cudaMemcpyAsync(h_fitness, pop.fitness_value, sizeof(float) * (size_t)n,
