@@ -699,7 +699,7 @@ def bench_e2e(L, dev, torch, args) -> dict:
             "d2h_bytes_per_step": n * 4, "steps": steps,
             "path": "speo_de_run_f32 (64 sub-islands of 100): the generations of API_DE_GenerateNewPopulation_f32 + "
                     "API_evaluateFitness_f32 + API_DE_SelectSurvival_f32, bit-identical, with the sub-islands "
-                    "resident in shared memory for 25 generations per launch; every generation's fitness vector "
+                    "resident in shared memory for up to 100 generations per launch; every generation's fitness vector "
                     "read back to pinned host memory (one copy per launch)",
             "python_loop_value": out["python"],
             "python_loop_path": "the same entry points called one by one from Python (ctypes), per-call host cost"}

@@ -19,7 +19,8 @@ namespace speo {
 namespace {
 
 constexpr int kBlock = 10;     // generations per captured graph (three-call path)
-constexpr int kStepGens = 25;  // generations per fused launch
+constexpr int kStepGens = 100;             // generations per fused launch (at most)
+constexpr size_t kHistFloats = 1u << 22;   // bound of one history buffer (16 MiB)
 
 struct DriverHistory {
     float *p = nullptr;
@@ -111,10 +112,15 @@ extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand
         // two history buffers: launch i writes buffer i % 2 while the copy stream reads the other
         // one back, so the read-back of a block of generations overlaps the next block
         float *d_hist = nullptr;
-        if (hist) e = history_buffer(2 * (size_t)kStepGens * n, &d_hist);
-        for (int i = 0; !e && done < generations; done += kStepGens, ++i) {
-            const int k = generations - done < kStepGens ? generations - done : kStepGens, b = i & 1;
-            float *hb = hist ? d_hist + (size_t)b * kStepGens * n : nullptr;
+        int per = kStepGens;  // generations per launch: the history of one launch within kHistFloats
+        if (hist) {
+            const size_t cap = kHistFloats / (size_t)n;
+            per = cap < 1 ? 1 : cap < (size_t)kStepGens ? (int)cap : kStepGens;
+            e = history_buffer(2 * (size_t)per * n, &d_hist);
+        }
+        for (int i = 0; !e && done < generations; done += per, ++i) {
+            const int k = generations - done < per ? generations - done : per, b = i & 1;
+            float *hb = hist ? d_hist + (size_t)b * per * n : nullptr;
             if (hist && i >= 2) e = check_cuda(cudaStreamWaitEvent(d->s, d->read[b], 0), "driver: wait");
             if (!e) e = dropin_step_f32(pop, cand, d_best, ii, d_info, rng, pi, d_shift, d_rot, k, hb, 0, d->s);
             if (!e && hist) {
