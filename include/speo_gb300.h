@@ -260,7 +260,10 @@ SPEO_API int speo_evaluate(const speo_segment *d_segs, const speo_work_item *d_i
                   int dim_lo, int dim_hi, const float *pop, float *fit, void *stream);
 
 /* Same, with the rotation on the tcgen05 tensor cores: BF16 hi/lo 3-term split product,
- * FP32 accumulation in tensor memory, fused shift/scale/objective/row-reduction epilogue.
+ * FP32 accumulation in tensor memory, fused shift/scale/objective/row-reduction epilogue (one
+ * tile row per thread; the per-coordinate sums 9 and 31 packed two columns per operation, the
+ * other rotated ids 1-7, 11-16 through the row accumulator). Ids 8, 10 (no rotation) and 17-30
+ * (several matrices) are flagged (SPEO_DEVERR_BAD_SEGMENT) and skipped.
  * The population is one flat buffer of n_rows rows, `ld` floats apart, shared by all segments
  * (it is read with TMA tensor loads); tiles are up to SPEO_TILE_TC rows and D <= 128. */
 SPEO_API int speo_evaluate_tc(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,

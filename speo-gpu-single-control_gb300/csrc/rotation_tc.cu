@@ -187,10 +187,61 @@ __device__ __forceinline__ float epilogue_row(uint32_t tmem, int warp, int D, in
     return a + b;
 }
 
+// The other rotated CEC2014 bodies (1-7, 11-16), one TMEM lane (= tile row) per thread: the row
+// accumulator of the CUDA-core paths (row_push / row_finish) over the row's columns in order, each
+// column pushed once its successor is known and the last one with column 0. The function id is a
+// template parameter, so each instance carries one body.
+template <int FID>
+__device__ __noinline__ float epi_generic(uint32_t lane_base, int D, int Np, float scale)
+{
+    using namespace tc;
+    const float fs = func_fixed_shift<float>(FID);
+    RowAcc<float> acc;
+    float z0 = 0.f, prev = 0.f;
+    for (int c = 0; c < Np; c += 32) {
+        uint32_t r[32];
+        tmem_ld32_nowait(lane_base + (uint32_t)c, r);
+        tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const int e = c + j;
+            if (e < D) {
+                const float z = __uint_as_float(r[j]) * scale + fs;
+                if (e == 0) z0 = z;
+                else row_push(acc, FID, e - 1, prev, z, D);
+                prev = z;
+            }
+        }
+    }
+    row_push(acc, FID, D - 1, prev, z0, D);
+    return row_finish(acc, FID, D);
+}
+
+__device__ __forceinline__ float epilogue_row_generic(uint32_t tmem, int warp, int D, int Np, int func, float scale)
+{
+    const uint32_t lb = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    switch (func) {
+    case 1: return epi_generic<1>(lb, D, Np, scale);
+    case 2: return epi_generic<2>(lb, D, Np, scale);
+    case 3: return epi_generic<3>(lb, D, Np, scale);
+    case 4: return epi_generic<4>(lb, D, Np, scale);
+    case 5: return epi_generic<5>(lb, D, Np, scale);
+    case 6: return epi_generic<6>(lb, D, Np, scale);
+    case 7: return epi_generic<7>(lb, D, Np, scale);
+    case 11: return epi_generic<11>(lb, D, Np, scale);
+    case 12: return epi_generic<12>(lb, D, Np, scale);
+    case 13: return epi_generic<13>(lb, D, Np, scale);
+    case 14: return epi_generic<14>(lb, D, Np, scale);
+    case 15: return epi_generic<15>(lb, D, Np, scale);
+    default: return epi_generic<16>(lb, D, Np, scale);
+    }
+}
+
 __device__ __forceinline__ bool tc_tile_ok(const speo_work_item &it, const speo_segment &s, const EvalTcArgs &a)
 {
-    // the tensor-core epilogue implements the sums of per-coordinate terms: ids 9 and 31
-    return (s.func_id == SPEO_FUNC_ROTATED_RASTRIGIN || s.func_id == SPEO_FUNC_ROTATED_SPHERE) && it.count >= 1 &&
+    // the rotated single-matrix ids (CEC2014 1-7, 9, 11-16 and 31); 8 and 10 do not rotate and
+    // 17-30 have several matrices
+    return func_supported(s.func_id) && func_rotated(s.func_id) && it.count >= 1 &&
            it.count <= kTileM && s.dim >= 1 && s.dim <= a.dim_hi && s.dim <= kTmemCols &&
            s.ld == a.ld && it.first >= 0 && it.first + it.count <= s.pop_size && s.row0 >= 0 &&
            s.row0 + it.first + it.count <= a.n_rows;
@@ -332,8 +383,11 @@ __global__ void __launch_bounds__(256, 1) k_evaluate_tc(const __grid_constant__ 
             const bool got = tc::mbar_wait(&bar_mma[i & 1], (uint32_t)((i >> 1) & 1), kWaitBudget);
             if (!__all_sync(0xffffffffu, got)) { *abort_flag = 1; break; }
             tc::fence_after_sync();
-            const float f = epilogue_row(tmem + (uint32_t)((i & 1) * kTmemCols), warp, cur.D, round16(cur.D),
-                                         cur.func, func_scale(cur.func));
+            const uint32_t acc_t = tmem + (uint32_t)((i & 1) * kTmemCols);
+            const float f = func_sum_form(cur.func)
+                                ? epilogue_row(acc_t, warp, cur.D, round16(cur.D), cur.func, func_scale(cur.func))
+                                : epilogue_row_generic(acc_t, warp, cur.D, round16(cur.D), cur.func,
+                                                       func_scale(cur.func));
             const int m = warp * 32 + lane;
             if (cur.ok && m < cur.count) a.fit[cur.row + m] = f;
             tc::fence_before_sync();
