@@ -24,10 +24,13 @@
  *         except in API_CheckCUDAError, which synchronises like the reference's.
  *
  *  2. GB300-native extensions (speo_*): a fused generate+evaluate+select generation kernel
- *     over a table of segments (islands / independent runs of uneven size), the on-device
- *     ring migration that replaces the reference's MPI exchange (src/migrate.cc:46-136),
- *     the tcgen05 rotation GEMM in BF16 3-term split precision, FP64 re-evaluation of each
- *     segment's best, and the online MLP surrogate.
+ *     over a table of segments (islands / independent runs of uneven size), island-resident
+ *     epochs, the on-device ring migration that replaces the reference's MPI exchange
+ *     (src/migrate.cc:46-136), the reference's migration policy family over an archipelago of
+ *     islands on one device (src/migrate.cc:34-186, src/buffer_manage.cc:36-313), the
+ *     reference's DE_CUDA::Run loop as one call, its DE configuration modes, the tcgen05
+ *     rotation GEMM in BF16 3-term split precision, FP64 re-evaluation of each segment's best,
+ *     and the online MLP surrogate.
  *
  * All pointers to population data are device pointers owned by the caller; no entry point
  * in group 1 allocates or frees device memory.
@@ -63,9 +66,10 @@ extern "C" {
 #define SPEO_DEVERR_WAIT_TIMEOUT  0x4u  /* a bounded device wait gave up                    */
 #define SPEO_DEVERR_BAD_SEGMENT   0x8u  /* a segment descriptor failed the device check     */
 
-/* Objective ids. 9 is CEC2014 F9 (rotated Rastrigin, scale 0.0512), the reference's
- * dispatch id (kernel_CEC2014_CUDA.cu:1704-1706). The reference has no GPU rotated sphere;
- * it gets an id outside the reference's 1..30 range. Both return f(x) - f*. */
+/* Objective ids: 1..30 are the CEC2014 functions of the reference's dispatch
+ * (kernel_CEC2014_CUDA.cu:1672-1797; CPU definitions CUDA_EA_library/CEC2014.cc), 9 being F9
+ * (rotated Rastrigin, scale 0.0512). The reference has no GPU rotated sphere; it gets an id
+ * outside the reference's 1..30 range. All return f(x) - f*. */
 #define SPEO_FUNC_ROTATED_RASTRIGIN  9
 #define SPEO_FUNC_ROTATED_SPHERE     31
 

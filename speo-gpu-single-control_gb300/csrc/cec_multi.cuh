@@ -10,8 +10,8 @@
 // M_c), rescaled as num * f / den; cf07 / cf08 take the hybrids hf01-03 / hf04-06 on (o_c, M_c,
 // S_c). cf_cal (:1481-1520) adds bias_c = 100 c and mixes the components with weights
 // w_c = S_c^-1/2 exp(-S_c / (2 D delta_c^2)), S_c = sum_j (x_j - o_cj)^2.
-// The bodies are the ones of ids 1-16 (schwefel = 10, rastrigin = 8, with those ids' rates and
-// fixed shifts), so every piece runs through RowAcc / row_push / row_finish.
+// The bodies are those of the single-component ids (schwefel = 10, rastrigin = 8, with those
+// ids' rates and fixed shifts), so every piece runs through RowAcc / row_push / row_finish.
 #pragma once
 
 #include "common.cuh"
