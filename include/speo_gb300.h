@@ -279,8 +279,9 @@ SPEO_API int speo_evaluate_tc(const speo_segment *d_segs, const speo_work_item *
  * (DE/<strategy>/bin + reflection), evaluate it, and write the winner of the strict-`<`
  * greedy selection into (pop_out, fit_out). Reads (pop_in, fit_in). *d_gen is read by every
  * block and advanced by one by the last block to finish (d_gen[1] is its scratch word; both
- * start at the caller's values, d_gen[1] = 0). `use_tc` selects the tcgen05 evaluation
- * (tiles of SPEO_TILE_TC rows, D <= 128); otherwise tiles have at most SPEO_TILE_SIMT rows.
+ * start at the caller's values, d_gen[1] = 0). Tiles have at most SPEO_TILE_SIMT rows.
+ * `use_tc` must be 0 (the tensor-core generation is speo_generation_tc, which needs the flat
+ * buffer's extent); 1 returns SPEO_ERR_UNSUPPORTED.
  * trial_out / trial_fit_out (may be NULL) receive every trial vector and its fitness. */
 SPEO_API int speo_generation(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,
                     int dim_lo, int dim_hi, const float *pop_in, const float *fit_in,
@@ -445,6 +446,16 @@ SPEO_API int speo_surrogate_generation(speo_surrogate *s, const speo_segment *d_
                                        long long rows, int ld, int k, const float *pop_in,
                                        const float *fit_in, float *pop_out, float *fit_out,
                                        uint32_t *d_gen, int train_steps, float explore, void *stream);
+
+/* One DE generation with the rotation on the tensor cores, over a flat population of n_rows rows
+ * (stride ld) planned with tiles of at most SPEO_TILE_TC rows: one trial per target
+ * (speo_make_trials, k = 1: the trial draws use tags 1 | 1 << 8 and 2 | 1 << 8), tcgen05 BF16x3
+ * evaluation (speo_evaluate_tc) into trial_fit, strict-`<` selection into (pop_out, fit_out)
+ * (speo_select_rows); *d_gen advances by one. trial / trial_fit: caller scratch of n_rows rows. */
+SPEO_API int speo_generation_tc(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,
+                                int dim_lo, int dim_hi, const float *pop_in, const float *fit_in, float *pop_out,
+                                float *fit_out, int64_t n_rows, int ld, uint32_t *d_gen, float *trial,
+                                float *trial_fit, void *stream);
 
 /* Strict-`<` greedy selection over a flat buffer of `rows` rows (stride ld, a multiple of 4):
  * row r of (pop_out, fit_out) = trial r if trial_fit[r] < fit_in[r], else parent r

@@ -458,9 +458,6 @@ size_t gen_smem(int Q)
 
 using namespace speo;
 
-extern "C" int speo_tc_generation(const speo_segment *, const speo_work_item *, int, int, int, const float *,
-                                  const float *, float *, float *, uint32_t *, float *, float *, void *);
-
 extern "C" int speo_generation(const speo_segment *segs, const speo_work_item *items, int n_items, int dim_lo,
                                int dim_hi, const float *pop_in, const float *fit_in, float *pop_out, float *fit_out,
                                uint32_t *d_gen, int use_tc, float *trial_out, float *trial_fit_out, void *stream)
@@ -471,9 +468,8 @@ extern "C" int speo_generation(const speo_segment *segs, const speo_work_item *i
         return fail(SPEO_ERR_INVALID_ARG, "speo_generation: input and output buffers must differ");
     if (dim_lo < 1 || dim_hi > SPEO_MAX_DIM || dim_lo > dim_hi)
         return fail(SPEO_ERR_INVALID_ARG, "speo_generation: dim range [%d, %d]", dim_lo, dim_hi);
-    if (use_tc)
-        return speo_tc_generation(segs, items, n_items, dim_lo, dim_hi, pop_in, fit_in, pop_out, fit_out, d_gen,
-                                  trial_out, trial_fit_out, stream);
+    if (use_tc)  // the tensor-core generation needs the flat buffer's extent: speo_generation_tc
+        return fail(SPEO_ERR_UNSUPPORTED, "speo_generation: use_tc = 1 is speo_generation_tc (rows, ld, trial buffers)");
     GenArgs a{segs, items, n_items, pop_in, fit_in, pop_out, fit_out, d_gen, trial_out, trial_fit_out};
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int qlo = q_class(dim_lo), qhi = q_class(dim_hi);

@@ -480,8 +480,22 @@ extern "C" int speo_evaluate_tc(const speo_segment *segs, const speo_work_item *
     return check_launch("k_evaluate_tc");
 }
 
-extern "C" int speo_tc_generation(const speo_segment *, const speo_work_item *, int, int, int, const float *,
-                                  const float *, float *, float *, uint32_t *, float *, float *, void *)
+__global__ void k_advance_gen_tc(uint32_t *gen) { gen[0] += 1u; }
+
+extern "C" int speo_generation_tc(const speo_segment *segs, const speo_work_item *items, int n_items, int dim_lo,
+                                  int dim_hi, const float *pop_in, const float *fit_in, float *pop_out,
+                                  float *fit_out, int64_t n_rows, int ld, uint32_t *d_gen, float *trial,
+                                  float *trial_fit, void *stream)
 {
-    return fail(SPEO_ERR_UNSUPPORTED, "speo_generation(use_tc=1): not built yet");
+    if (!segs || !items || !pop_in || !fit_in || !pop_out || !fit_out || !d_gen || !trial || !trial_fit ||
+        n_items < 1 || n_rows < 1)
+        return fail(SPEO_ERR_INVALID_ARG, "speo_generation_tc: bad arguments");
+    if (pop_in == pop_out || fit_in == fit_out || trial == pop_in || trial == pop_out)
+        return fail(SPEO_ERR_INVALID_ARG, "speo_generation_tc: input, output and trial buffers must differ");
+    if (int e = speo_make_trials(segs, items, n_items, dim_hi, 1, pop_in, fit_in, trial, d_gen, stream)) return e;
+    if (int e = speo_evaluate_tc(segs, items, n_items, dim_lo, dim_hi, trial, n_rows, ld, trial_fit, stream))
+        return e;
+    if (int e = speo_select_rows(pop_in, fit_in, trial, trial_fit, pop_out, fit_out, n_rows, ld, stream)) return e;
+    k_advance_gen_tc<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(d_gen);
+    return check_launch("k_advance_gen_tc");
 }

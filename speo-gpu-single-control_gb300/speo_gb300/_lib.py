@@ -124,6 +124,8 @@ SIGNATURES: dict[str, tuple] = {
                                       c_void_p, c_int, c_void_p]),
     "speo_generation_epoch_ex": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
                                          c_void_p, c_void_p, c_int, c_int, c_void_p]),
+    "speo_generation_tc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                   c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "speo_ring_migrate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),
     "speo_ring_migrate_noalloc": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p]),
     "speo_archipelago_state_bytes": (ctypes.c_size_t, [c_void_p]),

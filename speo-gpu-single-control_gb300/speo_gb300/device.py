@@ -139,14 +139,15 @@ class SegmentTable:
                                        self.dim_hi, self.pop[w].data_ptr(), fit.data_ptr(), self._stream()),
                        "speo_evaluate")
 
-    def generation(self, use_tc: bool = False, trial_out: torch.Tensor | None = None,
-                   trial_fit_out: torch.Tensor | None = None):
+    def generation(self, trial_out: torch.Tensor | None = None, trial_fit_out: torch.Tensor | None = None):
+        """One fused generation on the CUDA cores (speo_generation); tc_generation is the
+        tensor-core form."""
         L = _lib.load()
         a, b = self.cur, 1 - self.cur
         _lib.check(L.speo_generation(self.d_segs.data_ptr(), self.d_items.data_ptr(), self.n_items, self.dim_lo,
                                      self.dim_hi, self.pop[a].data_ptr(), self.fit[a].data_ptr(),
                                      self.pop[b].data_ptr(), self.fit[b].data_ptr(), self.gen.data_ptr(),
-                                     int(use_tc), None if trial_out is None else trial_out.data_ptr(),
+                                     0, None if trial_out is None else trial_out.data_ptr(),
                                      None if trial_fit_out is None else trial_fit_out.data_ptr(), self._stream()),
                    "speo_generation")
         self.cur = b
@@ -172,21 +173,12 @@ class SegmentTable:
         be planned with tiles of at most 128 rows."""
         L = _lib.load()
         a, b = self.cur, 1 - self.cur
-        st = self._stream()
-        _lib.check(L.speo_make_trials(self.d_segs.data_ptr(), self.d_items.data_ptr(), self.n_items, self.dim_hi, 1,
-                                      self.pop[a].data_ptr(), self.fit[a].data_ptr(), trial.data_ptr(),
-                                      self.gen.data_ptr(), st), "speo_make_trials")
-        _lib.check(L.speo_evaluate_tc(self.d_segs.data_ptr(), self.d_items.data_ptr(), self.n_items, self.dim_lo,
-                                      self.dim_hi, trial.data_ptr(), self.rows, self.ld, trial_fit.data_ptr(), st),
-                   "speo_evaluate_tc")
-        _lib.check(L.speo_select_rows(self.pop[a].data_ptr(), self.fit[a].data_ptr(), trial.data_ptr(),
-                                      trial_fit.data_ptr(), self.pop[b].data_ptr(), self.fit[b].data_ptr(), self.rows,
-                                      self.ld, st), "speo_select_rows")
-        self._advance_gen()
+        _lib.check(L.speo_generation_tc(self.d_segs.data_ptr(), self.d_items.data_ptr(), self.n_items, self.dim_lo,
+                                        self.dim_hi, self.pop[a].data_ptr(), self.fit[a].data_ptr(),
+                                        self.pop[b].data_ptr(), self.fit[b].data_ptr(), self.rows, self.ld,
+                                        self.gen.data_ptr(), trial.data_ptr(), trial_fit.data_ptr(), self._stream()),
+                   "speo_generation_tc")
         self.cur = b
-
-    def _advance_gen(self):
-        self.gen[0] += 1
 
     def surrogate_generation(self, surrogate, k: int = 8, train_steps: int = 16, explore: float = 0.25):
         """One surrogate-screened generation (speo_surrogate_generation); `surrogate` is an

@@ -628,6 +628,41 @@ def test_evaluate_tc_matches_oracle(oracle, cuda, layout):
     print(f"max relative error of the BF16x3 tensor-core fitness: {worst:.2e}")
 
 
+@pytest.mark.parametrize("layout", [[(128, 100, 9, 4)] * 3 + [(100, 30, 31, 6)], [(200, 50, 4, 4), (70, 64, 13, 2)]])
+def test_generation_tc_matches_oracle(oracle, cuda, layout):
+    """speo_generation_tc: one trial per target (the draws of speo_make_trials with k = 1),
+    tcgen05 BF16x3 evaluation, strict-`<` selection, generation counter advanced; two generations."""
+    import torch
+    from speo_gb300 import _lib
+
+    tab = _table(cuda, layout, n_inst=len(layout), tile_rows=_lib.TILE_TC)
+    tab.init_population()
+    trial = torch.zeros(tab.rows, tab.ld, device=cuda)
+    tfit = torch.zeros(tab.rows, device=cuda)
+    for g in range(2):
+        pin, fin = tab.pop[tab.cur].cpu().numpy(), tab.fit[tab.cur].cpu().numpy()
+        tab.tc_generation(trial, tfit)
+        torch.cuda.synchronize()
+        assert int(tab.gen[0].cpu()) == g + 1
+        got_t, got_f = trial.cpu().numpy(), tfit.cpu().numpy()
+        pout, fout = tab.pop[tab.cur].cpu().numpy(), tab.fit[tab.cur].cpu().numpy()
+        for s in tab.oracle_segments():
+            r0, P, D = s["row0"], s["P"], s["D"]
+            seg = pin[r0:r0 + P]
+            best = int(np.argmin(fin[r0:r0 + P]))
+            cand = np.zeros_like(seg)
+            d = oracle.philox_draws(s["seed"], g, pos0=r0, tag_hi=1 << 8)
+            assert oracle.de_generate(cand, seg, tab.ld, D, np.arange(P), [s["CR"]], [s["F"]], [s["strategy"]], [best],
+                                      s["lb"], s["ub"], d) == 0
+            assert np.array_equal(got_t[r0:r0 + P, :D], cand[:, :D])
+            ref = oracle.evaluate_rows(s["func"], cand, D, s["o"], s["M"])
+            rtol, atol = TC_TOL.get(s["func"], (TC_RTOL, 1e-4))
+            _assert_fitness(got_f[r0:r0 + P], ref, rtol=rtol, atol=atol)
+            win = got_f[r0:r0 + P] < fin[r0:r0 + P]
+            assert np.array_equal(fout[r0:r0 + P], np.where(win, got_f[r0:r0 + P], fin[r0:r0 + P]))
+            assert np.array_equal(pout[r0:r0 + P, :D], np.where(win[:, None], got_t[r0:r0 + P, :D], seg[:, :D]))
+
+
 # The rotated bodies other than 9 / 31 on the tensor cores: the BF16x3 product leaves each z_j
 # with an absolute error of ~2^-16 |x - o| |m_j|, which the bodies amplify as the CUDA-core path's
 # FP32 rounding is amplified (discus 3 weights z_0 by 1e6, Katsuura 12 and Weierstrass 6 multiply
