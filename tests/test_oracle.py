@@ -102,11 +102,11 @@ def _suite_instance(fid, D):
 
 
 @pytest.mark.skipif(not REF_DATA.exists(), reason="reference suite data not present")
-@pytest.mark.parametrize("fid", range(17, 31))
-@pytest.mark.parametrize("D", [10, 30])
-def test_hybrid_composition_on_suite_data(oracle, fid, D):
-    """The reference's own instances of 17-30 (read in place), evaluated by the reference's CEC2014.cc
-    and by the oracle."""
+@pytest.mark.parametrize("fid", range(1, 31))
+@pytest.mark.parametrize("D", [10, 20, 30, 50, 100])
+def test_every_function_on_suite_data(oracle, fid, D):
+    """The reference's own instances of every CEC2014 function (read in place), evaluated by the
+    reference's CEC2014.cc and by the oracle."""
     ref = oracle.ref_lib()
     if ref is None:
         pytest.skip("oracle/_ref not built")
