@@ -188,6 +188,14 @@ SPEO_API int speo_de_run_f32(speo_population_f32 d_population, speo_population_f
                              int *d_best_individual_ID, speo_problem_info_f32 problem_info, const float *d_shift,
                              const float *d_rotated, const int *d_shuffle, int generations, float *h_fitness,
                              int history, void *stream);
+/* The same loop in FP64 (API_DE_GenerateNewPopulation, API_evaluateFitness, API_DE_SelectSurvival),
+ * the precision the reference ships; h_fitness holds doubles. The fused launches keep one
+ * sub-island per block. */
+SPEO_API int speo_de_run_f64(speo_population_f64 d_population, speo_population_f64 d_candidate,
+                             speo_rng_state *d_rng, speo_island_info island_info, speo_de_info_f64 *d_DE_info,
+                             int *d_best_individual_ID, speo_problem_info_f64 problem_info, const double *d_shift,
+                             const double *d_rotated, const int *d_shuffle, int generations, double *h_fitness,
+                             int history, void *stream);
 
 /* Per-sub-island DE parameters, as DE_CUDA::ConfigureEA (CUDA_EA_library/DE_CUDA.cc:89-118)
  * fills them before copying them to the device: `dynamic` = 0 ("constant") gives every

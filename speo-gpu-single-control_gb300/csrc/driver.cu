@@ -23,25 +23,26 @@ constexpr int kStepGens = 100;             // generations per fused launch (at m
 constexpr size_t kHistFloats = 1u << 22;   // bound of one history buffer (16 MiB)
 
 struct DriverHistory {
-    float *p = nullptr;
-    size_t cap = 0;  // floats
+    void *p = nullptr;
+    size_t cap = 0;  // bytes
 };
 thread_local DriverHistory t_hist;
 
 // The device history buffer of this host thread, grown on demand (the previous call has
 // synchronised its stream, so nothing is using the old one).
-int history_buffer(size_t floats, float **out)
+template <typename T>
+int history_buffer(size_t count, T **out)
 {
     DriverHistory &h = t_hist;
-    if (h.cap < floats) {
+    const size_t bytes = sizeof(T) * count;
+    if (h.cap < bytes) {
         if (h.p) cudaFree(h.p);
         h.p = nullptr;
         h.cap = 0;
-        if (int e = check_cuda(cudaMalloc(reinterpret_cast<void **>(&h.p), sizeof(float) * floats), "driver: history"))
-            return e;
-        h.cap = floats;
+        if (int e = check_cuda(cudaMalloc(&h.p, bytes), "driver: history")) return e;
+        h.cap = bytes;
     }
-    *out = h.p;
+    *out = static_cast<T *>(h.p);
     return SPEO_OK;
 }
 
@@ -82,19 +83,64 @@ bool is_pinned(const void *p)
     return a.type == cudaMemoryTypeHost;
 }
 
-}  // namespace
-}  // namespace speo
+// The drop-in entry points and the fused step of one precision.
+inline int gen_call(speo_population_f32 c, speo_population_f32 p, int *b, speo_island_info ii, speo_de_info_f32 *info,
+                    speo_rng_state *r, speo_problem_info_f32 pi)
+{
+    return API_DE_GenerateNewPopulation_f32(c, p, b, ii, info, r, pi);
+}
+inline int gen_call(speo_population_f64 c, speo_population_f64 p, int *b, speo_island_info ii, speo_de_info_f64 *info,
+                    speo_rng_state *r, speo_problem_info_f64 pi)
+{
+    return API_DE_GenerateNewPopulation(c, p, b, ii, info, r, pi);
+}
+inline void eval_call(float *f, float *x, const float *o, const float *m, const int *sh, int n, int d, int fid)
+{
+    API_evaluateFitness_f32(f, nullptr, nullptr, x, const_cast<float *>(o), const_cast<float *>(m),
+                            const_cast<int *>(sh), nullptr, nullptr, nullptr, n, d, 0.f, fid);
+}
+inline void eval_call(double *f, double *x, const double *o, const double *m, const int *sh, int n, int d, int fid)
+{
+    API_evaluateFitness(f, nullptr, nullptr, x, const_cast<double *>(o), const_cast<double *>(m),
+                        const_cast<int *>(sh), nullptr, nullptr, nullptr, n, d, 0.0, fid);
+}
+inline int sel_call(speo_population_f32 p, speo_population_f32 c, speo_island_info ii, speo_problem_info_f32 pi)
+{
+    return API_DE_SelectSurvival_f32(p, c, ii, pi);
+}
+inline int sel_call(speo_population_f64 p, speo_population_f64 c, speo_island_info ii, speo_problem_info_f64 pi)
+{
+    return API_DE_SelectSurvival(p, c, ii, pi);
+}
+inline bool step_fits(float *, const speo_island_info &ii, int dim, int fid)
+{
+    return dropin_step_fits_f32(ii.island_size, ii.subisland_num, dim, fid);
+}
+inline bool step_fits(double *, const speo_island_info &ii, int dim, int fid)
+{
+    return dropin_step_fits_f64(ii.island_size, ii.subisland_num, dim, fid);
+}
+inline int step_call(speo_population_f32 p, speo_population_f32 c, int *b, speo_island_info ii, speo_de_info_f32 *info,
+                     speo_rng_state *r, speo_problem_info_f32 pi, const float *o, const float *m, int k, float *hist,
+                     cudaStream_t st)
+{
+    return dropin_step_f32(p, c, b, ii, info, r, pi, o, m, k, hist, 0, st);
+}
+inline int step_call(speo_population_f64 p, speo_population_f64 c, int *b, speo_island_info ii, speo_de_info_f64 *info,
+                     speo_rng_state *r, speo_problem_info_f64 pi, const double *o, const double *m, int k,
+                     double *hist, cudaStream_t st)
+{
+    return dropin_step_f64(p, c, b, ii, info, r, pi, o, m, k, hist, st);
+}
 
-using namespace speo;
-
-extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand, speo_rng_state *rng,
-                               speo_island_info ii, speo_de_info_f32 *d_info, int *d_best, speo_problem_info_f32 pi,
-                               const float *d_shift, const float *d_rot, const int *d_shuffle, int generations,
-                               float *h_fitness, int history, void *stream)
+template <typename T, typename Pop, typename Info, typename Prob>
+int de_run(Pop pop, Pop cand, speo_rng_state *rng, speo_island_info ii, Info *d_info, int *d_best, Prob pi,
+           const T *d_shift, const T *d_rot, const int *d_shuffle, int generations, T *h_fitness, int history,
+           void *stream, const char *who)
 {
     if (!pop.elements || !pop.fitness_value || !cand.elements || !cand.fitness_value || !rng || !d_info || !d_best ||
         !d_shift || !d_rot || !ii.permutated_index || generations < 0 || ii.island_size <= 0)
-        return fail(SPEO_ERR_INVALID_ARG, "speo_de_run_f32: bad arguments");
+        return fail(SPEO_ERR_INVALID_ARG, "%s: bad arguments", who);
     if (generations == 0) return SPEO_OK;
     DriverStream *d = nullptr;
     if (int e = driver_stream(&d)) return e;
@@ -105,13 +151,13 @@ extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand
     const cudaStream_t prev = api_stream();
     speo_set_stream(d->s);
 
-    const bool fused = dropin_step_fits_f32(ii.island_size, ii.subisland_num, pi.dim, pi.function_ID);
+    const bool fused = step_fits(static_cast<T *>(nullptr), ii, pi.dim, pi.function_ID);
     const bool hist = h_fitness && history;
     int e = SPEO_OK, done = 0;
     if (fused) {
         // two history buffers: launch i writes buffer i % 2 while the copy stream reads the other
         // one back, so the read-back of a block of generations overlaps the next block
-        float *d_hist = nullptr;
+        T *d_hist = nullptr;
         int per = kStepGens;  // generations per launch: the history of one launch within kHistFloats
         if (hist) {
             const size_t cap = kHistFloats / (size_t)n;
@@ -120,14 +166,14 @@ extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand
         }
         for (int i = 0; !e && done < generations; done += per, ++i) {
             const int k = generations - done < per ? generations - done : per, b = i & 1;
-            float *hb = hist ? d_hist + (size_t)b * per * n : nullptr;
+            T *hb = hist ? d_hist + (size_t)b * per * n : nullptr;
             if (hist && i >= 2) e = check_cuda(cudaStreamWaitEvent(d->s, d->read[b], 0), "driver: wait");
-            if (!e) e = dropin_step_f32(pop, cand, d_best, ii, d_info, rng, pi, d_shift, d_rot, k, hb, 0, d->s);
+            if (!e) e = step_call(pop, cand, d_best, ii, d_info, rng, pi, d_shift, d_rot, k, hb, d->s);
             if (!e && hist) {
                 e = check_cuda(cudaEventRecord(d->made[b], d->s), "driver: record");
                 if (!e) e = check_cuda(cudaStreamWaitEvent(d->copy, d->made[b], 0), "driver: wait");
                 if (!e)
-                    e = check_cuda(cudaMemcpyAsync(h_fitness + (size_t)done * n, hb, sizeof(float) * (size_t)k * n,
+                    e = check_cuda(cudaMemcpyAsync(h_fitness + (size_t)done * n, hb, sizeof(T) * (size_t)k * n,
                                                    cudaMemcpyDeviceToHost, d->copy),
                                    "driver: fitness read-back");
                 if (!e) e = check_cuda(cudaEventRecord(d->read[b], d->copy), "driver: record");
@@ -138,7 +184,7 @@ extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand
                 if (int e2 = check_cuda(cudaStreamWaitEvent(d->s, d->read[b], 0), "driver: wait"); e2 && !e) e = e2;
         }
         if (!e && h_fitness && !hist)
-            e = check_cuda(cudaMemcpyAsync(h_fitness, pop.fitness_value, sizeof(float) * (size_t)n,
+            e = check_cuda(cudaMemcpyAsync(h_fitness, pop.fitness_value, sizeof(T) * (size_t)n,
                                            cudaMemcpyDeviceToHost, d->s),
                            "driver: fitness read-back");
     }
@@ -146,18 +192,15 @@ extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand
     // the three entry points in turn; generation g's fitness goes to h_fitness (+ g n with history)
     int g_next = 0;
     auto one_generation = [&](bool in_graph) -> int {
-        if (int e2 = API_DE_GenerateNewPopulation_f32(cand, pop, d_best, ii, d_info, rng, pi)) return e2;
+        if (int e2 = gen_call(cand, pop, d_best, ii, d_info, rng, pi)) return e2;
         const int before = sticky_status();
-        API_evaluateFitness_f32(cand.fitness_value, nullptr, nullptr, cand.elements, const_cast<float *>(d_shift),
-                                const_cast<float *>(d_rot), const_cast<int *>(d_shuffle), nullptr, nullptr, nullptr, n,
-                                pi.dim, 0.f,
-                                pi.function_ID);
+        eval_call(cand.fitness_value, cand.elements, d_shift, d_rot, d_shuffle, n, pi.dim, pi.function_ID);
         if (sticky_status() != before) return sticky_status();
-        if (int e2 = API_DE_SelectSurvival_f32(pop, cand, ii, pi)) return e2;
-        float *dst = h_fitness + (hist && !in_graph ? (size_t)g_next * n : 0);
+        if (int e2 = sel_call(pop, cand, ii, pi)) return e2;
+        T *dst = h_fitness + (hist && !in_graph ? (size_t)g_next * n : 0);
         ++g_next;
         if (h_fitness)
-            return check_cuda(cudaMemcpyAsync(dst, pop.fitness_value, sizeof(float) * (size_t)n,
+            return check_cuda(cudaMemcpyAsync(dst, pop.fitness_value, sizeof(T) * (size_t)n,
                                               cudaMemcpyDeviceToHost, d->s),
                               "driver: fitness read-back");
         return SPEO_OK;
@@ -188,3 +231,27 @@ extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand
     if (!e) e = check_cuda(cudaStreamWaitEvent(caller, d->out, 0), "driver: wait");
     return e;
 }
+
+}  // namespace
+}  // namespace speo
+
+using namespace speo;
+
+extern "C" int speo_de_run_f32(speo_population_f32 pop, speo_population_f32 cand, speo_rng_state *rng,
+                               speo_island_info ii, speo_de_info_f32 *d_info, int *d_best, speo_problem_info_f32 pi,
+                               const float *d_shift, const float *d_rot, const int *d_shuffle, int generations,
+                               float *h_fitness, int history, void *stream)
+{
+    return de_run<float>(pop, cand, rng, ii, d_info, d_best, pi, d_shift, d_rot, d_shuffle, generations, h_fitness,
+                         history, stream, "speo_de_run_f32");
+}
+
+extern "C" int speo_de_run_f64(speo_population_f64 pop, speo_population_f64 cand, speo_rng_state *rng,
+                               speo_island_info ii, speo_de_info_f64 *d_info, int *d_best, speo_problem_info_f64 pi,
+                               const double *d_shift, const double *d_rot, const int *d_shuffle, int generations,
+                               double *h_fitness, int history, void *stream)
+{
+    return de_run<double>(pop, cand, rng, ii, d_info, d_best, pi, d_shift, d_rot, d_shuffle, generations,
+                          h_fitness, history, stream, "speo_de_run_f64");
+}
+

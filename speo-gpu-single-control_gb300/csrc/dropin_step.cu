@@ -561,6 +561,35 @@ bool dropin_step_fits_f32(int island_size, int subisland_num, int dim, int func)
     return step_smem_bytes<float>(q_of(dim), S, dim) <= (size_t)optin;
 }
 
+bool dropin_step_fits_f64(int island_size, int subisland_num, int dim, int func)
+{
+    if (subisland_num < 1 || island_size % subisland_num || dim < 1 || dim > SPEO_MAX_DIM || !func_supported(func))
+        return false;
+    const int S = island_size / subisland_num;
+    if (S < 2) return false;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return step_smem_bytes<double>(q_of(dim), S, dim) <= (size_t)optin;
+}
+
+int dropin_step_f64(speo_population_f64 pop, speo_population_f64 cand, int *d_best, speo_island_info ii,
+                    speo_de_info_f64 *d_info, speo_rng_state *rng, speo_problem_info_f64 pi, const double *shift,
+                    const double *rot, int generations, double *d_hist, cudaStream_t st)
+{
+    if (generations < 1) return SPEO_OK;
+    StepArgs<double> a{pop.elements, pop.fitness_value, cand.elements, cand.fitness_value, pi.dim,
+                       ii.island_size / ii.subisland_num, ii.permutated_index, d_info, d_best,
+                       pi.min_bound, pi.max_bound, reinterpret_cast<RngState *>(rng), shift, rot,
+                       pi.function_ID, generations, ii.island_size, d_hist};
+    switch (q_of(pi.dim)) {
+    case 1: return launch_step<double, 1>(a, ii.subisland_num, st);
+    case 2: return launch_step<double, 2>(a, ii.subisland_num, st);
+    case 4: return launch_step<double, 4>(a, ii.subisland_num, st);
+    default: return launch_step<double, 8>(a, ii.subisland_num, st);
+    }
+}
+
 int dropin_step_f32(speo_population_f32 pop, speo_population_f32 cand, int *d_best, speo_island_info ii,
                     speo_de_info_f32 *d_info, speo_rng_state *rng, speo_problem_info_f32 pi, const float *shift,
                     const float *rot, int generations, float *d_hist, int pair_mode, cudaStream_t st)

@@ -106,6 +106,8 @@ SIGNATURES: dict[str, tuple] = {
     "speo_configure_de_f64": (c_int, [c_void_p, c_int, c_int, c_double, c_double, c_int, c_int, c_uint64]),
     "speo_de_run_f32": (c_int, [PopulationF32, PopulationF32, c_void_p, IslandInfo, c_void_p, c_void_p, ProblemInfoF32,
                                 c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p]),
+    "speo_de_run_f64": (c_int, [PopulationF64, PopulationF64, c_void_p, IslandInfo, c_void_p, c_void_p, ProblemInfoF64,
+                                c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_void_p]),
     "API_evaluateFitness": (None, [c_void_p] * 10 + [c_int, c_int, c_double, c_int]),
     "API_evaluateFitness_f32": (None, [c_void_p] * 10 + [c_int, c_int, c_float, c_int]),
     "speo_set_stream": (c_int, [c_void_p]),

@@ -132,10 +132,11 @@ def test_dropin_generate_matches_oracle(lib, oracle, cuda, f64, P, D, nsub):
     (24, True, False, 300, 50, 3, 30, (4, 6, 2)),    # composition of hybrids: graph blocks
     (5, False, True, 120, 20, 2, 21, (6,)),          # hybrid, pageable buffer
 ])
-def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned, history, P, D, nsub, fid, strats):
-    """speo_de_run_f32 (the reference's DE_CUDA::Run loop, natively: sub-islands resident in shared
-    memory for blocks of generations, on two-block clusters when the GPU has SMs for two blocks per
-    sub-island, or the three calls replayed as a CUDA graph) gives the same
+@pytest.mark.parametrize("f64", [False, True])
+def test_de_run_matches_the_dropin_loop(lib, cuda, f64, gens, pinned, history, P, D, nsub, fid, strats):
+    """speo_de_run_f32 / _f64 (the reference's DE_CUDA::Run loop, natively: sub-islands resident in
+    shared memory for blocks of generations, in FP32 on two-block clusters when the GPU has SMs for
+    two blocks per sub-island, or the three calls replayed as a CUDA graph) gives the same
     populations, candidates, best ids, generation counter and per-generation fitness as the drop-in
     calls issued one by one."""
     import torch
@@ -143,22 +144,24 @@ def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned, history, P, D, 
 
     o, M, S = make_instance_multi(77, D, fid)       # component 0 = make_instance(77, D)
     nc, ld = o.shape[0], np2(D)
-    rot = np.zeros((nc, ld, D), dtype=np.float32)
+    dt = np.float64 if f64 else np.float32
+    rot = np.zeros((nc, ld, D), dtype=dt)
     rot[:, :D] = M.transpose(0, 2, 1)
-    shift = np.zeros((nc, ld), dtype=np.float32)
+    shift = np.zeros((nc, ld), dtype=dt)
     shift[:, :D] = o
     shuf = np.zeros((nc, ld), dtype=np.int32)
     shuf[:, :D] = S
     d_rot, d_sh = torch.from_numpy(rot).to(cuda), torch.from_numpy(shift).to(cuda)
     d_sf = torch.from_numpy(shuf).to(cuda)
     rng = np.random.default_rng(9)
-    pop0 = np.zeros((P, ld), dtype=np.float32)
+    pop0 = np.zeros((P, ld), dtype=dt)
     pop0[:, :D] = rng.uniform(-100, 100, (P, D))
     runs = []
     perm = np.random.default_rng(P + D).permutation(P).astype(np.int32)
     for mode in ("calls", "driver"):
-        d = DropIn(lib, cuda, P, D, nsub, False, seed=4321)
+        d = DropIn(lib, cuda, P, D, nsub, f64, seed=4321)
         d.problem.function_ID = fid
+        evaluate = getattr(d.lib, "API_evaluateFitness" + d.sfx)
         d.perm.copy_(torch.from_numpy(perm))
         info = (d.DI * nsub)(*[d.DI(0.9 if i % 2 == 0 else 0.1, 0.5, strats[i % len(strats)], P // nsub)
                                for i in range(nsub)])
@@ -168,25 +171,25 @@ def test_de_run_matches_the_dropin_loop(lib, cuda, gens, pinned, history, P, D, 
         d.pop.copy_(torch.from_numpy(pop0))
         args = (None, None, d.pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(), d_sf.data_ptr(), None, None, None, P,
                 D, 0.0, fid)
-        d.lib.API_evaluateFitness_f32(d.pfit.data_ptr(), *args)
+        evaluate(d.pfit.data_ptr(), *args)
         if mode == "calls":
             per_gen = []
             for _ in range(gens):
                 d.call("API_DE_GenerateNewPopulation", cand_s, pop_s, d.best.data_ptr(), d.island(),
                        d_info.data_ptr(), d.rng.data_ptr(), d.problem)
-                d.lib.API_evaluateFitness_f32(d.cfit.data_ptr(), None, None, d.cand.data_ptr(), d_sh.data_ptr(),
-                                              d_rot.data_ptr(), d_sf.data_ptr(), None, None, None, P, D, 0.0, fid)
+                evaluate(d.cfit.data_ptr(), None, None, d.cand.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(),
+                         d_sf.data_ptr(), None, None, None, P, D, 0.0, fid)
                 d.call("API_DE_SelectSurvival", pop_s, cand_s, d.island(), d.problem)
                 per_gen.append(d.pfit.cpu().numpy())
             h = np.stack(per_gen)
         else:
-            h = torch.zeros((gens if history else 1) * P, dtype=torch.float32)
+            h = torch.zeros((gens if history else 1) * P, dtype=d.dt)
             if pinned:
                 h = h.pin_memory()
-            d._lib.check(d.lib.speo_de_run_f32(pop_s, cand_s, d.rng.data_ptr(), d.island(), d_info.data_ptr(),
-                                               d.best.data_ptr(), d.problem, d_sh.data_ptr(), d_rot.data_ptr(),
-                                               d_sf.data_ptr(), gens,
-                                               h.data_ptr(), int(history), None), "speo_de_run_f32")
+            run = getattr(d.lib, "speo_de_run" + ("_f64" if f64 else "_f32"))
+            d._lib.check(run(pop_s, cand_s, d.rng.data_ptr(), d.island(), d_info.data_ptr(), d.best.data_ptr(),
+                             d.problem, d_sh.data_ptr(), d_rot.data_ptr(), d_sf.data_ptr(), gens, h.data_ptr(),
+                             int(history), None), "speo_de_run")
             h = h.numpy().reshape(-1, P)
         d._lib.check(d.lib.API_CheckCUDAError(), "API_CheckCUDAError")
         runs.append((d.pop.cpu().numpy(), d.pfit.cpu().numpy(), h.copy(),

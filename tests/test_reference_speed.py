@@ -5,7 +5,7 @@ compiled unmodified for sm_103a into oracle/_ref/*.fatbin; FP64 as shipped, FP32
 real = float shim) run DE_CUDA::Run's sequence (DE_CUDA.cc:200-216): best search, generate, F9
 shift-and-rotate + Rastrigin, select, with the device synchronisation its CudaCheckError does
 after each DE launch (kernel_DE_CUDA.cu:23-46). This library runs the same sequence through its
-drop-in entry points with the same synchronisations, and (FP32) as one speo_de_run_f32 call.
+drop-in entry points with the same synchronisations, and as one speo_de_run_f32 / _f64 call.
 Workload: one island of 6400 rows in 64 sub-islands of 100, D = 30, F9, DE/rand/1/bin CR 0.9
 F 0.5. Prints one JSON line with the rates; asserts this library's loop is the faster one.
 """
@@ -123,15 +123,15 @@ def test_generation_loop_against_reference_kernels(lib, cuda, prec, capsys):
     for _ in range(G):
         generation()
     rates["library_dropin_calls"] = P * G / (time.perf_counter() - t0)
-    if not f64:  # the same loop as one library call
-        h = torch.zeros(P, dtype=torch.float32).pin_memory()
-        run = lambda k: _lib.check(lib.speo_de_run_f32(b["P"], b["C"], rng.data_ptr(), b["ii"], d_info.data_ptr(),
-                                                       b["best"].data_ptr(), problem, d_sh.data_ptr(),
-                                                       d_mt.data_ptr(), None, k, h.data_ptr(), 0, None), "run")
-        run(25)
-        t0 = time.perf_counter()
-        run(G * 5)
-        rates["library_speo_de_run_f32"] = P * G * 5 / (time.perf_counter() - t0)
+    # the same loop as one library call
+    h = torch.zeros(P, dtype=dt).pin_memory()
+    de_run = getattr(lib, "speo_de_run_" + prec)
+    run = lambda k: _lib.check(de_run(b["P"], b["C"], rng.data_ptr(), b["ii"], d_info.data_ptr(), b["best"].data_ptr(),
+                                      problem, d_sh.data_ptr(), d_mt.data_ptr(), None, k, h.data_ptr(), 0, None), "run")
+    run(25)
+    t0 = time.perf_counter()
+    run(G * 5)
+    rates["library_speo_de_run_" + prec] = P * G * 5 / (time.perf_counter() - t0)
     with capsys.disabled():
         print("\n" + json.dumps({"reference_speed": {"precision": prec, "rows": P, "dim": D, "subislands": nsub,
                                                      "function": 9, "evals_per_s": rates,
@@ -145,8 +145,8 @@ def test_published_configuration_against_reference_kernels(lib, cuda, prec, caps
     DE/rand/1/bin CR 0.9 F 0.5) through the reference's own kernels on this GPU: best search,
     generate, CompFunc1's launch sequence (4 x ShiftAndRotation + f4/f1/f2/f3, Shift + f1, CalW,
     CombineFitness; kernel_CEC2014_CUDA.cu:1416-1451), select, with the reference's
-    synchronisations; beside this library's drop-in calls (same synchronisations) and, in FP32,
-    speo_de_run_f32."""
+    synchronisations; beside this library's drop-in calls (same synchronisations) and
+    speo_de_run_f32 / _f64."""
     if not rk.available(prec, ("de", "ea", "cec")):
         pytest.skip("reference fatbins not built (needs the reference sources at build time)")
     import torch
@@ -263,15 +263,15 @@ def test_published_configuration_against_reference_kernels(lib, cuda, prec, caps
     for _ in range(G):
         generation()
     rates["library_dropin_calls"] = P * G / (time.perf_counter() - t0)
-    if not f64:
-        h = torch.zeros(P, dtype=torch.float32).pin_memory()
-        run = lambda k: _lib.check(lib.speo_de_run_f32(b["P"], b["C"], rng.data_ptr(), b["ii"], d_info.data_ptr(),
-                                                       b["best"].data_ptr(), problem, d_sh.data_ptr(),
-                                                       d_rot.data_ptr(), None, k, h.data_ptr(), 0, None), "run")
-        run(10)
-        t0 = time.perf_counter()
-        run(G * 5)
-        rates["library_speo_de_run_f32"] = P * G * 5 / (time.perf_counter() - t0)
+    h = torch.zeros(P, dtype=dt).pin_memory()
+    de_run = getattr(lib, "speo_de_run_" + prec)
+    run = lambda k: _lib.check(de_run(b["P"], b["C"], rng.data_ptr(), b["ii"], d_info.data_ptr(), b["best"].data_ptr(),
+                                      problem, d_sh.data_ptr(), d_rot.data_ptr(), None, k, h.data_ptr(), 0, None),
+                               "run")
+    run(10)
+    t0 = time.perf_counter()
+    run(G * 5)
+    rates["library_speo_de_run_" + prec] = P * G * 5 / (time.perf_counter() - t0)
     with capsys.disabled():
         print("\n" + json.dumps({"published_configuration_speed": {"precision": prec, "rows": P, "dim": D,
                                                                    "function": fid, "evals_per_s": rates}}))
