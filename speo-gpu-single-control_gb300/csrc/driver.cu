@@ -130,7 +130,7 @@ inline int step_call(speo_population_f64 p, speo_population_f64 c, int *b, speo_
                      speo_rng_state *r, speo_problem_info_f64 pi, const double *o, const double *m, int k,
                      double *hist, cudaStream_t st)
 {
-    return dropin_step_f64(p, c, b, ii, info, r, pi, o, m, k, hist, st);
+    return dropin_step_f64(p, c, b, ii, info, r, pi, o, m, k, hist, 0, st);
 }
 
 template <typename T, typename Pop, typename Info, typename Prob>

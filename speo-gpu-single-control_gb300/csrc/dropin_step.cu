@@ -291,36 +291,49 @@ int launch_step(const StepArgs<T> &a, int nsub, cudaStream_t st)
 // buffer g % 2), and runs the draws, trials, evaluation and selection of half of the positions. Its
 // new rows (winner or parent) go to the next buffer of both replicas, the peer's through
 // distributed shared memory; one cluster barrier per generation makes both replicas whole. The
-// per-row arithmetic is k_de_step's, so the results are bit-identical. FP32.
+// per-row arithmetic is k_de_step's, so the results are bit-identical. FP32 and FP64.
 constexpr int kRowsPerWarp2 = 4;
 constexpr int kPassRows2 = kWarpsS * kRowsPerWarp2;  // 64 rows per evaluation pass
 
 __host__ __device__ inline int half_pos(int S) { return (S + 1) / 2; }
 
 //   Xp[2][S][W] fp[2][round_up(S,4)] | Xt[h][W] | Yt[hp][W] | Ms[D][W] | sF[hp] | o[W] | sR[GB][h][8]
+template <typename T>
 __host__ __device__ inline size_t step2_smem_bytes(int Q, int S, int D)
 {
     const size_t W = 32 * (size_t)Q, h = half_pos(S), hp = round_up_i((int)h, kPassRows2);
-    return sizeof(float) * (2 * ((size_t)S * W + round_up_i(S, 4)) + h * W + hp * W + (size_t)D * W + hp + W) +
+    return sizeof(T) * (2 * ((size_t)S * W + round_up_i(S, 4)) + h * W + hp * W + (size_t)D * W + hp + W) +
            sizeof(int) * (size_t)step_draw_gens((int)h) * h * 8;
 }
 
-template <int Q, bool G>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_step2(StepArgs<float> a)
+// A row chunk (one vector) or a fitness value into the peer block's shared memory.
+__device__ __forceinline__ void st_peer_v(uint32_t addr, float4 v) { st_peer4(addr, v); }
+__device__ __forceinline__ void st_peer_v(uint32_t addr, double2 v)
 {
-    using V = float4;
-    constexpr int VN = 4, W = 32 * Q;
+    asm volatile("st.shared::cluster.v2.f64 [%0], {%1, %2};" ::"r"(addr), "d"(v.x), "d"(v.y) : "memory");
+}
+__device__ __forceinline__ void st_peer_s(uint32_t addr, float v) { st_peer1(addr, v); }
+__device__ __forceinline__ void st_peer_s(uint32_t addr, double v)
+{
+    asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(addr), "d"(v) : "memory");
+}
+
+template <typename T, int Q, bool G>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_step2(StepArgs<T> a)
+{
+    using V = typename Vec<T>::type;
+    constexpr int VN = Vec<T>::n, W = 32 * Q;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int S = a.S, D = a.D, h = half_pos(S), hp = round_up_i(h, kPassRows2), Sf = round_up_i(S, 4);
-    float *const Xp0 = reinterpret_cast<float *>(smem_raw);  // buffer b at Xp0 + b * S * W
-    float *const fp0 = Xp0 + 2 * (size_t)S * W;              // buffer b at fp0 + b * Sf
-    float *Xt = fp0 + 2 * Sf;
-    float *Yt = Xt + (size_t)h * W;
-    float *Ms = Yt + (size_t)hp * W;
-    float *sF = Ms + (size_t)D * W;
-    float *so = sF + hp;
+    T *const Xp0 = reinterpret_cast<T *>(smem_raw);  // buffer b at Xp0 + b * S * W
+    T *const fp0 = Xp0 + 2 * (size_t)S * W;              // buffer b at fp0 + b * Sf
+    T *Xt = fp0 + 2 * Sf;
+    T *Yt = Xt + (size_t)h * W;
+    T *Ms = Yt + (size_t)hp * W;
+    T *sF = Ms + (size_t)D * W;
+    T *so = sF + hp;
     int *sR = reinterpret_cast<int *>(so + W);
-    __shared__ float s_bf[kWarpsS];
+    __shared__ T s_bf[kWarpsS];
     __shared__ int s_bp[kWarpsS];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -332,11 +345,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
     const uint2 key = make_uint2(a.rng->key0, a.rng->key1);
     const int nch = (D + VN - 1) / VN;
     const int GB = step_draw_gens(h);
-    const float F = a.info[isl].F;
-    const uint32_t thr = cr_threshold<float>(a.info[isl].CR);
+    const T F = a.info[isl].F;
+    const uint32_t thr = cr_threshold<T>(a.info[isl].CR);
     const int st = a.info[isl].strategy_ID;
     const int nd = ndonors(st);
-    const float scale = func_scale(a.func);
+    const T scale = sizeof(T) == 4 ? (T)func_scale(a.func) : (T)func_scale_f64(a.func);
 
     for (int i = tid; i < S * (W / VN); i += kThreadsS) {
         const int p = i / (W / VN), c = i - p * (W / VN);
@@ -344,19 +357,19 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
             reinterpret_cast<const V *>(a.pop + (size_t)a.perm[base + p] * W)[c];
     }
     for (int p = tid; p < S; p += kThreadsS) fp0[p] = a.pfit[a.perm[base + p]];
-    load_rot_rows<float, Q>(Ms, a.rot, D, D, 0, D);
-    for (int k = tid; k < W; k += kThreadsS) so[k] = k < D ? a.shift[k] : 0.f;
-    for (int i = tid; i < (hp - np) * W; i += kThreadsS) Yt[(size_t)np * W + i] = 0.f;
+    load_rot_rows<T, Q>(Ms, a.rot, D, D, 0, D);
+    for (int k = tid; k < W; k += kThreadsS) so[k] = k < D ? a.shift[k] : T(0);
+    for (int i = tid; i < (hp - np) * W; i += kThreadsS) Yt[(size_t)np * W + i] = T(0);
     if (nch * VN < W) {
         const int tail = W - nch * VN;
         for (int i = tid; i < np * tail; i += kThreadsS) {
             const int p = i / tail, k = nch * VN + (i - p * tail);
-            Xt[(size_t)p * W + k] = 0.f;
-            Yt[(size_t)p * W + k] = 0.f;
+            Xt[(size_t)p * W + k] = T(0);
+            Yt[(size_t)p * W + k] = T(0);
         }
         for (int i = tid; i < S * tail; i += kThreadsS) {  // and in the second population buffer
             const int p = i / tail, k = nch * VN + (i - p * tail);
-            Xp0[(size_t)S * W + (size_t)p * W + k] = 0.f;
+            Xp0[(size_t)S * W + (size_t)p * W + k] = T(0);
         }
     }
     const uint32_t peer_xp = map_peer(Xp0, peer), peer_fp = map_peer(fp0, peer);
@@ -367,17 +380,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
         const uint32_t gen = gen0 + (uint32_t)g;
         const bool last = g == a.gens - 1;
         const int cur = g & 1, nxt = cur ^ 1;
-        const float *Xp = Xp0 + (size_t)cur * S * W;
-        const float *fp = fp0 + cur * Sf;
+        const T *Xp = Xp0 + (size_t)cur * S * W;
+        const T *fp = fp0 + cur * Sf;
         {  // (the previous generation's cluster barrier ordered every access before this point)
-            float bf = INFINITY;
+            T bf = T(INFINITY);
             int bp = 0x7fffffff;
             for (int p = tid; p < S; p += kThreadsS) {
-                const float f = rank_t(fp[p]);
+                const T f = rank_t(fp[p]);
                 if (f < bf || (f == bf && p < bp)) { bf = f; bp = p; }
             }
             for (int o = 16; o > 0; o >>= 1) {
-                const float of = __shfl_xor_sync(0xffffffffu, bf, o);
+                const T of = __shfl_xor_sync(0xffffffffu, bf, o);
                 const int op = __shfl_xor_sync(0xffffffffu, bp, o);
                 if (of < bf || (of == bf && op < bp)) { bf = of; bp = op; }
             }
@@ -399,16 +412,16 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
         __syncthreads();
         int bp = s_bp[0];
         {
-            float bf = s_bf[0];
+            T bf = s_bf[0];
             for (int w = 1; w < kWarpsS; ++w)
                 if (s_bf[w] < bf || (s_bf[w] == bf && s_bp[w] < bp)) { bf = s_bf[w]; bp = s_bp[w]; }
         }
         if (last && me == 0 && tid == 0) a.best_id[isl] = a.perm[base + bp];
         const int *sRg = sR + (g % GB) * h * 8;
-        float *nXp = Xp0 + (size_t)nxt * S * W;
-        float *nfp = fp0 + nxt * Sf;
-        const uint32_t pxp = peer_xp + (uint32_t)((size_t)nxt * S * W * sizeof(float));
-        const uint32_t pfp = peer_fp + (uint32_t)(nxt * Sf * sizeof(float));
+        T *nXp = Xp0 + (size_t)nxt * S * W;
+        T *nfp = fp0 + nxt * Sf;
+        const uint32_t pxp = peer_xp + (uint32_t)((size_t)nxt * S * W * sizeof(T));
+        const uint32_t pfp = peer_fp + (uint32_t)(nxt * Sf * sizeof(T));
         // trials, evaluation and selection per warp, for its kRowsPerWarp2 positions of each
         // 64-position pass: a position's trial, fitness and selection stay in its warp
         for (int pb = 0; pb < np; pb += kPassRows2) {
@@ -419,8 +432,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
                 const int lp = lr0 + t / nch, c = t % nch;
                 const int p = pb0 + lp, pos = base + p;
                 const int e0 = VN * c;
-                const float *xi = Xp + (size_t)p * W;
-                const float *xb = Xp + (size_t)(strategy_uses_best(st) ? bp : p) * W;
+                const T *xi = Xp + (size_t)p * W;
+                const T *xb = Xp + (size_t)(strategy_uses_best(st) ? bp : p) * W;
                 const V ti = *reinterpret_cast<const V *>(xi + e0);
                 const V tb = strategy_uses_best(st) ? *reinterpret_cast<const V *>(xb + e0) : ti;
                 V tr[5];
@@ -433,48 +446,48 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
 #pragma unroll
                 for (int q = 0; q < VN; ++q) {
                     const int e = e0 + q;
-                    float v;
+                    T v;
                     if (e == jr || cr_take(pick(w, (uint32_t)(e & 3)), thr)) {
-                        float xr[5];
+                        T xr[5];
 #pragma unroll
-                        for (int k = 0; k < 5; ++k) xr[k] = vget<float>(tr[k], q);
-                        v = mutant<float>(st, F, vget<float>(ti, q), vget<float>(tb, q), xr);
+                        for (int k = 0; k < 5; ++k) xr[k] = vget<T>(tr[k], q);
+                        v = mutant<T>(st, F, vget<T>(ti, q), vget<T>(tb, q), xr);
                     } else {
-                        v = vget<float>(ti, q);
+                        v = vget<T>(ti, q);
                     }
-                    vset<float>(x, q, check_bound<float>(v, a.lb, a.ub, ok_bound));
+                    vset<T>(x, q, check_bound<T>(v, a.lb, a.ub, ok_bound));
                 }
                 *reinterpret_cast<V *>(Xt + (size_t)lp * W + e0) = x;
                 V y;
 #pragma unroll
                 for (int q = 0; q < VN; ++q) {
                     const int e = e0 + q;
-                    vset<float>(y, q, e < D ? sub_rn(vget<float>(x, q), so[e]) : 0.f);
+                    vset<T>(y, q, e < D ? sub_rn(vget<T>(x, q), so[e]) : T(0));
                 }
                 *reinterpret_cast<V *>(Yt + (size_t)lp * W + e0) = y;
                 if (last) {
-                    float *out = a.cand + (size_t)a.perm[pos] * W;
+                    T *out = a.cand + (size_t)a.perm[pos] * W;
                     if (e0 + VN <= D) {
                         *reinterpret_cast<V *>(out + e0) = x;
                     } else {
 #pragma unroll
                         for (int q = 0; q < VN; ++q)
-                            if (e0 + q < D) out[e0 + q] = vget<float>(x, q);
+                            if (e0 + q < D) out[e0 + q] = vget<T>(x, q);
                     }
                 }
             }
             __syncwarp();
-            float acc[kRowsPerWarp2][Q];
+            T acc[kRowsPerWarp2][Q];
 #pragma unroll
             for (int rr = 0; rr < kRowsPerWarp2; ++rr)
 #pragma unroll
-                for (int q = 0; q < Q; ++q) acc[rr][q] = 0.f;
+                for (int q = 0; q < Q; ++q) acc[rr][q] = T(0);
             if (func_rotated(a.func))
-                eval_accumulate<float, Q>(acc, Yt, W, lr0, Ms, W, 0, D, lane);
+                eval_accumulate<T, Q>(acc, Yt, W, lr0, Ms, W, 0, D, lane);
             else
-                eval_identity<float, Q>(acc, Yt, W, lr0, D, lane);
-            float f[kRowsPerWarp2];
-            eval_reduce<float, Q, kRowsPerWarp2, G>(acc, D, a.func, scale, lane, f);
+                eval_identity<T, Q>(acc, Yt, W, lr0, D, lane);
+            T f[kRowsPerWarp2];
+            eval_reduce<T, Q, kRowsPerWarp2, G>(acc, D, a.func, scale, lane, f);
             if (lane == 0)
 #pragma unroll
                 for (int rr = 0; rr < kRowsPerWarp2; ++rr) sF[lr0 + rr] = f[rr];
@@ -482,16 +495,16 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
             // selection into the next buffer of both replicas
             for (int t = lane; t < nrw * nch; t += 32) {
                 const int lp = lr0 + t / nch, c = t % nch, p = pb0 + lp;
-                const float tf = sF[lp];
+                const T tf = sF[lp];
                 const bool win = tf < fp[p];
                 const V v = *reinterpret_cast<const V *>((win ? Xt + (size_t)lp * W : Xp + (size_t)p * W) + VN * c);
                 *reinterpret_cast<V *>(nXp + (size_t)p * W + VN * c) = v;
-                st_peer4(pxp + (uint32_t)(((size_t)p * W + VN * c) * sizeof(float)), v);
+                st_peer_v(pxp + (uint32_t)(((size_t)p * W + VN * c) * sizeof(T)), v);
                 if (c == 0) {
                     const int row = a.perm[base + p];
-                    const float nf = win ? tf : fp[p];
+                    const T nf = win ? tf : fp[p];
                     nfp[p] = nf;
-                    st_peer1(pfp + (uint32_t)(p * sizeof(float)), nf);
+                    st_peer_s(pfp + (uint32_t)(p * sizeof(T)), nf);
                     if (last) a.cfit[row] = tf;
                     if (a.hist) a.hist[(size_t)g * a.P + row] = nf;
                 }
@@ -500,18 +513,18 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
         cluster_sync();
     }
     // this block's rows and fitness back (elements past D are never written)
-    const float *Xp = Xp0 + (size_t)(a.gens & 1) * S * W;
-    const float *fp = fp0 + (a.gens & 1) * Sf;
+    const T *Xp = Xp0 + (size_t)(a.gens & 1) * S * W;
+    const T *fp = fp0 + (a.gens & 1) * Sf;
     for (int t = tid; t < np * nch; t += kThreadsS) {
         const int lp = t / nch, c = t - lp * nch, e0 = VN * c, p = pb0 + lp;
-        float *dst = a.pop + (size_t)a.perm[base + p] * W;
+        T *dst = a.pop + (size_t)a.perm[base + p] * W;
         const V v = *reinterpret_cast<const V *>(Xp + (size_t)p * W + e0);
         if (e0 + VN <= D) {
             *reinterpret_cast<V *>(dst + e0) = v;
         } else {
 #pragma unroll
             for (int q = 0; q < VN; ++q)
-                if (e0 + q < D) dst[e0 + q] = vget<float>(v, q);
+                if (e0 + q < D) dst[e0 + q] = vget<T>(v, q);
         }
     }
     for (int lp = tid; lp < np; lp += kThreadsS) a.pfit[a.perm[base + pb0 + lp]] = fp[pb0 + lp];
@@ -529,20 +542,20 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
     }
 }
 
-template <int Q, bool G>
-int launch_step2_v(const StepArgs<float> &a, int nsub, cudaStream_t st)
+template <typename T, int Q, bool G>
+int launch_step2_v(const StepArgs<T> &a, int nsub, cudaStream_t st)
 {
-    const size_t smem = step2_smem_bytes(Q, a.S, a.D);
-    cudaError_t e = cudaFuncSetAttribute(k_de_step2<Q, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t smem = step2_smem_bytes<T>(Q, a.S, a.D);
+    cudaError_t e = cudaFuncSetAttribute(k_de_step2<T, Q, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_de_step2)");
-    k_de_step2<Q, G><<<2 * nsub, kThreadsS, smem, st>>>(a);
+    k_de_step2<T, Q, G><<<2 * nsub, kThreadsS, smem, st>>>(a);
     return check_launch("k_de_step2");
 }
 
-template <int Q>
-int launch_step2(const StepArgs<float> &a, int nsub, cudaStream_t st)
+template <typename T, int Q>
+int launch_step2(const StepArgs<T> &a, int nsub, cudaStream_t st)
 {
-    return func_sum_form(a.func) ? launch_step2_v<Q, false>(a, nsub, st) : launch_step2_v<Q, true>(a, nsub, st);
+    return func_sum_form(a.func) ? launch_step2_v<T, Q, false>(a, nsub, st) : launch_step2_v<T, Q, true>(a, nsub, st);
 }
 
 int q_of(int D) { return D <= 32 ? 1 : D <= 64 ? 2 : D <= 128 ? 4 : 8; }
@@ -573,21 +586,47 @@ bool dropin_step_fits_f64(int island_size, int subisland_num, int dim, int func)
     return step_smem_bytes<double>(q_of(dim), S, dim) <= (size_t)optin;
 }
 
+namespace {
+
+// Two-block clusters when there are SMs for two blocks per sub-island and the replicas fit, else
+// one block per sub-island.
+template <typename T>
+int run_step(const StepArgs<T> &a, int nsub, int pair_mode, cudaStream_t st)
+{
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const int Q = q_of(a.D);
+    const bool pair = pair_mode != 1 && a.S >= 4 && (pair_mode == 2 || 2LL * nsub <= sm_count()) &&
+                      step2_smem_bytes<T>(Q, a.S, a.D) <= (size_t)optin;
+    if (pair) {
+        switch (Q) {
+        case 1: return launch_step2<T, 1>(a, nsub, st);
+        case 2: return launch_step2<T, 2>(a, nsub, st);
+        case 4: return launch_step2<T, 4>(a, nsub, st);
+        default: return launch_step2<T, 8>(a, nsub, st);
+        }
+    }
+    switch (Q) {
+    case 1: return launch_step<T, 1>(a, nsub, st);
+    case 2: return launch_step<T, 2>(a, nsub, st);
+    case 4: return launch_step<T, 4>(a, nsub, st);
+    default: return launch_step<T, 8>(a, nsub, st);
+    }
+}
+
+}  // namespace
+
 int dropin_step_f64(speo_population_f64 pop, speo_population_f64 cand, int *d_best, speo_island_info ii,
                     speo_de_info_f64 *d_info, speo_rng_state *rng, speo_problem_info_f64 pi, const double *shift,
-                    const double *rot, int generations, double *d_hist, cudaStream_t st)
+                    const double *rot, int generations, double *d_hist, int pair_mode, cudaStream_t st)
 {
     if (generations < 1) return SPEO_OK;
     StepArgs<double> a{pop.elements, pop.fitness_value, cand.elements, cand.fitness_value, pi.dim,
                        ii.island_size / ii.subisland_num, ii.permutated_index, d_info, d_best,
                        pi.min_bound, pi.max_bound, reinterpret_cast<RngState *>(rng), shift, rot,
                        pi.function_ID, generations, ii.island_size, d_hist};
-    switch (q_of(pi.dim)) {
-    case 1: return launch_step<double, 1>(a, ii.subisland_num, st);
-    case 2: return launch_step<double, 2>(a, ii.subisland_num, st);
-    case 4: return launch_step<double, 4>(a, ii.subisland_num, st);
-    default: return launch_step<double, 8>(a, ii.subisland_num, st);
-    }
+    return run_step(a, ii.subisland_num, pair_mode, st);
 }
 
 int dropin_step_f32(speo_population_f32 pop, speo_population_f32 cand, int *d_best, speo_island_info ii,
@@ -599,27 +638,7 @@ int dropin_step_f32(speo_population_f32 pop, speo_population_f32 cand, int *d_be
                       ii.island_size / ii.subisland_num, ii.permutated_index, d_info, d_best,
                       (float)pi.min_bound, (float)pi.max_bound, reinterpret_cast<RngState *>(rng), shift, rot,
                       pi.function_ID, generations, ii.island_size, d_hist};
-    // two-block clusters when there are SMs for two blocks per sub-island and the replicas fit
-    int dev = 0, optin = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const int S = ii.island_size / ii.subisland_num, Q = q_of(pi.dim);
-    const bool pair = pair_mode != 1 && S >= 4 && (pair_mode == 2 || 2LL * ii.subisland_num <= sm_count()) &&
-                      step2_smem_bytes(Q, S, pi.dim) <= (size_t)optin;
-    if (pair) {
-        switch (Q) {
-        case 1: return launch_step2<1>(a, ii.subisland_num, st);
-        case 2: return launch_step2<2>(a, ii.subisland_num, st);
-        case 4: return launch_step2<4>(a, ii.subisland_num, st);
-        default: return launch_step2<8>(a, ii.subisland_num, st);
-        }
-    }
-    switch (Q) {
-    case 1: return launch_step<float, 1>(a, ii.subisland_num, st);
-    case 2: return launch_step<float, 2>(a, ii.subisland_num, st);
-    case 4: return launch_step<float, 4>(a, ii.subisland_num, st);
-    default: return launch_step<float, 8>(a, ii.subisland_num, st);
-    }
+    return run_step(a, ii.subisland_num, pair_mode, st);
 }
 
 }  // namespace speo

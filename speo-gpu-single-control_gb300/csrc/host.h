@@ -83,11 +83,11 @@ int eval_ref_multi(T *fit, const T *X, const T *shift, const T *rot, const int *
 int dropin_step_f32(speo_population_f32 pop, speo_population_f32 cand, int *d_best, speo_island_info ii,
                     speo_de_info_f32 *d_info, speo_rng_state *rng, speo_problem_info_f32 pi, const float *shift,
                     const float *rot, int generations, float *d_hist, int pair_mode, cudaStream_t st);
-// The same in FP64 (the reference's shipped precision), one block per sub-island.
+// The same in FP64 (the reference's shipped precision).
 bool dropin_step_fits_f64(int island_size, int subisland_num, int dim, int func);
 int dropin_step_f64(speo_population_f64 pop, speo_population_f64 cand, int *d_best, speo_island_info ii,
                     speo_de_info_f64 *d_info, speo_rng_state *rng, speo_problem_info_f64 pi, const double *shift,
-                    const double *rot, int generations, double *d_hist, cudaStream_t st);
+                    const double *rot, int generations, double *d_hist, int pair_mode, cudaStream_t st);
 
 // Byte offsets of the BF16 weight images inside `img`: W1 (h x 64), W2 (h x h), W2^T (h x h).
 size_t mlp_img_w2_offset(int h);
