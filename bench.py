@@ -713,10 +713,10 @@ PUBLISHED_2GPU_MEVALS = {23: 2.94, 24: 3.84, 25: 3.61, 26: 2.25, 27: 2.30, 28: 2
 
 def bench_published(L, dev, torch, gens: int = 300, gens64: int = 60, fids=range(23, 31), fp64: bool = True) -> dict:
     """F23-F30 at D = 100, one island of 4096 rows (one sub-island), through the drop-in entry
-    points on device-resident data: the FP32 loop as one speo_de_run_f32 call (last fitness read
-    back), and the FP64 loop (the reference's precision) as API_DE_GenerateNewPopulation +
-    API_evaluateFitness + API_DE_SelectSurvival called one by one; plus the evaluation kernel alone
-    (CUDA events). No migration (one island per GPU; the reference's numbers include its MPI
+    points on device-resident data: the FP32 loop and the FP64 loop (the reference's precision),
+    each as one speo_de_run_f32 / _f64 call (the generations of API_DE_GenerateNewPopulation +
+    API_evaluateFitness + API_DE_SelectSurvival; last fitness read back); plus the evaluation
+    kernel alone (CUDA events). No migration (one island per GPU; the reference's numbers include its MPI
     migration, 19-38% of its wall time at 2 GPUs)."""
     from speo_gb300 import _lib
     from speo_gb300.instances import make_instance_multi
@@ -769,24 +769,15 @@ def bench_published(L, dev, torch, gens: int = 300, gens64: int = 60, fids=range
             e1.record(stream)
             torch.cuda.synchronize()
             eval_us = e0.elapsed_time(e1) * 1e3 / reps
-            if not f64:
-                h = torch.zeros(n, dtype=torch.float32).pin_memory()
+            h = torch.zeros(n, dtype=dt).pin_memory()
+            de_run = L.speo_de_run_f64 if f64 else L.speo_de_run_f32
 
-                def run(k):
-                    _lib.check(L.speo_de_run_f32(P, C, rng_state.data_ptr(), ii, d_info.data_ptr(), best.data_ptr(),
-                                                 pi, d_sh.data_ptr(), d_rot.data_ptr(), d_sf.data_ptr(), k,
-                                                 h.data_ptr(), 0, stream.cuda_stream), "speo_de_run_f32")
-                    stream.synchronize()
-                k = gens
-            else:
-                def run(k):
-                    for _ in range(k):
-                        L.API_DE_GenerateNewPopulation(C, P, best.data_ptr(), ii, d_info.data_ptr(),
-                                                       rng_state.data_ptr(), pi)
-                        ev(cfit.data_ptr(), None, None, cand.data_ptr(), *eargs)
-                        L.API_DE_SelectSurvival(P, C, ii, pi)
-                    stream.synchronize()
-                k = gens64
+            def run(k):
+                _lib.check(de_run(P, C, rng_state.data_ptr(), ii, d_info.data_ptr(), best.data_ptr(), pi,
+                                  d_sh.data_ptr(), d_rot.data_ptr(), d_sf.data_ptr(), k, h.data_ptr(), 0,
+                                  stream.cuda_stream), "speo_de_run")
+                stream.synchronize()
+            k = gens64 if f64 else gens
             run(10)
             t0 = time.perf_counter()
             run(k)

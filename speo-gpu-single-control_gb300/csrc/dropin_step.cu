@@ -2,7 +2,8 @@
 //
 // DE_CUDA::Run (CUDA_EA_library/DE_CUDA.cc:200-216) issues API_DE_GenerateNewPopulation (best
 // search + generate), API_evaluateFitness and API_DE_SelectSurvival per generation. With the loop
-// in the library (speo_de_run_f32), one block per sub-island runs K generations from shared
+// in the library (speo_de_run_f32 / _f64), one block per sub-island (k_de_step), or a two-block
+// cluster per sub-island (k_de_step2), runs K generations from shared
 // memory: it reads the sub-island's rows (through the permutation) once, and per generation finds
 // its best position, draws donors and crossover masks from the same Philox counters as k_generate
 // (for several generations at once: they depend only on seed, position and generation), builds
