@@ -48,6 +48,28 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long l
         if (clock64() - t0 > budget) return false;
     return true;
 }
+// The same, with each test suspending the thread until the phase completes or `hint_ns`
+// nanoseconds pass: a waiting warp issues a few instructions per wait instead of polling, and
+// leaves the issue slots to the warps that work.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity, uint32_t hint_ns)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(hint_ns)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity, long long budget)
+{
+    const long long t0 = clock64();
+    while (!mbar_try_wait_sleep(bar, parity, 20000u))
+        if (clock64() - t0 > budget) return false;
+    return true;
+}
 
 // ---- TMA ---------------------------------------------------------------------------------
 // 2-D tiled load of the box at (x, y) of `map` into `dst`, completing on `bar` (tx bytes).
