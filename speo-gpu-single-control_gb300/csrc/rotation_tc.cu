@@ -3,16 +3,15 @@
 // Replaces global_ShiftAndRotation + global_f8 (CUDA_EA_library/kernel_CEC2014_CUDA.cu:147-181,
 // 557-587), an FP64 16x16 shared-memory GEMM that writes the rotated population back to HBM,
 // with one pass per 128-row tile:
-//   TMA (cp.async.bulk.tensor.2d) brings the FP32 rows into shared memory (two stages, the
-//   next tile in flight while this one is processed); the block subtracts o and splits
-//   y = y_hi + y_lo into BF16 K-major operands; M (B operand, [N][K] = M[n][k]) is split the
-//   same way once per instance; one thread issues, per 16-wide K step, the three products
-//   y_hi*M_hi + y_hi*M_lo + y_lo*M_hi into an FP32 accumulator in tensor memory
-//   (M = 128 rows, N = D rounded up to 16); the tile is converted and multiplied in two K
-//   halves, so that the products of one half run while the other half (or the next tile's first
-//   half) is converted; eight warps read the rows back with tcgen05.ld (two per TMEM lane
-//   quarter, each half of the columns), apply the scale and the objective term and reduce each
-//   row in registers.
+//   TMA (cp.async.bulk.tensor.2d) brings the FP32 rows into shared memory (a ring of up to three
+//   stages); converter warps subtract o and split y = y_hi + y_lo into BF16, each thread one row,
+//   and store the A operand straight into tensor memory (tcgen05.st, double-buffered by tile);
+//   M (B operand, [N][K] = M[n][k]) is split the same way once per instance into shared memory;
+//   one thread issues, per 16-wide K step, the three products y_hi*M_hi + y_hi*M_lo + y_lo*M_hi
+//   (A from tensor memory) into an FP32 accumulator in tensor memory (M = 128 rows, N = D rounded
+//   up to 16). The tile is converted and multiplied in two K halves (one converter warp per lane
+//   quarter and half); eight warps read the rows back with tcgen05.ld (two per lane quarter, each
+//   half of the columns), apply the scale and the objective term and reduce each row in registers.
 // Nothing but the fitness is written. D <= 128.
 #include <cuda.h>
 
@@ -29,11 +28,16 @@ namespace {
 
 constexpr int kTileM = 128;
 constexpr int kTmemCols = 128;   // one accumulator (N <= 128)
-constexpr int kTmemAlloc = 256;  // two accumulators: MMA of tile i+1 overlaps the epilogue of tile i
+// Tensor memory: accumulators b = 0, 1 at columns 128 b (MMA of tile i+1 overlaps the epilogue of
+// tile i); A operand of buffer b at 256 + 128 b (hi, <= 64 columns) and 320 + 128 b (lo).
+constexpr int kTmemAlloc = 512;
+constexpr int kAcolBase = 256;
 constexpr long long kWaitBudget = 2000000000LL;  // ~1 s at 2 GHz: any wait longer is a failure
-constexpr int kThreadsTc = 512;   // warps 0-7: epilogue; warps 8-15: conversion (+ TMA / MMA issue)
-constexpr int kEpiThreads = 256;
-constexpr int kCvtThreads = kThreadsTc - kEpiThreads;
+constexpr int kEpiThreads = 256;                 // warps 0-7: epilogue
+constexpr int kCvtThreads = 256;                 // warps 8-15: conversion
+constexpr int kThreadsTc = kEpiThreads + kCvtThreads + 32;  // warp 16: TMA and MMA issue
+constexpr int kIssuerWarp = (kEpiThreads + kCvtThreads) / 32;
+constexpr int kMaxStages = 3;
 
 __host__ __device__ __forceinline__ int round16(int x) { return (x + 15) & ~15; }
 
@@ -43,10 +47,11 @@ __host__ __device__ __forceinline__ int stage_ld(int ld) { return (ld & 7) ? ld 
 struct TcLayout {
     int kmax;         // round16(max D)
     int box_x;        // staged row stride (floats)
-    int nstage;       // 1 or 2
-    size_t stage_bytes, a_bytes, b_bytes, off_a, off_b, off_o, off_bar, off_psum, total;
+    int nstage;       // 1 to kMaxStages
+    size_t stage_bytes, b_bytes, off_b, off_o, off_bar, off_psum, total;
 };
 
+//   stage[nstage] | B hi, lo | o | barriers | psum[2][kTileM]
 __host__ __device__ inline TcLayout tc_layout(int dim_hi, int ld, int nstage)
 {
     TcLayout L;
@@ -54,13 +59,11 @@ __host__ __device__ inline TcLayout tc_layout(int dim_hi, int ld, int nstage)
     L.box_x = stage_ld(ld);
     L.nstage = nstage;
     L.stage_bytes = (size_t)kTileM * L.box_x * 4;
-    L.a_bytes = (size_t)kTileM * L.kmax * 2;         // one of hi / lo
     L.b_bytes = (size_t)L.kmax * L.kmax * 2;
-    L.off_a = ((L.stage_bytes * nstage) + 1023) & ~(size_t)1023;
-    L.off_b = L.off_a + 2 * L.a_bytes;
+    L.off_b = ((L.stage_bytes * nstage) + 1023) & ~(size_t)1023;
     L.off_o = L.off_b + 2 * L.b_bytes;
     L.off_bar = (L.off_o + (size_t)L.kmax * 4 + 15) & ~(size_t)15;
-    L.off_psum = L.off_bar + 128;                      // [2][kTileM] partial row sums
+    L.off_psum = L.off_bar + 256;
     L.total = L.off_psum + 2 * kTileM * 4;
     return L;
 }
@@ -100,65 +103,60 @@ __device__ __forceinline__ void build_b(const speo_segment &s, int Kp, uint8_t *
     for (int k = t; k < Kp; k += nthr) so[k] = k < D ? s.shift[k] : 0.f;
 }
 
-// Staged FP32 rows -> y = x - o -> BF16 hi/lo K-major A operand, K chunks [kc0, kc1) of 8
-// columns, `nthr` threads (a multiple of kTileM). Thread t converts row m = t % kTileM, chunks
-// kc0 + t / kTileM + j * nthr / kTileM: per chunk it reads 8 consecutive floats of its row with
-// two 16-byte loads (the staged row stride keeps 8 consecutive rows on distinct banks) and writes
-// one 16-byte chunk of each operand, core matrices 128 B apart along K. Rows >= count and columns
-// >= D become zero. The loop is unrolled so that the chunks' load-convert-store chains overlap.
-__device__ __forceinline__ void build_a(const float *stage, int box_x, int count, int D, int Kp, const float *so,
-                                        uint8_t *a_hi, uint8_t *a_lo, int kc0, int kc1, int t, int nthr)
+// One row's K step of the A operand: y = x - o over the 16 columns k0 .. k0+15 of a staged row
+// (zero past D or for a dead row), split into BF16 hi / lo and packed two per 32-bit word (even
+// k in the low half), as tcgen05.mma reads A from tensor memory.
+__device__ __forceinline__ void convert16(const float *row, const float *so, int k0, int D, bool live,
+                                          uint32_t (&hi)[8], uint32_t (&lo)[8])
 {
-    const int m = t % kTileM, kstep = nthr / kTileM;
-    const bool live = m < count;
-    const float *row = stage + (size_t)m * box_x;
-    const uint32_t base = tc::kmajor_offset(m, 0, Kp);
-#pragma unroll 4
-    for (int kc = kc0 + t / kTileM; kc < kc1; kc += kstep) {
-        const int kb = 8 * kc;
-        const float4 *src = reinterpret_cast<const float4 *>(row + kb);
-        const float4 *o4 = reinterpret_cast<const float4 *>(so + kb);
-        const float4 x0 = src[0], x1 = src[1], s0 = o4[0], s1 = o4[1];
-        float v[8];
-        if (live && kb + 8 <= D) {
-            v[0] = __fsub_rn(x0.x, s0.x); v[1] = __fsub_rn(x0.y, s0.y);
-            v[2] = __fsub_rn(x0.z, s0.z); v[3] = __fsub_rn(x0.w, s0.w);
-            v[4] = __fsub_rn(x1.x, s1.x); v[5] = __fsub_rn(x1.y, s1.y);
-            v[6] = __fsub_rn(x1.z, s1.z); v[7] = __fsub_rn(x1.w, s1.w);
+    float v[16];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float4 x = reinterpret_cast<const float4 *>(row + k0)[q];
+        const float4 o = reinterpret_cast<const float4 *>(so + k0)[q];
+        const int k = k0 + 4 * q;
+        if (live && k + 4 <= D) {
+            v[4 * q + 0] = __fsub_rn(x.x, o.x); v[4 * q + 1] = __fsub_rn(x.y, o.y);
+            v[4 * q + 2] = __fsub_rn(x.z, o.z); v[4 * q + 3] = __fsub_rn(x.w, o.w);
         } else {
-            v[0] = (live && kb + 0 < D) ? __fsub_rn(x0.x, s0.x) : 0.f;
-            v[1] = (live && kb + 1 < D) ? __fsub_rn(x0.y, s0.y) : 0.f;
-            v[2] = (live && kb + 2 < D) ? __fsub_rn(x0.z, s0.z) : 0.f;
-            v[3] = (live && kb + 3 < D) ? __fsub_rn(x0.w, s0.w) : 0.f;
-            v[4] = (live && kb + 4 < D) ? __fsub_rn(x1.x, s1.x) : 0.f;
-            v[5] = (live && kb + 5 < D) ? __fsub_rn(x1.y, s1.y) : 0.f;
-            v[6] = (live && kb + 6 < D) ? __fsub_rn(x1.z, s1.z) : 0.f;
-            v[7] = (live && kb + 7 < D) ? __fsub_rn(x1.w, s1.w) : 0.f;
+            v[4 * q + 0] = (live && k + 0 < D) ? __fsub_rn(x.x, o.x) : 0.f;
+            v[4 * q + 1] = (live && k + 1 < D) ? __fsub_rn(x.y, o.y) : 0.f;
+            v[4 * q + 2] = (live && k + 2 < D) ? __fsub_rn(x.z, o.z) : 0.f;
+            v[4 * q + 3] = (live && k + 3 < D) ? __fsub_rn(x.w, o.w) : 0.f;
         }
-        uint4 h, l;
-        tc::split8(v, h, l);
-        const uint32_t off = base + (uint32_t)kc * 128u;
-        *reinterpret_cast<uint4 *>(a_hi + off) = h;
-        *reinterpret_cast<uint4 *>(a_lo + off) = l;
+    }
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+        const __nv_bfloat162 hh = __floats2bfloat162_rn(v[2 * p], v[2 * p + 1]);
+        const float2 hf = __bfloat1622float2(hh);
+        const __nv_bfloat162 ll = __floats2bfloat162_rn(v[2 * p] - hf.x, v[2 * p + 1] - hf.y);
+        hi[p] = *reinterpret_cast<const uint32_t *>(&hh);
+        lo[p] = *reinterpret_cast<const uint32_t *>(&ll);
     }
 }
 
 // One thread: the 3-term split product over K steps [s0, s1) into the TMEM accumulator (step 0
-// overwrites it).
-__device__ __forceinline__ void issue_split_mma(uint32_t tmem, const uint8_t *a_hi, const uint8_t *a_lo,
-                                                const uint8_t *b_hi, const uint8_t *b_lo, int Kp, int Np, int s0,
-                                                int s1)
+// overwrites it); A hi / lo in tensor memory at a_hi / a_lo (8 columns per step), B in shared
+// memory.
+__device__ __forceinline__ void issue_split_mma(uint32_t acc, uint32_t a_hi, uint32_t a_lo, const uint8_t *b_hi,
+                                                const uint8_t *b_lo, int Kp, int Np, int s0, int s1)
 {
     const uint32_t idesc = tc::idesc_bf16_f32(kTileM, Np);
     const uint32_t sbo = (uint32_t)Kp * 16;  // 8-row groups
     const uint32_t lbo = 128;                // adjacent core matrices along K
-    const uint32_t ah = tc::smem_u32(a_hi), al = tc::smem_u32(a_lo);
-    const uint32_t bh = tc::smem_u32(b_hi), bl = tc::smem_u32(b_lo);
+    // a K step moves B by two core matrices (256 B: 16 in the descriptor's address field, which
+    // holds smem address >> 4 and cannot carry for addresses below 256 KB) and A by 8 columns
+    uint64_t dh = tc::smem_desc(tc::smem_u32(b_hi) + (uint32_t)s0 * 256u, lbo, sbo);
+    uint64_t dl = tc::smem_desc(tc::smem_u32(b_lo) + (uint32_t)s0 * 256u, lbo, sbo);
+    uint32_t ah = a_hi + (uint32_t)s0 * 8u, al = a_lo + (uint32_t)s0 * 8u;
     for (int s = s0; s < s1; ++s) {
-        const uint32_t koff = (uint32_t)s * 256;  // two core matrices per K step
-        tc::mma_bf16(tmem, tc::smem_desc(al + koff, lbo, sbo), tc::smem_desc(bh + koff, lbo, sbo), idesc, s > 0);
-        tc::mma_bf16(tmem, tc::smem_desc(ah + koff, lbo, sbo), tc::smem_desc(bl + koff, lbo, sbo), idesc, 1);
-        tc::mma_bf16(tmem, tc::smem_desc(ah + koff, lbo, sbo), tc::smem_desc(bh + koff, lbo, sbo), idesc, 1);
+        tc::mma_bf16_ta(acc, al, dh, idesc, s > 0);
+        tc::mma_bf16_ta(acc, ah, dl, idesc, 1);
+        tc::mma_bf16_ta(acc, ah, dh, idesc, 1);
+        dh += 16;
+        dl += 16;
+        ah += 8;
+        al += 8;
     }
 }
 
@@ -191,28 +189,20 @@ __device__ __forceinline__ float epilogue_row(uint32_t tmem, int warp, int D, in
     const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     const uint64_t sc = pk2(scale, scale);
     uint64_t acc = pk2(0.f, 0.f);
-    for (int c = c0; c < c1; c += 64) {
-        // both 32-column loads in flight before the wait (warp-uniform: c, c1 are)
-        uint32_t r[2][32];
-        const bool two = c + 32 < c1;
-        tmem_ld32_nowait(lane_base + (uint32_t)c, r[0]);
-        if (two) tmem_ld32_nowait(lane_base + (uint32_t)(c + 32), r[1]);
+    for (int c = c0; c < c1; c += 32) {
+        uint32_t r[32];
+        tmem_ld32_nowait(lane_base + (uint32_t)c, r);
         tmem_wait_ld();
+        if (c + 32 <= D) {
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            if (u == 1 && !two) break;
-            const int cu = c + 32 * u;
-            if (cu + 32 <= D) {
+            for (int j = 0; j < 32; j += 2)
+                acc = add2(acc, obj_term2(func, mul2(pk2(__uint_as_float(r[j]), __uint_as_float(r[j + 1])), sc)));
+        } else {
 #pragma unroll
-                for (int j = 0; j < 32; j += 2)
-                    acc = add2(acc, obj_term2(func, mul2(pk2(__uint_as_float(r[u][j]), __uint_as_float(r[u][j + 1])), sc)));
-            } else {
-#pragma unroll
-                for (int j = 0; j < 32; j += 2) {
-                    if (cu + j < D) {
-                        const float z1 = (cu + j + 1 < D) ? __uint_as_float(r[u][j + 1]) : 0.f;
-                        acc = add2(acc, obj_term2(func, mul2(pk2(__uint_as_float(r[u][j]), z1), sc)));
-                    }
+            for (int j = 0; j < 32; j += 2) {
+                if (c + j < D) {
+                    const float z1 = (c + j + 1 < D) ? __uint_as_float(r[j + 1]) : 0.f;
+                    acc = add2(acc, obj_term2(func, mul2(pk2(__uint_as_float(r[j]), z1), sc)));
                 }
             }
         }
@@ -282,17 +272,17 @@ __device__ __forceinline__ bool tc_tile_ok(const speo_work_item &it, const speo_
            s.row0 + it.first + it.count <= a.n_rows;
 }
 
-// Warp roles: warps 8..15 convert tile i (thread 256 also issues the TMA loads and the MMAs);
-// warps 0..7 run the epilogue of tile i-1 from the other TMEM accumulator meanwhile. The A
-// operand is converted and multiplied in two K halves: while the products of one half run, the
-// other half is converted.
-//   bar_tma[s]  stage s holds the rows of its tile         (TMA transaction bytes)
-//   bar_ah[h]   the products of half h of the last tile are done: its A half is free (tcgen05.commit)
-//   bar_mma[b]  accumulator b holds a finished product     (tcgen05.commit)
-//   bar_epi[b]  the epilogue is done reading accumulator b (256 arrivals)
-//   bar_fin     every product this block issued is done    (tcgen05.commit, on abort)
-// Everything a role needs about one tile, loaded ahead of use (two-stage register prefetch:
-// the work item two tiles ahead, its segment one tile ahead).
+// Warp roles: warps 8..15 convert tile i into the A buffer i % 2 in tensor memory (warp 8 + q + 4h:
+// lane quarter q, K half h); warp 16 issues the TMA loads and (one thread) the MMAs of each half
+// as soon as it is converted; warps 0..7 run the epilogue of tile i-1 from the other accumulator.
+//   bar_tma[s]      stage s holds the rows of its tile                 (TMA transaction bytes)
+//   bar_afull[b][h] half h of A buffer b is converted (and its stage rows read) (128 arrivals)
+//   bar_afree[b]    the products reading A buffer b are done          (tcgen05.commit)
+//   bar_mma[b]      accumulator b holds a finished product            (tcgen05.commit)
+//   bar_epi[b]      the epilogue is done reading accumulator b        (256 arrivals)
+//   bar_fin         every product this block issued is done           (tcgen05.commit, on abort)
+// Everything a role needs about one tile is loaded ahead of use (register prefetch of the work
+// items and segments of the next tiles).
 struct TileInfo {
     int ok, count, D, func, ld_rot;
     long long row;
@@ -318,31 +308,33 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     const TcLayout L = tc_layout(a.dim_hi, a.ld, a.nstage);
-    float *stage[2] = {reinterpret_cast<float *>(smem), reinterpret_cast<float *>(smem + L.stage_bytes)};
-    uint8_t *a_hi = smem + L.off_a, *a_lo = a_hi + L.a_bytes;
+    const int ns = a.nstage;
+    float *stage[kMaxStages];
+#pragma unroll
+    for (int k = 0; k < kMaxStages; ++k) stage[k] = reinterpret_cast<float *>(smem + (size_t)k * L.stage_bytes);
     uint8_t *b_hi = smem + L.off_b, *b_lo = b_hi + L.b_bytes;
     float *so = reinterpret_cast<float *>(smem + L.off_o);
     float *psum = reinterpret_cast<float *>(smem + L.off_psum);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
-    uint64_t *bar_tma = bars, *bar_mma = bars + 2, *bar_epi = bars + 4, *bar_ah = bars + 8, *bar_fin = bars + 10;
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 6);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 7);
+    uint64_t *bar_tma = bars, *bar_mma = bars + 3, *bar_epi = bars + 5, *bar_afull = bars + 7, *bar_afree = bars + 11,
+             *bar_fin = bars + 13;
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 14);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 15);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int ns = a.nstage;
 
     if (warp == 0) {
         tc::tmem_alloc(tmem_slot, kTmemAlloc);
         tc::tmem_relinquish();
     }
     if (tid == 32) {
-        tc::mbar_init(&bar_tma[0], 1);
-        tc::mbar_init(&bar_tma[1], 1);
-        tc::mbar_init(&bar_mma[0], 1);
-        tc::mbar_init(&bar_mma[1], 1);
-        tc::mbar_init(&bar_epi[0], kEpiThreads);
-        tc::mbar_init(&bar_epi[1], kEpiThreads);
-        tc::mbar_init(&bar_ah[0], 1);
-        tc::mbar_init(&bar_ah[1], 1);
+        for (int k = 0; k < kMaxStages; ++k) tc::mbar_init(&bar_tma[k], 1);
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&bar_mma[b], 1);
+            tc::mbar_init(&bar_epi[b], kEpiThreads);
+            tc::mbar_init(&bar_afull[2 * b], 128);
+            tc::mbar_init(&bar_afull[2 * b + 1], 128);
+            tc::mbar_init(&bar_afree[b], 1);
+        }
         tc::mbar_init(bar_fin, 1);
         *abort_flag = 0;
         tc::fence_mbar_init();
@@ -352,84 +344,114 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
+    auto a_hi_col = [&](int b) { return tmem + (uint32_t)(kAcolBase + 128 * b); };
+    auto a_lo_col = [&](int b) { return tmem + (uint32_t)(kAcolBase + 128 * b + 64); };
 
     const int my_items = a.n_items > (int)blockIdx.x ? (a.n_items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    auto item_of = [&](int i) { return a.items[blockIdx.x + i * gridDim.x]; };
-    int tma_issued = 0;      // issuer bookkeeping (thread kEpiThreads)
+    auto item_of = [&](int i) { return a.items[blockIdx.x + (i < my_items ? i : my_items - 1) * gridDim.x]; };
+    int tma_issued = 0;      // issuer bookkeeping (warp kIssuerWarp, lane 0)
     bool mma_any = false;
-    // t: the tile's information, loaded a tile ahead (no dependent global load on the issuer's path)
-    auto issue_tma = [&](int i, const TileInfo &t) {
-        if (i >= my_items) return;
-        const int sidx = i % ns;
-        tc::mbar_arrive_expect_tx(&bar_tma[sidx], (uint32_t)L.stage_bytes);
-        tc::tma_load_2d(stage[sidx], &xmap, 0, t.ok ? (int)t.row : 0, &bar_tma[sidx]);
-        tma_issued = i + 1;
-    };
 
-    if (warp >= kEpiThreads / 32) {
-        // ---- conversion group ---------------------------------------------------------------------
-        const int ct = tid - kEpiThreads;
-        const bool issuer = ct == 0;
-        // three-deep prefetch: tile i's information (cur), tile i+1's (nxt), tile i+2's work item
-        TileInfo cur = tile_info(a, item_of(0));
-        TileInfo nxt = tile_info(a, item_of(my_items > 1 ? 1 : 0));
-        speo_work_item it_nn = item_of(my_items > 2 ? 2 : 0);
-        if (issuer) {
-            issue_tma(0, cur);
-            if (ns > 1) issue_tma(1, nxt);
+    if (warp == kIssuerWarp) {
+        // ---- TMA and MMA issue: the whole warp runs the loop, lane 0 issues ----------------------
+        const bool leader = lane == 0;
+        auto issue_tma = [&](int i, const TileInfo &t) {
+            if (i >= my_items) return;
+            if (leader) {
+                const int sidx = i % ns;
+                tc::mbar_arrive_expect_tx(&bar_tma[sidx], (uint32_t)L.stage_bytes);
+                tc::tma_load_2d(stage[sidx], &xmap, 0, t.ok ? (int)t.row : 0, &bar_tma[sidx]);
+            }
+            tma_issued = i + 1;
+        };
+        for (int j = 0; j < ns; ++j) issue_tma(j, tile_info(a, item_of(j)));
+        TileInfo cur = tile_info(a, item_of(0)), nxt = tile_info(a, item_of(1));
+        speo_work_item it_n2 = item_of(2);
+        TileInfo tq = tile_info(a, item_of(ns));        // the tile whose TMA follows tile 0
+        speo_work_item it_q = item_of(ns + 1);
+        for (int i = 0; i < my_items; ++i) {
+            // work items a tile ahead of their segments: no dependent load waits in this iteration
+            const TileInfo n2 = tile_info(a, it_n2);
+            const speo_work_item it_n3 = item_of(i + 3);
+            const TileInfo tq_next = tile_info(a, it_q);
+            const speo_work_item it_q_next = item_of(i + ns + 2);
+            const int b = i & 1, Kp = round16(cur.D), S = Kp / 16, s_half = (S + 1) / 2;
+            bool ok = tc::mbar_wait_sleep(&bar_afull[2 * b], (uint32_t)((i >> 1) & 1), kWaitBudget);
+            if (i >= 2) ok = ok && tc::mbar_wait_sleep(&bar_epi[b], (uint32_t)(((i - 2) >> 1) & 1), kWaitBudget);
+            if (!__all_sync(0xffffffffu, ok && *abort_flag == 0)) { *abort_flag = 1; break; }
+            tc::fence_after_sync();
+            const uint32_t acc = tmem + (uint32_t)(b * kTmemCols);
+            if (leader) {
+                issue_split_mma(acc, a_hi_col(b), a_lo_col(b), b_hi, b_lo, Kp, Kp, 0, s_half);
+                mma_any = true;
+            }
+            ok = tc::mbar_wait_sleep(&bar_afull[2 * b + 1], (uint32_t)((i >> 1) & 1), kWaitBudget);
+            if (!__all_sync(0xffffffffu, ok && *abort_flag == 0)) { *abort_flag = 1; break; }
+            tc::fence_after_sync();
+            if (leader) {
+                issue_split_mma(acc, a_hi_col(b), a_lo_col(b), b_hi, b_lo, Kp, Kp, s_half, S);
+                tc::mma_commit(&bar_mma[b]);
+                tc::mma_commit(&bar_afree[b]);
+            }
+            // both halves' converters have read stage i % ns: it takes tile i + ns
+            issue_tma(i + ns, tq);
+            __syncwarp();
+            cur = nxt;
+            nxt = n2;
+            it_n2 = it_n3;
+            tq = tq_next;
+            it_q = it_q_next;
         }
+    } else if (warp >= kEpiThreads / 32) {
+        // ---- conversion: thread = row 32 q + lane, K half ch -------------------------------------
+        const int ct = tid - kEpiThreads, q = warp & 3, ch = (warp - kEpiThreads / 32) >> 2;
+        const int m = q * 32 + lane;
+        const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+        TileInfo cur = tile_info(a, item_of(0));
+        TileInfo nxt = tile_info(a, item_of(1));
+        speo_work_item it_nn = item_of(2);
         const float *c_rot = nullptr, *c_shift = nullptr;
         int c_dim = -1, c_ldrot = -1;
-        bool stop = false;
-        for (int i = 0; i < my_items && !stop; ++i) {
-            const speo_work_item it_n3 = item_of(i + 3 < my_items ? i + 3 : i);
-            const TileInfo nn = tile_info(a, it_nn);  // tile i+2
+        for (int i = 0; i < my_items; ++i) {
+            const speo_work_item it_n3 = item_of(i + 3);
+            const TileInfo nn = tile_info(a, it_nn);
+            const int sidx = i % ns, b = i & 1;
             const int D = cur.D, Kp = round16(D), S = Kp / 16, s_half = (S + 1) / 2;
-            bool to = !tc::mbar_wait_sleep(&bar_tma[i % ns], (uint32_t)((i / ns) & 1), kWaitBudget);
+            bool to = !tc::mbar_wait_sleep(&bar_tma[sidx], (uint32_t)((i / ns) & 1), kWaitBudget);
             const bool new_b = cur.ok && (cur.rot != c_rot || cur.shift != c_shift || D != c_dim ||
                                           cur.ld_rot != c_ldrot);
             // B and o are read by every product of the previous tile: rebuild them once those are done
             if (new_b && i >= 1)
                 to |= !tc::mbar_wait_sleep(&bar_mma[(i - 1) & 1], (uint32_t)(((i - 1) >> 1) & 1), kWaitBudget);
+            // the group's decision to stop is reduced over all converters, so that none waits at
+            // named barrier 1 for one that left
             if (tc::named_bar_or(1, kCvtThreads, to || *abort_flag != 0)) { *abort_flag = 1; break; }
             if (new_b) {
                 speo_segment sb;
                 sb.dim = D; sb.rot = cur.rot; sb.shift = cur.shift; sb.ld_rot = cur.ld_rot;
                 build_b(sb, Kp, b_hi, b_lo, so, ct, kCvtThreads);
                 c_rot = cur.rot; c_shift = cur.shift; c_dim = D; c_ldrot = cur.ld_rot;
+                tc::fence_proxy_async_smem();
                 tc::named_bar_sync(1, kCvtThreads);
             }
             if (!cur.ok && ct == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
-            for (int h = 0; h < 2; ++h) {
-                const int s0 = h == 0 ? 0 : s_half, s1 = h == 0 ? s_half : S;
-                // the products of half h of the previous tile must be done before its A half is rewritten
-                bool th = i >= 1 && !tc::mbar_wait_sleep(&bar_ah[h], (uint32_t)((i - 1) & 1), kWaitBudget);
-                if (cur.ok && !th) build_a(stage[i % ns], L.box_x, cur.count, D, Kp, so, a_hi, a_lo, 2 * s0, 2 * s1, ct,
-                                           kCvtThreads);
-                tc::fence_proxy_async_smem();
-                if (tc::named_bar_or(1, kCvtThreads, th || *abort_flag != 0)) {
-                    *abort_flag = 1;
-                    stop = true;
-                    break;
+            // A buffer b was last read by the products of tile i - 2
+            bool ok = i < 2 || tc::mbar_wait_sleep(&bar_afree[b], (uint32_t)(((i - 2) >> 1) & 1), kWaitBudget);
+            if (__all_sync(0xffffffffu, ok)) {
+                const int s0 = ch == 0 ? 0 : s_half, s1 = ch == 0 ? s_half : S;
+                const float *row = stage[sidx] + (size_t)m * L.box_x;
+                const bool live = cur.ok && m < cur.count;
+                for (int st = s0; st < s1; ++st) {
+                    uint32_t hi[8], lo[8];
+                    convert16(row, so, 16 * st, D, live, hi, lo);
+                    tc::tmem_st32x8(a_hi_col(b) + lane_off + (uint32_t)(8 * st), hi);
+                    tc::tmem_st32x8(a_lo_col(b) + lane_off + (uint32_t)(8 * st), lo);
                 }
-                if (issuer) {
-                    bool free_acc = true;
-                    if (h == 0 && i >= 2)
-                        free_acc = tc::mbar_wait_sleep(&bar_epi[i & 1], (uint32_t)(((i - 2) >> 1) & 1), kWaitBudget);
-                    if (!free_acc) {
-                        *abort_flag = 1;
-                    } else {
-                        tc::fence_after_sync();
-                        issue_split_mma(tmem + (uint32_t)((i & 1) * kTmemCols), a_hi, a_lo, b_hi, b_lo, Kp, Kp, s0, s1);
-                        mma_any = true;
-                        tc::mma_commit(&bar_ah[h]);
-                        if (h == 1) {
-                            tc::mma_commit(&bar_mma[i & 1]);
-                            // every converter has read the stage: it takes tile i + ns
-                            issue_tma(i + ns, ns > 1 ? nn : nxt);
-                        }
-                    }
-                }
+                tc::tmem_wait_st();
+                tc::fence_before_sync();
+                tc::mbar_arrive(&bar_afull[2 * b + ch]);
+            } else {
+                *abort_flag = 1;  // the next tile's barrier stops the group
             }
             cur = nxt;
             nxt = nn;
@@ -438,14 +460,14 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
     } else {
         // ---- epilogue group: one TMEM lane (= tile row) per thread, two warps per lane quarter ------
         const int q = warp & 3, ch = warp >> 2;  // lane quarter, column half
-        speo_work_item it_next = item_of(my_items > 1 ? 1 : 0);
+        speo_work_item it_next = item_of(1);
         TileInfo cur = tile_info(a, item_of(0));
         for (int i = 0; i < my_items; ++i) {
             // Decisions to stop are reduced over the quarter's two warps (named barrier 2 + q), so
             // that both leave together and neither waits at that barrier for the other; they are
             // then also warp-uniform, as the warp-collective tcgen05.ld below needs.
             if (tc::named_bar_or(2 + q, 64, *abort_flag != 0)) break;
-            const speo_work_item it_nn = item_of(i + 2 < my_items ? i + 2 : i);
+            const speo_work_item it_nn = item_of(i + 2);
             const TileInfo nxt = tile_info(a, it_next);
             const bool got = tc::mbar_wait_sleep(&bar_mma[i & 1], (uint32_t)((i >> 1) & 1), kWaitBudget);
             if (tc::named_bar_or(2 + q, 64, !got)) { *abort_flag = 1; break; }
@@ -474,15 +496,15 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
         }
     }
     __syncthreads();
-    if (*abort_flag && tid == kEpiThreads) {
+    if (*abort_flag && warp == kIssuerWarp && lane == 0) {
         // Let the copies and products this block started finish (bounded) before its shared and
         // tensor memory are released.
         atomicOr(&s_deverr, SPEO_DEVERR_WAIT_TIMEOUT);
         for (int j = (tma_issued > ns ? tma_issued - ns : 0); j < tma_issued; ++j)
-            tc::mbar_wait_sleep(&bar_tma[j % ns], (uint32_t)((j / ns) & 1), kWaitBudget);
+            tc::mbar_wait(&bar_tma[j % ns], (uint32_t)((j / ns) & 1), kWaitBudget);
         if (mma_any) {
             tc::mma_commit(bar_fin);
-            tc::mbar_wait_sleep(bar_fin, 0, kWaitBudget);
+            tc::mbar_wait(bar_fin, 0, kWaitBudget);
         }
     }
     tc::fence_before_sync();
@@ -545,8 +567,8 @@ extern "C" int speo_evaluate_tc(const speo_segment *segs, const speo_work_item *
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(SPEO_ERR_CUDA, "speo_evaluate_tc: cuTensorMapEncodeTiled failed (%d)", (int)r);
     const int limit = max_optin_smem();
-    int nstage = 2;
-    if ((int)tc_layout(dim_hi, ld, 2).total > limit) nstage = 1;
+    int nstage = kMaxStages;
+    while (nstage > 1 && (int)tc_layout(dim_hi, ld, nstage).total > limit) --nstage;
     const TcLayout Lay = tc_layout(dim_hi, ld, nstage);
     if ((int)Lay.total > limit) return fail(SPEO_ERR_UNSUPPORTED, "speo_evaluate_tc: needs %zu B of shared memory", Lay.total);
     // At least half of the SM's shared memory per block: one block (one TMEM allocation) per SM.
