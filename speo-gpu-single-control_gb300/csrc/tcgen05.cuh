@@ -1,8 +1,9 @@
 // tcgen05.cuh -- inline-PTX wrappers for the sm_100-family tensor-core path used by this
 // library: mbarriers with bounded waits, TMA (cp.async.bulk.tensor) loads, tensor-memory
-// allocation, tcgen05.mma (kind::f16, BF16 inputs, FP32 accumulation), commit and tcgen05.ld.
+// allocation, tcgen05.mma (kind::f16, BF16 inputs, FP32 accumulation; A from shared or tensor
+// memory), commit, tcgen05.ld and tcgen05.st.
 //
-// Operand layout: both operands K-major, no swizzle, in 8x8 "core matrices" of 16-bit
+// Shared-memory operand layout: K-major, no swizzle, in 8x8 "core matrices" of 16-bit
 // elements (8 rows x 16 bytes, 128 contiguous bytes). Element (r, k) of an R x Kp operand sits at
 //   ((r / 8) * (Kp / 8) + k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2   bytes,
 // so core matrices adjacent in K are 128 B apart (leading byte offset) and 8-row groups are
