@@ -97,6 +97,29 @@ def test_dropin_validation_happens_before_any_device_work(lib):
     assert lib.API_Initilize_f32(pop, None, ii, pi) == _lib.SPEO_ERR_INVALID_ARG
 
 
+@pytest.mark.parametrize("f64", [False, True])
+def test_de_run_validation_happens_before_any_device_work(lib, f64):
+    """speo_de_run_f32 / _f64 report missing buffers and negative generation counts as status
+    codes, naming the entry point, before touching the device."""
+    from speo_gb300 import _lib
+
+    Pop, PI, run = ((_lib.PopulationF64, _lib.ProblemInfoF64, lib.speo_de_run_f64) if f64 else
+                    (_lib.PopulationF32, _lib.ProblemInfoF32, lib.speo_de_run_f32))
+    name = b"speo_de_run_f64" if f64 else b"speo_de_run_f32"
+    pop = Pop(16, 16)                      # never dereferenced
+    ii = _lib.IslandInfo(100, 1, 16)
+    pi = PI(30, 9, 1, 0, 1, 0, 0, 100.0, -100.0)
+    args = [pop, pop, 16, ii, 16, 16, pi, 16, 16, None, 5, None, 0, None]
+    for k in (2, 4, 5, 7, 8):              # rng, DE info, best ids, shift, rotation
+        bad = list(args)
+        bad[k] = None
+        assert run(*bad) == _lib.SPEO_ERR_INVALID_ARG
+        assert name in lib.speo_last_error()
+    bad = list(args)
+    bad[10] = -1                           # generations
+    assert run(*bad) == _lib.SPEO_ERR_INVALID_ARG
+
+
 @pytest.mark.parametrize("fid", [-1, 0, 32, 33])
 def test_evaluate_rejects_unimplemented_function_id(lib, fid):
     """Ids 1-30 (CEC2014) and 31 (rotated sphere) are implemented; any other id is refused
