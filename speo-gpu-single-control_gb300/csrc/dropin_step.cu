@@ -117,7 +117,9 @@ __global__ void __launch_bounds__(kThreadsS) k_de_step(StepArgs<T> a)
         const bool last = g == a.gens - 1;
         __syncthreads();
         // ---- best position (k_best): argmin of fitness, NaN as +inf, ties lowest position -----
-        {
+        // read by the best-row strategies, and its id is left behind after the last generation
+        const bool need_best = strategy_uses_best(st) || last;
+        if (need_best) {
             T bf = T(INFINITY);
             int bp = 0x7fffffff;
             for (int p = tid; p < S; p += kThreadsS) {
@@ -145,9 +147,10 @@ __global__ void __launch_bounds__(kThreadsS) k_de_step(StepArgs<T> a)
                 o[5] = s.index(D);
             }
         }
-        __syncthreads();
-        int bp = s_bp[0];
-        {
+        if (need_best || g % GB == 0) __syncthreads();  // block-uniform condition
+        int bp = 0;
+        if (need_best) {
+            bp = s_bp[0];
             T bf = s_bf[0];
             for (int w = 1; w < kWarpsS; ++w)
                 if (s_bf[w] < bf || (s_bf[w] == bf && s_bp[w] < bp)) { bf = s_bf[w]; bp = s_bp[w]; }
@@ -383,7 +386,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
         const int cur = g & 1, nxt = cur ^ 1;
         const T *Xp = Xp0 + (size_t)cur * S * W;
         const T *fp = fp0 + cur * Sf;
-        {  // (the previous generation's cluster barrier ordered every access before this point)
+        // The best position is read by the best-row strategies, and its id is left behind after
+        // the last generation; other generations of other strategies skip the search.
+        const bool need_best = strategy_uses_best(st) || last;
+        if (need_best) {  // (the previous generation's cluster barrier ordered every access before this point)
             T bf = T(INFINITY);
             int bp = 0x7fffffff;
             for (int p = tid; p < S; p += kThreadsS) {
@@ -410,9 +416,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kThreadsS, 1) k_de_s
                 o[5] = s.index(D);
             }
         }
-        __syncthreads();
-        int bp = s_bp[0];
-        {
+        if (need_best || g % GB == 0) __syncthreads();  // block-uniform condition
+        int bp = 0;
+        if (need_best) {
+            bp = s_bp[0];
             T bf = s_bf[0];
             for (int w = 1; w < kWarpsS; ++w)
                 if (s_bf[w] < bf || (s_bf[w] == bf && s_bp[w] < bp)) { bf = s_bf[w]; bp = s_bp[w]; }
