@@ -8,7 +8,7 @@
 //      strict-`<` greedy selection;
 //   4. the exact evaluations are appended to a ring-buffer archive;
 //   5. Adam trains the MLP on batches sampled from the archive.
-// Exact evaluation stays the judge: the surrogate only chooses which trial is evaluated.
+// Exact evaluation stays the arbiter: the surrogate only chooses which trial is evaluated.
 #include <cmath>
 #include <cstring>
 #include <new>
