@@ -152,7 +152,8 @@ def test_regroup_options(oracle, regroup):
                                                      (17, 40, 50, 5, 7, 0.3, 1),
                                                      (1, 16, 1, 16, 1, 1.0, 1),      # one island: nobody to send to
                                                      (2, 4, 3, 4, 4, 1.0, 1),        # the smallest islands, k = P
-                                                     (4, 33, 100, 1, 32, 0.0, 1)])   # rate 0: lists stay empty
+                                                     (4, 33, 100, 1, 32, 0.0, 1),    # rate 0: lists stay empty
+                                                     (2, 128, 20, 64, 64, 1.0, 1)])  # capacity 64, the largest
 def test_archipelago_matches_oracle(lib, oracle, cuda, policy, regroup, N, P, D, k, C, rate, interval):
     import torch
     from speo_gb300 import _lib

@@ -81,7 +81,7 @@ def test_dropin_init_matches_oracle(lib, oracle, cuda, P, D):
 
 @pytest.mark.parametrize("f64", [False, True])
 @pytest.mark.parametrize("P,D,nsub", [(100, 30, 4), (64, 10, 1), (96, 100, 3), (8, 1, 2), (40, 33, 10), (2048, 10, 1),
-                                      (3000, 30, 2)])
+                                      (3000, 30, 2), (40, 256, 2)])   # last: D = SPEO_MAX_DIM
 def test_dropin_generate_matches_oracle(lib, oracle, cuda, f64, P, D, nsub):
     import torch
 
@@ -131,6 +131,7 @@ def test_dropin_generate_matches_oracle(lib, oracle, cuda, f64, P, D, nsub):
     (9, True, True, 200, 30, 2, 23, (4, 6)),         # composition: three calls, every generation's fitness
     (24, True, False, 300, 50, 3, 30, (4, 6, 2)),    # composition of hybrids: graph blocks
     (5, False, True, 120, 20, 2, 21, (6,)),          # hybrid, pageable buffer
+    (4, True, True, 64, 256, 2, 9, (4, 6)),          # D = SPEO_MAX_DIM
 ])
 @pytest.mark.parametrize("f64", [False, True])
 def test_de_run_matches_the_dropin_loop(lib, cuda, f64, gens, pinned, history, P, D, nsub, fid, strats):
@@ -248,7 +249,7 @@ def _tol(fid, f64):
 
 @pytest.mark.parametrize("f64", [False, True])
 @pytest.mark.parametrize("fid", ALL_FUNCS)
-@pytest.mark.parametrize("P,D", [(100, 10), (130, 30), (64, 50), (70, 100), (5, 200)])
+@pytest.mark.parametrize("P,D", [(100, 10), (130, 30), (64, 50), (70, 100), (5, 200), (3, 256)])
 def test_dropin_evaluate_matches_oracle(lib, oracle, cuda, f64, fid, P, D):
     """API_evaluateFitness for every implemented function id (CEC2014 1-16, rotated sphere 31)."""
     import torch
