@@ -98,6 +98,26 @@ def test_dropin_validation_happens_before_any_device_work(lib):
 
 
 @pytest.mark.parametrize("f64", [False, True])
+def test_empty_populations_are_status_codes(lib, f64):
+    """Zero-row islands and populations come back as SPEO_ERR_INVALID_ARG from every drop-in
+    entry point (the reference would launch empty grids or divide by zero)."""
+    from speo_gb300 import _lib
+
+    Pop, PI = (_lib.PopulationF64, _lib.ProblemInfoF64) if f64 else (_lib.PopulationF32, _lib.ProblemInfoF32)
+    sfx = "" if f64 else "_f32"
+    pop = Pop(16, 16)                      # never dereferenced
+    pi = PI(30, 9, 1, 0, 1, 0, 0, 100.0, -100.0)
+    for ii in (_lib.IslandInfo(0, 1, 16), _lib.IslandInfo(10, 0, 16)):
+        assert getattr(lib, "API_Initilize" + sfx)(pop, None, ii, pi) == _lib.SPEO_ERR_INVALID_ARG
+        assert getattr(lib, "API_DE_GenerateNewPopulation" + sfx)(pop, pop, 16, ii, 16, 16, pi) == \
+            _lib.SPEO_ERR_INVALID_ARG
+        assert getattr(lib, "API_DE_SelectSurvival" + sfx)(pop, pop, ii, pi) == _lib.SPEO_ERR_INVALID_ARG
+    # the void evaluation entry point records the failure (API_CheckCUDAError returns it on a GPU)
+    getattr(lib, "API_evaluateFitness" + sfx)(16, None, None, 16, 16, 16, None, None, None, None, 0, 30, 0.0, 9)
+    assert b"pop_size 0" in lib.speo_last_error()
+
+
+@pytest.mark.parametrize("f64", [False, True])
 def test_de_run_validation_happens_before_any_device_work(lib, f64):
     """speo_de_run_f32 / _f64 report missing buffers and negative generation counts as status
     codes, naming the entry point, before touching the device."""
