@@ -5,7 +5,8 @@
 // in the library (speo_de_run_f32 / _f64), one block per sub-island (k_de_step), or a two-block
 // cluster per sub-island (k_de_step2), runs K generations from shared
 // memory: it reads the sub-island's rows (through the permutation) once, and per generation finds
-// its best position, draws donors and crossover masks from the same Philox counters as k_generate
+// its best position (where a best-row strategy reads it, and after the last generation, whose best
+// ids the three calls leave behind), draws donors and crossover masks from the same Philox counters as k_generate
 // (for several generations at once: they depend only on seed, position and generation), builds
 // the trials, evaluates them with the same FMA order as k_eval_ref and applies the strict-`<`
 // selection. Each generation's fitness vector goes to a history buffer; after the last one the
