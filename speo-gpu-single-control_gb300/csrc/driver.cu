@@ -20,7 +20,7 @@ namespace {
 
 constexpr int kBlock = 10;     // generations per captured graph (three-call path)
 constexpr int kStepGens = 100;             // generations per fused launch (at most)
-constexpr size_t kHistFloats = 1u << 22;   // bound of one history buffer (16 MiB)
+constexpr size_t kHistElems = 1u << 22;    // bound of one history buffer (16 MiB FP32, 32 MiB FP64)
 
 struct DriverHistory {
     void *p = nullptr;
@@ -158,9 +158,9 @@ int de_run(Pop pop, Pop cand, speo_rng_state *rng, speo_island_info ii, Info *d_
         // two history buffers: launch i writes buffer i % 2 while the copy stream reads the other
         // one back, so the read-back of a block of generations overlaps the next block
         T *d_hist = nullptr;
-        int per = kStepGens;  // generations per launch: the history of one launch within kHistFloats
+        int per = kStepGens;  // generations per launch: the history of one launch within kHistElems
         if (hist) {
-            const size_t cap = kHistFloats / (size_t)n;
+            const size_t cap = kHistElems / (size_t)n;
             per = cap < 1 ? 1 : cap < (size_t)kStepGens ? (int)cap : kStepGens;
             e = history_buffer(2 * (size_t)per * n, &d_hist);
         }
