@@ -283,6 +283,8 @@ def bench_speo(args) -> dict:
         out["published_config"] = bench_published(L, dev, torch)
     if not args.no_e2e:
         out["e2e"] = bench_e2e(L, dev, torch, args)
+        # the same end-to-end loop in the reference's shipped precision
+        out["e2e_fp64"] = bench_e2e(L, dev, torch, args, f64=True)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(sample_s=args.cpu_sample_s)
     return out
@@ -621,68 +623,79 @@ def bench_mlp(L, dev, torch, steps: int = 16) -> dict:
             "train_steps_timed": steps}
 
 
-def bench_e2e(L, dev, torch, args) -> dict:
+def bench_e2e(L, dev, torch, args, f64: bool = False) -> dict:
     """Reference-shaped C ABI with host buffers: initial population + instance uploaded from
     pinned host memory, then per generation generate / evaluate / select and a read-back of
-    the generation's fitness vector; all inside the timed region."""
+    the generation's fitness vector; all inside the timed region. f64: the same in the
+    reference's shipped precision (`real` = double) through speo_de_run_f64 and the FP64 entry
+    points."""
     from speo_gb300 import _lib
     from speo_gb300.instances import make_instance
 
     n = N_ISLANDS * POP
     ld = 32
+    npt = np.float64 if f64 else np.float32
+    tdt = torch.float64 if f64 else torch.float32
+    es = 8 if f64 else 4
+    sfx = "" if f64 else "_f32"
+    Pop = _lib.PopulationF64 if f64 else _lib.PopulationF32
+    PI = _lib.ProblemInfoF64 if f64 else _lib.ProblemInfoF32
+    DI = _lib.DEInfoF64 if f64 else _lib.DEInfoF32
+    init, gen, ev, sel = (getattr(L, f + sfx) for f in ("API_Initilize", "API_DE_GenerateNewPopulation",
+                                                        "API_evaluateFitness", "API_DE_SelectSurvival"))
+    de_run = L.speo_de_run_f64 if f64 else L.speo_de_run_f32
+    run_name = "speo_de_run_f64" if f64 else "speo_de_run_f32"
     o, M = make_instance(run_seed(), DIM)
-    rot = np.zeros((ld, DIM), dtype=np.float32)
+    rot = np.zeros((ld, DIM), dtype=npt)
     rot[:DIM] = M.T
-    sh = np.zeros(ld, dtype=np.float32)
+    sh = np.zeros(ld, dtype=npt)
     sh[:DIM] = o
     rng = np.random.default_rng(0)
-    h_pop = torch.from_numpy(rng.uniform(-100, 100, (n, ld)).astype(np.float32)).pin_memory()
+    h_pop = torch.from_numpy(rng.uniform(-100, 100, (n, ld)).astype(npt)).pin_memory()
     h_pop[:, DIM:] = 0
     h_rot = torch.from_numpy(rot).pin_memory()
     h_sh = torch.from_numpy(sh).pin_memory()
-    h_fit = torch.zeros(n, dtype=torch.float32).pin_memory()
-    pop, cand = torch.empty(n, ld, device=dev), torch.zeros(n, ld, device=dev)
-    pfit, cfit = torch.empty(n, device=dev), torch.empty(n, device=dev)
-    d_rot, d_sh = torch.empty(ld, DIM, device=dev), torch.empty(ld, device=dev)
+    h_fit = torch.zeros(n, dtype=tdt).pin_memory()
+    pop, cand = torch.empty(n, ld, dtype=tdt, device=dev), torch.zeros(n, ld, dtype=tdt, device=dev)
+    pfit, cfit = torch.empty(n, dtype=tdt, device=dev), torch.empty(n, dtype=tdt, device=dev)
+    d_rot, d_sh = torch.empty(ld, DIM, dtype=tdt, device=dev), torch.empty(ld, dtype=tdt, device=dev)
     rng_state = torch.zeros(16, dtype=torch.int32, device=dev)
     perm = torch.arange(n, dtype=torch.int32, device=dev)
     best = torch.zeros(N_ISLANDS, dtype=torch.int32, device=dev)
-    info = (_lib.DEInfoF32 * N_ISLANDS)(*[_lib.DEInfoF32(0.9, 0.5, 4, POP) for _ in range(N_ISLANDS)])
+    info = (DI * N_ISLANDS)(*[DI(0.9, 0.5, 4, POP) for _ in range(N_ISLANDS)])
     h_info = torch.frombuffer(bytearray(bytes(info)), dtype=torch.uint8).pin_memory()
     d_info = torch.empty_like(h_info, device=dev)
     ii = _lib.IslandInfo(n, N_ISLANDS, perm.data_ptr())
-    pi = _lib.ProblemInfoF32(DIM, FUNC, 1, 0, run_seed(), 0, 0, 100.0, -100.0)
-    P = _lib.PopulationF32(pop.data_ptr(), pfit.data_ptr())
-    C = _lib.PopulationF32(cand.data_ptr(), cfit.data_ptr())
+    pi = PI(DIM, FUNC, 1, 0, run_seed(), 0, 0, 100.0, -100.0)
+    P = Pop(pop.data_ptr(), pfit.data_ptr())
+    C = Pop(cand.data_ptr(), cfit.data_ptr())
     stream = torch.cuda.current_stream()
     L.speo_set_stream(ctypes.c_void_p(stream.cuda_stream))
-    _lib.check(L.API_Initilize_f32(C, rng_state.data_ptr(), ii, pi), "API_Initilize_f32")
+    _lib.check(init(C, rng_state.data_ptr(), ii, pi), "API_Initilize" + sfx)
     steps = max(100, min(args.steps, 2000))
-    h_hist = torch.zeros(steps * n, dtype=torch.float32).pin_memory()  # every generation's fitness
+    h_hist = torch.zeros(steps * n, dtype=tdt).pin_memory()  # every generation's fitness
 
     def upload():
         pop.copy_(h_pop, non_blocking=True)
         d_rot.copy_(h_rot, non_blocking=True)
         d_sh.copy_(h_sh, non_blocking=True)
         d_info.copy_(h_info, non_blocking=True)
-        L.API_evaluateFitness_f32(pfit.data_ptr(), None, None, pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(),
-                                  None, None, None, None, n, DIM, 0.0, FUNC)
+        ev(pfit.data_ptr(), None, None, pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(), None, None, None, None, n,
+           DIM, 0.0, FUNC)
 
     def run_native(nsteps):  # the reference's DE_CUDA::Run loop as one library call (C++ host loop)
         upload()
-        _lib.check(L.speo_de_run_f32(P, C, rng_state.data_ptr(), ii, d_info.data_ptr(), best.data_ptr(), pi,
-                                     d_sh.data_ptr(), d_rot.data_ptr(), None, nsteps, h_hist.data_ptr(), 1,
-                                     stream.cuda_stream), "speo_de_run_f32")
+        _lib.check(de_run(P, C, rng_state.data_ptr(), ii, d_info.data_ptr(), best.data_ptr(), pi, d_sh.data_ptr(),
+                          d_rot.data_ptr(), None, nsteps, h_hist.data_ptr(), 1, stream.cuda_stream), run_name)
         stream.synchronize()
 
     def run_python(nsteps):  # the same calls issued one by one from Python (ctypes)
         upload()
         for _ in range(nsteps):
-            L.API_DE_GenerateNewPopulation_f32(C, P, best.data_ptr(), ii, d_info.data_ptr(), rng_state.data_ptr(),
-                                               pi)
-            L.API_evaluateFitness_f32(cfit.data_ptr(), None, None, cand.data_ptr(), d_sh.data_ptr(),
-                                      d_rot.data_ptr(), None, None, None, None, n, DIM, 0.0, FUNC)
-            L.API_DE_SelectSurvival_f32(P, C, ii, pi)
+            gen(C, P, best.data_ptr(), ii, d_info.data_ptr(), rng_state.data_ptr(), pi)
+            ev(cfit.data_ptr(), None, None, cand.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(), None, None, None, None,
+               n, DIM, 0.0, FUNC)
+            sel(P, C, ii, pi)
             h_fit.copy_(pfit, non_blocking=True)
         stream.synchronize()
 
@@ -694,11 +707,11 @@ def bench_e2e(L, dev, torch, args) -> dict:
         out[name] = n * steps / (time.perf_counter() - t0)
     _lib.check(L.API_CheckCUDAError(), "e2e")
     L.speo_set_stream(None)
-    h2d = (n * ld + ld * DIM + ld) * 4 + len(bytes(info))
+    h2d = (n * ld + ld * DIM + ld) * es + len(bytes(info))
     return {"value": out["native"], "unit": "evals/s", "h2d_bytes_per_step": h2d / steps,
-            "d2h_bytes_per_step": n * 4, "steps": steps,
-            "path": "speo_de_run_f32 (64 sub-islands of 100): the generations of API_DE_GenerateNewPopulation_f32 + "
-                    "API_evaluateFitness_f32 + API_DE_SelectSurvival_f32, bit-identical, with the sub-islands "
+            "d2h_bytes_per_step": n * es, "steps": steps, "dtype": "fp64" if f64 else "fp32",
+            "path": f"{run_name} (64 sub-islands of 100): the generations of API_DE_GenerateNewPopulation{sfx} + "
+                    f"API_evaluateFitness{sfx} + API_DE_SelectSurvival{sfx}, bit-identical, with the sub-islands "
                     "resident in shared memory for up to 100 generations per launch; every generation's fitness vector "
                     "read back to pinned host memory (one copy per launch)",
             "python_loop_value": out["python"],
@@ -871,7 +884,9 @@ def main() -> None:
         from speo_gb300 import _lib
 
         torch.cuda.set_device(0)
-        print(json.dumps({"e2e": bench_e2e(_lib.load(), "cuda:0", torch, args)}))
+        L = _lib.load()
+        print(json.dumps({"e2e": bench_e2e(L, "cuda:0", torch, args),
+                          "e2e_fp64": bench_e2e(L, "cuda:0", torch, args, f64=True)}))
         return
     if args.published_only:
         import torch
