@@ -277,7 +277,9 @@ SPEO_API int speo_evaluate(const speo_segment *d_segs, const speo_work_item *d_i
  * other rotated ids 1-7, 11-16 through the row accumulator). Ids 8, 10 (no rotation) and 17-30
  * (several matrices) are flagged (SPEO_DEVERR_BAD_SEGMENT) and skipped.
  * The population is one flat buffer of n_rows rows, `ld` floats apart, shared by all segments
- * (it is read with TMA tensor loads); tiles are up to SPEO_TILE_TC rows and D <= 128. */
+ * (it is read with TMA tensor loads); tiles are up to SPEO_TILE_TC rows and D <= 128. One
+ * persistent block per SM holds all 512 tensor-memory columns of its SM and more than half of
+ * its shared memory while it runs. */
 SPEO_API int speo_evaluate_tc(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,
                      int dim_lo, int dim_hi, const float *pop, int64_t n_rows, int ld, float *fit,
                      void *stream);
