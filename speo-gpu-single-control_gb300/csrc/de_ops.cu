@@ -285,8 +285,11 @@ int initilize(Pop pop, speo_rng_state *d_rng, speo_island_info ii, Prob pi)
     return check_launch("API_Initilize");
 }
 
+// with_best = false leaves d_best as it is (for callers that know no sub-island's strategy reads it
+// and that the ids are refreshed before anyone reads them).
 template <typename T, typename Pop, typename Info, typename Prob>
-int generate(Pop cand, Pop pop, int *d_best, speo_island_info ii, Info *d_info, speo_rng_state *d_rng, Prob pi)
+int generate(Pop cand, Pop pop, int *d_best, speo_island_info ii, Info *d_info, speo_rng_state *d_rng, Prob pi,
+             bool with_best = true)
 {
     if (int st = validate<T>(pop.elements, ii, pi.dim, "API_DE_GenerateNewPopulation")) return st;
     if (!cand.elements || !pop.fitness_value || !ii.permutated_index || !d_info || !d_rng || !d_best)
@@ -295,12 +298,14 @@ int generate(Pop cand, Pop pop, int *d_best, speo_island_info ii, Info *d_info, 
     if (S < 2) return fail(SPEO_ERR_INVALID_ARG, "API_DE_GenerateNewPopulation: sub-island size %d < 2", S);
     const int ld = np2_of(pi.dim);
     cudaStream_t st = api_stream();
-    if (S >= 1024)
-        k_best_block<T><<<ii.subisland_num, 512, 0, st>>>(pop.fitness_value, ii.permutated_index, S, d_best);
-    else
-        k_best<T><<<(ii.subisland_num + kWarps - 1) / kWarps, 32 * kWarps, 0, st>>>(
-            pop.fitness_value, ii.permutated_index, S, ii.subisland_num, d_best);
-    if (int e = check_launch("global_DE_FindBestIndividualInIsland")) return e;
+    if (with_best) {
+        if (S >= 1024)
+            k_best_block<T><<<ii.subisland_num, 512, 0, st>>>(pop.fitness_value, ii.permutated_index, S, d_best);
+        else
+            k_best<T><<<(ii.subisland_num + kWarps - 1) / kWarps, 32 * kWarps, 0, st>>>(
+                pop.fitness_value, ii.permutated_index, S, ii.subisland_num, d_best);
+        if (int e = check_launch("global_DE_FindBestIndividualInIsland")) return e;
+    }
     // 16-byte chunks cover D (np2 rows keep every chunk in bounds). Positions per warp: the
     // largest of 32, 16, 8, 4, 2, 1 that still gives about 16 warps per SM.
     int ppw = 32;
@@ -328,6 +333,18 @@ int select(Pop pop, Pop cand, speo_island_info ii, Prob pi)
 }
 
 }  // namespace
+
+int dropin_generate_f32(speo_population_f32 c, speo_population_f32 p, int *b, speo_island_info ii,
+                        speo_de_info_f32 *info, speo_rng_state *r, speo_problem_info_f32 pi, bool with_best)
+{
+    return generate<float>(c, p, b, ii, info, r, pi, with_best);
+}
+int dropin_generate_f64(speo_population_f64 c, speo_population_f64 p, int *b, speo_island_info ii,
+                        speo_de_info_f64 *info, speo_rng_state *r, speo_problem_info_f64 pi, bool with_best)
+{
+    return generate<double>(c, p, b, ii, info, r, pi, with_best);
+}
+
 }  // namespace speo
 
 using namespace speo;

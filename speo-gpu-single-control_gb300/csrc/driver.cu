@@ -4,7 +4,7 @@
 // API_DE_GenerateNewPopulation, CEC2014_CUDA::EvaluateFitness (-> API_evaluateFitness) and
 // API_DE_SelectSurvival, with a device synchronisation after each launch; the island driver then
 // reads results back to the host (src/island_EA.cc:78-113). speo_de_run_f32 runs that loop on a
-// private stream, ordered after the caller's stream:
+// private stream, ordered after the caller's stream (speo_de_run_f64: the same in FP64):
 //   * when a sub-island fits a block, kStepGens generations per launch of the fused kernel
 //     (dropin_step.cu, bit-identical to the three calls), each generation's fitness vector
 //     collected in one of two device history buffers and copied to the host on a second stream
@@ -12,7 +12,11 @@
 //   * otherwise over this library's drop-in entry points, where blocks of kBlock generations
 //     (each with its read-back of the fitness vector into pinned host memory) are captured once as
 //     a CUDA graph and replayed, so the per-generation host cost is one graph launch per block
-//     instead of a synchronisation per kernel.
+//     instead of a synchronisation per kernel. There the best-in-sub-island search is left out
+//     of generations whose strategies do not read it, except the last one.
+#include <vector>
+
+#include "common.cuh"
 #include "host.h"
 
 namespace speo {
@@ -85,14 +89,14 @@ bool is_pinned(const void *p)
 
 // The drop-in entry points and the fused step of one precision.
 inline int gen_call(speo_population_f32 c, speo_population_f32 p, int *b, speo_island_info ii, speo_de_info_f32 *info,
-                    speo_rng_state *r, speo_problem_info_f32 pi)
+                    speo_rng_state *r, speo_problem_info_f32 pi, bool with_best)
 {
-    return API_DE_GenerateNewPopulation_f32(c, p, b, ii, info, r, pi);
+    return dropin_generate_f32(c, p, b, ii, info, r, pi, with_best);
 }
 inline int gen_call(speo_population_f64 c, speo_population_f64 p, int *b, speo_island_info ii, speo_de_info_f64 *info,
-                    speo_rng_state *r, speo_problem_info_f64 pi)
+                    speo_rng_state *r, speo_problem_info_f64 pi, bool with_best)
 {
-    return API_DE_GenerateNewPopulation(c, p, b, ii, info, r, pi);
+    return dropin_generate_f64(c, p, b, ii, info, r, pi, with_best);
 }
 inline void eval_call(float *f, float *x, const float *o, const float *m, const int *sh, int n, int d, int fid)
 {
@@ -189,10 +193,26 @@ int de_run(Pop pop, Pop cand, speo_rng_state *rng, speo_island_info ii, Info *d_
                            "driver: fitness read-back");
     }
 
-    // the three entry points in turn; generation g's fitness goes to h_fitness (+ g n with history)
+    // the three entry points in turn; generation g's fitness goes to h_fitness (+ g n with history).
+    // The best-in-sub-island search runs where a sub-island's strategy reads it and in the last
+    // generation, whose ids the calls leave behind (the search reads the population before that
+    // generation's selection, so the last generation never runs inside a captured block).
+    bool any_best = true;
+    if (!e && !fused && generations >= 2 && ii.subisland_num > 0) {
+        std::vector<Info> h_info((size_t)ii.subisland_num);
+        e = check_cuda(cudaMemcpyAsync(h_info.data(), d_info, sizeof(Info) * h_info.size(), cudaMemcpyDeviceToHost,
+                                       d->s),
+                       "driver: DE info");
+        if (!e) e = check_cuda(cudaStreamSynchronize(d->s), "driver: sync");
+        if (!e) {
+            any_best = false;
+            for (const Info &x : h_info) any_best = any_best || strategy_uses_best(x.strategy_ID);
+        }
+    }
     int g_next = 0;
     auto one_generation = [&](bool in_graph) -> int {
-        if (int e2 = gen_call(cand, pop, d_best, ii, d_info, rng, pi)) return e2;
+        const bool with_best = any_best || (!in_graph && g_next == generations - 1);
+        if (int e2 = gen_call(cand, pop, d_best, ii, d_info, rng, pi, with_best)) return e2;
         const int before = sticky_status();
         eval_call(cand.fitness_value, cand.elements, d_shift, d_rot, d_shuffle, n, pi.dim, pi.function_ID);
         if (sticky_status() != before) return sticky_status();
@@ -215,7 +235,7 @@ int de_run(Pop pop, Pop cand, speo_rng_state *rng, speo_island_info ii, Info *d_
             if (!e) e = check_cuda(ce, "driver: end capture");
         }
         if (!e) e = check_cuda(cudaGraphInstantiate(&x, g, 0), "driver: instantiate");
-        for (; !e && done + kBlock <= generations; done += kBlock)
+        for (; !e && done + kBlock < generations; done += kBlock)  // the last generation runs below
             e = check_cuda(cudaGraphLaunch(x, d->s), "driver: graph launch");
         const int es = check_cuda(cudaStreamSynchronize(d->s), "driver: sync");
         if (!e) e = es;

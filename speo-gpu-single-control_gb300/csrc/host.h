@@ -89,6 +89,13 @@ int dropin_step_f64(speo_population_f64 pop, speo_population_f64 cand, int *d_be
                     speo_de_info_f64 *d_info, speo_rng_state *rng, speo_problem_info_f64 pi, const double *shift,
                     const double *rot, int generations, double *d_hist, int pair_mode, cudaStream_t st);
 
+// API_DE_GenerateNewPopulation(_f32) with the best-in-sub-island search optional (de_ops.cu):
+// with_best = false leaves d_best untouched.
+int dropin_generate_f32(speo_population_f32 c, speo_population_f32 p, int *b, speo_island_info ii,
+                        speo_de_info_f32 *info, speo_rng_state *r, speo_problem_info_f32 pi, bool with_best);
+int dropin_generate_f64(speo_population_f64 c, speo_population_f64 p, int *b, speo_island_info ii,
+                        speo_de_info_f64 *info, speo_rng_state *r, speo_problem_info_f64 pi, bool with_best);
+
 // Byte offsets of the BF16 weight images inside `img`: W1 (h x 64), W2 (h x h), W2^T (h x h).
 size_t mlp_img_w2_offset(int h);
 size_t mlp_img_w2t_offset(int h);
