@@ -19,7 +19,8 @@ REF_LIB_DIR = Path("/root/reference/SPEO-GPU-single-control/CUDA_EA_library")
 def declared_functions() -> list[str]:
     text = HEADER.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"^\s*(?:SPEO_API\s+)?(?:const\s+)?(?:int|void|char)\s*\*?\s*([A-Za-z_]\w*)\s*\(", text, flags=re.M)
+    names = re.findall(r"^\s*(?:SPEO_API\s+)?(?:const\s+)?(?:int|void|char|size_t|u?int(?:32|64)_t)\s*\*?\s*"
+                       r"([A-Za-z_]\w*)\s*\(", text, flags=re.M)
     return sorted(set(names))
 
 
@@ -33,6 +34,16 @@ def test_header_declares_reference_entry_points():
 def test_library_exports_every_declared_symbol(lib):
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_bindings_cover_the_header_exactly():
+    """Every function the header declares has a ctypes signature, and every signature names a
+    declared function."""
+    from speo_gb300 import _lib
+
+    declared = set(declared_functions())
+    assert "speo_archipelago_state_bytes" in declared
+    assert declared == set(_lib.SIGNATURES), (declared ^ set(_lib.SIGNATURES))
 
 
 def test_version(lib):
