@@ -1,17 +1,27 @@
 """Benchmark of the island-model DE generation loop on GB300.
 
-Workload (the island-model configuration the headline metric is quoted on): 64 islands x
-P = 100, D = 30, rotated Rastrigin z = M (0.0512 (x - o)) (CEC2014 F9 form, f - f*), F = 0.5,
-CR = 0.9, DE/rand/1/bin, ring migration of each island's best 5 into the next island's worst
-5 every 50 generations; seeded synthetic o ~ U[-80, 80]^30 and Haar M.
+Headline workload (the learned-surrogate configuration): 128 islands x P = 256, D = 50, rotated
+Rastrigin z = M (0.0512 (x - o)) (CEC2014 F9 form, f - f*), F = 0.5, CR = 0.9, DE/rand/1/bin,
+ring migration of each island's best 5 into the next island's worst 5 every 50 generations;
+seeded synthetic o ~ U[-80, 80]^50 and Haar M.
 
-A step is one generation over all islands (6400 exact evaluations). `value` is exact
-evaluations/s over the whole job with the population resident in HBM; `e2e` is the same rate
-through the reference-shaped C ABI (API_DE_GenerateNewPopulation_f32 / API_evaluateFitness_f32
-/ API_DE_SelectSurvival_f32) with host buffers, the initial upload and a per-generation
-fitness read-back inside the timed region.
+A step is one generation over all islands (32,768 exact evaluations). After --warmup untimed
+generations, exactly --steps generations are timed. Generations run island-resident (one
+launch per stretch between migrations); the L2 is flushed (512 MB write) before each launch.
+`value` is the plain DE loop's exact evaluations/s over the whole job with the population
+resident in HBM. `e2e` is the same loop through the reference-shaped C ABI (speo_de_run_f32 =
+the generations of API_DE_GenerateNewPopulation_f32 / API_evaluateFitness_f32 /
+API_DE_SelectSurvival_f32, plus the ring migration) with host buffers: the initial population
+and instance uploaded and every generation's fitness vector read back inside the timed region.
+`surrogate` sets the surrogate-screened DE beside the plain DE on the same GPU (exact
+evaluations and wall time to an FP64 error of 1e-8 on the rotated sphere of the same shape, and
+to the plain run's final error on the rotated Rastrigin).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl speo|reference]
+The last stdout line is the JSON record (a few KB). --full also measures the secondary
+sections (64 x 100 island ring at D = 30, operators at bandwidth scale, precision, batched runs,
+network kernels, the reference's published configuration) into --sections-out.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl speo|reference] [--full]
 """
 from __future__ import annotations
 
@@ -30,24 +40,22 @@ REPO = Path(__file__).resolve().parent
 sys.path.insert(0, str(REPO / "speo-gpu-single-control_gb300"))
 sys.path.insert(0, str(REPO / "oracle"))
 
-METRIC = "exact-eval gens/s & evals/s to 1e-8 error: surrogate vs plain DE, same GB300"
-N_ISLANDS, POP, DIM, FUNC = 64, 100, 30, 9
+METRIC = "exact-eval gens/s & evals to 1e-8 error: surrogate vs plain DE, same GB300"
+N_ISLANDS, POP, DIM, FUNC = 128, 256, 50, 9
 INTERVAL, MIGRANTS = 50, 5
-SEED = 9 * 2  # run_seed(node 1, function 9, run 1) = (1 + 9) * (1 + 9) is used below
-
-
-def run_seed() -> int:
-    from speo_gb300.instances import run_seed as rs
-
-    return rs(1, FUNC, 1)
+EVALS_PER_STEP = N_ISLANDS * POP
+WORKLOAD = ("learned-surrogate configuration, plain DE leg: 128 islands x P=256, D=50, rotated Rastrigin "
+            "(F9 form, scale 0.0512), DE/rand/1/bin F=0.5 CR=0.9, ring best-5 -> worst-5 every 50 generations")
+# FP32 FMA lanes of one SM (four partitions of 32): the CUDA-core roofline of the resident kernels
+FP32_FMA_PER_SM_CLK = 128
 
 
 def peaks() -> dict:
     p = REPO / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return {"hbm_gbs": d["hbm_gbs"], "src": "measured"}
-    return {"hbm_gbs": 6800.0, "src": "fallback"}
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d.get("bf16_tflops"), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "src": "fallback"}
 
 
 class ClockSampler:
@@ -60,19 +68,21 @@ class ClockSampler:
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
+        self.lines = []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)   # the first sample lands before the timed work starts
         except FileNotFoundError:
             self.proc = None
         return self
 
     def __exit__(self, *exc):
-        self.lines = []
         if self.proc is not None:
+            time.sleep(0.25)
             self.proc.terminate()
             out, _ = self.proc.communicate(timeout=10)
             self.lines = [ln for ln in out.splitlines() if ln.strip()]
@@ -80,7 +90,7 @@ class ClockSampler:
     def summary(self) -> dict:
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in getattr(self, "lines", []):
+        for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -98,27 +108,6 @@ class ClockSampler:
 
 def flush_l2(buf) -> None:
     buf.add_(1.0)   # writes 512 MB, > 4x the 129 MB L2
-
-
-def island_specs(rank: int):
-    """Config 1's island ring for one rank: under torchrun each rank runs an independent replica
-    of the ring (its own Philox seeds, the same instance), so per-GPU work is fixed as N grows."""
-    from speo_gb300.device import SegmentSpec
-    from speo_gb300.instances import make_instance
-
-    seed = run_seed()
-    inst = [make_instance(seed, DIM)]
-    specs = [SegmentSpec(pop_size=POP, dim=DIM, func_id=FUNC, instance=0, seed=seed * 1000003 + rank,
-                         ring_next=(i + 1) % N_ISLANDS) for i in range(N_ISLANDS)]
-    return specs, inst
-
-
-def island_table(device: str, rank: int):
-    from speo_gb300.device import SegmentTable
-
-    specs, inst = island_specs(rank)
-    # tiles of 50 rows: two balanced tiles per island
-    return SegmentTable(specs, inst, tile_rows=50, device=device)
 
 
 def max_over_ranks(value: float, device: str, world: int) -> float:
@@ -145,24 +134,6 @@ def capture(torch, fn):
     return g
 
 
-def capture_epoch(tab, torch):
-    """One CUDA graph = INTERVAL generations + the ring migration. Islands that fit one block's
-    shared memory run the epoch as one resident launch; otherwise INTERVAL fused launches (an
-    even number, so the double buffers end where they started)."""
-    assert INTERVAL % 2 == 0
-    if tab.epoch_fits():
-        def epoch():
-            tab.epoch(INTERVAL)
-            tab.migrate(MIGRANTS)
-        return capture(torch, epoch), "resident"
-
-    def epoch():
-        for _ in range(INTERVAL):
-            tab.generation()
-        tab.migrate(MIGRANTS)
-    return capture(torch, epoch), "per-generation"
-
-
 def time_graph(torch, graph, reps, flush):
     flush_l2(flush)
     s = torch.cuda.current_stream()
@@ -173,6 +144,33 @@ def time_graph(torch, graph, reps, flush):
     b.record(s)
     torch.cuda.synchronize()
     return a.elapsed_time(b) / reps
+
+
+def chunks(done: int, n: int, interval: int = INTERVAL):
+    """Split n generations, starting after `done` generations, at the migration points: yields
+    (generations, migrate_after) with a migration after every generation count that is a multiple
+    of `interval` (src/island_EA.cc:94-99 migrates when gen % interval == 0)."""
+    while n > 0:
+        k = min(n, interval - done % interval)
+        done += k
+        n -= k
+        yield k, done % interval == 0
+
+
+def headline_table(dev: str, rank: int = 0, func: int = FUNC):
+    from speo_gb300 import workloads as w
+
+    specs, inst = w.config4_specs(func, rank=rank)
+    return w.table(specs, inst, device=dev)
+
+
+def run_plain(tab, n: int, done: int) -> int:
+    """n plain generations (island-resident launches, ring migration at the migration points)."""
+    for k, mig in chunks(done, n):
+        tab.epoch(k)
+        if mig:
+            tab.migrate(MIGRANTS)
+    return done + n
 
 
 def bench_speo(args) -> dict:
@@ -190,104 +188,392 @@ def bench_speo(args) -> dict:
     from speo_gb300 import _lib
 
     L = _lib.load()
-    tab = island_table(dev, rank)
+    tab = headline_table(dev, rank)
+    if not tab.epoch_fits():
+        raise RuntimeError("the headline islands do not fit one block's shared memory on this GPU")
     tab.init_population()
-    graph, mode = capture_epoch(tab, torch)
-    epochs_w = max(1, (args.warmup + INTERVAL - 1) // INTERVAL)
-    epochs = max(1, (args.steps + INTERVAL - 1) // INTERVAL)
-    steps = epochs * INTERVAL
-    for _ in range(epochs_w):
-        graph.replay()
+    done = run_plain(tab, args.warmup, 0)                  # exactly W untimed generations
     torch.cuda.synchronize()
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(epochs)]
+    plan = list(chunks(done, args.steps))
+    ev = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(3)) for _ in plan]
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        for i in range(epochs):
-            flush_l2(flush)                        # L2 flushed between timed epochs
-            ev[i][0].record()
-            graph.replay()
-            ev[i][1].record()
+        for (k, mig), (a, b, c) in zip(plan, ev):
+            flush_l2(flush)                                # L2 flushed before every launch
+            a.record()
+            tab.epoch(k)
+            b.record()
+            if mig:
+                tab.migrate(MIGRANTS)
+            c.record()
         torch.cuda.synchronize()
+        # the dominant kernel alone, 50-generation launches back to back (clocks still sampled)
+        kg = capture(torch, lambda: tab.epoch(INTERVAL))
+        launch50_ms = time_graph(torch, kg, 20, flush)
     if world > 1:
         torch.distributed.barrier()
-    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev), dev, world)
-    evals_per_step = N_ISLANDS * POP
-    value = evals_per_step * steps * world / (ms / 1e3)
-
-    # ---- dominant kernel: average duration of one launch (graphs of back-to-back launches) ------
-    alg_bytes_gen = evals_per_step * (5 * DIM * 4 + 2 * 4)   # 4 row reads + 1 row write + 2 fitness
-    reps = 40
-    if mode == "resident":
-        kg = capture(torch, lambda: tab.epoch(INTERVAL))
-        launch_ms = time_graph(torch, kg, reps, flush)
-        if 2 * N_ISLANDS <= torch.cuda.get_device_properties(dev).multi_processor_count:
-            kernel = (f"k_island_epoch2<1> ({INTERVAL} generations per launch, each island resident in the "
-                      f"shared memory of a two-block cluster: {2 * N_ISLANDS} blocks)")
-        else:
-            kernel = f"k_island_epoch<1> ({INTERVAL} generations per launch, islands resident in shared memory)"
-        alg_bytes = alg_bytes_gen * INTERVAL
-    else:
-        kg = capture(torch, lambda: [tab.generation() for _ in range(INTERVAL)])
-        launch_ms = time_graph(torch, kg, reps, flush) / INTERVAL
-        kernel = "k_generation<1> (fused generate+evaluate+select)"
-        alg_bytes = alg_bytes_gen
-    # the per-generation fused kernel on the same islands, for comparison
-    pg = capture(torch, lambda: [tab.generation() for _ in range(INTERVAL)])
-    per_gen_us = time_graph(torch, pg, 10, flush) / INTERVAL * 1e3
-    pk = peaks()
-    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    step_ms = sum(a.elapsed_time(c) for a, _, c in ev)
+    kern_ms = sum(a.elapsed_time(b) for a, b, _ in ev)
+    ms = max_over_ranks(step_ms, dev, world)
+    value = EVALS_PER_STEP * args.steps * world / (ms / 1e3)
+    n_mig = sum(1 for _, m in plan if m)
     rows, errs = tab.best_f64()
     best_err = float(errs.min().item())
 
+    pk = peaks()
+    clocks = clk.summary()
+    alg_bytes_gen = EVALS_PER_STEP * (5 * DIM * 4 + 2 * 4)  # 4 row reads + 1 row write + 2 fitness per eval
+    achieved = alg_bytes_gen * args.steps / (kern_ms / 1e3) / 1e9
+    pair = 2 * N_ISLANDS <= sms
+    kernel = (f"k_island_epoch2<2> (two-block cluster per island, {2 * N_ISLANDS} blocks)" if pair else
+              f"k_island_epoch<2> (one 512-thread block per island, {N_ISLANDS} blocks; up to 50 generations "
+              "per launch with the island, its trials and M^T in shared memory)")
+    rot_flop_gen = EVALS_PER_STEP * 2 * DIM * DIM
+    sm_mhz = clocks["sm_max_mhz"] or 2070.0
+    fp32_peak = sms * FP32_FMA_PER_SM_CLK * 2 * sm_mhz * 1e6 / 1e12
+    fp32_achieved = rot_flop_gen * args.steps / (kern_ms / 1e3) / 1e12
     out = {
-        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": steps,
-        "warmup": epochs_w * INTERVAL, "ms_per_step": ms / steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": "island model: 64 islands x P=100, D=30, rotated Rastrigin (F9 form), "
-                               "DE/rand/1/bin F=0.5 CR=0.9, ring best-5 -> worst-5 every 50 generations",
-                   "islands": N_ISLANDS, "pop_size": POP, "dim": DIM, "migration_interval": INTERVAL,
-                   "migrants": MIGRANTS, "step": "one generation over all islands (6400 exact evaluations)",
-                   "l2": "flushed (512 MB write) before each timed 50-generation epoch; the population "
-                         "(1.5 MB) stays L2-resident within an epoch as in a real run",
-                   "graph": "one CUDA graph per epoch: the 50 generations (one island-resident launch, or 50 "
-                            "fused launches when an island does not fit shared memory) + 2 migration launches"},
-        "gens_per_s": steps * world / (ms / 1e3) / world,
-        "best_error_f64_after_run": best_err,
-        "roofline": {"kernel": kernel, "bound": "hbm",
-                     "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": achieved / pk["hbm_gbs"],
-                     "traffic": EPOCH_TRAFFIC_BYTES if mode == "resident" else None,
-                     "traffic_src": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_island_epoch2 launch "
-                                    "at this workload (the island is read once per launch; its writes stay in L2)"
-                     if mode == "resident" else None,
-                     "peak_src": pk["src"],
-                     "alg_bytes_per_launch": alg_bytes, "launch_us": launch_ms * 1e3,
-                     "note": "achieved = algorithmic bytes of a streaming generation (5 D s + 2 s per "
-                             "individual-generation) / launch time"},
-        "per_generation_kernel_us": per_gen_us,
-        "epoch_mode": mode,
-        "gpu_launches": epochs * ((1 if mode == "resident" else INTERVAL) + 2),
-        "clocks": clk.summary(),
+        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded o ~ U[-80,80]^50, Haar M, uniform init)",
+        "config": {"workload": WORKLOAD, "islands": N_ISLANDS, "pop_size": POP, "dim": DIM, "func_id": FUNC,
+                   "migration_interval": INTERVAL, "migrants": MIGRANTS,
+                   "step": f"one generation over all islands ({EVALS_PER_STEP} exact evaluations)",
+                   "l2": "flushed (512 MB write) before every timed launch; a launch runs up to 50 generations "
+                         "with each island resident in shared memory",
+                   "launches": f"{len(plan)} island-resident launches + {2 * n_mig} migration launches"},
+        "gens_per_s": args.steps / (ms / 1e3),
+        "best_error_f64": best_err,
+        "roofline": {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": EPOCH50_TRAFFIC_BYTES * args.steps / INTERVAL
+                     if EPOCH50_TRAFFIC_BYTES else None,
+                     "peak_src": f"{pk['src']} (MEASURED_PEAKS hbm_gbs)",
+                     "alg_bytes_per_step": alg_bytes_gen, "kernel_ms_timed": kern_ms,
+                     "launch_us_50_generations": launch50_ms * 1e3,
+                     "note": "achieved = streaming-equivalent bytes (5 D s + 2 s per individual-generation) / kernel "
+                             "time; the island stays in shared memory, so DRAM traffic is far below them",
+                     "fp32": {"achieved_tflops": fp32_achieved, "peak_tflops": fp32_peak, "frac": fp32_achieved / fp32_peak,
+                              "flop_per_eval": 2 * DIM * DIM,
+                              "peak_src": f"nominal: {sms} SMs x {FP32_FMA_PER_SM_CLK} FP32 FMA/clk x 2 x {sm_mhz:.0f} MHz"}},
+        "gpu_launches": len(plan) + 2 * n_mig,
+        "clocks": clocks,
     }
-    if rank != 0:  # the remaining sections are single-GPU measurements: rank 0 alone
+    if rank != 0:
         return out
-    if not args.no_ops:
-        out["operators_bandwidth_scale"] = bench_operators(L, dev, torch, pk)
-    if not args.no_configs:
-        out["config2_precision"] = bench_config2(L, dev, torch, flush)
-        out["config3_batched"] = bench_config3(L, dev, torch, flush)
-        out["config4_surrogate_vs_plain"] = bench_config4(L, dev, torch, args.c4_gens)
-        out["surrogate_mlp"] = bench_mlp(L, dev, torch)
-        out["published_config"] = bench_published(L, dev, torch)
+    if not args.no_surrogate:
+        out["surrogate"] = bench_surrogate(L, dev, torch)
     if not args.no_e2e:
-        out["e2e"] = bench_e2e(L, dev, torch, args)
-        # the same end-to-end loop in the reference's shipped precision
-        out["e2e_fp64"] = bench_e2e(L, dev, torch, args, f64=True)
-    if rank == 0 and not args.no_cpu:
+        out["e2e"] = bench_e2e(L, dev, torch, max(args.steps, 100))
+    if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(sample_s=args.cpu_sample_s)
     return out
+
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 50-generation island-resident
+# launch of the headline workload, from an ncu capture of that launch; None until captured.
+EPOCH50_TRAFFIC_BYTES = None
+C4_TRAIN_STEPS = 48   # Adam steps per generation: 48 x 4096 = 6 passes over a generation's 32768 new rows
+C4_EXPLORE = 0.05     # fraction of targets that take a uniformly drawn trial instead of the screened one
+
+
+def c4_run(L, dev, torch, func: int, mode: str, max_gens: int, log_every: int = 10, stop_at: float | None = None,
+           train_steps: int = 16, explore: float = 0.25, train_k: int = 8, train_every: int = 1,
+           use_graph: bool = True):
+    """One run of the headline shape (plain or surrogate-screened) logging the FP64 best error
+    every `log_every` generations; stops early once the error reaches `stop_at`. Blocks of
+    `log_every` generations replay one CUDA graph after the first (eager) block. The surrogate
+    trains `train_steps` Adam steps in every `train_every`-th generation of a block."""
+    import ctypes as C
+
+    from speo_gb300 import _lib
+    from speo_gb300 import workloads as w
+
+    specs, inst = w.config4_specs(func)
+    tab = w.table(specs, inst, device=dev)
+    tab.init_population()
+    surr = None
+    if mode == "surrogate":
+        surr = C.c_void_p()
+        _lib.check(L.speo_surrogate_create(C.byref(surr), 50, 256, 1 << 20, 4096, 1e-3, 0.01, 4242),
+                   "speo_surrogate_create")
+    assert log_every % 2 == 0 and INTERVAL % log_every == 0 and log_every % train_every == 0
+
+    def block():  # log_every generations (an even number: the double buffers end where they began)
+        if mode == "plain":
+            tab.epoch(log_every)
+        else:
+            for i in range(log_every):
+                steps = train_steps if (i + 1) % train_every == 0 else 0
+                tab.surrogate_generation(surr, k=train_k, train_steps=steps, explore=explore)
+
+    curve, t_total, graph = [], 0.0, None
+    try:
+        for g0 in range(0, max_gens, log_every):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            if graph is None:
+                block()   # first block eagerly: scratch allocation, archive seeding
+            else:
+                graph.replay()
+            if (g0 + log_every) % INTERVAL == 0:
+                tab.migrate(MIGRANTS)
+            b.record()
+            torch.cuda.synchronize()
+            t_total += a.elapsed_time(b) / 1e3
+            if graph is None and use_graph:  # later blocks replay one CUDA graph (not executed by capture)
+                graph = torch.cuda.CUDAGraph()
+                cs = torch.cuda.Stream()
+                cs.wait_stream(torch.cuda.current_stream())
+                with torch.cuda.stream(cs), torch.cuda.graph(graph, stream=cs):
+                    block()
+                torch.cuda.current_stream().wait_stream(cs)
+            rows, errs = tab.best_f64()
+            curve.append({"gen": g0 + log_every, "exact_evals": (g0 + log_every) * tab.rows, "wall_s": t_total,
+                          "best_err": float(errs.min().item())})
+            if stop_at is not None and curve[-1]["best_err"] <= stop_at:
+                break
+    finally:
+        if surr is not None:
+            L.speo_surrogate_destroy(surr)
+    gens = curve[-1]["gen"]
+    hit = next((c for c in curve if stop_at is not None and c["best_err"] <= stop_at), None)
+    return {"final_err": curve[-1]["best_err"], "generations": gens, "wall_s": t_total,
+            "gens_per_s": gens / t_total, "exact_evals_per_s": gens * tab.rows / t_total,
+            "exact_evals_to_target": None if hit is None else hit["exact_evals"],
+            "wall_s_to_target": None if hit is None else hit["wall_s"]}, curve
+
+
+def first_reach(curve, target):
+    return next((c for c in curve if c["best_err"] <= target), None)
+
+
+def bench_surrogate(L, dev, torch, ras_gens: int = 200, schedule: dict | None = None) -> dict:
+    """Surrogate-screened DE against the plain DE on the headline shape, same GPU: (a) the
+    rotated sphere of the same shape run to an FP64 error of 1e-8 (capped), which gives the
+    exact evaluations and wall time each method needs to get there; (b) the rotated Rastrigin
+    for `ras_gens` generations, and where the surrogate first reaches the plain run's final
+    error. Both methods spend 32,768 exact evaluations per generation."""
+    from speo_gb300 import _lib
+
+    sch = dict(train_steps=C4_TRAIN_STEPS, explore=C4_EXPLORE, train_k=8, train_every=1)
+    if schedule:
+        sch.update(schedule)
+    out = {"network": "MLP 50-256-256-1, BF16 tcgen05 screening and training, FP32 accumulate, Adam lr 1e-3, "
+                      "batch 4096, archive 2^20, k=8 trials per target", "schedule": sch}
+    sp, _ = c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "plain", 4000, stop_at=1e-8)
+    ss, _ = c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8, **sch)
+    sph = {"target": 1e-8,
+           "plain": {k: sp[k] for k in ("generations", "exact_evals_to_target", "wall_s_to_target", "final_err")},
+           "surrogate": {k: ss[k] for k in ("generations", "exact_evals_to_target", "wall_s_to_target", "final_err")}}
+    ep, es = sp["exact_evals_to_target"], ss["exact_evals_to_target"]
+    wp, ws = sp["wall_s_to_target"], ss["wall_s_to_target"]
+    sph["exact_evals_ratio_plain_over_surrogate"] = ep / es if ep and es else None
+    sph["wall_ratio_plain_over_surrogate"] = wp / ws if wp and ws else None
+    out["rotated_sphere"] = sph
+    rp, cp = c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, "plain", ras_gens)
+    rs, cs = c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, "surrogate", ras_gens, **sch)
+    hit = first_reach(cs, rp["final_err"])
+    hit_p = first_reach(cp, rp["final_err"])
+    out["rotated_rastrigin"] = {
+        "generations": ras_gens, "plain_final_err": rp["final_err"], "surrogate_final_err": rs["final_err"],
+        "plain_gens_per_s": rp["gens_per_s"], "surrogate_gens_per_s": rs["gens_per_s"],
+        "surrogate_reaches_plain_final_error": None if hit is None else {
+            "at_gen": hit["gen"], "exact_evals_ratio_plain_over_surrogate": hit_p["exact_evals"] / hit["exact_evals"],
+            "wall_ratio_plain_over_surrogate": hit_p["wall_s"] / hit["wall_s"]},
+        "note": "1e-8 is not reached by either method on the rotated Rastrigin at D=50 (multimodal); the "
+                "comparison is at the smallest error both reach"}
+    return out
+
+
+def bench_e2e(L, dev, torch, steps: int) -> dict:
+    """The headline loop through the reference-shaped C ABI with host buffers: the initial
+    population, o, M^T and the per-sub-island DEInfo uploaded from pinned host memory, the
+    initial API_evaluateFitness_f32, then `steps` generations of speo_de_run_f32 (128 sub-islands
+    of 256 in the reference layout, np2 = 64) with every generation's fitness vector read back to
+    pinned host memory, and speo_ring_migrate (best 5 -> next sub-island's worst 5) every 50
+    generations; all inside the timed region (wall clock, synchronous calls)."""
+    from speo_gb300 import _lib
+    from speo_gb300 import workloads as w
+
+    n, ld = EVALS_PER_STEP, 64
+    specs, inst = w.config4_specs(FUNC)
+    o, M = inst[0]
+    seed = specs[0].seed
+    rot = np.zeros((ld, DIM), dtype=np.float32)
+    rot[:DIM] = M.T
+    sh = np.zeros(ld, dtype=np.float32)
+    sh[:DIM] = o
+    rng = np.random.default_rng(0)
+    h_pop = torch.from_numpy(rng.uniform(-100, 100, (n, ld)).astype(np.float32)).pin_memory()
+    h_pop[:, DIM:] = 0
+    h_rot, h_sh = torch.from_numpy(rot).pin_memory(), torch.from_numpy(sh).pin_memory()
+    pop, cand = torch.empty(n, ld, device=dev), torch.zeros(n, ld, device=dev)
+    pfit, cfit = torch.empty(n, device=dev), torch.empty(n, device=dev)
+    d_rot, d_sh = torch.empty(ld, DIM, device=dev), torch.empty(ld, device=dev)
+    rng_state = torch.zeros(16, dtype=torch.int32, device=dev)
+    perm = torch.arange(n, dtype=torch.int32, device=dev)
+    best = torch.zeros(N_ISLANDS, dtype=torch.int32, device=dev)
+    info = (_lib.DEInfoF32 * N_ISLANDS)(*[_lib.DEInfoF32(0.9, 0.5, 4, POP) for _ in range(N_ISLANDS)])
+    h_info = torch.frombuffer(bytearray(bytes(info)), dtype=torch.uint8).pin_memory()
+    d_info = torch.empty_like(h_info, device=dev)
+    segs = (_lib.Segment * N_ISLANDS)()
+    for i in range(N_ISLANDS):  # the sub-islands as ring segments (identity permutation)
+        s = segs[i]
+        s.row0, s.pop_size, s.dim, s.ld, s.func_id, s.ring_next = i * POP, POP, DIM, ld, FUNC, (i + 1) % N_ISLANDS
+    d_segs = torch.frombuffer(bytearray(bytes(segs)), dtype=torch.uint8).to(dev)
+    staging = torch.zeros(N_ISLANDS * MIGRANTS * (ld + 1), device=dev)
+    ii = _lib.IslandInfo(n, N_ISLANDS, perm.data_ptr())
+    pi = _lib.ProblemInfoF32(DIM, FUNC, 1, 0, seed & 0x7fffffff, 0, 0, 100.0, -100.0)
+    P = _lib.PopulationF32(pop.data_ptr(), pfit.data_ptr())
+    C = _lib.PopulationF32(cand.data_ptr(), cfit.data_ptr())
+    stream = torch.cuda.current_stream()
+    L.speo_set_stream(ctypes.c_void_p(stream.cuda_stream))
+    h_hist = torch.zeros(steps * n, dtype=torch.float32).pin_memory()  # every generation's fitness
+
+    def run(nsteps):
+        _lib.check(L.API_Initilize_f32(C, rng_state.data_ptr(), ii, pi), "API_Initilize_f32")
+        pop.copy_(h_pop, non_blocking=True)
+        d_rot.copy_(h_rot, non_blocking=True)
+        d_sh.copy_(h_sh, non_blocking=True)
+        d_info.copy_(h_info, non_blocking=True)
+        L.API_evaluateFitness_f32(pfit.data_ptr(), None, None, pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(),
+                                  None, None, None, None, n, DIM, 0.0, FUNC)
+        g = 0
+        for k, mig in chunks(0, nsteps):
+            _lib.check(L.speo_de_run_f32(P, C, rng_state.data_ptr(), ii, d_info.data_ptr(), best.data_ptr(), pi,
+                                         d_sh.data_ptr(), d_rot.data_ptr(), None, k,
+                                         ctypes.c_void_p(h_hist.data_ptr() + 4 * g * n), 1, stream.cuda_stream),
+                       "speo_de_run_f32")
+            g += k
+            if mig:
+                _lib.check(L.speo_ring_migrate(d_segs.data_ptr(), N_ISLANDS, MIGRANTS, pop.data_ptr(), pfit.data_ptr(),
+                                               staging.data_ptr(), ld, stream.cuda_stream), "speo_ring_migrate")
+        stream.synchronize()
+
+    run(20)
+    t0 = time.perf_counter()
+    run(steps)
+    dt = time.perf_counter() - t0
+    _lib.check(L.API_CheckCUDAError(), "e2e")
+    L.speo_set_stream(None)
+    h2d = (n * ld + ld * DIM + ld) * 4 + len(bytes(info))
+    return {"value": n * steps / dt, "unit": "evals/s", "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": n * 4,
+            "steps": steps, "dtype": "fp32",
+            "path": "speo_de_run_f32 over 128 sub-islands of 256 (reference layout, np2=64): the generations of "
+                    "API_DE_GenerateNewPopulation_f32 + API_evaluateFitness_f32 + API_DE_SelectSurvival_f32 "
+                    "(bit-identical), every generation's fitness read back; speo_ring_migrate every 50 generations"}
+
+
+def cpu_setup():
+    import speo_oracle
+    from speo_gb300 import workloads as w
+
+    specs, inst = w.config4_specs(FUNC)
+    o, M = inst[0]
+    ld = 64
+    seed = specs[0].seed
+    pop = speo_oracle.init_population(EVALS_PER_STEP, ld, DIM, -100.0, 100.0, seed).astype(np.float64)
+    fit = speo_oracle.evaluate_rows(FUNC, pop.astype(np.float32), DIM, o, M)
+    return o, M, ld, seed, pop, fit
+
+
+def cpu_generations(state, gen0: int, gens: int, threads: int) -> int:
+    """gens generations of the headline workload on the host cores in FP64: the oracle port of the
+    reference's DE generation (kernel_DE_CUDA.cu:172-327) and CEC2014 objective, ring migration
+    at the migration points, islands spread over `threads` threads."""
+    import speo_oracle
+
+    o, M, ld, seed, pop, fit = state
+    return speo_oracle.run_islands_f64(N_ISLANDS, POP, DIM, ld, FUNC, 0.5, 0.9, -100.0, 100.0, o, M, seed, gen0, gens,
+                                       INTERVAL, MIGRANTS, pop, fit, threads)
+
+
+def cpu_baseline(sample_s: float = 10.0) -> dict:
+    threads = os.cpu_count() or 1
+    state = cpu_setup()
+    gens, evals, t_used, chunk = 0, 0, 0.0, 1
+    while t_used < sample_s:
+        t0 = time.perf_counter()
+        evals += cpu_generations(state, gens, chunk, threads)
+        t_used += time.perf_counter() - t0
+        gens += chunk
+        chunk = min(chunk * 2, 50)
+    return {"value": evals / t_used, "unit": "evals/s", "cores": threads, "kind": "port",
+            "sample": f"{gens} generations of the headline workload (128 x 256, D=50) in FP64, {t_used:.1f} s: the "
+                      "oracle restatement of the reference's DE and CEC2014 objective, islands over "
+                      f"{threads} threads"}
+
+
+def bench_reference(args) -> dict | None:
+    """The reference's CPU implementation of the path on the host cores: the oracle port (the
+    reference's compiled CEC2014.cc is x86-only here), all host threads, exactly --warmup untimed
+    and --steps timed generations of the headline workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    state = cpu_setup()
+    cpu_generations(state, 0, args.warmup, threads)
+    t0 = time.perf_counter()
+    evals = cpu_generations(state, args.warmup, args.steps, threads)
+    t = time.perf_counter() - t0
+    rate = evals / t
+    return {"metric": METRIC, "value": rate, "unit": "evals/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+            "data": "synthetic (seeded o ~ U[-80,80]^50, Haar M, uniform init)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "islands": N_ISLANDS, "pop_size": POP, "dim": DIM, "func_id": FUNC,
+                       "migration_interval": INTERVAL, "migrants": MIGRANTS,
+                       "step": f"one generation over all islands ({EVALS_PER_STEP} exact evaluations)"},
+            "cpu_baseline": {"value": rate, "unit": "evals/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} timed generations after {args.warmup} warm-up, {t:.2f} s, "
+                                       f"{threads} threads over islands (oracle port: the reference's compiled "
+                                       "CEC2014.cc is x86-only and its sources are absent on the GPU host)"},
+            "e2e": {"value": rate, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# ---- secondary sections (--full): written to --sections-out, not to the record line ----------
+C1_ISLANDS, C1_POP, C1_DIM = 64, 100, 30
+
+
+def c1_seed() -> int:
+    from speo_gb300.instances import run_seed as rs
+
+    return rs(1, FUNC, 1)
+
+
+def bench_config1(L, dev, torch, flush) -> dict:
+    """Config 1, the 64 x 100 island ring at D = 30 (rotated Rastrigin, ring best-5 -> worst-5 every
+    50 generations): one CUDA graph per 50-generation epoch (one island-resident launch + two
+    migration launches), L2 flushed before each timed epoch; the resident kernel alone from a graph
+    of back-to-back launches."""
+    from speo_gb300 import workloads as w
+
+    specs, inst = w.config1_specs()
+    tab = w.table(specs, inst, device=dev, tile_rows=50)
+    tab.init_population()
+
+    def epoch():
+        tab.epoch(INTERVAL)
+        tab.migrate(MIGRANTS)
+    g = capture(torch, epoch)
+    for _ in range(3):
+        g.replay()
+    ms = time_graph(torch, g, 20, flush) / INTERVAL
+    kg = capture(torch, lambda: tab.epoch(INTERVAL))
+    launch_ms = time_graph(torch, kg, 20, flush)
+    evals = C1_ISLANDS * C1_POP
+    alg = evals * (5 * C1_DIM * 4 + 2 * 4) * INTERVAL
+    pk = peaks()
+    return {"workload": "64 islands x P=100, D=30, rotated Rastrigin, ring best-5 -> worst-5 every 50 generations",
+            "ms_per_generation": ms, "evals_per_s": evals / (ms / 1e3), "gens_per_s": 1e3 / ms,
+            "kernel": "k_island_epoch2<1> (two-block cluster per island, 128 blocks)",
+            "launch_us_50_generations": launch_ms * 1e3, "hbm_equiv_frac": alg / (launch_ms / 1e3) / 1e9 / pk["hbm_gbs"],
+            "fp32_rotation_tflops": evals * INTERVAL * 2 * C1_DIM * C1_DIM / (launch_ms / 1e3) / 1e12}
 
 
 def bench_operators(L, dev, torch, pk, n_isl: int = 16384) -> dict:
@@ -300,7 +586,7 @@ def bench_operators(L, dev, torch, pk, n_isl: int = 16384) -> dict:
     from speo_gb300.instances import make_instance
 
     P, D = 128, 100
-    inst = [make_instance(run_seed() + 1, D)]
+    inst = [make_instance(c1_seed() + 1, D)]
     specs = [SegmentSpec(pop_size=P, dim=D, func_id=FUNC, instance=0, seed=77 + i) for i in range(n_isl)]
     tab = SegmentTable(specs, inst, tile_rows=_lib.TILE_SIMT, device=dev)
     tab_tc = SegmentTable(specs, inst, tile_rows=_lib.TILE_TC, device=dev)
@@ -335,7 +621,7 @@ def bench_operators(L, dev, torch, pk, n_isl: int = 16384) -> dict:
     # tcgen05 evaluation: read D floats, write 1
     tab_tc.pop[0].copy_(tab.pop[tab.cur])
     out_fit = torch.empty(rows, device=dev)
-    rec("k_evaluate_tc (TMA + tcgen05 BF16x3)", timed(lambda: tab_tc.evaluate(which=0, use_tc=True, out=out_fit)),
+    rec("k_evaluate_tc (TMA + tcgen05, three-way BF16 split)", timed(lambda: tab_tc.evaluate(which=0, use_tc=True, out=out_fit)),
         rows * (D * s + s))
     rec("k_eval_seg<4> (CUDA-core evaluation)", timed(lambda: tab.evaluate(which=tab.cur, out=out_fit)),
         rows * (D * s + s))
@@ -384,9 +670,10 @@ def bench_operators(L, dev, torch, pk, n_isl: int = 16384) -> dict:
     return out
 
 
+
 def bench_config2(L, dev, torch, flush) -> dict:
     """Config 2: 256 islands x 128, D = 100, mixed objectives; the rotation runs on the tcgen05
-    tensor cores in BF16x3 (trial generation, tensor-core evaluation and selection per generation,
+    tensor cores in three-way split BF16 (trial generation, tensor-core evaluation and selection per generation,
     20 generations per CUDA graph). Precision: tensor-core and CUDA-core FP32 fitness of 4096
     sampled rows against the FP64 oracle; FP64 re-evaluation of every island's best."""
     import speo_oracle
@@ -421,15 +708,16 @@ def bench_config2(L, dev, torch, flush) -> dict:
     rel_cc = np.abs(fit_cc.cpu().numpy()[sample] - ref) / np.maximum(np.abs(ref), 1e-30)
     rows, errs = tab.best_f64()
     return {"workload": "256 islands x P=128, D=100, per island rotated sphere or rotated Rastrigin (seeded), "
-                        "BF16x3 tcgen05 evaluation",
+                        "three-way split BF16 tcgen05 evaluation (six products)",
             "ms_per_generation": ms, "gens_per_s": 1e3 / ms, "evals_per_s": tab.rows / (ms / 1e3),
             "launches_per_generation": 3,
-            "fitness_rel_err_vs_fp64": {"tcgen05_bf16x3": {"max": float(rel_tc.max()), "median": float(np.median(rel_tc)),
+            "fitness_rel_err_vs_fp64": {"tcgen05_bf16_split3": {"max": float(rel_tc.max()), "median": float(np.median(rel_tc)),
                                                            "p99": float(np.quantile(rel_tc, 0.99))},
                                         "cuda_core_fp32": {"max": float(rel_cc.max()), "median": float(np.median(rel_cc)),
                                                            "p99": float(np.quantile(rel_cc, 0.99))},
                                         "rows_sampled": int(len(sample))},
             "best_error_f64_min_over_islands": float(errs.min().item())}
+
 
 
 def bench_config3(L, dev, torch, flush) -> dict:
@@ -456,121 +744,6 @@ def bench_config3(L, dev, torch, flush) -> dict:
 
 
 # DRAM bytes of one 50-generation island-resident launch of this workload (64 x 100, D = 30), from
-# an ncu capture (dram__bytes_read.sum 932,352 + dram__bytes_write.sum 0): the algorithmic bytes of
-# the same 50 streaming generations are 194.6 MB.
-EPOCH_TRAFFIC_BYTES = 932352
-C4_TRAIN_STEPS = 48   # Adam steps per generation: 48 x 4096 = 6 passes over a generation's 32768 new rows
-C4_EXPLORE = 0.05     # fraction of targets that take a uniformly drawn trial instead of the screened one
-
-
-def _c4_run(L, dev, torch, func: int, mode: str, max_gens: int, log_every: int = 10, stop_at: float | None = None,
-            train_steps: int = 16, explore: float = 0.25, train_k: int = 8, use_graph: bool = True):
-    """One config-4 run (plain or surrogate-screened) logging the FP64 best error every
-    `log_every` generations; stops early once the error reaches `stop_at`. Blocks of `log_every`
-    generations replay one CUDA graph after the first (eager) block."""
-    import ctypes as C
-
-    from speo_gb300 import _lib
-    from speo_gb300 import workloads as w
-
-    specs, inst = w.config4_specs(func)
-    tab = w.table(specs, inst, device=dev)
-    tab.init_population()
-    surr = None
-    if mode == "surrogate":
-        surr = C.c_void_p()
-        _lib.check(L.speo_surrogate_create(C.byref(surr), 50, 256, 1 << 20, 4096, 1e-3, 0.01, 4242),
-                   "speo_surrogate_create")
-    assert log_every % 2 == 0 and 50 % log_every == 0
-
-    def block():  # log_every generations (an even number: the double buffers end where they began)
-        if mode == "plain":
-            if tab.epoch_fits():
-                tab.epoch(log_every)
-            else:
-                for _ in range(log_every):
-                    tab.generation()
-        else:
-            for _ in range(log_every):
-                tab.surrogate_generation(surr, k=train_k, train_steps=train_steps, explore=explore)
-
-    curve, t_total, graph = [], 0.0, None
-    try:
-        for g0 in range(0, max_gens, log_every):
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record()
-            if graph is None:
-                block()   # first block eagerly: scratch allocation, archive seeding
-            else:
-                graph.replay()
-            if (g0 + log_every) % 50 == 0:
-                tab.migrate(5)
-            b.record()
-            torch.cuda.synchronize()
-            t_total += a.elapsed_time(b) / 1e3
-            if graph is None and use_graph:  # later blocks replay one CUDA graph (not executed by capture)
-                graph = torch.cuda.CUDAGraph()
-                cs = torch.cuda.Stream()
-                cs.wait_stream(torch.cuda.current_stream())
-                with torch.cuda.stream(cs), torch.cuda.graph(graph, stream=cs):
-                    block()
-                torch.cuda.current_stream().wait_stream(cs)
-            rows, errs = tab.best_f64()
-            curve.append({"gen": g0 + log_every, "exact_evals": (g0 + log_every) * tab.rows, "wall_s": t_total,
-                          "best_err": float(errs.min().item())})
-            if stop_at is not None and curve[-1]["best_err"] <= stop_at:
-                break
-    finally:
-        if surr is not None:
-            L.speo_surrogate_destroy(surr)
-    gens = curve[-1]["gen"]
-    hit = next((c for c in curve if c["best_err"] <= 1e-8), None)
-    kept = curve[:: max(1, len(curve) // 40)]
-    if kept[-1] is not curve[-1]:
-        kept.append(curve[-1])
-    return {"curve": kept, "final_err": curve[-1]["best_err"], "generations": gens, "wall_s": t_total,
-            "gens_per_s": gens / t_total, "exact_evals_per_s": gens * tab.rows / t_total,
-            "exact_evals_to_1e-8": None if hit is None else hit["exact_evals"],
-            "wall_s_to_1e-8": None if hit is None else hit["wall_s"]}, curve
-
-
-def bench_config4(L, dev, torch, gens: int) -> dict:
-    """Config 4: 128 islands x 256, D = 50. Plain DE against the surrogate-screened DE (MLP
-    50-256-256-1, screening and training on the tensor cores in BF16 with FP32 accumulation,
-    archive 2^20, Adam lr 1e-3, batch 4096, k = 8 trials per target, C4_TRAIN_STEPS Adam steps per
-    generation, C4_EXPLORE exploration picks; blocks of 10 generations replay a CUDA graph); ring migration
-    of 5 every 50 generations in both, both spend 32768 exact evaluations per generation. Best
-    FP64 error every 10 generations; wall time from CUDA events around the generations only.
-    (a) rotated Rastrigin for `gens` generations; (b) the rotated sphere of the same shape run to
-    an error of 1e-8 (capped), which gives the exact evaluations each method needs to get there."""
-    from speo_gb300 import _lib
-
-    out = {"workload": "128 islands x P=256, D=50; surrogate MLP 50-256-256-1 (BF16 tcgen05 screening and "
-                       "training), k=8", "train_steps_per_gen": C4_TRAIN_STEPS, "explore": C4_EXPLORE}
-    ras = {"objective": "rotated Rastrigin", "generations": gens}
-    curves = {}
-    for mode in ("plain", "surrogate"):
-        ras[mode], curves[mode] = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, mode, gens,
-                                          train_steps=C4_TRAIN_STEPS, explore=C4_EXPLORE)
-    target = ras["plain"]["final_err"]
-    hit = next((c for c in curves["surrogate"] if c["best_err"] <= target), None)
-    ras["surrogate_reaches_plain_final_error"] = None if hit is None else {
-        "at_gen": hit["gen"], "exact_evals_ratio_plain_over_surrogate": curves["plain"][-1]["exact_evals"]
-        / hit["exact_evals"], "wall_ratio_plain_over_surrogate": ras["plain"]["wall_s"] / hit["wall_s"]}
-    out["rastrigin"] = ras
-    sph = {"objective": "rotated sphere", "target_err": 1e-8}
-    sph["plain"], _ = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "plain", 4000, stop_at=1e-8)
-    sph["surrogate"], _ = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8,
-                                  train_steps=C4_TRAIN_STEPS, explore=C4_EXPLORE)
-    light, _ = _c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8, train_steps=16,
-                       explore=C4_EXPLORE)
-    sph["surrogate_16_steps"] = {k: v for k, v in light.items() if k != "curve"}
-    ep, es = sph["plain"]["exact_evals_to_1e-8"], sph["surrogate"]["exact_evals_to_1e-8"]
-    wp, ws = sph["plain"]["wall_s_to_1e-8"], sph["surrogate"]["wall_s_to_1e-8"]
-    sph["exact_evals_ratio_plain_over_surrogate"] = ep / es if ep and es else None
-    sph["wall_ratio_plain_over_surrogate"] = wp / ws if wp and ws else None
-    out["sphere_to_1e-8"] = sph
-    return out
 
 
 def bench_mlp(L, dev, torch, steps: int = 16) -> dict:
@@ -623,8 +796,9 @@ def bench_mlp(L, dev, torch, steps: int = 16) -> dict:
             "train_steps_timed": steps}
 
 
-def bench_e2e(L, dev, torch, args, f64: bool = False) -> dict:
-    """Reference-shaped C ABI with host buffers: initial population + instance uploaded from
+
+def bench_e2e_config1(L, dev, torch, steps: int, f64: bool = False) -> dict:
+    """Config 1 (64 x 100, D = 30) through the reference-shaped C ABI with host buffers: initial population + instance uploaded from
     pinned host memory, then per generation generate / evaluate / select and a read-back of
     the generation's fitness vector; all inside the timed region. f64: the same in the
     reference's shipped precision (`real` = double) through speo_de_run_f64 and the FP64 entry
@@ -632,7 +806,7 @@ def bench_e2e(L, dev, torch, args, f64: bool = False) -> dict:
     from speo_gb300 import _lib
     from speo_gb300.instances import make_instance
 
-    n = N_ISLANDS * POP
+    n = C1_ISLANDS * C1_POP
     ld = 32
     npt = np.float64 if f64 else np.float32
     tdt = torch.float64 if f64 else torch.float32
@@ -645,34 +819,33 @@ def bench_e2e(L, dev, torch, args, f64: bool = False) -> dict:
                                                         "API_evaluateFitness", "API_DE_SelectSurvival"))
     de_run = L.speo_de_run_f64 if f64 else L.speo_de_run_f32
     run_name = "speo_de_run_f64" if f64 else "speo_de_run_f32"
-    o, M = make_instance(run_seed(), DIM)
-    rot = np.zeros((ld, DIM), dtype=npt)
-    rot[:DIM] = M.T
+    o, M = make_instance(c1_seed(), C1_DIM)
+    rot = np.zeros((ld, C1_DIM), dtype=npt)
+    rot[:C1_DIM] = M.T
     sh = np.zeros(ld, dtype=npt)
-    sh[:DIM] = o
+    sh[:C1_DIM] = o
     rng = np.random.default_rng(0)
     h_pop = torch.from_numpy(rng.uniform(-100, 100, (n, ld)).astype(npt)).pin_memory()
-    h_pop[:, DIM:] = 0
+    h_pop[:, C1_DIM:] = 0
     h_rot = torch.from_numpy(rot).pin_memory()
     h_sh = torch.from_numpy(sh).pin_memory()
     h_fit = torch.zeros(n, dtype=tdt).pin_memory()
     pop, cand = torch.empty(n, ld, dtype=tdt, device=dev), torch.zeros(n, ld, dtype=tdt, device=dev)
     pfit, cfit = torch.empty(n, dtype=tdt, device=dev), torch.empty(n, dtype=tdt, device=dev)
-    d_rot, d_sh = torch.empty(ld, DIM, dtype=tdt, device=dev), torch.empty(ld, dtype=tdt, device=dev)
+    d_rot, d_sh = torch.empty(ld, C1_DIM, dtype=tdt, device=dev), torch.empty(ld, dtype=tdt, device=dev)
     rng_state = torch.zeros(16, dtype=torch.int32, device=dev)
     perm = torch.arange(n, dtype=torch.int32, device=dev)
-    best = torch.zeros(N_ISLANDS, dtype=torch.int32, device=dev)
-    info = (DI * N_ISLANDS)(*[DI(0.9, 0.5, 4, POP) for _ in range(N_ISLANDS)])
+    best = torch.zeros(C1_ISLANDS, dtype=torch.int32, device=dev)
+    info = (DI * C1_ISLANDS)(*[DI(0.9, 0.5, 4, C1_POP) for _ in range(C1_ISLANDS)])
     h_info = torch.frombuffer(bytearray(bytes(info)), dtype=torch.uint8).pin_memory()
     d_info = torch.empty_like(h_info, device=dev)
-    ii = _lib.IslandInfo(n, N_ISLANDS, perm.data_ptr())
-    pi = PI(DIM, FUNC, 1, 0, run_seed(), 0, 0, 100.0, -100.0)
+    ii = _lib.IslandInfo(n, C1_ISLANDS, perm.data_ptr())
+    pi = PI(C1_DIM, FUNC, 1, 0, c1_seed(), 0, 0, 100.0, -100.0)
     P = Pop(pop.data_ptr(), pfit.data_ptr())
     C = Pop(cand.data_ptr(), cfit.data_ptr())
     stream = torch.cuda.current_stream()
     L.speo_set_stream(ctypes.c_void_p(stream.cuda_stream))
     _lib.check(init(C, rng_state.data_ptr(), ii, pi), "API_Initilize" + sfx)
-    steps = max(100, min(args.steps, 2000))
     h_hist = torch.zeros(steps * n, dtype=tdt).pin_memory()  # every generation's fitness
 
     def upload():
@@ -681,7 +854,7 @@ def bench_e2e(L, dev, torch, args, f64: bool = False) -> dict:
         d_sh.copy_(h_sh, non_blocking=True)
         d_info.copy_(h_info, non_blocking=True)
         ev(pfit.data_ptr(), None, None, pop.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(), None, None, None, None, n,
-           DIM, 0.0, FUNC)
+           C1_DIM, 0.0, FUNC)
 
     def run_native(nsteps):  # the reference's DE_CUDA::Run loop as one library call (C++ host loop)
         upload()
@@ -694,7 +867,7 @@ def bench_e2e(L, dev, torch, args, f64: bool = False) -> dict:
         for _ in range(nsteps):
             gen(C, P, best.data_ptr(), ii, d_info.data_ptr(), rng_state.data_ptr(), pi)
             ev(cfit.data_ptr(), None, None, cand.data_ptr(), d_sh.data_ptr(), d_rot.data_ptr(), None, None, None, None,
-               n, DIM, 0.0, FUNC)
+               n, C1_DIM, 0.0, FUNC)
             sel(P, C, ii, pi)
             h_fit.copy_(pfit, non_blocking=True)
         stream.synchronize()
@@ -707,7 +880,7 @@ def bench_e2e(L, dev, torch, args, f64: bool = False) -> dict:
         out[name] = n * steps / (time.perf_counter() - t0)
     _lib.check(L.API_CheckCUDAError(), "e2e")
     L.speo_set_stream(None)
-    h2d = (n * ld + ld * DIM + ld) * es + len(bytes(info))
+    h2d = (n * ld + ld * C1_DIM + ld) * es + len(bytes(info))
     return {"value": out["native"], "unit": "evals/s", "h2d_bytes_per_step": h2d / steps,
             "d2h_bytes_per_step": n * es, "steps": steps, "dtype": "fp64" if f64 else "fp32",
             "path": f"{run_name} (64 sub-islands of 100): the generations of API_DE_GenerateNewPopulation{sfx} + "
@@ -716,6 +889,8 @@ def bench_e2e(L, dev, torch, args, f64: bool = False) -> dict:
                     "read back to pinned host memory (one copy per launch)",
             "python_loop_value": out["python"],
             "python_loop_path": "the same entry points called one by one from Python (ctypes), per-call host cost"}
+
+
 
 
 # The reference's published runs (CEC2014 composition functions, D = 100, 4096 individuals per
@@ -740,7 +915,7 @@ def bench_published(L, dev, torch, gens: int = 300, gens64: int = 60, fids=range
     stream = torch.cuda.current_stream()
     L.speo_set_stream(ctypes.c_void_p(stream.cuda_stream))
     for fid in fids:
-        o, M, S = make_instance_multi(run_seed() + fid, D, fid)
+        o, M, S = make_instance_multi(c1_seed() + fid, D, fid)
         nc = o.shape[0]
         rot = np.zeros((nc, ld, D), dtype=np.float32)
         rot[:, :D] = M.transpose(0, 2, 1)
@@ -765,7 +940,7 @@ def bench_published(L, dev, torch, gens: int = 300, gens64: int = 60, fids=range
             info = (DI * 1)(DI(0.9, 0.5, 4, n))
             d_info = torch.frombuffer(bytearray(bytes(info)), dtype=torch.uint8).to(dev)
             ii = _lib.IslandInfo(n, 1, perm.data_ptr())
-            pi = PI(D, fid, 1, 0, run_seed(), 0, 0, 100.0, -100.0)
+            pi = PI(D, fid, 1, 0, c1_seed(), 0, 0, 100.0, -100.0)
             P, C = Pop(pop.data_ptr(), pfit.data_ptr()), Pop(cand.data_ptr(), cfit.data_ptr())
             _lib.check(getattr(L, "API_Initilize" + sfx)(P, rng_state.data_ptr(), ii, pi), "API_Initilize")
             ev = getattr(L, "API_evaluateFitness" + sfx)
@@ -807,131 +982,100 @@ def bench_published(L, dev, torch, gens: int = 300, gens64: int = 60, fids=range
     return out
 
 
-def cpu_workload_sample(sample_s: float, threads: int):
-    """FP64 island loop of the oracle port on the host cores: (evals/s, gens done)."""
-    import speo_oracle
-    from speo_gb300.instances import make_instance
 
-    o, M = make_instance(run_seed(), DIM)
-    ld = 32
-    n = N_ISLANDS * POP
-    pop = speo_oracle.init_population(n, ld, DIM, -100.0, 100.0, run_seed()).astype(np.float64)
-    fit = speo_oracle.evaluate_rows(FUNC, pop.astype(np.float32), DIM, o, M)
-    gens, total_evals, t_used = 0, 0, 0.0
-    chunk = 2
-    while t_used < sample_s:
-        t0 = time.perf_counter()
-        total_evals += speo_oracle.run_islands_f64(N_ISLANDS, POP, DIM, ld, FUNC, 0.5, 0.9, -100.0, 100.0, o, M,
-                                                   run_seed(), gens, chunk, INTERVAL, MIGRANTS, pop, fit, threads)
-        t_used += time.perf_counter() - t0
-        gens += chunk
-        chunk = min(chunk * 2, 200)
-    return total_evals / t_used, gens, t_used
+def sections(args) -> dict:
+    """The secondary measurements (rank 0, one GPU)."""
+    import torch
+    from speo_gb300 import _lib
 
-
-def cpu_baseline(sample_s: float = 12.0) -> dict:
-    threads = os.cpu_count() or 1
-    rate, gens, t = cpu_workload_sample(sample_s, threads)
-    return {"value": rate, "unit": "evals/s", "cores": threads, "kind": "port",
-            "sample": f"{gens} generations of the same 64x100 D=30 island workload in FP64 "
-                      f"(oracle restatement of the reference's DE + CEC2014 objective), {t:.1f} s, "
-                      f"{threads} threads over islands"}
+    dev = "cuda:0"
+    torch.cuda.set_device(0)
+    L = _lib.load()
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
+    out = {"config1_island_d30": bench_config1(L, dev, torch, flush),
+           "operators_bandwidth_scale": bench_operators(L, dev, torch, peaks(), args.ops_islands),
+           "config2_precision": bench_config2(L, dev, torch, flush),
+           "config3_batched": bench_config3(L, dev, torch, flush),
+           "surrogate_mlp": bench_mlp(L, dev, torch),
+           "e2e_config1_fp32": bench_e2e_config1(L, dev, torch, 1000),
+           "e2e_config1_fp64": bench_e2e_config1(L, dev, torch, 1000, f64=True),
+           "published_config": bench_published(L, dev, torch)}
+    return out
 
 
-def bench_reference(args) -> dict:
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+def one_section(args) -> dict | None:
+    """--ops-only / --e2e-only / --published-only / --mlp-case / --c4-only / --configs-only."""
+    import torch
+    from speo_gb300 import _lib
+
+    if not (args.ops_only or args.e2e_only or args.published_only or args.mlp_case or args.c4_only
+            or args.configs_only):
         return None
-    threads = os.cpu_count() or 1
-    rate, gens, t = cpu_workload_sample(min(60.0, max(10.0, 0.002 * args.steps)), threads)
-    return {"metric": METRIC, "value": rate, "unit": "evals/s", "n_gpus": 0, "steps": gens, "warmup": 0,
-            "ms_per_step": t * 1e3 / gens, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": "island model: 64 islands x P=100, D=30, rotated Rastrigin (F9 form), "
-                                   "DE/rand/1/bin F=0.5 CR=0.9, ring best-5 -> worst-5 every 50 generations"},
-            "cpu_baseline": {"value": rate, "unit": "evals/s", "cores": threads, "kind": "port",
-                             "sample": f"{gens} generations, {t:.1f} s (the reference's compiled CPU objective "
-                                       "cannot run on the Arm box; the oracle port restates it)"},
-            "e2e": {"value": rate, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    dev = "cuda:0"
+    torch.cuda.set_device(0)
+    L = _lib.load()
+    if args.ops_only:
+        return bench_operators(L, dev, torch, peaks(), args.ops_islands)
+    if args.e2e_only:
+        return {"e2e": bench_e2e(L, dev, torch, max(args.steps, 100)),
+                "e2e_config1_fp32": bench_e2e_config1(L, dev, torch, 1000),
+                "e2e_config1_fp64": bench_e2e_config1(L, dev, torch, 1000, f64=True)}
+    if args.published_only:
+        a, b = (int(v) for v in args.published_fids.split("-"))
+        return {"published_config": bench_published(L, dev, torch, fids=range(a, b + 1),
+                                                    fp64=not args.published_fp32_only)}
+    if args.mlp_case:
+        return {"surrogate_mlp": bench_mlp(L, dev, torch)}
+    if args.c4_only:
+        return {"surrogate": bench_surrogate(L, dev, torch, args.c4_gens)}
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
+    return {"config1_island_d30": bench_config1(L, dev, torch, flush),
+            "config2_precision": bench_config2(L, dev, torch, flush),
+            "config3_batched": bench_config3(L, dev, torch, flush),
+            "surrogate": bench_surrogate(L, dev, torch, args.c4_gens)}
 
 
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20000)
-    ap.add_argument("--warmup", type=int, default=500)
+    ap.add_argument("--steps", type=int, default=1000, help="timed generations")
+    ap.add_argument("--warmup", type=int, default=50, help="untimed generations before the timed ones")
     ap.add_argument("--impl", default="speo", choices=["speo", "reference"])
-    ap.add_argument("--cpu-sample-s", type=float, default=12.0)
+    ap.add_argument("--cpu-sample-s", type=float, default=10.0)
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI leg (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
-    ap.add_argument("--no-ops", action="store_true", help="skip the bandwidth-scale operator measurements")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain comparison")
+    ap.add_argument("--full", action="store_true", help="also measure the secondary sections into --sections-out")
+    ap.add_argument("--sections-out", default="gpurun_out/bench_sections.json")
     ap.add_argument("--ops-only", action="store_true", help="only the bandwidth-scale operator measurements")
     ap.add_argument("--ops-islands", type=int, default=16384, help="islands of 128 rows in the operator variant")
-    ap.add_argument("--no-configs", action="store_true", help="skip the config 2 / 3 / 4 sections")
-    ap.add_argument("--c4-gens", type=int, default=200, help="generations of each config-4 run")
-    ap.add_argument("--configs-only", action="store_true", help="only the config 2 / 3 / 4 sections")
-    ap.add_argument("--c4-only", action="store_true", help="only the config 4 section")
-    ap.add_argument("--mlp-case", action="store_true", help="only the surrogate network's kernels at config-4 shapes")
-    ap.add_argument("--e2e-only", action="store_true", help="only the end-to-end drop-in measurement")
+    ap.add_argument("--configs-only", action="store_true", help="only the configuration sections")
+    ap.add_argument("--c4-gens", type=int, default=200, help="rotated-Rastrigin generations of the surrogate section")
+    ap.add_argument("--c4-only", action="store_true", help="only the surrogate-vs-plain section")
+    ap.add_argument("--mlp-case", action="store_true", help="only the surrogate network's kernels")
+    ap.add_argument("--e2e-only", action="store_true", help="only the end-to-end drop-in measurements")
     ap.add_argument("--published-only", action="store_true",
                     help="only the reference's published configuration (F23-F30, D=100, 4096 rows)")
     ap.add_argument("--published-fids", default="23-30", help="function ids a-b of the published configuration")
     ap.add_argument("--published-fp32-only", action="store_true", help="skip the FP64 leg of the published configuration")
     args = ap.parse_args()
-    args.warmup = max(args.warmup, 3)
-    if args.e2e_only:
-        import torch
-        from speo_gb300 import _lib
-
-        torch.cuda.set_device(0)
-        L = _lib.load()
-        print(json.dumps({"e2e": bench_e2e(L, "cuda:0", torch, args),
-                          "e2e_fp64": bench_e2e(L, "cuda:0", torch, args, f64=True)}))
-        return
-    if args.published_only:
-        import torch
-        from speo_gb300 import _lib
-
-        torch.cuda.set_device(0)
-        a, b = (int(v) for v in args.published_fids.split("-"))
-        print(json.dumps({"published_config": bench_published(_lib.load(), "cuda:0", torch, fids=range(a, b + 1),
-                                                               fp64=not args.published_fp32_only)}))
-        return
-    if args.mlp_case:
-        import torch
-        from speo_gb300 import _lib
-
-        torch.cuda.set_device(0)
-        print(json.dumps({"surrogate_mlp": bench_mlp(_lib.load(), "cuda:0", torch)}))
-        return
-    if args.c4_only:
-        import torch
-        from speo_gb300 import _lib
-
-        torch.cuda.set_device(0)
-        print(json.dumps({"config4_surrogate_vs_plain": bench_config4(_lib.load(), "cuda:0", torch, args.c4_gens)}))
-        return
-    if args.configs_only:
-        import torch
-        from speo_gb300 import _lib
-
-        torch.cuda.set_device(0)
-        L = _lib.load()
-        flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device="cuda:0")
-        print(json.dumps({"config2_precision": bench_config2(L, "cuda:0", torch, flush),
-                          "config3_batched": bench_config3(L, "cuda:0", torch, flush),
-                          "config4_surrogate_vs_plain": bench_config4(L, "cuda:0", torch, args.c4_gens)}))
-        return
-    if args.ops_only:
-        import torch
-        from speo_gb300 import _lib
-
-        torch.cuda.set_device(0)
-        print(json.dumps(bench_operators(_lib.load(), "cuda:0", torch, peaks(), args.ops_islands)))
-        return
+    if args.steps < 1 or args.warmup < 0:
+        raise SystemExit("--steps must be >= 1 and --warmup >= 0")
+    if args.impl == "speo":
+        single = one_section(args)
+        if single is not None:
+            print(json.dumps(single))
+            return
     out = bench_reference(args) if args.impl == "reference" else bench_speo(args)
-    if out is not None and int(os.environ.get("RANK", "0")) == 0:
-        print(json.dumps(out))
+    if out is None or int(os.environ.get("RANK", "0")) != 0:
+        return
+    if args.full and args.impl == "speo":
+        extra = sections(args)
+        path = Path(args.sections_out)
+        path.parent.mkdir(parents=True, exist_ok=True)
+        path.write_text(json.dumps(extra, indent=1))
+        out["sections_file"] = str(path)
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":

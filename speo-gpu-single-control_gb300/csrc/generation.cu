@@ -511,8 +511,85 @@ extern "C" int speo_init_population(const speo_segment *segs, int n_segs, const 
 // device image. Every GPU that loads the library holds it until the process exits.
 namespace {
 static __device__ __align__(256) float g_migration_staging[SPEO_NOALLOC_STAGING_FLOATS];
+
+// The array's device address belongs to the CUDA context that loaded the module: a device reset
+// makes a new primary context, and a caller may bind a context of its own. So the address is
+// kept per (device, context) and looked up again on every call made outside stream capture;
+// a call during capture (when the lookup may not run) takes the address that the last call
+// outside capture found in the same context.
+struct StagingAddr {
+    int dev;
+    void *ctx;
+    float *addr;
+};
+constexpr int kStagingSlots = 64;
 std::mutex g_staging_mu;
-float *g_staging_addr[64] = {};  // device address of g_migration_staging, per device
+StagingAddr g_staging[kStagingSlots];
+int g_staging_used = 0;
+
+// The current context (CUcontext) through the driver's cuCtxGetCurrent, found by the runtime's
+// entry-point query (the library does not link the driver API); null where it is unavailable.
+void *current_context()
+{
+    using CtxGetCurrent = int (*)(void **);
+    static CtxGetCurrent fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return static_cast<CtxGetCurrent>(nullptr);
+        }
+        return reinterpret_cast<CtxGetCurrent>(p);
+    }();
+    void *ctx = nullptr;
+    if (!fn || fn(&ctx) != 0) return nullptr;
+    return ctx;
+}
+
+StagingAddr *staging_slot(int dev, void *ctx)
+{
+    for (int i = 0; i < g_staging_used; ++i)
+        if (g_staging[i].dev == dev && g_staging[i].ctx == ctx) return &g_staging[i];
+    return nullptr;
+}
+
+// Device address of g_migration_staging for the current device and context.
+int staging_address(cudaStream_t st, float **out)
+{
+    int dev = 0;
+    if (int e = check_cuda(cudaGetDevice(&dev), "speo_ring_migrate_noalloc: cudaGetDevice")) return e;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+        cudaGetLastError();  // e.g. the legacy stream queried while another stream captures: no lookup now
+        cap = cudaStreamCaptureStatusActive;
+    }
+    std::lock_guard<std::mutex> lock(g_staging_mu);
+    if (cap == cudaStreamCaptureStatusNone) {
+        void *addr = nullptr;
+        if (int e = check_cuda(cudaGetSymbolAddress(&addr, g_migration_staging),
+                               "speo_ring_migrate_noalloc: cudaGetSymbolAddress"))
+            return e;
+        void *ctx = current_context();  // the lookup above made the device's context current
+        StagingAddr *slot = staging_slot(dev, ctx);
+        if (!slot) {
+            slot = &g_staging[g_staging_used < kStagingSlots ? g_staging_used++ : kStagingSlots - 1];
+            slot->dev = dev;
+            slot->ctx = ctx;
+        }
+        slot->addr = static_cast<float *>(addr);
+        *out = slot->addr;
+        return SPEO_OK;
+    }
+    const StagingAddr *slot = staging_slot(dev, current_context());
+    if (!slot)
+        return fail(SPEO_ERR_INVALID_ARG,
+                    "speo_ring_migrate_noalloc: called during stream capture before any call outside capture on "
+                    "device %d in this context; make one call outside capture first",
+                    dev);
+    *out = slot->addr;
+    return SPEO_OK;
+}
 }  // namespace
 
 extern "C" int speo_ring_migrate_noalloc(const speo_segment *segs, int n_segs, int k, float *pop, float *fit,
@@ -522,29 +599,15 @@ extern "C" int speo_ring_migrate_noalloc(const speo_segment *segs, int n_segs, i
         return fail(SPEO_ERR_INVALID_ARG, "speo_ring_migrate_noalloc: bad arguments");
     if (k < 1 || k > kMaxMigrants)
         return fail(SPEO_ERR_INVALID_ARG, "speo_ring_migrate_noalloc: k = %d outside [1, %d]", k, kMaxMigrants);
-    const unsigned long long need = (unsigned long long)n_segs * (unsigned long long)k * (unsigned long long)(max_ld + 1);
+    const unsigned long long need = (unsigned long long)n_segs * (unsigned long long)k * ((unsigned long long)max_ld + 1ULL);
     if (need > SPEO_NOALLOC_STAGING_FLOATS)
         return fail(SPEO_ERR_INVALID_ARG,
                     "speo_ring_migrate_noalloc: %d segments x %d migrants x (max_ld %d + 1) = %llu staging floats "
                     "exceed the fixed %d; use speo_ring_migrate with a caller buffer",
                     n_segs, k, max_ld, need, SPEO_NOALLOC_STAGING_FLOATS);
-    int dev = 0;
-    if (int e = check_cuda(cudaGetDevice(&dev), "speo_ring_migrate_noalloc: cudaGetDevice")) return e;
-    if (dev < 0 || dev >= 64) return fail(SPEO_ERR_INVALID_ARG, "speo_ring_migrate_noalloc: device %d", dev);
-    float *staging = nullptr;
-    {
-        // first call on this device (with it current): look up the array's device address once
-        std::lock_guard<std::mutex> lock(g_staging_mu);
-        if (!g_staging_addr[dev]) {
-            void *addr = nullptr;
-            if (int e = check_cuda(cudaGetSymbolAddress(&addr, g_migration_staging),
-                                   "speo_ring_migrate_noalloc: cudaGetSymbolAddress"))
-                return e;
-            g_staging_addr[dev] = static_cast<float *>(addr);
-        }
-        staging = g_staging_addr[dev];
-    }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    float *staging = nullptr;
+    if (int e = staging_address(st, &staging)) return e;
     k_emigrate<<<n_segs, 256, 0, st>>>(segs, k, pop, fit, staging, max_ld);
     if (int e = check_launch("k_emigrate")) return e;
     k_immigrate<<<n_segs, 256, 0, st>>>(segs, n_segs, k, pop, fit, staging, max_ld);

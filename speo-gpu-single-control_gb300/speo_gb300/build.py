@@ -100,13 +100,19 @@ def build_oracle() -> Path:
     return REPO_ROOT / "oracle" / "lib" / "libspeo_oracle.so"
 
 
+# Where this build recipe looks for the reference project's sources (read in place, never
+# copied): SPEO_REFERENCE_DIR, else the reference's mount point in the build container. The
+# resolved directory is recorded in oracle/_ref/REFERENCE_ROOT for the tests that read it.
+REFERENCE_MOUNT = "/root/reference/SPEO-GPU-single-control"
+
+
 def build_reference_objective() -> Path | None:
-    """Compiles the reference's own CEC2014.cc into oracle/_ref when its sources are present."""
-    ref_dir = Path(os.environ.get("SPEO_REFERENCE_LIB_DIR",
-                                  "/root/reference/SPEO-GPU-single-control/CUDA_EA_library"))
-    if not (ref_dir / "CEC2014.cc").exists():
+    """Compiles the reference's own CEC2014.cc, immigrant buffers and kernels into oracle/_ref
+    when its sources are present."""
+    ref_root = Path(os.environ.get("SPEO_REFERENCE_DIR", REFERENCE_MOUNT))
+    if not (ref_root / "CUDA_EA_library" / "CEC2014.cc").exists():
         return None
-    res = subprocess.run(["make", "-s", "-C", str(REPO_ROOT / "oracle"), "ref", f"REF_DIR={ref_dir}"],
+    res = subprocess.run(["make", "-s", "-C", str(REPO_ROOT / "oracle"), "ref", f"REF_ROOT={ref_root}"],
                          capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"reference objective build failed:\n{res.stdout}\n{res.stderr}")

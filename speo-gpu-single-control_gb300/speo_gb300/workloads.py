@@ -3,7 +3,7 @@
   config 1  island model: 64 islands x P=100, D=30, rotated Rastrigin, ring best-5 -> worst-5
             every 50 generations
   config 2  precision: 256 islands x P=128, D=100, per island a seeded choice of rotated sphere /
-            rotated Rastrigin with its own o and M; tensor-core BF16x3 evaluation, FP64 re-check
+            rotated Rastrigin with its own o and M; tensor-core split-BF16 evaluation, FP64 re-check
   config 3  batched uneven runs: 1024 independent runs, D ~ U{10,30,50,100}, P ~ U[50,200],
             each with its own o, M and objective; one launch per generation
   config 4  learned surrogate: 128 islands x P=256, D=50, rotated Rastrigin; MLP 50-256-256-1
@@ -52,12 +52,13 @@ def config3_specs(n_runs: int = 1024):
     return specs, inst
 
 
-def config4_specs(func: int = RASTRIGIN):
+def config4_specs(func: int = RASTRIGIN, rank: int = 0):
     """Config 4's islands; `func` = SPHERE gives the same shape on the rotated sphere, where an
-    error of 1e-8 is reachable and the evaluations needed to get there can be compared."""
+    error of 1e-8 is reachable and the evaluations needed to get there can be compared. `rank`
+    gives an independent replica of the ring (its own Philox seeds, the same instance)."""
     seed = run_seed(1, func, 4)
     inst = [make_instance(seed, 50)]
-    specs = [SegmentSpec(pop_size=256, dim=50, func_id=func, instance=0, seed=seed * 31 + i,
+    specs = [SegmentSpec(pop_size=256, dim=50, func_id=func, instance=0, seed=seed * 31 + i + 1000003 * rank,
                          ring_next=(i + 1) % 128) for i in range(128)]
     return specs, inst
 

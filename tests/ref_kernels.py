@@ -12,6 +12,17 @@ from pathlib import Path
 
 REPO = Path(__file__).resolve().parent.parent
 REF_DIR = REPO / "oracle" / "_ref"
+
+
+def reference_root() -> Path | None:
+    """The reference project directory the oracle build read its sources from (recorded by
+    `make -C oracle ref` in oracle/_ref/REFERENCE_ROOT), or None where it was not built or the
+    sources are absent."""
+    rec = REF_DIR / "REFERENCE_ROOT"
+    if not rec.exists():
+        return None
+    root = Path(rec.read_text().strip())
+    return root if root.is_dir() else None
 CAPTURE = REPO / "oracle" / "lib" / "xorwow_capture.fatbin"
 
 # Itanium-mangled names of the reference's kernels (host stub names of the same build).

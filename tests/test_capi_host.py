@@ -6,6 +6,7 @@ from __future__ import annotations
 import ctypes
 import re
 import subprocess
+import sys
 from pathlib import Path
 
 import numpy as np
@@ -13,7 +14,11 @@ import pytest
 
 REPO = Path(__file__).resolve().parent.parent
 HEADER = REPO / "include" / "speo_gb300.h"
-REF_LIB_DIR = Path("/root/reference/SPEO-GPU-single-control/CUDA_EA_library")
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+from ref_kernels import reference_root  # noqa: E402
+
+_REF_ROOT = reference_root()
+REF_LIB_DIR = (_REF_ROOT / "CUDA_EA_library") if _REF_ROOT else Path("/nonexistent")
 
 
 def declared_functions() -> list[str]:
@@ -106,6 +111,20 @@ def test_dropin_validation_happens_before_any_device_work(lib):
     assert lib.API_Initilize_f32(pop, None, ii, pi) == _lib.SPEO_ERR_INVALID_ARG
     pi.dim = 300
     assert lib.API_Initilize_f32(pop, None, ii, pi) == _lib.SPEO_ERR_INVALID_ARG
+
+
+def test_noalloc_migration_validation_happens_before_any_device_work(lib):
+    """speo_ring_migrate_noalloc rejects k outside [1, 32], no segments and a staging need one
+    float past its fixed array, all before it touches the device (pointers never dereferenced)."""
+    from speo_gb300 import _lib
+
+    lim = _lib.NOALLOC_STAGING_FLOATS
+    for n_segs, k, max_ld, what in ((1, 0, 64, b"outside"), (1, 33, 64, b"outside"), (0, 5, 64, b"bad arguments"),
+                                    (1, 5, 0, b"bad arguments"), (1, 1, lim, b"exceed the fixed"),
+                                    (2, 1, lim // 2, b"exceed the fixed"), (64, 32, 2 ** 31 - 1, b"exceed the fixed")):
+        st = lib.speo_ring_migrate_noalloc(1, n_segs, k, 1, 1, max_ld, None)
+        assert st == _lib.SPEO_ERR_INVALID_ARG, (n_segs, k, max_ld)
+        assert what in lib.speo_last_error(), (n_segs, k, max_ld, lib.speo_last_error())
 
 
 @pytest.mark.parametrize("f64", [False, True])

@@ -4,13 +4,18 @@ properties of the DE restatement that the reference's kernel implies."""
 from __future__ import annotations
 
 import os
+import sys
 from pathlib import Path
 
 import numpy as np
 import pytest
 
 GOLDEN = Path(__file__).resolve().parent / "golden" / "objective_f9.npz"
-REF_DATA = Path("/root/reference/SPEO-GPU-single-control/bin/input_data")
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+from ref_kernels import reference_root  # noqa: E402
+
+_REF_ROOT = reference_root()
+REF_DATA = (_REF_ROOT / "bin" / "input_data") if _REF_ROOT else Path("/nonexistent")
 
 
 # Random123 v1.09 kat_vectors, philox4x32_10

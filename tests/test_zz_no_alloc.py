@@ -60,3 +60,30 @@ def test_noalloc_migration_rejects_oversize(lib, cuda):
                                        too_big_ld, None)
     assert st == _lib.SPEO_ERR_INVALID_ARG
     assert b"exceed the fixed" in lib.speo_last_error()
+
+
+def test_noalloc_migration_at_the_exact_staging_limit(lib, cuda):
+    """One segment migrating into itself with max_ld = 2^20 - 1 needs exactly the fixed array
+    (1 x 1 x 2^20 floats): accepted, and equal to the caller-staged version; one float more is
+    rejected before any device work."""
+    import torch
+    from speo_gb300 import _lib
+
+    a, b = _ring(cuda, n_islands=1), _ring(cuda, n_islands=1)
+    a.init_population()
+    b.init_population()
+    a.generation()
+    b.generation()
+    lim = _lib.NOALLOC_STAGING_FLOATS
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    staging = torch.zeros(lim, device=cuda)
+    _lib.check(lib.speo_ring_migrate(a.d_segs.data_ptr(), 1, 1, a.pop[a.cur].data_ptr(), a.fit[a.cur].data_ptr(),
+                                     staging.data_ptr(), lim - 1, stream), "speo_ring_migrate")
+    _lib.check(lib.speo_ring_migrate_noalloc(b.d_segs.data_ptr(), 1, 1, b.pop[b.cur].data_ptr(),
+                                             b.fit[b.cur].data_ptr(), lim - 1, stream), "speo_ring_migrate_noalloc")
+    torch.cuda.synchronize()
+    assert np.array_equal(a.pop[a.cur].cpu().numpy(), b.pop[b.cur].cpu().numpy())
+    assert np.array_equal(a.fit[a.cur].cpu().numpy(), b.fit[b.cur].cpu().numpy())
+    st = lib.speo_ring_migrate_noalloc(b.d_segs.data_ptr(), 1, 1, b.pop[b.cur].data_ptr(), b.fit[b.cur].data_ptr(),
+                                       lim, stream)
+    assert st == _lib.SPEO_ERR_INVALID_ARG
