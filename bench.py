@@ -157,19 +157,31 @@ def chunks(done: int, n: int, interval: int = INTERVAL):
         yield k, done % interval == 0
 
 
-def headline_table(dev: str, rank: int = 0, func: int = FUNC):
+def headline_table(dev: str, rank: int = 0, func: int = FUNC, extra_rows: int = 0):
     from speo_gb300 import workloads as w
 
     specs, inst = w.config4_specs(func, rank=rank)
-    return w.table(specs, inst, device=dev)
+    return w.table(specs, inst, device=dev, extra_rows=extra_rows)
 
 
-def run_plain(tab, n: int, done: int) -> int:
+def ring_migration(tab, dev: str, rank: int, world: int):
+    """The ring step of the headline: on one GPU the library's ring over the 128 islands; across
+    ranks, one global ring over all ranks' islands (contiguous blocks of 128 per rank, boundary
+    migrants through point-to-point messages into local ghost rows, speo_gb300.ring)."""
+    if world == 1:
+        return lambda: tab.migrate(MIGRANTS)
+    from speo_gb300.ring import DeviceRingOps, RingBlock
+
+    blk, ops = RingBlock(N_ISLANDS, POP, DIM, tab.ld, MIGRANTS, rank, world), DeviceRingOps(dev)
+    return lambda: blk.migrate(ops, tab.pop[tab.cur], tab.fit[tab.cur])
+
+
+def run_plain(epoch, migrate, n: int, done: int) -> int:
     """n plain generations (island-resident launches, ring migration at the migration points)."""
     for k, mig in chunks(done, n):
-        tab.epoch(k)
+        epoch(k)
         if mig:
-            tab.migrate(MIGRANTS)
+            migrate()
     return done + n
 
 
@@ -188,11 +200,14 @@ def bench_speo(args) -> dict:
     from speo_gb300 import _lib
 
     L = _lib.load()
-    tab = headline_table(dev, rank)
-    if not tab.epoch_fits():
+    tab = headline_table(dev, rank, extra_rows=2 * MIGRANTS if world > 1 else 0)
+    use_tc = args.epoch == "tc" or (args.epoch == "auto" and tab.epoch_tc_fits())
+    if not (tab.epoch_tc_fits() if use_tc else tab.epoch_fits()):
         raise RuntimeError("the headline islands do not fit one block's shared memory on this GPU")
+    epoch = tab.epoch_tc if use_tc else tab.epoch
+    migrate = ring_migration(tab, dev, rank, world)
     tab.init_population()
-    done = run_plain(tab, args.warmup, 0)                  # exactly W untimed generations
+    done = run_plain(epoch, migrate, args.warmup, 0)       # exactly W untimed generations
     torch.cuda.synchronize()
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
     plan = list(chunks(done, args.steps))
@@ -205,14 +220,14 @@ def bench_speo(args) -> dict:
         for (k, mig), (a, b, c) in zip(plan, ev):
             flush_l2(flush)                                # L2 flushed before every launch
             a.record()
-            tab.epoch(k)
+            epoch(k)
             b.record()
             if mig:
-                tab.migrate(MIGRANTS)
+                migrate()
             c.record()
         torch.cuda.synchronize()
         # the dominant kernel alone, 50-generation launches back to back (clocks still sampled)
-        kg = capture(torch, lambda: tab.epoch(INTERVAL))
+        kg = capture(torch, lambda: epoch(INTERVAL))
         launch50_ms = time_graph(torch, kg, 20, flush)
     if world > 1:
         torch.distributed.barrier()
@@ -228,11 +243,20 @@ def bench_speo(args) -> dict:
     clocks = clk.summary()
     alg_bytes_gen = EVALS_PER_STEP * (5 * DIM * 4 + 2 * 4)  # 4 row reads + 1 row write + 2 fitness per eval
     achieved = alg_bytes_gen * args.steps / (kern_ms / 1e3) / 1e9
-    pair = 2 * N_ISLANDS <= sms
-    kernel = (f"k_island_epoch2<2> (two-block cluster per island, {2 * N_ISLANDS} blocks)" if pair else
-              f"k_island_epoch<2> (one 512-thread block per island, {N_ISLANDS} blocks; up to 50 generations "
-              "per launch with the island, its trials and M^T in shared memory)")
+    gens_per_launch = args.steps / len(plan)
+    if use_tc:
+        kernel = (f"k_island_epoch_tc<2> (one 512-thread block per island, {N_ISLANDS} blocks; up to 50 generations "
+                  "per launch with the island and its trials in shared memory, the rotation on tcgen05: five "
+                  "split-BF16 products per K step into TMEM accumulators)")
+    elif 2 * N_ISLANDS <= sms:
+        kernel = f"k_island_epoch2<2> (two-block cluster per island, {2 * N_ISLANDS} blocks)"
+    else:
+        kernel = (f"k_island_epoch<2> (one 512-thread block per island, {N_ISLANDS} blocks; up to 50 generations "
+                  "per launch with the island, its trials and M^T in shared memory)")
+    traffic = EPOCH_LAUNCH_TRAFFIC_BYTES["tc" if use_tc else "simt"]
     rot_flop_gen = EVALS_PER_STEP * 2 * DIM * DIM
+    kp = (DIM + 15) // 16 * 16
+    tensor_flop_gen = N_ISLANDS * ((POP + 127) // 128) * 5 * 2 * 128 * kp * kp   # executed split products
     sm_mhz = clocks["sm_max_mhz"] or 2070.0
     fp32_peak = sms * FP32_FMA_PER_SM_CLK * 2 * sm_mhz * 1e6 / 1e12
     fp32_achieved = rot_flop_gen * args.steps / (kern_ms / 1e3) / 1e12
@@ -249,16 +273,22 @@ def bench_speo(args) -> dict:
         "gens_per_s": args.steps / (ms / 1e3),
         "best_error_f64": best_err,
         "roofline": {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / pk["hbm_gbs"], "traffic": EPOCH50_TRAFFIC_BYTES * args.steps / INTERVAL
-                     if EPOCH50_TRAFFIC_BYTES else None,
+                     "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+                     "traffic_src": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on "
+                                    "this workload (the island is read once per launch; its writes stay in L2)",
                      "peak_src": f"{pk['src']} (MEASURED_PEAKS hbm_gbs)",
-                     "alg_bytes_per_step": alg_bytes_gen, "kernel_ms_timed": kern_ms,
-                     "launch_us_50_generations": launch50_ms * 1e3,
+                     "alg_bytes_per_launch": alg_bytes_gen * gens_per_launch, "generations_per_launch": gens_per_launch,
+                     "kernel_ms_timed": kern_ms, "launch_us_50_generations": launch50_ms * 1e3,
                      "note": "achieved = streaming-equivalent bytes (5 D s + 2 s per individual-generation) / kernel "
                              "time; the island stays in shared memory, so DRAM traffic is far below them",
                      "fp32": {"achieved_tflops": fp32_achieved, "peak_tflops": fp32_peak, "frac": fp32_achieved / fp32_peak,
                               "flop_per_eval": 2 * DIM * DIM,
-                              "peak_src": f"nominal: {sms} SMs x {FP32_FMA_PER_SM_CLK} FP32 FMA/clk x 2 x {sm_mhz:.0f} MHz"}},
+                              "peak_src": f"nominal: {sms} SMs x {FP32_FMA_PER_SM_CLK} FP32 FMA/clk x 2 x {sm_mhz:.0f} MHz"},
+                     **({"tensor": {"achieved_tflops": tensor_flop_gen * args.steps / (kern_ms / 1e3) / 1e12,
+                                    "peak_tflops": pk["bf16_tflops"],
+                                    "frac": tensor_flop_gen * args.steps / (kern_ms / 1e3) / 1e12 / pk["bf16_tflops"],
+                                    "flop_per_step": tensor_flop_gen,
+                                    "peak_src": f"{pk['src']} (MEASURED_PEAKS bf16_tflops, burst)"}} if use_tc else {})},
         "gpu_launches": len(plan) + 2 * n_mig,
         "clocks": clocks,
     }
@@ -273,9 +303,10 @@ def bench_speo(args) -> dict:
     return out
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one 50-generation island-resident
-# launch of the headline workload, from an ncu capture of that launch; None until captured.
-EPOCH50_TRAFFIC_BYTES = None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one island-resident launch of the
+# headline workload, from an ncu capture of that launch (45 generations; the island is read once per
+# launch and its writes stay in L2, so the figure does not grow with the generations per launch).
+EPOCH_LAUNCH_TRAFFIC_BYTES = {"simt": 7040512 + 11008, "tc": None}
 C4_TRAIN_STEPS = 48   # Adam steps per generation: 48 x 4096 = 6 passes over a generation's 32768 new rows
 C4_EXPLORE = 0.05     # fraction of targets that take a uniformly drawn trial instead of the screened one
 
@@ -387,6 +418,53 @@ def bench_surrogate(L, dev, torch, ras_gens: int = 200, schedule: dict | None = 
         "note": "1e-8 is not reached by either method on the rotated Rastrigin at D=50 (multimodal); the "
                 "comparison is at the smallest error both reach"}
     return out
+
+
+def bench_surrogate_sweep(L, dev, torch, ks=(2, 4, 8), steps=(1, 4, 16, 48), every=(1, 5, 10),
+                          ras_gens: int = 200) -> dict:
+    """The surrogate's schedule against the plain DE on the headline shape: trials per target k,
+    Adam steps per training generation, and training every G-th generation. For each point, the
+    exact evaluations and wall time to an FP64 error of 1e-8 on the rotated sphere, and the
+    exact evaluations and wall time to the plain run's 200-generation error on the rotated
+    Rastrigin, each as a ratio plain / surrogate (> 1: the surrogate needs less). The Pareto
+    front is over (exact-evaluation ratio, wall ratio)."""
+    from speo_gb300 import _lib
+
+    sp, _ = c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "plain", 4000, stop_at=1e-8)
+    rp, cp = c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, "plain", ras_gens)
+    target = rp["final_err"]
+    hit_p = first_reach(cp, target)
+    points = []
+    for k in ks:
+        for st in steps:
+            for ev in every:
+                sch = dict(train_steps=st, explore=C4_EXPLORE, train_k=k, train_every=ev)
+                ss, _ = c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8, **sch)
+                rs, cs = c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, "surrogate", ras_gens, **sch)
+                pt = {"k": k, "train_steps": st, "train_every": ev, "gens_per_s": rs["gens_per_s"]}
+                if ss["exact_evals_to_target"]:
+                    pt["sphere"] = {"evals_ratio": sp["exact_evals_to_target"] / ss["exact_evals_to_target"],
+                                    "wall_ratio": sp["wall_s_to_target"] / ss["wall_s_to_target"],
+                                    "generations": ss["generations"]}
+                else:
+                    pt["sphere"] = {"reached": False, "final_err": ss["final_err"]}
+                hit = first_reach(cs, target)
+                pt["rastrigin"] = ({"evals_ratio": hit_p["exact_evals"] / hit["exact_evals"],
+                                    "wall_ratio": hit_p["wall_s"] / hit["wall_s"], "at_gen": hit["gen"]}
+                                   if hit else {"reached": False, "final_err": rs["final_err"]})
+                points.append(pt)
+
+    def front(key):
+        pts = [p for p in points if "evals_ratio" in p[key]]
+        return [(p["k"], p["train_steps"], p["train_every"]) for p in pts
+                if not any(q[key]["evals_ratio"] >= p[key]["evals_ratio"] and q[key]["wall_ratio"] >= p[key]["wall_ratio"]
+                           and (q[key]["evals_ratio"], q[key]["wall_ratio"]) != (p[key]["evals_ratio"], p[key]["wall_ratio"])
+                           for q in pts)]
+    return {"plain": {"sphere_generations_to_1e-8": sp["generations"], "sphere_wall_s": sp["wall_s_to_target"],
+                      "rastrigin_final_err": target, "gens_per_s": rp["gens_per_s"]},
+            "points": points, "pareto_sphere": front("sphere"), "pareto_rastrigin": front("rastrigin"),
+            "note": "points as (k, Adam steps per training generation, training every G generations); ratios are "
+                    "plain / surrogate, so the north-star target is evals_ratio >= 5 and wall_ratio >= 3"}
 
 
 def bench_e2e(L, dev, torch, steps: int) -> dict:
@@ -723,24 +801,22 @@ def bench_config2(L, dev, torch, flush) -> dict:
 def bench_config3(L, dev, torch, flush) -> dict:
     """Config 3: 1024 independent runs with D ~ U{10,30,50,100}, P ~ U[50,200], each with its own
     instance and objective; one launch per generation (the mixed-class kernel), 20 generations per
-    CUDA graph. The tile size is tuned by measurement over the candidates."""
+    CUDA graph. The tile height is the library tuner's choice (speo_autotune_tile_rows: each
+    candidate timed on this table, the fastest cached for its shape bucket)."""
     from speo_gb300 import workloads as w
 
     specs, inst = w.config3_specs(1024)
     evals = sum(sp.pop_size for sp in specs)
-    tuned = {}
-    for tile in (32, 48, 64):
-        tab = w.table(specs, inst, device=dev, tile_rows=tile)
-        tab.init_population()
-        g = capture(torch, lambda: [tab.generation() for _ in range(20)])
-        g.replay()
-        tuned[tile] = time_graph(torch, g, 5, flush) / 20
-    best = min(tuned, key=tuned.get)
-    ms = tuned[best]
+    tab = w.table(specs, inst, device=dev, tile_rows="auto")
+    tab.init_population()
+    g = capture(torch, lambda: [tab.generation() for _ in range(20)])
+    g.replay()
+    ms = time_graph(torch, g, 5, flush) / 20
     return {"workload": f"1024 runs, D in {{10,30,50,100}}, P in [50,200] ({evals} rows), mixed objectives",
             "ms_per_generation": ms, "gens_per_s": 1e3 / ms, "evals_per_s": evals / (ms / 1e3),
-            "launches_per_generation": 1, "autotune_tile_rows_ms": {str(k): v for k, v in tuned.items()},
-            "tile_rows": best}
+            "launches_per_generation": 1, "tile_rows": tab.tile_rows,
+            "autotune_ms_per_generation": {str(k): v for k, v in tab.autotune["ms"].items()},
+            "autotune_cached": tab.autotune["cached"]}
 
 
 # DRAM bytes of one 50-generation island-resident launch of this workload (64 x 100, D = 30), from
@@ -1009,7 +1085,7 @@ def one_section(args) -> dict | None:
     from speo_gb300 import _lib
 
     if not (args.ops_only or args.e2e_only or args.published_only or args.mlp_case or args.c4_only
-            or args.configs_only):
+            or args.configs_only or args.surrogate_sweep):
         return None
     dev = "cuda:0"
     torch.cuda.set_device(0)
@@ -1028,6 +1104,8 @@ def one_section(args) -> dict | None:
         return {"surrogate_mlp": bench_mlp(L, dev, torch)}
     if args.c4_only:
         return {"surrogate": bench_surrogate(L, dev, torch, args.c4_gens)}
+    if args.surrogate_sweep:
+        return {"surrogate_sweep": bench_surrogate_sweep(L, dev, torch)}
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
     return {"config1_island_d30": bench_config1(L, dev, torch, flush),
             "config2_precision": bench_config2(L, dev, torch, flush),
@@ -1045,6 +1123,8 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI leg (profiling runs)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the surrogate-vs-plain comparison")
+    ap.add_argument("--epoch", default="auto", choices=["auto", "simt", "tc"],
+                    help="island-resident kernel: tensor-core rotation where supported (auto), or the CUDA-core one")
     ap.add_argument("--full", action="store_true", help="also measure the secondary sections into --sections-out")
     ap.add_argument("--sections-out", default="gpurun_out/bench_sections.json")
     ap.add_argument("--ops-only", action="store_true", help="only the bandwidth-scale operator measurements")
@@ -1053,6 +1133,8 @@ def main() -> None:
     ap.add_argument("--c4-gens", type=int, default=200, help="rotated-Rastrigin generations of the surrogate section")
     ap.add_argument("--c4-only", action="store_true", help="only the surrogate-vs-plain section")
     ap.add_argument("--mlp-case", action="store_true", help="only the surrogate network's kernels")
+    ap.add_argument("--surrogate-sweep", action="store_true",
+                    help="only the surrogate schedule sweep (k, Adam steps, training interval) against plain DE")
     ap.add_argument("--e2e-only", action="store_true", help="only the end-to-end drop-in measurements")
     ap.add_argument("--published-only", action="store_true",
                     help="only the reference's published configuration (F23-F30, D=100, 4096 rows)")

@@ -181,8 +181,10 @@ SPEO_API void API_evaluateFitness_f32(float *d_fitness_value, float *d_shuffled_
  * be null): with history = 0, island_size floats that receive the last generation's fitness;
  * with history != 0, generations x island_size floats that receive every generation's fitness
  * (generation g at h_fitness + g * island_size). Runs on a private stream ordered after
- * `stream`. Synchronous: returns when the generations are done. No counterpart function in the
- * reference (it is the reference's caller loop, as a library call). */
+ * `stream`. Synchronous: returns when the generations are done. d_DE_info is read at the start
+ * of the call (on the three-call path its strategy set decides where the best-row search runs)
+ * and must not change while the call runs. No counterpart function in the reference (it is the
+ * reference's caller loop, as a library call). */
 SPEO_API int speo_de_run_f32(speo_population_f32 d_population, speo_population_f32 d_candidate,
                              speo_rng_state *d_rng, speo_island_info island_info, speo_de_info_f32 *d_DE_info,
                              int *d_best_individual_ID, speo_problem_info_f32 problem_info, const float *d_shift,
@@ -271,8 +273,10 @@ SPEO_API int speo_init_population(const speo_segment *d_segs, int n_segs, const 
 SPEO_API int speo_evaluate(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,
                   int dim_lo, int dim_hi, const float *pop, float *fit, void *stream);
 
-/* Same, with the rotation on the tcgen05 tensor cores: BF16 hi/lo 3-term split product,
- * FP32 accumulation in tensor memory, fused shift/scale/objective/row-reduction epilogue (one
+/* Same, with the rotation on the tcgen05 tensor cores: y = x - o and M each split three ways
+ * into BF16 (hi + mid + lo, ~2^-27 relative residue), the six products of size >= 2^-18 of the
+ * leading one per K step, FP32 accumulation in tensor memory (as exact as an FP32 CUDA-core
+ * rotation: fitness within 1e-5 relative of FP64 for the rotated Rastrigin and sphere), fused shift/scale/objective/row-reduction epilogue (one
  * tile row per thread; the per-coordinate sums 9 and 31 packed two columns per operation, the
  * other rotated ids 1-7, 11-16 through the row accumulator). Ids 8, 10 (no rotation) and 17-30
  * (several matrices) are flagged (SPEO_DEVERR_BAD_SEGMENT) and skipped.
@@ -318,6 +322,42 @@ SPEO_API int speo_generation_epoch_ex(const speo_segment *d_segs, int n_segs, in
                                       const float *pop_in, const float *fit_in, float *pop_out, float *fit_out,
                                       uint32_t *d_gen, int generations, int cluster, void *stream);
 
+/* The island-resident epoch with the rotation on the tcgen05 tensor cores (one block per island,
+ * P <= 256, D <= 64, the rotated Rastrigin 9 and sphere 31; other segments are flagged with
+ * SPEO_DEVERR_BAD_SEGMENT and left unchanged). Each generation builds the same trial rows as
+ * speo_generation (same Philox counters, bit-identical), evaluates them with the split-BF16
+ * product and epilogue of speo_evaluate_tc (bit-identical fitness per row) and selects with
+ * strict `<`; `generations` such generations equal, row for row, speo_generation's trials +
+ * speo_evaluate_tc + speo_select_rows repeated. Replaces DE_CUDA::Run's generation
+ * (CUDA_EA_library/DE_CUDA.cc:200-216) with the rotation of kernel_CEC2014_CUDA.cu:147-181 on
+ * the tensor cores. One block per SM holds all 512 tensor-memory columns of its SM while it
+ * runs. speo_epoch_tc_fits: 1 when islands of max_pop rows and dimension dim_hi are supported. */
+SPEO_API int speo_epoch_tc_fits(int max_pop, int dim_hi);
+SPEO_API int speo_generation_epoch_tc(const speo_segment *d_segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
+                                      const float *pop_in, const float *fit_in, float *pop_out, float *fit_out,
+                                      uint32_t *d_gen, int generations, void *stream);
+
+/* The library's tile-shape tuner for speo_generation (k_generation / k_generation_mixed), in
+ * place of the reference's fixed launch shapes (CUDA_EA_library/kernel_CEC2014_CUDA.cu:56-73,
+ * kernel_DE_CUDA.cu:48-62). h_segs is a HOST copy of a segment table whose shift / rot pointers are
+ * device pointers. Each of the n_cand candidate tile heights (rows per work item, 1 to 1024; at
+ * most 16 candidates) is timed over `reps` generations (after two warm-up ones) on scratch
+ * buffers of the table's shape (the call allocates and frees them; the caller's buffers are not
+ * touched) with its own work plan; *tile_out receives the fastest, ms_out (may be null) the
+ * milliseconds per generation of each candidate. The choice is cached per shape bucket (device,
+ * column classes of the smallest and largest D, log2 of rows, of the largest island and of the
+ * number of segments, candidate list): a later call with a table of the same bucket returns it
+ * without timing (*cached = 1, ms_out as measured, or -1 for a choice that was set). Every
+ * candidate gives the same rows bit for bit: the choice changes the speed alone. Synchronous.
+ * No counterpart function in the reference. */
+SPEO_API int speo_autotune_tile_rows(const speo_segment *h_segs, int n_segs, const int *candidates, int n_cand,
+                                     int reps, int *tile_out, float *ms_out, int *cached, void *stream);
+/* Sets the cached choice of the bucket of h_segs (and candidates) to `tile`, as if it had been
+ * measured: later speo_autotune_tile_rows calls of that bucket return it without timing. Host
+ * only (no device work). */
+SPEO_API int speo_autotune_set_tile_rows(const speo_segment *h_segs, int n_segs, const int *candidates, int n_cand,
+                                         int tile);
+
 /* Ring migration: each segment's k best rows (by fitness, then row) replace the k worst
  * rows (by fitness, then row, from the worst) of segment ring_next. All emigrants are
  * chosen before any row is replaced. `staging` holds n_segs*k*(max ld + 1) floats. */
@@ -331,10 +371,15 @@ SPEO_API int speo_ring_migrate(const speo_segment *d_segs, int n_segs, int k, fl
  * The staging lives in a fixed array of SPEO_NOALLOC_STAGING_FLOATS floats (4 MiB) inside the
  * library, held by every GPU that loads the library until the process exits;
  * n_segs * k * (max_ld + 1) beyond that is rejected with SPEO_ERR_INVALID_ARG. The function
- * allocates nothing: the first call on a device (with that device current) looks up the array's
- * device address once, so make that first call before any stream capture. Every call shares
- * the one array, each call writes every staging slot it reads (nothing needs clearing), and
- * calls that overlap on the GPU (other streams, other threads) race on it. */
+ * allocates nothing. The array's device address belongs to the CUDA context that loaded the
+ * library's module, so every call made outside stream capture looks it up (in the current
+ * device's current context: after a device reset, or with a context the caller bound, the new
+ * address is found), and a call during stream capture takes the address that the last call
+ * outside capture found in the same context: make one call outside capture, on that device and
+ * in that context, before capturing one (otherwise the captured call fails with
+ * SPEO_ERR_INVALID_ARG). Every call shares the one array, each call writes every staging slot
+ * it reads (nothing needs clearing), and calls that overlap on the GPU (other streams, other
+ * threads) race on it. */
 #define SPEO_NOALLOC_STAGING_FLOATS (1 << 20)
 SPEO_API int speo_ring_migrate_noalloc(const speo_segment *d_segs, int n_segs, int k, float *pop,
                                        float *fit, int max_ld, void *stream);
@@ -459,7 +504,7 @@ SPEO_API int speo_surrogate_generation(speo_surrogate *s, const speo_segment *d_
 
 /* One DE generation with the rotation on the tensor cores, over a flat population of n_rows rows
  * (stride ld) planned with tiles of at most SPEO_TILE_TC rows: one trial per target
- * (speo_make_trials, k = 1: the trial draws use tags 1 | 1 << 8 and 2 | 1 << 8), tcgen05 BF16x3
+ * (speo_make_trials, k = 1: the trial draws use tags 1 | 1 << 8 and 2 | 1 << 8), tcgen05 split-BF16
  * evaluation (speo_evaluate_tc) into trial_fit, strict-`<` selection into (pop_out, fit_out)
  * (speo_select_rows); *d_gen advances by one. trial / trial_fit: caller scratch of n_rows rows. */
 SPEO_API int speo_generation_tc(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,

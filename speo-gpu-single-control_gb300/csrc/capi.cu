@@ -16,7 +16,7 @@ int g_sm_count[64] = {0};
 
 // The device error words of every translation unit, gathered (read and cleared) by one kernel
 // into a mapped host word: one launch and one synchronisation per read instead of a copy per unit.
-constexpr int kErrUnits = 9;
+constexpr int kErrUnits = 10;
 struct DevErr {
     bool ready = false;
     unsigned int **d_addrs = nullptr;
@@ -42,7 +42,8 @@ int deverr_state(DevErr **out)
     if (!s.ready) {
         void *addrs[kErrUnits] = {speo_deverr_de_ops(),  speo_deverr_objective(),  speo_deverr_generation(),
                                   speo_deverr_tc(),      speo_deverr_resident(),   speo_deverr_surrogate(),
-                                  speo_deverr_mlp(),     speo_deverr_dropin_step(), speo_deverr_objective_multi()};
+                                  speo_deverr_mlp(),     speo_deverr_dropin_step(), speo_deverr_objective_multi(),
+                                  speo_deverr_resident_tc()};
         for (void *a : addrs)
             if (!a) return fail(SPEO_ERR_CUDA, "speo_device_error_bits: cannot locate the device flags");
         if (int e = check_cuda(cudaMalloc(reinterpret_cast<void **>(&s.d_addrs), sizeof addrs), "deverr: alloc"))

@@ -112,3 +112,4 @@ extern "C" void *speo_deverr_surrogate(void);
 extern "C" void *speo_deverr_mlp(void);
 extern "C" void *speo_deverr_dropin_step(void);
 extern "C" void *speo_deverr_objective_multi(void);
+extern "C" void *speo_deverr_resident_tc(void);

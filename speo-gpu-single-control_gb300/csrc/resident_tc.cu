@@ -1,0 +1,370 @@
+// resident_tc.cu -- island-resident DE epochs with the rotation on the tcgen05 tensor cores.
+//
+// The reference runs each generation as separate launches over HBM-resident buffers, with the
+// rotation of every trial as an FP64 16x16 shared-memory GEMM (CUDA_EA_library/DE_CUDA.cc:200-216,
+// kernel_CEC2014_CUDA.cu:147-181) followed by the objective kernel (:557-587). Here one block
+// keeps an island (P <= 256 rows, D <= 64) in shared memory for up to `interval` generations,
+// as k_island_epoch does, and each generation
+//   (1) draws donors and builds the trial rows on the CUDA cores (the same Philox counters and
+//       arithmetic as speo_generation: the trials are bit-identical);
+//   (2) splits y = x - o of every trial three ways into BF16 and stores it into tensor memory as
+//       the A operand (one thread per row and K half);
+//   (3) one thread issues the six split products per 16-wide K step for each 128-row tile
+//       (tcgen05.mma, M^T's three-way split resident in shared memory as the B operand) into an
+//       FP32 accumulator in tensor memory;
+//   (4) one thread per row reads its z row back (tcgen05.ld) and reduces the objective with the
+//       same packed arithmetic as speo_evaluate_tc, so the fitness of a row is bit-identical to
+//       that kernel's;
+//   (5) greedy selection (strict `<`, kernel_DE_CUDA.cu:312) in place.
+// The rotated Rastrigin (9) and sphere (31) only.
+#include "host.h"
+#include "tc_split.cuh"
+
+SPEO_DEFINE_DEVERR(speo_deverr_resident_tc)
+
+namespace speo {
+namespace {
+
+constexpr int kThreadsE = 512;
+constexpr int kWarpsE = kThreadsE / 32;
+constexpr int kMaxPopE = 2 * tcs::kTileM;  // two 128-row MMA tiles
+constexpr int kMaxDimE = 64;               // K = N = round16(D) <= 64
+constexpr int kTmemAllocE = 512;           // whole SM: one block per SM
+constexpr int kAccColsE = 64;              // accumulator of tile t at columns 64 t
+constexpr int kAcolE = 128;                // A operand of tile t at 128 + 96 t (hi, mid, lo 32 apart)
+constexpr int kApartE = 32;                // columns of one A part (K <= 64: 32 BF16 pairs)
+constexpr long long kWaitBudgetE = 2000000000LL;  // ~1 s at 2 GHz: a longer wait is a failure
+
+__device__ __forceinline__ float4 ld4e(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st4e(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+__device__ __forceinline__ float f4ge(const float4 &v, int q) { return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w; }
+__device__ __forceinline__ void f4se(float4 &v, int q, float x)
+{
+    if (q == 0) v.x = x; else if (q == 1) v.y = x; else if (q == 2) v.z = x; else v.w = x;
+}
+
+__host__ __device__ __forceinline__ int donors_of(int st)
+{
+    switch (st) {
+    case 0: case 2: case 6: return 2;
+    case 3: case 4: case 8: return 3;
+    case 1: case 7: return 4;
+    default: return 5;
+    }
+}
+
+__host__ __device__ inline int up_to(int x, int m) { return (x + m - 1) / m * m; }
+__host__ __device__ inline int draw_gens_e(int Pmax)
+{
+    const int g = kThreadsE / Pmax;
+    return g < 1 ? 1 : g > 8 ? 8 : g;
+}
+
+// Shared memory of one island (W = 32 Q floats per population row; trial rows XW = W + 4 apart so
+// that the conversion's one-row-per-thread reads are free of bank conflicts):
+//   B (three-way split M^T: hi, mid, lo) | pop[Pmax][W] | fit[Pmax (to 4)] | Xs[Pmax][XW] | sR[GB][Pmax][8] |
+//   sF[Pmax (to 4)] | o[W]
+struct EpochTcLayout {
+    size_t b_bytes, off_pop, off_fit, off_xs, off_r, off_f, off_o, total;
+};
+
+__host__ __device__ inline EpochTcLayout epoch_tc_layout(int Q, int Pmax)
+{
+    const int W = 32 * Q, XW = W + 4, Kmax = W;  // K = N <= W
+    EpochTcLayout L;
+    L.b_bytes = (size_t)Kmax * Kmax * 2;
+    L.off_pop = (3 * L.b_bytes + 1023) & ~(size_t)1023;
+    L.off_fit = L.off_pop + (size_t)Pmax * W * 4;
+    L.off_xs = L.off_fit + (size_t)up_to(Pmax, 4) * 4;
+    L.off_r = L.off_xs + (size_t)Pmax * XW * 4;
+    L.off_f = L.off_r + (size_t)draw_gens_e(Pmax) * Pmax * 8 * 4;
+    L.off_o = L.off_f + (size_t)up_to(Pmax, 4) * 4;
+    L.total = L.off_o + (size_t)W * 4;
+    return L;
+}
+
+__device__ __forceinline__ bool tc_objective(int f) { return f == SPEO_FUNC_ROTATED_RASTRIGIN || f == SPEO_FUNC_ROTATED_SPHERE; }
+
+template <int Q>
+__global__ void __launch_bounds__(kThreadsE, 1)
+    k_island_epoch_tc(const speo_segment *__restrict__ segs, int Pmax, const float *pop_in, const float *fit_in,
+                      float *pop_out, float *fit_out, uint32_t *gen_ctr, int generations)
+{
+    constexpr int W = 32 * Q, XW = W + 4, G = Q == 1 ? 8 : 16, RPP = kThreadsE / G;
+    extern __shared__ __align__(1024) uint8_t smem_e[];
+    const EpochTcLayout L = epoch_tc_layout(Q, Pmax);
+    uint8_t *b_hi = smem_e;
+    float *pop = reinterpret_cast<float *>(smem_e + L.off_pop);
+    float *fit = reinterpret_cast<float *>(smem_e + L.off_fit);
+    float *Xs = reinterpret_cast<float *>(smem_e + L.off_xs);
+    int *sR = reinterpret_cast<int *>(smem_e + L.off_r);
+    float *sF = reinterpret_cast<float *>(smem_e + L.off_f);
+    float *so = reinterpret_cast<float *>(smem_e + L.off_o);
+    __shared__ float s_bf[kWarpsE];
+    __shared__ int s_bi[kWarpsE];
+    __shared__ __align__(8) uint64_t bar_mma;
+    __shared__ uint32_t tmem_slot;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int grp = tid / G, gl = tid % G;
+    const speo_segment &s = segs[blockIdx.x];
+    const int D = s.dim, P = s.pop_size, ld = s.ld, nch = (D + 3) >> 2;
+    const uint32_t gen0 = *(volatile uint32_t *)gen_ctr;
+    // every thread of the block reads the same segment: the branch below is block-uniform
+    const bool seg_ok = P >= 2 && P <= Pmax && Pmax <= kMaxPopE && D >= 1 && D <= W && D <= kMaxDimE &&
+                        (ld & 3) == 0 && ld >= D && tc_objective(s.func_id);
+    if (seg_ok) {
+        const long long row0 = s.row0;
+        const uint2 key = seed_key(s.seed);
+        const int st = s.strategy, ndon = donors_of(st);
+        const float F = s.F, CR = s.CR, lb = s.lb, ub = s.ub;
+        const float scale = func_scale(s.func_id);
+        const int Kp = tcs::round16(D), S = Kp / 16, s_half = (S + 1) / 2, ntile = (P + tcs::kTileM - 1) / tcs::kTileM;
+        const int GB = draw_gens_e(Pmax);
+
+        if (warp == 0) {
+            tc::tmem_alloc(&tmem_slot, kTmemAllocE);
+            tc::tmem_relinquish();
+        }
+        if (tid == 32) {
+            tc::mbar_init(&bar_mma, 1);
+            tc::fence_mbar_init();
+        }
+        // ---- load the island; split M^T into the B operand (and o into so) ---------------------
+        for (int i = tid; i < P * nch; i += kThreadsE) {
+            const int r = i / nch, c = i - r * nch;
+            st4e(pop + r * W + 4 * c, *reinterpret_cast<const float4 *>(pop_in + (row0 + r) * ld + 4 * c));
+        }
+        for (int r = tid; r < P; r += kThreadsE) fit[r] = fit_in[row0 + r];
+        for (int k = tid; k < W; k += kThreadsE) so[k] = 0.f;
+        __syncthreads();
+        tcs::build_b(s, Kp, b_hi, L.b_bytes, so, tid, kThreadsE);
+        tc::fence_proxy_async_smem();  // B is read by the tensor cores (async proxy)
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        const uint32_t tmem = tmem_slot;
+
+        bool ok_draw = true, ok_bound = true, aborted = false;
+        int g = 0;
+        for (; g < generations; ++g) {
+            const uint32_t gen = gen0 + (uint32_t)g;
+            __syncthreads();
+            // best row (strategies that use it): argmin of fit, NaN as +inf, ties lowest row
+            int best = -1;
+            if (strategy_uses_best(st)) {
+                float bf = __int_as_float(0x7f800000);
+                int bi = 0x7fffffff;
+                for (int r = tid; r < P; r += kThreadsE) {
+                    const float f = rank_key(fit[r]);
+                    if (f < bf || (f == bf && r < bi)) { bf = f; bi = r; }
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float of = __shfl_xor_sync(0xffffffffu, bf, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (of < bf || (of == bf && oi < bi)) { bf = of; bi = oi; }
+                }
+                if (lane == 0) { s_bf[warp] = bf; s_bi[warp] = bi; }
+                __syncthreads();
+                bf = s_bf[0]; bi = s_bi[0];
+                for (int w = 1; w < kWarpsE; ++w)
+                    if (s_bf[w] < bf || (s_bf[w] == bf && s_bi[w] < bi)) { bf = s_bf[w]; bi = s_bi[w]; }
+                best = bi;
+            }
+            // (1a) donor positions + jrand of generations g .. g + GB - 1, one thread per (gen, row)
+            if (g % GB == 0) {
+                const int nb = generations - g < GB ? generations - g : GB;
+                for (int t = tid; t < nb * P; t += kThreadsE) {
+                    const int gi = t / P, r = t - gi * P;
+                    IdxStream is(key, (uint32_t)(row0 + r), gen + (uint32_t)gi, kTagIdx);
+                    int rr[5];
+                    ok_draw &= draw_donors(is, P, rr);
+                    int *o = sR + (gi * Pmax + r) * 8;
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) o[k] = rr[k];
+                    o[5] = is.index(D);
+                }
+                __syncthreads();
+            }
+            const int *sRg = sR + (g % GB) * Pmax * 8;
+            // (1b) trial rows from the shared-memory population (speo_generation's arithmetic)
+            for (int r = grp; r < P; r += RPP) {
+                const int jrand = sRg[r * 8 + 5];
+                int dr[5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) dr[k] = sRg[r * 8 + k];
+                const float *xi = pop + r * W;
+                const float *xb = pop + (best >= 0 ? best : r) * W;
+                for (int c = gl; c < nch; c += G) {
+                    const int e0 = 4 * c;
+                    const float4 ti = ld4e(xi + e0);
+                    const float4 tb = best >= 0 ? ld4e(xb + e0) : ti;
+                    float4 tr[5];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) tr[k] = k < ndon ? ld4e(pop + dr[k] * W + e0) : ti;
+                    const uint4 w = philox(make_uint4((uint32_t)c, (uint32_t)(row0 + r), gen, kTagCr), key);
+                    float4 x4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int e = e0 + q;
+                        if (e < D) {
+                            const float u = u01(pick(w, (uint32_t)q));
+                            float x;
+                            if (e == jrand || u < CR) {
+                                float xr[5];
+#pragma unroll
+                                for (int k = 0; k < 5; ++k) xr[k] = f4ge(tr[k], q);
+                                x = mutant<float>(st, F, f4ge(ti, q), f4ge(tb, q), xr);
+                            } else {
+                                x = f4ge(ti, q);
+                            }
+                            x = check_bound<float>(x, lb, ub, ok_bound);
+                            f4se(x4, q, x);
+                        }
+                    }
+                    st4e(Xs + r * XW + e0, x4);
+                }
+            }
+            __syncthreads();
+            // (2) A operand: warp w converts rows of tile (w >> 2) & 1, lane quarter w & 3, K half w >> 3
+            {
+                const int q = warp & 3, t = (warp >> 2) & 1, h = warp >> 3;
+                if (t < ntile) {
+                    const int m = t * tcs::kTileM + q * 32 + lane;
+                    const bool live = m < P;
+                    const float *row = Xs + (size_t)(live ? m : 0) * XW;
+                    const int s0 = h == 0 ? 0 : s_half, s1 = h == 0 ? s_half : S;
+                    const uint32_t a = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(kAcolE + 3 * kApartE * t);
+                    for (int k = s0; k < s1; ++k) {
+                        uint32_t hi[8], mid[8], lo[8];
+                        tcs::convert16(row, so, 16 * k, D, live, hi, mid, lo);
+                        tc::tmem_st32x8(a + (uint32_t)(8 * k), hi);
+                        tc::tmem_st32x8(a + (uint32_t)(kApartE + 8 * k), mid);
+                        tc::tmem_st32x8(a + (uint32_t)(2 * kApartE + 8 * k), lo);
+                    }
+                    tc::tmem_wait_st();
+                }
+                tc::fence_before_sync();
+            }
+            __syncthreads();
+            // (3) products of every tile, one thread
+            if (tid == 0) {
+                tc::fence_after_sync();
+                for (int t = 0; t < ntile; ++t)
+                    tcs::issue_split_mma(tmem + (uint32_t)(kAccColsE * t), tmem + (uint32_t)(kAcolE + 3 * kApartE * t),
+                                         kApartE, b_hi, L.b_bytes, Kp, Kp, 0, S);
+                tc::mma_commit(&bar_mma);
+            }
+            // (4) one thread per row reads its z row and reduces the objective
+            bool ok = true;
+            if (warp < 4 * ntile) ok = tc::mbar_wait_sleep(&bar_mma, (uint32_t)(g & 1), kWaitBudgetE);
+            if (__syncthreads_or(!ok)) {
+                aborted = true;
+                break;
+            }
+            if (warp < 4 * ntile) {
+                tc::fence_after_sync();
+                const int t = warp >> 2, m = t * tcs::kTileM + (warp & 3) * 32 + lane;
+                float f = tcs::epilogue_row(tmem + (uint32_t)(kAccColsE * t), warp, D, 0, Kp, s.func_id, scale);
+                f = f + 0.f;  // speo_evaluate_tc adds the (empty) second column half
+                if (m < P) sF[m] = f;
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+            // (5) greedy selection in place: strict `<` (kernel_DE_CUDA.cu:312)
+            for (int r = grp; r < P; r += RPP) {
+                const float tf = sF[r];
+                if (tf < fit[r]) {
+                    for (int c = gl; c < nch; c += G) st4e(pop + r * W + 4 * c, ld4e(Xs + r * XW + 4 * c));
+                    if (gl == 0) fit[r] = tf;
+                }
+            }
+        }
+        if (!ok_draw) atomicOr(&s_deverr, SPEO_DEVERR_REDRAW_LIMIT);
+        if (!ok_bound) atomicOr(&s_deverr, SPEO_DEVERR_BOUND_LIMIT);
+        if (aborted && tid == 0) {
+            // the products of generation g may still be running: let them finish (bounded)
+            // before the tensor memory is released
+            atomicOr(&s_deverr, SPEO_DEVERR_WAIT_TIMEOUT);
+            tc::mbar_wait(&bar_mma, (uint32_t)(g & 1), kWaitBudgetE);
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (warp == 0) tc::tmem_dealloc(tmem, kTmemAllocE);
+        // ---- write the island back (after a timeout: the rows of the last whole generation) -----
+        for (int i = tid; i < P * nch; i += kThreadsE) {
+            const int r = i / nch, c = i - r * nch;
+            *reinterpret_cast<float4 *>(pop_out + (row0 + r) * ld + 4 * c) = ld4e(pop + r * W + 4 * c);
+        }
+        for (int r = tid; r < P; r += kThreadsE) fit_out[row0 + r] = fit[r];
+    } else if (tid == 0) {
+        atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+    }
+    // ---- advance the generation counter by `generations` once every block has read it -------
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        const unsigned done = atomicAdd(gen_ctr + 1, 1u);
+        if (done == gridDim.x - 1) {
+            gen_ctr[1] = 0;
+            gen_ctr[0] = gen0 + (uint32_t)generations;
+            __threadfence();
+        }
+    }
+}
+
+int optin_smem()
+{
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return v;
+}
+
+template <int Q>
+int launch_epoch_tc(const speo_segment *segs, int n_segs, int max_pop, const float *pop_in, const float *fit_in,
+                    float *pop_out, float *fit_out, uint32_t *d_gen, int generations, cudaStream_t st)
+{
+    const EpochTcLayout L = epoch_tc_layout(Q, max_pop);
+    const int limit = optin_smem();
+    // more than half of the SM's shared memory: one block (one tensor-memory allocation) per SM
+    const size_t smem = L.total > (size_t)limit / 2 + 1024 ? L.total : (size_t)limit / 2 + 1024;
+    cudaError_t e = cudaFuncSetAttribute(k_island_epoch_tc<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_island_epoch_tc)");
+    k_island_epoch_tc<Q><<<n_segs, kThreadsE, smem, st>>>(segs, max_pop, pop_in, fit_in, pop_out, fit_out, d_gen,
+                                                          generations);
+    return check_launch("k_island_epoch_tc");
+}
+
+}  // namespace
+}  // namespace speo
+
+using namespace speo;
+
+extern "C" int speo_epoch_tc_fits(int max_pop, int dim_hi)
+{
+    if (max_pop < 2 || max_pop > kMaxPopE || dim_hi < 1 || dim_hi > kMaxDimE) return 0;
+    const int Q = dim_hi <= 32 ? 1 : 2;
+    return epoch_tc_layout(Q, max_pop).total <= (size_t)optin_smem() ? 1 : 0;
+}
+
+extern "C" int speo_generation_epoch_tc(const speo_segment *segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
+                                        const float *pop_in, const float *fit_in, float *pop_out, float *fit_out,
+                                        uint32_t *d_gen, int generations, void *stream)
+{
+    if (!segs || !pop_in || !fit_in || !pop_out || !fit_out || !d_gen || n_segs < 1 || generations < 1)
+        return fail(SPEO_ERR_INVALID_ARG, "speo_generation_epoch_tc: bad arguments");
+    if (dim_lo < 1 || dim_lo > dim_hi) return fail(SPEO_ERR_INVALID_ARG, "speo_generation_epoch_tc: dim range");
+    if (!speo_epoch_tc_fits(max_pop, dim_hi))
+        return fail(SPEO_ERR_UNSUPPORTED,
+                    "speo_generation_epoch_tc: islands of P <= %d, D <= %d (the tensor-core epochs take P <= %d, "
+                    "D <= %d)",
+                    max_pop, dim_hi, kMaxPopE, kMaxDimE);
+    const int Q = dim_hi <= 32 ? 1 : 2;
+    if (dim_lo <= 32 && Q == 2)
+        return fail(SPEO_ERR_UNSUPPORTED, "speo_generation_epoch_tc: segments must share one column class");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return Q == 1 ? launch_epoch_tc<1>(segs, n_segs, max_pop, pop_in, fit_in, pop_out, fit_out, d_gen, generations, st)
+                  : launch_epoch_tc<2>(segs, n_segs, max_pop, pop_in, fit_in, pop_out, fit_out, d_gen, generations, st);
+}

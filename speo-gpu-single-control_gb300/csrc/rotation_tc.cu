@@ -4,12 +4,13 @@
 // 557-587), an FP64 16x16 shared-memory GEMM that writes the rotated population back to HBM,
 // with one pass per 128-row tile:
 //   TMA (cp.async.bulk.tensor.2d) brings the FP32 rows into shared memory (a ring of up to three
-//   stages); converter warps subtract o and split y = y_hi + y_lo into BF16, each thread one row,
-//   and store the A operand straight into tensor memory (tcgen05.st, double-buffered by tile);
-//   M (B operand, [N][K] = M[n][k]) is split the same way once per instance into shared memory;
-//   one thread issues, per 16-wide K step, the three products y_hi*M_hi + y_hi*M_lo + y_lo*M_hi
-//   (A from tensor memory) into an FP32 accumulator in tensor memory (M = 128 rows, N = D rounded
-//   up to 16). The tile is converted and multiplied in two K halves (one converter warp per lane
+//   stages); converter warps subtract o and split y = x - o three ways into BF16 (tc_split.cuh),
+//   each thread one row, and store the A operand straight into tensor memory (tcgen05.st,
+//   a ring of K-half slots); M (B operand, [N][K] = M[n][k]) is split the same way once per
+//   instance into shared memory; one thread issues, per 16-wide K step, the six products of
+//   tc_split.cuh (A from tensor memory) into an FP32 accumulator in tensor memory (M = 128 rows,
+//   N = D rounded up to 16, two accumulators): the fitness is as exact as the CUDA-core FP32
+//   rotation's. The tile is converted and multiplied in two K halves (one converter warp per lane
 //   quarter and half); eight warps read the rows back with tcgen05.ld (two per lane quarter, each
 //   half of the columns), apply the scale and the objective term and reduce each row in registers.
 // Nothing but the fitness is written. D <= 128.
@@ -19,6 +20,7 @@
 
 #include "common.cuh"
 #include "host.h"
+#include "tc_split.cuh"
 #include "tcgen05.cuh"
 
 SPEO_DEFINE_DEVERR(speo_deverr_tc)
@@ -26,20 +28,34 @@ SPEO_DEFINE_DEVERR(speo_deverr_tc)
 namespace speo {
 namespace {
 
-constexpr int kTileM = 128;
-constexpr int kTmemCols = 128;   // one accumulator (N <= 128)
-// Tensor memory: accumulators b = 0, 1 at columns 128 b (MMA of tile i+1 overlaps the epilogue of
-// tile i); A operand of buffer b at 256 + 128 b (hi, <= 64 columns) and 320 + 128 b (lo).
+using tcs::kTileM;
+using tcs::round16;
+using tcs::build_b;
+using tcs::convert16;
+using tcs::issue_split_mma;
+using tcs::epilogue_row;
+constexpr int kTmemCols = 128;   // widest accumulator (N <= 128)
+// Tensor memory (kmax = round16(largest D) columns per accumulator): accumulators b = 0, 1 at
+// columns kmax b (the products of tile i + 1 overlap the epilogue of tile i); then a ring of A
+// slots of kSlotCols columns from 2 kmax, as many as fit (up to 4: 4 at D <= 64, 3 at D <= 112, 2
+// above). K half h of tile i (half-index j = 2 i + h) goes to slot j % slots; a slot holds the
+// hi, mid and lo parts of one K half (<= 4 steps: 32 columns each) kApart = 32 columns apart.
+// With three or more slots a half is converted while the products of the previous half run.
 constexpr int kTmemAlloc = 512;
-constexpr int kAcolBase = 256;
+constexpr int kApart = 32;
+constexpr int kSlotCols = 3 * kApart;
+constexpr int kMaxSlots = 4;
+__host__ __device__ __forceinline__ int a_slots(int kmax)
+{
+    const int n = (kTmemAlloc - 2 * kmax) / kSlotCols;
+    return n > kMaxSlots ? kMaxSlots : n;
+}
 constexpr long long kWaitBudget = 2000000000LL;  // ~1 s at 2 GHz: any wait longer is a failure
 constexpr int kEpiThreads = 256;                 // warps 0-7: epilogue
 constexpr int kCvtThreads = 256;                 // warps 8-15: conversion
 constexpr int kThreadsTc = kEpiThreads + kCvtThreads + 32;  // warp 16: TMA and MMA issue
 constexpr int kIssuerWarp = (kEpiThreads + kCvtThreads) / 32;
 constexpr int kMaxStages = 3;
-
-__host__ __device__ __forceinline__ int round16(int x) { return (x + 15) & ~15; }
 
 // Row stride of a staged tile: ld padded so that 8 consecutive rows start in different banks.
 __host__ __device__ __forceinline__ int stage_ld(int ld) { return (ld & 7) ? ld : ld + 4; }
@@ -51,7 +67,7 @@ struct TcLayout {
     size_t stage_bytes, b_bytes, off_b, off_o, off_bar, off_psum, total;
 };
 
-//   stage[nstage] | B hi, lo | o | barriers | psum[2][kTileM]
+//   stage[nstage] | B hi, mid, lo | o | barriers | psum[2][kTileM]
 __host__ __device__ inline TcLayout tc_layout(int dim_hi, int ld, int nstage)
 {
     TcLayout L;
@@ -61,7 +77,7 @@ __host__ __device__ inline TcLayout tc_layout(int dim_hi, int ld, int nstage)
     L.stage_bytes = (size_t)kTileM * L.box_x * 4;
     L.b_bytes = (size_t)L.kmax * L.kmax * 2;
     L.off_b = ((L.stage_bytes * nstage) + 1023) & ~(size_t)1023;
-    L.off_o = L.off_b + 2 * L.b_bytes;
+    L.off_o = L.off_b + 3 * L.b_bytes;
     L.off_bar = (L.off_o + (size_t)L.kmax * 4 + 15) & ~(size_t)15;
     L.off_psum = L.off_bar + 256;
     L.total = L.off_psum + 2 * kTileM * 4;
@@ -78,139 +94,6 @@ struct EvalTcArgs {
     int nstage;
     float *fit;
 };
-
-// Builds B = split(M) for an instance with `nthr` threads (index t): B[n][k] = M[n][k] =
-// rot[k*ld_rot + n] (zero past D), and the shift o.
-__device__ __forceinline__ void build_b(const speo_segment &s, int Kp, uint8_t *b_hi, uint8_t *b_lo, float *so, int t,
-                                        int nthr)
-{
-    const int D = s.dim;
-    const int pairs = Kp * (Kp / 8);
-    for (int i = t; i < pairs; i += nthr) {
-        const int n = i % Kp, kc = i / Kp;
-        float v[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-            const int k = 8 * kc + e;
-            v[e] = (n < D && k < D) ? s.rot[(size_t)k * s.ld_rot + n] : 0.f;
-        }
-        uint4 h, l;
-        tc::split8(v, h, l);
-        const uint32_t off = tc::kmajor_offset(n, 8 * kc, Kp);
-        *reinterpret_cast<uint4 *>(b_hi + off) = h;
-        *reinterpret_cast<uint4 *>(b_lo + off) = l;
-    }
-    for (int k = t; k < Kp; k += nthr) so[k] = k < D ? s.shift[k] : 0.f;
-}
-
-// One row's K step of the A operand: y = x - o over the 16 columns k0 .. k0+15 of a staged row
-// (zero past D or for a dead row), split into BF16 hi / lo and packed two per 32-bit word (even
-// k in the low half), as tcgen05.mma reads A from tensor memory.
-__device__ __forceinline__ void convert16(const float *row, const float *so, int k0, int D, bool live,
-                                          uint32_t (&hi)[8], uint32_t (&lo)[8])
-{
-    float v[16];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        const float4 x = reinterpret_cast<const float4 *>(row + k0)[q];
-        const float4 o = reinterpret_cast<const float4 *>(so + k0)[q];
-        const int k = k0 + 4 * q;
-        if (live && k + 4 <= D) {
-            v[4 * q + 0] = __fsub_rn(x.x, o.x); v[4 * q + 1] = __fsub_rn(x.y, o.y);
-            v[4 * q + 2] = __fsub_rn(x.z, o.z); v[4 * q + 3] = __fsub_rn(x.w, o.w);
-        } else {
-            v[4 * q + 0] = (live && k + 0 < D) ? __fsub_rn(x.x, o.x) : 0.f;
-            v[4 * q + 1] = (live && k + 1 < D) ? __fsub_rn(x.y, o.y) : 0.f;
-            v[4 * q + 2] = (live && k + 2 < D) ? __fsub_rn(x.z, o.z) : 0.f;
-            v[4 * q + 3] = (live && k + 3 < D) ? __fsub_rn(x.w, o.w) : 0.f;
-        }
-    }
-#pragma unroll
-    for (int p = 0; p < 8; ++p) {
-        const __nv_bfloat162 hh = __floats2bfloat162_rn(v[2 * p], v[2 * p + 1]);
-        const float2 hf = __bfloat1622float2(hh);
-        const __nv_bfloat162 ll = __floats2bfloat162_rn(v[2 * p] - hf.x, v[2 * p + 1] - hf.y);
-        hi[p] = *reinterpret_cast<const uint32_t *>(&hh);
-        lo[p] = *reinterpret_cast<const uint32_t *>(&ll);
-    }
-}
-
-// One thread: the 3-term split product over K steps [s0, s1) into the TMEM accumulator (step 0
-// overwrites it); A hi / lo in tensor memory at a_hi / a_lo (8 columns per step), B in shared
-// memory.
-__device__ __forceinline__ void issue_split_mma(uint32_t acc, uint32_t a_hi, uint32_t a_lo, const uint8_t *b_hi,
-                                                const uint8_t *b_lo, int Kp, int Np, int s0, int s1)
-{
-    const uint32_t idesc = tc::idesc_bf16_f32(kTileM, Np);
-    const uint32_t sbo = (uint32_t)Kp * 16;  // 8-row groups
-    const uint32_t lbo = 128;                // adjacent core matrices along K
-    // a K step moves B by two core matrices (256 B: 16 in the descriptor's address field, which
-    // holds smem address >> 4 and cannot carry for addresses below 256 KB) and A by 8 columns
-    uint64_t dh = tc::smem_desc(tc::smem_u32(b_hi) + (uint32_t)s0 * 256u, lbo, sbo);
-    uint64_t dl = tc::smem_desc(tc::smem_u32(b_lo) + (uint32_t)s0 * 256u, lbo, sbo);
-    uint32_t ah = a_hi + (uint32_t)s0 * 8u, al = a_lo + (uint32_t)s0 * 8u;
-    for (int s = s0; s < s1; ++s) {
-        tc::mma_bf16_ta(acc, al, dh, idesc, s > 0);
-        tc::mma_bf16_ta(acc, ah, dl, idesc, 1);
-        tc::mma_bf16_ta(acc, ah, dh, idesc, 1);
-        dh += 16;
-        dl += 16;
-        ah += 8;
-        al += 8;
-    }
-}
-
-// Two objective terms at once (f32x2); per element the same operations as obj_term: z - rint(z)
-// (rint by adding and subtracting 1.5 * 2^23, exact for |z| < 2^22), the Taylor sine, and
-// z*z + (20 s) s.
-__device__ __forceinline__ uint64_t obj_term2(int func, uint64_t z)
-{
-    using namespace tc;
-    if (func != SPEO_FUNC_ROTATED_RASTRIGIN) return mul2(z, z);
-    const uint64_t C = pk2(12582912.0f, 12582912.0f);
-    const uint64_t r = sub2(z, sub2(add2(z, C), C));
-    const uint64_t r2 = mul2(r, r);
-    uint64_t p = pk2(-7.3704309762e-03f, -7.3704309762e-03f);
-    p = fma2(p, r2, pk2(8.2145884633e-02f, 8.2145884633e-02f));
-    p = fma2(p, r2, pk2(-5.9926450253e-01f, -5.9926450253e-01f));
-    p = fma2(p, r2, pk2(2.5501639843e+00f, 2.5501639843e+00f));
-    p = fma2(p, r2, pk2(-5.1677126884e+00f, -5.1677126884e+00f));
-    p = fma2(p, r2, pk2(3.1415927410e+00f, 3.1415927410e+00f));
-    const uint64_t sn = mul2(r, p);
-    return fma2(z, z, mul2(mul2(pk2(20.0f, 20.0f), sn), sn));
-}
-
-// Warps of one TMEM lane quarter (warp % 4), one lane (= tile row) per thread:
-// sum_j term(scale * z_j) over the columns j in [c0, c1), j < D, two columns per packed op, 32
-// columns per TMEM load (c0 a multiple of 32).
-__device__ __forceinline__ float epilogue_row(uint32_t tmem, int warp, int D, int c0, int c1, int func, float scale)
-{
-    using namespace tc;
-    const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
-    const uint64_t sc = pk2(scale, scale);
-    uint64_t acc = pk2(0.f, 0.f);
-    for (int c = c0; c < c1; c += 32) {
-        uint32_t r[32];
-        tmem_ld32_nowait(lane_base + (uint32_t)c, r);
-        tmem_wait_ld();
-        if (c + 32 <= D) {
-#pragma unroll
-            for (int j = 0; j < 32; j += 2)
-                acc = add2(acc, obj_term2(func, mul2(pk2(__uint_as_float(r[j]), __uint_as_float(r[j + 1])), sc)));
-        } else {
-#pragma unroll
-            for (int j = 0; j < 32; j += 2) {
-                if (c + j < D) {
-                    const float z1 = (c + j + 1 < D) ? __uint_as_float(r[j + 1]) : 0.f;
-                    acc = add2(acc, obj_term2(func, mul2(pk2(__uint_as_float(r[j]), z1), sc)));
-                }
-            }
-        }
-    }
-    float a, b;
-    upk2(acc, a, b);
-    return a + b;
-}
 
 // The other rotated CEC2014 bodies (1-7, 11-16), one TMEM lane (= tile row) per thread: the row
 // accumulator of the CUDA-core paths (row_push / row_finish) over the row's columns in order, each
@@ -274,12 +157,12 @@ __device__ __forceinline__ bool tc_tile_ok(const speo_work_item &it, const speo_
 
 // Warp roles: warps 8..15 convert tile i into the A buffer i % 2 in tensor memory (warp 8 + q + 4h:
 // lane quarter q, K half h); warp 16 issues the TMA loads and (one thread) the MMAs of each half
-// as soon as it is converted; warps 0..7 run the epilogue of tile i-1 from the other accumulator.
+// as soon as it is converted and the accumulator is free; warps 0..7 run the epilogue.
 //   bar_tma[s]      stage s holds the rows of its tile                 (TMA transaction bytes)
-//   bar_afull[b][h] half h of A buffer b is converted (and its stage rows read) (128 arrivals)
-//   bar_afree[b]    the products reading A buffer b are done          (tcgen05.commit)
-//   bar_mma[b]      accumulator b holds a finished product            (tcgen05.commit)
-//   bar_epi[b]      the epilogue is done reading accumulator b        (256 arrivals)
+//   bar_afull[s]    slot s holds its K half (and its stage rows are read)       (128 arrivals)
+//   bar_afree[s]    the products reading slot s are done                        (tcgen05.commit)
+//   bar_mma[b]      accumulator b holds a finished product                      (tcgen05.commit)
+//   bar_epi[b]      the epilogue is done reading accumulator b                  (256 arrivals)
 //   bar_fin         every product this block issued is done           (tcgen05.commit, on abort)
 // Everything a role needs about one tile is loaded ahead of use (register prefetch of the work
 // items and segments of the next tiles).
@@ -312,14 +195,14 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
     float *stage[kMaxStages];
 #pragma unroll
     for (int k = 0; k < kMaxStages; ++k) stage[k] = reinterpret_cast<float *>(smem + (size_t)k * L.stage_bytes);
-    uint8_t *b_hi = smem + L.off_b, *b_lo = b_hi + L.b_bytes;
+    uint8_t *b_hi = smem + L.off_b;
     float *so = reinterpret_cast<float *>(smem + L.off_o);
     float *psum = reinterpret_cast<float *>(smem + L.off_psum);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
     uint64_t *bar_tma = bars, *bar_mma = bars + 3, *bar_epi = bars + 5, *bar_afull = bars + 7, *bar_afree = bars + 11,
-             *bar_fin = bars + 13;
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 14);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 15);
+             *bar_fin = bars + 15;
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 16);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 17);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (warp == 0) {
@@ -331,9 +214,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&bar_mma[b], 1);
             tc::mbar_init(&bar_epi[b], kEpiThreads);
-            tc::mbar_init(&bar_afull[2 * b], 128);
-            tc::mbar_init(&bar_afull[2 * b + 1], 128);
-            tc::mbar_init(&bar_afree[b], 1);
+        }
+        for (int k = 0; k < kMaxSlots; ++k) {
+            tc::mbar_init(&bar_afull[k], 128);
+            tc::mbar_init(&bar_afree[k], 1);
         }
         tc::mbar_init(bar_fin, 1);
         *abort_flag = 0;
@@ -344,8 +228,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
-    auto a_hi_col = [&](int b) { return tmem + (uint32_t)(kAcolBase + 128 * b); };
-    auto a_lo_col = [&](int b) { return tmem + (uint32_t)(kAcolBase + 128 * b + 64); };
+    const int nslot = a_slots(L.kmax);
+    // K half h of tile i: its slot, the slot's column, and how often the slot was used before
+    auto slot_of = [&](int i, int h) { return (2 * i + h) % nslot; };
+    auto use_of = [&](int i, int h) { return (2 * i + h) / nslot; };
+    auto slot_col = [&](int sl) { return tmem + (uint32_t)(2 * L.kmax + kSlotCols * sl); };
 
     const int my_items = a.n_items > (int)blockIdx.x ? (a.n_items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     auto item_of = [&](int i) { return a.items[blockIdx.x + (i < my_items ? i : my_items - 1) * gridDim.x]; };
@@ -376,22 +263,26 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             const TileInfo tq_next = tile_info(a, it_q);
             const speo_work_item it_q_next = item_of(i + ns + 2);
             const int b = i & 1, Kp = round16(cur.D), S = Kp / 16, s_half = (S + 1) / 2;
-            bool ok = tc::mbar_wait_sleep(&bar_afull[2 * b], (uint32_t)((i >> 1) & 1), kWaitBudget);
+            const int sl0 = slot_of(i, 0), sl1 = slot_of(i, 1);
+            bool ok = tc::mbar_wait_sleep(&bar_afull[sl0], (uint32_t)(use_of(i, 0) & 1), kWaitBudget);
             if (i >= 2) ok = ok && tc::mbar_wait_sleep(&bar_epi[b], (uint32_t)(((i - 2) >> 1) & 1), kWaitBudget);
             if (!__all_sync(0xffffffffu, ok && *abort_flag == 0)) { *abort_flag = 1; break; }
             tc::fence_after_sync();
-            const uint32_t acc = tmem + (uint32_t)(b * kTmemCols);
+            const uint32_t acc = tmem + (uint32_t)(b * L.kmax);
             if (leader) {
-                issue_split_mma(acc, a_hi_col(b), a_lo_col(b), b_hi, b_lo, Kp, Kp, 0, s_half);
+                issue_split_mma(acc, slot_col(sl0), kApart, b_hi, L.b_bytes, Kp, Kp, 0, s_half);
+                tc::mma_commit(&bar_afree[sl0]);
                 mma_any = true;
             }
-            ok = tc::mbar_wait_sleep(&bar_afull[2 * b + 1], (uint32_t)((i >> 1) & 1), kWaitBudget);
+            ok = tc::mbar_wait_sleep(&bar_afull[sl1], (uint32_t)(use_of(i, 1) & 1), kWaitBudget);
             if (!__all_sync(0xffffffffu, ok && *abort_flag == 0)) { *abort_flag = 1; break; }
             tc::fence_after_sync();
             if (leader) {
-                issue_split_mma(acc, a_hi_col(b), a_lo_col(b), b_hi, b_lo, Kp, Kp, s_half, S);
+                // the slot holds steps s_half .. S - 1 from its first column
+                issue_split_mma(acc, slot_col(sl1) - (uint32_t)(8 * s_half), kApart, b_hi, L.b_bytes, Kp, Kp, s_half,
+                                S);
                 tc::mma_commit(&bar_mma[b]);
-                tc::mma_commit(&bar_afree[b]);
+                tc::mma_commit(&bar_afree[sl1]);
             }
             // both halves' converters have read stage i % ns: it takes tile i + ns
             issue_tma(i + ns, tq);
@@ -415,7 +306,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
         for (int i = 0; i < my_items; ++i) {
             const speo_work_item it_n3 = item_of(i + 3);
             const TileInfo nn = tile_info(a, it_nn);
-            const int sidx = i % ns, b = i & 1;
+            const int sidx = i % ns;
             const int D = cur.D, Kp = round16(D), S = Kp / 16, s_half = (S + 1) / 2;
             bool to = !tc::mbar_wait_sleep(&bar_tma[sidx], (uint32_t)((i / ns) & 1), kWaitBudget);
             const bool new_b = cur.ok && (cur.rot != c_rot || cur.shift != c_shift || D != c_dim ||
@@ -429,27 +320,30 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             if (new_b) {
                 speo_segment sb;
                 sb.dim = D; sb.rot = cur.rot; sb.shift = cur.shift; sb.ld_rot = cur.ld_rot;
-                build_b(sb, Kp, b_hi, b_lo, so, ct, kCvtThreads);
+                build_b(sb, Kp, b_hi, L.b_bytes, so, ct, kCvtThreads);
                 c_rot = cur.rot; c_shift = cur.shift; c_dim = D; c_ldrot = cur.ld_rot;
                 tc::fence_proxy_async_smem();
                 tc::named_bar_sync(1, kCvtThreads);
             }
             if (!cur.ok && ct == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
-            // A buffer b was last read by the products of tile i - 2
-            bool ok = i < 2 || tc::mbar_wait_sleep(&bar_afree[b], (uint32_t)(((i - 2) >> 1) & 1), kWaitBudget);
+            // the slot of this K half was last read by the products of the half nslot half-steps back
+            const int sl = slot_of(i, ch), u = use_of(i, ch);
+            bool ok = u < 1 || tc::mbar_wait_sleep(&bar_afree[sl], (uint32_t)((u - 1) & 1), kWaitBudget);
             if (__all_sync(0xffffffffu, ok)) {
                 const int s0 = ch == 0 ? 0 : s_half, s1 = ch == 0 ? s_half : S;
                 const float *row = stage[sidx] + (size_t)m * L.box_x;
                 const bool live = cur.ok && m < cur.count;
                 for (int st = s0; st < s1; ++st) {
-                    uint32_t hi[8], lo[8];
-                    convert16(row, so, 16 * st, D, live, hi, lo);
-                    tc::tmem_st32x8(a_hi_col(b) + lane_off + (uint32_t)(8 * st), hi);
-                    tc::tmem_st32x8(a_lo_col(b) + lane_off + (uint32_t)(8 * st), lo);
+                    uint32_t hi[8], mid[8], lo[8];
+                    convert16(row, so, 16 * st, D, live, hi, mid, lo);
+                    const uint32_t col = slot_col(sl) + lane_off + (uint32_t)(8 * (st - s0));
+                    tc::tmem_st32x8(col, hi);
+                    tc::tmem_st32x8(col + (uint32_t)kApart, mid);
+                    tc::tmem_st32x8(col + (uint32_t)(2 * kApart), lo);
                 }
                 tc::tmem_wait_st();
                 tc::fence_before_sync();
-                tc::mbar_arrive(&bar_afull[2 * b + ch]);
+                tc::mbar_arrive(&bar_afull[sl]);
             } else {
                 *abort_flag = 1;  // the next tile's barrier stops the group
             }
@@ -472,7 +366,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             const bool got = tc::mbar_wait_sleep(&bar_mma[i & 1], (uint32_t)((i >> 1) & 1), kWaitBudget);
             if (tc::named_bar_or(2 + q, 64, !got)) { *abort_flag = 1; break; }
             tc::fence_after_sync();
-            const uint32_t acc_t = tmem + (uint32_t)((i & 1) * kTmemCols);
+            const uint32_t acc_t = tmem + (uint32_t)((i & 1) * L.kmax);
             const int Np = round16(cur.D), m = q * 32 + lane;
             float f = 0.f;
             bool writer = ch == 0;

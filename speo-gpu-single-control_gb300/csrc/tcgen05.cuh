@@ -217,6 +217,28 @@ __device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo
     lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
+// BF16 three-way split of 8 floats: v = hi + mid + lo + O(2^-27 |v|) (v - hi and v - hi - mid
+// are exact in binary32). Packs as split8.
+__device__ __forceinline__ void split8x3(const float (&v)[8], uint4 &hi, uint4 &mid, uint4 &lo)
+{
+    uint32_t h[4], m[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const __nv_bfloat162 hh = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+        const float2 hf = __bfloat1622float2(hh);
+        const float r0 = v[2 * i] - hf.x, r1 = v[2 * i + 1] - hf.y;
+        const __nv_bfloat162 mm = __floats2bfloat162_rn(r0, r1);
+        const float2 mf = __bfloat1622float2(mm);
+        const __nv_bfloat162 ll = __floats2bfloat162_rn(r0 - mf.x, r1 - mf.y);
+        h[i] = *reinterpret_cast<const uint32_t *>(&hh);
+        m[i] = *reinterpret_cast<const uint32_t *>(&mm);
+        l[i] = *reinterpret_cast<const uint32_t *>(&ll);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    mid = make_uint4(m[0], m[1], m[2], m[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
 // Warp-collective: 32 TMEM lanes x 32 consecutive 32-bit columns (no wait).
 __device__ __forceinline__ void tmem_ld32_nowait(uint32_t taddr, uint32_t (&r)[32])
 {

@@ -126,6 +126,12 @@ SIGNATURES: dict[str, tuple] = {
                                       c_void_p, c_int, c_void_p]),
     "speo_generation_epoch_ex": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
                                          c_void_p, c_void_p, c_int, c_int, c_void_p]),
+    "speo_epoch_tc_fits": (c_int, [c_int, c_int]),
+    "speo_autotune_tile_rows": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                        c_void_p]),
+    "speo_autotune_set_tile_rows": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int]),
+    "speo_generation_epoch_tc": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                         c_void_p, c_void_p, c_int, c_void_p]),
     "speo_generation_tc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
                                    c_void_p, c_int64, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "speo_ring_migrate": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p, c_int, c_void_p]),

@@ -34,6 +34,24 @@ class SegmentSpec:
     ld: int | None = None
 
 
+AUTOTUNE_CANDIDATES = (32, 48, 64)
+
+
+def tune_tile_rows(host_segs: ctypes.Array, n_segs: int, candidates=AUTOTUNE_CANDIDATES, reps: int = 5):
+    """The library's tuner (speo_autotune_tile_rows) on a host segment table: (tile rows,
+    {"ms": {tile: ms per generation}, "cached": bool})."""
+    L = _lib.load()
+    cand = (ctypes.c_int * len(candidates))(*candidates)
+    tile = ctypes.c_int(0)
+    cached = ctypes.c_int(0)
+    ms = (ctypes.c_float * len(candidates))()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(L.speo_autotune_tile_rows(ctypes.addressof(host_segs), n_segs, ctypes.addressof(cand), len(candidates),
+                                         reps, ctypes.byref(tile), ctypes.addressof(ms), ctypes.byref(cached), stream),
+               "speo_autotune_tile_rows")
+    return tile.value, {"ms": {c: ms[i] for i, c in enumerate(candidates)}, "cached": bool(cached.value)}
+
+
 def _bytes_to_device(buf: ctypes.Array, device) -> torch.Tensor:
     host = torch.frombuffer(bytearray(bytes(buf)), dtype=torch.uint8)
     return host.to(device)
@@ -44,8 +62,9 @@ class SegmentTable:
     specs: list[SegmentSpec]
     # (o, M) float32, or (o, M, S) for ids 17-30: o (nc, D), M (nc, D, D), S (nc, D) 1-based int32
     instances: list[tuple]
-    tile_rows: int = _lib.TILE_SIMT
+    tile_rows: int | str = _lib.TILE_SIMT  # rows per work item, or "auto": the library's tuner picks it
     device: str = "cuda"
+    extra_rows: int = 0           # rows past the segments' rows in the population buffers (ring ghost rows)
     rows: int = field(init=False)
 
     def __post_init__(self):
@@ -95,6 +114,9 @@ class SegmentTable:
         self.max_ld = self.ld
         self.host_segs = segs
         self.d_segs = _bytes_to_device(segs, dev)
+        self.autotune = None
+        if self.tile_rows == "auto":
+            self.tile_rows, self.autotune = tune_tile_rows(segs, len(self.specs))
         n = ctypes.c_int(0)
         _lib.check(L.speo_plan_work(ctypes.addressof(segs), len(self.specs), self.tile_rows, None, 0, ctypes.byref(n)),
                    "speo_plan_work")
@@ -106,8 +128,9 @@ class SegmentTable:
         self.d_items = _bytes_to_device(items, dev)
         self.dim_lo = min(sp.dim for sp in self.specs)
         self.dim_hi = max(sp.dim for sp in self.specs)
-        self.pop = [torch.zeros(self.rows, self.ld, device=dev), torch.zeros(self.rows, self.ld, device=dev)]
-        self.fit = [torch.zeros(self.rows, device=dev), torch.zeros(self.rows, device=dev)]
+        n = self.rows + self.extra_rows
+        self.pop = [torch.zeros(n, self.ld, device=dev), torch.zeros(n, self.ld, device=dev)]
+        self.fit = [torch.zeros(n, device=dev), torch.zeros(n, device=dev)]
         self.gen = torch.zeros(2, dtype=torch.int32, device=dev)
         self.cur = 0
         self.staging = torch.zeros(len(self.specs) * 32 * (self.max_ld + 1), device=dev)
@@ -126,7 +149,7 @@ class SegmentTable:
 
     def evaluate(self, which: int | None = None, use_tc: bool = False, out: torch.Tensor | None = None):
         """Fitness of population buffer `which` (default: current) into `out` (default: its own
-        fitness buffer). use_tc selects the tcgen05 BF16x3 kernel (tiles of 128 rows)."""
+        fitness buffer). use_tc selects the tcgen05 split-BF16 kernel (tiles of 128 rows)."""
         L = _lib.load()
         w = self.cur if which is None else which
         fit = self.fit[w] if out is None else out
@@ -167,9 +190,24 @@ class SegmentTable:
                                               self.gen.data_ptr(), generations, cluster, self._stream()),
                    "speo_generation_epoch_ex")
 
+    def epoch_tc_fits(self) -> bool:
+        L = _lib.load()
+        return bool(L.speo_epoch_tc_fits(max(sp.pop_size for sp in self.specs), self.dim_hi))
+
+    def epoch_tc(self, generations: int):
+        """`generations` generations with every island resident in shared memory and the rotation
+        on the tensor cores (speo_generation_epoch_tc; in place)."""
+        L = _lib.load()
+        w = self.cur
+        _lib.check(L.speo_generation_epoch_tc(self.d_segs.data_ptr(), len(self.specs), self.dim_lo, self.dim_hi,
+                                              max(sp.pop_size for sp in self.specs), self.pop[w].data_ptr(),
+                                              self.fit[w].data_ptr(), self.pop[w].data_ptr(), self.fit[w].data_ptr(),
+                                              self.gen.data_ptr(), generations, self._stream()),
+                   "speo_generation_epoch_tc")
+
     def tc_generation(self, trial: torch.Tensor, trial_fit: torch.Tensor):
         """One generation with the rotation on the tensor cores: one DE trial per target
-        (speo_make_trials, k = 1), tcgen05 BF16x3 evaluation, strict-`<` selection. The table must
+        (speo_make_trials, k = 1), tcgen05 split-BF16 evaluation, strict-`<` selection. The table must
         be planned with tiles of at most 128 rows."""
         L = _lib.load()
         a, b = self.cur, 1 - self.cur

@@ -63,5 +63,5 @@ def config4_specs(func: int = RASTRIGIN, rank: int = 0):
     return specs, inst
 
 
-def table(specs, inst, device="cuda", tile_rows=_lib.TILE_SIMT):
-    return SegmentTable(specs, inst, tile_rows=tile_rows, device=device)
+def table(specs, inst, device="cuda", tile_rows=_lib.TILE_SIMT, extra_rows=0):
+    return SegmentTable(specs, inst, tile_rows=tile_rows, device=device, extra_rows=extra_rows)

@@ -127,6 +127,39 @@ def test_noalloc_migration_validation_happens_before_any_device_work(lib):
         assert what in lib.speo_last_error(), (n_segs, k, max_ld, lib.speo_last_error())
 
 
+def test_autotune_cache_buckets_without_a_device(lib):
+    """The tuner's cache: a choice set for one table is returned, without device work, for any
+    table of the same shape bucket (column classes, log2 of rows, largest island, segments and the
+    candidate list); a table of another bucket is not answered from it."""
+    import ctypes as C
+
+    from speo_gb300 import _lib
+
+    def table(P_list, D):
+        segs = _segments(P_list, D)
+        for sg in segs:
+            sg.ld = (D + 3) // 4 * 4
+        return segs
+
+    cand = (C.c_int * 3)(32, 48, 64)
+    a = table([100] * 64, 30)
+    assert lib.speo_autotune_set_tile_rows(C.addressof(a), 64, C.addressof(cand), 3, 48) == 0
+    tile, cached, ms = C.c_int(0), C.c_int(0), (C.c_float * 3)()
+    b = table([90] * 70, 31)                     # same classes and log2 buckets: answered from the cache
+    assert lib.speo_autotune_tile_rows(C.addressof(b), 70, C.addressof(cand), 3, 5, C.byref(tile), C.addressof(ms),
+                                       C.byref(cached), None) == 0
+    assert tile.value == 48 and cached.value == 1 and list(ms) == [-1.0] * 3
+    for other, n in ((table([100] * 64, 50), 64), (table([300] * 64, 30), 64), (table([100] * 8, 30), 8)):
+        st = lib.speo_autotune_tile_rows(C.addressof(other), n, C.addressof(cand), 3, 5, C.byref(tile), None,
+                                         C.byref(cached), None)
+        assert cached.value == 0 and st != 0      # another bucket: it would have to be timed
+    cand2 = (C.c_int * 2)(32, 64)                # another candidate list is another bucket
+    assert lib.speo_autotune_tile_rows(C.addressof(b), 70, C.addressof(cand2), 2, 5, C.byref(tile), None,
+                                       C.byref(cached), None) != 0
+    bad = (C.c_int * 1)(0)
+    assert lib.speo_autotune_set_tile_rows(C.addressof(a), 64, C.addressof(bad), 1, 8) == _lib.SPEO_ERR_INVALID_ARG
+
+
 @pytest.mark.parametrize("f64", [False, True])
 def test_empty_populations_are_status_codes(lib, f64):
     """Zero-row islands and populations come back as SPEO_ERR_INVALID_ARG from every drop-in
