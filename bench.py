@@ -246,7 +246,7 @@ def bench_speo(args) -> dict:
     gens_per_launch = args.steps / len(plan)
     if use_tc:
         kernel = (f"k_island_epoch_tc<2> (one 512-thread block per island, {N_ISLANDS} blocks; up to 50 generations "
-                  "per launch with the island and its trials in shared memory, the rotation on tcgen05: five "
+                  "per launch with the island and its trials in shared memory, the rotation on tcgen05: six "
                   "split-BF16 products per K step into TMEM accumulators)")
     elif 2 * N_ISLANDS <= sms:
         kernel = f"k_island_epoch2<2> (two-block cluster per island, {2 * N_ISLANDS} blocks)"

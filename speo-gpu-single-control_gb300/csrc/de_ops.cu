@@ -204,57 +204,66 @@ __global__ void __launch_bounds__(256) k_generate(T *cand, const T *pop, int ld,
 }
 
 // global_DE_SelectSurvival (kernel_DE_CUDA.cu:305-327): strict `<`. One warp per group of 32
-// rows: a coalesced compare of the two fitness arrays, a ballot, then the winning rows copied up
-// to kBatch at a time with every load issued before the first store (bytes in flight, not
-// instruction count, bound a sparse row copy). Rows whose trial loses move no data.
+// rows: a coalesced compare of the two fitness arrays (the next group's pair is loaded before the
+// current group's rows move), a ballot, then the winners' (row, chunk) copies dealt round-robin to
+// all 32 lanes, kTasks per lane at a time with every load issued before the first store (bytes in
+// flight, not instruction count, bound a sparse row copy; a chunk per lane per row would leave 7
+// of 32 lanes idle at D = 100). Rows whose trial loses move no data.
 template <typename T>
 __global__ void __launch_bounds__(256) k_select(T *pop, T *pop_fit, const T *cand, const T *cand_fit, int n, int ld,
                                                 int dim)
 {
     using V = typename Vec<T>::type;
-    constexpr int VN = Vec<T>::n, kBatch = 8;
-    const int lane = threadIdx.x & 31;
-    const int nch = (dim + VN - 1) / VN;
-    const bool ragged = (dim % VN) != 0;
+    constexpr int VN = Vec<T>::n, kTasks = 8;
+    __shared__ int s_rows[8][32];  // the winners of each warp's current group, in lane order
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int nch = (dim + VN - 1) / VN, full_ch = dim / VN;
     const long long groups = ((long long)n + 31) / 32;
     const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
-    for (long long g = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); g < groups; g += nwarps) {
+    long long g = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+    T fc = T(0), fp = T(0);
+    if (g < groups && g * 32 + lane < n) {
+        fc = cand_fit[g * 32 + lane];
+        fp = pop_fit[g * 32 + lane];
+    }
+    for (; g < groups; g += nwarps) {
         const long long row = g * 32 + lane;
-        bool win = false;
-        if (row < n) {
-            const T fc = cand_fit[row];
-            win = fc < pop_fit[row];
-            if (win) pop_fit[row] = fc;
+        const bool win = row < n && fc < fp;
+        if (win) pop_fit[row] = fc;
+        const long long gn = g + nwarps, rn = gn * 32 + lane;
+        if (gn < groups && rn < n) {
+            fc = cand_fit[rn];
+            fp = pop_fit[rn];
         }
-        unsigned m = __ballot_sync(0xffffffffu, win);
-        while (m) {
-            int rr[kBatch];
-            int cnt = 0;
+        const unsigned m = __ballot_sync(0xffffffffu, win);
+        if (win) s_rows[wib][__popc(m & ((1u << lane) - 1u))] = (int)row;
+        __syncwarp();
+        const int tasks = __popc(m) * nch;
+        for (int t0 = 0; t0 < tasks; t0 += 32 * kTasks) {
+            V v[kTasks];
 #pragma unroll
-            for (int q = 0; q < kBatch; ++q) {
-                rr[q] = 0;
-                if (m) {
-                    rr[q] = (int)(g * 32) + (__ffs(m) - 1);
-                    m &= m - 1;
-                    ++cnt;
+            for (int k = 0; k < kTasks; ++k) {
+                const int t = t0 + 32 * k + lane;
+                if (t < tasks) {
+                    const int q = t / nch, c = t - q * nch;
+                    if (c < full_ch) v[k] = *reinterpret_cast<const V *>(cand + (size_t)s_rows[wib][q] * ld + VN * c);
                 }
             }
-            for (int c0 = 0; c0 < nch; c0 += 32) {
-                const int c = c0 + lane;
-                const bool full = c < nch && (!ragged || c < nch - 1);
-                V v[kBatch];
 #pragma unroll
-                for (int q = 0; q < kBatch; ++q)
-                    if (q < cnt && full) v[q] = *reinterpret_cast<const V *>(cand + (size_t)rr[q] * ld + VN * c);
-#pragma unroll
-                for (int q = 0; q < kBatch; ++q)
-                    if (q < cnt && full) *reinterpret_cast<V *>(pop + (size_t)rr[q] * ld + VN * c) = v[q];
-                if (c < nch && !full) {  // ragged last chunk: elements past D are never written
-                    for (int q = 0; q < cnt; ++q)
-                        for (int e = VN * c; e < dim; ++e) pop[(size_t)rr[q] * ld + e] = cand[(size_t)rr[q] * ld + e];
+            for (int k = 0; k < kTasks; ++k) {
+                const int t = t0 + 32 * k + lane;
+                if (t < tasks) {
+                    const int q = t / nch, c = t - q * nch;
+                    const size_t base = (size_t)s_rows[wib][q] * ld;
+                    if (c < full_ch) {
+                        *reinterpret_cast<V *>(pop + base + VN * c) = v[k];
+                    } else {  // ragged last chunk: elements past D are never written
+                        for (int e = VN * c; e < dim; ++e) pop[base + e] = cand[base + e];
+                    }
                 }
             }
         }
+        __syncwarp();
     }
 }
 

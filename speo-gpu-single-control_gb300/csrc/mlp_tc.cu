@@ -6,10 +6,11 @@
 //     out exactly as the K-major no-swizzle shared-memory operands, so one bulk copy per image
 //     brings them into shared memory, where they stay for every tile the block processes;
 //   * per 128-row tile: the block standardises and converts the rows into the A operand, one
-//     thread issues layer 1 (M = 128, N = H, K = 64) into tensor memory, all 8 warps read the
-//     accumulators back (bias, ReLU, BF16) into the layer-2 A operand, layer 2 (K = H) reuses
-//     the same tensor-memory columns, and the epilogue folds bias, ReLU and the H -> 1 head into
-//     a per-row dot product.
+//     thread issues layer 1 (M = 128, N = H, K = 64) into tensor memory, all 16 warps read the
+//     accumulators back (bias, ReLU, BF16; four warps per TMEM lane quarter, each a quarter of
+//     the columns) into the layer-2 A operand, layer 2 (K = H) reuses the same tensor-memory
+//     columns, and the epilogue folds bias, ReLU and the H -> 1 head into per-row dot products
+//     of each column quarter, added in a fixed order.
 // H is 64, 128 or 256 (tensor-memory columns = H). Every wait is bounded; a timeout sets the
 // device error word and the block returns after releasing its tensor memory.
 #include <cuda_bf16.h>
@@ -26,13 +27,15 @@ namespace {
 constexpr int kRows = 128;                       // rows per tile (MMA M)
 constexpr int kK1 = 64;                          // layer-1 K (din padded)
 constexpr long long kWaitBudget = 2000000000LL;  // ~1 s at 2 GHz
+constexpr int kFwdThreads = 512;                 // screening forward: 16 warps
+constexpr int kFwdParts = 4;                     // column parts of a row in its epilogues (H >= 128)
 
 __host__ __device__ constexpr size_t w1_bytes(int H) { return (size_t)H * kK1 * 2; }
 __host__ __device__ constexpr size_t w2_bytes(int H) { return (size_t)H * H * 2; }
 __host__ __device__ constexpr size_t a_bytes(int H) { return (size_t)kRows * (H > kK1 ? H : kK1) * 2; }
 __host__ __device__ constexpr size_t smem_total(int H)
 {
-    return w1_bytes(H) + w2_bytes(H) + a_bytes(H) + 2 * kRows * sizeof(float) + 64;
+    return w1_bytes(H) + w2_bytes(H) + a_bytes(H) + kFwdParts * kRows * sizeof(float) + 64;
 }
 
 __device__ __forceinline__ uint32_t bf2(float a, float b)
@@ -93,12 +96,12 @@ struct MlpArgs {
 };
 
 template <int H>
-__global__ void __launch_bounds__(256, 1) k_mlp_fwd_tc(MlpArgs a)
+__global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd_tc(MlpArgs a)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sw1 = smem, *sw2 = smem + w1_bytes(H), *sa = sw2 + w2_bytes(H);
     float *red = reinterpret_cast<float *>(sa + a_bytes(H));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(red + 2 * kRows);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(red + kFwdParts * kRows);
     uint64_t *bar_w = bars, *bar_mma = bars + 1;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -127,7 +130,9 @@ __global__ void __launch_bounds__(256, 1) k_mlp_fwd_tc(MlpArgs a)
 
     constexpr uint32_t idesc = tc::idesc_bf16_f32(kRows, H);
     const uint32_t sa_u = tc::smem_u32(sa), sw1_u = tc::smem_u32(sw1), sw2_u = tc::smem_u32(sw2);
-    const int q = warp & 3, half = warp >> 2;       // TMEM lane quadrant, column half
+    // TMEM lane quadrant and column part (H / kParts columns; H = 64 uses two parts of 32)
+    constexpr int kParts = H >= 128 ? kFwdParts : 2, kPartCols = H / kParts;
+    const int q = warp & 3, part = warp >> 2;
     const int row_l = 32 * q + lane;                // tile row this thread reads back
     const uint32_t t_row = tmem + ((uint32_t)(32 * q) << 16);
     const long long ntiles = (a.n + kRows - 1) / kRows;
@@ -136,14 +141,14 @@ __global__ void __launch_bounds__(256, 1) k_mlp_fwd_tc(MlpArgs a)
 
     // This thread's share of a tile's inputs: rows r = tid % 128 (lanes = consecutive rows, so
     // each 8-lane phase of the shared-memory stores covers 128 contiguous bytes), 16-byte chunks
-    // k0 = 8 ((tid + 256 j) / 128). The next tile's rows are loaded into registers before the
+    // k0 = 8 ((tid + 512 j) / 128). The next tile's rows are loaded into registers before the
     // current tile's products start, so their latency overlaps the tensor-core work.
-    constexpr int kItems = kRows * (kK1 / 8) / 256;
+    constexpr int kItems = kRows * (kK1 / 8) / kFwdThreads;
     float xin[kItems][8];
     auto load_rows = [&](long long r0) {
 #pragma unroll
         for (int j = 0; j < kItems; ++j) {
-            const int item = tid + 256 * j;
+            const int item = tid + kFwdThreads * j;
             const int r = item % kRows, k0 = (item / kRows) * 8;
             const long long gr = r0 + r;
 #pragma unroll
@@ -169,7 +174,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_fwd_tc(MlpArgs a)
         // ---- A1 = bf16((x - mu) * isig), zero past din and past n ----------------------------
 #pragma unroll
         for (int j = 0; j < kItems; ++j) {
-            const int item = tid + 256 * j;
+            const int item = tid + kFwdThreads * j;
             const int r = item % kRows, k0 = (item / kRows) * 8;
             float v[8];
 #pragma unroll
@@ -197,7 +202,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_fwd_tc(MlpArgs a)
         tc::fence_after_sync();
         // ---- H1 = bf16(relu(acc + b1)) into the layer-2 A operand ------------------------------
 #pragma unroll 1
-        for (int c0 = half * (H / 2); c0 < (half + 1) * (H / 2); c0 += 32) {
+        for (int c0 = part * kPartCols; part < kParts && c0 < (part + 1) * kPartCols; c0 += 32) {
             uint32_t r[32];
             tc::tmem_ld32_nowait(t_row + (uint32_t)c0, r);
             tc::tmem_wait_ld();
@@ -228,7 +233,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_fwd_tc(MlpArgs a)
         // ---- y = b3 + sum_c relu(acc + b2) w3 ----------------------------------------------------
         float s = 0.f;
 #pragma unroll 1
-        for (int c0 = half * (H / 2); c0 < (half + 1) * (H / 2); c0 += 32) {
+        for (int c0 = part * kPartCols; part < kParts && c0 < (part + 1) * kPartCols; c0 += 32) {
             uint32_t r[32];
             tc::tmem_ld32_nowait(t_row + (uint32_t)c0, r);
             tc::tmem_wait_ld();
@@ -236,10 +241,15 @@ __global__ void __launch_bounds__(256, 1) k_mlp_fwd_tc(MlpArgs a)
             for (int e = 0; e < 32; ++e)
                 s = __fmaf_rn(fmaxf(__fadd_rn(__uint_as_float(r[e]), a.b2[c0 + e]), 0.f), a.w3[c0 + e], s);
         }
-        red[half * kRows + row_l] = s;
+        if (part < kParts) red[part * kRows + row_l] = s;
         tc::fence_before_sync();
         __syncthreads();
-        if (tid < kRows && r0 + tid < a.n) a.y[r0 + tid] = __fadd_rn(__fadd_rn(red[tid], red[kRows + tid]), a.b3[0]);
+        if (tid < kRows && r0 + tid < a.n) {
+            float y = red[tid];
+#pragma unroll
+            for (int p = 1; p < kParts; ++p) y = __fadd_rn(y, red[p * kRows + tid]);
+            a.y[r0 + tid] = __fadd_rn(y, a.b3[0]);
+        }
     }
     if (abort && tid == 0) {
         // let the copy and the products this block started finish (bounded) before its shared and
@@ -271,7 +281,7 @@ int launch_fwd(const MlpArgs &a, cudaStream_t st)
     const long long ntiles = (a.n + kRows - 1) / kRows;
     const long long cap = (long long)sm_count() * per_sm;
     const int grid = (int)(ntiles < cap ? ntiles : cap);
-    k_mlp_fwd_tc<H><<<grid, 256, smem, st>>>(a);
+    k_mlp_fwd_tc<H><<<grid, kFwdThreads, smem, st>>>(a);
     return check_launch("k_mlp_fwd_tc");
 }
 

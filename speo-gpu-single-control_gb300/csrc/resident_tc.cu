@@ -12,11 +12,12 @@
 //   (3) one thread issues the six split products per 16-wide K step for each 128-row tile
 //       (tcgen05.mma, M^T's three-way split resident in shared memory as the B operand) into an
 //       FP32 accumulator in tensor memory;
-//   (4) one thread per row reads its z row back (tcgen05.ld) and reduces the objective with the
-//       same packed arithmetic as speo_evaluate_tc, so the fitness of a row is bit-identical to
-//       that kernel's;
+//   (4) two threads per row read its z row back (tcgen05.ld, the column split of tcs::epi_split)
+//       and reduce the objective with the same packed arithmetic as speo_evaluate_tc, so the
+//       fitness of a row is bit-identical to that kernel's;
 //   (5) greedy selection (strict `<`, kernel_DE_CUDA.cu:312) in place.
 // The rotated Rastrigin (9) and sphere (31) only.
+#include "dropin.cuh"
 #include "host.h"
 #include "tc_split.cuh"
 
@@ -43,16 +44,6 @@ __device__ __forceinline__ void f4se(float4 &v, int q, float x)
     if (q == 0) v.x = x; else if (q == 1) v.y = x; else if (q == 2) v.z = x; else v.w = x;
 }
 
-__host__ __device__ __forceinline__ int donors_of(int st)
-{
-    switch (st) {
-    case 0: case 2: case 6: return 2;
-    case 3: case 4: case 8: return 3;
-    case 1: case 7: return 4;
-    default: return 5;
-    }
-}
-
 __host__ __device__ inline int up_to(int x, int m) { return (x + m - 1) / m * m; }
 __host__ __device__ inline int draw_gens_e(int Pmax)
 {
@@ -63,7 +54,7 @@ __host__ __device__ inline int draw_gens_e(int Pmax)
 // Shared memory of one island (W = 32 Q floats per population row; trial rows XW = W + 4 apart so
 // that the conversion's one-row-per-thread reads are free of bank conflicts):
 //   B (three-way split M^T: hi, mid, lo) | pop[Pmax][W] | fit[Pmax (to 4)] | Xs[Pmax][XW] | sR[GB][Pmax][8] |
-//   sF[Pmax (to 4)] | o[W]
+//   sF[2][Pmax (to 4)] (the two column parts of each trial's fitness) | o[W]
 struct EpochTcLayout {
     size_t b_bytes, off_pop, off_fit, off_xs, off_r, off_f, off_o, total;
 };
@@ -78,12 +69,63 @@ __host__ __device__ inline EpochTcLayout epoch_tc_layout(int Q, int Pmax)
     L.off_xs = L.off_fit + (size_t)up_to(Pmax, 4) * 4;
     L.off_r = L.off_xs + (size_t)Pmax * XW * 4;
     L.off_f = L.off_r + (size_t)draw_gens_e(Pmax) * Pmax * 8 * 4;
-    L.off_o = L.off_f + (size_t)up_to(Pmax, 4) * 4;
+    L.off_o = L.off_f + 2 * (size_t)up_to(Pmax, 4) * 4;
     L.total = L.off_o + (size_t)W * 4;
     return L;
 }
 
 __device__ __forceinline__ bool tc_objective(int f) { return f == SPEO_FUNC_ROTATED_RASTRIGIN || f == SPEO_FUNC_ROTATED_SPHERE; }
+
+// The trial rows of one generation from the shared-memory population, with speo_generation's
+// arithmetic: the island's (row, 4-element chunk) tasks dealt to all threads of the block (a
+// thread's next task is found by stepping, not dividing). ST >= 0 compiles one DE strategy, so the
+// mutant carries no dispatch and loads only its donors; ST < 0 reads the strategy at run time.
+// The crossover test u01(w) < CR is the exact integer compare cr_take(w, ceil(CR 2^24)).
+template <int ST, int W, int XW>
+__device__ __forceinline__ void trial_rows(const float *pop, float *Xs, const int *sRg, int P, int D, int nch,
+                                           int best, int st_rt, float F, uint32_t thr, float lb, float ub, uint2 key,
+                                           long long row0, uint32_t gen, bool &ok_bound)
+{
+    const int st = ST >= 0 ? ST : st_rt;
+    const int ndon = ndonors(st);
+    const int tasks = P * nch, dr = kThreadsE / nch, dc = kThreadsE - dr * nch;
+    int r = (int)threadIdx.x / nch, c = (int)threadIdx.x - r * nch;
+    for (int t = (int)threadIdx.x; t < tasks; t += kThreadsE) {
+        const int *sr = sRg + r * 8;
+        const int jrand = sr[5], e0 = 4 * c;
+        const float4 ti = ld4e(pop + r * W + e0);
+        const float4 tb = best >= 0 ? ld4e(pop + best * W + e0) : ti;
+        float4 tr[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) tr[k] = k < ndon ? ld4e(pop + sr[k] * W + e0) : ti;
+        const uint4 w = philox(make_uint4((uint32_t)c, (uint32_t)(row0 + r), gen, kTagCr), key);
+        float4 x4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = e0 + q;
+            if (e < D) {
+                float x;
+                if (e == jrand || cr_take(pick(w, (uint32_t)q), thr)) {
+                    float xr[5];
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) xr[k] = f4ge(tr[k], q);
+                    x = mutant<float>(st, F, f4ge(ti, q), f4ge(tb, q), xr);
+                } else {
+                    x = f4ge(ti, q);
+                }
+                x = check_bound<float>(x, lb, ub, ok_bound);
+                f4se(x4, q, x);
+            }
+        }
+        st4e(Xs + r * XW + e0, x4);
+        c += dc;
+        r += dr;
+        if (c >= nch) {
+            c -= nch;
+            ++r;
+        }
+    }
+}
 
 template <int Q>
 __global__ void __launch_bounds__(kThreadsE, 1)
@@ -116,11 +158,12 @@ __global__ void __launch_bounds__(kThreadsE, 1)
     if (seg_ok) {
         const long long row0 = s.row0;
         const uint2 key = seed_key(s.seed);
-        const int st = s.strategy, ndon = donors_of(st);
-        const float F = s.F, CR = s.CR, lb = s.lb, ub = s.ub;
+        const int st = s.strategy;
+        const float F = s.F, lb = s.lb, ub = s.ub;
+        const uint32_t thr = cr_threshold<float>(s.CR);
         const float scale = func_scale(s.func_id);
         const int Kp = tcs::round16(D), S = Kp / 16, s_half = (S + 1) / 2, ntile = (P + tcs::kTileM - 1) / tcs::kTileM;
-        const int GB = draw_gens_e(Pmax);
+        const int GB = draw_gens_e(Pmax), Pf = up_to(Pmax, 4);
 
         if (warp == 0) {
             tc::tmem_alloc(&tmem_slot, kTmemAllocE);
@@ -187,44 +230,12 @@ __global__ void __launch_bounds__(kThreadsE, 1)
                 __syncthreads();
             }
             const int *sRg = sR + (g % GB) * Pmax * 8;
-            // (1b) trial rows from the shared-memory population (speo_generation's arithmetic)
-            for (int r = grp; r < P; r += RPP) {
-                const int jrand = sRg[r * 8 + 5];
-                int dr[5];
-#pragma unroll
-                for (int k = 0; k < 5; ++k) dr[k] = sRg[r * 8 + k];
-                const float *xi = pop + r * W;
-                const float *xb = pop + (best >= 0 ? best : r) * W;
-                for (int c = gl; c < nch; c += G) {
-                    const int e0 = 4 * c;
-                    const float4 ti = ld4e(xi + e0);
-                    const float4 tb = best >= 0 ? ld4e(xb + e0) : ti;
-                    float4 tr[5];
-#pragma unroll
-                    for (int k = 0; k < 5; ++k) tr[k] = k < ndon ? ld4e(pop + dr[k] * W + e0) : ti;
-                    const uint4 w = philox(make_uint4((uint32_t)c, (uint32_t)(row0 + r), gen, kTagCr), key);
-                    float4 x4 = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const int e = e0 + q;
-                        if (e < D) {
-                            const float u = u01(pick(w, (uint32_t)q));
-                            float x;
-                            if (e == jrand || u < CR) {
-                                float xr[5];
-#pragma unroll
-                                for (int k = 0; k < 5; ++k) xr[k] = f4ge(tr[k], q);
-                                x = mutant<float>(st, F, f4ge(ti, q), f4ge(tb, q), xr);
-                            } else {
-                                x = f4ge(ti, q);
-                            }
-                            x = check_bound<float>(x, lb, ub, ok_bound);
-                            f4se(x4, q, x);
-                        }
-                    }
-                    st4e(Xs + r * XW + e0, x4);
-                }
-            }
+            // (1b) trial rows from the shared-memory population (the common DE/rand/1 compiled alone)
+            if (st == SPEO_DE_RAND_1)
+                trial_rows<SPEO_DE_RAND_1, W, XW>(pop, Xs, sRg, P, D, nch, best, st, F, thr, lb, ub, key, row0, gen,
+                                                  ok_bound);
+            else
+                trial_rows<-1, W, XW>(pop, Xs, sRg, P, D, nch, best, st, F, thr, lb, ub, key, row0, gen, ok_bound);
             __syncthreads();
             // (2) A operand: warp w converts rows of tile (w >> 2) & 1, lane quarter w & 3, K half w >> 3
             {
@@ -255,25 +266,30 @@ __global__ void __launch_bounds__(kThreadsE, 1)
                                          kApartE, b_hi, L.b_bytes, Kp, Kp, 0, S);
                 tc::mma_commit(&bar_mma);
             }
-            // (4) one thread per row reads its z row and reduces the objective
+            // (4) two threads per row (warp w: lane quarter w & 3, tile (w >> 2) & 1, column part
+            // w >> 3) read z back and reduce the objective; part p of row m lands in sF[p][m]
+            const int te = (warp >> 2) & 1, he = warp >> 3;
             bool ok = true;
-            if (warp < 4 * ntile) ok = tc::mbar_wait_sleep(&bar_mma, (uint32_t)(g & 1), kWaitBudgetE);
+            if (te < ntile) ok = tc::mbar_wait_sleep(&bar_mma, (uint32_t)(g & 1), kWaitBudgetE);
             if (__syncthreads_or(!ok)) {
                 aborted = true;
                 break;
             }
-            if (warp < 4 * ntile) {
+            if (te < ntile) {
                 tc::fence_after_sync();
-                const int t = warp >> 2, m = t * tcs::kTileM + (warp & 3) * 32 + lane;
-                float f = tcs::epilogue_row(tmem + (uint32_t)(kAccColsE * t), warp, D, 0, Kp, s.func_id, scale);
-                f = f + 0.f;  // speo_evaluate_tc adds the (empty) second column half
-                if (m < P) sF[m] = f;
+                const int m = te * tcs::kTileM + (warp & 3) * 32 + lane, h = tcs::epi_split(Kp);
+                const int c0 = he == 0 ? 0 : h, c1 = he == 0 ? (Kp < h ? Kp : h) : Kp;
+                const float f = c0 < c1 ? tcs::epilogue_row(tmem + (uint32_t)(kAccColsE * te), warp, D, c0, c1,
+                                                            s.func_id, scale)
+                                        : 0.f;
+                if (m < P) sF[he * Pf + m] = f;
             }
             tc::fence_before_sync();
             __syncthreads();
-            // (5) greedy selection in place: strict `<` (kernel_DE_CUDA.cu:312)
+            // (5) greedy selection in place: strict `<` (kernel_DE_CUDA.cu:312); the fitness is the
+            // first column part's sum plus the second's, as speo_evaluate_tc adds them
             for (int r = grp; r < P; r += RPP) {
-                const float tf = sF[r];
+                const float tf = sF[r] + sF[Pf + r];
                 if (tf < fit[r]) {
                     for (int c = gl; c < nch; c += G) st4e(pop + r * W + 4 * c, ld4e(Xs + r * XW + 4 * c));
                     if (gl == 0) fit[r] = tf;

@@ -371,9 +371,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             float f = 0.f;
             bool writer = ch == 0;
             if (func_sum_form(cur.func)) {
-                // columns [0, 64) on the first warp of the quarter, [64, Np) on the second; the
-                // second warp's partial sums meet the first's through psum[i % 2]
-                const int c0 = ch * 64, c1 = ch == 0 ? (Np < 64 ? Np : 64) : Np;
+                // columns [0, h) on the first warp of the quarter, [h, Np) on the second
+                // (tcs::epi_split); the second warp's partial sums meet the first's through psum[i % 2]
+                const int h = tcs::epi_split(Np);
+                const int c0 = ch == 0 ? 0 : h, c1 = ch == 0 ? (Np < h ? Np : h) : Np;
                 f = c0 < c1 ? epilogue_row(acc_t, warp, cur.D, c0, c1, cur.func, func_scale(cur.func)) : 0.f;
                 float *ps = psum + (i & 1) * kTileM;
                 if (ch == 1) ps[m] = f;

@@ -138,6 +138,11 @@ __device__ __forceinline__ uint64_t obj_term2(int func, uint64_t z)
     return fma2(z, z, mul2(mul2(pk2(20.0f, 20.0f), sn), sn));
 }
 
+// The per-coordinate-sum epilogue splits a row's Np accumulator columns between two threads:
+// [0, h) and [h, Np) with h = 32 ceil(Np / 64); the second part's sum is added to the first's. Every
+// kernel using this epilogue splits the same way, so a row's fitness does not depend on the kernel.
+__host__ __device__ __forceinline__ int epi_split(int Np) { return 32 * ((Np + 63) / 64); }
+
 // sum_j term(scale * z_j) of one 32-column chunk starting at column c (j < D), added to the packed
 // pair accumulator two columns per operation, in column order.
 __device__ __forceinline__ void row_terms32(uint64_t &acc, const uint32_t (&r)[32], int c, int D, int func,
