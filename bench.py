@@ -298,6 +298,8 @@ def bench_speo(args) -> dict:
         out["surrogate"] = bench_surrogate(L, dev, torch)
     if not args.no_e2e:
         out["e2e"] = bench_e2e(L, dev, torch, max(args.steps, 100))
+        d = bench_e2e_dropin(L, dev, torch, max(args.steps, 100))
+        out["e2e_dropin"] = {"value": d["value"], "unit": d["unit"], "path": d["path"]}
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(sample_s=args.cpu_sample_s)
     return out
@@ -468,6 +470,50 @@ def bench_surrogate_sweep(L, dev, torch, ks=(2, 4, 8), steps=(1, 4, 16, 48), eve
 
 
 def bench_e2e(L, dev, torch, steps: int) -> dict:
+    """The headline loop over host buffers through the C ABI's island loop (speo_island_run_tc: the
+    reference's IslandEA::Execute, generations and ring migration, as one call): the initial
+    population, o and M^T uploaded from pinned host memory, the initial fitness evaluated, then
+    `steps` generations with every generation's fitness vector read back to pinned host memory
+    (on a second stream while the next launch runs); all inside the timed region (wall clock)."""
+    from speo_gb300 import _lib
+
+    tab = headline_table(dev)
+    n, ld = tab.rows, tab.ld
+    rng = np.random.default_rng(0)
+    h_pop = torch.from_numpy(rng.uniform(-100, 100, (n, ld)).astype(np.float32)).pin_memory()
+    h_pop[:, DIM:] = 0
+    h_sh = tab.inst_shift[0].cpu().pin_memory()
+    h_rot = tab.inst_rot[0].cpu().pin_memory()
+    h_hist = torch.zeros(steps * n, dtype=torch.float32).pin_memory()   # every generation's fitness
+    stream = torch.cuda.current_stream()
+
+    def run(nsteps):
+        tab.pop[tab.cur].copy_(h_pop, non_blocking=True)
+        tab.inst_shift[0].copy_(h_sh, non_blocking=True)
+        tab.inst_rot[0].copy_(h_rot, non_blocking=True)
+        tab.gen.zero_()
+        tab.evaluate(use_tc=False)
+        _lib.check(L.speo_island_run_tc(tab.d_segs.data_ptr(), N_ISLANDS, DIM, DIM, POP, tab.pop[tab.cur].data_ptr(),
+                                        tab.fit[tab.cur].data_ptr(), n, tab.gen.data_ptr(), 0, nsteps, INTERVAL,
+                                        MIGRANTS, tab.staging.data_ptr(), tab.max_ld, h_hist.data_ptr(),
+                                        stream.cuda_stream), "speo_island_run_tc")
+
+    run(20)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run(steps)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    h2d = (n * ld + h_sh.numel() + h_rot.numel()) * 4
+    return {"value": n * steps / dt, "unit": "evals/s", "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": n * 4,
+            "steps": steps, "dtype": "fp32",
+            "path": "speo_island_run_tc (the island loop of 128 islands of 256 as one C-ABI call: tensor-core "
+                    "island-resident epochs of up to 50 generations and speo_ring_migrate every 50 generations); "
+                    "initial rows, o and M^T uploaded and the initial fitness evaluated inside the timed region, every "
+                    "generation's fitness vector read back to pinned host memory"}
+
+
+def bench_e2e_dropin(L, dev, torch, steps: int) -> dict:
     """The headline loop through the reference-shaped C ABI with host buffers: the initial
     population, o, M^T and the per-sub-island DEInfo uploaded from pinned host memory, the
     initial API_evaluateFitness_f32, then `steps` generations of speo_de_run_f32 (128 sub-islands
@@ -1094,6 +1140,7 @@ def one_section(args) -> dict | None:
         return bench_operators(L, dev, torch, peaks(), args.ops_islands)
     if args.e2e_only:
         return {"e2e": bench_e2e(L, dev, torch, max(args.steps, 100)),
+                "e2e_dropin": bench_e2e_dropin(L, dev, torch, max(args.steps, 100)),
                 "e2e_config1_fp32": bench_e2e_config1(L, dev, torch, 1000),
                 "e2e_config1_fp64": bench_e2e_config1(L, dev, torch, 1000, f64=True)}
     if args.published_only:

@@ -337,6 +337,21 @@ SPEO_API int speo_generation_epoch_tc(const speo_segment *d_segs, int n_segs, in
                                       const float *pop_in, const float *fit_in, float *pop_out, float *fit_out,
                                       uint32_t *d_gen, int generations, void *stream);
 
+/* The island loop of IslandEA::Execute (src/island_EA.cc:78-113) as one call: `generations`
+ * generations of speo_generation_epoch_tc on the islands of d_segs (in place in pop / fit, rows
+ * rows, P <= 256, D <= 64), in launches of up to `interval` generations, and speo_ring_migrate
+ * (migrants rows, caller staging of n_segs * migrants * (max_ld + 1) floats) after every
+ * generation count that is a multiple of `interval`, counted from the start of the run: `first` is
+ * the number of generations the run has already done. h_fitness (may be null; pinned host memory
+ * for the copies to overlap): generations x rows floats that receive every generation's fitness
+ * (generation g of this call at h_fitness + g * rows), read back on a second stream while the next
+ * launch runs. Runs on `stream`; synchronous (returns when the generations and copies are done).
+ * The results equal speo_generation_epoch_tc + speo_ring_migrate called in the same order. */
+SPEO_API int speo_island_run_tc(const speo_segment *d_segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
+                                float *pop, float *fit, long long rows, uint32_t *d_gen, int first, int generations,
+                                int interval, int migrants, float *staging, int max_ld, float *h_fitness,
+                                void *stream);
+
 /* The library's tile-shape tuner for speo_generation (k_generation / k_generation_mixed), in
  * place of the reference's fixed launch shapes (CUDA_EA_library/kernel_CEC2014_CUDA.cu:56-73,
  * kernel_DE_CUDA.cu:48-62). h_segs is a HOST copy of a segment table whose shift / rot pointers are

@@ -130,7 +130,8 @@ __device__ __forceinline__ void trial_rows(const float *pop, float *Xs, const in
 template <int Q>
 __global__ void __launch_bounds__(kThreadsE, 1)
     k_island_epoch_tc(const speo_segment *__restrict__ segs, int Pmax, const float *pop_in, const float *fit_in,
-                      float *pop_out, float *fit_out, uint32_t *gen_ctr, int generations)
+                      float *pop_out, float *fit_out, uint32_t *gen_ctr, int generations, float *hist,
+                      long long hist_ld)
 {
     constexpr int W = 32 * Q, XW = W + 4, G = Q == 1 ? 8 : 16, RPP = kThreadsE / G;
     extern __shared__ __align__(1024) uint8_t smem_e[];
@@ -287,12 +288,19 @@ __global__ void __launch_bounds__(kThreadsE, 1)
             tc::fence_before_sync();
             __syncthreads();
             // (5) greedy selection in place: strict `<` (kernel_DE_CUDA.cu:312); the fitness is the
-            // first column part's sum plus the second's, as speo_evaluate_tc adds them
+            // first column part's sum plus the second's, as speo_evaluate_tc adds them. The G lanes
+            // of a row (one warp) all read its fitness before one of them replaces it; with a
+            // history buffer, generation g's fitness of the row goes to hist[g][row].
+            const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (lane & ~(G - 1));
             for (int r = grp; r < P; r += RPP) {
-                const float tf = sF[r] + sF[Pf + r];
-                if (tf < fit[r]) {
+                const float tf = sF[r] + sF[Pf + r], fo = fit[r];
+                const bool win = tf < fo;
+                if (win)
                     for (int c = gl; c < nch; c += G) st4e(pop + r * W + 4 * c, ld4e(Xs + r * XW + 4 * c));
-                    if (gl == 0) fit[r] = tf;
+                __syncwarp(gmask);
+                if (gl == 0) {
+                    if (win) fit[r] = tf;
+                    if (hist) hist[(size_t)g * (size_t)hist_ld + (size_t)(row0 + r)] = win ? tf : fo;
                 }
             }
         }
@@ -340,7 +348,8 @@ int optin_smem()
 
 template <int Q>
 int launch_epoch_tc(const speo_segment *segs, int n_segs, int max_pop, const float *pop_in, const float *fit_in,
-                    float *pop_out, float *fit_out, uint32_t *d_gen, int generations, cudaStream_t st)
+                    float *pop_out, float *fit_out, uint32_t *d_gen, int generations, float *hist, long long hist_ld,
+                    cudaStream_t st)
 {
     const EpochTcLayout L = epoch_tc_layout(Q, max_pop);
     const int limit = optin_smem();
@@ -349,7 +358,7 @@ int launch_epoch_tc(const speo_segment *segs, int n_segs, int max_pop, const flo
     cudaError_t e = cudaFuncSetAttribute(k_island_epoch_tc<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_island_epoch_tc)");
     k_island_epoch_tc<Q><<<n_segs, kThreadsE, smem, st>>>(segs, max_pop, pop_in, fit_in, pop_out, fit_out, d_gen,
-                                                          generations);
+                                                          generations, hist, hist_ld);
     return check_launch("k_island_epoch_tc");
 }
 
@@ -381,6 +390,100 @@ extern "C" int speo_generation_epoch_tc(const speo_segment *segs, int n_segs, in
     if (dim_lo <= 32 && Q == 2)
         return fail(SPEO_ERR_UNSUPPORTED, "speo_generation_epoch_tc: segments must share one column class");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    return Q == 1 ? launch_epoch_tc<1>(segs, n_segs, max_pop, pop_in, fit_in, pop_out, fit_out, d_gen, generations, st)
-                  : launch_epoch_tc<2>(segs, n_segs, max_pop, pop_in, fit_in, pop_out, fit_out, d_gen, generations, st);
+    return Q == 1 ? launch_epoch_tc<1>(segs, n_segs, max_pop, pop_in, fit_in, pop_out, fit_out, d_gen, generations,
+                                       nullptr, 0, st)
+                  : launch_epoch_tc<2>(segs, n_segs, max_pop, pop_in, fit_in, pop_out, fit_out, d_gen, generations,
+                                       nullptr, 0, st);
+}
+
+// ---- the island loop over host buffers ------------------------------------------------------
+// IslandEA::Execute (src/island_EA.cc:78-113) runs generations (DE_CUDA::Run) and, every `interval`
+// generations, the migration; the island driver reads results back to the host. Here that loop is
+// one call: tensor-core epochs of up to `interval` generations per launch, each writing every
+// generation's fitness into one of two device history buffers that a second stream copies to the
+// caller's host buffer while the next launch runs, and the ring migration at the migration points.
+namespace {
+struct IslandRunState {
+    cudaStream_t copy = nullptr;
+    cudaEvent_t made[2] = {nullptr, nullptr}, read[2] = {nullptr, nullptr};
+    float *hist = nullptr;
+    size_t cap = 0;  // floats
+};
+thread_local IslandRunState t_island_run;
+
+int island_run_state(size_t hist_floats, IslandRunState **out)
+{
+    IslandRunState &r = t_island_run;
+    if (!r.copy) {
+        if (int e = check_cuda(cudaStreamCreateWithFlags(&r.copy, cudaStreamNonBlocking), "island run: stream"))
+            return e;
+        for (int b = 0; b < 2; ++b) {
+            if (int e = check_cuda(cudaEventCreateWithFlags(&r.made[b], cudaEventDisableTiming), "island run: event"))
+                return e;
+            if (int e = check_cuda(cudaEventCreateWithFlags(&r.read[b], cudaEventDisableTiming), "island run: event"))
+                return e;
+        }
+    }
+    if (r.cap < hist_floats) {  // the previous call synchronised: nothing uses the old buffer
+        if (r.hist) cudaFree(r.hist);
+        r.hist = nullptr;
+        r.cap = 0;
+        if (int e = check_cuda(cudaMalloc(&r.hist, sizeof(float) * hist_floats), "island run: history")) return e;
+        r.cap = hist_floats;
+    }
+    *out = &r;
+    return SPEO_OK;
+}
+}  // namespace
+
+extern "C" int speo_island_run_tc(const speo_segment *segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
+                                  float *pop, float *fit, long long rows, uint32_t *d_gen, int first, int generations,
+                                  int interval, int migrants, float *staging, int max_ld, float *h_fitness,
+                                  void *stream)
+{
+    if (!segs || !pop || !fit || !d_gen || n_segs < 1 || rows < 1 || generations < 0 || first < 0 || interval < 1)
+        return fail(SPEO_ERR_INVALID_ARG, "speo_island_run_tc: bad arguments");
+    if (migrants > 0 && (!staging || max_ld < 1))
+        return fail(SPEO_ERR_INVALID_ARG, "speo_island_run_tc: migration needs a staging buffer and max_ld");
+    if (dim_lo < 1 || dim_lo > dim_hi) return fail(SPEO_ERR_INVALID_ARG, "speo_island_run_tc: dim range");
+    if (!speo_epoch_tc_fits(max_pop, dim_hi))
+        return fail(SPEO_ERR_UNSUPPORTED, "speo_island_run_tc: islands of P <= %d, D <= %d are not supported",
+                    max_pop, dim_hi);
+    const int Q = dim_hi <= 32 ? 1 : 2;
+    if (dim_lo <= 32 && Q == 2)
+        return fail(SPEO_ERR_UNSUPPORTED, "speo_island_run_tc: segments must share one column class");
+    if (generations == 0) return SPEO_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    IslandRunState *rs = nullptr;
+    const size_t per = (size_t)interval * (size_t)rows;  // one launch's history
+    if (int e = island_run_state(h_fitness ? 2 * per : 0, &rs)) return e;
+    int e = SPEO_OK, done = 0;
+    for (int i = 0; !e && done < generations; ++i) {
+        const int pos = first + done;
+        const int k = generations - done < interval - pos % interval ? generations - done : interval - pos % interval;
+        const int b = i & 1;
+        float *hb = h_fitness ? rs->hist + (size_t)b * per : nullptr;
+        if (h_fitness && i >= 2) e = check_cuda(cudaStreamWaitEvent(st, rs->read[b], 0), "island run: wait");
+        if (!e)
+            e = Q == 1 ? launch_epoch_tc<1>(segs, n_segs, max_pop, pop, fit, pop, fit, d_gen, k, hb, rows, st)
+                       : launch_epoch_tc<2>(segs, n_segs, max_pop, pop, fit, pop, fit, d_gen, k, hb, rows, st);
+        if (!e && h_fitness) {
+            e = check_cuda(cudaEventRecord(rs->made[b], st), "island run: record");
+            if (!e) e = check_cuda(cudaStreamWaitEvent(rs->copy, rs->made[b], 0), "island run: wait");
+            if (!e)
+                e = check_cuda(cudaMemcpyAsync(h_fitness + (size_t)done * (size_t)rows, hb,
+                                               sizeof(float) * (size_t)k * (size_t)rows, cudaMemcpyDeviceToHost,
+                                               rs->copy),
+                               "island run: fitness read-back");
+            if (!e) e = check_cuda(cudaEventRecord(rs->read[b], rs->copy), "island run: record");
+        }
+        done += k;
+        if (!e && migrants > 0 && (first + done) % interval == 0)
+            e = speo_ring_migrate(segs, n_segs, migrants, pop, fit, staging, max_ld, st);
+    }
+    if (h_fitness)
+        for (int b = 0; b < 2; ++b)
+            if (int e2 = check_cuda(cudaStreamWaitEvent(st, rs->read[b], 0), "island run: wait"); e2 && !e) e = e2;
+    const int es = check_cuda(cudaStreamSynchronize(st), "island run: sync");
+    return e ? e : es;
 }

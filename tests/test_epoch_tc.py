@@ -133,3 +133,44 @@ def test_epoch_tc_refuses_what_it_does_not_run(lib, cuda):
     bits = ctypes.c_uint32(0)
     assert lib.speo_device_error_bits(ctypes.byref(bits)) == 0
     assert bits.value == _lib.SPEO_DEVERR_BAD_SEGMENT
+
+
+def test_island_run_equals_epochs_and_ring_calls(lib, cuda):
+    """speo_island_run_tc (the island loop as one call, host fitness history) equals
+    speo_generation_epoch_tc one generation at a time with speo_ring_migrate at every 10th
+    generation of the run; the history holds every generation's fitness."""
+    import ctypes
+
+    import torch
+    from speo_gb300 import _lib
+    from speo_gb300.device import SegmentSpec, SegmentTable
+    from speo_gb300.instances import make_instance
+
+    def table():
+        inst = [make_instance(4242, 50)]
+        specs = [SegmentSpec(pop_size=256, dim=50, func_id=9, instance=0, seed=900 + i, ring_next=(i + 1) % 4)
+                 for i in range(4)]
+        return SegmentTable(specs, inst, device=str(cuda))
+
+    a, b = table(), table()
+    a.init_population()
+    b.init_population()
+    first, gens, interval, k = 3, 24, 10, 5
+    for t in (a, b):                              # the run's first 3 generations, before the call
+        t.epoch_tc(first)
+    hist = torch.full((gens, a.rows), float("nan")).pin_memory()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.speo_island_run_tc(a.d_segs.data_ptr(), 4, 50, 50, 256, a.pop[a.cur].data_ptr(),
+                                      a.fit[a.cur].data_ptr(), a.rows, a.gen.data_ptr(), first, gens, interval, k,
+                                      a.staging.data_ptr(), a.max_ld, hist.data_ptr(), stream), "speo_island_run_tc")
+    want = []
+    for g in range(first, first + gens):
+        b.epoch_tc(1)
+        want.append(b.fit[b.cur].cpu().numpy().copy())
+        if (g + 1) % interval == 0:
+            b.migrate(k)
+    torch.cuda.synchronize()
+    assert np.array_equal(a.pop[a.cur].cpu().numpy(), b.pop[b.cur].cpu().numpy())
+    assert np.array_equal(a.fit[a.cur].cpu().numpy(), b.fit[b.cur].cpu().numpy())
+    assert np.array_equal(hist.numpy(), np.stack(want))
+    assert int(a.gen[0].cpu()) == int(b.gen[0].cpu()) == first + gens
