@@ -246,8 +246,8 @@ def bench_speo(args) -> dict:
     gens_per_launch = args.steps / len(plan)
     if use_tc:
         kernel = (f"k_island_epoch_tc<2> (one 512-thread block per island, {N_ISLANDS} blocks; up to 50 generations "
-                  "per launch with the island and its trials in shared memory, the rotation on tcgen05: six "
-                  "split-BF16 products per K step into TMEM accumulators)")
+                  "per launch with the island and its trials in shared memory, the rotation on tcgen05: three "
+                  "split-FP16 products per K step into TMEM accumulators)")
     elif 2 * N_ISLANDS <= sms:
         kernel = f"k_island_epoch2<2> (two-block cluster per island, {2 * N_ISLANDS} blocks)"
     else:
@@ -256,7 +256,8 @@ def bench_speo(args) -> dict:
     traffic = EPOCH_LAUNCH_TRAFFIC_BYTES["tc" if use_tc else "simt"]
     rot_flop_gen = EVALS_PER_STEP * 2 * DIM * DIM
     kp = (DIM + 15) // 16 * 16
-    tensor_flop_gen = N_ISLANDS * ((POP + 127) // 128) * 5 * 2 * 128 * kp * kp   # executed split products
+    # executed split products: three FP16 products per K step, M = 128 rows per tile, N = K = kp
+    tensor_flop_gen = N_ISLANDS * ((POP + 127) // 128) * 3 * 2 * 128 * kp * kp
     sm_mhz = clocks["sm_max_mhz"] or 2070.0
     fp32_peak = sms * FP32_FMA_PER_SM_CLK * 2 * sm_mhz * 1e6 / 1e12
     fp32_achieved = rot_flop_gen * args.steps / (kern_ms / 1e3) / 1e12
@@ -310,12 +311,18 @@ def bench_speo(args) -> dict:
 # launch and its writes stay in L2, so the figure does not grow with the generations per launch).
 EPOCH_LAUNCH_TRAFFIC_BYTES = {"simt": 7040512 + 11008, "tc": 7058688 + 13824}
 C4_TRAIN_STEPS = 48   # Adam steps per generation: 48 x 4096 = 6 passes over a generation's 32768 new rows
-C4_EXPLORE = 0.05     # fraction of targets that take a uniformly drawn trial instead of the screened one
+C4_EXPLORE = 0.05
+# Training batch x Adam steps per generation at about the same samples per generation (k = 8,
+# training every generation): larger batches fill more SMs per step.
+SURROGATE_BATCH_GRID = [dict(k=8, train_steps=st, train_every=1, train_batch=b, lr=lr)
+                        for b, st, lr in ((4096, 48, 1e-3), (8192, 24, 1e-3), (8192, 24, 2e-3), (16384, 12, 2e-3),
+                                          (16384, 12, 4e-3), (16384, 24, 2e-3), (32768, 6, 4e-3), (32768, 6, 8e-3),
+                                          (32768, 12, 4e-3))]     # fraction of targets that take a uniformly drawn trial instead of the screened one
 
 
 def c4_run(L, dev, torch, func: int, mode: str, max_gens: int, log_every: int = 10, stop_at: float | None = None,
            train_steps: int = 16, explore: float = 0.25, train_k: int = 8, train_every: int = 1,
-           use_graph: bool = True):
+           use_graph: bool = True, train_batch: int = 4096, lr: float = 1e-3):
     """One run of the headline shape (plain or surrogate-screened) logging the FP64 best error
     every `log_every` generations; stops early once the error reaches `stop_at`. Blocks of
     `log_every` generations replay one CUDA graph after the first (eager) block. The surrogate
@@ -331,7 +338,7 @@ def c4_run(L, dev, torch, func: int, mode: str, max_gens: int, log_every: int = 
     surr = None
     if mode == "surrogate":
         surr = C.c_void_p()
-        _lib.check(L.speo_surrogate_create(C.byref(surr), 50, 256, 1 << 20, 4096, 1e-3, 0.01, 4242),
+        _lib.check(L.speo_surrogate_create(C.byref(surr), 50, 256, 1 << 20, train_batch, lr, 0.01, 4242),
                    "speo_surrogate_create")
     assert log_every % 2 == 0 and INTERVAL % log_every == 0 and log_every % train_every == 0
 
@@ -423,13 +430,14 @@ def bench_surrogate(L, dev, torch, ras_gens: int = 200, schedule: dict | None = 
 
 
 def bench_surrogate_sweep(L, dev, torch, ks=(2, 4, 8), steps=(1, 4, 16, 48), every=(1, 5, 10),
-                          ras_gens: int = 200) -> dict:
+                          ras_gens: int = 200, grid: list | None = None) -> dict:
     """The surrogate's schedule against the plain DE on the headline shape: trials per target k,
     Adam steps per training generation, and training every G-th generation. For each point, the
     exact evaluations and wall time to an FP64 error of 1e-8 on the rotated sphere, and the
     exact evaluations and wall time to the plain run's 200-generation error on the rotated
     Rastrigin, each as a ratio plain / surrogate (> 1: the surrogate needs less). The Pareto
-    front is over (exact-evaluation ratio, wall ratio)."""
+    front is over (exact-evaluation ratio, wall ratio). `grid`, if given, lists the points
+    instead (dicts of k, train_steps, train_every and optionally train_batch and lr)."""
     from speo_gb300 import _lib
 
     sp, _ = c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "plain", 4000, stop_at=1e-8)
@@ -437,28 +445,31 @@ def bench_surrogate_sweep(L, dev, torch, ks=(2, 4, 8), steps=(1, 4, 16, 48), eve
     target = rp["final_err"]
     hit_p = first_reach(cp, target)
     points = []
-    for k in ks:
-        for st in steps:
-            for ev in every:
-                sch = dict(train_steps=st, explore=C4_EXPLORE, train_k=k, train_every=ev)
-                ss, _ = c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8, **sch)
-                rs, cs = c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, "surrogate", ras_gens, **sch)
-                pt = {"k": k, "train_steps": st, "train_every": ev, "gens_per_s": rs["gens_per_s"]}
-                if ss["exact_evals_to_target"]:
-                    pt["sphere"] = {"evals_ratio": sp["exact_evals_to_target"] / ss["exact_evals_to_target"],
-                                    "wall_ratio": sp["wall_s_to_target"] / ss["wall_s_to_target"],
-                                    "generations": ss["generations"]}
-                else:
-                    pt["sphere"] = {"reached": False, "final_err": ss["final_err"]}
-                hit = first_reach(cs, target)
-                pt["rastrigin"] = ({"evals_ratio": hit_p["exact_evals"] / hit["exact_evals"],
-                                    "wall_ratio": hit_p["wall_s"] / hit["wall_s"], "at_gen": hit["gen"]}
-                                   if hit else {"reached": False, "final_err": rs["final_err"]})
-                points.append(pt)
+    if grid is None:
+        grid = [dict(k=k, train_steps=st, train_every=ev) for k in ks for st in steps for ev in every]
+    for g in grid:
+        k, st, ev = g["k"], g["train_steps"], g["train_every"]
+        sch = dict(train_steps=st, explore=C4_EXPLORE, train_k=k, train_every=ev,
+                   train_batch=g.get("train_batch", 4096), lr=g.get("lr", 1e-3))
+        ss, _ = c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8, **sch)
+        rs, cs = c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, "surrogate", ras_gens, **sch)
+        pt = {"k": k, "train_steps": st, "train_every": ev, "train_batch": sch["train_batch"], "lr": sch["lr"],
+              "gens_per_s": rs["gens_per_s"]}
+        if ss["exact_evals_to_target"]:
+            pt["sphere"] = {"evals_ratio": sp["exact_evals_to_target"] / ss["exact_evals_to_target"],
+                            "wall_ratio": sp["wall_s_to_target"] / ss["wall_s_to_target"],
+                            "generations": ss["generations"]}
+        else:
+            pt["sphere"] = {"reached": False, "final_err": ss["final_err"]}
+        hit = first_reach(cs, target)
+        pt["rastrigin"] = ({"evals_ratio": hit_p["exact_evals"] / hit["exact_evals"],
+                            "wall_ratio": hit_p["wall_s"] / hit["wall_s"], "at_gen": hit["gen"]}
+                           if hit else {"reached": False, "final_err": rs["final_err"]})
+        points.append(pt)
 
     def front(key):
         pts = [p for p in points if "evals_ratio" in p[key]]
-        return [(p["k"], p["train_steps"], p["train_every"]) for p in pts
+        return [(p["k"], p["train_steps"], p["train_every"], p["train_batch"], p["lr"]) for p in pts
                 if not any(q[key]["evals_ratio"] >= p[key]["evals_ratio"] and q[key]["wall_ratio"] >= p[key]["wall_ratio"]
                            and (q[key]["evals_ratio"], q[key]["wall_ratio"]) != (p[key]["evals_ratio"], p[key]["wall_ratio"])
                            for q in pts)]
@@ -745,7 +756,7 @@ def bench_operators(L, dev, torch, pk, n_isl: int = 16384) -> dict:
     # tcgen05 evaluation: read D floats, write 1
     tab_tc.pop[0].copy_(tab.pop[tab.cur])
     out_fit = torch.empty(rows, device=dev)
-    rec("k_evaluate_tc (TMA + tcgen05, three-way BF16 split)", timed(lambda: tab_tc.evaluate(which=0, use_tc=True, out=out_fit)),
+    rec("k_evaluate_tc (TMA + tcgen05, two-way FP16 split)", timed(lambda: tab_tc.evaluate(which=0, use_tc=True, out=out_fit)),
         rows * (D * s + s))
     rec("k_eval_seg<4> (CUDA-core evaluation)", timed(lambda: tab.evaluate(which=tab.cur, out=out_fit)),
         rows * (D * s + s))
@@ -797,7 +808,7 @@ def bench_operators(L, dev, torch, pk, n_isl: int = 16384) -> dict:
 
 def bench_config2(L, dev, torch, flush) -> dict:
     """Config 2: 256 islands x 128, D = 100, mixed objectives; the rotation runs on the tcgen05
-    tensor cores in three-way split BF16 (trial generation, tensor-core evaluation and selection per generation,
+    tensor cores in two-way split FP16 (trial generation, tensor-core evaluation and selection per generation,
     20 generations per CUDA graph). Precision: tensor-core and CUDA-core FP32 fitness of 4096
     sampled rows against the FP64 oracle; FP64 re-evaluation of every island's best."""
     import speo_oracle
@@ -832,10 +843,10 @@ def bench_config2(L, dev, torch, flush) -> dict:
     rel_cc = np.abs(fit_cc.cpu().numpy()[sample] - ref) / np.maximum(np.abs(ref), 1e-30)
     rows, errs = tab.best_f64()
     return {"workload": "256 islands x P=128, D=100, per island rotated sphere or rotated Rastrigin (seeded), "
-                        "three-way split BF16 tcgen05 evaluation (six products)",
+                        "two-way split FP16 tcgen05 evaluation (three products, power-of-two row scaling)",
             "ms_per_generation": ms, "gens_per_s": 1e3 / ms, "evals_per_s": tab.rows / (ms / 1e3),
             "launches_per_generation": 3,
-            "fitness_rel_err_vs_fp64": {"tcgen05_bf16_split3": {"max": float(rel_tc.max()), "median": float(np.median(rel_tc)),
+            "fitness_rel_err_vs_fp64": {"tcgen05_f16_split2": {"max": float(rel_tc.max()), "median": float(np.median(rel_tc)),
                                                            "p99": float(np.quantile(rel_tc, 0.99))},
                                         "cuda_core_fp32": {"max": float(rel_cc.max()), "median": float(np.median(rel_cc)),
                                                            "p99": float(np.quantile(rel_cc, 0.99))},
@@ -1131,7 +1142,7 @@ def one_section(args) -> dict | None:
     from speo_gb300 import _lib
 
     if not (args.ops_only or args.e2e_only or args.published_only or args.mlp_case or args.c4_only
-            or args.configs_only or args.surrogate_sweep):
+            or args.configs_only or args.surrogate_sweep or args.surrogate_batch_sweep):
         return None
     dev = "cuda:0"
     torch.cuda.set_device(0)
@@ -1153,6 +1164,8 @@ def one_section(args) -> dict | None:
         return {"surrogate": bench_surrogate(L, dev, torch, args.c4_gens)}
     if args.surrogate_sweep:
         return {"surrogate_sweep": bench_surrogate_sweep(L, dev, torch)}
+    if args.surrogate_batch_sweep:
+        return {"surrogate_batch_sweep": bench_surrogate_sweep(L, dev, torch, grid=SURROGATE_BATCH_GRID)}
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
     return {"config1_island_d30": bench_config1(L, dev, torch, flush),
             "config2_precision": bench_config2(L, dev, torch, flush),
@@ -1182,6 +1195,8 @@ def main() -> None:
     ap.add_argument("--mlp-case", action="store_true", help="only the surrogate network's kernels")
     ap.add_argument("--surrogate-sweep", action="store_true",
                     help="only the surrogate schedule sweep (k, Adam steps, training interval) against plain DE")
+    ap.add_argument("--surrogate-batch-sweep", action="store_true",
+                    help="only the surrogate's training batch / Adam steps / learning rate sweep against plain DE")
     ap.add_argument("--e2e-only", action="store_true", help="only the end-to-end drop-in measurements")
     ap.add_argument("--published-only", action="store_true",
                     help="only the reference's published configuration (F23-F30, D=100, 4096 rows)")

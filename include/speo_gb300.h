@@ -29,7 +29,8 @@
  *     (src/migrate.cc:46-136), the reference's migration policy family over an archipelago of
  *     islands on one device (src/migrate.cc:34-186, src/buffer_manage.cc:36-313), the
  *     reference's DE_CUDA::Run loop as one call, its DE configuration modes, the tcgen05
- *     rotation GEMM in BF16 3-term split precision, FP64 re-evaluation of each segment's best,
+ *     rotation GEMM in two-way split FP16 precision (power-of-two row scaling), FP64
+ *     re-evaluation of each segment's best,
  *     and the online MLP surrogate.
  *
  * All pointers to population data are device pointers owned by the caller; no entry point
@@ -273,10 +274,12 @@ SPEO_API int speo_init_population(const speo_segment *d_segs, int n_segs, const 
 SPEO_API int speo_evaluate(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,
                   int dim_lo, int dim_hi, const float *pop, float *fit, void *stream);
 
-/* Same, with the rotation on the tcgen05 tensor cores: y = x - o and M each split three ways
- * into BF16 (hi + mid + lo, ~2^-27 relative residue), the six products of size >= 2^-18 of the
- * leading one per K step, FP32 accumulation in tensor memory (as exact as an FP32 CUDA-core
- * rotation: fitness within 1e-5 relative of FP64 for the rotated Rastrigin and sphere), fused shift/scale/objective/row-reduction epilogue (one
+/* Same, with the rotation on the tcgen05 tensor cores: each row y = x - o scaled by its own power
+ * of two (largest |y_j| into [2^14, 2^15)) and M by one per instance, each split two ways into
+ * FP16 (hi + lo, ~2^-22 relative residue), three products per K step (y_lo M_hi, y_hi M_lo,
+ * y_hi M_hi), FP32 accumulation in tensor memory (as exact as an FP32 CUDA-core rotation: fitness
+ * within 1e-5 relative of FP64 for the rotated Rastrigin and sphere), fused
+ * unscale/shift/scale/objective/row-reduction epilogue (one
  * tile row per thread; the per-coordinate sums 9 and 31 packed two columns per operation, the
  * other rotated ids 1-7, 11-16 through the row accumulator). Ids 8, 10 (no rotation) and 17-30
  * (several matrices) are flagged (SPEO_DEVERR_BAD_SEGMENT) and skipped.
@@ -325,7 +328,7 @@ SPEO_API int speo_generation_epoch_ex(const speo_segment *d_segs, int n_segs, in
 /* The island-resident epoch with the rotation on the tcgen05 tensor cores (one block per island,
  * P <= 256, D <= 64, the rotated Rastrigin 9 and sphere 31; other segments are flagged with
  * SPEO_DEVERR_BAD_SEGMENT and left unchanged). Each generation builds the same trial rows as
- * speo_generation (same Philox counters, bit-identical), evaluates them with the split-BF16
+ * speo_generation (same Philox counters, bit-identical), evaluates them with the split-FP16
  * product and epilogue of speo_evaluate_tc (bit-identical fitness per row) and selects with
  * strict `<`; `generations` such generations equal, row for row, speo_generation's trials +
  * speo_evaluate_tc + speo_select_rows repeated. Replaces DE_CUDA::Run's generation
@@ -519,7 +522,7 @@ SPEO_API int speo_surrogate_generation(speo_surrogate *s, const speo_segment *d_
 
 /* One DE generation with the rotation on the tensor cores, over a flat population of n_rows rows
  * (stride ld) planned with tiles of at most SPEO_TILE_TC rows: one trial per target
- * (speo_make_trials, k = 1: the trial draws use tags 1 | 1 << 8 and 2 | 1 << 8), tcgen05 split-BF16
+ * (speo_make_trials, k = 1: the trial draws use tags 1 | 1 << 8 and 2 | 1 << 8), tcgen05 split-FP16
  * evaluation (speo_evaluate_tc) into trial_fit, strict-`<` selection into (pop_out, fit_out)
  * (speo_select_rows); *d_gen advances by one. trial / trial_fit: caller scratch of n_rows rows. */
 SPEO_API int speo_generation_tc(const speo_segment *d_segs, const speo_work_item *d_items, int n_items,

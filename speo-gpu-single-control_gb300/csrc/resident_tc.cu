@@ -7,11 +7,12 @@
 // as k_island_epoch does, and each generation
 //   (1) draws donors and builds the trial rows on the CUDA cores (the same Philox counters and
 //       arithmetic as speo_generation: the trials are bit-identical);
-//   (2) splits y = x - o of every trial three ways into BF16 and stores it into tensor memory as
-//       the A operand (one thread per row and K half);
-//   (3) one thread issues the six split products per 16-wide K step for each 128-row tile
-//       (tcgen05.mma, M^T's three-way split resident in shared memory as the B operand) into an
-//       FP32 accumulator in tensor memory;
+//   (2) scales y = x - o of every trial by the row's power of two (its largest |y_j| into
+//       [2^14, 2^15)), splits it two ways into FP16 and stores it into tensor memory as the A
+//       operand (one thread per row and K half);
+//   (3) one thread issues the three split products per 16-wide K step for each 128-row tile
+//       (tcgen05.mma, the scaled M^T's two-way split resident in shared memory as the B operand)
+//       into an FP32 accumulator in tensor memory;
 //   (4) two threads per row read its z row back (tcgen05.ld, the column split of tcs::epi_split)
 //       and reduce the objective with the same packed arithmetic as speo_evaluate_tc, so the
 //       fitness of a row is bit-identical to that kernel's;
@@ -32,8 +33,8 @@ constexpr int kMaxPopE = 2 * tcs::kTileM;  // two 128-row MMA tiles
 constexpr int kMaxDimE = 64;               // K = N = round16(D) <= 64
 constexpr int kTmemAllocE = 512;           // whole SM: one block per SM
 constexpr int kAccColsE = 64;              // accumulator of tile t at columns 64 t
-constexpr int kAcolE = 128;                // A operand of tile t at 128 + 96 t (hi, mid, lo 32 apart)
-constexpr int kApartE = 32;                // columns of one A part (K <= 64: 32 BF16 pairs)
+constexpr int kAcolE = 128;                // A operand of tile t at 128 + 64 t (hi, lo 32 apart)
+constexpr int kApartE = 32;                // columns of one A part (K <= 64: 32 FP16 pairs)
 constexpr long long kWaitBudgetE = 2000000000LL;  // ~1 s at 2 GHz: a longer wait is a failure
 
 __device__ __forceinline__ float4 ld4e(const float *p) { return *reinterpret_cast<const float4 *>(p); }
@@ -53,10 +54,12 @@ __host__ __device__ inline int draw_gens_e(int Pmax)
 
 // Shared memory of one island (W = 32 Q floats per population row; trial rows XW = W + 4 apart so
 // that the conversion's one-row-per-thread reads are free of bank conflicts):
-//   B (three-way split M^T: hi, mid, lo) | pop[Pmax][W] | fit[Pmax (to 4)] | Xs[Pmax][XW] | sR[GB][Pmax][8] |
-//   sF[2][Pmax (to 4)] (the two column parts of each trial's fitness) | o[W]
+//   B (two-way split of M^T 2^k_M: hi, lo) | pop[Pmax][W] | fit[Pmax (to 4)] | Xs[Pmax][XW] |
+//   sR[GB][Pmax][8] | sF[2][Pmax (to 4)] (the two column parts of each trial's fitness; before
+//   the products, the largest |y| of each row's two K halves) | o[W] | rm[Pmax (to 4)] (each
+//   trial's epilogue scale)
 struct EpochTcLayout {
-    size_t b_bytes, off_pop, off_fit, off_xs, off_r, off_f, off_o, total;
+    size_t b_bytes, off_pop, off_fit, off_xs, off_r, off_f, off_o, off_rm, total;
 };
 
 __host__ __device__ inline EpochTcLayout epoch_tc_layout(int Q, int Pmax)
@@ -64,13 +67,14 @@ __host__ __device__ inline EpochTcLayout epoch_tc_layout(int Q, int Pmax)
     const int W = 32 * Q, XW = W + 4, Kmax = W;  // K = N <= W
     EpochTcLayout L;
     L.b_bytes = (size_t)Kmax * Kmax * 2;
-    L.off_pop = (3 * L.b_bytes + 1023) & ~(size_t)1023;
+    L.off_pop = (tcs::kParts * L.b_bytes + 1023) & ~(size_t)1023;
     L.off_fit = L.off_pop + (size_t)Pmax * W * 4;
     L.off_xs = L.off_fit + (size_t)up_to(Pmax, 4) * 4;
     L.off_r = L.off_xs + (size_t)Pmax * XW * 4;
     L.off_f = L.off_r + (size_t)draw_gens_e(Pmax) * Pmax * 8 * 4;
     L.off_o = L.off_f + 2 * (size_t)up_to(Pmax, 4) * 4;
-    L.total = L.off_o + (size_t)W * 4;
+    L.off_rm = L.off_o + (size_t)W * 4;
+    L.total = L.off_rm + (size_t)up_to(Pmax, 4) * 4;
     return L;
 }
 
@@ -143,6 +147,7 @@ __global__ void __launch_bounds__(kThreadsE, 1)
     int *sR = reinterpret_cast<int *>(smem_e + L.off_r);
     float *sF = reinterpret_cast<float *>(smem_e + L.off_f);
     float *so = reinterpret_cast<float *>(smem_e + L.off_o);
+    float *rm = reinterpret_cast<float *>(smem_e + L.off_rm);
     __shared__ float s_bf[kWarpsE];
     __shared__ int s_bi[kWarpsE];
     __shared__ __align__(8) uint64_t bar_mma;
@@ -181,8 +186,14 @@ __global__ void __launch_bounds__(kThreadsE, 1)
         }
         for (int r = tid; r < P; r += kThreadsE) fit[r] = fit_in[row0 + r];
         for (int k = tid; k < W; k += kThreadsE) so[k] = 0.f;
+        float bm = tcs::b_absmax(s, tid, kThreadsE);
+        for (int o = 16; o > 0; o >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+        if (lane == 0) s_bf[warp] = bm;
         __syncthreads();
-        tcs::build_b(s, Kp, b_hi, L.b_bytes, so, tid, kThreadsE);
+        bm = s_bf[0];
+        for (int w = 1; w < kWarpsE; ++w) bm = fmaxf(bm, s_bf[w]);
+        const int k_m = tcs::scale_exp(bm);
+        tcs::build_b(s, Kp, b_hi, L.b_bytes, so, tid, kThreadsE, tcs::pow2i(k_m));
         tc::fence_proxy_async_smem();  // B is read by the tensor cores (async proxy)
         tc::fence_before_sync();
         __syncthreads();
@@ -238,21 +249,26 @@ __global__ void __launch_bounds__(kThreadsE, 1)
             else
                 trial_rows<-1, W, XW>(pop, Xs, sRg, P, D, nch, best, st, F, thr, lb, ub, key, row0, gen, ok_bound);
             __syncthreads();
-            // (2) A operand: warp w converts rows of tile (w >> 2) & 1, lane quarter w & 3, K half w >> 3
+            // (2) A operand: warp w converts rows of tile (w >> 2) & 1, lane quarter w & 3, K half
+            // w >> 3; the row's scale from the largest |y| of its two halves (through sF)
             {
                 const int q = warp & 3, t = (warp >> 2) & 1, h = warp >> 3;
+                const int m = t * tcs::kTileM + q * 32 + lane;
+                const bool live = t < ntile && m < P;
+                const float *row = Xs + (size_t)(live ? m : 0) * XW;
+                const int s0 = h == 0 ? 0 : s_half, s1 = h == 0 ? s_half : S;
+                if (live) sF[h * Pf + m] = tcs::row_absmax(row, so, 16 * s0, 16 * s1, D, true);
+                __syncthreads();
                 if (t < ntile) {
-                    const int m = t * tcs::kTileM + q * 32 + lane;
-                    const bool live = m < P;
-                    const float *row = Xs + (size_t)(live ? m : 0) * XW;
-                    const int s0 = h == 0 ? 0 : s_half, s1 = h == 0 ? s_half : S;
-                    const uint32_t a = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(kAcolE + 3 * kApartE * t);
+                    const int k_row = live ? tcs::scale_exp(fmaxf(sF[m], sF[Pf + m])) : 0;
+                    if (live && h == 0) rm[m] = tcs::row_scale(scale, k_m, k_row);
+                    const float rs = tcs::pow2i(k_row);
+                    const uint32_t a = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(kAcolE + tcs::kParts * kApartE * t);
                     for (int k = s0; k < s1; ++k) {
-                        uint32_t hi[8], mid[8], lo[8];
-                        tcs::convert16(row, so, 16 * k, D, live, hi, mid, lo);
+                        uint32_t hi[8], lo[8];
+                        tcs::convert16(row, so, 16 * k, D, live, rs, hi, lo);
                         tc::tmem_st32x8(a + (uint32_t)(8 * k), hi);
-                        tc::tmem_st32x8(a + (uint32_t)(kApartE + 8 * k), mid);
-                        tc::tmem_st32x8(a + (uint32_t)(2 * kApartE + 8 * k), lo);
+                        tc::tmem_st32x8(a + (uint32_t)(kApartE + 8 * k), lo);
                     }
                     tc::tmem_wait_st();
                 }
@@ -263,7 +279,8 @@ __global__ void __launch_bounds__(kThreadsE, 1)
             if (tid == 0) {
                 tc::fence_after_sync();
                 for (int t = 0; t < ntile; ++t)
-                    tcs::issue_split_mma(tmem + (uint32_t)(kAccColsE * t), tmem + (uint32_t)(kAcolE + 3 * kApartE * t),
+                    tcs::issue_split_mma(tmem + (uint32_t)(kAccColsE * t),
+                                         tmem + (uint32_t)(kAcolE + tcs::kParts * kApartE * t),
                                          kApartE, b_hi, L.b_bytes, Kp, Kp, 0, S);
                 tc::mma_commit(&bar_mma);
             }
@@ -281,7 +298,7 @@ __global__ void __launch_bounds__(kThreadsE, 1)
                 const int m = te * tcs::kTileM + (warp & 3) * 32 + lane, h = tcs::epi_split(Kp);
                 const int c0 = he == 0 ? 0 : h, c1 = he == 0 ? (Kp < h ? Kp : h) : Kp;
                 const float f = c0 < c1 ? tcs::epilogue_row(tmem + (uint32_t)(kAccColsE * te), warp, D, c0, c1,
-                                                            s.func_id, scale)
+                                                            s.func_id, m < P ? rm[m] : 0.f)
                                         : 0.f;
                 if (m < P) sF[he * Pf + m] = f;
             }

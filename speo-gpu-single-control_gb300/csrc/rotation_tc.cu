@@ -4,15 +4,17 @@
 // 557-587), an FP64 16x16 shared-memory GEMM that writes the rotated population back to HBM,
 // with one pass per 128-row tile:
 //   TMA (cp.async.bulk.tensor.2d) brings the FP32 rows into shared memory (a ring of up to three
-//   stages); converter warps subtract o and split y = x - o three ways into BF16 (tc_split.cuh),
-//   each thread one row, and store the A operand straight into tensor memory (tcgen05.st,
-//   a ring of K-half slots); M (B operand, [N][K] = M[n][k]) is split the same way once per
-//   instance into shared memory; one thread issues, per 16-wide K step, the six products of
-//   tc_split.cuh (A from tensor memory) into an FP32 accumulator in tensor memory (M = 128 rows,
-//   N = D rounded up to 16, two accumulators): the fitness is as exact as the CUDA-core FP32
-//   rotation's. The tile is converted and multiplied in two K halves (one converter warp per lane
-//   quarter and half); eight warps read the rows back with tcgen05.ld (two per lane quarter, each
-//   half of the columns), apply the scale and the objective term and reduce each row in registers.
+//   stages); converter warps subtract o, find each row's largest |y| (the two threads of a row
+//   exchange their halves' maxima), scale y = x - o by the row's power of two and split it two ways
+//   into FP16 (tc_split.cuh), each thread one row, and store the A operand straight into tensor
+//   memory (tcgen05.st, a ring of K-half slots); M (B operand, [N][K] = M[n][k]) is scaled and
+//   split the same way once per instance into shared memory; one thread issues, per 16-wide K
+//   step, the three products of tc_split.cuh (A from tensor memory) into an FP32 accumulator in
+//   tensor memory (M = 128 rows, N = D rounded up to 16, two accumulators): the fitness is as exact
+//   as the CUDA-core FP32 rotation's. The tile is converted and multiplied in two K halves (one
+//   converter warp per lane quarter and half); eight warps read the rows back with tcgen05.ld (two
+//   per lane quarter, each half of the columns), apply the row's scale and the objective term and
+//   reduce each row in registers.
 // Nothing but the fitness is written. D <= 128.
 #include <cuda.h>
 
@@ -37,14 +39,17 @@ using tcs::epilogue_row;
 constexpr int kTmemCols = 128;   // widest accumulator (N <= 128)
 // Tensor memory (kmax = round16(largest D) columns per accumulator): accumulators b = 0, 1 at
 // columns kmax b (the products of tile i + 1 overlap the epilogue of tile i); then a ring of A
-// slots of kSlotCols columns from 2 kmax, as many as fit (up to 4: 4 at D <= 64, 3 at D <= 112, 2
-// above). K half h of tile i (half-index j = 2 i + h) goes to slot j % slots; a slot holds the
-// hi, mid and lo parts of one K half (<= 4 steps: 32 columns each) kApart = 32 columns apart.
-// With three or more slots a half is converted while the products of the previous half run.
+// slots of kSlotCols columns from 2 kmax (four at every D <= 128). K half h of tile i (half-index
+// j = 2 i + h) goes to slot j % 4; a slot holds the hi and lo parts of one K half (<= 4 steps: 32
+// columns each) kApart = 32 columns apart. A half is converted while the products of the
+// previous halves run.
 constexpr int kTmemAlloc = 512;
 constexpr int kApart = 32;
-constexpr int kSlotCols = 3 * kApart;
+constexpr int kSlotCols = tcs::kParts * kApart;
 constexpr int kMaxSlots = 4;
+// Every D <= kTmemCols gets four slots: the ring of four row-scale buffers (rmul, bar_rs) relies
+// on it (the converters of tile i + 4 pass the slot wait only after the epilogue of tile i).
+static_assert((kTmemAlloc - 2 * kTmemCols) / kSlotCols >= kMaxSlots, "four A slots at every D");
 __host__ __device__ __forceinline__ int a_slots(int kmax)
 {
     const int n = (kTmemAlloc - 2 * kmax) / kSlotCols;
@@ -64,10 +69,12 @@ struct TcLayout {
     int kmax;         // round16(max D)
     int box_x;        // staged row stride (floats)
     int nstage;       // 1 to kMaxStages
-    size_t stage_bytes, b_bytes, off_b, off_o, off_bar, off_psum, total;
+    size_t stage_bytes, b_bytes, off_b, off_o, off_bar, off_psum, off_pmax, off_rmul, total;
 };
 
-//   stage[nstage] | B hi, mid, lo | o | barriers | psum[2][kTileM]
+//   stage[nstage] | B hi, lo | o | barriers | psum[2][kTileM] | pmax[2][2][kTileM] | rmul[4][kTileM]
+// pmax[i % 2][h][m]: the largest |y| of row m's K half h in tile i; rmul[i % 4][m]: the objective's
+// scale times 2^-(k_row + k_M) of row m in tile i (written by the converters, read by the epilogue).
 __host__ __device__ inline TcLayout tc_layout(int dim_hi, int ld, int nstage)
 {
     TcLayout L;
@@ -77,10 +84,12 @@ __host__ __device__ inline TcLayout tc_layout(int dim_hi, int ld, int nstage)
     L.stage_bytes = (size_t)kTileM * L.box_x * 4;
     L.b_bytes = (size_t)L.kmax * L.kmax * 2;
     L.off_b = ((L.stage_bytes * nstage) + 1023) & ~(size_t)1023;
-    L.off_o = L.off_b + 3 * L.b_bytes;
+    L.off_o = L.off_b + tcs::kParts * L.b_bytes;
     L.off_bar = (L.off_o + (size_t)L.kmax * 4 + 15) & ~(size_t)15;
     L.off_psum = L.off_bar + 256;
-    L.total = L.off_psum + 2 * kTileM * 4;
+    L.off_pmax = L.off_psum + 2 * kTileM * 4;
+    L.off_rmul = L.off_pmax + 4 * kTileM * 4;
+    L.total = L.off_rmul + 4 * kTileM * 4;
     return L;
 }
 
@@ -198,11 +207,14 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
     uint8_t *b_hi = smem + L.off_b;
     float *so = reinterpret_cast<float *>(smem + L.off_o);
     float *psum = reinterpret_cast<float *>(smem + L.off_psum);
+    float *pmax = reinterpret_cast<float *>(smem + L.off_pmax);
+    float *rmul = reinterpret_cast<float *>(smem + L.off_rmul);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
     uint64_t *bar_tma = bars, *bar_mma = bars + 3, *bar_epi = bars + 5, *bar_afull = bars + 7, *bar_afree = bars + 11,
-             *bar_fin = bars + 15;
+             *bar_fin = bars + 15, *bar_rs = bars + 18;
     volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 16);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 17);
+    float *red = reinterpret_cast<float *>(bars + 22);  // 8 floats: the converter warps' |M| maxima
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (warp == 0) {
@@ -220,6 +232,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             tc::mbar_init(&bar_afree[k], 1);
         }
         tc::mbar_init(bar_fin, 1);
+        for (int k = 0; k < 4; ++k) tc::mbar_init(&bar_rs[k], 128);
         *abort_flag = 0;
         tc::fence_mbar_init();
         tc::prefetch_tensormap(&xmap);
@@ -302,15 +315,20 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
         TileInfo nxt = tile_info(a, item_of(1));
         speo_work_item it_nn = item_of(2);
         const float *c_rot = nullptr, *c_shift = nullptr;
-        int c_dim = -1, c_ldrot = -1;
+        int c_dim = -1, c_ldrot = -1, c_km = 0;
         for (int i = 0; i < my_items; ++i) {
             const speo_work_item it_n3 = item_of(i + 3);
             const TileInfo nn = tile_info(a, it_nn);
             const int sidx = i % ns;
             const int D = cur.D, Kp = round16(D), S = Kp / 16, s_half = (S + 1) / 2;
+            const int s0 = ch == 0 ? 0 : s_half, s1 = ch == 0 ? s_half : S;
+            const float *row = stage[sidx] + (size_t)m * L.box_x;
+            const bool live = cur.ok && m < cur.count;
+            float *pm = pmax + (i & 1) * 2 * kTileM;  // read by the row's other thread after barrier 1
             bool to = !tc::mbar_wait_sleep(&bar_tma[sidx], (uint32_t)((i / ns) & 1), kWaitBudget);
             const bool new_b = cur.ok && (cur.rot != c_rot || cur.shift != c_shift || D != c_dim ||
                                           cur.ld_rot != c_ldrot);
+            if (!new_b) pm[ch * kTileM + m] = tcs::row_absmax(row, so, 16 * s0, 16 * s1, D, live);
             // B and o are read by every product of the previous tile: rebuild them once those are done
             if (new_b && i >= 1)
                 to |= !tc::mbar_wait_sleep(&bar_mma[(i - 1) & 1], (uint32_t)(((i - 1) >> 1) & 1), kWaitBudget);
@@ -320,26 +338,39 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             if (new_b) {
                 speo_segment sb;
                 sb.dim = D; sb.rot = cur.rot; sb.shift = cur.shift; sb.ld_rot = cur.ld_rot;
-                build_b(sb, Kp, b_hi, L.b_bytes, so, ct, kCvtThreads);
+                float bm = tcs::b_absmax(sb, ct, kCvtThreads);
+                for (int o = 16; o > 0; o >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+                if (lane == 0) red[warp - kEpiThreads / 32] = bm;
+                tc::named_bar_sync(1, kCvtThreads);
+                bm = red[0];
+                for (int w = 1; w < kCvtThreads / 32; ++w) bm = fmaxf(bm, red[w]);
+                c_km = tcs::scale_exp(bm);
+                build_b(sb, Kp, b_hi, L.b_bytes, so, ct, kCvtThreads, tcs::pow2i(c_km));
                 c_rot = cur.rot; c_shift = cur.shift; c_dim = D; c_ldrot = cur.ld_rot;
                 tc::fence_proxy_async_smem();
+                tc::named_bar_sync(1, kCvtThreads);  // B, o and red are complete
+                pm[ch * kTileM + m] = tcs::row_absmax(row, so, 16 * s0, 16 * s1, D, live);
                 tc::named_bar_sync(1, kCvtThreads);
             }
             if (!cur.ok && ct == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+            const int k_row = tcs::scale_exp(fmaxf(pm[m], pm[kTileM + m]));
             // the slot of this K half was last read by the products of the half nslot half-steps back
             const int sl = slot_of(i, ch), u = use_of(i, ch);
             bool ok = u < 1 || tc::mbar_wait_sleep(&bar_afree[sl], (uint32_t)((u - 1) & 1), kWaitBudget);
             if (__all_sync(0xffffffffu, ok)) {
-                const int s0 = ch == 0 ? 0 : s_half, s1 = ch == 0 ? s_half : S;
-                const float *row = stage[sidx] + (size_t)m * L.box_x;
-                const bool live = cur.ok && m < cur.count;
+                if (ch == 0) {
+                    // the epilogue of tile i - 4, the last reader of rmul[i % 4], finished before
+                    // the products that freed this slot were issued
+                    rmul[(i & 3) * kTileM + m] = tcs::row_scale(func_scale(cur.func), c_km, k_row);
+                    tc::mbar_arrive(&bar_rs[i & 3]);
+                }
+                const float rs = tcs::pow2i(k_row);
                 for (int st = s0; st < s1; ++st) {
-                    uint32_t hi[8], mid[8], lo[8];
-                    convert16(row, so, 16 * st, D, live, hi, mid, lo);
+                    uint32_t hi[8], lo[8];
+                    convert16(row, so, 16 * st, D, live, rs, hi, lo);
                     const uint32_t col = slot_col(sl) + lane_off + (uint32_t)(8 * (st - s0));
                     tc::tmem_st32x8(col, hi);
-                    tc::tmem_st32x8(col + (uint32_t)kApart, mid);
-                    tc::tmem_st32x8(col + (uint32_t)(2 * kApart), lo);
+                    tc::tmem_st32x8(col + (uint32_t)kApart, lo);
                 }
                 tc::tmem_wait_st();
                 tc::fence_before_sync();
@@ -363,11 +394,13 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             if (tc::named_bar_or(2 + q, 64, *abort_flag != 0)) break;
             const speo_work_item it_nn = item_of(i + 2);
             const TileInfo nxt = tile_info(a, it_next);
-            const bool got = tc::mbar_wait_sleep(&bar_mma[i & 1], (uint32_t)((i >> 1) & 1), kWaitBudget);
+            const bool got = tc::mbar_wait_sleep(&bar_mma[i & 1], (uint32_t)((i >> 1) & 1), kWaitBudget) &&
+                             tc::mbar_wait_sleep(&bar_rs[i & 3], (uint32_t)((i >> 2) & 1), kWaitBudget);
             if (tc::named_bar_or(2 + q, 64, !got)) { *abort_flag = 1; break; }
             tc::fence_after_sync();
             const uint32_t acc_t = tmem + (uint32_t)((i & 1) * L.kmax);
             const int Np = round16(cur.D), m = q * 32 + lane;
+            const float rsc = rmul[(i & 3) * kTileM + m];
             float f = 0.f;
             bool writer = ch == 0;
             if (func_sum_form(cur.func)) {
@@ -375,13 +408,13 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
                 // (tcs::epi_split); the second warp's partial sums meet the first's through psum[i % 2]
                 const int h = tcs::epi_split(Np);
                 const int c0 = ch == 0 ? 0 : h, c1 = ch == 0 ? (Np < h ? Np : h) : Np;
-                f = c0 < c1 ? epilogue_row(acc_t, warp, cur.D, c0, c1, cur.func, func_scale(cur.func)) : 0.f;
+                f = c0 < c1 ? epilogue_row(acc_t, warp, cur.D, c0, c1, cur.func, rsc) : 0.f;
                 float *ps = psum + (i & 1) * kTileM;
                 if (ch == 1) ps[m] = f;
                 tc::named_bar_sync(2 + q, 64);
                 if (ch == 0) f += ps[m];
             } else if (ch == 0) {
-                f = epilogue_row_generic(acc_t, warp, cur.D, Np, cur.func, func_scale(cur.func));
+                f = epilogue_row_generic(acc_t, warp, cur.D, Np, cur.func, rsc);
             }
             if (writer && cur.ok && m < cur.count) a.fit[cur.row + m] = f;
             tc::fence_before_sync();

@@ -1,7 +1,7 @@
 // tcgen05.cuh -- inline-PTX wrappers for the sm_100-family tensor-core path used by this
 // library: mbarriers with bounded waits, TMA (cp.async.bulk.tensor) loads, tensor-memory
-// allocation, tcgen05.mma (kind::f16, BF16 inputs, FP32 accumulation; A from shared or tensor
-// memory), commit, tcgen05.ld and tcgen05.st.
+// allocation, tcgen05.mma (kind::f16, BF16 or FP16 inputs, FP32 accumulation; A from shared or
+// tensor memory), commit, tcgen05.ld and tcgen05.st.
 //
 // Shared-memory operand layout: K-major, no swizzle, in 8x8 "core matrices" of 16-bit
 // elements (8 rows x 16 bytes, 128 contiguous bytes). Element (r, k) of an R x Kp operand sits at
@@ -150,6 +150,13 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N)
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// The same with A = B = FP16 (bits 7-9, 10-12 = 0). Both operands of one product are always
+// of the type the descriptor names.
+__host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N)
+{
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
 // D[tmem] (+)= A[smem] * B[smem]^T, issued by one thread.
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate)
 {
@@ -161,7 +168,8 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
         : "memory");
 }
 // D[tmem] (+)= A[tmem] * B[smem]^T, issued by one thread. A (M = 128 rows) sits in lanes 0-127,
-// one row per lane, two BF16 per 32-bit column (even k in the low half), K = 16 in 8 columns.
+// one row per lane, two 16-bit elements (BF16 or FP16, as idesc says) per 32-bit column (even k in
+// the low half), K = 16 in 8 columns.
 __device__ __forceinline__ void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
                                             uint32_t accumulate)
 {
@@ -198,45 +206,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 __host__ __device__ __forceinline__ uint32_t kmajor_offset(int r, int k, int Kp)
 {
     return (uint32_t)(((r >> 3) * (Kp >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
-}
-
-// BF16 hi/lo split of 8 floats: v = hi + lo + O(2^-16 |v|). Packs 8 bf16 into a uint4
-// (element 2i in the low half of word i), two elements per cvt.rn.bf16x2.f32.
-__device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo)
-{
-    uint32_t h[4], l[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const __nv_bfloat162 hh = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-        const float2 hf = __bfloat1622float2(hh);
-        const __nv_bfloat162 ll = __floats2bfloat162_rn(v[2 * i] - hf.x, v[2 * i + 1] - hf.y);
-        h[i] = *reinterpret_cast<const uint32_t *>(&hh);
-        l[i] = *reinterpret_cast<const uint32_t *>(&ll);
-    }
-    hi = make_uint4(h[0], h[1], h[2], h[3]);
-    lo = make_uint4(l[0], l[1], l[2], l[3]);
-}
-
-// BF16 three-way split of 8 floats: v = hi + mid + lo + O(2^-27 |v|) (v - hi and v - hi - mid
-// are exact in binary32). Packs as split8.
-__device__ __forceinline__ void split8x3(const float (&v)[8], uint4 &hi, uint4 &mid, uint4 &lo)
-{
-    uint32_t h[4], m[4], l[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const __nv_bfloat162 hh = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
-        const float2 hf = __bfloat1622float2(hh);
-        const float r0 = v[2 * i] - hf.x, r1 = v[2 * i + 1] - hf.y;
-        const __nv_bfloat162 mm = __floats2bfloat162_rn(r0, r1);
-        const float2 mf = __bfloat1622float2(mm);
-        const __nv_bfloat162 ll = __floats2bfloat162_rn(r0 - mf.x, r1 - mf.y);
-        h[i] = *reinterpret_cast<const uint32_t *>(&hh);
-        m[i] = *reinterpret_cast<const uint32_t *>(&mm);
-        l[i] = *reinterpret_cast<const uint32_t *>(&ll);
-    }
-    hi = make_uint4(h[0], h[1], h[2], h[3]);
-    mid = make_uint4(m[0], m[1], m[2], m[3]);
-    lo = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
 // Warp-collective: 32 TMEM lanes x 32 consecutive 32-bit columns (no wait).

@@ -149,7 +149,7 @@ class SegmentTable:
 
     def evaluate(self, which: int | None = None, use_tc: bool = False, out: torch.Tensor | None = None):
         """Fitness of population buffer `which` (default: current) into `out` (default: its own
-        fitness buffer). use_tc selects the tcgen05 split-BF16 kernel (tiles of 128 rows)."""
+        fitness buffer). use_tc selects the tcgen05 split-FP16 kernel (tiles of 128 rows)."""
         L = _lib.load()
         w = self.cur if which is None else which
         fit = self.fit[w] if out is None else out
@@ -207,7 +207,7 @@ class SegmentTable:
 
     def tc_generation(self, trial: torch.Tensor, trial_fit: torch.Tensor):
         """One generation with the rotation on the tensor cores: one DE trial per target
-        (speo_make_trials, k = 1), tcgen05 split-BF16 evaluation, strict-`<` selection. The table must
+        (speo_make_trials, k = 1), tcgen05 split-FP16 evaluation, strict-`<` selection. The table must
         be planned with tiles of at most 128 rows."""
         L = _lib.load()
         a, b = self.cur, 1 - self.cur

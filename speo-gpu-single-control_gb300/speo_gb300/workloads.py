@@ -3,7 +3,7 @@
   config 1  island model: 64 islands x P=100, D=30, rotated Rastrigin, ring best-5 -> worst-5
             every 50 generations
   config 2  precision: 256 islands x P=128, D=100, per island a seeded choice of rotated sphere /
-            rotated Rastrigin with its own o and M; tensor-core split-BF16 evaluation, FP64 re-check
+            rotated Rastrigin with its own o and M; tensor-core split-FP16 evaluation, FP64 re-check
   config 3  batched uneven runs: 1024 independent runs, D ~ U{10,30,50,100}, P ~ U[50,200],
             each with its own o, M and objective; one launch per generation
   config 4  learned surrogate: 128 islands x P=256, D=50, rotated Rastrigin; MLP 50-256-256-1

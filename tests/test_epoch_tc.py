@@ -2,7 +2,7 @@
 
 Its generations must equal, row for row and bit for bit, the composition of the entry points it
 fuses: the trial rows of speo_generation (Philox draws, bit-exact against the oracle), their
-split-BF16 tensor-core fitness from speo_evaluate_tc, and strict-`<` selection
+split-FP16 tensor-core fitness from speo_evaluate_tc, and strict-`<` selection
 (kernel_DE_CUDA.cu:312). Every generation's tensor-core fitness is also held to the FP32 bar
 against the FP64 oracle (1e-5 relative), and the trials of the first generation to the oracle's
 restatement of the reference's DE operator.

@@ -206,11 +206,13 @@ def test_de_run_matches_the_dropin_loop(lib, cuda, f64, gens, pinned, history, P
     assert np.array_equal(ca, cb) and np.array_equal(cfa, cfb) and np.array_equal(ba, bb)
 
 
+# P = 5000 spans several batches of 2048 rows per block; D = 1 and 3 have no 16-byte bulk part
+# in FP32 (rows copied element by element), D = 30 a ragged tail, D = 100 and 256 none.
+@pytest.mark.parametrize("P,D", [(100, 30), (5000, 1), (5000, 3), (5000, 4), (5000, 30), (5000, 100), (777, 256)])
 @pytest.mark.parametrize("f64", [False, True])
-def test_dropin_select_matches_oracle(lib, oracle, cuda, f64):
+def test_dropin_select_matches_oracle(lib, oracle, cuda, f64, P, D):
     import torch
 
-    P, D = 100, 30
     d = DropIn(lib, cuda, P, D, 1, f64)
     rng = np.random.default_rng(4)
     pop = rng.uniform(-100, 100, (P, d.ld)).astype(d.np_dt)
@@ -593,9 +595,9 @@ def test_no_device_error_flags(lib, cuda):
 
 
 # ---------------------------------------------------------------------------------------------
-# tcgen05 evaluation (y split into BF16 hi + lo, M into hi + mid + lo, five products, FP32
-# accumulation): each rotated coordinate keeps ~2^-18 relative error per term (the y split and
-# the dropped y_lo M_lo), so the rotated Rastrigin and sphere are held to the FP32 bar of 1e-5.
+# tcgen05 evaluation (each row y and M scaled by powers of two and split two ways into FP16,
+# three products, FP32 accumulation): each rotated coordinate keeps ~2^-22 relative error per term
+# (the dropped y_lo M_lo), so the rotated Rastrigin and sphere are held to the FP32 bar of 1e-5.
 # ---------------------------------------------------------------------------------------------
 
 
@@ -630,13 +632,44 @@ def test_evaluate_tc_matches_oracle(oracle, cuda, layout):
         worst = max(worst, float(np.max(np.where(ref > 1e-3, rel, 0))))
         _assert_fitness(got[r], ref, rtol=FIT_RTOL_F32, atol=FIT_ATOL_F32)
     assert got[0] == 0.0
-    print(f"max relative error of the split-BF16 tensor-core fitness: {worst:.2e}")
+    print(f"max relative error of the split-FP16 tensor-core fitness: {worst:.2e}")
+
+
+@pytest.mark.parametrize("func", [9, 31])
+def test_evaluate_tc_row_scaling_near_optimum(cuda, func):
+    """Rows at x = o + d with |d| from 1e2 down to 1e-6 (and a row of mixed magnitudes): each row's
+    power-of-two scale keeps the FP16 parts of small y normal, so the tensor-core fitness agrees with
+    the CUDA-core FP32 evaluation of the same rows (the same y = x - o in FP32) to the FP32 bar."""
+    import torch
+    from speo_gb300 import _lib
+
+    P, D = 128, 100
+    tab = _table(cuda, [(P, D, func, 4)], n_inst=1, tile_rows=_lib.TILE_TC)
+    tab_s = _table(cuda, [(P, D, func, 4)], n_inst=1, tile_rows=_lib.TILE_SIMT)
+    tab.init_population()
+    s = tab.oracle_segments()[0]
+    rng = np.random.default_rng(17)
+    pop = tab.pop[tab.cur].cpu().numpy()
+    mags = 10.0 ** rng.uniform(-6, 2, P)
+    for r in range(P):
+        pop[r, :D] = (s["o"] + mags[r] * rng.standard_normal(D)).astype(np.float32)
+    pop[0, :D] = (s["o"] + np.where(np.arange(D) % 2 == 0, 1e-5, 10.0)).astype(np.float32)
+    tab.pop[tab.cur].copy_(torch.from_numpy(pop))
+    tab_s.pop[tab_s.cur].copy_(torch.from_numpy(pop))
+    tc_fit = torch.full_like(tab.fit[0], float("nan"))
+    simt_fit = torch.full_like(tab_s.fit[0], float("nan"))
+    tab.evaluate(use_tc=True, out=tc_fit)
+    tab_s.evaluate(use_tc=False, out=simt_fit)
+    torch.cuda.synchronize()
+    a, b = tc_fit.cpu().numpy()[:P], simt_fit.cpu().numpy()[:P]
+    assert np.all(np.isfinite(a))
+    np.testing.assert_allclose(a, b, rtol=FIT_RTOL_F32, atol=0)
 
 
 @pytest.mark.parametrize("layout", [[(128, 100, 9, 4)] * 3 + [(100, 30, 31, 6)], [(200, 50, 4, 4), (70, 64, 13, 2)]])
 def test_generation_tc_matches_oracle(oracle, cuda, layout):
     """speo_generation_tc: one trial per target (the draws of speo_make_trials with k = 1),
-    tcgen05 split-BF16 evaluation, strict-`<` selection, generation counter advanced; two
+    tcgen05 split-FP16 evaluation, strict-`<` selection, generation counter advanced; two
     generations. Selection decisions are checked against the FP64 oracle's fitness wherever the
     trial and the parent differ by more than the fitness bar."""
     import torch
