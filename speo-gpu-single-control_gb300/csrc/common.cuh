@@ -102,7 +102,11 @@ __device__ __forceinline__ bool draw_donors(IdxStream &s, int S, int r[5])
 template <typename T>
 __device__ __forceinline__ T check_bound(T v, T lb, T ub, bool &ok)
 {
-    int it = 0;
+    // the loop's first pass as selects (a value in bounds passes through unchanged), the rest
+    // only for a value still outside after one reflection each way
+    v = (v < lb) ? lb + (lb - v) : v;
+    v = (v > ub) ? ub - (v - ub) : v;
+    int it = 1;
     while ((v < lb) || (v > ub)) {
         if (v < lb) v = lb + (lb - v);
         if (v > ub) v = ub - (v - ub);

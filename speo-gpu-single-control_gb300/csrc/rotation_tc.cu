@@ -4,17 +4,16 @@
 // 557-587), an FP64 16x16 shared-memory GEMM that writes the rotated population back to HBM,
 // with one pass per 128-row tile:
 //   TMA (cp.async.bulk.tensor.2d) brings the FP32 rows into shared memory (a ring of up to three
-//   stages); converter warps subtract o, find each row's largest |y| (the two threads of a row
-//   exchange their halves' maxima), scale y = x - o by the row's power of two and split it two ways
-//   into FP16 (tc_split.cuh), each thread one row, and store the A operand straight into tensor
-//   memory (tcgen05.st, a ring of K-half slots); M (B operand, [N][K] = M[n][k]) is scaled and
-//   split the same way once per instance into shared memory; one thread issues, per 16-wide K
-//   step, the three products of tc_split.cuh (A from tensor memory) into an FP32 accumulator in
-//   tensor memory (M = 128 rows, N = D rounded up to 16, two accumulators): the fitness is as exact
-//   as the CUDA-core FP32 rotation's. The tile is converted and multiplied in two K halves (one
-//   converter warp per lane quarter and half); eight warps read the rows back with tcgen05.ld (two
-//   per lane quarter, each half of the columns), apply the row's scale and the objective term and
-//   reduce each row in registers.
+//   stages); two groups of four converter warps take alternate tiles, a thread per row: it
+//   subtracts o, finds the row's largest |y|, scales y = x - o by the row's power of two and splits
+//   it two ways into FP16 (tc_split.cuh), and stores the A operand straight into tensor memory
+//   (tcgen05.st, a ring of K-half slots); M (B operand, [N][K] = M[n][k]) is scaled and split the
+//   same way once per instance into shared memory; one thread issues, per 16-wide K step, the three
+//   products of tc_split.cuh (A from tensor memory) into an FP32 accumulator in tensor memory
+//   (M = 128 rows, N = D rounded up to 16, two accumulators): the fitness is as exact as the
+//   CUDA-core FP32 rotation's. Each K half is handed to the products as soon as it is converted;
+//   eight warps read the rows back with tcgen05.ld (two per lane quarter, each half of the
+//   columns), apply the row's scale and the objective term and reduce each row in registers.
 // Nothing but the fitness is written. D <= 128.
 #include <cuda.h>
 
@@ -69,12 +68,13 @@ struct TcLayout {
     int kmax;         // round16(max D)
     int box_x;        // staged row stride (floats)
     int nstage;       // 1 to kMaxStages
-    size_t stage_bytes, b_bytes, off_b, off_o, off_bar, off_psum, off_pmax, off_rmul, total;
+    size_t stage_bytes, b_bytes, off_b, off_o, off_bar, off_psum, off_rmul, total;
 };
 
-//   stage[nstage] | B hi, lo | o | barriers | psum[2][kTileM] | pmax[2][2][kTileM] | rmul[4][kTileM]
-// pmax[i % 2][h][m]: the largest |y| of row m's K half h in tile i; rmul[i % 4][m]: the objective's
-// scale times 2^-(k_row + k_M) of row m in tile i (written by the converters, read by the epilogue).
+//   stage[nstage] | B hi, lo | o[2][kmax] (each converter group's copy) | barriers | psum[2][kTileM] |
+//   rmul[4][kTileM]
+// rmul[i % 4][m]: the objective's scale times 2^-(k_row + k_M) of row m in tile i (written by the
+// converters, read by the epilogue).
 __host__ __device__ inline TcLayout tc_layout(int dim_hi, int ld, int nstage)
 {
     TcLayout L;
@@ -85,10 +85,9 @@ __host__ __device__ inline TcLayout tc_layout(int dim_hi, int ld, int nstage)
     L.b_bytes = (size_t)L.kmax * L.kmax * 2;
     L.off_b = ((L.stage_bytes * nstage) + 1023) & ~(size_t)1023;
     L.off_o = L.off_b + tcs::kParts * L.b_bytes;
-    L.off_bar = (L.off_o + (size_t)L.kmax * 4 + 15) & ~(size_t)15;
+    L.off_bar = (L.off_o + 2 * (size_t)L.kmax * 4 + 15) & ~(size_t)15;
     L.off_psum = L.off_bar + 256;
-    L.off_pmax = L.off_psum + 2 * kTileM * 4;
-    L.off_rmul = L.off_pmax + 4 * kTileM * 4;
+    L.off_rmul = L.off_psum + 2 * kTileM * 4;
     L.total = L.off_rmul + 4 * kTileM * 4;
     return L;
 }
@@ -164,15 +163,19 @@ __device__ __forceinline__ bool tc_tile_ok(const speo_work_item &it, const speo_
            s.row0 + it.first + it.count <= a.n_rows;
 }
 
-// Warp roles: warps 8..15 convert tile i into the A buffer i % 2 in tensor memory (warp 8 + q + 4h:
-// lane quarter q, K half h); warp 16 issues the TMA loads and (one thread) the MMAs of each half
-// as soon as it is converted and the accumulator is free; warps 0..7 run the epilogue.
+// Warp roles: warps 8..11 convert the even tiles and warps 12..15 the odd ones into the A slots in
+// tensor memory (warp 8 + q + 4g: lane quarter q, group g; each group with its own copy of o and
+// named barrier 1 or 6); warp 16 issues the TMA loads and (one thread) the MMAs of each half as
+// soon as it is converted and the accumulator is free; warps 0..7 run the epilogue. B is rebuilt
+// by the group whose tile is the first of a new instance, once the previous tile's products are
+// done.
 //   bar_tma[s]      stage s holds the rows of its tile                 (TMA transaction bytes)
 //   bar_afull[s]    slot s holds its K half (and its stage rows are read)       (128 arrivals)
 //   bar_afree[s]    the products reading slot s are done                        (tcgen05.commit)
 //   bar_mma[b]      accumulator b holds a finished product                      (tcgen05.commit)
 //   bar_epi[b]      the epilogue is done reading accumulator b                  (256 arrivals)
 //   bar_fin         every product this block issued is done           (tcgen05.commit, on abort)
+//   bar_rs[i % 4]   rmul of tile i is written (its converter group)                (128 arrivals)
 // Everything a role needs about one tile is loaded ahead of use (register prefetch of the work
 // items and segments of the next tiles).
 struct TileInfo {
@@ -207,14 +210,13 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
     uint8_t *b_hi = smem + L.off_b;
     float *so = reinterpret_cast<float *>(smem + L.off_o);
     float *psum = reinterpret_cast<float *>(smem + L.off_psum);
-    float *pmax = reinterpret_cast<float *>(smem + L.off_pmax);
     float *rmul = reinterpret_cast<float *>(smem + L.off_rmul);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
     uint64_t *bar_tma = bars, *bar_mma = bars + 3, *bar_epi = bars + 5, *bar_afull = bars + 7, *bar_afree = bars + 11,
              *bar_fin = bars + 15, *bar_rs = bars + 18;
     volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 16);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 17);
-    float *red = reinterpret_cast<float *>(bars + 22);  // 8 floats: the converter warps' |M| maxima
+    float *red = reinterpret_cast<float *>(bars + 22);  // 2 x 4 floats: each converter group's |M| maxima
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (warp == 0) {
@@ -307,67 +309,74 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             it_q = it_q_next;
         }
     } else if (warp >= kEpiThreads / 32) {
-        // ---- conversion: thread = row 32 q + lane, K half ch -------------------------------------
-        const int ct = tid - kEpiThreads, q = warp & 3, ch = (warp - kEpiThreads / 32) >> 2;
+        // ---- conversion: group g = tiles g, g + 2, ...; thread = row 32 q + lane, both K halves ----
+        const int g = (warp - kEpiThreads / 32) >> 2, q = warp & 3, gt = q * 32 + lane;
+        const int gbar = g == 0 ? 1 : 6;  // the group's named barrier (128 threads)
         const int m = q * 32 + lane;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-        TileInfo cur = tile_info(a, item_of(0));
-        TileInfo nxt = tile_info(a, item_of(1));
-        speo_work_item it_nn = item_of(2);
-        const float *c_rot = nullptr, *c_shift = nullptr;
-        int c_dim = -1, c_ldrot = -1, c_km = 0;
-        for (int i = 0; i < my_items; ++i) {
-            const speo_work_item it_n3 = item_of(i + 3);
-            const TileInfo nn = tile_info(a, it_nn);
+        float *so_g = so + g * L.kmax;
+        float *red_g = red + 4 * g;
+        const float *g_rot = nullptr, *g_shift = nullptr;
+        int g_dim = -1, g_ldrot = -1, g_km = 0;
+        auto same_inst = [](const TileInfo &x, const TileInfo &y) {
+            return x.rot == y.rot && x.shift == y.shift && x.D == y.D && x.ld_rot == y.ld_rot;
+        };
+        TileInfo prv = tile_info(a, item_of(g > 0 ? g - 1 : 0)), cur = tile_info(a, item_of(g));
+        for (int i = g; i < my_items; i += 2) {
+            const TileInfo prv_n = tile_info(a, item_of(i + 1)), cur_n = tile_info(a, item_of(i + 2));
             const int sidx = i % ns;
             const int D = cur.D, Kp = round16(D), S = Kp / 16, s_half = (S + 1) / 2;
-            const int s0 = ch == 0 ? 0 : s_half, s1 = ch == 0 ? s_half : S;
             const float *row = stage[sidx] + (size_t)m * L.box_x;
             const bool live = cur.ok && m < cur.count;
-            float *pm = pmax + (i & 1) * 2 * kTileM;  // read by the row's other thread after barrier 1
             bool to = !tc::mbar_wait_sleep(&bar_tma[sidx], (uint32_t)((i / ns) & 1), kWaitBudget);
-            const bool new_b = cur.ok && (cur.rot != c_rot || cur.shift != c_shift || D != c_dim ||
-                                          cur.ld_rot != c_ldrot);
-            if (!new_b) pm[ch * kTileM + m] = tcs::row_absmax(row, so, 16 * s0, 16 * s1, D, live);
-            // B and o are read by every product of the previous tile: rebuild them once those are done
+            const bool new_inst = cur.ok && (cur.rot != g_rot || cur.shift != g_shift || D != g_dim ||
+                                             cur.ld_rot != g_ldrot);
+            // B holds the instance of tile i - 1 when that tile was valid
+            const bool new_b = cur.ok && (i == 0 || !prv.ok || !same_inst(cur, prv));
+            // B is read by every product of the previous tile: rebuild it once those are done
             if (new_b && i >= 1)
                 to |= !tc::mbar_wait_sleep(&bar_mma[(i - 1) & 1], (uint32_t)(((i - 1) >> 1) & 1), kWaitBudget);
-            // the group's decision to stop is reduced over all converters, so that none waits at
-            // named barrier 1 for one that left
-            if (tc::named_bar_or(1, kCvtThreads, to || *abort_flag != 0)) { *abort_flag = 1; break; }
-            if (new_b) {
+            // the group's decision to stop is reduced over its threads, so that none waits at its
+            // named barrier for one that left
+            if (tc::named_bar_or(gbar, 128, to || *abort_flag != 0)) { *abort_flag = 1; break; }
+            if (new_inst || new_b) {
                 speo_segment sb;
                 sb.dim = D; sb.rot = cur.rot; sb.shift = cur.shift; sb.ld_rot = cur.ld_rot;
-                float bm = tcs::b_absmax(sb, ct, kCvtThreads);
-                for (int o = 16; o > 0; o >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
-                if (lane == 0) red[warp - kEpiThreads / 32] = bm;
-                tc::named_bar_sync(1, kCvtThreads);
-                bm = red[0];
-                for (int w = 1; w < kCvtThreads / 32; ++w) bm = fmaxf(bm, red[w]);
-                c_km = tcs::scale_exp(bm);
-                build_b(sb, Kp, b_hi, L.b_bytes, so, ct, kCvtThreads, tcs::pow2i(c_km));
-                c_rot = cur.rot; c_shift = cur.shift; c_dim = D; c_ldrot = cur.ld_rot;
-                tc::fence_proxy_async_smem();
-                tc::named_bar_sync(1, kCvtThreads);  // B, o and red are complete
-                pm[ch * kTileM + m] = tcs::row_absmax(row, so, 16 * s0, 16 * s1, D, live);
-                tc::named_bar_sync(1, kCvtThreads);
+                if (new_inst) {
+                    float bm = tcs::b_absmax(sb, gt, 128);
+                    for (int o = 16; o > 0; o >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+                    if (lane == 0) red_g[q] = bm;
+                    for (int k = gt; k < Kp; k += 128) so_g[k] = k < D ? cur.shift[k] : 0.f;
+                    tc::named_bar_sync(gbar, 128);
+                    bm = fmaxf(fmaxf(red_g[0], red_g[1]), fmaxf(red_g[2], red_g[3]));
+                    g_km = tcs::scale_exp(bm);
+                    g_rot = cur.rot; g_shift = cur.shift; g_dim = D; g_ldrot = cur.ld_rot;
+                }
+                if (new_b) {
+                    build_b(sb, Kp, b_hi, L.b_bytes, so_g, gt, 128, tcs::pow2i(g_km));
+                    tc::fence_proxy_async_smem();
+                }
+                tc::named_bar_sync(gbar, 128);  // B, o and red are complete
             }
-            if (!cur.ok && ct == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
-            const int k_row = tcs::scale_exp(fmaxf(pm[m], pm[kTileM + m]));
-            // the slot of this K half was last read by the products of the half nslot half-steps back
-            const int sl = slot_of(i, ch), u = use_of(i, ch);
-            bool ok = u < 1 || tc::mbar_wait_sleep(&bar_afree[sl], (uint32_t)((u - 1) & 1), kWaitBudget);
-            if (__all_sync(0xffffffffu, ok)) {
-                if (ch == 0) {
+            if (!cur.ok && gt == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+            const int k_row = tcs::scale_exp(tcs::row_absmax(row, so_g, 0, 16 * S, D, live));
+            const float rs = tcs::pow2i(k_row);
+            bool ok = true;
+            for (int h = 0; h < 2 && ok; ++h) {
+                // the slot of this K half was last read by the products of the half four half-steps back
+                const int sl = slot_of(i, h), u = use_of(i, h);
+                ok = u < 1 || tc::mbar_wait_sleep(&bar_afree[sl], (uint32_t)((u - 1) & 1), kWaitBudget);
+                if (!__all_sync(0xffffffffu, ok)) { ok = false; break; }
+                if (h == 0) {
                     // the epilogue of tile i - 4, the last reader of rmul[i % 4], finished before
                     // the products that freed this slot were issued
-                    rmul[(i & 3) * kTileM + m] = tcs::row_scale(func_scale(cur.func), c_km, k_row);
+                    rmul[(i & 3) * kTileM + m] = tcs::row_scale(func_scale(cur.func), g_km, k_row);
                     tc::mbar_arrive(&bar_rs[i & 3]);
                 }
-                const float rs = tcs::pow2i(k_row);
+                const int s0 = h == 0 ? 0 : s_half, s1 = h == 0 ? s_half : S;
                 for (int st = s0; st < s1; ++st) {
                     uint32_t hi[8], lo[8];
-                    convert16(row, so, 16 * st, D, live, rs, hi, lo);
+                    convert16(row, so_g, 16 * st, D, live, rs, hi, lo);
                     const uint32_t col = slot_col(sl) + lane_off + (uint32_t)(8 * (st - s0));
                     tc::tmem_st32x8(col, hi);
                     tc::tmem_st32x8(col + (uint32_t)kApart, lo);
@@ -375,12 +384,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
                 tc::tmem_wait_st();
                 tc::fence_before_sync();
                 tc::mbar_arrive(&bar_afull[sl]);
-            } else {
-                *abort_flag = 1;  // the next tile's barrier stops the group
             }
-            cur = nxt;
-            nxt = nn;
-            it_nn = it_n3;
+            if (!ok) *abort_flag = 1;  // the next tile's barrier stops the group
+            prv = prv_n;
+            cur = cur_n;
         }
     } else {
         // ---- epilogue group: one TMEM lane (= tile row) per thread, two warps per lane quarter ------
