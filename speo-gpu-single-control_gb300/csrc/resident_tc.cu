@@ -46,11 +46,16 @@ __device__ __forceinline__ void f4se(float4 &v, int q, float x)
 }
 
 __host__ __device__ inline int up_to(int x, int m) { return (x + m - 1) / m * m; }
+__host__ __device__ inline int draw_gens_e(int Pmax)
+{
+    const int g = kThreadsE / Pmax;
+    return g < 1 ? 1 : g > 8 ? 8 : g;
+}
 
 // Shared memory of one island (W = 32 Q floats per population row; trial rows XW = W + 4 apart so
 // that the conversion's one-row-per-thread reads are free of bank conflicts):
 //   B (two-way split of M^T 2^k_M: hi, lo) | pop[Pmax][W] | fit[Pmax (to 4)] | Xs[Pmax][XW] |
-//   sR[2][Pmax][8] (donor positions and jrand of this generation and the next) | sF[2][Pmax (to 4)] (the two column parts of each trial's fitness; before
+//   sR[GB][Pmax][8] | sF[2][Pmax (to 4)] (the two column parts of each trial's fitness; before
 //   the products, the largest |y| of each row's two K halves) | o[W] | rm[Pmax (to 4)] (each
 //   trial's epilogue scale)
 struct EpochTcLayout {
@@ -66,7 +71,7 @@ __host__ __device__ inline EpochTcLayout epoch_tc_layout(int Q, int Pmax)
     L.off_fit = L.off_pop + (size_t)Pmax * W * 4;
     L.off_xs = L.off_fit + (size_t)up_to(Pmax, 4) * 4;
     L.off_r = L.off_xs + (size_t)Pmax * XW * 4;
-    L.off_f = L.off_r + (size_t)2 * Pmax * 8 * 4;
+    L.off_f = L.off_r + (size_t)draw_gens_e(Pmax) * Pmax * 8 * 4;
     L.off_o = L.off_f + 2 * (size_t)up_to(Pmax, 4) * 4;
     L.off_rm = L.off_o + (size_t)W * 4;
     L.total = L.off_rm + (size_t)up_to(Pmax, 4) * 4;
@@ -164,7 +169,7 @@ __global__ void __launch_bounds__(kThreadsE, 1)
         const uint32_t thr = cr_threshold<float>(s.CR);
         const float scale = func_scale(s.func_id);
         const int Kp = tcs::round16(D), S = Kp / 16, s_half = (S + 1) / 2, ntile = (P + tcs::kTileM - 1) / tcs::kTileM;
-        const int Pf = up_to(Pmax, 4);
+        const int GB = draw_gens_e(Pmax), Pf = up_to(Pmax, 4);
 
         if (warp == 0) {
             tc::tmem_alloc(&tmem_slot, kTmemAllocE);
@@ -196,19 +201,6 @@ __global__ void __launch_bounds__(kThreadsE, 1)
         const uint32_t tmem = tmem_slot;
 
         bool ok_draw = true, ok_bound = true, aborted = false;
-        // donor positions + jrand of (generation, row), one thread per row, into sR[gen & 1]
-        auto draw_gen = [&](int gi) {
-            for (int r = tid; r < P; r += kThreadsE) {
-                IdxStream is(key, (uint32_t)(row0 + r), gen0 + (uint32_t)gi, kTagIdx);
-                int rr[5];
-                ok_draw &= draw_donors(is, P, rr);
-                int *o = sR + ((gi & 1) * Pmax + r) * 8;
-#pragma unroll
-                for (int k = 0; k < 5; ++k) o[k] = rr[k];
-                o[5] = is.index(D);
-            }
-        };
-        if (generations > 0) draw_gen(0);
         int g = 0;
         for (; g < generations; ++g) {
             const uint32_t gen = gen0 + (uint32_t)g;
@@ -234,8 +226,22 @@ __global__ void __launch_bounds__(kThreadsE, 1)
                     if (s_bf[w] < bf || (s_bf[w] == bf && s_bi[w] < bi)) { bf = s_bf[w]; bi = s_bi[w]; }
                 best = bi;
             }
-            // (1a) donor positions + jrand of generation g: drawn during generation g - 1's products
-            const int *sRg = sR + (g & 1) * Pmax * 8;
+            // (1a) donor positions + jrand of generations g .. g + GB - 1, one thread per (gen, row)
+            if (g % GB == 0) {
+                const int nb = generations - g < GB ? generations - g : GB;
+                for (int t = tid; t < nb * P; t += kThreadsE) {
+                    const int gi = t / P, r = t - gi * P;
+                    IdxStream is(key, (uint32_t)(row0 + r), gen + (uint32_t)gi, kTagIdx);
+                    int rr[5];
+                    ok_draw &= draw_donors(is, P, rr);
+                    int *o = sR + (gi * Pmax + r) * 8;
+#pragma unroll
+                    for (int k = 0; k < 5; ++k) o[k] = rr[k];
+                    o[5] = is.index(D);
+                }
+                __syncthreads();
+            }
+            const int *sRg = sR + (g % GB) * Pmax * 8;
             // (1b) trial rows from the shared-memory population (the common DE/rand/1 compiled alone)
             if (st == SPEO_DE_RAND_1)
                 trial_rows<SPEO_DE_RAND_1, W, XW>(pop, Xs, sRg, P, D, nch, best, st, F, thr, lb, ub, key, row0, gen,
@@ -278,9 +284,6 @@ __global__ void __launch_bounds__(kThreadsE, 1)
                                          kApartE, b_hi, L.b_bytes, Kp, Kp, 0, S);
                 tc::mma_commit(&bar_mma);
             }
-            // the next generation's draws while the products run (its trials read them after the
-            // barriers below; this generation's trials are done with the other half of sR)
-            if (g + 1 < generations) draw_gen(g + 1);
             // (4) two threads per row (warp w: lane quarter w & 3, tile (w >> 2) & 1, column part
             // w >> 3) read z back and reduce the objective; part p of row m lands in sF[p][m]
             const int te = (warp >> 2) & 1, he = warp >> 3;
