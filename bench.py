@@ -309,20 +309,20 @@ def bench_speo(args) -> dict:
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one island-resident launch of the
 # headline workload, from an ncu capture of that launch (45 generations; the island is read once per
 # launch and its writes stay in L2, so the figure does not grow with the generations per launch).
-EPOCH_LAUNCH_TRAFFIC_BYTES = {"simt": 7040512 + 11008, "tc": 7058688 + 13824}
+EPOCH_LAUNCH_TRAFFIC_BYTES = {"simt": 7040512 + 11008, "tc": 7070208 + 9472}
 C4_TRAIN_STEPS = 48   # Adam steps per generation: 48 x 4096 = 6 passes over a generation's 32768 new rows
-C4_EXPLORE = 0.05
+C4_EXPLORE = 0.05     # fraction of targets that take a uniformly drawn trial instead of the screened one
 # Training batch x Adam steps per generation at about the same samples per generation (k = 8,
 # training every generation): larger batches fill more SMs per step.
 SURROGATE_BATCH_GRID = [dict(k=8, train_steps=st, train_every=1, train_batch=b, lr=lr)
                         for b, st, lr in ((4096, 48, 1e-3), (8192, 24, 1e-3), (8192, 24, 2e-3), (16384, 12, 2e-3),
                                           (16384, 12, 4e-3), (16384, 24, 2e-3), (32768, 6, 4e-3), (32768, 6, 8e-3),
-                                          (32768, 12, 4e-3))]     # fraction of targets that take a uniformly drawn trial instead of the screened one
+                                          (32768, 12, 4e-3))]
 
 
 def c4_run(L, dev, torch, func: int, mode: str, max_gens: int, log_every: int = 10, stop_at: float | None = None,
            train_steps: int = 16, explore: float = 0.25, train_k: int = 8, train_every: int = 1,
-           use_graph: bool = True, train_batch: int = 4096, lr: float = 1e-3):
+           use_graph: bool = True, train_batch: int = 4096, lr: float = 1e-3, uneven: bool = False):
     """One run of the headline shape (plain or surrogate-screened) logging the FP64 best error
     every `log_every` generations; stops early once the error reaches `stop_at`. Blocks of
     `log_every` generations replay one CUDA graph after the first (eager) block. The surrogate
@@ -332,7 +332,7 @@ def c4_run(L, dev, torch, func: int, mode: str, max_gens: int, log_every: int = 
     from speo_gb300 import _lib
     from speo_gb300 import workloads as w
 
-    specs, inst = w.config4_specs(func)
+    specs, inst = (w.config4_uneven_specs if uneven else w.config4_specs)(func)
     tab = w.table(specs, inst, device=dev)
     tab.init_population()
     surr = None
@@ -391,7 +391,7 @@ def first_reach(curve, target):
     return next((c for c in curve if c["best_err"] <= target), None)
 
 
-def bench_surrogate(L, dev, torch, ras_gens: int = 200, schedule: dict | None = None) -> dict:
+def bench_surrogate(L, dev, torch, ras_gens: int = 200, schedule: dict | None = None, uneven: bool = False) -> dict:
     """Surrogate-screened DE against the plain DE on the headline shape, same GPU: (a) the
     rotated sphere of the same shape run to an FP64 error of 1e-8 (capped), which gives the
     exact evaluations and wall time each method needs to get there; (b) the rotated Rastrigin
@@ -404,8 +404,8 @@ def bench_surrogate(L, dev, torch, ras_gens: int = 200, schedule: dict | None = 
         sch.update(schedule)
     out = {"network": "MLP 50-256-256-1, BF16 tcgen05 screening and training, FP32 accumulate, Adam lr 1e-3, "
                       "batch 4096, archive 2^20, k=8 trials per target", "schedule": sch}
-    sp, _ = c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "plain", 4000, stop_at=1e-8)
-    ss, _ = c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8, **sch)
+    sp, _ = c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "plain", 4000, stop_at=1e-8, uneven=uneven)
+    ss, _ = c4_run(L, dev, torch, _lib.FUNC_ROTATED_SPHERE, "surrogate", 1500, stop_at=1e-8, uneven=uneven, **sch)
     sph = {"target": 1e-8,
            "plain": {k: sp[k] for k in ("generations", "exact_evals_to_target", "wall_s_to_target", "final_err")},
            "surrogate": {k: ss[k] for k in ("generations", "exact_evals_to_target", "wall_s_to_target", "final_err")}}
@@ -414,8 +414,8 @@ def bench_surrogate(L, dev, torch, ras_gens: int = 200, schedule: dict | None = 
     sph["exact_evals_ratio_plain_over_surrogate"] = ep / es if ep and es else None
     sph["wall_ratio_plain_over_surrogate"] = wp / ws if wp and ws else None
     out["rotated_sphere"] = sph
-    rp, cp = c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, "plain", ras_gens)
-    rs, cs = c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, "surrogate", ras_gens, **sch)
+    rp, cp = c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, "plain", ras_gens, uneven=uneven)
+    rs, cs = c4_run(L, dev, torch, _lib.FUNC_ROTATED_RASTRIGIN, "surrogate", ras_gens, uneven=uneven, **sch)
     hit = first_reach(cs, rp["final_err"])
     hit_p = first_reach(cp, rp["final_err"])
     out["rotated_rastrigin"] = {
@@ -1142,7 +1142,7 @@ def one_section(args) -> dict | None:
     from speo_gb300 import _lib
 
     if not (args.ops_only or args.e2e_only or args.published_only or args.mlp_case or args.c4_only
-            or args.configs_only or args.surrogate_sweep or args.surrogate_batch_sweep):
+            or args.configs_only or args.surrogate_sweep or args.surrogate_batch_sweep or args.surrogate_uneven):
         return None
     dev = "cuda:0"
     torch.cuda.set_device(0)
@@ -1164,6 +1164,8 @@ def one_section(args) -> dict | None:
         return {"surrogate": bench_surrogate(L, dev, torch, args.c4_gens)}
     if args.surrogate_sweep:
         return {"surrogate_sweep": bench_surrogate_sweep(L, dev, torch)}
+    if args.surrogate_uneven:
+        return {"surrogate_uneven_islands": bench_surrogate(L, dev, torch, args.c4_gens, uneven=True)}
     if args.surrogate_batch_sweep:
         return {"surrogate_batch_sweep": bench_surrogate_sweep(L, dev, torch, grid=SURROGATE_BATCH_GRID)}
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
@@ -1195,6 +1197,8 @@ def main() -> None:
     ap.add_argument("--mlp-case", action="store_true", help="only the surrogate network's kernels")
     ap.add_argument("--surrogate-sweep", action="store_true",
                     help="only the surrogate schedule sweep (k, Adam steps, training interval) against plain DE")
+    ap.add_argument("--surrogate-uneven", action="store_true",
+                    help="only the surrogate-vs-plain section on 144 islands of uneven size (config 4's instance)")
     ap.add_argument("--surrogate-batch-sweep", action="store_true",
                     help="only the surrogate's training batch / Adam steps / learning rate sweep against plain DE")
     ap.add_argument("--e2e-only", action="store_true", help="only the end-to-end drop-in measurements")

@@ -86,6 +86,15 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap *map)
 {
     asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)map) : "memory");
 }
+// 1-D bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) from global memory
+// into shared memory, completing on `bar` (tx bytes).
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"((uint64_t)src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
 
 // Arrives once on `bar` (no transaction bytes).
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar)

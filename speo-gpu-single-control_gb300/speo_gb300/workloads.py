@@ -63,5 +63,17 @@ def config4_specs(func: int = RASTRIGIN, rank: int = 0):
     return specs, inst
 
 
+def config4_uneven_specs(func: int = RASTRIGIN, rank: int = 0):
+    """Config 4's instance on 144 islands of uneven size (P uniform in [160, 256], seeded; about
+    30k rows, one island per SM): the screened and plain generations over islands of different
+    sizes in one table."""
+    seed = run_seed(1, func, 4)
+    inst = [make_instance(seed, 50)]
+    sizes = np.random.default_rng(seed + 77).integers(160, 257, 144)
+    specs = [SegmentSpec(pop_size=int(sizes[i]), dim=50, func_id=func, instance=0,
+                         seed=seed * 31 + i + 1000003 * rank, ring_next=(i + 1) % 144) for i in range(144)]
+    return specs, inst
+
+
 def table(specs, inst, device="cuda", tile_rows=_lib.TILE_SIMT, extra_rows=0):
     return SegmentTable(specs, inst, tile_rows=tile_rows, device=device, extra_rows=extra_rows)

@@ -268,12 +268,14 @@ def test_adam_matches_oracle(lib, oracle, cuda):
 
 
 def _islands(cuda, n_isl, P, D, func=31, seed=11):
+    """n_isl islands of one instance; P an int, or a list of per-island sizes (uneven islands)."""
     from speo_gb300.device import SegmentSpec, SegmentTable
     from speo_gb300.instances import make_instance
 
     inst = [make_instance(seed, D)]
-    specs = [SegmentSpec(pop_size=P, dim=D, func_id=func, instance=0, seed=seed * 100 + i, ring_next=(i + 1) % n_isl)
-             for i in range(n_isl)]
+    sizes = P if isinstance(P, (list, tuple)) else [P] * n_isl
+    specs = [SegmentSpec(pop_size=sizes[i], dim=D, func_id=func, instance=0, seed=seed * 100 + i,
+                         ring_next=(i + 1) % n_isl) for i in range(n_isl)]
     return SegmentTable(specs, inst, device=str(cuda))
 
 
@@ -378,6 +380,42 @@ def test_surrogate_beats_plain_de_at_equal_exact_evaluations(lib, cuda):
         print(f"rastrigin seed {seed}: plain {_run(lib, cuda, False, gens, seed, func=9):.3e}, "
               f"screened {_run(lib, cuda, True, gens, seed, func=9):.3e}")
     assert np.median(ratios) > 10.0, ratios
+
+
+def test_surrogate_on_uneven_islands(lib, cuda):
+    """The screened generation over islands of uneven size in one table (one launch per stage):
+    every island keeps exactly its own rows, the kept fitness is the exact fitness of the kept rows
+    (re-evaluated), and at equal exact evaluations the screened run is ahead of plain DE."""
+    import torch
+
+    sizes = [40, 64, 100, 33, 77, 128, 52, 90]
+    errs = {}
+    for use in (False, True):
+        tab = _islands(cuda, len(sizes), sizes, 10, func=31, seed=31)
+        tab.init_population()
+        s = Surr(lib, din=10, h=64, cap=8 * sum(sizes), batch=1024, lr=3e-3, seed=31) if use else None
+        try:
+            for g in range(80):
+                if use:
+                    tab.surrogate_generation(s.p, k=8, train_steps=32, explore=0.25)
+                else:
+                    tab.generation()
+                if (g + 1) % 20 == 0:
+                    tab.migrate(2)
+            torch.cuda.synchronize()
+            assert tab.rows == sum(sizes)
+            fit = tab.fit[tab.cur].clone()
+            again = torch.full_like(fit, float("nan"))
+            tab.evaluate(out=again)
+            torch.cuda.synchronize()
+            assert torch.equal(fit[:tab.rows], again[:tab.rows])
+            rows, e = tab.best_f64()
+            errs[use] = float(e.min().item())
+        finally:
+            if s is not None:
+                s.close()
+    print(f"uneven islands, sphere D=10: plain {errs[False]:.3e}, screened {errs[True]:.3e}")
+    assert errs[True] < errs[False] / 10.0
 
 
 def test_surrogate_generation_replays_from_a_cuda_graph(lib, cuda):
