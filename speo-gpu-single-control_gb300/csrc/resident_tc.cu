@@ -98,27 +98,47 @@ __device__ __forceinline__ void trial_rows(const float *pop, float *Xs, const in
         const int *sr = sRg + r * 8;
         const int jrand = sr[5], e0 = 4 * c;
         const float4 ti = ld4e(pop + r * W + e0);
-        const float4 tb = best >= 0 ? ld4e(pop + best * W + e0) : ti;
+        const float4 tb = (ST >= 0 ? strategy_uses_best(ST) && best >= 0 : best >= 0) ? ld4e(pop + best * W + e0) : ti;
         float4 tr[5];
 #pragma unroll
         for (int k = 0; k < 5; ++k) tr[k] = k < ndon ? ld4e(pop + sr[k] * W + e0) : ti;
         const uint4 w = philox(make_uint4((uint32_t)c, (uint32_t)(row0 + r), gen, kTagCr), key);
         float4 x4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr (ST >= 0) {
+            // one strategy compiled: the mutant of every element, then a select (no branch per
+            // element); the chunk's elements past D stay 0 and are not bound-checked
+            const bool full = e0 + 4 <= D;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int e = e0 + q;
-            if (e < D) {
-                float x;
-                if (e == jrand || cr_take(pick(w, (uint32_t)q), thr)) {
-                    float xr[5];
+            for (int q = 0; q < 4; ++q) {
+                const int e = e0 + q;
+                float xr[5];
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) xr[k] = f4ge(tr[k], q);
-                    x = mutant<float>(st, F, f4ge(ti, q), f4ge(tb, q), xr);
-                } else {
-                    x = f4ge(ti, q);
+                for (int k = 0; k < 5; ++k) xr[k] = f4ge(tr[k], q);
+                const float m = mutant<float>(st, F, f4ge(ti, q), f4ge(tb, q), xr);
+                const bool take = e == jrand || cr_take(pick(w, (uint32_t)q), thr);
+                float x = take ? m : f4ge(ti, q);
+                if (full || e < D) {
+                    x = check_bound<float>(x, lb, ub, ok_bound);
+                    f4se(x4, q, x);
                 }
-                x = check_bound<float>(x, lb, ub, ok_bound);
-                f4se(x4, q, x);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = e0 + q;
+                if (e < D) {
+                    float x;
+                    if (e == jrand || cr_take(pick(w, (uint32_t)q), thr)) {
+                        float xr[5];
+#pragma unroll
+                        for (int k = 0; k < 5; ++k) xr[k] = f4ge(tr[k], q);
+                        x = mutant<float>(st, F, f4ge(ti, q), f4ge(tb, q), xr);
+                    } else {
+                        x = f4ge(ti, q);
+                    }
+                    x = check_bound<float>(x, lb, ub, ok_bound);
+                    f4se(x4, q, x);
+                }
             }
         }
         st4e(Xs + r * XW + e0, x4);
@@ -137,7 +157,7 @@ __global__ void __launch_bounds__(kThreadsE, 1)
                       float *pop_out, float *fit_out, uint32_t *gen_ctr, int generations, float *hist,
                       long long hist_ld)
 {
-    constexpr int W = 32 * Q, XW = W + 4, G = Q == 1 ? 8 : 16, RPP = kThreadsE / G;
+    constexpr int W = 32 * Q, XW = W + 4;
     extern __shared__ __align__(1024) uint8_t smem_e[];
     const EpochTcLayout L = epoch_tc_layout(Q, Pmax);
     uint8_t *b_hi = smem_e;
@@ -154,7 +174,6 @@ __global__ void __launch_bounds__(kThreadsE, 1)
     __shared__ uint32_t tmem_slot;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int grp = tid / G, gl = tid % G;
     const speo_segment &s = segs[blockIdx.x];
     const int D = s.dim, P = s.pop_size, ld = s.ld, nch = (D + 3) >> 2;
     const uint32_t gen0 = *(volatile uint32_t *)gen_ctr;
@@ -305,19 +324,29 @@ __global__ void __launch_bounds__(kThreadsE, 1)
             tc::fence_before_sync();
             __syncthreads();
             // (5) greedy selection in place: strict `<` (kernel_DE_CUDA.cu:312); the fitness is the
-            // first column part's sum plus the second's, as speo_evaluate_tc adds them. The G lanes
-            // of a row (one warp) all read its fitness before one of them replaces it; with a
+            // first column part's sum plus the second's, as speo_evaluate_tc adds them; with a
             // history buffer, generation g's fitness of the row goes to hist[g][row].
-            const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (lane & ~(G - 1));
-            for (int r = grp; r < P; r += RPP) {
+            // (5a) one thread per row decides, updates fit and leaves the decision in sF[r]
+            for (int r = tid; r < P; r += kThreadsE) {
                 const float tf = sF[r] + sF[Pf + r], fo = fit[r];
                 const bool win = tf < fo;
-                if (win)
-                    for (int c = gl; c < nch; c += G) st4e(pop + r * W + 4 * c, ld4e(Xs + r * XW + 4 * c));
-                __syncwarp(gmask);
-                if (gl == 0) {
-                    if (win) fit[r] = tf;
-                    if (hist) hist[(size_t)g * (size_t)hist_ld + (size_t)(row0 + r)] = win ? tf : fo;
+                if (win) fit[r] = tf;
+                if (hist) hist[(size_t)g * (size_t)hist_ld + (size_t)(row0 + r)] = win ? tf : fo;
+                sF[r] = win ? 1.f : 0.f;
+            }
+            __syncthreads();
+            // (5b) the winners' rows move, (row, chunk) tasks dealt to all threads
+            {
+                const int tasks = P * nch, dr = kThreadsE / nch, dc = kThreadsE - dr * nch;
+                int r = tid / nch, c = tid - r * nch;
+                for (int t = tid; t < tasks; t += kThreadsE) {
+                    if (sF[r] != 0.f) st4e(pop + r * W + 4 * c, ld4e(Xs + r * XW + 4 * c));
+                    c += dc;
+                    r += dr;
+                    if (c >= nch) {
+                        c -= nch;
+                        ++r;
+                    }
                 }
             }
         }
