@@ -860,6 +860,7 @@ def bench_config3(L, dev, torch, flush) -> dict:
     instance and objective; one launch per generation (the mixed-class kernel), 20 generations per
     CUDA graph. The tile height is the library tuner's choice (speo_autotune_tile_rows: each
     candidate timed on this table, the fastest cached for its shape bucket)."""
+    from speo_gb300 import _lib
     from speo_gb300 import workloads as w
 
     specs, inst = w.config3_specs(1024)
@@ -869,11 +870,22 @@ def bench_config3(L, dev, torch, flush) -> dict:
     g = capture(torch, lambda: [tab.generation() for _ in range(20)])
     g.replay()
     ms = time_graph(torch, g, 5, flush) / 20
+    # the same runs with the rotation on the tensor cores: trials (k = 1), speo_evaluate_tc over
+    # 128-row tiles (B rebuilt at every change of instance), selection; three launches per generation
+    tab_tc = w.table(specs, inst, device=dev, tile_rows=_lib.TILE_TC)
+    tab_tc.init_population()
+    trial = torch.zeros_like(tab_tc.pop[0])
+    trial_fit = torch.zeros_like(tab_tc.fit[0])
+    g_tc = capture(torch, lambda: [tab_tc.tc_generation(trial, trial_fit) for _ in range(20)])
+    g_tc.replay()
+    ms_tc = time_graph(torch, g_tc, 5, flush) / 20
     return {"workload": f"1024 runs, D in {{10,30,50,100}}, P in [50,200] ({evals} rows), mixed objectives",
             "ms_per_generation": ms, "gens_per_s": 1e3 / ms, "evals_per_s": evals / (ms / 1e3),
             "launches_per_generation": 1, "tile_rows": tab.tile_rows,
             "autotune_ms_per_generation": {str(k): v for k, v in tab.autotune["ms"].items()},
-            "autotune_cached": tab.autotune["cached"]}
+            "autotune_cached": tab.autotune["cached"],
+            "tensor_core_form": {"ms_per_generation": ms_tc, "evals_per_s": evals / (ms_tc / 1e3),
+                                 "launches_per_generation": 3, "tile_rows": _lib.TILE_TC}}
 
 
 # DRAM bytes of one 50-generation island-resident launch of this workload (64 x 100, D = 30), from

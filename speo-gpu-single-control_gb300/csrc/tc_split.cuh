@@ -201,9 +201,11 @@ __device__ __forceinline__ void issue_split_mma(uint32_t acc, uint32_t a_hi, uin
     }
 }
 
-// Two objective terms at once (f32x2); per element the same operations as obj_term: z - rint(z)
-// (rint by adding and subtracting 1.5 * 2^23, exact for |z| < 2^22), the Taylor sine, and
-// z*z + (20 s) s.
+// Two objective terms at once (f32x2): z - rint(z) (rint by adding and subtracting 1.5 * 2^23,
+// exact for |z| < 2^22), sin(pi r) = r P(r^2) with P of degree 4, and z*z + (20 s) s. P is a
+// near-minimax fit of sin(pi r) / r over |r| <= 1/2 (iteratively reweighted least squares on
+// Chebyshev nodes, relative weights): evaluated in FP32 its relative error is 1.8e-7, the same as
+// the degree-11 Taylor sine of the CUDA-core objective (one fused multiply-add fewer per pair).
 __device__ __forceinline__ uint64_t obj_term2(int func, uint64_t z)
 {
     using namespace tc;
@@ -211,12 +213,11 @@ __device__ __forceinline__ uint64_t obj_term2(int func, uint64_t z)
     const uint64_t C = pk2(12582912.0f, 12582912.0f);
     const uint64_t r = sub2(z, sub2(add2(z, C), C));
     const uint64_t r2 = mul2(r, r);
-    uint64_t p = pk2(-7.3704309762e-03f, -7.3704309762e-03f);
-    p = fma2(p, r2, pk2(8.2145884633e-02f, 8.2145884633e-02f));
-    p = fma2(p, r2, pk2(-5.9926450253e-01f, -5.9926450253e-01f));
-    p = fma2(p, r2, pk2(2.5501639843e+00f, 2.5501639843e+00f));
-    p = fma2(p, r2, pk2(-5.1677126884e+00f, -5.1677126884e+00f));
-    p = fma2(p, r2, pk2(3.1415927410e+00f, 3.1415927410e+00f));
+    uint64_t p = pk2(7.756077498e-02f, 7.756077498e-02f);
+    p = fma2(p, r2, pk2(-5.982423425e-01f, -5.982423425e-01f));
+    p = fma2(p, r2, pk2(2.550069809e+00f, 2.550069809e+00f));
+    p = fma2(p, r2, pk2(-5.167709827e+00f, -5.167709827e+00f));
+    p = fma2(p, r2, pk2(3.141592741e+00f, 3.141592741e+00f));
     const uint64_t sn = mul2(r, p);
     return fma2(z, z, mul2(mul2(pk2(20.0f, 20.0f), sn), sn));
 }
