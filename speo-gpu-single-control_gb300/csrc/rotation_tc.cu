@@ -32,7 +32,6 @@ namespace {
 using tcs::kTileM;
 using tcs::round16;
 using tcs::build_b;
-using tcs::convert16;
 using tcs::issue_split_mma;
 using tcs::epilogue_row;
 constexpr int kTmemCols = 128;   // widest accumulator (N <= 128)
@@ -326,7 +325,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             const TileInfo prv_n = tile_info(a, item_of(i + 1)), cur_n = tile_info(a, item_of(i + 2));
             const int sidx = i % ns;
             const int D = cur.D, Kp = round16(D), S = Kp / 16, s_half = (S + 1) / 2;
-            const float *row = stage[sidx] + (size_t)m * L.box_x;
+            float *row = stage[sidx] + (size_t)m * L.box_x;
             const bool live = cur.ok && m < cur.count;
             bool to = !tc::mbar_wait_sleep(&bar_tma[sidx], (uint32_t)((i / ns) & 1), kWaitBudget);
             const bool new_inst = cur.ok && (cur.rot != g_rot || cur.shift != g_shift || D != g_dim ||
@@ -359,7 +358,26 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
                 tc::named_bar_sync(gbar, 128);  // B, o and red are complete
             }
             if (!cur.ok && gt == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
-            const int k_row = tcs::scale_exp(tcs::row_absmax(row, so_g, 0, 16 * S, D, live));
+            // y = x - o replaces x in the staged row (columns < D) while the largest |y| is found;
+            // the conversion then reads y
+            float mx = 0.f;
+            if (live) {
+                for (int k = 0; k < D; k += 4) {
+                    const float4 x = *reinterpret_cast<const float4 *>(row + k);
+                    const float4 o = *reinterpret_cast<const float4 *>(so_g + k);
+                    float4 y;
+                    tc::upk2(tc::sub2(tc::pk2(x.x, x.y), tc::pk2(o.x, o.y)), y.x, y.y);
+                    tc::upk2(tc::sub2(tc::pk2(x.z, x.w), tc::pk2(o.z, o.w)), y.z, y.w);
+                    if (k + 4 > D) {  // the row's own padding past D: zero, as the conversion reads it
+                        if (k + 1 >= D) y.y = 0.f;
+                        if (k + 2 >= D) y.z = 0.f;
+                        y.w = 0.f;
+                    }
+                    mx = fmaxf(fmaxf(mx, fabsf(y.x)), fmaxf(fabsf(y.y), fmaxf(fabsf(y.z), fabsf(y.w))));
+                    *reinterpret_cast<float4 *>(row + k) = y;
+                }
+            }
+            const int k_row = tcs::scale_exp(mx);
             const float rs = tcs::pow2i(k_row);
             bool ok = true;
             for (int h = 0; h < 2 && ok; ++h) {
@@ -376,7 +394,15 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
                 const int s0 = h == 0 ? 0 : s_half, s1 = h == 0 ? s_half : S;
                 for (int st = s0; st < s1; ++st) {
                     uint32_t hi[8], lo[8];
-                    convert16(row, so_g, 16 * st, D, live, rs, hi, lo);
+                    float v[16];
+#pragma unroll
+                    for (int q4 = 0; q4 < 4; ++q4) {
+                        const int k = 16 * st + 4 * q4;
+                        const float4 y = (live && k < D) ? *reinterpret_cast<const float4 *>(row + k)
+                                                         : make_float4(0.f, 0.f, 0.f, 0.f);
+                        v[4 * q4 + 0] = y.x; v[4 * q4 + 1] = y.y; v[4 * q4 + 2] = y.z; v[4 * q4 + 3] = y.w;
+                    }
+                    tcs::split16(v, rs, hi, lo);
                     const uint32_t col = slot_col(sl) + lane_off + (uint32_t)(8 * (st - s0));
                     tc::tmem_st32x8(col, hi);
                     tc::tmem_st32x8(col + (uint32_t)kApart, lo);
