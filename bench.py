@@ -206,11 +206,18 @@ def bench_speo(args) -> dict:
         raise RuntimeError("the headline islands do not fit one block's shared memory on this GPU")
     epoch = tab.epoch_tc if use_tc else tab.epoch
     migrate = ring_migration(tab, dev, rank, world)
+    # one GPU, tensor-core epochs: the migrations run inside one cooperative launch of all the
+    # generations (speo_island_epochs_tc); otherwise a launch per interval and migration launches
+    fused = world == 1 and use_tc and not args.launch_per_interval
     tab.init_population()
-    done = run_plain(epoch, migrate, args.warmup, 0)       # exactly W untimed generations
+    if fused:
+        tab.island_epochs_tc(args.warmup, 0, INTERVAL, MIGRANTS)   # exactly W untimed generations
+        done = args.warmup
+    else:
+        done = run_plain(epoch, migrate, args.warmup, 0)       # exactly W untimed generations
     torch.cuda.synchronize()
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
-    plan = list(chunks(done, args.steps))
+    plan = [(args.steps, False)] if fused else list(chunks(done, args.steps))
     ev = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(3)) for _ in plan]
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     if world > 1:
@@ -220,7 +227,10 @@ def bench_speo(args) -> dict:
         for (k, mig), (a, b, c) in zip(plan, ev):
             flush_l2(flush)                                # L2 flushed before every launch
             a.record()
-            epoch(k)
+            if fused:
+                tab.island_epochs_tc(k, done, INTERVAL, MIGRANTS)
+            else:
+                epoch(k)
             b.record()
             if mig:
                 migrate()
@@ -235,7 +245,7 @@ def bench_speo(args) -> dict:
     kern_ms = sum(a.elapsed_time(b) for a, b, _ in ev)
     ms = max_over_ranks(step_ms, dev, world)
     value = EVALS_PER_STEP * args.steps * world / (ms / 1e3)
-    n_mig = sum(1 for _, m in plan if m)
+    n_mig = (done + args.steps) // INTERVAL - done // INTERVAL if fused else sum(1 for _, m in plan if m)
     rows, errs = tab.best_f64()
     best_err = float(errs.min().item())
 
@@ -245,9 +255,10 @@ def bench_speo(args) -> dict:
     achieved = alg_bytes_gen * args.steps / (kern_ms / 1e3) / 1e9
     gens_per_launch = args.steps / len(plan)
     if use_tc:
-        kernel = (f"k_island_epoch_tc<2> (one 512-thread block per island, {N_ISLANDS} blocks; up to 50 generations "
-                  "per launch with the island and its trials in shared memory, the rotation on tcgen05: three "
-                  "split-FP16 products per K step into TMEM accumulators)")
+        kernel = (f"k_island_epoch_tc<2> (one 512-thread block per island, {N_ISLANDS} blocks, the island and its "
+                  "trials in shared memory, the rotation on tcgen05: three split-FP16 products per K step into TMEM "
+                  "accumulators; " + ("all the timed generations in one cooperative launch, each ring migration "
+                                      "inside it at a grid barrier)" if fused else "up to 50 generations per launch)"))
     elif 2 * N_ISLANDS <= sms:
         kernel = f"k_island_epoch2<2> (two-block cluster per island, {2 * N_ISLANDS} blocks)"
     else:
@@ -268,9 +279,11 @@ def bench_speo(args) -> dict:
         "config": {"workload": WORKLOAD, "islands": N_ISLANDS, "pop_size": POP, "dim": DIM, "func_id": FUNC,
                    "migration_interval": INTERVAL, "migrants": MIGRANTS,
                    "step": f"one generation over all islands ({EVALS_PER_STEP} exact evaluations)",
-                   "l2": "flushed (512 MB write) before every timed launch; a launch runs up to 50 generations "
-                         "with each island resident in shared memory",
-                   "launches": f"{len(plan)} island-resident launches + {2 * n_mig} migration launches"},
+                   "l2": "flushed (512 MB write) before every timed launch; each island stays resident in shared "
+                         "memory for the whole launch",
+                   "launches": (f"1 cooperative island-resident launch of {args.steps} generations with the {n_mig} "
+                                "ring migrations inside it" if fused else
+                                f"{len(plan)} island-resident launches + {2 * n_mig} migration launches")},
         "gens_per_s": args.steps / (ms / 1e3),
         "best_error_f64": best_err,
         "roofline": {"kernel": kernel, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
@@ -290,7 +303,7 @@ def bench_speo(args) -> dict:
                                     "frac": tensor_flop_gen * args.steps / (kern_ms / 1e3) / 1e12 / pk["bf16_tflops"],
                                     "flop_per_step": tensor_flop_gen,
                                     "peak_src": f"{pk['src']} (MEASURED_PEAKS bf16_tflops, burst)"}} if use_tc else {})},
-        "gpu_launches": len(plan) + 2 * n_mig,
+        "gpu_launches": len(plan) if fused else len(plan) + 2 * n_mig,
         "clocks": clocks,
     }
     if rank != 0:
@@ -518,8 +531,9 @@ def bench_e2e(L, dev, torch, steps: int) -> dict:
     h2d = (n * ld + h_sh.numel() + h_rot.numel()) * 4
     return {"value": n * steps / dt, "unit": "evals/s", "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": n * 4,
             "steps": steps, "dtype": "fp32",
-            "path": "speo_island_run_tc (the island loop of 128 islands of 256 as one C-ABI call: tensor-core "
-                    "island-resident epochs of up to 50 generations and speo_ring_migrate every 50 generations); "
+            "path": "speo_island_run_tc (the island loop of 128 islands of 256 as one C-ABI call: cooperative "
+                    "tensor-core island-resident launches of 200 generations with the ring migration every 50 "
+                    "generations inside them); "
                     "initial rows, o and M^T uploaded and the initial fitness evaluated inside the timed region, every "
                     "generation's fitness vector read back to pinned host memory"}
 
@@ -1209,6 +1223,8 @@ def main() -> None:
     ap.add_argument("--mlp-case", action="store_true", help="only the surrogate network's kernels")
     ap.add_argument("--surrogate-sweep", action="store_true",
                     help="only the surrogate schedule sweep (k, Adam steps, training interval) against plain DE")
+    ap.add_argument("--launch-per-interval", action="store_true",
+                    help="time the headline as one launch per migration interval with migration launches between")
     ap.add_argument("--surrogate-uneven", action="store_true",
                     help="only the surrogate-vs-plain section on 144 islands of uneven size (config 4's instance)")
     ap.add_argument("--surrogate-batch-sweep", action="store_true",

@@ -342,18 +342,29 @@ SPEO_API int speo_generation_epoch_tc(const speo_segment *d_segs, int n_segs, in
 
 /* The island loop of IslandEA::Execute (src/island_EA.cc:78-113) as one call: `generations`
  * generations of speo_generation_epoch_tc on the islands of d_segs (in place in pop / fit, rows
- * rows, P <= 256, D <= 64), in launches of up to `interval` generations, and speo_ring_migrate
- * (migrants rows, caller staging of n_segs * migrants * (max_ld + 1) floats) after every
- * generation count that is a multiple of `interval`, counted from the start of the run: `first` is
- * the number of generations the run has already done. h_fitness (may be null; pinned host memory
- * for the copies to overlap): generations x rows floats that receive every generation's fitness
- * (generation g of this call at h_fitness + g * rows), read back on a second stream while the next
- * launch runs. Runs on `stream`; synchronous (returns when the generations and copies are done).
- * The results equal speo_generation_epoch_tc + speo_ring_migrate called in the same order. */
+ * rows, P <= 256, D <= 64) and the ring migration of speo_ring_migrate (migrants rows, caller
+ * staging of n_segs * migrants * (max_ld + 1) floats) after every generation count that is a
+ * multiple of `interval`, counted from the start of the run: `first` is the number of generations
+ * the run has already done. When every island's block can be resident at once (one block per SM:
+ * n_segs <= the SM count) and migrants <= 32, the migrations run inside the launches (a cooperative
+ * launch; each island sends its best rows through a staging area the library owns, the blocks meet
+ * at a grid barrier with a bounded wait, and each island takes its predecessor's rows), one launch
+ * for the whole call or, with h_fitness, four intervals per launch; otherwise launches of up to
+ * `interval` generations with speo_ring_migrate between them. h_fitness (may be null; pinned host
+ * memory for the copies to overlap): generations x rows floats that receive every generation's
+ * fitness (generation g of this call at h_fitness + g * rows), read back on a second stream while
+ * the next launch runs. Runs on `stream`; synchronous (returns when the generations and copies are
+ * done). The results equal speo_generation_epoch_tc + speo_ring_migrate called in the same order. */
 SPEO_API int speo_island_run_tc(const speo_segment *d_segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
                                 float *pop, float *fit, long long rows, uint32_t *d_gen, int first, int generations,
                                 int interval, int migrants, float *staging, int max_ld, float *h_fitness,
                                 void *stream);
+/* The same generations and migrations without read-back and without waiting: enqueued on `stream`
+ * (asynchronous), for callers that keep the population on the device. */
+SPEO_API int speo_island_epochs_tc(const speo_segment *d_segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
+                                   float *pop, float *fit, long long rows, uint32_t *d_gen, int first,
+                                   int generations, int interval, int migrants, float *staging, int max_ld,
+                                   void *stream);
 
 /* The library's tile-shape tuner for speo_generation (k_generation / k_generation_mixed), in
  * place of the reference's fixed launch shapes (CUDA_EA_library/kernel_CEC2014_CUDA.cu:56-73,

@@ -387,15 +387,21 @@ __global__ void __launch_bounds__(256) k_immigrate(const speo_segment *segs, int
     __shared__ long long sel[kMaxMigrants];
     __shared__ float sf[8];
     __shared__ long long sr[8];
-    __shared__ int src;
+    __shared__ int src, nsrc;
     const int d = blockIdx.x;
     const speo_segment &s = segs[d];
+    // the predecessor (the lowest-numbered segment whose ring_next is d), all threads scanning
+    if (threadIdx.x == 0) { src = 0x7fffffff; nsrc = 0; }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n_segs; i += blockDim.x)
+        if (segs[i].ring_next == d) {
+            atomicMin(&src, i);
+            atomicAdd(&nsrc, 1);
+        }
+    __syncthreads();
     if (threadIdx.x == 0) {
-        int found = -1, count = 0;
-        for (int i = 0; i < n_segs; ++i)
-            if (segs[i].ring_next == d) { if (found < 0) found = i; ++count; }
-        if (count > 1) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
-        src = found;
+        if (nsrc > 1) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+        if (nsrc == 0) src = -1;
     }
     __syncthreads();
     if (src < 0) return;

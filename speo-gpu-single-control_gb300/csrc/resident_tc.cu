@@ -18,6 +18,8 @@
 //       fitness of a row is bit-identical to that kernel's;
 //   (5) greedy selection (strict `<`, kernel_DE_CUDA.cu:312) in place.
 // The rotated Rastrigin (9) and sphere (31) only.
+#include <mutex>
+
 #include "dropin.cuh"
 #include "host.h"
 #include "tc_split.cuh"
@@ -151,11 +153,62 @@ __device__ __forceinline__ void trial_rows(const float *pop, float *Xs, const in
     }
 }
 
+// Ring migration inside a launch (k > 0): after every generation g with (pos + g + 1) % interval
+// == 0 (pos: the run's generation count at the launch's first generation), each island sends its
+// k best rows to the staging area, every block of the launch meets at a grid barrier, and each
+// island replaces its k worst rows with its ring predecessor's (speo_ring_migrate's semantics:
+// best by ascending (fitness, row), worst by descending, NaN ranks as +inf, the worst row takes
+// the best emigrant). The launch is cooperative (every block resident), so the barrier ends.
+constexpr int kMaxMigrantsE = 32;
+struct EpochMig {
+    int interval, k, pos;
+    float *staging;  // 2 (parity of the migration) x islands x k x (W + 1) floats
+    unsigned *bar;   // grid-barrier arrivals, zeroed before the launch
+};
+
+// Arrival number `target` of the launch's grid barrier (target = (migration + 1) x blocks);
+// bounded wait. Every thread of the block calls it; returns false after a timeout.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(bar, 1u);
+        const long long t0 = clock64();
+        bool ok = true;
+        while (*(volatile unsigned *)bar < target)
+            if (clock64() - t0 > kWaitBudgetE) { ok = false; break; }
+        __threadfence();
+        s_ok = ok ? 1 : 0;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Arrival only, for a block that has stopped (after a timeout): the blocks still running are not
+// left waiting for it, and it does not wait for them.
+__device__ __forceinline__ void grid_arrive(unsigned *bar)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(bar, 1u);
+    }
+}
+
+// Number of migration points among the launch's generations.
+__device__ __forceinline__ int migrations_in(const EpochMig &mg, int generations)
+{
+    if (mg.k <= 0 || mg.interval <= 0) return 0;
+    return (mg.pos + generations) / mg.interval - mg.pos / mg.interval;
+}
+
 template <int Q>
 __global__ void __launch_bounds__(kThreadsE, 1)
     k_island_epoch_tc(const speo_segment *__restrict__ segs, int Pmax, const float *pop_in, const float *fit_in,
                       float *pop_out, float *fit_out, uint32_t *gen_ctr, int generations, float *hist,
-                      long long hist_ld)
+                      long long hist_ld, EpochMig mg)
 {
     constexpr int W = 32 * Q, XW = W + 4;
     extern __shared__ __align__(1024) uint8_t smem_e[];
@@ -177,6 +230,25 @@ __global__ void __launch_bounds__(kThreadsE, 1)
     const speo_segment &s = segs[blockIdx.x];
     const int D = s.dim, P = s.pop_size, ld = s.ld, nch = (D + 3) >> 2;
     const uint32_t gen0 = *(volatile uint32_t *)gen_ctr;
+    __shared__ int s_src, s_nsrc, s_best[kMaxMigrantsE], s_worst[kMaxMigrantsE];
+    const int nmig = migrations_in(mg, generations);
+    int m_done = 0;  // migrations this block has taken part in (its grid-barrier arrivals)
+    if (nmig > 0) {
+        // the ring predecessor: the lowest-numbered segment whose ring_next is this one (several:
+        // flagged, as speo_ring_migrate does), the segments scanned by all threads at once
+        if (tid == 0) { s_src = 0x7fffffff; s_nsrc = 0; }
+        __syncthreads();
+        for (int i = tid; i < (int)gridDim.x; i += kThreadsE)
+            if (segs[i].ring_next == (int)blockIdx.x) {
+                atomicMin(&s_src, i);
+                atomicAdd(&s_nsrc, 1);
+            }
+        __syncthreads();
+        if (tid == 0) {
+            if (s_nsrc > 1) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+            if (s_nsrc == 0) s_src = -1;
+        }
+    }
     // every thread of the block reads the same segment: the branch below is block-uniform
     const bool seg_ok = P >= 2 && P <= Pmax && Pmax <= kMaxPopE && D >= 1 && D <= W && D <= kMaxDimE &&
                         (ld & 3) == 0 && ld >= D && tc_objective(s.func_id);
@@ -349,7 +421,60 @@ __global__ void __launch_bounds__(kThreadsE, 1)
                     }
                 }
             }
+            // (6) ring migration at the run's migration points
+            if (nmig > 0 && (mg.pos + g + 1) % mg.interval == 0) {
+                const int k = mg.k, SW = W + 1;
+                float *stg = mg.staging + (size_t)(m_done & 1) * gridDim.x * k * SW;
+                __syncthreads();
+                // each row's place in the best order (ascending (f, r)) and in the worst order
+                for (int r = tid; r < P; r += kThreadsE) {
+                    const float fr = rank_key(fit[r]);
+                    int rb = 0, rw = 0;
+                    for (int j = 0; j < P; ++j) {
+                        const float fj = rank_key(fit[j]);
+                        rb += (fj < fr || (fj == fr && j < r)) ? 1 : 0;
+                        rw += (fj > fr || (fj == fr && j > r)) ? 1 : 0;
+                    }
+                    if (rb < k) s_best[rb] = r;
+                    if (rw < k) s_worst[rw] = r;
+                }
+                __syncthreads();
+                const bool emit = s.ring_next >= 0 && P >= k;
+                if (s.ring_next >= 0 && P < k && tid == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+                if (emit) {
+                    for (int i = tid; i < k * D; i += kThreadsE) {
+                        const int t = i / D, e = i - t * D;
+                        stg[((size_t)blockIdx.x * k + t) * SW + e] = pop[s_best[t] * W + e];
+                    }
+                    for (int t = tid; t < k; t += kThreadsE) stg[((size_t)blockIdx.x * k + t) * SW + W] = fit[s_best[t]];
+                }
+                const bool met = grid_barrier(mg.bar, (unsigned)(m_done + 1) * gridDim.x);
+                ++m_done;
+                if (!met) {
+                    aborted = true;
+                    break;
+                }
+                const int src = s_src;
+                if (src >= 0) {
+                    const speo_segment &sp = segs[src];
+                    if (P < k || sp.pop_size < k || sp.ring_next < 0) {
+                        if (tid == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+                    } else {
+                        const int dm = D < sp.dim ? D : sp.dim;
+                        const float *from = stg + (size_t)src * k * SW;
+                        for (int i = tid; i < k * dm; i += kThreadsE) {
+                            const int t = i / dm, e = i - t * dm;
+                            pop[s_worst[t] * W + e] = __ldcg(from + (size_t)t * SW + e);
+                        }
+                        for (int t = tid; t < k; t += kThreadsE) fit[s_worst[t]] = __ldcg(from + (size_t)t * SW + W);
+                    }
+                }
+                __syncthreads();
+            }
         }
+        // a block that stopped early (a timed-out wait) still arrives at the launch's remaining grid
+        // barriers, without waiting
+        for (; m_done < nmig; ++m_done) grid_arrive(mg.bar);
         if (!ok_draw) atomicOr(&s_deverr, SPEO_DEVERR_REDRAW_LIMIT);
         if (!ok_bound) atomicOr(&s_deverr, SPEO_DEVERR_BOUND_LIMIT);
         if (aborted && tid == 0) {
@@ -368,8 +493,9 @@ __global__ void __launch_bounds__(kThreadsE, 1)
             *reinterpret_cast<float4 *>(pop_out + (row0 + r) * ld + 4 * c) = ld4e(pop + r * W + 4 * c);
         }
         for (int r = tid; r < P; r += kThreadsE) fit_out[row0 + r] = fit[r];
-    } else if (tid == 0) {
-        atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+    } else {
+        if (tid == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+        for (; m_done < nmig; ++m_done) (void)grid_barrier(mg.bar, (unsigned)(m_done + 1) * gridDim.x);
     }
     // ---- advance the generation counter by `generations` once every block has read it -------
     __syncthreads();
@@ -392,19 +518,86 @@ int optin_smem()
     return v;
 }
 
-template <int Q>
-int launch_epoch_tc(const speo_segment *segs, int n_segs, int max_pop, const float *pop_in, const float *fit_in,
-                    float *pop_out, float *fit_out, uint32_t *d_gen, int generations, float *hist, long long hist_ld,
-                    cudaStream_t st)
+size_t epoch_tc_smem(int Q, int max_pop)
 {
     const EpochTcLayout L = epoch_tc_layout(Q, max_pop);
     const int limit = optin_smem();
     // more than half of the SM's shared memory: one block (one tensor-memory allocation) per SM
-    const size_t smem = L.total > (size_t)limit / 2 + 1024 ? L.total : (size_t)limit / 2 + 1024;
+    return L.total > (size_t)limit / 2 + 1024 ? L.total : (size_t)limit / 2 + 1024;
+}
+
+// Per (device, Q, max_pop): the launch's shared memory and how many of its blocks fit on the device
+// at once (found once: a launch then costs the host one lookup and one attribute call, and a short
+// run's timed region includes the host's time to issue it). The attribute is set again on every
+// launch, so a device reset (which clears it) needs nothing more.
+struct EpochTcShape {
+    int dev, Q, max_pop, resident;
+    size_t smem;
+};
+std::mutex g_epoch_shape_mu;
+EpochTcShape g_epoch_shape[16];
+int g_epoch_shapes = 0;
+
+template <int Q>
+int epoch_tc_shape(int max_pop, EpochTcShape *out)
+{
+    int dev = 0;
+    if (int e = check_cuda(cudaGetDevice(&dev), "cudaGetDevice")) return e;
+    std::lock_guard<std::mutex> lock(g_epoch_shape_mu);
+    for (int i = 0; i < g_epoch_shapes; ++i)
+        if (g_epoch_shape[i].dev == dev && g_epoch_shape[i].Q == Q && g_epoch_shape[i].max_pop == max_pop) {
+            *out = g_epoch_shape[i];
+            return SPEO_OK;
+        }
+    EpochTcShape sh{dev, Q, max_pop, 0, epoch_tc_smem(Q, max_pop)};
+    cudaError_t e = cudaFuncSetAttribute(k_island_epoch_tc<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_island_epoch_tc)");
+    int coop = 0, sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_island_epoch_tc<Q>, kThreadsE, sh.smem) != cudaSuccess) {
+        cudaGetLastError();
+        per_sm = 0;
+    }
+    sh.resident = coop ? per_sm * sms : 0;
+    if (g_epoch_shapes < 16) g_epoch_shape[g_epoch_shapes++] = sh;
+    *out = sh;
+    return SPEO_OK;
+}
+
+// Whether n_segs blocks of the epoch kernel can all be resident at once (the in-launch migration's
+// grid barrier needs every block running).
+template <int Q>
+bool epoch_tc_coresident(int n_segs, int max_pop)
+{
+    EpochTcShape sh;
+    return epoch_tc_shape<Q>(max_pop, &sh) == SPEO_OK && sh.resident >= n_segs;
+}
+
+template <int Q>
+int launch_epoch_tc(const speo_segment *segs, int n_segs, int max_pop, const float *pop_in, const float *fit_in,
+                    float *pop_out, float *fit_out, uint32_t *d_gen, int generations, float *hist, long long hist_ld,
+                    cudaStream_t st, EpochMig mg = EpochMig{0, 0, 0, nullptr, nullptr})
+{
+    EpochTcShape sh;
+    if (int e = epoch_tc_shape<Q>(max_pop, &sh)) return e;
+    const size_t smem = sh.smem;
     cudaError_t e = cudaFuncSetAttribute(k_island_epoch_tc<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_island_epoch_tc)");
+    if (mg.k > 0 && mg.interval > 0 && (mg.pos + generations) / mg.interval == mg.pos / mg.interval)
+        mg.k = 0;  // no migration point among this launch's generations: an ordinary launch
+    if (mg.k > 0) {
+        // in-launch migration: every block resident (cooperative launch), barrier count from 0
+        if (int r = check_cuda(cudaMemsetAsync(mg.bar, 0, sizeof(unsigned), st), "epoch: barrier reset")) return r;
+        void *args[] = {(void *)&segs, (void *)&max_pop, (void *)&pop_in, (void *)&fit_in, (void *)&pop_out,
+                        (void *)&fit_out, (void *)&d_gen, (void *)&generations, (void *)&hist, (void *)&hist_ld,
+                        (void *)&mg};
+        return check_cuda(cudaLaunchCooperativeKernel((const void *)k_island_epoch_tc<Q>, dim3(n_segs),
+                                                      dim3(kThreadsE), args, smem, st),
+                          "cooperative launch of k_island_epoch_tc");
+    }
     k_island_epoch_tc<Q><<<n_segs, kThreadsE, smem, st>>>(segs, max_pop, pop_in, fit_in, pop_out, fit_out, d_gen,
-                                                          generations, hist, hist_ld);
+                                                          generations, hist, hist_ld, mg);
     return check_launch("k_island_epoch_tc");
 }
 
@@ -454,7 +647,27 @@ struct IslandRunState {
     cudaEvent_t made[2] = {nullptr, nullptr}, read[2] = {nullptr, nullptr};
     float *hist = nullptr;
     size_t cap = 0;  // floats
+    float *mstg = nullptr;  // in-launch migration staging
+    size_t mcap = 0;        // floats
+    unsigned *mbar = nullptr;
 };
+// Generations per launch of the in-launch-migration path when the fitness is read back: four
+// migration intervals (the history of one launch is copied while the next runs).
+constexpr int kFusedIntervals = 4;
+
+int island_mig_state(IslandRunState *r, size_t floats)
+{
+    if (!r->mbar)
+        if (int e = check_cuda(cudaMalloc(&r->mbar, 256), "island run: barrier")) return e;
+    if (r->mcap < floats) {
+        if (r->mstg) cudaFree(r->mstg);
+        r->mstg = nullptr;
+        r->mcap = 0;
+        if (int e = check_cuda(cudaMalloc(&r->mstg, sizeof(float) * floats), "island run: migration staging")) return e;
+        r->mcap = floats;
+    }
+    return SPEO_OK;
+}
 thread_local IslandRunState t_island_run;
 
 int island_run_state(size_t hist_floats, IslandRunState **out)
@@ -482,37 +695,52 @@ int island_run_state(size_t hist_floats, IslandRunState **out)
 }
 }  // namespace
 
-extern "C" int speo_island_run_tc(const speo_segment *segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
-                                  float *pop, float *fit, long long rows, uint32_t *d_gen, int first, int generations,
-                                  int interval, int migrants, float *staging, int max_ld, float *h_fitness,
-                                  void *stream)
+namespace {
+int island_run(const speo_segment *segs, int n_segs, int dim_lo, int dim_hi, int max_pop, float *pop, float *fit,
+               long long rows, uint32_t *d_gen, int first, int generations, int interval, int migrants,
+               float *staging, int max_ld, float *h_fitness, bool sync, void *stream)
 {
     if (!segs || !pop || !fit || !d_gen || n_segs < 1 || rows < 1 || generations < 0 || first < 0 || interval < 1)
-        return fail(SPEO_ERR_INVALID_ARG, "speo_island_run_tc: bad arguments");
+        return fail(SPEO_ERR_INVALID_ARG, "island run: bad arguments");
     if (migrants > 0 && (!staging || max_ld < 1))
-        return fail(SPEO_ERR_INVALID_ARG, "speo_island_run_tc: migration needs a staging buffer and max_ld");
-    if (dim_lo < 1 || dim_lo > dim_hi) return fail(SPEO_ERR_INVALID_ARG, "speo_island_run_tc: dim range");
+        return fail(SPEO_ERR_INVALID_ARG, "island run: migration needs a staging buffer and max_ld");
+    if (dim_lo < 1 || dim_lo > dim_hi) return fail(SPEO_ERR_INVALID_ARG, "island run: dim range");
     if (!speo_epoch_tc_fits(max_pop, dim_hi))
-        return fail(SPEO_ERR_UNSUPPORTED, "speo_island_run_tc: islands of P <= %d, D <= %d are not supported",
+        return fail(SPEO_ERR_UNSUPPORTED, "island run: islands of P <= %d, D <= %d are not supported",
                     max_pop, dim_hi);
     const int Q = dim_hi <= 32 ? 1 : 2;
     if (dim_lo <= 32 && Q == 2)
-        return fail(SPEO_ERR_UNSUPPORTED, "speo_island_run_tc: segments must share one column class");
+        return fail(SPEO_ERR_UNSUPPORTED, "island run: segments must share one column class");
     if (generations == 0) return SPEO_OK;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     IslandRunState *rs = nullptr;
-    const size_t per = (size_t)interval * (size_t)rows;  // one launch's history
+    // With every island resident at once (cooperative launch), the migrations run inside the
+    // launches: one launch for the whole run, or kFusedIntervals intervals per launch when the
+    // fitness is read back; otherwise one launch per interval and speo_ring_migrate between.
+    const bool fused = migrants > 0 && migrants <= kMaxMigrantsE &&
+                       (Q == 1 ? epoch_tc_coresident<1>(n_segs, max_pop) : epoch_tc_coresident<2>(n_segs, max_pop));
+    const long long span = fused ? (h_fitness ? (long long)interval * kFusedIntervals : (long long)generations)
+                                 : (long long)interval;
+    const size_t per = (size_t)(span < generations ? span : generations) * (size_t)rows;  // one launch's history
     if (int e = island_run_state(h_fitness ? 2 * per : 0, &rs)) return e;
+    EpochMig mg{0, 0, 0, nullptr, nullptr};
+    if (fused) {
+        if (int e = island_mig_state(rs, (size_t)2 * n_segs * migrants * (32 * Q + 1))) return e;
+        mg = EpochMig{interval, migrants, 0, rs->mstg, rs->mbar};
+    }
     int e = SPEO_OK, done = 0;
     for (int i = 0; !e && done < generations; ++i) {
         const int pos = first + done;
-        const int k = generations - done < interval - pos % interval ? generations - done : interval - pos % interval;
+        const int k = fused ? (int)(generations - done < span ? generations - done : span)
+                            : (generations - done < interval - pos % interval ? generations - done
+                                                                             : interval - pos % interval);
         const int b = i & 1;
         float *hb = h_fitness ? rs->hist + (size_t)b * per : nullptr;
         if (h_fitness && i >= 2) e = check_cuda(cudaStreamWaitEvent(st, rs->read[b], 0), "island run: wait");
+        mg.pos = pos;
         if (!e)
-            e = Q == 1 ? launch_epoch_tc<1>(segs, n_segs, max_pop, pop, fit, pop, fit, d_gen, k, hb, rows, st)
-                       : launch_epoch_tc<2>(segs, n_segs, max_pop, pop, fit, pop, fit, d_gen, k, hb, rows, st);
+            e = Q == 1 ? launch_epoch_tc<1>(segs, n_segs, max_pop, pop, fit, pop, fit, d_gen, k, hb, rows, st, mg)
+                       : launch_epoch_tc<2>(segs, n_segs, max_pop, pop, fit, pop, fit, d_gen, k, hb, rows, st, mg);
         if (!e && h_fitness) {
             e = check_cuda(cudaEventRecord(rs->made[b], st), "island run: record");
             if (!e) e = check_cuda(cudaStreamWaitEvent(rs->copy, rs->made[b], 0), "island run: wait");
@@ -524,12 +752,32 @@ extern "C" int speo_island_run_tc(const speo_segment *segs, int n_segs, int dim_
             if (!e) e = check_cuda(cudaEventRecord(rs->read[b], rs->copy), "island run: record");
         }
         done += k;
-        if (!e && migrants > 0 && (first + done) % interval == 0)
+        if (!e && !fused && migrants > 0 && (first + done) % interval == 0)
             e = speo_ring_migrate(segs, n_segs, migrants, pop, fit, staging, max_ld, st);
     }
     if (h_fitness)
         for (int b = 0; b < 2; ++b)
             if (int e2 = check_cuda(cudaStreamWaitEvent(st, rs->read[b], 0), "island run: wait"); e2 && !e) e = e2;
+    if (!sync) return e;
     const int es = check_cuda(cudaStreamSynchronize(st), "island run: sync");
     return e ? e : es;
+}
+}  // namespace
+
+extern "C" int speo_island_run_tc(const speo_segment *segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
+                                  float *pop, float *fit, long long rows, uint32_t *d_gen, int first, int generations,
+                                  int interval, int migrants, float *staging, int max_ld, float *h_fitness,
+                                  void *stream)
+{
+    return island_run(segs, n_segs, dim_lo, dim_hi, max_pop, pop, fit, rows, d_gen, first, generations, interval,
+                      migrants, staging, max_ld, h_fitness, true, stream);
+}
+
+extern "C" int speo_island_epochs_tc(const speo_segment *segs, int n_segs, int dim_lo, int dim_hi, int max_pop,
+                                     float *pop, float *fit, long long rows, uint32_t *d_gen, int first,
+                                     int generations, int interval, int migrants, float *staging, int max_ld,
+                                     void *stream)
+{
+    return island_run(segs, n_segs, dim_lo, dim_hi, max_pop, pop, fit, rows, d_gen, first, generations, interval,
+                      migrants, staging, max_ld, nullptr, false, stream);
 }

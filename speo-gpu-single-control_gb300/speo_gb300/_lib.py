@@ -129,6 +129,8 @@ SIGNATURES: dict[str, tuple] = {
     "speo_epoch_tc_fits": (c_int, [c_int, c_int]),
     "speo_island_run_tc": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int64, c_void_p, c_int,
                                    c_int, c_int, c_int, c_void_p, c_int, c_void_p, c_void_p]),
+    "speo_island_epochs_tc": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_int64, c_void_p,
+                                      c_int, c_int, c_int, c_int, c_void_p, c_int, c_void_p]),
     "speo_autotune_tile_rows": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p,
                                         c_void_p]),
     "speo_autotune_set_tile_rows": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int]),

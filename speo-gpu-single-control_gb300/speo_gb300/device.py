@@ -230,6 +230,19 @@ class SegmentTable:
                                                self._stream()), "speo_surrogate_generation")
         self.cur = b
 
+    def island_epochs_tc(self, generations: int, first: int, interval: int, migrants: int):
+        """`generations` tensor-core generations with the ring migration of `migrants` rows after
+        every multiple of `interval` generations of the run (`first` already done), in place and
+        asynchronous (speo_island_epochs_tc: the migrations inside the launch when every island
+        is resident at once)."""
+        L = _lib.load()
+        w = self.cur
+        _lib.check(L.speo_island_epochs_tc(self.d_segs.data_ptr(), len(self.specs), self.dim_lo, self.dim_hi,
+                                           max(sp.pop_size for sp in self.specs), self.pop[w].data_ptr(),
+                                           self.fit[w].data_ptr(), self.rows, self.gen.data_ptr(), first,
+                                           generations, interval, migrants, self.staging.data_ptr(), self.max_ld,
+                                           self._stream()), "speo_island_epochs_tc")
+
     def migrate(self, k: int):
         L = _lib.load()
         _lib.check(L.speo_ring_migrate(self.d_segs.data_ptr(), len(self.specs), k, self.pop[self.cur].data_ptr(),

@@ -174,3 +174,61 @@ def test_island_run_equals_epochs_and_ring_calls(lib, cuda):
     assert np.array_equal(a.fit[a.cur].cpu().numpy(), b.fit[b.cur].cpu().numpy())
     assert np.array_equal(hist.numpy(), np.stack(want))
     assert int(a.gen[0].cpu()) == int(b.gen[0].cpu()) == first + gens
+
+
+def _island_run_vs_calls(lib, cuda, sizes, ring, D, gens, interval, k, first=0):
+    """speo_island_run_tc without read-back against speo_generation_epoch_tc + speo_ring_migrate."""
+    import ctypes
+
+    import torch
+    from speo_gb300 import _lib
+    from speo_gb300.device import SegmentSpec, SegmentTable
+    from speo_gb300.instances import make_instance
+
+    def table():
+        inst = [make_instance(777, D)]
+        specs = [SegmentSpec(pop_size=sizes[i], dim=D, func_id=31 if i % 2 else 9, instance=0, seed=300 + i,
+                             ring_next=ring[i]) for i in range(len(sizes))]
+        return SegmentTable(specs, inst, device=str(cuda))
+
+    a, b = table(), table()
+    a.init_population()
+    b.init_population()
+    n = len(sizes)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.speo_island_run_tc(a.d_segs.data_ptr(), n, D, D, max(sizes), a.pop[a.cur].data_ptr(),
+                                      a.fit[a.cur].data_ptr(), a.rows, a.gen.data_ptr(), first, gens, interval, k,
+                                      a.staging.data_ptr(), a.max_ld, None, stream), "speo_island_run_tc")
+    done = 0
+    while done < gens:
+        step = min(gens - done, interval - (first + done) % interval)
+        b.epoch_tc(step)
+        done += step
+        if (first + done) % interval == 0:
+            b.migrate(k)
+    torch.cuda.synchronize()
+    assert np.array_equal(a.pop[a.cur].cpu().numpy(), b.pop[b.cur].cpu().numpy())
+    assert np.array_equal(a.fit[a.cur].cpu().numpy(), b.fit[b.cur].cpu().numpy())
+    assert int(a.gen[0].cpu()) == int(b.gen[0].cpu()) == gens
+    bits = ctypes.c_uint32(0xFFFF)
+    assert lib.speo_device_error_bits(ctypes.byref(bits)) == 0
+    assert bits.value == 0
+
+
+def test_island_run_migrates_inside_one_launch(lib, cuda):
+    """Every island resident at once: the whole run (six migrations) is one cooperative launch
+    whose migrations meet at a grid barrier; uneven islands, a ring of five and one island outside
+    it (no successor, no predecessor). Bit-identical to separate epochs and ring calls."""
+    sizes = [256, 100, 64, 200, 128, 77]
+    ring = [1, 2, 3, 4, 0, -1]
+    _island_run_vs_calls(lib, cuda, sizes, ring, 50, 60, 10, 5, first=0)
+    _island_run_vs_calls(lib, cuda, sizes, ring, 20, 37, 8, 3, first=0)
+
+
+def test_island_run_more_islands_than_resident_blocks(lib, cuda):
+    """More islands than SMs (one resident block per SM): the run falls back to one launch per
+    interval and speo_ring_migrate between them, with the same result."""
+    import torch
+
+    n = torch.cuda.get_device_properties(0).multi_processor_count + 8
+    _island_run_vs_calls(lib, cuda, [16] * n, [(i + 1) % n for i in range(n)], 8, 12, 5, 2)
