@@ -204,6 +204,57 @@ __device__ __forceinline__ int migrations_in(const EpochMig &mg, int generations
     return (mg.pos + generations) / mg.interval - mg.pos / mg.interval;
 }
 
+// One in-launch migration of this block's island (rows of W floats in shared memory): each row's
+// place in the best order (ascending (f, r)) and in the worst order, the k best rows to the
+// staging half of this migration's parity, the grid barrier, then the k worst rows from the ring
+// predecessor's emigrants (src; -1: none). Returns whether the barrier was met.
+template <int W>
+__device__ __noinline__ bool migrate_in_launch(float *pop, float *fit, int P, int D, const speo_segment *segs,
+                                               const EpochMig &mg, int m_done, int src, int *s_best, int *s_worst)
+{
+    const int tid = threadIdx.x, k = mg.k, SW = W + 1;
+    float *stg = mg.staging + (size_t)(m_done & 1) * gridDim.x * k * SW;
+    __syncthreads();
+    for (int r = tid; r < P; r += kThreadsE) {
+        const float fr = rank_key(fit[r]);
+        int rb = 0, rw = 0;
+        for (int j = 0; j < P; ++j) {
+            const float fj = rank_key(fit[j]);
+            rb += (fj < fr || (fj == fr && j < r)) ? 1 : 0;
+            rw += (fj > fr || (fj == fr && j > r)) ? 1 : 0;
+        }
+        if (rb < k) s_best[rb] = r;
+        if (rw < k) s_worst[rw] = r;
+    }
+    __syncthreads();
+    const int next = segs[blockIdx.x].ring_next;
+    if (next >= 0 && P < k && tid == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+    if (next >= 0 && P >= k) {
+        for (int i = tid; i < k * D; i += kThreadsE) {
+            const int t = i / D, e = i - t * D;
+            stg[((size_t)blockIdx.x * k + t) * SW + e] = pop[s_best[t] * W + e];
+        }
+        for (int t = tid; t < k; t += kThreadsE) stg[((size_t)blockIdx.x * k + t) * SW + W] = fit[s_best[t]];
+    }
+    if (!grid_barrier(mg.bar, (unsigned)(m_done + 1) * gridDim.x)) return false;
+    if (src >= 0) {
+        const speo_segment &sp = segs[src];
+        if (P < k || sp.pop_size < k || sp.ring_next < 0) {
+            if (tid == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
+        } else {
+            const int dm = D < sp.dim ? D : sp.dim;
+            const float *from = stg + (size_t)src * k * SW;
+            for (int i = tid; i < k * dm; i += kThreadsE) {
+                const int t = i / dm, e = i - t * dm;
+                pop[s_worst[t] * W + e] = __ldcg(from + (size_t)t * SW + e);
+            }
+            for (int t = tid; t < k; t += kThreadsE) fit[s_worst[t]] = __ldcg(from + (size_t)t * SW + W);
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
 template <int Q>
 __global__ void __launch_bounds__(kThreadsE, 1)
     k_island_epoch_tc(const speo_segment *__restrict__ segs, int Pmax, const float *pop_in, const float *fit_in,
@@ -421,55 +472,15 @@ __global__ void __launch_bounds__(kThreadsE, 1)
                     }
                 }
             }
-            // (6) ring migration at the run's migration points
+            // (6) ring migration at the run's migration points (out of line: the generation loop
+            // keeps its registers)
             if (nmig > 0 && (mg.pos + g + 1) % mg.interval == 0) {
-                const int k = mg.k, SW = W + 1;
-                float *stg = mg.staging + (size_t)(m_done & 1) * gridDim.x * k * SW;
-                __syncthreads();
-                // each row's place in the best order (ascending (f, r)) and in the worst order
-                for (int r = tid; r < P; r += kThreadsE) {
-                    const float fr = rank_key(fit[r]);
-                    int rb = 0, rw = 0;
-                    for (int j = 0; j < P; ++j) {
-                        const float fj = rank_key(fit[j]);
-                        rb += (fj < fr || (fj == fr && j < r)) ? 1 : 0;
-                        rw += (fj > fr || (fj == fr && j > r)) ? 1 : 0;
-                    }
-                    if (rb < k) s_best[rb] = r;
-                    if (rw < k) s_worst[rw] = r;
-                }
-                __syncthreads();
-                const bool emit = s.ring_next >= 0 && P >= k;
-                if (s.ring_next >= 0 && P < k && tid == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
-                if (emit) {
-                    for (int i = tid; i < k * D; i += kThreadsE) {
-                        const int t = i / D, e = i - t * D;
-                        stg[((size_t)blockIdx.x * k + t) * SW + e] = pop[s_best[t] * W + e];
-                    }
-                    for (int t = tid; t < k; t += kThreadsE) stg[((size_t)blockIdx.x * k + t) * SW + W] = fit[s_best[t]];
-                }
-                const bool met = grid_barrier(mg.bar, (unsigned)(m_done + 1) * gridDim.x);
+                const bool met = migrate_in_launch<W>(pop, fit, P, D, segs, mg, m_done, s_src, s_best, s_worst);
                 ++m_done;
                 if (!met) {
                     aborted = true;
                     break;
                 }
-                const int src = s_src;
-                if (src >= 0) {
-                    const speo_segment &sp = segs[src];
-                    if (P < k || sp.pop_size < k || sp.ring_next < 0) {
-                        if (tid == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);
-                    } else {
-                        const int dm = D < sp.dim ? D : sp.dim;
-                        const float *from = stg + (size_t)src * k * SW;
-                        for (int i = tid; i < k * dm; i += kThreadsE) {
-                            const int t = i / dm, e = i - t * dm;
-                            pop[s_worst[t] * W + e] = __ldcg(from + (size_t)t * SW + e);
-                        }
-                        for (int t = tid; t < k; t += kThreadsE) fit[s_worst[t]] = __ldcg(from + (size_t)t * SW + W);
-                    }
-                }
-                __syncthreads();
             }
         }
         // a block that stopped early (a timed-out wait) still arrives at the launch's remaining grid
