@@ -742,9 +742,12 @@ int island_run(const speo_segment *segs, int n_segs, int dim_lo, int dim_hi, int
     int e = SPEO_OK, done = 0;
     for (int i = 0; !e && done < generations; ++i) {
         const int pos = first + done;
-        const int k = fused ? (int)(generations - done < span ? generations - done : span)
-                            : (generations - done < interval - pos % interval ? generations - done
-                                                                             : interval - pos % interval);
+        const int left = generations - done;
+        // fused with read-back: launches of `span`, the last one at most an interval long, so that
+        // the history copy left after the last launch is short
+        const int k = fused ? (!h_fitness || left <= interval ? (int)(left < span ? left : span)
+                                                              : (int)(left - interval < span ? left - interval : span))
+                            : (left < interval - pos % interval ? left : interval - pos % interval);
         const int b = i & 1;
         float *hb = h_fitness ? rs->hist + (size_t)b * per : nullptr;
         if (h_fitness && i >= 2) e = check_cuda(cudaStreamWaitEvent(st, rs->read[b], 0), "island run: wait");
