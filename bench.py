@@ -336,6 +336,8 @@ C4_TRAIN_STEPS = 48   # Adam steps per generation: 48 x 4096 = 6 passes over a g
 C4_EXPLORE = 0.05     # fraction of targets that take a uniformly drawn trial instead of the screened one
 # Training batch x Adam steps per generation at about the same samples per generation (k = 8,
 # training every generation): larger batches fill more SMs per step.
+# Trials screened per target and Adam steps per generation at the default batch (4096) and rate.
+SURROGATE_K_GRID = [dict(k=k, train_steps=st, train_every=1) for k in (8, 12, 16) for st in (48, 64)]
 SURROGATE_BATCH_GRID = [dict(k=8, train_steps=st, train_every=1, train_batch=b, lr=lr)
                         for b, st, lr in ((4096, 48, 1e-3), (8192, 24, 1e-3), (8192, 24, 2e-3), (16384, 12, 2e-3),
                                           (16384, 12, 4e-3), (16384, 24, 2e-3), (32768, 6, 4e-3), (32768, 6, 8e-3),
@@ -1177,7 +1179,8 @@ def one_section(args) -> dict | None:
     from speo_gb300 import _lib
 
     if not (args.ops_only or args.e2e_only or args.published_only or args.mlp_case or args.c4_only
-            or args.configs_only or args.surrogate_sweep or args.surrogate_batch_sweep or args.surrogate_uneven):
+            or args.configs_only or args.surrogate_sweep or args.surrogate_batch_sweep or args.surrogate_uneven
+            or args.surrogate_k_sweep):
         return None
     dev = "cuda:0"
     torch.cuda.set_device(0)
@@ -1203,6 +1206,8 @@ def one_section(args) -> dict | None:
         return {"surrogate_uneven_islands": bench_surrogate(L, dev, torch, args.c4_gens, uneven=True)}
     if args.surrogate_batch_sweep:
         return {"surrogate_batch_sweep": bench_surrogate_sweep(L, dev, torch, grid=SURROGATE_BATCH_GRID)}
+    if args.surrogate_k_sweep:
+        return {"surrogate_k_sweep": bench_surrogate_sweep(L, dev, torch, grid=SURROGATE_K_GRID)}
     flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)
     return {"config1_island_d30": bench_config1(L, dev, torch, flush),
             "config2_precision": bench_config2(L, dev, torch, flush),
@@ -1234,6 +1239,8 @@ def main() -> None:
                     help="only the surrogate schedule sweep (k, Adam steps, training interval) against plain DE")
     ap.add_argument("--launch-per-interval", action="store_true",
                     help="time the headline as one launch per migration interval with migration launches between")
+    ap.add_argument("--surrogate-k-sweep", action="store_true",
+                    help="only the surrogate's trials-per-target x Adam-steps sweep against plain DE")
     ap.add_argument("--surrogate-uneven", action="store_true",
                     help="only the surrogate-vs-plain section on 144 islands of uneven size (config 4's instance)")
     ap.add_argument("--surrogate-batch-sweep", action="store_true",
