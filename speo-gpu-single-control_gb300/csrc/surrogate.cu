@@ -233,8 +233,10 @@ __global__ void k_archive_sample(const float *AX, int lda, const float *AT, cons
 
 // ---- k trials per target ----------------------------------------------------------------------
 // Trial t of the row `row` uses Philox tags TAG_IDX | (t+1) << 8 and TAG_CR | (t+1) << 8.
-// One warp per 32 (row, trial) pairs of a work item, lanes drawing in parallel, then G lanes per
-// pair building the vector. Output: T[(row * k + t) * ld + e].
+// Each warp takes up to 32 (row, trial) pairs of a work item (fewer when the item has few pairs,
+// so that all warps of the block work), its lanes drawing the pairs' donors in parallel; the
+// batch's (pair, 4-element chunk) tasks are then dealt to all 32 lanes. Output:
+// T[(row * k + t) * ld + e].
 __device__ __forceinline__ int ndon(int st)
 {
     switch (st) {
@@ -245,14 +247,12 @@ __device__ __forceinline__ int ndon(int st)
     }
 }
 
-template <int G>
 __global__ void __launch_bounds__(256) k_make_trials(const speo_segment *segs, const speo_work_item *items, int n_items,
                                                      int k, const float *pop, const float *fit, float *T,
                                                      const uint32_t *gen_ctr)
 {
     const uint32_t gen = *(volatile const uint32_t *)gen_ctr;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int R = 32 / G;
     for (int t_item = blockIdx.x; t_item < n_items; t_item += gridDim.x) {
         const speo_work_item it = items[t_item];
         const speo_segment &s = segs[it.segment];
@@ -273,12 +273,16 @@ __global__ void __launch_bounds__(256) k_make_trials(const speo_segment *segs, c
             if (best_row < 0) best_row = s.row0;
         }
         const int pairs = it.count * k;
-        for (int pb = warp * 32; pb < pairs; pb += (blockDim.x >> 5) * 32) {
-            // lane draws for pair pb + lane
+        // pairs per warp: up to 32, fewer when the item has few pairs, so that every warp works
+        const int nwarps = (int)(blockDim.x >> 5);
+        int ppw = (pairs + nwarps - 1) / nwarps;
+        ppw = ppw > 32 ? 32 : ppw;
+        for (int pb = warp * ppw; pb < pairs; pb += nwarps * ppw) {
+            // lane < ppw draws for pair pb + lane
             int d0 = 0, d1 = 0, d2 = 0, d3 = 0, d4 = 0, jr = 0;
             {
                 const int p = pb + lane;
-                if (p < pairs) {
+                if (lane < ppw && p < pairs) {
                     const int lr = p / k, tt = p - lr * k;
                     const long long row = s.row0 + it.first + lr;
                     IdxStream is(key, (uint32_t)row, gen, kTagIdx | ((uint32_t)(tt + 1) << 8));
@@ -289,20 +293,24 @@ __global__ void __launch_bounds__(256) k_make_trials(const speo_segment *segs, c
                 }
             }
             bool ok_bound = true;
-            for (int step = 0; step < 32; step += R) {
-                const int src = step + lane / G;
-                const int p = pb + src;
+            // the batch's (pair, 4-element chunk) tasks dealt to all 32 lanes; a task reads its
+            // pair's draws from the drawing lane
+            const int np = pairs - pb < ppw ? pairs - pb : ppw, tasks = np * nch;
+            for (int t0 = 0; t0 < tasks; t0 += 32) {
+                const int t = t0 + lane;
+                const int src = t < tasks ? t / nch : 0, c = t - src * nch;
                 const int rd[5] = {__shfl_sync(0xffffffffu, d0, src), __shfl_sync(0xffffffffu, d1, src),
                                    __shfl_sync(0xffffffffu, d2, src), __shfl_sync(0xffffffffu, d3, src),
                                    __shfl_sync(0xffffffffu, d4, src)};
                 const int rjr = __shfl_sync(0xffffffffu, jr, src);
-                if (p >= pairs) continue;
+                if (t >= tasks) continue;
+                const int p = pb + src;
                 const int lr = p / k, tt = p - lr * k;
                 const long long row = s.row0 + it.first + lr;
                 const float *xi = pop + row * ld;
                 const float *xb = pop + (best_row >= 0 ? best_row : row) * ld;
                 float *out = T + (row * k + tt) * (long long)ld;
-                for (int c = lane % G; c < nch; c += G) {
+                {
                     const int e0 = 4 * c;
                     const float4 ti = *reinterpret_cast<const float4 *>(xi + e0);
                     const float4 tb = best_row >= 0 ? *reinterpret_cast<const float4 *>(xb + e0) : ti;
@@ -828,12 +836,9 @@ extern "C" int speo_make_trials(const speo_segment *segs, const speo_work_item *
 {
     if (!segs || !items || !pop || !fit || !T || !d_gen || n_items < 1 || k < 1 || k > 64)
         return fail(SPEO_ERR_INVALID_ARG, "speo_make_trials: bad arguments");
-    const int nch = (dim_hi + 3) / 4;
+    (void)dim_hi;
     const int grid = n_items < 4 * sm_count() ? n_items : 4 * sm_count();
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (nch <= 8) k_make_trials<8><<<grid, 256, 0, st>>>(segs, items, n_items, k, pop, fit, T, d_gen);
-    else if (nch <= 16) k_make_trials<16><<<grid, 256, 0, st>>>(segs, items, n_items, k, pop, fit, T, d_gen);
-    else k_make_trials<32><<<grid, 256, 0, st>>>(segs, items, n_items, k, pop, fit, T, d_gen);
+    k_make_trials<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(segs, items, n_items, k, pop, fit, T, d_gen);
     return check_launch("k_make_trials");
 }
 
