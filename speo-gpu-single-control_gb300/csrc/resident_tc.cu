@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(kThreadsE, 1)
         __syncthreads();
         bm = s_bf[0];
         for (int w = 1; w < kWarpsE; ++w) bm = fmaxf(bm, s_bf[w]);
-        const int k_m = tcs::scale_exp(bm);
+        const int k_m = tcs::b_exp(bm);
         tcs::build_b(s, Kp, b_hi, L.b_bytes, so, tid, kThreadsE, tcs::pow2i(k_m));
         tc::fence_proxy_async_smem();  // B is read by the tensor cores (async proxy)
         tc::fence_before_sync();

@@ -342,19 +342,24 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
                 speo_segment sb;
                 sb.dim = D; sb.rot = cur.rot; sb.shift = cur.shift; sb.ld_rot = cur.ld_rot;
                 if (new_inst) {
-                    float bm = tcs::b_absmax(sb, gt, 128);
+                    // a new instance for this group: o, and k_M from the largest |M|; when B changes
+                    // too, one pass over M builds it with 2^14 while finding that value (b_exp keeps
+                    // 14 for the usual range; a second pass otherwise)
+                    float bm = new_b ? build_b(sb, Kp, b_hi, L.b_bytes, so_g, gt, 128, tcs::pow2i(14))
+                                     : tcs::b_absmax(sb, gt, 128);
                     for (int o = 16; o > 0; o >>= 1) bm = fmaxf(bm, __shfl_xor_sync(0xffffffffu, bm, o));
                     if (lane == 0) red_g[q] = bm;
                     for (int k = gt; k < Kp; k += 128) so_g[k] = k < D ? cur.shift[k] : 0.f;
                     tc::named_bar_sync(gbar, 128);
                     bm = fmaxf(fmaxf(red_g[0], red_g[1]), fmaxf(red_g[2], red_g[3]));
-                    g_km = tcs::scale_exp(bm);
+                    g_km = tcs::b_exp(bm);
                     g_rot = cur.rot; g_shift = cur.shift; g_dim = D; g_ldrot = cur.ld_rot;
-                }
-                if (new_b) {
+                    if (new_b && g_km != 14) build_b(sb, Kp, b_hi, L.b_bytes, so_g, gt, 128, tcs::pow2i(g_km));
+                } else {
+                    // B changed under this group (the other group's tile), the instance did not
                     build_b(sb, Kp, b_hi, L.b_bytes, so_g, gt, 128, tcs::pow2i(g_km));
-                    tc::fence_proxy_async_smem();
                 }
+                if (new_b) tc::fence_proxy_async_smem();
                 tc::named_bar_sync(gbar, 128);  // B, o and red are complete
             }
             if (!cur.ok && gt == 0) atomicOr(&s_deverr, SPEO_DEVERR_BAD_SEGMENT);

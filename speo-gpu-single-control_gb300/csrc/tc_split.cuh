@@ -63,8 +63,13 @@ __device__ __forceinline__ void split2h(float a, float b, uint32_t &hi, uint32_t
     lo = *reinterpret_cast<const uint32_t *>(&l);
 }
 
+// The exponent k_M of M's scale: 14 while the largest |M[n][k]| lies in [2^-6, 2) (2^14 M then stays
+// below 2^15 and its low parts stay normal, so B can be built in the same pass that finds the
+// largest value), else the general rule scale_exp.
+__device__ __forceinline__ int b_exp(float m) { return (m >= 0.015625f && m < 2.f) ? 14 : scale_exp(m); }
+
 // Largest |M[n][k]| = |rot[k*ld_rot + n]| over the entries thread t of `nthr` visits (the caller
-// reduces the threads' values and takes k_M = scale_exp of the maximum).
+// reduces the threads' values and takes k_M = b_exp of the maximum).
 __device__ __forceinline__ float b_absmax(const speo_segment &s, int t, int nthr)
 {
     const int D = s.dim;
@@ -78,18 +83,22 @@ __device__ __forceinline__ float b_absmax(const speo_segment &s, int t, int nthr
 
 // Builds B = split2(M 2^k_M) (mscale = 2^k_M) for an instance with `nthr` threads (index t):
 // B[n][k] = M[n][k] = rot[k*ld_rot + n] (zero past D), and the shift o. The parts are b_bytes apart.
-__device__ __forceinline__ void build_b(const speo_segment &s, int Kp, uint8_t *b_hi, size_t b_bytes, float *so, int t,
-                                        int nthr, float mscale)
+// Returns the largest |M[n][k]| this thread read (for b_exp after the threads' reduction).
+__device__ __forceinline__ float build_b(const speo_segment &s, int Kp, uint8_t *b_hi, size_t b_bytes, float *so, int t,
+                                         int nthr, float mscale)
 {
     const int D = s.dim;
     const int pairs = Kp * (Kp / 8);
+    float mx = 0.f;
     for (int i = t; i < pairs; i += nthr) {
         const int n = i % Kp, kc = i / Kp;
         float v[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
             const int k = 8 * kc + e;
-            v[e] = (n < D && k < D) ? s.rot[(size_t)k * s.ld_rot + n] * mscale : 0.f;
+            const float mv = (n < D && k < D) ? s.rot[(size_t)k * s.ld_rot + n] : 0.f;
+            mx = fmaxf(mx, fabsf(mv));
+            v[e] = mv * mscale;
         }
         uint32_t h[4], l[4];
 #pragma unroll
@@ -99,6 +108,7 @@ __device__ __forceinline__ void build_b(const speo_segment &s, int Kp, uint8_t *
         *reinterpret_cast<uint4 *>(b_hi + b_bytes + off) = make_uint4(l[0], l[1], l[2], l[3]);
     }
     for (int k = t; k < Kp; k += nthr) so[k] = k < D ? s.shift[k] : 0.f;
+    return mx;
 }
 
 // y = x - o over the 16 columns k0 .. k0+15 of a staged row (zero past D or for a dead row); whole
