@@ -263,14 +263,18 @@ __global__ void __launch_bounds__(256) k_make_trials(const speo_segment *segs, c
         }
         const uint2 key = seed_key(s.seed);
         const int st = s.strategy, nd = ndon(st);
+        // the segment's fields in registers: the trial stores below may alias `segs` for the
+        // compiler, which would otherwise load them again after every store
+        const long long row0 = s.row0;
+        const float sF = s.F, sCR = s.CR, slb = s.lb, sub = s.ub;
         long long best_row = -1;
         if (strategy_uses_best(st)) {  // argmin of the segment's fitness (every lane, small P)
             float bf = __int_as_float(0x7f800000);
             for (int i = 0; i < P; ++i) {
-                const float f = rank_key(fit[s.row0 + i]);
-                if (f < bf) { bf = f; best_row = s.row0 + i; }
+                const float f = rank_key(fit[row0 + i]);
+                if (f < bf) { bf = f; best_row = row0 + i; }
             }
-            if (best_row < 0) best_row = s.row0;
+            if (best_row < 0) best_row = row0;
         }
         const int pairs = it.count * k;
         // pairs per warp: up to 32, fewer when the item has few pairs, so that every warp works
@@ -284,7 +288,7 @@ __global__ void __launch_bounds__(256) k_make_trials(const speo_segment *segs, c
                 const int p = pb + lane;
                 if (lane < ppw && p < pairs) {
                     const int lr = p / k, tt = p - lr * k;
-                    const long long row = s.row0 + it.first + lr;
+                    const long long row = row0 + it.first + lr;
                     IdxStream is(key, (uint32_t)row, gen, kTagIdx | ((uint32_t)(tt + 1) << 8));
                     int r[5];
                     if (!draw_donors(is, P, r)) atomicOr(&s_deverr, SPEO_DEVERR_REDRAW_LIMIT);
@@ -306,7 +310,7 @@ __global__ void __launch_bounds__(256) k_make_trials(const speo_segment *segs, c
                 if (t >= tasks) continue;
                 const int p = pb + src;
                 const int lr = p / k, tt = p - lr * k;
-                const long long row = s.row0 + it.first + lr;
+                const long long row = row0 + it.first + lr;
                 const float *xi = pop + row * ld;
                 const float *xb = pop + (best_row >= 0 ? best_row : row) * ld;
                 float *out = T + (row * k + tt) * (long long)ld;
@@ -317,7 +321,7 @@ __global__ void __launch_bounds__(256) k_make_trials(const speo_segment *segs, c
                     float4 tr[5];
 #pragma unroll
                     for (int q = 0; q < 5; ++q)
-                        tr[q] = q < nd ? *reinterpret_cast<const float4 *>(pop + (s.row0 + rd[q]) * ld + e0) : ti;
+                        tr[q] = q < nd ? *reinterpret_cast<const float4 *>(pop + (row0 + rd[q]) * ld + e0) : ti;
                     const uint4 w = philox(make_uint4((uint32_t)c, (uint32_t)row, gen,
                                                       kTagCr | ((uint32_t)(tt + 1) << 8)), key);
                     float o[4] = {0.f, 0.f, 0.f, 0.f};
@@ -328,16 +332,16 @@ __global__ void __launch_bounds__(256) k_make_trials(const speo_segment *segs, c
                         if (e >= D) continue;
                         const float u = u01(pick(w, (uint32_t)q));
                         float x;
-                        if (e == rjr || u < s.CR) {
+                        if (e == rjr || u < sCR) {
                             float xr[5];
 #pragma unroll
                             for (int z = 0; z < 5; ++z)
                                 xr[z] = q == 0 ? tr[z].x : q == 1 ? tr[z].y : q == 2 ? tr[z].z : tr[z].w;
-                            x = mutant<float>(st, s.F, tiv[q], tbv[q], xr);
+                            x = mutant<float>(st, sF, tiv[q], tbv[q], xr);
                         } else {
                             x = tiv[q];
                         }
-                        o[q] = check_bound<float>(x, s.lb, s.ub, ok_bound);
+                        o[q] = check_bound<float>(x, slb, sub, ok_bound);
                     }
                     *reinterpret_cast<float4 *>(out + e0) = make_float4(o[0], o[1], o[2], o[3]);
                 }
