@@ -437,8 +437,8 @@ __global__ void __launch_bounds__(kThreadsE, 1)
             }
             if (te < ntile) {
                 tc::fence_after_sync();
-                const int m = te * tcs::kTileM + (warp & 3) * 32 + lane, h = tcs::epi_split(Kp);
-                const int c0 = he == 0 ? 0 : h, c1 = he == 0 ? (Kp < h ? Kp : h) : Kp;
+                const int m = te * tcs::kTileM + (warp & 3) * 32 + lane, h = tcs::epi_split(D);
+                const int c0 = he == 0 ? 0 : h, c1 = he == 0 ? (D < h ? D : h) : D;
                 const float f = c0 < c1 ? tcs::epilogue_row(tmem + (uint32_t)(kAccColsE * te), warp, D, c0, c1,
                                                             s.func_id, m < P ? rm[m] : 0.f)
                                         : 0.f;

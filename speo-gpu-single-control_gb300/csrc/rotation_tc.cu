@@ -442,10 +442,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             float f = 0.f;
             bool writer = ch == 0;
             if (func_sum_form(cur.func)) {
-                // columns [0, h) on the first warp of the quarter, [h, Np) on the second
+                // columns [0, h) on the first warp of the quarter, [h, D) on the second
                 // (tcs::epi_split); the second warp's partial sums meet the first's through psum[i % 2]
-                const int h = tcs::epi_split(Np);
-                const int c0 = ch == 0 ? 0 : h, c1 = ch == 0 ? (Np < h ? Np : h) : Np;
+                const int h = tcs::epi_split(cur.D);
+                const int c0 = ch == 0 ? 0 : h, c1 = ch == 0 ? (cur.D < h ? cur.D : h) : cur.D;
                 f = c0 < c1 ? epilogue_row(acc_t, warp, cur.D, c0, c1, cur.func, rsc) : 0.f;
                 float *ps = psum + (i & 1) * kTileM;
                 if (ch == 1) ps[m] = f;

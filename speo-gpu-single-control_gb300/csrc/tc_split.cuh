@@ -232,24 +232,29 @@ __device__ __forceinline__ uint64_t obj_term2(int func, uint64_t z)
     return fma2(z, z, mul2(mul2(pk2(20.0f, 20.0f), sn), sn));
 }
 
-// The per-coordinate-sum epilogue splits a row's Np accumulator columns between two threads:
-// [0, h) and [h, Np) with h = 32 ceil(Np / 64); the second part's sum is added to the first's. Every
-// kernel using this epilogue splits the same way, so a row's fitness does not depend on the kernel.
-__host__ __device__ __forceinline__ int epi_split(int Np) { return 32 * ((Np + 63) / 64); }
+// The per-coordinate-sum epilogue splits a row's columns between two threads: [0, h) and [h, D)
+// with h = D / 2 rounded to a multiple of 16 (at least 16), so both parts hold about half the
+// columns (D = 100: 48 and 52); the second part's sum is added to the first's. Every kernel using
+// this epilogue splits the same way, so a row's fitness does not depend on the kernel.
+__host__ __device__ __forceinline__ int epi_split(int D)
+{
+    const int h = 16 * ((D + 16) / 32);
+    return h < 16 ? 16 : h;
+}
 
-// sum_j term(scale * z_j) of one 32-column chunk starting at column c (j < D), added to the packed
+// sum_j term(scale * z_j) of one 16-column chunk starting at column c (j < D), added to the packed
 // pair accumulator two columns per operation, in column order.
-__device__ __forceinline__ void row_terms32(uint64_t &acc, const uint32_t (&r)[32], int c, int D, int func,
+__device__ __forceinline__ void row_terms16(uint64_t &acc, const uint32_t (&r)[16], int c, int D, int func,
                                             uint64_t sc)
 {
     using namespace tc;
-    if (c + 32 <= D) {
+    if (c + 16 <= D) {
 #pragma unroll
-        for (int j = 0; j < 32; j += 2)
+        for (int j = 0; j < 16; j += 2)
             acc = add2(acc, obj_term2(func, mul2(pk2(__uint_as_float(r[j]), __uint_as_float(r[j + 1])), sc)));
     } else {
 #pragma unroll
-        for (int j = 0; j < 32; j += 2) {
+        for (int j = 0; j < 16; j += 2) {
             if (c + j < D) {
                 const float z1 = (c + j + 1 < D) ? __uint_as_float(r[j + 1]) : 0.f;
                 acc = add2(acc, obj_term2(func, mul2(pk2(__uint_as_float(r[j]), z1), sc)));
@@ -266,19 +271,19 @@ __device__ __forceinline__ float pair_sum(uint64_t acc)
 }
 
 // Warps of one TMEM lane quarter (warp % 4), one lane (= tile row) per thread:
-// sum_j term(scale * z_j) over the columns j in [c0, c1), j < D, two columns per packed op, 32
-// columns per TMEM load (c0 a multiple of 32). `scale` is the row's: the objective's input scale
-// times 2^-(k_row + k_M).
+// sum_j term(scale * z_j) over the columns j in [c0, c1), j < D, two columns per packed op, 16
+// columns per TMEM load (c0 a multiple of 16). `scale` is the row's: the objective's input scale
+// times 2^-(k_row + k_M). (Loading the next 16 columns while a chunk is summed measured slower.)
 __device__ __forceinline__ float epilogue_row(uint32_t tmem, int warp, int D, int c0, int c1, int func, float scale)
 {
     const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     const uint64_t sc = tc::pk2(scale, scale);
     uint64_t acc = tc::pk2(0.f, 0.f);
-    for (int c = c0; c < c1; c += 32) {
-        uint32_t r[32];
-        tc::tmem_ld32_nowait(lane_base + (uint32_t)c, r);
-        tc::tmem_wait_ld();
-        row_terms32(acc, r, c, D, func, sc);
+    for (int c = c0; c < c1; c += 16) {
+        uint32_t r[16];
+        tc::tmem_ld16_nowait(lane_base + (uint32_t)c, r);
+        tc::tmem_wait_ld16(r);
+        row_terms16(acc, r, c, D, func, sc);
     }
     return pair_sum(acc);
 }
