@@ -43,6 +43,7 @@ sys.path.insert(0, str(REPO / "oracle"))
 METRIC = "exact-eval gens/s & evals to 1e-8 error: surrogate vs plain DE, same GB300"
 N_ISLANDS, POP, DIM, FUNC = 128, 256, 50, 9
 INTERVAL, MIGRANTS = 50, 5
+E2E_REPEATS = 5  # the end-to-end loops are timed this many times each (wall clock); the median is reported
 EVALS_PER_STEP = N_ISLANDS * POP
 WORKLOAD = ("learned-surrogate configuration, plain DE leg: 128 islands x P=256, D=50, rotated Rastrigin "
             "(F9 form, scale 0.0512), DE/rand/1/bin F=0.5 CR=0.9, ring best-5 -> worst-5 every 50 generations")
@@ -509,7 +510,8 @@ def bench_e2e(L, dev, torch, steps: int) -> dict:
     reference's IslandEA::Execute, generations and ring migration, as one call): the initial
     population, o and M^T uploaded from pinned host memory, the initial fitness evaluated, then
     `steps` generations with every generation's fitness vector read back to pinned host memory
-    (on a second stream while the next launch runs); all inside the timed region (wall clock)."""
+    (on a second stream while the next launch runs); all inside the timed region (wall clock, the
+    median of E2E_REPEATS runs)."""
     from speo_gb300 import _lib
 
     tab = headline_table(dev)
@@ -535,13 +537,16 @@ def bench_e2e(L, dev, torch, steps: int) -> dict:
 
     run(20)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    run(steps)
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
+    dts = []
+    for _ in range(E2E_REPEATS):
+        t0 = time.perf_counter()
+        run(steps)
+        torch.cuda.synchronize()
+        dts.append(time.perf_counter() - t0)
+    dt = float(np.median(dts))
     h2d = (n * ld + h_sh.numel() + h_rot.numel()) * 4
     return {"value": n * steps / dt, "unit": "evals/s", "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": n * 4,
-            "steps": steps, "dtype": "fp32",
+            "steps": steps, "repeats": E2E_REPEATS, "wall_s_each": [round(x, 6) for x in dts], "dtype": "fp32",
             "path": "speo_island_run_tc (the island loop of 128 islands of 256 as one C-ABI call: cooperative "
                     "tensor-core island-resident launches of 200 generations with the ring migration every 50 "
                     "generations inside them); "
@@ -555,7 +560,8 @@ def bench_e2e_dropin(L, dev, torch, steps: int) -> dict:
     initial API_evaluateFitness_f32, then `steps` generations of speo_de_run_f32 (128 sub-islands
     of 256 in the reference layout, np2 = 64) with every generation's fitness vector read back to
     pinned host memory, and speo_ring_migrate (best 5 -> next sub-island's worst 5) every 50
-    generations; all inside the timed region (wall clock, synchronous calls)."""
+    generations; all inside the timed region (wall clock, synchronous calls; the median of
+    E2E_REPEATS runs)."""
     from speo_gb300 import _lib
     from speo_gb300 import workloads as w
 
@@ -615,14 +621,17 @@ def bench_e2e_dropin(L, dev, torch, steps: int) -> dict:
         stream.synchronize()
 
     run(20)
-    t0 = time.perf_counter()
-    run(steps)
-    dt = time.perf_counter() - t0
+    dts = []
+    for _ in range(E2E_REPEATS):
+        t0 = time.perf_counter()
+        run(steps)
+        dts.append(time.perf_counter() - t0)
+    dt = float(np.median(dts))
     _lib.check(L.API_CheckCUDAError(), "e2e")
     L.speo_set_stream(None)
     h2d = (n * ld + ld * DIM + ld) * 4 + len(bytes(info))
     return {"value": n * steps / dt, "unit": "evals/s", "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": n * 4,
-            "steps": steps, "dtype": "fp32",
+            "steps": steps, "repeats": E2E_REPEATS, "wall_s_each": [round(x, 6) for x in dts], "dtype": "fp32",
             "path": "speo_de_run_f32 over 128 sub-islands of 256 (reference layout, np2=64): the generations of "
                     "API_DE_GenerateNewPopulation_f32 + API_evaluateFitness_f32 + API_DE_SelectSurvival_f32 "
                     "(bit-identical), every generation's fitness read back; speo_ring_migrate every 50 generations"}
