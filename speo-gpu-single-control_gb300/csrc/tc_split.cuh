@@ -242,19 +242,19 @@ __host__ __device__ __forceinline__ int epi_split(int D)
     return h < 16 ? 16 : h;
 }
 
-// sum_j term(scale * z_j) of one 16-column chunk starting at column c (j < D), added to the packed
+// sum_j term(scale * z_j) of one N-column chunk starting at column c (j < D), added to the packed
 // pair accumulator two columns per operation, in column order.
-__device__ __forceinline__ void row_terms16(uint64_t &acc, const uint32_t (&r)[16], int c, int D, int func,
-                                            uint64_t sc)
+template <int N>
+__device__ __forceinline__ void row_terms(uint64_t &acc, const uint32_t (&r)[N], int c, int D, int func, uint64_t sc)
 {
     using namespace tc;
-    if (c + 16 <= D) {
+    if (c + N <= D) {
 #pragma unroll
-        for (int j = 0; j < 16; j += 2)
+        for (int j = 0; j < N; j += 2)
             acc = add2(acc, obj_term2(func, mul2(pk2(__uint_as_float(r[j]), __uint_as_float(r[j + 1])), sc)));
     } else {
 #pragma unroll
-        for (int j = 0; j < 16; j += 2) {
+        for (int j = 0; j < N; j += 2) {
             if (c + j < D) {
                 const float z1 = (c + j + 1 < D) ? __uint_as_float(r[j + 1]) : 0.f;
                 acc = add2(acc, obj_term2(func, mul2(pk2(__uint_as_float(r[j]), z1), sc)));
@@ -272,18 +272,26 @@ __device__ __forceinline__ float pair_sum(uint64_t acc)
 
 // Warps of one TMEM lane quarter (warp % 4), one lane (= tile row) per thread:
 // sum_j term(scale * z_j) over the columns j in [c0, c1), j < D, two columns per packed op, 16
-// columns per TMEM load (c0 a multiple of 16). `scale` is the row's: the objective's input scale
-// times 2^-(k_row + k_M). (Loading the next 16 columns while a chunk is summed measured slower.)
+// columns per TMEM load (c0 a multiple of 16), a last chunk of at most 4 columns by a 4-column
+// load. `scale` is the row's: the objective's input scale times 2^-(k_row + k_M). (Loads of 8 or
+// 32 columns, and loading the next chunk while one is summed, measured slower.)
 __device__ __forceinline__ float epilogue_row(uint32_t tmem, int warp, int D, int c0, int c1, int func, float scale)
 {
     const uint32_t lane_base = tmem + ((uint32_t)((warp & 3) * 32) << 16);
     const uint64_t sc = tc::pk2(scale, scale);
     uint64_t acc = tc::pk2(0.f, 0.f);
     for (int c = c0; c < c1; c += 16) {
+        if (c + 4 >= D) {
+            uint32_t r[4];
+            tc::tmem_ld4_nowait(lane_base + (uint32_t)c, r);
+            tc::tmem_wait_ld4(r);
+            row_terms<4>(acc, r, c, D, func, sc);
+            break;
+        }
         uint32_t r[16];
         tc::tmem_ld16_nowait(lane_base + (uint32_t)c, r);
         tc::tmem_wait_ld16(r);
-        row_terms16(acc, r, c, D, func, sc);
+        row_terms<16>(acc, r, c, D, func, sc);
     }
     return pair_sum(acc);
 }
