@@ -56,8 +56,9 @@ __host__ __device__ __forceinline__ int a_slots(int kmax)
 constexpr long long kWaitBudget = 2000000000LL;  // ~1 s at 2 GHz: any wait longer is a failure
 constexpr int kEpiThreads = 256;                 // warps 0-7: epilogue
 constexpr int kCvtThreads = 256;                 // warps 8-15: conversion
-constexpr int kThreadsTc = kEpiThreads + kCvtThreads + 32;  // warp 16: TMA and MMA issue
+constexpr int kThreadsTc = kEpiThreads + kCvtThreads + 64;  // warp 16: MMA issue, warp 17: TMA issue
 constexpr int kIssuerWarp = (kEpiThreads + kCvtThreads) / 32;
+constexpr int kTmaWarp = kIssuerWarp + 1;
 constexpr int kMaxStages = 3;
 
 // Row stride of a staged tile: ld padded so that 8 consecutive rows start in different banks.
@@ -198,6 +199,16 @@ __device__ __forceinline__ TileInfo tile_info(const EvalTcArgs &a, const speo_wo
     return t;
 }
 
+// An mbarrier wait that also gives up once another role has raised the abort flag (checked between
+// suspend-hinted tests), or after the wait budget.
+__device__ __forceinline__ bool wait_or_abort(uint64_t *bar, uint32_t parity, volatile int *abort_flag)
+{
+    const long long t0 = clock64();
+    while (!tc::mbar_try_wait_sleep(bar, parity, 20000u))
+        if (*abort_flag != 0 || clock64() - t0 > kWaitBudget) return false;
+    return true;
+}
+
 __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_constant__ CUtensorMap xmap, EvalTcArgs a)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -212,7 +223,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
     float *rmul = reinterpret_cast<float *>(smem + L.off_rmul);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
     uint64_t *bar_tma = bars, *bar_mma = bars + 3, *bar_epi = bars + 5, *bar_afull = bars + 7, *bar_afree = bars + 11,
-             *bar_fin = bars + 15, *bar_rs = bars + 18;
+             *bar_fin = bars + 15, *bar_rs = bars + 18, *bar_sfree = bars + 26;
+    // tile i's D, written by its converters before their first A half is handed over (ring of 4)
+    int *s_dim = reinterpret_cast<int *>(bars + 29);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 16);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 17);
     float *red = reinterpret_cast<float *>(bars + 22);  // 2 x 4 floats: each converter group's |M| maxima
@@ -223,7 +236,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
         tc::tmem_relinquish();
     }
     if (tid == 32) {
-        for (int k = 0; k < kMaxStages; ++k) tc::mbar_init(&bar_tma[k], 1);
+        for (int k = 0; k < kMaxStages; ++k) {
+            tc::mbar_init(&bar_tma[k], 1);
+            tc::mbar_init(&bar_sfree[k], 128);
+        }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&bar_mma[b], 1);
             tc::mbar_init(&bar_epi[b], kEpiThreads);
@@ -250,38 +266,36 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
 
     const int my_items = a.n_items > (int)blockIdx.x ? (a.n_items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     auto item_of = [&](int i) { return a.items[blockIdx.x + (i < my_items ? i : my_items - 1) * gridDim.x]; };
-    int tma_issued = 0;      // issuer bookkeeping (warp kIssuerWarp, lane 0)
+    int tma_issued = 0;      // TMA bookkeeping (warp kTmaWarp, lane 0)
     bool mma_any = false;
 
-    if (warp == kIssuerWarp) {
-        // ---- TMA and MMA issue: the whole warp runs the loop, lane 0 issues ----------------------
-        const bool leader = lane == 0;
-        auto issue_tma = [&](int i, const TileInfo &t) {
-            if (i >= my_items) return;
-            if (leader) {
+    if (warp == kTmaWarp) {
+        // ---- TMA issue, lane 0: tile i into stage i % ns once the converters of tile i - ns have
+        // finished with that stage --------------------------------------------------------------
+        if (lane == 0) {
+            for (int i = 0; i < my_items; ++i) {
                 const int sidx = i % ns;
+                const TileInfo t = tile_info(a, item_of(i));
+                if (i >= ns && !wait_or_abort(&bar_sfree[sidx], (uint32_t)((i / ns - 1) & 1), abort_flag)) {
+                    *abort_flag = 1;
+                    break;
+                }
                 tc::mbar_arrive_expect_tx(&bar_tma[sidx], (uint32_t)L.stage_bytes);
                 tc::tma_load_2d(stage[sidx], &xmap, 0, t.ok ? (int)t.row : 0, &bar_tma[sidx]);
+                tma_issued = i + 1;
             }
-            tma_issued = i + 1;
-        };
-        for (int j = 0; j < ns; ++j) issue_tma(j, tile_info(a, item_of(j)));
-        TileInfo cur = tile_info(a, item_of(0)), nxt = tile_info(a, item_of(1));
-        speo_work_item it_n2 = item_of(2);
-        TileInfo tq = tile_info(a, item_of(ns));        // the tile whose TMA follows tile 0
-        speo_work_item it_q = item_of(ns + 1);
+        }
+    } else if (warp == kIssuerWarp) {
+        // ---- MMA issue: the whole warp runs the loop, lane 0 issues ------------------------------
+        const bool leader = lane == 0;
         for (int i = 0; i < my_items; ++i) {
-            // work items a tile ahead of their segments: no dependent load waits in this iteration
-            const TileInfo n2 = tile_info(a, it_n2);
-            const speo_work_item it_n3 = item_of(i + 3);
-            const TileInfo tq_next = tile_info(a, it_q);
-            const speo_work_item it_q_next = item_of(i + ns + 2);
-            const int b = i & 1, Kp = round16(cur.D), S = Kp / 16, s_half = (S + 1) / 2;
+            const int b = i & 1;
             const int sl0 = slot_of(i, 0), sl1 = slot_of(i, 1);
             bool ok = tc::mbar_wait_sleep(&bar_afull[sl0], (uint32_t)(use_of(i, 0) & 1), kWaitBudget);
             if (i >= 2) ok = ok && tc::mbar_wait_sleep(&bar_epi[b], (uint32_t)(((i - 2) >> 1) & 1), kWaitBudget);
             if (!__all_sync(0xffffffffu, ok && *abort_flag == 0)) { *abort_flag = 1; break; }
             tc::fence_after_sync();
+            const int Kp = round16(s_dim[i & 3]), S = Kp / 16, s_half = (S + 1) / 2;
             const uint32_t acc = tmem + (uint32_t)(b * L.kmax);
             if (leader) {
                 issue_split_mma(acc, slot_col(sl0), kApart, b_hi, L.b_bytes, Kp, Kp, 0, s_half);
@@ -298,14 +312,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
                 tc::mma_commit(&bar_mma[b]);
                 tc::mma_commit(&bar_afree[sl1]);
             }
-            // both halves' converters have read stage i % ns: it takes tile i + ns
-            issue_tma(i + ns, tq);
             __syncwarp();
-            cur = nxt;
-            nxt = n2;
-            it_n2 = it_n3;
-            tq = tq_next;
-            it_q = it_q_next;
         }
     } else if (warp >= kEpiThreads / 32) {
         // ---- conversion: group g = tiles g, g + 2, ...; thread = row 32 q + lane, both K halves ----
@@ -395,6 +402,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
                     // the products that freed this slot were issued
                     rmul[(i & 3) * kTileM + m] = tcs::row_scale(func_scale(cur.func), g_km, k_row);
                     tc::mbar_arrive(&bar_rs[i & 3]);
+                    if (gt == 0) s_dim[i & 3] = D;
                 }
                 const int s0 = h == 0 ? 0 : s_half, s1 = h == 0 ? s_half : S;
                 for (int st = s0; st < s1; ++st) {
@@ -417,6 +425,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
                 tc::mbar_arrive(&bar_afull[sl]);
             }
             if (!ok) *abort_flag = 1;  // the next tile's barrier stops the group
+            else tc::mbar_arrive(&bar_sfree[sidx]);  // this group's reads of the staged tile are done
             prv = prv_n;
             cur = cur_n;
         }
@@ -462,13 +471,15 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
         }
     }
     __syncthreads();
-    if (*abort_flag && warp == kIssuerWarp && lane == 0) {
+    if (*abort_flag && lane == 0) {
         // Let the copies and products this block started finish (bounded) before its shared and
         // tensor memory are released.
-        atomicOr(&s_deverr, SPEO_DEVERR_WAIT_TIMEOUT);
-        for (int j = (tma_issued > ns ? tma_issued - ns : 0); j < tma_issued; ++j)
-            tc::mbar_wait(&bar_tma[j % ns], (uint32_t)((j / ns) & 1), kWaitBudget);
-        if (mma_any) {
+        if (warp == kTmaWarp) {
+            atomicOr(&s_deverr, SPEO_DEVERR_WAIT_TIMEOUT);
+            for (int j = (tma_issued > ns ? tma_issued - ns : 0); j < tma_issued; ++j)
+                tc::mbar_wait(&bar_tma[j % ns], (uint32_t)((j / ns) & 1), kWaitBudget);
+        }
+        if (warp == kIssuerWarp && mma_any) {
             tc::mma_commit(bar_fin);
             tc::mbar_wait(bar_fin, 0, kWaitBudget);
         }
