@@ -204,8 +204,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd_tc(MlpArgs a)
 #pragma unroll 1
         for (int c0 = part * kPartCols; part < kParts && c0 < (part + 1) * kPartCols; c0 += 32) {
             uint32_t r[32];
-            tc::tmem_ld32_nowait(t_row + (uint32_t)c0, r);
-            tc::tmem_wait_ld();
+            tc::tmem_ld32(t_row + (uint32_t)c0, r);
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
                 float v[8];
@@ -235,8 +234,7 @@ __global__ void __launch_bounds__(kFwdThreads, 1) k_mlp_fwd_tc(MlpArgs a)
 #pragma unroll 1
         for (int c0 = part * kPartCols; part < kParts && c0 < (part + 1) * kPartCols; c0 += 32) {
             uint32_t r[32];
-            tc::tmem_ld32_nowait(t_row + (uint32_t)c0, r);
-            tc::tmem_wait_ld();
+            tc::tmem_ld32(t_row + (uint32_t)c0, r);
 #pragma unroll
             for (int e = 0; e < 32; ++e)
                 s = __fmaf_rn(fmaxf(__fadd_rn(__uint_as_float(r[e]), a.b2[c0 + e]), 0.f), a.w3[c0 + e], s);
@@ -433,8 +431,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_train_tc(TrainArgs a)
         for (int ci = 0; ci < H / 64; ++ci) {
             const int c0 = half * (H / 2) + 32 * ci;
             uint32_t r[32];
-            tc::tmem_ld32_nowait(t_row + (uint32_t)c0, r);
-            tc::tmem_wait_ld();
+            tc::tmem_ld32(t_row + (uint32_t)c0, r);
             uint32_t bits = 0;
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
@@ -480,8 +477,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_train_tc(TrainArgs a)
 #pragma unroll 1
         for (int c0 = half * (H / 2); c0 < (half + 1) * (H / 2); c0 += 32) {
             uint32_t r[32];
-            tc::tmem_ld32_nowait(t_row + (uint32_t)c0, r);
-            tc::tmem_wait_ld();
+            tc::tmem_ld32(t_row + (uint32_t)c0, r);
 #pragma unroll
             for (int e = 0; e < 32; ++e)
                 s = __fmaf_rn(fmaxf(__fadd_rn(__uint_as_float(r[e]), a.b2[c0 + e]), 0.f), a.w3[c0 + e], s);
@@ -506,8 +502,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_train_tc(TrainArgs a)
 #pragma unroll 1
         for (int c0 = half * (H / 2); c0 < (half + 1) * (H / 2); c0 += 32) {
             uint32_t r[32];
-            tc::tmem_ld32_nowait(t_row + (uint32_t)c0, r);
-            tc::tmem_wait_ld();
+            tc::tmem_ld32(t_row + (uint32_t)c0, r);
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
                 float dz[8], h2[8];
@@ -552,8 +547,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_train_tc(TrainArgs a)
         for (int ci = 0; ci < H / 64; ++ci) {
             const int c0 = half * (H / 2) + 32 * ci;
             uint32_t r[32];
-            tc::tmem_ld32_nowait(t_row + (uint32_t)c0, r);
-            tc::tmem_wait_ld();
+            tc::tmem_ld32(t_row + (uint32_t)c0, r);
 #pragma unroll
             for (int g = 0; g < 4; ++g) {
                 float v[8];
@@ -684,8 +678,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_wgrad_tc(WgradArgs a)
 #pragma unroll 1
         for (int cc = half * (H / 2); cc < (half + 1) * (H / 2); cc += 32) {
             uint32_t r[32];
-            tc::tmem_ld32_nowait(t_row + (uint32_t)cc, r);
-            tc::tmem_wait_ld();
+            tc::tmem_ld32(t_row + (uint32_t)cc, r);
 #pragma unroll
             for (int e = 0; e < 32; e += 4)
                 if (live) *reinterpret_cast<float4 *>(gW2 + cc + e) =
@@ -694,8 +687,7 @@ __global__ void __launch_bounds__(256, 1) k_mlp_wgrad_tc(WgradArgs a)
         }
         {
             uint32_t r[32];
-            tc::tmem_ld32_nowait(t_row + (uint32_t)(H + 32 * half), r);
-            tc::tmem_wait_ld();
+            tc::tmem_ld32(t_row + (uint32_t)(H + 32 * half), r);
             float *gW1 = g + (size_t)(live ? i : 0) * a.din;
 #pragma unroll
             for (int e = 0; e < 32; ++e)

@@ -116,8 +116,7 @@ __device__ __noinline__ float epi_generic(uint32_t lane_base, int D, int Np, flo
     float z0 = 0.f, prev = 0.f;
     for (int c = 0; c < Np; c += 32) {
         uint32_t r[32];
-        tmem_ld32_nowait(lane_base + (uint32_t)c, r);
-        tmem_wait_ld();
+        tmem_ld32(lane_base + (uint32_t)c, r);
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
             const int e = c + j;

@@ -283,14 +283,12 @@ __device__ __forceinline__ float epilogue_row(uint32_t tmem, int warp, int D, in
     for (int c = c0; c < c1; c += 16) {
         if (c + 4 >= D) {
             uint32_t r[4];
-            tc::tmem_ld4_nowait(lane_base + (uint32_t)c, r);
-            tc::tmem_wait_ld4(r);
+            tc::tmem_ld4(lane_base + (uint32_t)c, r);
             row_terms<4>(acc, r, c, D, func, sc);
             break;
         }
         uint32_t r[16];
-        tc::tmem_ld16_nowait(lane_base + (uint32_t)c, r);
-        tc::tmem_wait_ld16(r);
+        tc::tmem_ld16(lane_base + (uint32_t)c, r);
         row_terms<16>(acc, r, c, D, func, sc);
     }
     return pair_sum(acc);
