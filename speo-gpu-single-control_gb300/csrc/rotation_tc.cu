@@ -35,24 +35,21 @@ using tcs::build_b;
 using tcs::issue_split_mma;
 using tcs::epilogue_row;
 constexpr int kTmemCols = 128;   // widest accumulator (N <= 128)
-// Tensor memory (kmax = round16(largest D) columns per accumulator): accumulators b = 0, 1 at
-// columns kmax b (the products of tile i + 1 overlap the epilogue of tile i); then a ring of A
-// slots of kSlotCols columns from 2 kmax (four at every D <= 128). K half h of tile i (half-index
-// j = 2 i + h) goes to slot j % 4; a slot holds the hi and lo parts of one K half (<= 4 steps: 32
-// columns each) kApart = 32 columns apart. A half is converted while the products of the
-// previous halves run.
+// Tensor memory (kmax = round16(largest D) columns per accumulator): accumulators b = 0, 1, 2 at
+// columns kmax b (tile i uses accumulator i % 3: the products of tiles i + 1 and i + 2 run while
+// the epilogue of tile i reads its accumulator); then two A slots of kSlotCols columns from
+// 3 kmax, one per K half: a slot holds the hi and lo parts of one K half (<= 4 steps: 32 columns
+// each) kApart = 32 columns apart, and K half h of tile i is converted once the products of K
+// half h of tile i - 1 have read the slot.
 constexpr int kTmemAlloc = 512;
 constexpr int kApart = 32;
 constexpr int kSlotCols = tcs::kParts * kApart;
-constexpr int kMaxSlots = 4;
-// Every D <= kTmemCols gets four slots: the ring of four row-scale buffers (rmul, bar_rs) relies
-// on it (the converters of tile i + 4 pass the slot wait only after the epilogue of tile i).
-static_assert((kTmemAlloc - 2 * kTmemCols) / kSlotCols >= kMaxSlots, "four A slots at every D");
-__host__ __device__ __forceinline__ int a_slots(int kmax)
-{
-    const int n = (kTmemAlloc - 2 * kmax) / kSlotCols;
-    return n > kMaxSlots ? kMaxSlots : n;
-}
+constexpr int kAcc = 3;
+constexpr int kSlots = 2;
+// The ring of four row-scale buffers (rmul, bar_rs) relies on this layout: the converters of tile
+// i + 4 pass their first slot wait only after the products of tile i + 3, which start after the
+// epilogue of tile i.
+static_assert(kAcc * kTmemCols + kSlots * kSlotCols <= kTmemAlloc, "three accumulators and two A slots");
 constexpr long long kWaitBudget = 2000000000LL;  // ~1 s at 2 GHz: any wait longer is a failure
 constexpr int kEpiThreads = 256;                 // warps 0-7: epilogue
 constexpr int kCvtThreads = 256;                 // warps 8-15: conversion
@@ -221,7 +218,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
     float *psum = reinterpret_cast<float *>(smem + L.off_psum);
     float *rmul = reinterpret_cast<float *>(smem + L.off_rmul);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.off_bar);
-    uint64_t *bar_tma = bars, *bar_mma = bars + 3, *bar_epi = bars + 5, *bar_afull = bars + 7, *bar_afree = bars + 11,
+    uint64_t *bar_tma = bars, *bar_mma = bars + 3, *bar_epi = bars + 6, *bar_afull = bars + 9, *bar_afree = bars + 11,
              *bar_fin = bars + 15, *bar_rs = bars + 18, *bar_sfree = bars + 26;
     // tile i's D, written by its converters before their first A half is handed over (ring of 4)
     int *s_dim = reinterpret_cast<int *>(bars + 29);
@@ -239,11 +236,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             tc::mbar_init(&bar_tma[k], 1);
             tc::mbar_init(&bar_sfree[k], 128);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < kAcc; ++b) {
             tc::mbar_init(&bar_mma[b], 1);
             tc::mbar_init(&bar_epi[b], kEpiThreads);
         }
-        for (int k = 0; k < kMaxSlots; ++k) {
+        for (int k = 0; k < kSlots; ++k) {
             tc::mbar_init(&bar_afull[k], 128);
             tc::mbar_init(&bar_afree[k], 1);
         }
@@ -257,11 +254,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
-    const int nslot = a_slots(L.kmax);
+    const int nslot = kSlots;
     // K half h of tile i: its slot, the slot's column, and how often the slot was used before
     auto slot_of = [&](int i, int h) { return (2 * i + h) % nslot; };
     auto use_of = [&](int i, int h) { return (2 * i + h) / nslot; };
-    auto slot_col = [&](int sl) { return tmem + (uint32_t)(2 * L.kmax + kSlotCols * sl); };
+    auto slot_col = [&](int sl) { return tmem + (uint32_t)(kAcc * L.kmax + kSlotCols * sl); };
 
     const int my_items = a.n_items > (int)blockIdx.x ? (a.n_items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     auto item_of = [&](int i) { return a.items[blockIdx.x + (i < my_items ? i : my_items - 1) * gridDim.x]; };
@@ -288,10 +285,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
         // ---- MMA issue: the whole warp runs the loop, lane 0 issues ------------------------------
         const bool leader = lane == 0;
         for (int i = 0; i < my_items; ++i) {
-            const int b = i & 1;
+            const int b = i % kAcc;
             const int sl0 = slot_of(i, 0), sl1 = slot_of(i, 1);
             bool ok = tc::mbar_wait_sleep(&bar_afull[sl0], (uint32_t)(use_of(i, 0) & 1), kWaitBudget);
-            if (i >= 2) ok = ok && tc::mbar_wait_sleep(&bar_epi[b], (uint32_t)(((i - 2) >> 1) & 1), kWaitBudget);
+            if (i >= kAcc)
+                ok = ok && tc::mbar_wait_sleep(&bar_epi[b], (uint32_t)((i / kAcc - 1) & 1), kWaitBudget);
             if (!__all_sync(0xffffffffu, ok && *abort_flag == 0)) { *abort_flag = 1; break; }
             tc::fence_after_sync();
             const int Kp = round16(s_dim[i & 3]), S = Kp / 16, s_half = (S + 1) / 2;
@@ -340,7 +338,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             const bool new_b = cur.ok && (i == 0 || !prv.ok || !same_inst(cur, prv));
             // B is read by every product of the previous tile: rebuild it once those are done
             if (new_b && i >= 1)
-                to |= !tc::mbar_wait_sleep(&bar_mma[(i - 1) & 1], (uint32_t)(((i - 1) >> 1) & 1), kWaitBudget);
+                to |= !tc::mbar_wait_sleep(&bar_mma[(i - 1) % kAcc], (uint32_t)(((i - 1) / kAcc) & 1), kWaitBudget);
             // the group's decision to stop is reduced over its threads, so that none waits at its
             // named barrier for one that left
             if (tc::named_bar_or(gbar, 128, to || *abort_flag != 0)) { *abort_flag = 1; break; }
@@ -440,11 +438,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             if (tc::named_bar_or(2 + q, 64, *abort_flag != 0)) break;
             const speo_work_item it_nn = item_of(i + 2);
             const TileInfo nxt = tile_info(a, it_next);
-            const bool got = tc::mbar_wait_sleep(&bar_mma[i & 1], (uint32_t)((i >> 1) & 1), kWaitBudget) &&
+            const bool got = tc::mbar_wait_sleep(&bar_mma[i % kAcc], (uint32_t)((i / kAcc) & 1), kWaitBudget) &&
                              tc::mbar_wait_sleep(&bar_rs[i & 3], (uint32_t)((i >> 2) & 1), kWaitBudget);
             if (tc::named_bar_or(2 + q, 64, !got)) { *abort_flag = 1; break; }
             tc::fence_after_sync();
-            const uint32_t acc_t = tmem + (uint32_t)((i & 1) * L.kmax);
+            const uint32_t acc_t = tmem + (uint32_t)((i % kAcc) * L.kmax);
             const int Np = round16(cur.D), m = q * 32 + lane;
             const float rsc = rmul[(i & 3) * kTileM + m];
             float f = 0.f;
@@ -464,7 +462,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_evaluate_tc(const __grid_cons
             }
             if (writer && cur.ok && m < cur.count) a.fit[cur.row + m] = f;
             tc::fence_before_sync();
-            tc::mbar_arrive(&bar_epi[i & 1]);
+            tc::mbar_arrive(&bar_epi[i % kAcc]);
             cur = nxt;
             it_next = it_nn;
         }
