@@ -10,7 +10,7 @@
 //   (tcgen05.st, a ring of K-half slots); M (B operand, [N][K] = M[n][k]) is scaled and split the
 //   same way once per instance into shared memory; one thread issues, per 16-wide K step, the three
 //   products of tc_split.cuh (A from tensor memory) into an FP32 accumulator in tensor memory
-//   (M = 128 rows, N = D rounded up to 16, two accumulators): the fitness is as exact as the
+//   (M = 128 rows, N = D rounded up to 16, three accumulators): the fitness is as exact as the
 //   CUDA-core FP32 rotation's. Each K half is handed to the products as soon as it is converted;
 //   eight warps read the rows back with tcgen05.ld (two per lane quarter, each half of the
 //   columns), apply the row's scale and the objective term and reduce each row in registers.
@@ -161,19 +161,22 @@ __device__ __forceinline__ bool tc_tile_ok(const speo_work_item &it, const speo_
 
 // Warp roles: warps 8..11 convert the even tiles and warps 12..15 the odd ones into the A slots in
 // tensor memory (warp 8 + q + 4g: lane quarter q, group g; each group with its own copy of o and
-// named barrier 1 or 6); warp 16 issues the TMA loads and (one thread) the MMAs of each half as
-// soon as it is converted and the accumulator is free; warps 0..7 run the epilogue. B is rebuilt
-// by the group whose tile is the first of a new instance, once the previous tile's products are
-// done.
+// named barrier 1 or 6); warp 16 (one thread) issues the MMAs of each half as soon as it is
+// converted and the accumulator is free; warp 17 (one thread) issues the TMA loads, each stage
+// once the converters of the tile before are done with it; warps 0..7 run the epilogue. B is
+// rebuilt by the group whose tile is the first of a new instance, once the previous tile's
+// products are done.
 //   bar_tma[s]      stage s holds the rows of its tile                 (TMA transaction bytes)
 //   bar_afull[s]    slot s holds its K half (and its stage rows are read)       (128 arrivals)
 //   bar_afree[s]    the products reading slot s are done                        (tcgen05.commit)
 //   bar_mma[b]      accumulator b holds a finished product                      (tcgen05.commit)
 //   bar_epi[b]      the epilogue is done reading accumulator b                  (256 arrivals)
+//   bar_sfree[s]    the converters are done with stage s                        (128 arrivals)
 //   bar_fin         every product this block issued is done           (tcgen05.commit, on abort)
 //   bar_rs[i % 4]   rmul of tile i is written (its converter group)                (128 arrivals)
-// Everything a role needs about one tile is loaded ahead of use (register prefetch of the work
-// items and segments of the next tiles).
+// The converters and the epilogue load what they need about a tile a tile ahead (register prefetch
+// of the work items and segments); the MMA warp reads each tile's D from s_dim, written by the
+// converters.
 struct TileInfo {
     int ok, count, D, func, ld_rot;
     long long row;
