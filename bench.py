@@ -508,7 +508,8 @@ def bench_surrogate_sweep(L, dev, torch, ks=(2, 4, 8), steps=(1, 4, 16, 48), eve
 def bench_e2e(L, dev, torch, steps: int) -> dict:
     """The headline loop over host buffers through the C ABI's island loop (speo_island_run_tc: the
     reference's IslandEA::Execute, generations and ring migration, as one call): the initial
-    population, o and M^T uploaded from pinned host memory, the initial fitness evaluated, then
+    population, o and M^T uploaded from pinned host memory, the initial fitness evaluated (tensor
+    cores), then
     `steps` generations with every generation's fitness vector read back to pinned host memory
     (on a second stream while the next launch runs); all inside the timed region (wall clock, the
     median of E2E_REPEATS runs)."""
@@ -529,7 +530,7 @@ def bench_e2e(L, dev, torch, steps: int) -> dict:
         tab.inst_shift[0].copy_(h_sh, non_blocking=True)
         tab.inst_rot[0].copy_(h_rot, non_blocking=True)
         tab.gen.zero_()
-        tab.evaluate(use_tc=False)
+        tab.evaluate(use_tc=True)
         _lib.check(L.speo_island_run_tc(tab.d_segs.data_ptr(), N_ISLANDS, DIM, DIM, POP, tab.pop[tab.cur].data_ptr(),
                                         tab.fit[tab.cur].data_ptr(), n, tab.gen.data_ptr(), 0, nsteps, INTERVAL,
                                         MIGRANTS, tab.staging.data_ptr(), tab.max_ld, h_hist.data_ptr(),

@@ -665,6 +665,7 @@ struct IslandRunState {
 // Generations per launch of the in-launch-migration path when the fitness is read back: four
 // migration intervals (the history of one launch is copied while the next runs).
 constexpr int kFusedIntervals = 4;
+constexpr int kTailGensE = 8;  // generations of the last launch of a run that reads its fitness back
 
 int island_mig_state(IslandRunState *r, size_t floats)
 {
@@ -743,10 +744,11 @@ int island_run(const speo_segment *segs, int n_segs, int dim_lo, int dim_hi, int
     for (int i = 0; !e && done < generations; ++i) {
         const int pos = first + done;
         const int left = generations - done;
-        // fused with read-back: launches of `span`, the last one at most an interval long, so that
-        // the history copy left after the last launch is short
-        const int k = fused ? (!h_fitness || left <= interval ? (int)(left < span ? left : span)
-                                                              : (int)(left - interval < span ? left - interval : span))
+        // fused with read-back: launches of `span`, the last one at most kTailGensE generations
+        // long, so that the history copy left after the last launch is short
+        const int tail = interval < kTailGensE ? interval : kTailGensE;
+        const int k = fused ? (!h_fitness || left <= tail ? (int)(left < span ? left : span)
+                                                          : (int)(left - tail < span ? left - tail : span))
                             : (left < interval - pos % interval ? left : interval - pos % interval);
         const int b = i & 1;
         float *hb = h_fitness ? rs->hist + (size_t)b * per : nullptr;
