@@ -349,7 +349,8 @@ SPEO_API int speo_generation_epoch_tc(const speo_segment *d_segs, int n_segs, in
  * n_segs <= the SM count) and migrants <= 32, the migrations run inside the launches (a cooperative
  * launch; each island sends its best rows through a staging area the library owns, the blocks meet
  * at a grid barrier with a bounded wait, and each island takes its predecessor's rows), one launch
- * for the whole call or, with h_fitness, four intervals per launch; otherwise launches of up to
+ * for the whole call or, with h_fitness, four intervals per launch (the last launch at most 8
+ * generations, so that little of the history copy is left after it); otherwise launches of up to
  * `interval` generations with speo_ring_migrate between them. h_fitness (may be null; pinned host
  * memory for the copies to overlap): generations x rows floats that receive every generation's
  * fitness (generation g of this call at h_fitness + g * rows), read back on a second stream while
