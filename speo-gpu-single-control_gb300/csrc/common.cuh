@@ -35,9 +35,9 @@ __device__ __forceinline__ uint4 philox(uint4 c, uint2 k)
     return c;
 }
 
-// Out-of-line copy for the rarely refilled index-draw stream: keeps one Philox body in the
-// instruction stream instead of one per draw site.
-__device__ __noinline__ static uint4 philox_block(uint4 c, uint2 k) { return philox(c, k); }
+// The index-draw stream's block refill (inline: an out-of-line call measured slower in the
+// island-resident kernels, its saved registers going through local memory).
+__device__ __forceinline__ uint4 philox_block(uint4 c, uint2 k) { return philox(c, k); }
 
 __device__ __forceinline__ uint2 seed_key(uint64_t seed)
 {
@@ -95,6 +95,34 @@ __device__ __forceinline__ bool draw_donors(IdxStream &s, int S, int r[5])
         }
         if (r[i] == S) r[i]--;
     }
+    return ok;
+}
+
+// draw_donors followed by index(D) (jrand) on one IdxStream, with the common case made short: the
+// first eight draws come from two Philox blocks computed side by side; when the five donors of
+// words 0-4 are distinct, the sequential algorithm redraws nothing, so they and word 5 (jrand)
+// are its result; otherwise it runs from the start of the stream.
+__device__ __forceinline__ bool draw_donors_jrand(uint2 key, uint32_t row, uint32_t gen, uint32_t tag, int S, int D,
+                                                  int r[5], int &jrand)
+{
+    const uint4 b0 = philox(make_uint4(0u, row, gen, tag), key);
+    const uint4 b1 = philox(make_uint4(1u, row, gen, tag), key);
+    const uint32_t w[5] = {b0.x, b0.y, b0.z, b0.w, b1.x};
+    bool distinct = true;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const int v = (int)__fmul_rn(u01(w[i]), (float)S);
+        r[i] = v == S ? S - 1 : v;
+#pragma unroll
+        for (int j = 0; j < i; ++j) distinct &= r[i] != r[j];
+    }
+    if (distinct) {
+        jrand = (int)__fmul_rn(u01(b1.y), (float)D);
+        return true;
+    }
+    IdxStream is(key, row, gen, tag);
+    const bool ok = draw_donors(is, S, r);
+    jrand = is.index(D);
     return ok;
 }
 

@@ -50,7 +50,7 @@ __device__ __forceinline__ void f4se(float4 &v, int q, float x)
 __host__ __device__ inline int up_to(int x, int m) { return (x + m - 1) / m * m; }
 __host__ __device__ inline int draw_gens_e(int Pmax)
 {
-    const int g = kThreadsE / Pmax;
+    const int g = 4 * kThreadsE / Pmax;
     return g < 1 ? 1 : g > 8 ? 8 : g;
 }
 
@@ -373,13 +373,12 @@ __global__ void __launch_bounds__(kThreadsE, 1)
                 const int nb = generations - g < GB ? generations - g : GB;
                 for (int t = tid; t < nb * P; t += kThreadsE) {
                     const int gi = t / P, r = t - gi * P;
-                    IdxStream is(key, (uint32_t)(row0 + r), gen + (uint32_t)gi, kTagIdx);
-                    int rr[5];
-                    ok_draw &= draw_donors(is, P, rr);
+                    int rr[5], jr;
+                    ok_draw &= draw_donors_jrand(key, (uint32_t)(row0 + r), gen + (uint32_t)gi, kTagIdx, P, D, rr, jr);
                     int *o = sR + (gi * Pmax + r) * 8;
 #pragma unroll
                     for (int k = 0; k < 5; ++k) o[k] = rr[k];
-                    o[5] = is.index(D);
+                    o[5] = jr;
                 }
                 __syncthreads();
             }
