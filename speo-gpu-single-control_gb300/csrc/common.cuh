@@ -35,9 +35,9 @@ __device__ __forceinline__ uint4 philox(uint4 c, uint2 k)
     return c;
 }
 
-// The index-draw stream's block refill (inline: an out-of-line call measured slower in the
-// island-resident kernels, its saved registers going through local memory).
-__device__ __forceinline__ uint4 philox_block(uint4 c, uint2 k) { return philox(c, k); }
+// Out-of-line copy for the rarely refilled index-draw stream: keeps one Philox body in the
+// instruction stream instead of one per draw site (IdxStreamT<true> refills inline instead).
+__device__ __noinline__ static uint4 philox_block(uint4 c, uint2 k) { return philox(c, k); }
 
 __device__ __forceinline__ uint2 seed_key(uint64_t seed)
 {
@@ -56,17 +56,22 @@ __device__ __forceinline__ uint32_t pick(uint4 v, uint32_t i)
 }
 
 // Sequential index-draw stream of one target: draw k is word k%4 of
-// philox({k/4, row, gen, tag}, key).
-struct IdxStream {
+// philox({k/4, row, gen, tag}, key). Inline: the refill in line rather than through the
+// out-of-line philox_block (faster in the island-resident tensor-core kernel, whose register
+// state an out-of-line call saves through local memory; slower in the others).
+template <bool Inline>
+struct IdxStreamT {
     uint2 key;
     uint32_t row, gen, tag;
     uint32_t k;
     uint4 blk;
-    __device__ __forceinline__ IdxStream(uint2 key_, uint32_t row_, uint32_t gen_, uint32_t tag_)
+    __device__ __forceinline__ IdxStreamT(uint2 key_, uint32_t row_, uint32_t gen_, uint32_t tag_)
         : key(key_), row(row_), gen(gen_), tag(tag_), k(0), blk(make_uint4(0, 0, 0, 0)) {}
     __device__ __forceinline__ float next()
     {
-        if ((k & 3u) == 0) blk = philox_block(make_uint4(k >> 2, row, gen, tag), key);
+        if ((k & 3u) == 0)
+            blk = Inline ? philox(make_uint4(k >> 2, row, gen, tag), key)
+                         : philox_block(make_uint4(k >> 2, row, gen, tag), key);
         const float u = u01(pick(blk, k & 3u));
         ++k;
         return u;
@@ -74,11 +79,13 @@ struct IdxStream {
     // (int)(u * n) in binary32, as kernel_DE_CUDA.cu:193 (GPU_SINGLE_PRECISION build).
     __device__ __forceinline__ int index(int n) { return (int)__fmul_rn(next(), (float)n); }
 };
+using IdxStream = IdxStreamT<false>;
 
 // The five donor positions of kernel_DE_CUDA.cu:187-212, in [0, S), including the reference's
 // sequential (not pairwise-complete) distinctness check. Returns false if the bounded
 // rejection loop gave up.
-__device__ __forceinline__ bool draw_donors(IdxStream &s, int S, int r[5])
+template <typename Stream>
+__device__ __forceinline__ bool draw_donors(Stream &s, int S, int r[5])
 {
     bool ok = true;
 #pragma unroll 1
@@ -120,7 +127,7 @@ __device__ __forceinline__ bool draw_donors_jrand(uint2 key, uint32_t row, uint3
         jrand = (int)__fmul_rn(u01(b1.y), (float)D);
         return true;
     }
-    IdxStream is(key, row, gen, tag);
+    IdxStreamT<true> is(key, row, gen, tag);
     const bool ok = draw_donors(is, S, r);
     jrand = is.index(D);
     return ok;
