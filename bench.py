@@ -332,7 +332,7 @@ def bench_speo(args) -> dict:
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one island-resident launch of the
 # headline workload, from an ncu capture of that launch (45 generations; the island is read once per
 # launch and its writes stay in L2, so the figure does not grow with the generations per launch).
-EPOCH_LAUNCH_TRAFFIC_BYTES = {"simt": 7040512 + 11008, "tc": 7070208 + 9472}
+EPOCH_LAUNCH_TRAFFIC_BYTES = {"simt": 7040512 + 11008, "tc": 7065344 + 191232}
 C4_TRAIN_STEPS = 48   # Adam steps per generation: 48 x 4096 = 6 passes over a generation's 32768 new rows
 C4_EXPLORE = 0.05     # fraction of targets that take a uniformly drawn trial instead of the screened one
 # Training batch x Adam steps per generation at about the same samples per generation (k = 8,
